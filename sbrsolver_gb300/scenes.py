@@ -1,0 +1,311 @@
+"""Seeded synthetic scenes for the SBR hot path.
+
+The reference ships no benchmark scenes, so workloads are generated here:
+an axis-aligned-box city over a ground plane (small and urban-canyon sizes),
+and a fractal terrain with extruded polygons (large scene).  Every random
+draw comes from a project-written PCG32 stream and every coordinate is
+formed with IEEE +,-,*,/ only before rounding to float32, so the same seed
+gives bit-identical triangles on any host.  Scenes are written as binary
+STL (the reference's input format, SBRSolver_rev2/StlReader.h) plus a
+per-triangle material-id list, because the reference assigns materials per
+triangle after loading (Triangle::materialId, SBRSolver_rev2/Triangle.h:30).
+
+Material constants: relative permittivity as given for each workload;
+conductivities follow ITU-R P.2040-1 Table 3 (sigma = c * f_GHz**d) for
+concrete (c=0.0326, d=0.8095) and glass (c=0.0043, d=1.1925).
+"""
+from __future__ import annotations
+
+import math
+import os
+import struct
+from dataclasses import dataclass, field
+from typing import List, Sequence, Tuple
+
+import numpy as np
+
+
+class PCG32:
+    """PCG-XSH-RR 64/32 (O'Neill 2014), the published minimal generator."""
+
+    MULT = 6364136223846793005
+    MASK = (1 << 64) - 1
+
+    def __init__(self, seed: int, stream: int = 54):
+        self.state = 0
+        self.inc = ((stream << 1) | 1) & self.MASK
+        self.next_u32()
+        self.state = (self.state + seed) & self.MASK
+        self.next_u32()
+
+    def next_u32(self) -> int:
+        old = self.state
+        self.state = (old * self.MULT + self.inc) & self.MASK
+        xorshifted = (((old >> 18) ^ old) >> 27) & 0xFFFFFFFF
+        rot = old >> 59
+        return ((xorshifted >> rot) | (xorshifted << ((-rot) & 31))) & 0xFFFFFFFF
+
+    def uniform(self, lo: float, hi: float) -> float:
+        """lo + (hi-lo)*k/2**32 with k a 32-bit draw: exact dyadic arithmetic."""
+        return lo + (hi - lo) * (self.next_u32() / 4294967296.0)
+
+    def randint(self, n: int) -> int:
+        return self.next_u32() % n
+
+    def normal(self) -> float:
+        """Box-Muller; used only for scenes that are not golden fixtures."""
+        u1 = (self.next_u32() + 1.0) / 4294967297.0
+        u2 = self.next_u32() / 4294967296.0
+        return math.sqrt(-2.0 * math.log(u1)) * math.cos(2.0 * math.pi * u2)
+
+
+def p2040_sigma(c: float, d: float, f_hz: float) -> float:
+    return c * (f_hz / 1e9) ** d
+
+
+# (frequency, transmissionLoss, reflectionLoss, relPermittivityRe,
+#  relPermittivityIm, relConductivity): MaterialProperties field order,
+#  SBRSolver_rev2/common/DataStructures.h:20-28.
+Material = Tuple[float, float, float, float, float, float]
+
+
+@dataclass
+class Scene:
+    name: str
+    tri: np.ndarray          # (n, 3, 3) float32 vertices v1, v2, v3
+    normal: np.ndarray       # (n, 3) float32 facet normals (as written to the STL)
+    material_id: np.ndarray  # (n,) int32
+    materials: List[Material]
+
+    @property
+    def n_tri(self) -> int:
+        return int(self.tri.shape[0])
+
+
+@dataclass
+class Request:
+    """One propagation solve; argument meaning of RTSolver::ExecuteRayTracing
+    (SBRSolver_rev2/RTSolver.h:25-37) plus the antenna type the reference
+    hard-codes (FieldCompute.cpp:117, 1 = Hertzian)."""
+
+    tx: Tuple[float, float, float]
+    rx: np.ndarray                      # (m, 3) float64
+    max_reflection: int
+    max_transmission: int
+    frequency: float
+    tessellation: int
+    tx_coord_sys: Tuple[float, ...] = (1, 0, 0, 0, 1, 0, 0, 0, 1)  # row-major 3x3
+    pt: float = 1.0
+    use_fresnel: bool = True
+    antenna: int = 1
+
+
+@dataclass
+class Workload:
+    name: str
+    scene: Scene
+    request: Request
+    notes: dict = field(default_factory=dict)
+
+
+# ---------------------------------------------------------------- geometry
+
+class _MeshBuilder:
+    def __init__(self):
+        self.tris: List[Tuple[Tuple[float, float, float], ...]] = []
+        self.normals: List[Tuple[float, float, float]] = []
+        self.mats: List[int] = []
+
+    def tri(self, a, b, c, n, mat):
+        self.tris.append((tuple(a), tuple(b), tuple(c)))
+        self.normals.append(tuple(n))
+        self.mats.append(int(mat))
+
+    def quad(self, a, b, c, d, n, mat):
+        """Quad a-b-c-d (counter-clockwise seen from the normal side)."""
+        self.tri(a, b, c, n, mat)
+        self.tri(a, c, d, n, mat)
+
+    def box(self, x0, y0, x1, y1, z0, z1, mat):
+        """Axis-aligned box: 6 faces x 2 triangles, outward facet normals."""
+        self.quad((x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1), (0, 0, 1), mat)
+        self.quad((x0, y0, z0), (x0, y1, z0), (x1, y1, z0), (x1, y0, z0), (0, 0, -1), mat)
+        self.quad((x0, y0, z0), (x1, y0, z0), (x1, y0, z1), (x0, y0, z1), (0, -1, 0), mat)
+        self.quad((x1, y1, z0), (x0, y1, z0), (x0, y1, z1), (x1, y1, z1), (0, 1, 0), mat)
+        self.quad((x0, y1, z0), (x0, y0, z0), (x0, y0, z1), (x0, y1, z1), (-1, 0, 0), mat)
+        self.quad((x1, y0, z0), (x1, y1, z0), (x1, y1, z1), (x1, y0, z1), (1, 0, 0), mat)
+
+    def build(self, name, materials) -> Scene:
+        tri = np.asarray(self.tris, dtype=np.float64).astype(np.float32)
+        nrm = np.asarray(self.normals, dtype=np.float64).astype(np.float32)
+        mat = np.asarray(self.mats, dtype=np.int32)
+        return Scene(name, tri, nrm, mat, list(materials))
+
+
+def _f32(x: float) -> float:
+    return float(np.float32(x))
+
+
+def _ground(mb: _MeshBuilder, half: float, mat: int):
+    mb.quad((-half, -half, 0.0), (half, -half, 0.0), (half, half, 0.0), (-half, half, 0.0),
+            (0, 0, 1), mat)
+
+
+def _box_city(seed: int, half: float, n_boxes: int, foot: Tuple[float, float],
+              height: Tuple[float, float], keep_clear: Sequence[Tuple[float, float]],
+              box_mats: Sequence[int], pitch: float = 0.0, gap: float = 5.0):
+    """Box footprints/heights.  pitch > 0 places one box per cell of a
+    pitch x pitch lattice (streets between cells); pitch == 0 scatters boxes
+    with rejection of overlaps.  Boxes never cover a point in keep_clear."""
+    rng = PCG32(seed)
+    boxes = []
+
+    def covers(x0, y0, x1, y1, pts, margin=2.0):
+        return any(x0 - margin <= px <= x1 + margin and y0 - margin <= py <= y1 + margin
+                   for px, py in pts)
+
+    if pitch > 0:
+        n_side = int(round(2 * half / pitch))
+        cells = [(i, j) for i in range(n_side) for j in range(n_side)]
+        for (i, j) in cells[:n_boxes]:
+            cx0 = -half + i * pitch
+            cy0 = -half + j * pitch
+            for _attempt in range(64):
+                w = _f32(rng.uniform(*foot))
+                d = _f32(rng.uniform(*foot))
+                x0 = _f32(cx0 + gap + rng.uniform(0.0, max(pitch - 2 * gap - w, 0.0)))
+                y0 = _f32(cy0 + gap + rng.uniform(0.0, max(pitch - 2 * gap - d, 0.0)))
+                h = _f32(rng.uniform(*height))
+                mat = box_mats[rng.randint(len(box_mats))]
+                x1, y1 = _f32(x0 + w), _f32(y0 + d)
+                if not covers(x0, y0, x1, y1, keep_clear):
+                    boxes.append((x0, y0, x1, y1, h, mat))
+                    break
+    else:
+        while len(boxes) < n_boxes:
+            w = _f32(rng.uniform(*foot))
+            d = _f32(rng.uniform(*foot))
+            cx = rng.uniform(-half + 20.0, half - 20.0)
+            cy = rng.uniform(-half + 20.0, half - 20.0)
+            h = _f32(rng.uniform(*height))
+            mat = box_mats[rng.randint(len(box_mats))]
+            x0, y0 = _f32(cx - w / 2), _f32(cy - d / 2)
+            x1, y1 = _f32(x0 + w), _f32(y0 + d)
+            if covers(x0, y0, x1, y1, keep_clear):
+                continue
+            if any(not (x1 + 1 < b[0] or b[2] + 1 < x0 or y1 + 1 < b[1] or b[3] + 1 < y0)
+                   for b in boxes):
+                continue
+            boxes.append((x0, y0, x1, y1, h, mat))
+    return boxes
+
+
+def small_scene(seed: int = 0x5B5) -> Workload:
+    """Plain small workload: 200 m ground (eps_r=15, sigma=0.005) plus 10
+    axis-aligned boxes (footprints U(10,30) m, heights U(10,40) m), one
+    half-wave dipole Tx at (0,0,10), 2.4 GHz, level-6 icosahedron, 16 Rx on a
+    4x4 grid at 1.5 m, 3 reflections, no transmission.  122 triangles."""
+    f = 2.4e9
+    tx = (0.0, 0.0, 10.0)
+    g = [-75.0, -25.0, 25.0, 75.0]
+    rx = np.array([(x, y, 1.5) for x in g for y in g], dtype=np.float64)
+    clear = [(tx[0], tx[1])] + [(p[0], p[1]) for p in rx]
+    mats = [(f, 0.0, 0.0, 15.0, 0.0, 0.005),
+            (f, 0.0, 0.0, 5.31, 0.0, round(p2040_sigma(0.0326, 0.8095, f), 6))]
+    mb = _MeshBuilder()
+    _ground(mb, 100.0, 0)
+    for (x0, y0, x1, y1, h, m) in _box_city(seed, 100.0, 10, (10.0, 30.0), (10.0, 40.0),
+                                            clear, [1]):
+        mb.box(x0, y0, x1, y1, 0.0, h, m)
+    scene = mb.build("small", mats)
+    req = Request(tx=tx, rx=rx, max_reflection=3, max_transmission=0, frequency=f,
+                  tessellation=6, antenna=2)
+    return Workload("small_L6_R3", scene, req, {"seed": seed})
+
+
+def urban_scene(seed: int = 0x5B5 + 1, level: int = 9, rx_pitch: float = 10.0,
+                max_reflection: int = 6, max_transmission: int = 1) -> Workload:
+    """Synthetic urban canyon: 1 km x 1 km ground plus 400 boxes on a 50 m
+    lattice (streets >= 10 m), heights U(10,60) m, concrete (eps_r=5.31) or
+    glass (eps_r=6.27) 50/50, isotropic Tx at 28 GHz at a street crossing,
+    level-9 icosahedron (2,621,442 rays), 6 reflections + 1 transmission,
+    10,000 Rx on a 10 m grid at 1.5 m.  4,802 triangles."""
+    f = 28e9
+    tx = (0.0, 0.0, 20.0)
+    n = int(round(1000.0 / rx_pitch))
+    coords = [-500.0 + rx_pitch / 2 + rx_pitch * i for i in range(n)]
+    rx = np.array([(x, y, 1.5) for x in coords for y in coords], dtype=np.float64)
+    concrete = (f, 0.0, 0.0, 5.31, 0.0, round(p2040_sigma(0.0326, 0.8095, f), 6))
+    glass = (f, 0.0, 0.0, 6.27, 0.0, round(p2040_sigma(0.0043, 1.1925, f), 6))
+    mats = [concrete, concrete, glass]  # 0 ground, 1 concrete walls, 2 glass
+    mb = _MeshBuilder()
+    _ground(mb, 500.0, 0)
+    for (x0, y0, x1, y1, h, m) in _box_city(seed, 500.0, 400, (15.0, 35.0), (10.0, 60.0),
+                                            [(tx[0], tx[1])], [1, 2], pitch=50.0):
+        mb.box(x0, y0, x1, y1, 0.0, h, m)
+    scene = mb.build("urban", mats)
+    req = Request(tx=tx, rx=rx, max_reflection=max_reflection,
+                  max_transmission=max_transmission, frequency=f, tessellation=level,
+                  antenna=0)
+    return Workload(f"urban_L{level}_R{max_reflection}T{max_transmission}", scene, req,
+                    {"seed": seed, "rx_pitch": rx_pitch})
+
+
+def reference_main_scene(stl_bytes: bytes | None = None) -> Workload:
+    """The scene the reference's main() runs (SBRSolver_rev2.cpp:24-136):
+    ground.stl (10 m x 1001 m strip), Tx (0,0,5), Rx line (0,0..2999,3),
+    metal material, 1.8 GHz, 1 reflection, level 2, txCoordSys rows
+    {0,1,0},{0,0,1},{1,0,0}, Hertzian pattern."""
+    # ground.stl: two facets, normal +z (SBRSolver_rev2/data/stl_files/ground.stl)
+    tri = np.array([[[-5, -1, 0], [5, -1, 0], [5, 1000, 0]],
+                    [[-5, -1, 0], [5, 1000, 0], [-5, 1000, 0]]], dtype=np.float32)
+    nrm = np.array([[0, 0, 1], [0, 0, 1]], dtype=np.float32)
+    scene = Scene("reference_main", tri, nrm, np.zeros(2, np.int32),
+                  [(1.8e9, 221.13, 0.05, 1.0, 0.0, 1e6)])
+    rx = np.array([(0.0, float(i), 3.0) for i in range(3000)], dtype=np.float64)
+    req = Request(tx=(0.0, 0.0, 5.0), rx=rx, max_reflection=1, max_transmission=0,
+                  frequency=1.8e9, tessellation=2, tx_coord_sys=(0, 1, 0, 0, 0, 1, 1, 0, 0),
+                  pt=1.0, use_fresnel=True, antenna=1)
+    return Workload("reference_main", scene, req)
+
+
+# ------------------------------------------------------------------ output
+
+def write_stl(scene: Scene, path: str) -> None:
+    """Binary STL: 80-byte header, uint32 count, 50-byte facets."""
+    n = scene.n_tri
+    rec = np.zeros(n, dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")]))
+    rec["n"] = scene.normal
+    rec["v"] = scene.tri
+    with open(path, "wb") as fh:
+        fh.write(b"sbr synthetic scene".ljust(80, b" "))
+        fh.write(struct.pack("<I", n))
+        fh.write(rec.tobytes())
+
+
+def write_oracle_case(wl: Workload, directory: str, antenna: int | None = None) -> str:
+    """Writes the STL, material ids, receivers and a case file in the format
+    the reference harness reads; returns the case-file path."""
+    os.makedirs(directory, exist_ok=True)
+    sc, rq = wl.scene, wl.request
+    stl = os.path.join(directory, "scene.stl")
+    write_stl(sc, stl)
+    tm = os.path.join(directory, "trimat.txt")
+    np.savetxt(tm, sc.material_id, fmt="%d")
+    rxp = os.path.join(directory, "rx.txt")
+    with open(rxp, "w") as fh:
+        fh.write(f"{len(rq.rx)}\n")
+        for p in rq.rx:
+            fh.write("%.17g %.17g %.17g\n" % tuple(p))
+    case = os.path.join(directory, "case.txt")
+    with open(case, "w") as fh:
+        fh.write(f"stl {stl}\ntrimat {tm}\nrx {rxp}\nout {os.path.join(directory, 'out.txt')}\n")
+        fh.write(f"materials {len(sc.materials)}\n")
+        for m in sc.materials:
+            fh.write(" ".join("%.17g" % v for v in m) + "\n")
+        fh.write("tx %.17g %.17g %.17g\n" % tuple(rq.tx))
+        fh.write("txcs " + " ".join("%.17g" % v for v in rq.tx_coord_sys) + "\n")
+        fh.write(f"refl {rq.max_reflection}\ntrans {rq.max_transmission}\n")
+        fh.write(f"tess {rq.tessellation}\nantenna {rq.antenna if antenna is None else antenna}\n")
+        fh.write("freq %.17g\npt %.17g\nfresnel %d\n" % (rq.frequency, rq.pt, int(rq.use_fresnel)))
+    return case
