@@ -1,0 +1,162 @@
+/* sbr.h - C ABI of the GB300 shoot-bounce-reflect (SBR) propagation path.
+ *
+ * Drop-in boundary for SBRSolver's hot path.  Each entry point replaces one
+ * piece of the reference's C++ interface (paths relative to SBRSolver_rev2/):
+ *
+ *   sbr_scene_create / _from_stl  Preprocessor::StlToGeometry (Preprocessor.h:24-31,
+ *                                 Preprocessor.cpp:69-114) + BVH<Triangle>::ConstructBVH
+ *                                 (BVH/BVH.h:25,51-55) + RTSolver::Init (RTSolver.h:23,
+ *                                 RTSolver.cpp:13-22): triangles, coplanar ids, SAH BVH and
+ *                                 the material table, resident on the GPU.
+ *   sbr_solve                     RTSolver::ExecuteRayTracing (RTSolver.h:25-37,
+ *                                 RTSolver.cpp:52-126): ray launch, bounces, reception
+ *                                 spheres, image correction, duplicate removal, field.
+ *   sbr_solve_batch               many ExecuteRayTracing calls (one per transmitter) in one
+ *                                 device pass; no reference counterpart (the reference runs
+ *                                 one transmitter per call).
+ *   sbr_result_field              FieldCompute::FieldAtReceiver (FieldCompute.h:37,
+ *                                 FieldCompute.cpp:11-25) for every receiver.
+ *   sbr_result_paths              RTSolver::_rayPaths after duplicate removal (the data
+ *                                 SavePathsAsVtk writes, RTSolver.cpp:510-610).
+ *   sbr_last_error                none in the reference (it reports no errors); every call
+ *                                 here returns an sbr_status and leaves a message.
+ *
+ * Conventions: plain pointers and sizes, host memory unless a field says
+ * otherwise, row-major 3x3 matrices, no exceptions across the boundary.
+ * Results match the reference's FP64 CPU code: identical path sets
+ * (facet-id sequences, launch ids, ray counts) and received fields within
+ * 1e-4 relative magnitude / 1e-3 rad phase in the default precision mode.
+ */
+#ifndef SBR_H
+#define SBR_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sbr_status {
+  SBR_OK = 0,
+  SBR_ERR_INVALID_ARG = 1,
+  SBR_ERR_OOM = 2,           /* device or host allocation failed, or over the memory budget */
+  SBR_ERR_CAPACITY = 3,      /* a work queue or table stayed full after the allowed regrowth */
+  SBR_ERR_TIMEOUT = 4,
+  SBR_ERR_CUDA = 5,
+  SBR_ERR_IO = 6,
+  SBR_ERR_NOT_READY = 7
+} sbr_status;
+
+/* MaterialProperties (common/DataStructures.h:20-28), same field order.
+ * The field uses rel_permittivity_re and rel_conductivity only, like the
+ * reference (FieldCompute.cpp:185-235). */
+typedef struct sbr_material {
+  double frequency, transmission_loss, reflection_loss;
+  double rel_permittivity_re, rel_permittivity_im, rel_conductivity;
+} sbr_material;
+
+/* Antenna patterns of FieldCompute::GetAnalyticEfieldPattern
+ * (FieldCompute.cpp:153-183); the reference always uses SBR_ANTENNA_HERTZIAN. */
+enum { SBR_ANTENNA_ISOTROPIC = 0, SBR_ANTENNA_HERTZIAN = 1, SBR_ANTENNA_HALF_WAVE = 2 };
+
+/* Field precision: FP64 everywhere, or FP32 Fresnel/rotation arithmetic
+ * with FP64 path length and phase and a compensated FP32 per-receiver sum. */
+enum { SBR_FIELD_FP64 = 0, SBR_FIELD_FP32 = 1 };
+
+typedef struct sbr_scene sbr_scene;
+typedef struct sbr_result sbr_result;
+
+typedef struct sbr_scene_info {
+  int n_triangles, n_bvh_nodes, bvh_depth, n_coplanar;
+  double extent;          /* max |coordinate| of the scene */
+  long long device_bytes; /* resident scene size */
+} sbr_scene_info;
+
+/* Arguments of RTSolver::ExecuteRayTracing (RTSolver.h:25-37) plus the
+ * pattern and precision knobs the reference hard-codes. */
+typedef struct sbr_request {
+  double tx[3];
+  double tx_coord_sys[9];  /* row-major; the reference's txCoordSys */
+  int max_reflection, max_transmission;
+  double frequency, pt;
+  int use_fresnel;         /* useFresnelCoeff */
+  int tessellation;        /* icosahedron subdivision level (txTesslation) */
+  int antenna;             /* SBR_ANTENNA_*; SBR_ANTENNA_HERTZIAN reproduces the reference */
+  int field_precision;     /* SBR_FIELD_* */
+  int n_rx;
+  const double* rx;        /* 3 doubles per receiver */
+  int rx_on_device;        /* rx is a device pointer (already resident) */
+} sbr_request;
+
+typedef struct sbr_counts {
+  long long segments;      /* executed ray segments = closest-hit queries (rays x bounces) */
+  long long captured;      /* receiver captures before image correction */
+  long long corrected;     /* captures whose image correction succeeded */
+  long long paths;         /* surviving paths after duplicate removal */
+  long long rays;          /* rays over all surviving paths */
+  long long fp64_triangle_tests, fallback_rays, fp64_capture_tests;
+  long long launches;
+} sbr_counts;
+
+/* One surviving path; its rays are [ray_offset, ray_offset + n_rays) in the
+ * flat arrays of sbr_result_paths. */
+typedef struct sbr_path {
+  int request, receiver, n_rays, heap;  /* heap: BFS position in the launch's ray tree */
+  long long launch;
+  long long ray_offset;
+  double field[6];                      /* this path's contribution (Ex re, im, Ey, Ez) */
+} sbr_path;
+
+/* Stage times from CUDA events on the engine's stream.  device_ms spans
+ * everything after the receivers are on the device (grid, trace, capture,
+ * correction, field) and before results are copied back. */
+typedef struct sbr_timing {
+  double total_ms, trace_ms, capture_ms, correct_ms, field_ms, h2d_ms, d2h_ms, device_ms;
+} sbr_timing;
+
+/* ---- scene ---------------------------------------------------------- */
+/* vertices: 9 floats per triangle (v1, v2, v3); normals: 3 floats per
+ * triangle (facet normals as in the STL); material_ids may be NULL (all 0). */
+sbr_status sbr_scene_create(int n_triangles, const float* vertices, const float* normals,
+                            const int* material_ids, const sbr_material* materials,
+                            int n_materials, sbr_scene** out);
+sbr_status sbr_scene_create_from_stl(const char* path, const int* material_ids,
+                                     const sbr_material* materials, int n_materials,
+                                     sbr_scene** out);
+sbr_status sbr_scene_info_get(const sbr_scene* scene, sbr_scene_info* out);
+/* Triangle id at each position of the caller's triangle vector once
+ * BVH::ConstructBVH has sorted it (BVH/BVH.h:152,214).  The reference indexes
+ * that vector by triangle id during image correction and the field stage
+ * (RTSolver.cpp:356,415; FieldCompute.cpp:107), so this order is part of its
+ * result; sbr_scene_create installs it by default. */
+sbr_status sbr_scene_mesh_order(const sbr_scene* scene, int* out);
+/* Replace that order (e.g. identity for a caller whose vector is in file order). */
+sbr_status sbr_scene_set_mesh_order(sbr_scene* scene, const int* order);
+sbr_status sbr_scene_coplanar_ids(const sbr_scene* scene, int* out);
+sbr_status sbr_scene_destroy(sbr_scene* scene);
+
+/* ---- solve ---------------------------------------------------------- */
+sbr_status sbr_solve(sbr_scene* scene, const sbr_request* request, sbr_result** out);
+sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_requests,
+                           sbr_result** out);
+
+sbr_status sbr_result_counts(const sbr_result* result, sbr_counts* out);
+/* 6 doubles per receiver (Ex re, Ex im, Ey re, Ey im, Ez re, Ez im), requests
+ * concatenated in order. */
+sbr_status sbr_result_field(const sbr_result* result, double* out);
+/* paths: counts.paths entries; tri/cop/kind: counts.rays entries
+ * (kind 0 = launch, 1 = reflected, 2 = transmitted; tri/cop -1 on the last
+ * ray); points: 6 doubles per ray (corrected source, target).  Any output
+ * pointer may be NULL. */
+sbr_status sbr_result_paths(const sbr_result* result, sbr_path* paths, int* tri, int* cop,
+                            int* kind, double* points);
+sbr_status sbr_result_timing(const sbr_result* result, sbr_timing* out);
+sbr_status sbr_result_destroy(sbr_result* result);
+
+const char* sbr_last_error(void);
+const char* sbr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SBR_H */

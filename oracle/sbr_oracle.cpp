@@ -232,6 +232,49 @@ void coplanar_ids(std::vector<Tri>& tris, const std::vector<int>& vidx) {
   }
 }
 
+// Exact vertex merge (StlReader.h:448-508): equal float triples share an id;
+// triangles whose corners collapse are dropped while their normals stay in
+// place, as in the reference reader.  Then frames, boxes, coplanar ids.
+bool tris_from_soup(const std::vector<float>& coords, const std::vector<float>& normals,
+                    std::vector<Tri>& tris) {
+  const size_t nvtx = coords.size() / 3;
+  std::vector<size_t> order(nvtx);
+  std::iota(order.begin(), order.end(), 0);
+  auto key = [&](size_t i) { return std::make_tuple(coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]); };
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return key(a) < key(b); });
+  std::vector<int> uid(nvtx);
+  int cur = -1;
+  for (size_t k = 0; k < nvtx; ++k) {
+    if (k == 0 || key(order[k]) != key(order[k - 1])) ++cur;
+    uid[order[k]] = cur;
+  }
+  std::vector<int> vidx;
+  std::vector<size_t> src;  // first vertex slot of each kept triangle
+  for (size_t t = 0; t < nvtx / 3; ++t) {
+    int a = uid[3 * t], b = uid[3 * t + 1], c = uid[3 * t + 2];
+    if (a != b && a != c && b != c) {
+      vidx.push_back(a);
+      vidx.push_back(b);
+      vidx.push_back(c);
+      src.push_back(3 * t);
+    }
+  }
+  tris.clear();
+  for (size_t t = 0; t < src.size(); ++t) {
+    Tri tr;
+    const float* p = &coords[3 * src[t]];
+    tr.v1 = V3(p[0], p[1], p[2]);
+    tr.v2 = V3(p[3], p[4], p[5]);
+    tr.v3 = V3(p[6], p[7], p[8]);
+    tr.n = V3(normals[3 * t], normals[3 * t + 1], normals[3 * t + 2]);
+    tr.id = int(t);
+    finish_tri(tr);
+    tris.push_back(tr);
+  }
+  coplanar_ids(tris, vidx);
+  return true;
+}
+
 bool read_stl(const std::string& path, std::vector<Tri>& tris) {
   std::ifstream in(path, std::ios::binary);
   if (!in) return false;
@@ -276,44 +319,7 @@ bool read_stl(const std::string& path, std::vector<Tri>& tris) {
       for (int i = 3; i < 12; ++i) coords.push_back(d[i]);
     }
   }
-  // Merge exactly equal vertices; drop triangles that collapse (their
-  // normals stay in place, as in the reference reader).
-  const size_t nvtx = coords.size() / 3;
-  std::vector<size_t> order(nvtx);
-  std::iota(order.begin(), order.end(), 0);
-  auto key = [&](size_t i) { return std::make_tuple(coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]); };
-  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return key(a) < key(b); });
-  std::vector<int> uid(nvtx);
-  int cur = -1;
-  for (size_t k = 0; k < nvtx; ++k) {
-    if (k == 0 || key(order[k]) != key(order[k - 1])) ++cur;
-    uid[order[k]] = cur;
-  }
-  std::vector<int> vidx;
-  std::vector<size_t> src;  // first vertex slot of each kept triangle
-  for (size_t t = 0; t < nvtx / 3; ++t) {
-    int a = uid[3 * t], b = uid[3 * t + 1], c = uid[3 * t + 2];
-    if (a != b && a != c && b != c) {
-      vidx.push_back(a);
-      vidx.push_back(b);
-      vidx.push_back(c);
-      src.push_back(3 * t);
-    }
-  }
-  tris.clear();
-  for (size_t t = 0; t < src.size(); ++t) {
-    Tri tr;
-    const float* p = &coords[3 * src[t]];
-    tr.v1 = V3(p[0], p[1], p[2]);
-    tr.v2 = V3(p[3], p[4], p[5]);
-    tr.v3 = V3(p[6], p[7], p[8]);
-    tr.n = V3(normals[3 * t], normals[3 * t + 1], normals[3 * t + 2]);
-    tr.id = int(t);
-    finish_tri(tr);
-    tris.push_back(tr);
-  }
-  coplanar_ids(tris, vidx);
-  return true;
+  return tris_from_soup(coords, normals, tris);
 }
 
 // BVH/BVH.h:251-267
@@ -906,29 +912,13 @@ int oracle_scene_from_stl(const char* path, oracle_scene** out) {
 }
 
 int oracle_scene_from_triangles(int n, const float* v, const float* nrm, oracle_scene** out) {
-  // Same path as a binary STL (vertex merge, coplanar ids, BVH).
-  std::string tmp;
   auto* sc = new oracle_scene();
-  std::vector<orc::Tri>& tris = sc->s.tris;
   std::vector<float> coords(v, v + 9 * size_t(n));
   std::vector<float> normals(nrm, nrm + 3 * size_t(n));
-  // reuse the STL merge logic through an in-memory image
-  std::string img(84 + 50 * size_t(n), '\0');
-  uint32_t cnt = uint32_t(n);
-  std::memcpy(&img[80], &cnt, 4);
-  for (int t = 0; t < n; ++t) {
-    std::memcpy(&img[84 + 50 * size_t(t)], &normals[3 * size_t(t)], 12);
-    std::memcpy(&img[84 + 50 * size_t(t) + 12], &coords[9 * size_t(t)], 36);
+  if (!orc::tris_from_soup(coords, normals, sc->s.tris)) {
+    delete sc;
+    return 1;
   }
-  char name[] = "/tmp/sbr_oracle_XXXXXX";
-  int fd = mkstemp(name);
-  if (fd < 0) { delete sc; return 2; }
-  FILE* f = fdopen(fd, "wb");
-  std::fwrite(img.data(), 1, img.size(), f);
-  std::fclose(f);
-  bool ok = orc::read_stl(name, tris);
-  std::remove(name);
-  if (!ok) { delete sc; return 1; }
   orc::build_bvh(sc->s);
   *out = sc;
   return 0;

@@ -1,0 +1,113 @@
+"""ctypes binding of the C ABI (include/sbr.h).  Loads the in-tree
+``libsbr.so``; there is no fallback: if the library or a GPU is missing the
+calls fail with the library's error message."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsbr.so")
+
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_CAPACITY, ERR_TIMEOUT, ERR_CUDA, ERR_IO, ERR_NOT_READY = range(8)
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CAPACITY", 4: "TIMEOUT", 5: "CUDA",
+                6: "IO", 7: "NOT_READY"}
+
+# Every symbol include/sbr.h declares.
+EXPORTS = (
+    "sbr_scene_create", "sbr_scene_create_from_stl", "sbr_scene_info_get", "sbr_scene_mesh_order",
+    "sbr_scene_set_mesh_order", "sbr_scene_coplanar_ids", "sbr_scene_destroy", "sbr_solve",
+    "sbr_solve_batch", "sbr_result_counts", "sbr_result_field", "sbr_result_paths",
+    "sbr_result_timing", "sbr_result_destroy", "sbr_last_error", "sbr_version",
+)
+
+
+class SbrError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Material(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("frequency", "transmission_loss", "reflection_loss",
+                                           "rel_permittivity_re", "rel_permittivity_im",
+                                           "rel_conductivity")]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("n_triangles", C.c_int), ("n_bvh_nodes", C.c_int), ("bvh_depth", C.c_int),
+                ("n_coplanar", C.c_int), ("extent", C.c_double), ("device_bytes", C.c_longlong)]
+
+
+class Request(C.Structure):
+    _fields_ = [("tx", C.c_double * 3), ("tx_coord_sys", C.c_double * 9),
+                ("max_reflection", C.c_int), ("max_transmission", C.c_int),
+                ("frequency", C.c_double), ("pt", C.c_double), ("use_fresnel", C.c_int),
+                ("tessellation", C.c_int), ("antenna", C.c_int), ("field_precision", C.c_int),
+                ("n_rx", C.c_int), ("rx", C.POINTER(C.c_double)), ("rx_on_device", C.c_int)]
+
+
+class Counts(C.Structure):
+    _fields_ = [(n, C.c_longlong) for n in ("segments", "captured", "corrected", "paths", "rays",
+                                             "fp64_triangle_tests", "fallback_rays",
+                                             "fp64_capture_tests", "launches")]
+
+
+class Path(C.Structure):
+    _fields_ = [("request", C.c_int), ("receiver", C.c_int), ("n_rays", C.c_int),
+                ("heap", C.c_int), ("launch", C.c_longlong), ("ray_offset", C.c_longlong),
+                ("field", C.c_double * 6)]
+
+
+class Timing(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("total_ms", "trace_ms", "capture_ms", "correct_ms",
+                                           "field_ms", "h2d_ms", "d2h_ms", "device_ms")]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(path: str = LIB_PATH):
+    """Loads libsbr.so (once) and declares the signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise OSError(f"{path} is not built; run sbrsolver_gb300.build.build_library()")
+        lib = C.CDLL(path)
+        P, I, D = C.POINTER, C.c_int, C.c_double
+        vp = C.c_void_p
+        sig = {
+            "sbr_scene_create": [I, P(C.c_float), P(C.c_float), P(I), P(Material), I, P(vp)],
+            "sbr_scene_create_from_stl": [C.c_char_p, P(I), P(Material), I, P(vp)],
+            "sbr_scene_info_get": [vp, P(SceneInfo)],
+            "sbr_scene_mesh_order": [vp, P(I)],
+            "sbr_scene_set_mesh_order": [vp, P(I)],
+            "sbr_scene_coplanar_ids": [vp, P(I)],
+            "sbr_scene_destroy": [vp],
+            "sbr_solve": [vp, P(Request), P(vp)],
+            "sbr_solve_batch": [vp, P(Request), I, P(vp)],
+            "sbr_result_counts": [vp, P(Counts)],
+            "sbr_result_field": [vp, P(D)],
+            "sbr_result_paths": [vp, P(Path), P(I), P(I), P(I), P(D)],
+            "sbr_result_timing": [vp, P(Timing)],
+            "sbr_result_destroy": [vp],
+        }
+        for name, args in sig.items():
+            f = getattr(lib, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        lib.sbr_last_error.restype = C.c_char_p
+        lib.sbr_last_error.argtypes = []
+        lib.sbr_version.restype = C.c_char_p
+        lib.sbr_version.argtypes = []
+        _lib = lib
+        return lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        raise SbrError(status, load().sbr_last_error().decode(errors="replace"))

@@ -1,0 +1,345 @@
+"""Host-side mirror of the reference's interface for the SBR path.
+
+Names, argument order and argument meaning follow the reference
+(SBRSolver_rev2/): ``Preprocessor`` (Preprocessor.h:18-75), ``BVH``
+(BVH/BVH.h:13-37), ``RTSolver`` (RTSolver.h:18-83), ``FieldCompute``
+(FieldCompute.h:9-94), ``GlobalConfig`` (GlobalConfig.h:5-7, given the
+settings the reference hard-codes) and ``MaterialProperties``
+(common/DataStructures.h:20-28).  The work runs on the GPU through the C ABI
+(include/sbr.h); nothing here computes propagation on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .scenes import Scene, Request as WorkRequest
+
+
+@dataclass
+class MaterialProperties:
+    frequency: float = 0.0
+    transmissionLoss: float = 0.0
+    reflectionLoss: float = 0.0
+    relPermittivityRe: float = 1.0
+    relPermittivityIm: float = 0.0
+    relConductivity: float = 0.0
+
+    def as_c(self) -> _lib.Material:
+        return _lib.Material(self.frequency, self.transmissionLoss, self.reflectionLoss,
+                             self.relPermittivityRe, self.relPermittivityIm, self.relConductivity)
+
+
+@dataclass
+class GlobalConfig:
+    """Settings the reference hard-codes.  antennaType 1 (Hertzian) is what
+    FieldCompute.cpp:117 always uses; fieldPrecision 'fp64' reproduces the
+    reference arithmetic, 'fp32' computes per-path rotations and Fresnel
+    coefficients in FP32 (FP64 length and phase, compensated FP32 sums)."""
+
+    antennaType: int = 1
+    fieldPrecision: str = "fp64"
+
+
+@dataclass
+class Mesh:
+    """The reference's std::vector<Triangle*>: float vertices and facet
+    normals in file order, per-triangle material ids (Triangle::materialId,
+    default 0)."""
+
+    vertices: np.ndarray   # (n, 3, 3) float32
+    normals: np.ndarray    # (n, 3) float32
+    materialId: np.ndarray  # (n,) int32
+
+    def __len__(self) -> int:
+        return int(self.vertices.shape[0])
+
+
+class Preprocessor:
+    """Namespace of free functions (Preprocessor.h:18-75)."""
+
+    @staticmethod
+    def StlToGeometry(fileName: str, output: Optional[list] = None, saveEdges: bool = False,
+                      saveFaces: bool = False, dataDir: str = "") -> Mesh:
+        data = open(fileName, "rb").read()
+        head = data[:256].lower()
+        if b"solid" in head and b"\n" in head and b"facet" in head and b"normal" in head:
+            v, n = [], []
+            for line in data.decode(errors="replace").splitlines():
+                t = line.split()
+                if not t:
+                    continue
+                if t[0] == "vertex":
+                    v.append([float(x) for x in t[1:4]])
+                elif t[0] == "facet":
+                    n.append([float(x) for x in t[2:5]])
+            vv = np.asarray(v, np.float64).astype(np.float32).reshape(-1, 3, 3)
+            nn = np.asarray(n, np.float64).astype(np.float32).reshape(-1, 3)
+        else:
+            cnt = int.from_bytes(data[80:84], "little")
+            rec = np.frombuffer(data, dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)),
+                                                       ("a", "<u2")]), count=cnt, offset=84)
+            vv = np.array(rec["v"], dtype=np.float32)
+            nn = np.array(rec["n"], dtype=np.float32)
+        mesh = Mesh(vv, nn, np.zeros(len(vv), np.int32))
+        if output is not None:
+            output.append(mesh)
+        return mesh
+
+    @staticmethod
+    def GenerateRxPlane(xMin, yMin, xMax, yMax, height, resolution, output: list) -> None:
+        nx = int((xMax - xMin) / resolution)
+        ny = int((yMax - yMin) / resolution)
+        for i in range(nx + 1):
+            x = xMin + i * resolution
+            for j in range(ny + 1):
+                output.append((x, yMin + j * resolution, height))
+
+    @staticmethod
+    def GenerateRXLine(start, end, resolution, output: list) -> None:
+        s = np.asarray(start, np.float64)
+        d = np.asarray(end, np.float64) - s
+        n = int(math.floor(math.sqrt(float(d @ d)) / resolution))
+        nrm = math.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
+        d = d / nrm if nrm > 0 else d
+        for i in range(n):
+            output.append(tuple(s + (i * resolution) * d))
+
+    @staticmethod
+    def ReadLocationFile(fileName: str, output: list) -> bool:
+        try:
+            with open(fileName) as fh:
+                for line in fh:
+                    t = line.split()
+                    if len(t) == 3:
+                        try:
+                            output.append(tuple(float(x) for x in t))
+                        except ValueError:
+                            continue
+            return True
+        except OSError:
+            return False
+
+
+class BVH:
+    """BVH<Triangle> (BVH/BVH.h:13-37).  The SAH build runs inside the scene
+    upload (sbr_scene_create); ConstructBVH records the mesh, and, like the
+    reference, the order it leaves the caller's triangle vector in is the one
+    image correction and the field stage index by triangle id."""
+
+    def __init__(self):
+        self.mesh: Optional[Mesh] = None
+
+    def ConstructBVH(self, objects: Mesh) -> None:
+        self.mesh = objects
+
+
+class DeviceScene:
+    """Resident scene (triangles, BVH, materials) on the GPU."""
+
+    def __init__(self, mesh: Mesh, materials: Sequence[MaterialProperties]):
+        lib = _lib.load()
+        mats = (_lib.Material * len(materials))(*[m.as_c() for m in materials])
+        v = np.ascontiguousarray(mesh.vertices, np.float32)
+        n = np.ascontiguousarray(mesh.normals, np.float32)
+        ids = np.ascontiguousarray(mesh.materialId, np.int32)
+        h = C.c_void_p()
+        _lib.check(lib.sbr_scene_create(
+            len(mesh), v.ctypes.data_as(C.POINTER(C.c_float)),
+            n.ctypes.data_as(C.POINTER(C.c_float)), ids.ctypes.data_as(C.POINTER(C.c_int)),
+            mats, len(materials), C.byref(h)))
+        self.handle = h
+        self.n_triangles = len(mesh)
+        self._lib = lib
+
+    @classmethod
+    def from_scene(cls, scene: Scene) -> "DeviceScene":
+        mats = [MaterialProperties(*m) for m in scene.materials]
+        return cls(Mesh(scene.tri, scene.normal, scene.material_id), mats)
+
+    def info(self) -> _lib.SceneInfo:
+        out = _lib.SceneInfo()
+        _lib.check(self._lib.sbr_scene_info_get(self.handle, C.byref(out)))
+        return out
+
+    def mesh_order(self) -> np.ndarray:
+        out = np.zeros(self.n_triangles, np.int32)
+        _lib.check(self._lib.sbr_scene_mesh_order(self.handle, out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
+    def set_mesh_order(self, order: np.ndarray) -> None:
+        o = np.ascontiguousarray(order, np.int32)
+        _lib.check(self._lib.sbr_scene_set_mesh_order(self.handle, o.ctypes.data_as(C.POINTER(C.c_int))))
+
+    def coplanar_ids(self) -> np.ndarray:
+        out = np.zeros(self.n_triangles, np.int32)
+        _lib.check(self._lib.sbr_scene_coplanar_ids(self.handle, out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.sbr_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Result:
+    field: np.ndarray          # (n_rx, 3) complex128
+    counts: dict
+    timing: dict
+    paths: List[dict] = field(default_factory=list)
+
+
+def make_request(tx, tx_coord_sys, max_reflection, max_transmission, frequency, pt, use_fresnel,
+                 rx: np.ndarray, tessellation: int, antenna: int = 1,
+                 precision: str = "fp64") -> tuple:
+    rx = np.ascontiguousarray(rx, np.float64).reshape(-1, 3)
+    q = _lib.Request()
+    for i in range(3):
+        q.tx[i] = float(tx[i])
+    cs = np.asarray(tx_coord_sys, np.float64).reshape(9)
+    for i in range(9):
+        q.tx_coord_sys[i] = float(cs[i])
+    q.max_reflection = int(max_reflection)
+    q.max_transmission = int(max_transmission)
+    q.frequency = float(frequency)
+    q.pt = float(pt)
+    q.use_fresnel = 1 if use_fresnel else 0
+    q.tessellation = int(tessellation)
+    q.antenna = int(antenna)
+    q.field_precision = 1 if precision == "fp32" else 0
+    q.n_rx = int(rx.shape[0])
+    q.rx = rx.ctypes.data_as(C.POINTER(C.c_double))
+    q.rx_on_device = 0
+    return q, rx  # keep rx alive with the request
+
+
+def request_from_workload(req: WorkRequest, precision: str = "fp64") -> tuple:
+    return make_request(req.tx, req.tx_coord_sys, req.max_reflection, req.max_transmission,
+                        req.frequency, req.pt, req.use_fresnel, req.rx, req.tessellation,
+                        req.antenna, precision)
+
+
+def solve(scene: DeviceScene, requests, with_paths: bool = True) -> Result:
+    """Runs one or more requests (a batch) and returns fields, counts and paths."""
+    lib = _lib.load()
+    if isinstance(requests, tuple) and len(requests) == 2 and isinstance(requests[0], _lib.Request):
+        requests = [requests]  # one (request, receiver array) pair
+    arr = (_lib.Request * len(requests))(*[r[0] for r in requests])
+    h = C.c_void_p()
+    _lib.check(lib.sbr_solve_batch(scene.handle, arr, len(requests), C.byref(h)))
+    try:
+        cnt = _lib.Counts()
+        _lib.check(lib.sbr_result_counts(h, C.byref(cnt)))
+        n_rx = sum(r[0].n_rx for r in requests)
+        f = np.zeros(6 * n_rx, np.float64)
+        if n_rx:
+            _lib.check(lib.sbr_result_field(h, f.ctypes.data_as(C.POINTER(C.c_double))))
+        tm = _lib.Timing()
+        _lib.check(lib.sbr_result_timing(h, C.byref(tm)))
+        counts = {k: int(getattr(cnt, k)) for k, _ in _lib.Counts._fields_}
+        timing = {k: float(getattr(tm, k)) for k, _ in _lib.Timing._fields_}
+        paths = []
+        if with_paths and cnt.paths:
+            P = (_lib.Path * cnt.paths)()
+            nr = max(1, cnt.rays)
+            tri = np.zeros(nr, np.int32)
+            cop = np.zeros(nr, np.int32)
+            kind = np.zeros(nr, np.int32)
+            pts = np.zeros(6 * nr, np.float64)
+            ip = C.POINTER(C.c_int)
+            _lib.check(lib.sbr_result_paths(h, P, tri.ctypes.data_as(ip), cop.ctypes.data_as(ip),
+                                            kind.ctypes.data_as(ip),
+                                            pts.ctypes.data_as(C.POINTER(C.c_double))))
+            for p in P:
+                o, n = int(p.ray_offset), int(p.n_rays)
+                paths.append({
+                    "request": p.request, "receiver": p.receiver, "launch": int(p.launch),
+                    "heap": p.heap, "n_rays": n, "tri": tri[o:o + n].tolist(),
+                    "cop": cop[o:o + n].tolist(), "kind": kind[o:o + n].tolist(),
+                    "points": pts[6 * o:6 * (o + n)].reshape(n, 6).copy(),
+                    "field": np.array(p.field[:], np.float64)})
+        fc = f.reshape(-1, 3, 2)
+        field_c = fc[..., 0] + 1j * fc[..., 1]
+        return Result(field_c, counts, timing, paths)
+    finally:
+        lib.sbr_result_destroy(h)
+
+
+class FieldCompute:
+    """FieldCompute (FieldCompute.h:9-94): the field stage is fused into the
+    GPU solve; FieldAtReceiver reads the result."""
+
+    def __init__(self, result: Result):
+        self._result = result
+
+    def FieldAtReceiver(self, receiverId: int) -> np.ndarray:
+        return self._result.field[receiverId]
+
+
+class RTSolver:
+    """RTSolver (RTSolver.h:18-83)."""
+
+    def __init__(self, config: Optional[GlobalConfig] = None):
+        self.config = config or GlobalConfig()
+        self._scene: Optional[DeviceScene] = None
+        self._result: Optional[Result] = None
+        self._receivers = None
+
+    def Init(self, materialProperties: Sequence[MaterialProperties], materialPropertiesCount: int,
+             triangles: BVH) -> int:
+        if triangles.mesh is None:
+            raise ValueError("BVH.ConstructBVH was not called")
+        self._scene = DeviceScene(triangles.mesh, list(materialProperties)[:materialPropertiesCount])
+        return 0
+
+    def ExecuteRayTracing(self, sourcePoint, txCoordSys, maxReflectionCount: int,
+                          maxTransmissionCount: int, frequency: float, pt: float,
+                          useFresnelCoeff: bool, receivers, triangleMesh: Mesh,
+                          txTesslation: int) -> int:
+        if self._scene is None:
+            raise RuntimeError("Init was not called")
+        rx = np.asarray(receivers, np.float64).reshape(-1, 3)
+        req = make_request(sourcePoint, txCoordSys, maxReflectionCount, maxTransmissionCount,
+                           frequency, pt, useFresnelCoeff, rx, txTesslation,
+                           self.config.antennaType, self.config.fieldPrecision)
+        self._result = solve(self._scene, req)
+        self._receivers = rx
+        return int(self._result.counts["launches"]) * int(rx.shape[0])
+
+    @property
+    def result(self) -> Result:
+        return self._result
+
+    def field_compute(self) -> FieldCompute:
+        return FieldCompute(self._result)
+
+    def SaveFieldAsCsv(self, fname: str) -> bool:
+        """RTSolver::SaveFieldAsCsv (RTSolver.cpp:692-717), including its
+        sticky std::showpos after the first receiver row."""
+        rx, f = self._receivers, self._result.field
+
+        def num(x: float, plus: bool) -> str:
+            s = "%g" % x
+            if s in ("inf", "-inf", "nan", "-nan"):
+                s = s
+            return ("+" + s) if plus and not s.startswith("-") else s
+
+        with open(fname, "w") as fh:
+            fh.write("X,Y,Z,Ex,Ey,Ez\n")
+            for i in range(len(rx)):
+                p = i > 0
+                fh.write(",".join(num(v, p) for v in rx[i]) + ",")
+                fh.write(",".join(num(c.real, True) + num(c.imag, True) + "i" for c in f[i]) + "\n")
+        return True

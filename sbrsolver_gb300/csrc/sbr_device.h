@@ -1,0 +1,200 @@
+// Device data layout and arithmetic shared by the SBR kernels.
+//
+// Precision scheme.  Every decision that selects a path (which triangle a
+// ray hits, whether a receiver is inside a reception sphere, whether an image
+// correction finds its facet) must come out exactly as the reference's FP64
+// code decides it.  Two kinds of arithmetic are therefore used:
+//   * x64::* — FP64 with __dadd_rn/__dmul_rn/__ddiv_rn/__dsqrt_rn, which are
+//     never contracted into FMA, evaluated in the reference's operation order.
+//     On IEEE hardware these give bit-identical results to the reference
+//     compiled without FP contraction.  They carry the ray state (origins,
+//     directions, path lengths) and settle every close decision.
+//   * FP32 filters with explicit error margins.  They answer the common case
+//     (a triangle clearly missed, a receiver clearly outside its sphere) and
+//     hand anything within the margin to the FP64 form.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sbr {
+
+constexpr uint32_t kRootClass = 0xFFFFFFFFu;  // class id of the empty path prefix
+constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
+constexpr int kHeapBits = 17;                  // rank = launch << 17 | BFS heap index
+constexpr int kMaxDepth = 16;                  // max interactions per path (R + T)
+constexpr int kStack = 96;                     // traversal stack entries
+
+// FP32 traversal node: the boxes of both children of one reference BVH node.
+// child >= 0: internal node index; child < 0: ~(leaf node index).
+struct __align__(16) Node32 {
+  float lo0[3], hi0[3], lo1[3], hi1[3];
+  int child[2];
+  int pad[2];
+};
+
+// FP64 reference node (depth-first numbering).
+struct RefNode {
+  double bb[6];
+  int c0, c1, first, count, parent, pad;
+};
+
+// Triangle, depth-first leaf order (index == closest-hit tie rank).
+struct __align__(16) Tri32 {
+  float v1[3], nv1;  // |v1|
+  float e1[3], ne1;  // |e1|
+  float e2[3], ne2;  // |e2|
+};
+struct Tri64 {
+  double v1[3], e1[3], e2[3], n[3];
+  int id, cop, mat, node;  // node: leaf that holds it
+};
+
+// What the reference's triangleMesh[i] holds for position i of the caller's
+// vector (after ConstructBVH reordered it): used by image correction and the
+// field stage, which index the mesh by triangle id.
+struct CorrTri {
+  double v1[3], e1[3], e2[3], n[3], cs[9];
+  int mat, pad;
+};
+
+struct Material {
+  double eps_re, sigma;
+};
+
+struct DevScene {
+  const Node32* node32;
+  const RefNode* ref;
+  const Tri32* tri32;
+  const Tri64* tri64;
+  const CorrTri* corr;
+  const Material* mats;
+  int n_tri, n_nodes, n_mats;
+  int root_leaf;
+  float box_margin;  // absolute FP32 box expansion (metres)
+};
+
+// One ray of the wavefront: the RayLaunch call that will create one tree node.
+struct __align__(16) RayRec {
+  double o[3], d[3];
+  double total;    // totalPathLength argument of RayLaunch (RTSolver.cpp:137)
+  double S;        // pathLength argument RayCapture will give the node (RTSolver.cpp:288)
+  uint32_t parent; // node index of the parent, 0xFFFFFFFF for a root
+  uint32_t cls;    // class (interned tri/kind prefix) of the node
+  uint32_t cop;    // coplanar-prefix class of the node
+  uint32_t launch;
+  uint32_t heap;   // BFS heap index (root 1, transmit child 2h, reflect child 2h+1)
+  uint16_t rc, tc;
+  uint32_t tx;     // transmitter (request) index
+  uint32_t pad;
+};
+
+// One executed segment (tree node).
+struct __align__(16) NodeRec {
+  double s[3], t[3];
+  double S;
+  uint32_t parent, cls, launch, heap;
+  float u[3], len;  // FP32 unit direction and length for the capture filter
+  uint32_t tx, pad;
+};
+
+// Per transmitter (one request of a batch).
+struct TxParams {
+  double tx[3];
+  double txcs[9];
+  double freq, pt, tan_beta, k;
+  double cmax;       // max |receiver| of this request's receivers
+  int R, T, antenna, fresnel;
+  int n_launch, level;
+  int rx_first, n_rx;          // receivers of this request in the batch arrays
+  long long launch_first;      // first global launch index
+  int grid;                    // receiver grid index
+  int pad;
+};
+
+struct RxGrid {
+  float org[3], cell;
+  int dim[3], pad;
+  const int* cell_start;  // ncell + 1
+  const float4* rx32;     // sorted by cell: xyz, w = receiver index (int bits)
+  float bmin[3], bmax[3];
+};
+
+struct HashTable {
+  unsigned long long* keys;
+  uint32_t mask;
+};
+
+struct ClassInfo {
+  uint32_t parent;
+  int tri;
+  uint32_t cop;
+  uint8_t kind, depth, pad0, pad1;
+};
+
+struct Counters {
+  unsigned long long nodes;      // executed segments
+  unsigned long long queue[kMaxDepth + 2];
+  unsigned long long events;     // captured paths (before correction)
+  unsigned long long corrected;  // captured paths whose correction succeeded
+  unsigned long long survivors;
+  unsigned long long fp64_tri;   // exact triangle tests run
+  unsigned long long fallback;   // rays that needed the reference-order traversal
+  unsigned long long fp64_capture;
+  unsigned int overflow;         // bit mask of capacity overflows
+  unsigned int pad;
+};
+
+enum OverflowBits : unsigned {
+  kOvNodes = 1, kOvQueue = 2, kOvClass = 4, kOvCop = 8, kOvGroup = 16, kOvDedup = 32,
+  kOvSurv = 64, kOvStack = 128
+};
+
+// ------------------------------------------------------------------ FP64
+namespace x64 {
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double sqrt_(double a) { return __dsqrt_rn(a); }
+// ((a0 b0 + a1 b1) + a2 b2): Eigen's reduction order for 3-vectors
+__device__ __forceinline__ double dot(const double* a, const double* b) {
+  return add(add(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2]));
+}
+__device__ __forceinline__ double sqn(const double* a) { return dot(a, a); }
+__device__ __forceinline__ double norm(const double* a) { return sqrt_(sqn(a)); }
+__device__ __forceinline__ void cross(const double* a, const double* b, double* r) {
+  r[0] = sub(mul(a[1], b[2]), mul(a[2], b[1]));
+  r[1] = sub(mul(a[2], b[0]), mul(a[0], b[2]));
+  r[2] = sub(mul(a[0], b[1]), mul(a[1], b[0]));
+}
+__device__ __forceinline__ void sub3(const double* a, const double* b, double* r) {
+  r[0] = sub(a[0], b[0]);
+  r[1] = sub(a[1], b[1]);
+  r[2] = sub(a[2], b[2]);
+}
+__device__ __forceinline__ void normalize(const double* a, double* r) {
+  double z = sqn(a);
+  if (z > 0) {
+    double s = sqrt_(z);
+    r[0] = div(a[0], s);
+    r[1] = div(a[1], s);
+    r[2] = div(a[2], s);
+  } else {
+    r[0] = a[0];
+    r[1] = a[1];
+    r[2] = a[2];
+  }
+}
+}  // namespace x64
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  x ^= x >> 31;
+  return x;
+}
+
+}  // namespace sbr

@@ -1,0 +1,1610 @@
+// GB300 SBR engine: device-resident scene, wavefront ray tracing, reception
+// capture, image correction, duplicate removal and the received field, behind
+// the C ABI declared in include/sbr.h.
+//
+// Pipeline per solve (one CUDA stream, no host round trip between stages):
+//   grid     receivers -> uniform grid (bbox, count, scan, scatter)
+//   trace    one kernel per bounce depth over a compacted wavefront queue;
+//            each ray runs the closest-hit query, writes its tree node and
+//            spawns its reflected / transmitted children (RTSolver.cpp:128-257)
+//   capture  every node tests the receivers near its segment against its
+//            reception sphere (RTSolver.cpp:805-863); a capture counts unless an
+//            ancestor captured the same receiver (RayCapture deletes the
+//            subtree, RTSolver.cpp:277-284).  Captures are grouped by
+//            (receiver, path class) with the minimum (launch, BFS) rank
+//   correct  one image-method correction per group (RTSolver.cpp:299-433)
+//   dedup    minimum rank per (receiver, coplanar key) over corrected groups
+//            (RTSolver.cpp:435-459); the minimum is the reference's survivor
+//   field    per survivor (FieldCompute.cpp:71-151), summed per receiver in
+//            (launch, BFS) order (FieldCompute.cpp:11-25)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sbr.h"
+#include "sbr_device.h"
+#include "sbr_field.cuh"
+#include "sbr_host.h"
+#include "sbr_kernels.cuh"
+
+namespace sbr {
+
+// ------------------------------------------------------------ error state
+static thread_local std::string g_err;
+static void set_err(const std::string& s) { g_err = s; }
+
+struct CudaError {
+  cudaError_t e;
+  std::string where;
+};
+#define CK(x)                                                             \
+  do {                                                                    \
+    cudaError_t _e = (x);                                                 \
+    if (_e != cudaSuccess) throw CudaError{_e, std::string(#x)};          \
+  } while (0)
+
+// ------------------------------------------------------------ device buffer
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void ensure(size_t want) {
+    if (want <= n) return;
+    release();
+    if (want == 0) return;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, want * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw CudaError{e, "cudaMalloc " + std::to_string(want * sizeof(T)) + " bytes"};
+    }
+    p = static_cast<T*>(q);
+    n = want;
+  }
+  void upload(const T* src, size_t cnt, cudaStream_t st) {
+    ensure(cnt);
+    if (cnt) CK(cudaMemcpyAsync(p, src, cnt * sizeof(T), cudaMemcpyHostToDevice, st));
+  }
+};
+
+static uint32_t next_pow2(uint64_t x) {
+  uint64_t p = 1;
+  while (p < x) p <<= 1;
+  return uint32_t(std::min<uint64_t>(p, 1ull << 31));
+}
+
+// ============================================================ kernels
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated slot reservation: every active lane asks for `cnt` (0..2)
+// entries; one atomicAdd per warp.
+__device__ __forceinline__ unsigned long long warp_reserve(unsigned long long* ctr, unsigned cnt) {
+  const unsigned mask = __activemask();
+  const unsigned b1 = __ballot_sync(mask, cnt >= 1);
+  const unsigned b2 = __ballot_sync(mask, cnt >= 2);
+  const unsigned lt = (1u << lane_id()) - 1u;
+  const unsigned before = __popc(b1 & lt) + __popc(b2 & lt);
+  const unsigned total = __popc(b1) + __popc(b2);
+  const int leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if (lane_id() == unsigned(leader) && total) base = atomicAdd(ctr, (unsigned long long)total);
+  base = __shfl_sync(mask, base, leader);
+  return base + before;
+}
+
+__device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long key, unsigned* ov,
+                                              unsigned bit) {
+  uint32_t h = uint32_t(mix64(key)) & t.mask;
+  for (uint32_t i = 0; i <= t.mask; ++i) {
+    unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&t.keys[h]);
+    if (k == key) return h;
+    if (k == kEmptyKey) {
+      unsigned long long old = atomicCAS(&t.keys[h], kEmptyKey, key);
+      if (old == kEmptyKey || old == key) return h;
+    }
+    h = (h + 1) & t.mask;
+  }
+  atomicOr(ov, bit);
+  return 0xFFFFFFFFu;
+}
+
+__device__ __forceinline__ uint32_t ht_find(HashTable t, unsigned long long key) {
+  uint32_t h = uint32_t(mix64(key)) & t.mask;
+  for (uint32_t i = 0; i <= t.mask; ++i) {
+    unsigned long long k = t.keys[h];
+    if (k == key) return h;
+    if (k == kEmptyKey) return 0xFFFFFFFFu;
+    h = (h + 1) & t.mask;
+  }
+  return 0xFFFFFFFFu;
+}
+
+__global__ void k_fill_u64(unsigned long long* p, size_t n, unsigned long long v) {
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+       i += size_t(gridDim.x) * blockDim.x)
+    p[i] = v;
+}
+
+// ---- receiver grid ------------------------------------------------------
+
+// Order-preserving float <-> int mapping for atomicMin/Max on floats.
+__device__ __forceinline__ int f2o(float f) {
+  int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
+
+struct GridBuild {
+  int bmin[3], bmax[3];  // ordered ints
+  float cmax;            // max |rx| (as float, atomicMax on ordered int below)
+  int cmax_o;
+  int ncell;
+};
+
+__global__ void k_rx_bounds(const double* rx, const TxParams* txp, int n_tx, GridBuild* gb) {
+  const int r = blockIdx.y;  // request
+  if (r >= n_tx) return;
+  const TxParams& P = txp[r];
+  int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN}, cm = INT_MIN;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_rx; i += gridDim.x * blockDim.x) {
+    const double* c = rx + 3 * size_t(P.rx_first + i);
+    float c32[3] = {float(c[0]), float(c[1]), float(c[2])};
+    for (int a = 0; a < 3; ++a) {
+      mn[a] = min(mn[a], f2o(c32[a]));
+      mx[a] = max(mx[a], f2o(c32[a]));
+    }
+    cm = max(cm, f2o(float(sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]))));
+  }
+  for (int a = 0; a < 3; ++a) {
+    for (int o = 16; o; o >>= 1) {
+      mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+      mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+    }
+  }
+  for (int o = 16; o; o >>= 1) cm = max(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+  if (lane_id() == 0) {
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&gb[r].bmin[a], mn[a]);
+      atomicMax(&gb[r].bmax[a], mx[a]);
+    }
+    atomicMax(&gb[r].cmax_o, cm);
+  }
+}
+
+// Grid shape: cells of equal size sized for ~4 receivers per cell over the
+// axes with extent, at most max_cells cells.
+__global__ void k_grid_shape(GridBuild* gb, RxGrid* grids, const TxParams* txp, int n_tx,
+                             int max_cells, int* cell_base) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int base = 0;
+  for (int r = 0; r < n_tx; ++r) {
+    RxGrid& g = grids[r];
+    float lo[3], hi[3], ext[3];
+    float emax = 0;
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = o2f(gb[r].bmin[a]);
+      hi[a] = o2f(gb[r].bmax[a]);
+      if (txp[r].n_rx == 0) lo[a] = hi[a] = 0;
+      ext[a] = hi[a] - lo[a];
+      emax = fmaxf(emax, ext[a]);
+    }
+    int k = 0;
+    double vol = 1;
+    for (int a = 0; a < 3; ++a)
+      if (ext[a] > 1e-6f * emax && ext[a] > 0) {
+        ++k;
+        vol *= ext[a];
+      }
+    float cell = 1.0f;
+    if (k > 0) {
+      double target = fmax(1.0, txp[r].n_rx / 4.0);
+      cell = float(pow(vol / target, 1.0 / k));
+    }
+    if (cell <= 0) cell = 1.0f;
+    int dim[3];
+    long long tot;
+    for (;;) {
+      tot = 1;
+      for (int a = 0; a < 3; ++a) {
+        dim[a] = max(1, min(1 << 20, int(ext[a] / cell) + 1));
+        tot *= dim[a];
+      }
+      if (tot <= max_cells) break;
+      cell *= 1.25f;
+    }
+    for (int a = 0; a < 3; ++a) {
+      g.org[a] = lo[a];
+      g.dim[a] = dim[a];
+      g.bmin[a] = lo[a];
+      g.bmax[a] = hi[a];
+    }
+    g.cell = cell;
+    gb[r].ncell = int(tot);
+    gb[r].cmax = o2f(gb[r].cmax_o);
+    cell_base[r] = base;
+    base += int(tot) + 1;
+  }
+  cell_base[n_tx] = base;
+}
+
+__device__ __forceinline__ int cell_of(const RxGrid& g, float x, float y, float z) {
+  int ix = min(g.dim[0] - 1, max(0, int((x - g.org[0]) / g.cell)));
+  int iy = min(g.dim[1] - 1, max(0, int((y - g.org[1]) / g.cell)));
+  int iz = min(g.dim[2] - 1, max(0, int((z - g.org[2]) / g.cell)));
+  return (iz * g.dim[1] + iy) * g.dim[0] + ix;
+}
+
+__global__ void k_rx_count(const double* rx, const TxParams* txp, int n_tx, const RxGrid* grids,
+                           const int* cell_base, int* counts) {
+  const int r = blockIdx.y;
+  if (r >= n_tx) return;
+  const RxGrid g = grids[r];
+  const TxParams& P = txp[r];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_rx; i += gridDim.x * blockDim.x) {
+    const double* c = rx + 3 * size_t(P.rx_first + i);
+    atomicAdd(&counts[cell_base[r] + cell_of(g, float(c[0]), float(c[1]), float(c[2]))], 1);
+  }
+}
+
+// Single-block exclusive scan (n up to a few million): each thread scans a
+// contiguous chunk, then the chunk totals are scanned across the block.
+__global__ void k_scan_exclusive(const int* in, int* out, int n) {
+  __shared__ int part[1024];
+  const int t = threadIdx.x, T = blockDim.x;
+  const int chunk = (n + T - 1) / T;
+  const int b = min(n, t * chunk), e = min(n, b + chunk);
+  int s = 0;
+  for (int i = b; i < e; ++i) s += in[i];
+  part[t] = s;
+  __syncthreads();
+  for (int off = 1; off < T; off <<= 1) {
+    int v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int run = t ? part[t - 1] : 0;
+  for (int i = b; i < e; ++i) {
+    int v = in[i];
+    out[i] = run;
+    run += v;
+  }
+  if (t == T - 1) out[n] = part[T - 1];
+}
+
+__global__ void k_rx_scatter(const double* rx, const TxParams* txp, int n_tx, const RxGrid* grids,
+                             const int* cell_base, const int* starts, int* cursor, float4* rx32) {
+  const int r = blockIdx.y;
+  if (r >= n_tx) return;
+  const RxGrid g = grids[r];
+  const TxParams& P = txp[r];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_rx; i += gridDim.x * blockDim.x) {
+    const int gi = P.rx_first + i;
+    const double* c = rx + 3 * size_t(gi);
+    const int cid = cell_base[r] + cell_of(g, float(c[0]), float(c[1]), float(c[2]));
+    const int pos = starts[cid] + atomicAdd(&cursor[cid], 1);
+    rx32[pos] = make_float4(float(c[0]), float(c[1]), float(c[2]), __int_as_float(gi));
+  }
+}
+
+__global__ void k_grid_finish(RxGrid* grids, const int* starts, const int* cell_base,
+                              const float4* rx32, int n_tx) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_tx) return;
+  grids[r].cell_start = starts + cell_base[r];
+  grids[r].rx32 = rx32;
+}
+
+// ---- trace ------------------------------------------------------------------
+
+struct TraceArgs {
+  DevScene sc;
+  const TxParams* txp;
+  int n_tx;
+  const double* const* dirs;  // per level
+  const RayRec* in;
+  RayRec* out;
+  unsigned long long out_cap;
+  NodeRec* nodes;
+  unsigned long long node_cap;
+  HashTable cls_tab, cop_tab;
+  ClassInfo* cls_info;
+  const int* tri_cop;  // coplanar id by rank
+  Counters* ctr;
+  int depth;
+  long long n_root;    // total launches (depth 0)
+};
+
+__device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long long g) {
+  int lo = 0, hi = n_tx - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (txp[mid].launch_first <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
+  const long long n_in =
+      A.depth == 0 ? A.n_root
+                   : (long long)min(A.ctr->queue[A.depth], (unsigned long long)A.out_cap);
+  TraceStats st{0, 0};
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in; i += stride) {
+    RayRec r;
+    if (A.depth == 0) {
+      const int q = find_request(A.txp, A.n_tx, i);
+      const TxParams& P = A.txp[q];
+      const long long li = i - P.launch_first;
+      const double* d = A.dirs[P.level] + 3 * li;
+      r.o[0] = P.tx[0]; r.o[1] = P.tx[1]; r.o[2] = P.tx[2];
+      r.d[0] = d[0]; r.d[1] = d[1]; r.d[2] = d[2];
+      r.total = 0.0;
+      r.S = 0.0;
+      r.parent = 0xFFFFFFFFu;
+      r.cls = kRootClass;
+      r.cop = kRootClass;
+      r.launch = uint32_t(li);
+      r.heap = 1;
+      r.rc = r.tc = 0;
+      r.tx = uint32_t(q);
+    } else {
+      r = A.in[i];
+    }
+    const TxParams& P = A.txp[r.tx];
+    Hit h;
+    const bool hit = closest_hit(A.sc, r.o, r.d, h, st, &A.ctr->overflow);
+    const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
+    const bool root = A.depth == 0;
+    if (ni < A.node_cap) {
+      NodeRec n;
+      n.s[0] = r.o[0]; n.s[1] = r.o[1]; n.s[2] = r.o[2];
+      if (hit) {
+        n.t[0] = h.p[0]; n.t[1] = h.p[1]; n.t[2] = h.p[2];
+        n.len = float(h.dist);
+      } else {
+        const double sc = root ? 1E10 : 1E2;  // RTSolver.cpp:231,249
+        n.t[0] = x64::add(r.o[0], x64::mul(r.d[0], sc));
+        n.t[1] = x64::add(r.o[1], x64::mul(r.d[1], sc));
+        n.t[2] = x64::add(r.o[2], x64::mul(r.d[2], sc));
+        n.len = float(sc);
+      }
+      n.u[0] = float(r.d[0]); n.u[1] = float(r.d[1]); n.u[2] = float(r.d[2]);
+      n.S = r.S;
+      n.parent = r.parent;
+      n.cls = r.cls;
+      n.launch = r.launch;
+      n.heap = r.heap;
+      n.tx = r.tx;
+      n.pad = 0;
+      A.nodes[ni] = n;
+    } else {
+      atomicOr(&A.ctr->overflow, kOvNodes);
+    }
+    // children (RTSolver.cpp:186-221)
+    unsigned nch = 0;
+    bool do_r = false, do_t = false;
+    if (hit) {
+      do_r = r.rc < P.R;
+      do_t = r.tc < P.T;
+      nch = unsigned(do_r) + unsigned(do_t);
+    }
+    const unsigned long long base = warp_reserve(&A.ctr->queue[A.depth + 1], nch);
+    if (nch) {
+      const Tri64& T = A.sc.tri64[h.rank];
+      const double cum = x64::add(r.total, h.dist);  // node pathLength
+      RayRec c;
+      c.o[0] = h.p[0]; c.o[1] = h.p[1]; c.o[2] = h.p[2];
+      c.total = cum;
+      c.S = x64::add(r.S, cum);
+      c.parent = uint32_t(ni);
+      c.launch = r.launch;
+      c.tx = r.tx;
+      c.pad = 0;
+      const int cop = A.tri_cop[h.rank];
+      const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
+      const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop);
+      unsigned long long slot = base;
+      if (do_t) {  // transmitted: same direction, heap 2h
+        c.d[0] = r.d[0]; c.d[1] = r.d[1]; c.d[2] = r.d[2];
+        c.heap = r.heap * 2;
+        c.rc = r.rc;
+        c.tc = r.tc + 1;
+        const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
+        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass);
+        c.cop = cop_cls;
+        if (c.cls != 0xFFFFFFFFu) {
+          A.cls_info[c.cls] = ClassInfo{r.cls, h.rank, cop_cls, uint8_t(2), uint8_t(A.depth + 1), 0, 0};
+        }
+        if (slot < A.out_cap) A.out[slot] = c;
+        else atomicOr(&A.ctr->overflow, kOvQueue);
+        ++slot;
+      }
+      if (do_r) {  // reflected: Reflect(d, n).normalized(), heap 2h+1
+        const double dn = x64::dot(T.n, r.d);
+        double v[3];
+        for (int a = 0; a < 3; ++a) v[a] = x64::sub(r.d[a], x64::mul(x64::mul(2.0, T.n[a]), dn));
+        x64::normalize(v, c.d);
+        c.heap = r.heap * 2 + 1;
+        c.rc = r.rc + 1;
+        c.tc = r.tc;
+        const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1);
+        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass);
+        c.cop = cop_cls;
+        if (c.cls != 0xFFFFFFFFu) {
+          A.cls_info[c.cls] = ClassInfo{r.cls, h.rank, cop_cls, uint8_t(1), uint8_t(A.depth + 1), 0, 0};
+        }
+        if (slot < A.out_cap) A.out[slot] = c;
+        else atomicOr(&A.ctr->overflow, kOvQueue);
+      }
+    }
+  }
+  if (st.fp64_tri) atomicAdd(&A.ctr->fp64_tri, (unsigned long long)st.fp64_tri);
+  if (st.fallback) atomicAdd(&A.ctr->fallback, (unsigned long long)st.fallback);
+}
+
+// ---- capture ----------------------------------------------------------------
+
+struct CaptureArgs {
+  const NodeRec* nodes;
+  const TxParams* txp;
+  const RxGrid* grids;
+  const GridBuild* gb;
+  const double* rx;
+  HashTable grp;
+  unsigned long long* grp_rank;
+  unsigned* grp_count;
+  Counters* ctr;
+  unsigned long long node_cap;
+};
+
+__device__ __forceinline__ int capture_test(const NodeRec& n, const float3& c32, const double* c64,
+                                            float tanb32, double tanb, unsigned& n64) {
+  const float3 s = make_float3(float(n.s[0]), float(n.s[1]), float(n.s[2]));
+  const float3 u = make_float3(n.u[0], n.u[1], n.u[2]);
+  int v = reception32(s, u, n.len, float(n.S), c32, tanb32);
+  if (v >= 0) return v;
+  ++n64;
+  return reception64(n.s, n.t, c64, n.S, tanb) ? 1 : 0;
+}
+
+__global__ void __launch_bounds__(128) k_capture(CaptureArgs A) {
+  const unsigned long long n_nodes = min(A.ctr->nodes, A.node_cap);
+  unsigned long long events = 0;
+  unsigned n64 = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+       i < n_nodes; i += (unsigned long long)gridDim.x * blockDim.x) {
+    const NodeRec n = A.nodes[i];
+    const TxParams& P = A.txp[n.tx];
+    if (P.n_rx == 0) continue;
+    const RxGrid g = A.grids[n.tx];
+    const float tanb = float(P.tan_beta);
+    const float S = float(n.S);
+    // Upper bound of any capture radius on this segment: |P| is bounded by
+    // (cmax + S tan b) / (1 - tan b) for any point that can capture.
+    const float cmax = A.gb[n.tx].cmax;
+    const float pmax = (cmax + S * tanb) / fmaxf(1e-6f, 1.0f - tanb) * 1.0001f + 1.0f;
+    const float3 s = make_float3(float(n.s[0]), float(n.s[1]), float(n.s[2]));
+    const float3 u = make_float3(n.u[0], n.u[1], n.u[2]);
+    // parameter range with |s + l u| <= pmax
+    const float su = s.x * u.x + s.y * u.y + s.z * u.z;
+    const float ss = s.x * s.x + s.y * s.y + s.z * s.z;
+    const float disc = su * su - (ss - pmax * pmax);
+    if (disc < 0.0f) continue;
+    const float sq = sqrtf(disc);
+    float lo = fmaxf(0.0f, -su - sq), hi = fminf(n.len, -su + sq);
+    const float rb = (S + pmax) * tanb * 1.0001f + 1e-3f;
+    // clip to the receiver box grown by rb
+    for (int a = 0; a < 3 && lo <= hi; ++a) {
+      const float sa = a == 0 ? s.x : (a == 1 ? s.y : s.z);
+      const float ua = a == 0 ? u.x : (a == 1 ? u.y : u.z);
+      const float bl = g.bmin[a] - rb, bh = g.bmax[a] + rb;
+      if (fabsf(ua) < 1e-20f) {
+        if (sa < bl || sa > bh) hi = -1.0f;
+      } else {
+        float t1 = (bl - sa) / ua, t2 = (bh - sa) / ua;
+        lo = fmaxf(lo, fminf(t1, t2) - 1e-3f);
+        hi = fminf(hi, fmaxf(t1, t2) + 1e-3f);
+      }
+    }
+    if (lo > hi) continue;
+    const float lc = fmaxf(g.cell, 2.0f * rb);
+    int nchunk = int(ceilf((hi - lo) / lc));
+    if (nchunk < 1) nchunk = 1;
+    if (nchunk > 4096) nchunk = 4096;
+    const float step = (hi - lo) / nchunk;
+    const float pad = rb + g.cell * 0.01f + 1e-3f;
+    for (int ch = 0; ch < nchunk; ++ch) {
+      const float a = lo + ch * step, b = (ch == nchunk - 1) ? hi : lo + (ch + 1) * step;
+      float bl[3], bh[3];
+      const float pa[3] = {s.x + a * u.x, s.y + a * u.y, s.z + a * u.z};
+      const float pb[3] = {s.x + b * u.x, s.y + b * u.y, s.z + b * u.z};
+      int c0[3], c1[3];
+      for (int k = 0; k < 3; ++k) {
+        bl[k] = fminf(pa[k], pb[k]) - pad;
+        bh[k] = fmaxf(pa[k], pb[k]) + pad;
+        c0[k] = max(0, int(floorf((bl[k] - g.org[k]) / g.cell)));
+        c1[k] = min(g.dim[k] - 1, int(floorf((bh[k] - g.org[k]) / g.cell)));
+      }
+      for (int iz = c0[2]; iz <= c1[2]; ++iz)
+        for (int iy = c0[1]; iy <= c1[1]; ++iy)
+          for (int ix = c0[0]; ix <= c1[0]; ++ix) {
+            const int cid = (iz * g.dim[1] + iy) * g.dim[0] + ix;
+            const int e = g.cell_start[cid + 1];
+            for (int j = g.cell_start[cid]; j < e; ++j) {
+              const float4 c4 = g.rx32[j];
+              const float3 c = make_float3(c4.x, c4.y, c4.z);
+              const float lam = u.x * (c.x - s.x) + u.y * (c.y - s.y) + u.z * (c.z - s.z);
+              // each receiver is owned by exactly one chunk
+              if (ch > 0 && lam < a) continue;
+              if (ch < nchunk - 1 && lam >= b) continue;
+              const int gi = __float_as_int(c4.w);
+              const double* c64 = A.rx + 3 * size_t(gi);
+              if (!capture_test(n, c, c64, tanb, P.tan_beta, n64)) continue;
+              // suppressed if an ancestor captured the same receiver
+              bool sup = false;
+              for (uint32_t p = n.parent; p != 0xFFFFFFFFu;) {
+                if (p >= A.node_cap) break;  // node pool overflowed: this pass is redone
+                const NodeRec an = A.nodes[p];
+                if (capture_test(an, c, c64, tanb, P.tan_beta, n64)) {
+                  sup = true;
+                  break;
+                }
+                p = an.parent;
+              }
+              if (sup) continue;
+              ++events;
+              const unsigned long long key = (unsigned long long)uint32_t(gi) << 32 | n.cls;
+              const uint32_t slot = ht_insert(A.grp, key, &A.ctr->overflow, kOvGroup);
+              if (slot != 0xFFFFFFFFu) {
+                const unsigned long long rank =
+                    (unsigned long long)n.launch << kHeapBits | n.heap;
+                atomicMin(&A.grp_rank[slot], rank);
+                atomicAdd(&A.grp_count[slot], 1u);
+              }
+            }
+          }
+    }
+  }
+  if (events) atomicAdd(&A.ctr->events, events);
+  if (n64) atomicAdd(&A.ctr->fp64_capture, (unsigned long long)n64);
+}
+
+// ---- correction / dedup -----------------------------------------------------
+
+struct PathBuf {
+  int n;            // rays
+  int tri[kMaxDepth + 1];
+  int kind[kMaxDepth + 1];
+  double pts[kMaxDepth + 2][3];
+};
+
+// Path of a class: tri of each ray (ray i ends on tri[i]; the last ray ends at
+// the receiver) and kind of each ray's start.
+__device__ __forceinline__ bool class_path(const ClassInfo* info, uint32_t cls, PathBuf& pb) {
+  int depth = 0;
+  int tri_rev[kMaxDepth], kind_rev[kMaxDepth];
+  for (uint32_t c = cls; c != kRootClass; c = info[c].parent) {
+    if (depth >= kMaxDepth) return false;
+    tri_rev[depth] = info[c].tri;
+    kind_rev[depth] = info[c].kind;
+    ++depth;
+  }
+  pb.n = depth + 1;
+  pb.kind[0] = 0;
+  for (int i = 0; i < depth; ++i) {
+    pb.tri[i] = tri_rev[depth - 1 - i];   // rank of the triangle hit by ray i
+    pb.kind[i + 1] = kind_rev[depth - 1 - i];
+  }
+  pb.tri[depth] = -1;
+  return true;
+}
+
+struct CorrectArgs {
+  DevScene sc;
+  const TxParams* txp;
+  int n_tx;
+  const double* rx;
+  const int* rx_req;      // request of each receiver
+  HashTable grp;
+  const unsigned long long* grp_rank;
+  const unsigned* grp_count;
+  unsigned char* grp_ok;
+  const ClassInfo* cls_info;
+  HashTable dedup;
+  unsigned long long* dedup_rank;
+  const int* rank_to_id;  // triangle id of each rank
+  Counters* ctr;
+};
+
+// GetImageSources + MultiPathCorrection / DirectPathCorrection
+// (RTSolver.cpp:330-433).  Fills pb.pts with the corrected points.
+__device__ bool correct_path(const DevScene& sc, const int* rank_to_id, const TxParams& P,
+                             const double* rxp, PathBuf& pb, unsigned* overflow) {
+  using namespace x64;
+  const double* tx = P.tx;
+  if (pb.n == 1) {
+    double d[3];
+    sub3(rxp, tx, d);
+    Hit h;
+    const bool has = exact_closest(sc, tx, d, h, overflow);
+    if (has && !(norm(d) < h.dist)) return false;
+    for (int a = 0; a < 3; ++a) {
+      pb.pts[0][a] = tx[a];
+      pb.pts[1][a] = rxp[a];
+    }
+    return true;
+  }
+  const int n = pb.n;
+  double img[kMaxDepth + 1][3];
+  for (int a = 0; a < 3; ++a) img[0][a] = tx[a];
+  for (int i = 0; i + 1 < n; ++i) {
+    const CorrTri& T = sc.corr[rank_to_id[pb.tri[i]]];
+    if (pb.kind[i + 1] == 1) {  // ImagePoint (RTSolver.cpp:910-924)
+      double w[3];
+      sub3(img[i], T.v1, w);
+      const double dist = dot(T.n, w);
+      for (int a = 0; a < 3; ++a) img[i + 1][a] = sub(img[i][a], mul(mul(2.0, dist), T.n[a]));
+    } else {
+      for (int a = 0; a < 3; ++a) img[i + 1][a] = img[i][a];
+    }
+  }
+  double target[3] = {rxp[0], rxp[1], rxp[2]};
+  for (int a = 0; a < 3; ++a) pb.pts[n][a] = rxp[a];
+  for (int i = n - 1; i >= 1; --i) {
+    const CorrTri& T = sc.corr[rank_to_id[pb.tri[i - 1]]];
+    double d[3], P3[3];
+    sub3(target, img[i], d);
+    if (!mt64c(T, img[i], d, P3)) return false;
+    for (int a = 0; a < 3; ++a) {
+      pb.pts[i][a] = P3[a];
+      target[a] = P3[a];
+    }
+  }
+  for (int a = 0; a < 3; ++a) pb.pts[0][a] = tx[a];
+  return true;
+}
+
+__global__ void k_correct(CorrectArgs A) {
+  unsigned long long corrected = 0;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= A.grp.mask;
+       s += gridDim.x * blockDim.x) {
+    const unsigned long long key = A.grp.keys[s];
+    if (key == kEmptyKey) continue;
+    const uint32_t gi = uint32_t(key >> 32), cls = uint32_t(key);
+    const TxParams& P = A.txp[A.rx_req[gi]];
+    PathBuf pb;
+    bool ok = class_path(A.cls_info, cls, pb) &&
+              correct_path(A.sc, A.rank_to_id, P, A.rx + 3 * size_t(gi), pb, &A.ctr->overflow);
+    A.grp_ok[s] = ok ? 1 : 0;
+    if (!ok) continue;
+    corrected += A.grp_count[s];
+    const uint32_t cop = cls == kRootClass ? kRootClass : A.cls_info[cls].cop;
+    const unsigned long long dk = (unsigned long long)gi << 32 | cop;
+    const uint32_t ds = ht_insert(A.dedup, dk, &A.ctr->overflow, kOvDedup);
+    if (ds != 0xFFFFFFFFu) atomicMin(&A.dedup_rank[ds], A.grp_rank[s]);
+  }
+  if (corrected) atomicAdd(&A.ctr->corrected, corrected);
+}
+
+struct Survivor {
+  uint32_t slot, rx;
+  unsigned long long rank;
+};
+
+__global__ void k_select(HashTable grp, const unsigned long long* grp_rank,
+                         const unsigned char* grp_ok, const ClassInfo* cls_info, HashTable dedup,
+                         const unsigned long long* dedup_rank, Survivor* surv,
+                         unsigned long long cap, Counters* ctr) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= grp.mask;
+       s += gridDim.x * blockDim.x) {
+    const unsigned long long key = grp.keys[s];
+    if (key == kEmptyKey || !grp_ok[s]) continue;
+    const uint32_t gi = uint32_t(key >> 32), cls = uint32_t(key);
+    const uint32_t cop = cls == kRootClass ? kRootClass : cls_info[cls].cop;
+    const uint32_t ds = ht_find(dedup, (unsigned long long)gi << 32 | cop);
+    if (ds == 0xFFFFFFFFu || dedup_rank[ds] != grp_rank[s]) continue;
+    const unsigned long long i = atomicAdd(&ctr->survivors, 1ull);
+    if (i < cap) surv[i] = Survivor{s, gi, grp_rank[s]};
+    else atomicOr(&ctr->overflow, kOvSurv);
+  }
+}
+
+// ---- field ---------------------------------------------------------------
+
+struct FieldArgs {
+  DevScene sc;
+  const TxParams* txp;
+  const double* rx;
+  const int* rx_req;
+  HashTable grp;
+  const ClassInfo* cls_info;
+  const int* rank_to_id;
+  const Survivor* surv;
+  Counters* ctr;
+  unsigned long long cap;
+  FieldConsts K;
+  int precision;
+  double* path_field;   // 6 per survivor
+  int* path_nray;
+  int* path_tri;        // (kMaxDepth + 1) per survivor: triangle id
+  int* path_cop;
+  int* path_kind;
+  double* path_pts;     // (kMaxDepth + 2) * 3 per survivor
+};
+
+__global__ void k_field(FieldArgs A) {
+  const unsigned long long ns = min(A.ctr->survivors, A.cap);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const Survivor sv = A.surv[i];
+    const uint32_t cls = uint32_t(A.grp.keys[sv.slot]);
+    const TxParams& P = A.txp[A.rx_req[sv.rx]];
+    PathBuf pb;
+    class_path(A.cls_info, cls, pb);
+    correct_path(A.sc, A.rank_to_id, P, A.rx + 3 * size_t(sv.rx), pb, &A.ctr->overflow);
+    const double* frames[kMaxDepth + 1];
+    int mat[kMaxDepth + 1];
+    mat[0] = 0;
+    for (int r = 0; r < pb.n; ++r) {
+      frames[r] = pb.tri[r] >= 0 ? A.sc.corr[A.rank_to_id[pb.tri[r]]].cs : nullptr;
+      if (r + 1 < pb.n) mat[r + 1] = A.sc.tri64[pb.tri[r]].mat;
+    }
+    Cx<double> e[3];
+    if (A.precision == 1)
+      path_field<float>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
+                        P.antenna, P.fresnel != 0, A.K, e);
+    else
+      path_field<double>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
+                         P.antenna, P.fresnel != 0, A.K, e);
+    for (int j = 0; j < 3; ++j) {
+      A.path_field[6 * i + 2 * j] = e[j].re;
+      A.path_field[6 * i + 2 * j + 1] = e[j].im;
+    }
+    A.path_nray[i] = pb.n;
+    const size_t b = size_t(i) * (kMaxDepth + 1);
+    for (int r = 0; r < pb.n; ++r) {
+      const int t = pb.tri[r];
+      A.path_tri[b + r] = t >= 0 ? A.rank_to_id[t] : -1;
+      A.path_cop[b + r] = t >= 0 ? A.sc.tri64[t].cop : -1;
+      A.path_kind[b + r] = pb.kind[r];
+    }
+    const size_t bp = size_t(i) * (kMaxDepth + 2) * 3;
+    for (int r = 0; r <= pb.n; ++r)
+      for (int a = 0; a < 3; ++a) A.path_pts[bp + 3 * r + a] = pb.pts[r][a];
+  }
+}
+
+// ---- per-receiver ordered sum -------------------------------------------
+
+__global__ void k_surv_hist(const Survivor* surv, const Counters* ctr, unsigned long long cap,
+                            int* counts) {
+  const unsigned long long ns = min(ctr->survivors, cap);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    atomicAdd(&counts[surv[i].rx], 1);
+}
+
+__global__ void k_surv_scatter(const Survivor* surv, const Counters* ctr, unsigned long long cap,
+                               const int* starts, int* cursor, int* order) {
+  const unsigned long long ns = min(ctr->survivors, cap);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint32_t r = surv[i].rx;
+    order[starts[r] + atomicAdd(&cursor[r], 1)] = int(i);
+  }
+}
+
+// Sort each receiver's survivors by (launch, BFS) rank and sum their fields in
+// that order: FP64, or compensated FP32 (Neumaier) in FP32 mode.
+__global__ void k_rx_sum(const Survivor* surv, const int* starts, int* order, int n_rx,
+                         const double* path_field, int precision, double* field) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rx; r += gridDim.x * blockDim.x) {
+    const int b = starts[r], e = starts[r + 1];
+    for (int i = b + 1; i < e; ++i) {
+      const int v = order[i];
+      const unsigned long long key = surv[v].rank;
+      int j = i - 1;
+      while (j >= b && surv[order[j]].rank > key) {
+        order[j + 1] = order[j];
+        --j;
+      }
+      order[j + 1] = v;
+    }
+    if (precision == 1) {
+      float s[6] = {0, 0, 0, 0, 0, 0}, c[6] = {0, 0, 0, 0, 0, 0};
+      for (int i = b; i < e; ++i)
+        for (int k = 0; k < 6; ++k) {
+          const float x = float(path_field[6 * size_t(order[i]) + k]);
+          const float t = s[k] + x;
+          c[k] += fabsf(s[k]) >= fabsf(x) ? (s[k] - t) + x : (x - t) + s[k];
+          s[k] = t;
+        }
+      for (int k = 0; k < 6; ++k) field[6 * size_t(r) + k] = double(s[k]) + double(c[k]);
+    } else {
+      double s[6] = {0, 0, 0, 0, 0, 0};
+      for (int i = b; i < e; ++i)
+        for (int k = 0; k < 6; ++k) s[k] = __dadd_rn(s[k], path_field[6 * size_t(order[i]) + k]);
+      for (int k = 0; k < 6; ++k) field[6 * size_t(r) + k] = s[k];
+    }
+  }
+}
+
+// ============================================================ host side
+
+struct SceneImpl {
+  HostScene host;
+  std::vector<sbr_material> materials;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DBuf<Node32> node32;
+  DBuf<RefNode> ref;
+  DBuf<Tri32> tri32;
+  DBuf<Tri64> tri64;
+  DBuf<CorrTri> corr;
+  DBuf<Material> mats;
+  DBuf<int> tri_cop;     // by rank
+  DBuf<int> rank_to_id;
+  DevScene dev{};
+  long long dev_bytes = 0;
+  int n_cop = 0;
+  // launch directions per icosahedron level (0..12), resident once built
+  std::vector<std::unique_ptr<DBuf<double>>> dirs;
+  DBuf<const double*> dir_table;
+  std::mutex mu;
+  // workspace
+  DBuf<TxParams> txp;
+  DBuf<double> rx;
+  DBuf<int> rx_req;
+  DBuf<GridBuild> gb;
+  DBuf<RxGrid> grids;
+  DBuf<int> cell_base, cell_counts, cell_starts, cell_cursor;
+  DBuf<float4> rx32;
+  DBuf<RayRec> q0, q1;
+  DBuf<NodeRec> nodes;
+  DBuf<unsigned long long> cls_keys, cop_keys, grp_keys, grp_rank, dd_keys, dd_rank;
+  DBuf<ClassInfo> cls_info;
+  DBuf<unsigned> grp_count;
+  DBuf<unsigned char> grp_ok;
+  DBuf<Survivor> surv;
+  DBuf<int> s_counts, s_starts, s_cursor, s_order;
+  DBuf<double> path_field, path_pts, field;
+  DBuf<int> path_nray, path_tri, path_cop, path_kind;
+  DBuf<Counters> ctr;
+  // capacities (grow on overflow)
+  unsigned long long cap_nodes = 1 << 20, cap_queue = 1 << 20, cap_surv = 1 << 16;
+  uint32_t cap_cls = 1 << 20, cap_cop = 1 << 18, cap_grp = 1 << 22, cap_dd = 1 << 20;
+  cudaEvent_t ev[8] = {};
+};
+
+}  // namespace sbr
+
+struct sbr_scene {
+  sbr::SceneImpl impl;
+};
+
+struct sbr_result {
+  std::vector<double> field;
+  std::vector<sbr_path> paths;
+  std::vector<int> tri, cop, kind;
+  std::vector<double> points;
+  sbr_counts counts{};
+  sbr_timing timing{};
+};
+
+namespace sbr {
+
+static void upload_scene(SceneImpl& S) {
+  const HostScene& H = S.host;
+  const int nt = int(H.tris.size()), nn = int(H.nodes.size());
+  std::vector<Node32> n32(nn);
+  std::vector<RefNode> ref(nn);
+  const double margin_m = std::ldexp(H.extent + 1.0, -14);
+  for (int i = 0; i < nn; ++i) {
+    const HostNode& h = H.nodes[i];
+    RefNode& r = ref[i];
+    std::memcpy(r.bb, h.bb, sizeof r.bb);
+    r.c0 = h.c0;
+    r.c1 = h.c1;
+    r.first = h.first;
+    r.count = h.count;
+    r.parent = h.parent;
+    r.pad = 0;
+    Node32& m = n32[i];
+    std::memset(&m, 0, sizeof m);
+    if (h.c0 >= 0) {
+      const int cs[2] = {h.c0, h.c1};
+      for (int k = 0; k < 2; ++k) {
+        const HostNode& c = H.nodes[cs[k]];
+        float* lo = k == 0 ? m.lo0 : m.lo1;
+        float* hi = k == 0 ? m.hi0 : m.hi1;
+        for (int a = 0; a < 3; ++a) {
+          // outward rounding keeps the FP32 box around the FP64 one
+          lo[a] = std::nextafter(float(c.bb[a]), -INFINITY);
+          hi[a] = std::nextafter(float(c.bb[3 + a]), INFINITY);
+        }
+        m.child[k] = c.c0 >= 0 ? cs[k] : ~cs[k];
+      }
+    }
+  }
+  std::vector<Tri32> t32(nt);
+  std::vector<Tri64> t64(nt);
+  std::vector<int> cop(nt), r2i(nt);
+  for (int r = 0; r < nt; ++r) {
+    const HostTri& t = H.tris[H.dfs_tris[r]];
+    Tri64& d = t64[r];
+    Tri32& f = t32[r];
+    for (int a = 0; a < 3; ++a) {
+      d.v1[a] = t.v1[a];
+      d.e1[a] = t.v2[a] - t.v1[a];
+      d.e2[a] = t.v3[a] - t.v1[a];
+      d.n[a] = t.n[a];
+      f.v1[a] = float(d.v1[a]);
+      f.e1[a] = float(d.e1[a]);
+      f.e2[a] = float(d.e2[a]);
+    }
+    f.nv1 = float(std::sqrt(d.v1[0] * d.v1[0] + d.v1[1] * d.v1[1] + d.v1[2] * d.v1[2])) * 1.0001f;
+    f.ne1 = float(std::sqrt(d.e1[0] * d.e1[0] + d.e1[1] * d.e1[1] + d.e1[2] * d.e1[2])) * 1.0001f;
+    f.ne2 = float(std::sqrt(d.e2[0] * d.e2[0] + d.e2[1] * d.e2[1] + d.e2[2] * d.e2[2])) * 1.0001f;
+    d.id = t.id;
+    d.cop = t.cop;
+    d.mat = t.mat;
+    d.node = -1;
+    cop[r] = t.cop;
+    r2i[r] = t.id;
+  }
+  for (int i = 0; i < nn; ++i)
+    if (H.nodes[i].c0 < 0)
+      for (int r = H.nodes[i].first; r < H.nodes[i].first + H.nodes[i].count; ++r) t64[r].node = i;
+  S.n_cop = 0;
+  for (auto& t : H.tris) S.n_cop = std::max(S.n_cop, t.cop + 1);
+  std::vector<Material> mats(S.materials.size());
+  for (size_t i = 0; i < mats.size(); ++i)
+    mats[i] = Material{S.materials[i].rel_permittivity_re, S.materials[i].rel_conductivity};
+  cudaStream_t st = S.stream;
+  S.node32.upload(n32.data(), n32.size(), st);
+  S.ref.upload(ref.data(), ref.size(), st);
+  S.tri32.upload(t32.data(), t32.size(), st);
+  S.tri64.upload(t64.data(), t64.size(), st);
+  S.mats.upload(mats.data(), mats.size(), st);
+  S.tri_cop.upload(cop.data(), cop.size(), st);
+  S.rank_to_id.upload(r2i.data(), r2i.size(), st);
+  S.dev.node32 = S.node32.p;
+  S.dev.ref = S.ref.p;
+  S.dev.tri32 = S.tri32.p;
+  S.dev.tri64 = S.tri64.p;
+  S.dev.mats = S.mats.p;
+  S.dev.n_tri = nt;
+  S.dev.n_nodes = nn;
+  S.dev.n_mats = int(mats.size());
+  S.dev.root_leaf = H.nodes[0].c0 < 0 ? 1 : 0;
+  S.dev.box_margin = float(margin_m);
+  S.dev_bytes = (long long)(n32.size() * sizeof(Node32) + ref.size() * sizeof(RefNode) +
+                            t32.size() * sizeof(Tri32) + t64.size() * sizeof(Tri64) +
+                            2 * nt * sizeof(int) + nt * sizeof(CorrTri));
+  CK(cudaStreamSynchronize(st));
+}
+
+// corr[id] = the triangle at mesh position id (what triangleMesh[id] returns).
+static void upload_mesh_order(SceneImpl& S, const std::vector<int>& order) {
+  const HostScene& H = S.host;
+  const int nt = int(H.tris.size());
+  std::vector<CorrTri> c(nt);
+  for (int i = 0; i < nt; ++i) {
+    const HostTri& t = H.tris[order[i]];
+    CorrTri& d = c[i];
+    for (int a = 0; a < 3; ++a) {
+      d.v1[a] = t.v1[a];
+      d.e1[a] = t.v2[a] - t.v1[a];
+      d.e2[a] = t.v3[a] - t.v1[a];
+      d.n[a] = t.n[a];
+    }
+    std::memcpy(d.cs, t.cs, sizeof d.cs);
+    d.mat = t.mat;
+    d.pad = 0;
+  }
+  S.corr.upload(c.data(), c.size(), S.stream);
+  S.dev.corr = S.corr.p;
+  CK(cudaStreamSynchronize(S.stream));
+}
+
+static void ensure_dirs(SceneImpl& S, int level) {
+  if (S.dirs.size() < 13) S.dirs.resize(13);
+  if (level < 0 || level > 12) throw std::string("tessellation level must be 0..12");
+  if (!S.dirs[level]) {
+    std::vector<double> d;
+    icosphere(level, d);
+    auto b = std::make_unique<DBuf<double>>();
+    b->upload(d.data(), d.size(), S.stream);
+    S.dirs[level] = std::move(b);
+  }
+  std::vector<const double*> tab(13, nullptr);
+  for (int l = 0; l < 13; ++l)
+    if (S.dirs[l]) tab[l] = S.dirs[l]->p;
+  S.dir_table.upload(tab.data(), tab.size(), S.stream);
+}
+
+static long long n_launch_of(int level) { return 10LL * (1LL << (2 * level)) + 2; }
+
+static int grid_for(long long n, int block) {
+  int dev_sms = 152;
+  long long g = (n + block - 1) / block;
+  return int(std::max<long long>(1, std::min<long long>(g, (long long)dev_sms * 32)));
+}
+
+static FieldConsts field_consts() {
+  // Constants.h:6-23 evaluated the way the reference evaluates them (EIGEN_PI
+  // is a long double literal).
+  const long double piL = 3.141592653589793238462643383279502884197169399375105820974944592307816406L;
+  const double c = 2.99792458e8;
+  const double u0 = 4 * piL * 1e-7;
+  FieldConsts K;
+  K.e0 = 1.0 / (u0 * c * c);
+  K.eta0 = u0 * c;
+  K.pi_hi = double(piL);
+  K.pi_lo = double(piL - (long double)K.pi_hi);
+  return K;
+}
+
+static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_result& out) {
+  std::lock_guard<std::mutex> lock(S.mu);
+  cudaStream_t st = S.stream;
+  CK(cudaSetDevice(S.device));
+  if (!S.ev[0])
+    for (auto& e : S.ev) CK(cudaEventCreate(&e));
+  // ---- request table
+  std::vector<TxParams> tp(n_req);
+  long long launches = 0;
+  int rx_total = 0, max_depth = 0;
+  for (int r = 0; r < n_req; ++r) {
+    const sbr_request& q = reqs[r];
+    if (q.n_rx < 0 || (q.n_rx > 0 && !q.rx)) throw std::string("receivers missing");
+    if (q.max_reflection < 0 || q.max_transmission < 0 ||
+        q.max_reflection + q.max_transmission > kMaxDepth)
+      throw std::string("max_reflection + max_transmission must be 0..16");
+    if (q.tessellation < 0 || q.tessellation > 12) throw std::string("tessellation must be 0..12");
+    if (!(q.frequency > 0)) throw std::string("frequency must be > 0");
+    if (q.antenna < 0 || q.antenna > 2) throw std::string("antenna must be 0, 1 or 2");
+    ensure_dirs(S, q.tessellation);
+    TxParams& P = tp[r];
+    std::memset(&P, 0, sizeof P);
+    for (int a = 0; a < 3; ++a) P.tx[a] = q.tx[a];
+    for (int a = 0; a < 9; ++a) P.txcs[a] = q.tx_coord_sys[a];
+    P.freq = q.frequency;
+    P.pt = q.pt;
+    const int tess = q.tessellation + 1;  // RTSolver.cpp:70
+    const double beta = 1.0 / (3.0 * tess) * std::acos(-1.0 / std::sqrt(5.0));  // RTSolver.cpp:839
+    P.tan_beta = std::tan(beta);
+    P.R = q.max_reflection;
+    P.T = q.max_transmission;
+    P.antenna = q.antenna;
+    P.fresnel = q.use_fresnel ? 1 : 0;
+    P.level = q.tessellation;
+    P.n_launch = int(n_launch_of(q.tessellation));
+    P.rx_first = rx_total;
+    P.n_rx = q.n_rx;
+    P.launch_first = launches;
+    P.grid = r;
+    launches += P.n_launch;
+    rx_total += q.n_rx;
+    max_depth = std::max(max_depth, q.max_reflection + q.max_transmission);
+  }
+  const int precision = reqs[0].field_precision == SBR_FIELD_FP32 ? 1 : 0;
+  auto t0 = std::chrono::steady_clock::now();
+  CK(cudaEventRecord(S.ev[0], st));
+  S.txp.upload(tp.data(), tp.size(), st);
+  // receivers
+  S.rx.ensure(std::max(1, 3 * rx_total));
+  {
+    std::vector<int> req_of(std::max(1, rx_total));
+    for (int r = 0; r < n_req; ++r) {
+      const sbr_request& q = reqs[r];
+      if (q.n_rx)
+        CK(cudaMemcpyAsync(S.rx.p + 3 * size_t(tp[r].rx_first), q.rx, 3 * sizeof(double) * q.n_rx,
+                           q.rx_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+      for (int i = 0; i < q.n_rx; ++i) req_of[tp[r].rx_first + i] = r;
+    }
+    S.rx_req.upload(req_of.data(), req_of.size(), st);
+  }
+  CK(cudaEventRecord(S.ev[1], st));
+  // ---- receiver grid
+  const int max_cells = 1 << 20;
+  S.gb.ensure(n_req);
+  {
+    std::vector<GridBuild> g0(n_req);
+    for (auto& g : g0) {
+      for (int a = 0; a < 3; ++a) {
+        g.bmin[a] = INT_MAX;
+        g.bmax[a] = INT_MIN;
+      }
+      g.cmax_o = INT_MIN;
+      g.cmax = 0;
+      g.ncell = 0;
+    }
+    CK(cudaMemcpyAsync(S.gb.p, g0.data(), sizeof(GridBuild) * n_req, cudaMemcpyHostToDevice, st));
+  }
+  S.grids.ensure(n_req);
+  S.cell_base.ensure(n_req + 1);
+  const size_t cell_cap = size_t(n_req) * (max_cells + 1) + 1;
+  S.cell_counts.ensure(cell_cap);
+  S.cell_starts.ensure(cell_cap + 1);
+  S.cell_cursor.ensure(cell_cap);
+  S.rx32.ensure(std::max(1, rx_total));
+  CK(cudaMemsetAsync(S.cell_counts.p, 0, sizeof(int) * cell_cap, st));
+  CK(cudaMemsetAsync(S.cell_cursor.p, 0, sizeof(int) * cell_cap, st));
+  int max_rx = 1;
+  for (auto& p : tp) max_rx = std::max(max_rx, p.n_rx);
+  dim3 rg(std::min(1024, (max_rx + 255) / 256), n_req);
+  k_rx_bounds<<<rg, 256, 0, st>>>(S.rx.p, S.txp.p, n_req, S.gb.p);
+  k_grid_shape<<<1, 1, 0, st>>>(S.gb.p, S.grids.p, S.txp.p, n_req, max_cells, S.cell_base.p);
+  k_rx_count<<<rg, 256, 0, st>>>(S.rx.p, S.txp.p, n_req, S.grids.p, S.cell_base.p, S.cell_counts.p);
+  k_scan_exclusive<<<1, 1024, 0, st>>>(S.cell_counts.p, S.cell_starts.p, int(cell_cap));
+  k_rx_scatter<<<rg, 256, 0, st>>>(S.rx.p, S.txp.p, n_req, S.grids.p, S.cell_base.p,
+                                   S.cell_starts.p, S.cell_cursor.p, S.rx32.p);
+  k_grid_finish<<<(n_req + 127) / 128, 128, 0, st>>>(S.grids.p, S.cell_starts.p, S.cell_base.p,
+                                                    S.rx32.p, n_req);
+  CK(cudaGetLastError());
+
+  const FieldConsts K = field_consts();
+  for (int attempt = 0;; ++attempt) {
+    if (attempt > 6) throw std::string("capacity: tables kept overflowing");
+    S.ctr.ensure(1);
+    S.nodes.ensure(S.cap_nodes);
+    S.q0.ensure(S.cap_queue);
+    S.q1.ensure(S.cap_queue);
+    S.cls_keys.ensure(S.cap_cls);
+    S.cls_info.ensure(S.cap_cls);
+    S.cop_keys.ensure(S.cap_cop);
+    S.grp_keys.ensure(S.cap_grp);
+    S.grp_rank.ensure(S.cap_grp);
+    S.grp_count.ensure(S.cap_grp);
+    S.grp_ok.ensure(S.cap_grp);
+    S.dd_keys.ensure(S.cap_dd);
+    S.dd_rank.ensure(S.cap_dd);
+    S.surv.ensure(S.cap_surv);
+    CK(cudaMemsetAsync(S.ctr.p, 0, sizeof(Counters), st));
+    const int fb = 256;
+    k_fill_u64<<<grid_for(S.cap_cls, fb), fb, 0, st>>>(S.cls_keys.p, S.cap_cls, kEmptyKey);
+    k_fill_u64<<<grid_for(S.cap_cop, fb), fb, 0, st>>>(S.cop_keys.p, S.cap_cop, kEmptyKey);
+    k_fill_u64<<<grid_for(S.cap_grp, fb), fb, 0, st>>>(S.grp_keys.p, S.cap_grp, kEmptyKey);
+    k_fill_u64<<<grid_for(S.cap_grp, fb), fb, 0, st>>>(S.grp_rank.p, S.cap_grp, kEmptyKey);
+    k_fill_u64<<<grid_for(S.cap_dd, fb), fb, 0, st>>>(S.dd_keys.p, S.cap_dd, kEmptyKey);
+    k_fill_u64<<<grid_for(S.cap_dd, fb), fb, 0, st>>>(S.dd_rank.p, S.cap_dd, kEmptyKey);
+    CK(cudaMemsetAsync(S.grp_count.p, 0, sizeof(unsigned) * S.cap_grp, st));
+    CK(cudaEventRecord(S.ev[2], st));
+    // ---- trace
+    TraceArgs ta;
+    ta.sc = S.dev;
+    ta.txp = S.txp.p;
+    ta.n_tx = n_req;
+    ta.dirs = S.dir_table.p;
+    ta.nodes = S.nodes.p;
+    ta.node_cap = S.cap_nodes;
+    ta.out_cap = S.cap_queue;
+    ta.cls_tab = HashTable{S.cls_keys.p, S.cap_cls - 1};
+    ta.cop_tab = HashTable{S.cop_keys.p, S.cap_cop - 1};
+    ta.cls_info = S.cls_info.p;
+    ta.tri_cop = S.tri_cop.p;
+    ta.ctr = S.ctr.p;
+    ta.n_root = launches;
+    for (int d = 0; d <= max_depth; ++d) {
+      ta.depth = d;
+      ta.in = (d % 2 == 0) ? S.q1.p : S.q0.p;
+      ta.out = (d % 2 == 0) ? S.q0.p : S.q1.p;
+      const long long width = d == 0 ? launches : (long long)std::min<unsigned long long>(S.cap_queue, 1ull << 40);
+      k_trace<<<grid_for(width, 128), 128, 0, st>>>(ta);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(S.ev[3], st));
+    // ---- capture
+    CaptureArgs ca;
+    ca.nodes = S.nodes.p;
+    ca.txp = S.txp.p;
+    ca.grids = S.grids.p;
+    ca.gb = S.gb.p;
+    ca.rx = S.rx.p;
+    ca.grp = HashTable{S.grp_keys.p, S.cap_grp - 1};
+    ca.grp_rank = S.grp_rank.p;
+    ca.grp_count = S.grp_count.p;
+    ca.ctr = S.ctr.p;
+    ca.node_cap = S.cap_nodes;
+    k_capture<<<152 * 16, 128, 0, st>>>(ca);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(S.ev[4], st));
+    // ---- correct, dedup, select
+    CorrectArgs co;
+    co.sc = S.dev;
+    co.txp = S.txp.p;
+    co.n_tx = n_req;
+    co.rx = S.rx.p;
+    co.rx_req = S.rx_req.p;
+    co.grp = ca.grp;
+    co.grp_rank = S.grp_rank.p;
+    co.grp_count = S.grp_count.p;
+    co.grp_ok = S.grp_ok.p;
+    co.cls_info = S.cls_info.p;
+    co.dedup = HashTable{S.dd_keys.p, S.cap_dd - 1};
+    co.dedup_rank = S.dd_rank.p;
+    co.rank_to_id = S.rank_to_id.p;
+    co.ctr = S.ctr.p;
+    k_correct<<<grid_for(S.cap_grp, 128), 128, 0, st>>>(co);
+    k_select<<<grid_for(S.cap_grp, 256), 256, 0, st>>>(co.grp, S.grp_rank.p, S.grp_ok.p,
+                                                       S.cls_info.p, co.dedup, S.dd_rank.p,
+                                                       S.surv.p, S.cap_surv, S.ctr.p);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(S.ev[5], st));
+    Counters c;
+    CK(cudaMemcpyAsync(&c, S.ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (c.overflow & kOvStack) throw std::string("BVH deeper than the traversal stack");
+    if (c.overflow) {
+      if (c.overflow & kOvNodes) S.cap_nodes = std::max(S.cap_nodes * 2, c.nodes + c.nodes / 8);
+      if (c.overflow & kOvQueue) {
+        unsigned long long mx = 0;
+        for (auto v : c.queue) mx = std::max(mx, v);
+        S.cap_queue = std::max(S.cap_queue * 2, mx + mx / 8);
+      }
+      if (c.overflow & kOvClass) S.cap_cls *= 4;
+      if (c.overflow & kOvCop) S.cap_cop *= 4;
+      if (c.overflow & kOvGroup) S.cap_grp *= 4;
+      if (c.overflow & kOvDedup) S.cap_dd *= 4;
+      if (c.overflow & kOvSurv) S.cap_surv = next_pow2(c.survivors + c.survivors / 4);
+      continue;
+    }
+    // ---- field + ordered per-receiver sum
+    const unsigned long long ns = c.survivors;
+    const size_t nsa = std::max<size_t>(1, ns);
+    S.path_field.ensure(6 * nsa);
+    S.path_nray.ensure(nsa);
+    S.path_tri.ensure(nsa * (kMaxDepth + 1));
+    S.path_cop.ensure(nsa * (kMaxDepth + 1));
+    S.path_kind.ensure(nsa * (kMaxDepth + 1));
+    S.path_pts.ensure(nsa * (kMaxDepth + 2) * 3);
+    S.field.ensure(std::max(1, 6 * rx_total));
+    S.s_counts.ensure(rx_total + 1);
+    S.s_starts.ensure(rx_total + 2);
+    S.s_cursor.ensure(rx_total + 1);
+    S.s_order.ensure(nsa);
+    FieldArgs fa;
+    fa.sc = S.dev;
+    fa.txp = S.txp.p;
+    fa.rx = S.rx.p;
+    fa.rx_req = S.rx_req.p;
+    fa.grp = co.grp;
+    fa.cls_info = S.cls_info.p;
+    fa.rank_to_id = S.rank_to_id.p;
+    fa.surv = S.surv.p;
+    fa.ctr = S.ctr.p;
+    fa.cap = S.cap_surv;
+    fa.K = K;
+    fa.precision = precision;
+    fa.path_field = S.path_field.p;
+    fa.path_nray = S.path_nray.p;
+    fa.path_tri = S.path_tri.p;
+    fa.path_cop = S.path_cop.p;
+    fa.path_kind = S.path_kind.p;
+    fa.path_pts = S.path_pts.p;
+    if (ns) k_field<<<grid_for(ns, 64), 64, 0, st>>>(fa);
+    CK(cudaMemsetAsync(S.s_counts.p, 0, sizeof(int) * (rx_total + 1), st));
+    CK(cudaMemsetAsync(S.s_cursor.p, 0, sizeof(int) * (rx_total + 1), st));
+    if (ns) k_surv_hist<<<grid_for(ns, 256), 256, 0, st>>>(S.surv.p, S.ctr.p, S.cap_surv, S.s_counts.p);
+    k_scan_exclusive<<<1, 1024, 0, st>>>(S.s_counts.p, S.s_starts.p, rx_total);
+    if (ns)
+      k_surv_scatter<<<grid_for(ns, 256), 256, 0, st>>>(S.surv.p, S.ctr.p, S.cap_surv,
+                                                        S.s_starts.p, S.s_cursor.p, S.s_order.p);
+    if (rx_total)
+      k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(S.surv.p, S.s_starts.p, S.s_order.p,
+                                                        rx_total, S.path_field.p, precision,
+                                                        S.field.p);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(S.ev[6], st));
+    // ---- results to the host
+    out.field.resize(6 * size_t(rx_total));
+    if (rx_total)
+      CK(cudaMemcpyAsync(out.field.data(), S.field.p, sizeof(double) * 6 * rx_total,
+                         cudaMemcpyDeviceToHost, st));
+    std::vector<int> order(ns), nray(ns), starts(rx_total + 1);
+    std::vector<Survivor> sv(ns);
+    std::vector<double> pf(6 * ns), pts(ns * (kMaxDepth + 2) * 3);
+    std::vector<int> ptri(ns * (kMaxDepth + 1)), pcop(ns * (kMaxDepth + 1)),
+        pkind(ns * (kMaxDepth + 1));
+    if (ns) {
+      CK(cudaMemcpyAsync(order.data(), S.s_order.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(nray.data(), S.path_nray.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(sv.data(), S.surv.p, sizeof(Survivor) * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pf.data(), S.path_field.p, sizeof(double) * 6 * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(ptri.data(), S.path_tri.p, sizeof(int) * ptri.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pcop.data(), S.path_cop.p, sizeof(int) * pcop.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pkind.data(), S.path_kind.p, sizeof(int) * pkind.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pts.data(), S.path_pts.p, sizeof(double) * pts.size(), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaEventRecord(S.ev[7], st));
+    CK(cudaStreamSynchronize(st));
+    // assemble paths in receiver order, then (launch, BFS) order
+    std::vector<int> req_of(rx_total);
+    for (int r = 0; r < n_req; ++r)
+      for (int i = 0; i < tp[r].n_rx; ++i) req_of[tp[r].rx_first + i] = r;
+    out.paths.clear();
+    out.tri.clear();
+    out.cop.clear();
+    out.kind.clear();
+    out.points.clear();
+    for (size_t k = 0; k < ns; ++k) {
+      const int i = order[k];
+      sbr_path p;
+      p.receiver = int(sv[i].rx) - tp[req_of[sv[i].rx]].rx_first;
+      p.request = req_of[sv[i].rx];
+      p.n_rays = nray[i];
+      p.launch = (long long)(sv[i].rank >> kHeapBits);
+      p.heap = int(sv[i].rank & ((1u << kHeapBits) - 1));
+      p.ray_offset = (long long)out.tri.size();
+      for (int j = 0; j < 6; ++j) p.field[j] = pf[6 * size_t(i) + j];
+      for (int r = 0; r < p.n_rays; ++r) {
+        const size_t b = size_t(i) * (kMaxDepth + 1) + r;
+        out.tri.push_back(ptri[b]);
+        out.cop.push_back(pcop[b]);
+        out.kind.push_back(pkind[b]);
+        const size_t q = size_t(i) * (kMaxDepth + 2) * 3 + 3 * r;
+        for (int a = 0; a < 6; ++a) out.points.push_back(pts[q + a]);
+      }
+      out.paths.push_back(p);
+    }
+    // paths are ordered by survivor order within a receiver; receivers ascend
+    // because s_order is grouped by receiver index.
+    out.counts.segments = (long long)c.nodes;
+    out.counts.captured = (long long)c.events;
+    out.counts.corrected = (long long)c.corrected;
+    out.counts.paths = (long long)ns;
+    out.counts.rays = (long long)out.tri.size();
+    out.counts.fp64_triangle_tests = (long long)c.fp64_tri;
+    out.counts.fallback_rays = (long long)c.fallback;
+    out.counts.fp64_capture_tests = (long long)c.fp64_capture;
+    out.counts.launches = launches;
+    float ms[8] = {};
+    for (int i = 1; i < 8; ++i) CK(cudaEventElapsedTime(&ms[i], S.ev[i - 1], S.ev[i]));
+    out.timing.h2d_ms = ms[1];
+    out.timing.trace_ms = ms[3];
+    out.timing.capture_ms = ms[4];
+    out.timing.correct_ms = ms[5];
+    out.timing.field_ms = ms[6];
+    out.timing.d2h_ms = ms[7];
+    float all = 0, dev = 0;
+    CK(cudaEventElapsedTime(&all, S.ev[0], S.ev[7]));
+    CK(cudaEventElapsedTime(&dev, S.ev[1], S.ev[6]));
+    out.timing.total_ms = all;
+    out.timing.device_ms = dev;
+    (void)t0;
+    return;
+  }
+}
+
+}  // namespace sbr
+
+// ============================================================ C ABI
+
+using namespace sbr;
+
+#define ABI_GUARD(...)                                                     \
+  try {                                                                     \
+    __VA_ARGS__                                                             \
+  } catch (const CudaError& e) {                                            \
+    set_err(std::string("CUDA error in ") + e.where + ": " + cudaGetErrorString(e.e)); \
+    return e.e == cudaErrorMemoryAllocation ? SBR_ERR_OOM : SBR_ERR_CUDA;   \
+  } catch (const std::bad_alloc&) {                                         \
+    set_err("host allocation failed");                                      \
+    return SBR_ERR_OOM;                                                     \
+  } catch (const std::string& s) {                                          \
+    set_err(s);                                                             \
+    return s.rfind("capacity", 0) == 0 ? SBR_ERR_CAPACITY : SBR_ERR_INVALID_ARG; \
+  }
+
+extern "C" {
+
+const char* sbr_last_error(void) { return g_err.c_str(); }
+const char* sbr_version(void) { return "sbr-gb300 0.1 (sm_103a)"; }
+
+static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, const int* mat_ids,
+                               const sbr_material* materials, int n_materials, sbr_scene** out) {
+  ABI_GUARD({
+    if (!out) throw std::string("out is NULL");
+    *out = nullptr;
+    if (n_materials <= 0 || !materials) throw std::string("at least one material is required");
+    const int nt = int(n.size() / 3);
+    if (mat_ids)
+      for (int i = 0; i < nt; ++i)
+        if (mat_ids[i] < 0 || mat_ids[i] >= n_materials)
+          throw std::string("material id out of range at triangle ") + std::to_string(i);
+    auto sc = std::make_unique<sbr_scene>();
+    SceneImpl& S = sc->impl;
+    std::string err;
+    if (!prepare_scene(nt, v.data(), n.data(), mat_ids, S.host, err)) throw err;
+    if (S.host.max_depth + 4 > kStack)
+      throw std::string("BVH depth ") + std::to_string(S.host.max_depth) +
+          " exceeds the traversal stack (" + std::to_string(kStack) + ")";
+    S.materials.assign(materials, materials + n_materials);
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+      cudaGetLastError();
+      throw CudaError{cudaErrorNoDevice, "no CUDA device"};
+    }
+    CK(cudaGetDevice(&S.device));
+    CK(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+    upload_scene(S);
+    upload_mesh_order(S, S.host.mesh_order);
+    *out = sc.release();
+    return SBR_OK;
+  })
+}
+
+sbr_status sbr_scene_create(int n_triangles, const float* vertices, const float* normals,
+                            const int* material_ids, const sbr_material* materials,
+                            int n_materials, sbr_scene** out) {
+  if (n_triangles <= 0 || !vertices || !normals) {
+    set_err("sbr_scene_create: empty triangle list");
+    return SBR_ERR_INVALID_ARG;
+  }
+  std::vector<float> v(vertices, vertices + 9 * size_t(n_triangles));
+  std::vector<float> n(normals, normals + 3 * size_t(n_triangles));
+  return scene_common(v, n, material_ids, materials, n_materials, out);
+}
+
+sbr_status sbr_scene_create_from_stl(const char* path, const int* material_ids,
+                                     const sbr_material* materials, int n_materials,
+                                     sbr_scene** out) {
+  std::vector<float> v, n;
+  std::string err;
+  if (!path || !read_stl(path, v, n, err)) {
+    set_err(path ? err : std::string("path is NULL"));
+    return SBR_ERR_IO;
+  }
+  return scene_common(v, n, material_ids, materials, n_materials, out);
+}
+
+sbr_status sbr_scene_info_get(const sbr_scene* scene, sbr_scene_info* out) {
+  if (!scene || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const SceneImpl& S = scene->impl;
+  out->n_triangles = int(S.host.tris.size());
+  out->n_bvh_nodes = int(S.host.nodes.size());
+  out->bvh_depth = S.host.max_depth;
+  out->n_coplanar = S.n_cop;
+  out->extent = S.host.extent;
+  out->device_bytes = S.dev_bytes;
+  return SBR_OK;
+}
+
+sbr_status sbr_scene_mesh_order(const sbr_scene* scene, int* out) {
+  if (!scene || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  std::copy(scene->impl.host.mesh_order.begin(), scene->impl.host.mesh_order.end(), out);
+  return SBR_OK;
+}
+
+sbr_status sbr_scene_set_mesh_order(sbr_scene* scene, const int* order) {
+  if (!scene || !order) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const int nt = int(scene->impl.host.tris.size());
+  std::vector<int> o(order, order + nt), seen(nt, 0);
+  for (int v : o) {
+    if (v < 0 || v >= nt || seen[v]++) {
+      set_err("mesh order is not a permutation of the triangle ids");
+      return SBR_ERR_INVALID_ARG;
+    }
+  }
+  ABI_GUARD({
+    std::lock_guard<std::mutex> lock(scene->impl.mu);
+    scene->impl.host.mesh_order = o;
+    upload_mesh_order(scene->impl, o);
+    return SBR_OK;
+  })
+}
+
+sbr_status sbr_scene_coplanar_ids(const sbr_scene* scene, int* out) {
+  if (!scene || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  for (size_t i = 0; i < scene->impl.host.tris.size(); ++i) out[i] = scene->impl.host.tris[i].cop;
+  return SBR_OK;
+}
+
+sbr_status sbr_scene_destroy(sbr_scene* scene) {
+  if (!scene) return SBR_OK;
+  if (scene->impl.stream) cudaStreamSynchronize(scene->impl.stream);
+  for (auto& e : scene->impl.ev)
+    if (e) cudaEventDestroy(e);
+  cudaStream_t st = scene->impl.stream;
+  delete scene;
+  if (st) cudaStreamDestroy(st);
+  return SBR_OK;
+}
+
+sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_requests,
+                           sbr_result** out) {
+  if (!scene || !requests || n_requests <= 0 || !out) {
+    set_err("sbr_solve_batch: NULL argument or empty batch");
+    return SBR_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  ABI_GUARD({
+    auto res = std::make_unique<sbr_result>();
+    solve_impl(scene->impl, requests, n_requests, *res);
+    *out = res.release();
+    return SBR_OK;
+  })
+}
+
+sbr_status sbr_solve(sbr_scene* scene, const sbr_request* request, sbr_result** out) {
+  return sbr_solve_batch(scene, request, 1, out);
+}
+
+sbr_status sbr_result_counts(const sbr_result* r, sbr_counts* out) {
+  if (!r || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  *out = r->counts;
+  return SBR_OK;
+}
+
+sbr_status sbr_result_field(const sbr_result* r, double* out) {
+  if (!r || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  std::copy(r->field.begin(), r->field.end(), out);
+  return SBR_OK;
+}
+
+sbr_status sbr_result_paths(const sbr_result* r, sbr_path* paths, int* tri, int* cop, int* kind,
+                            double* points) {
+  if (!r) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  if (paths) std::copy(r->paths.begin(), r->paths.end(), paths);
+  if (tri) std::copy(r->tri.begin(), r->tri.end(), tri);
+  if (cop) std::copy(r->cop.begin(), r->cop.end(), cop);
+  if (kind) std::copy(r->kind.begin(), r->kind.end(), kind);
+  if (points) std::copy(r->points.begin(), r->points.end(), points);
+  return SBR_OK;
+}
+
+sbr_status sbr_result_timing(const sbr_result* r, sbr_timing* out) {
+  if (!r || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  *out = r->timing;
+  return SBR_OK;
+}
+
+sbr_status sbr_result_destroy(sbr_result* r) {
+  delete r;
+  return SBR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,263 @@
+// Received field of one corrected path (FieldCompute::FieldForPath,
+// FieldCompute.cpp:71-151, with GetAnalyticEfieldPattern :153-183,
+// ComputeRefcField/ComputeTransField :185-235, GetTECoeff/GetTMCoeff/
+// GetTransAngle :237-302 and the VecMatDef.h:51-155 helpers).
+//
+// Templated on the real type: double reproduces the reference's FP64
+// arithmetic; float computes the per-segment rotations and Fresnel
+// coefficients in FP32 while the path length and the phase k*L stay FP64
+// (k*L reaches ~1e6 rad at 28 GHz and 1 km, far beyond FP32 resolution).
+// Complex functions are written from their textbook definitions
+// (principal branches), not copied from any math library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace sbr {
+
+template <class R>
+struct Cx {
+  R re, im;
+};
+template <class R>
+__device__ __forceinline__ Cx<R> cx(R a, R b = R(0)) {
+  return Cx<R>{a, b};
+}
+template <class R>
+__device__ __forceinline__ Cx<R> operator+(Cx<R> a, Cx<R> b) {
+  return cx(a.re + b.re, a.im + b.im);
+}
+template <class R>
+__device__ __forceinline__ Cx<R> operator-(Cx<R> a, Cx<R> b) {
+  return cx(a.re - b.re, a.im - b.im);
+}
+template <class R>
+__device__ __forceinline__ Cx<R> operator-(Cx<R> a) {
+  return cx(-a.re, -a.im);
+}
+template <class R>
+__device__ __forceinline__ Cx<R> operator*(Cx<R> a, Cx<R> b) {
+  return cx(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+template <class R>
+__device__ __forceinline__ Cx<R> operator*(R s, Cx<R> a) {
+  return cx(s * a.re, s * a.im);
+}
+template <class R>
+__device__ __forceinline__ Cx<R> operator*(Cx<R> a, R s) {
+  return cx(a.re * s, a.im * s);
+}
+// Smith's division (Smith 1962).
+template <class R>
+__device__ __forceinline__ Cx<R> operator/(Cx<R> a, Cx<R> b) {
+  if (fabs(b.re) >= fabs(b.im)) {
+    R r = b.im / b.re, den = b.re + b.im * r;
+    return cx((a.re + a.im * r) / den, (a.im - a.re * r) / den);
+  }
+  R r = b.re / b.im, den = b.im + b.re * r;
+  return cx((a.re * r + a.im) / den, (a.im * r - a.re) / den);
+}
+template <class R>
+__device__ __forceinline__ Cx<R> operator/(R s, Cx<R> b) {
+  return cx(s) / b;
+}
+template <class R>
+__device__ __forceinline__ Cx<R> operator/(Cx<R> a, R s) {
+  return cx(a.re / s, a.im / s);
+}
+// Principal square root: with r = |z|, sqrt(z) = (sqrt((r+x)/2), y/(2t)) for
+// x >= 0, else (|y|/(2t), sign(y) t) with t = sqrt((r-x)/2).
+template <class R>
+__device__ __forceinline__ Cx<R> csqrt(Cx<R> z) {
+  if (z.re == R(0) && z.im == R(0)) return cx(R(0), z.im);
+  R r = hypot(z.re, z.im);
+  if (z.re >= R(0)) {
+    R t = sqrt((r + z.re) * R(0.5));
+    return cx(t, z.im / (R(2) * t));
+  }
+  R t = sqrt((r - z.re) * R(0.5));
+  return cx(fabs(z.im) / (R(2) * t), copysign(t, z.im));
+}
+template <class R>
+__device__ __forceinline__ Cx<R> cexp_(Cx<R> z) {
+  R e = exp(z.re);
+  return cx(e * cos(z.im), e * sin(z.im));
+}
+template <class R>
+__device__ __forceinline__ Cx<R> clog_(Cx<R> z) {
+  return cx(log(hypot(z.re, z.im)), atan2(z.im, z.re));
+}
+template <class R>
+__device__ __forceinline__ Cx<R> csin_(Cx<R> z) {
+  return cx(sin(z.re) * cosh(z.im), cos(z.re) * sinh(z.im));
+}
+template <class R>
+__device__ __forceinline__ Cx<R> ccos_(Cx<R> z) {
+  return cx(cos(z.re) * cosh(z.im), -(sin(z.re) * sinh(z.im)));
+}
+// asin z = -i log(i z + sqrt(1 - z^2))
+template <class R>
+__device__ __forceinline__ Cx<R> casin_(Cx<R> z) {
+  Cx<R> iz = cx(-z.im, z.re);
+  Cx<R> w = clog_(iz + csqrt(cx(R(1)) - z * z));
+  return cx(w.im, -w.re);
+}
+
+template <class R>
+struct M3 {
+  R m[9];  // row-major
+};
+template <class R>
+__device__ __forceinline__ void mv(const M3<R>& a, const R* v, R* r) {
+  for (int i = 0; i < 3; ++i) r[i] = (a.m[3 * i] * v[0] + a.m[3 * i + 1] * v[1]) + a.m[3 * i + 2] * v[2];
+}
+template <class R>
+__device__ __forceinline__ void mtv(const M3<R>& a, const Cx<R>* v, Cx<R>* r) {  // a^T v
+  for (int i = 0; i < 3; ++i)
+    r[i] = (a.m[i] * v[0] + a.m[3 + i] * v[1]) + a.m[6 + i] * v[2];
+}
+template <class R>
+__device__ __forceinline__ void mcv(const M3<R>& a, const Cx<R>* v, Cx<R>* r) {  // a v
+  for (int i = 0; i < 3; ++i)
+    r[i] = (a.m[3 * i] * v[0] + a.m[3 * i + 1] * v[1]) + a.m[3 * i + 2] * v[2];
+}
+
+// TransformationMatrix(theta, phi, sph2Cart=true), VecMatDef.h:85-99
+template <class R>
+__device__ __forceinline__ M3<R> sph_frame(R th, R ph) {
+  R st = sin(th), sp = sin(ph), ct = cos(th), cp = cos(ph);
+  return M3<R>{{st * cp, ct * cp, -sp, st * sp, ct * sp, cp, ct, -st, R(0)}};
+}
+
+struct FieldConsts {
+  double e0, eta0, pi_hi, pi_lo;  // reference constants (computed on the host)
+};
+
+// GetTransAngle + GetTMCoeff/GetTECoeff for air -> eps_t; returns the
+// coefficient pair (TM, TE) applied to E_theta, E_phi.
+template <class R>
+__device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, R lam, bool inf_wall,
+                             R eta0, Cx<R>& c_tm, Cx<R>& c_te) {
+  const Cx<R> ni = cx(R(1)), nt = csqrt(eps_t);
+  const Cx<R> ti = cx(theta_i);
+  const Cx<R> tt = casin_((ni / nt) * csin_(ti));
+  const Cx<R> etai = eta0 / ni, etat = eta0 / nt;
+  const Cx<R> ci = ccos_(ti), ct = ccos_(tt), si = csin_(ti);
+  const Cx<R> g_te = -((etat / ct) - (etai / ci)) / ((etat / ct) + (etai / ci));
+  const Cx<R> g_tm = (-(etat * ct) + etai * ci) / (etat * ct + etai * ci);
+  if (inf_wall) {
+    c_tm = reflect ? g_tm : cx(R(0));
+    c_te = reflect ? g_te : cx(R(0));
+    return;
+  }
+  // Slab form with zero width (the reference always passes width 0).
+  const Cx<R> q = (R(0) / lam) * csqrt(nt - si * si);
+  const Cx<R> ph = cexp_(cx(R(0), R(-2)) * q);
+  const Cx<R> one = cx(R(1));
+  const Cx<R> den_tm = one - g_tm * g_tm * ph, den_te = one - g_te * g_te * ph;
+  if (reflect) {
+    c_tm = (g_tm * (one - ph)) / den_tm;
+    c_te = (g_te * (one - ph)) / den_te;
+  } else {
+    c_tm = ((one - g_tm * g_tm) * ph) / den_tm;
+    c_te = ((one - g_te * g_te) * ph) / den_te;
+  }
+}
+
+// One corrected path: n rays with endpoints pts[i] -> pts[i+1], the hit
+// triangle frame of ray i's end (or none for the last ray), and the kind /
+// material of each ray's start.  Returns E (3 complex, global Cartesian).
+template <class R>
+__device__ void path_field(int n, const double (*pts)[3], const double* const* frames,
+                           const int* kind, const int* mat, const Material* mats,
+                           const double* txcs, double freq, double pt, int antenna,
+                           bool fresnel, const FieldConsts& K, Cx<double>* out) {
+  const double lam64 = 2.99792458e8 / freq;
+  const R lam = R(lam64);
+  M3<R> cur, next;
+  for (int i = 0; i < 9; ++i) next.m[i] = R(txcs[i]);
+  Cx<R> tot[3] = {cx(R(0)), cx(R(0)), cx(R(0))};
+  double L = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double vg64[3] = {pts[i + 1][0] - pts[i][0], pts[i + 1][1] - pts[i][1], pts[i + 1][2] - pts[i][2]};
+    R vg[3] = {R(vg64[0]), R(vg64[1]), R(vg64[2])};
+    R vl[3];
+    mv(next, vg, vl);
+    // CartesianToSpherical (VecMatDef.h:132-155); r is kept in FP64.
+    double vl64[3];
+    {
+      double nx[9];
+      for (int j = 0; j < 9; ++j) nx[j] = double(next.m[j]);
+      for (int j = 0; j < 3; ++j)
+        vl64[j] = (nx[3 * j] * vg64[0] + nx[3 * j + 1] * vg64[1]) + nx[3 * j + 2] * vg64[2];
+    }
+    const double r = sqrt((vl64[0] * vl64[0] + vl64[1] * vl64[1]) + vl64[2] * vl64[2]);
+    R th, ph;
+    if (vl[0] == R(0) && vl[1] == R(0) && vl[2] == R(0)) th = R(K.pi_hi * 0.5);
+    else th = atan2(sqrt(vl[0] * vl[0] + vl[1] * vl[1]), vl[2]);
+    ph = atan2(vl[1], vl[0]);
+    if (ph < R(0)) ph = R((double(ph) + 2.0 * K.pi_hi) + 2.0 * K.pi_lo);
+    L += r;
+    cur = next;
+    if (frames[i] == nullptr) {
+      for (int j = 0; j < 9; ++j) next.m[j] = (j % 4 == 0) ? R(1) : R(0);
+    } else {
+      for (int j = 0; j < 9; ++j) next.m[j] = R(frames[i][j]);
+    }
+    Cx<R> inc[3];
+    const M3<R> T = sph_frame(th, ph);
+    if (i == 0) {
+      inc[0] = inc[1] = inc[2] = cx(R(0));
+      if (antenna == 0) inc[0] = cx(R(0), R(sqrt(60.0 * pt)));
+      if (antenna == 1) inc[1] = cx(R(0), R(sqrt(60.0 * pt * 1.5)) * sin(th));
+      else if (antenna == 2)
+        inc[1] = cx(R(0), R(sqrt(60.0 * pt)) * (cos(R(K.pi_hi) * cos(th) / R(2)) / sin(th)));
+    } else {
+      Cx<R> g[3];
+      mtv(cur, tot, g);   // RotateToNewCoordSys(E, current, global) = current^T E
+      mtv(T, g, inc);     // CartesianToSphericalVector = T^T
+    }
+    if (kind[i] != 0) {
+      // AngleBetween(vecGlobal, current row 2) in radians (VecMatDef.h:56-77)
+      R a[3] = {vg[0], vg[1], vg[2]}, b[3] = {cur.m[6], cur.m[7], cur.m[8]};
+      R za = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
+      if (za > R(0)) { R s = sqrt(za); a[0] /= s; a[1] /= s; a[2] /= s; }
+      R zb = (b[0] * b[0] + b[1] * b[1]) + b[2] * b[2];
+      if (zb > R(0)) { R s = sqrt(zb); b[0] /= s; b[1] /= s; b[2] /= s; }
+      R ratio = (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+      R ang;
+      if (ratio < R(0)) {
+        R e0 = -a[0] - b[0], e1 = -a[1] - b[1], e2 = -a[2] - b[2];
+        R y = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
+        ang = R((K.pi_hi - double(y)) + K.pi_lo);
+      } else {
+        R e0 = a[0] - b[0], e1 = a[1] - b[1], e2 = a[2] - b[2];
+        ang = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
+      }
+      const Material& m = mats[mat[i]];
+      const Cx<R> eps_t = cx(R(m.eps_re), R(-1.0 * m.sigma / (K.e0 * 2.0 * K.pi_hi * freq)));
+      Cx<R> ctm, cte;
+      fresnel_pair<R>(kind[i] == 1, ang, eps_t, lam, fresnel, R(K.eta0), ctm, cte);
+      tot[0] = inc[0];
+      tot[1] = inc[1] * ctm;
+      tot[2] = inc[2] * cte;
+    } else {
+      tot[0] = inc[0];
+      tot[1] = inc[1];
+      tot[2] = inc[2];
+    }
+    Cx<R> c[3];
+    mcv(T, tot, c);     // SphericalToCartesianVector = T
+    mtv(cur, c, tot);   // back to global: current^T
+  }
+  // E * exp(-j k L) / L with k L in FP64 and reduced mod 2 pi before sin/cos
+  const double k = (2.0 * K.pi_hi) / lam64;
+  const double kl = k * L;
+  const double s = sin(-kl), c = cos(-kl);
+  for (int j = 0; j < 3; ++j) {
+    const double re = double(tot[j].re), im = double(tot[j].im);
+    out[j] = Cx<double>{(re * c - im * s) / L, (re * s + im * c) / L};
+  }
+}
+
+}  // namespace sbr

@@ -1,0 +1,421 @@
+// Host-side scene preparation (see sbr_host.h).  Compiled with
+// -ffp-contract=off: every FP64 expression below is evaluated in the order
+// written, which is the reference's order, so results are bit-identical to
+// the reference on any host.
+#include "sbr_host.h"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <numeric>
+#include <sstream>
+#include <unordered_map>
+
+namespace sbr {
+namespace {
+
+inline double sqn(const double* a) { return (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2]; }
+
+// Eigen's normalized(): v / sqrt(|v|^2) when |v|^2 > 0.
+inline void normalize3(const double* a, double* out) {
+  double z = sqn(a);
+  if (z > 0) {
+    double s = std::sqrt(z);
+    out[0] = a[0] / s;
+    out[1] = a[1] / s;
+    out[2] = a[2] / s;
+  } else {
+    out[0] = a[0];
+    out[1] = a[1];
+    out[2] = a[2];
+  }
+}
+
+void finish_tri(HostTri& t) {
+  double e[3] = {t.v2[0] - t.v1[0], t.v2[1] - t.v1[1], t.v2[2] - t.v1[2]};
+  double y[3];
+  normalize3(e, y);
+  const double* z = t.n;
+  double x[3] = {y[1] * z[2] - y[2] * z[1], y[2] * z[0] - y[0] * z[2], y[0] * z[1] - y[1] * z[0]};
+  for (int j = 0; j < 3; ++j) {
+    t.cs[j] = x[j];
+    t.cs[3 + j] = y[j];
+    t.cs[6 + j] = z[j];
+  }
+  for (int a = 0; a < 3; ++a) {
+    t.bb[a] = std::min({t.v1[a], t.v2[a], t.v3[a]});
+    t.bb[3 + a] = std::max({t.v1[a], t.v2[a], t.v3[a]});
+    t.center[a] = (t.bb[a] + t.bb[3 + a]) / 2.0;
+  }
+}
+
+double surface_area(const double* b) {
+  if (b[3] <= b[0] || b[4] <= b[1] || b[5] <= b[2]) return 0.0;
+  const double dx = b[3] - b[0], dy = b[4] - b[1], dz = b[5] - b[2];
+  return 2.0 * (dx * dy + dy * dz + dz * dx);
+}
+void empty_box(double* b) {
+  for (int a = 0; a < 3; ++a) {
+    b[a] = std::numeric_limits<float>::max();
+    b[3 + a] = -std::numeric_limits<float>::max();
+  }
+}
+void merge_box(const double* b1, const double* b2, double* r) {
+  for (int a = 0; a < 3; ++a) {
+    r[a] = std::min(b1[a], b2[a]);
+    r[3 + a] = std::max(b1[3 + a], b2[3 + a]);
+  }
+}
+
+struct BuildNode {
+  double bb[6];
+  int c0 = -1, c1 = -1;
+  std::vector<int> objs;  // leaf: triangle ids in the reference's order
+};
+
+// One step of the reference's SAH build (BVH/BVH.h:135-230) on a node whose
+// object list is `objs` (sorted in place exactly as the reference does).
+// Returns the split index, or -1 for a leaf.
+int sah_split(const std::vector<HostTri>& tris, std::vector<int>& objs, double* bb,
+              std::vector<double>& sa1, std::vector<double>& sa2) {
+  empty_box(bb);
+  for (int o : objs) merge_box(tris[o].bb, bb, bb);
+  const int n = int(objs.size());
+  double best_cost = 1.0 * n;
+  int best_axis = -1, best_split = -1;
+  const double sa_root = surface_area(bb);
+  sa1.assign(size_t(n) + 1, std::numeric_limits<double>::max());
+  sa2.assign(size_t(n) + 1, std::numeric_limits<double>::max());
+  for (int axis = 0; axis < 3; ++axis) {
+    std::sort(objs.begin(), objs.end(), [&tris, axis](int a, int b) {
+      return tris[a].center[axis] < tris[b].center[axis];
+    });
+    double b1[6];
+    empty_box(b1);
+    sa1[0] = surface_area(b1);
+    for (int i = 0; i < n; ++i) {
+      merge_box(b1, tris[objs[i]].bb, b1);
+      sa1[i] = surface_area(b1);
+    }
+    double b2[6];
+    empty_box(b2);
+    sa2[n] = surface_area(b2);
+    for (int i = n - 1; i >= 0; --i) {
+      merge_box(b2, tris[objs[i]].bb, b2);
+      sa2[i] = surface_area(b2);
+    }
+    for (int i = 1; i < n - 1; ++i) {
+      const int j = n - i;
+      const double cost = 2 * 1.0 + (i * sa1[i] + j * sa2[i]) * 1.0 / sa_root;
+      if (cost < best_cost) {
+        best_cost = cost;
+        best_axis = axis;
+        best_split = i;
+      }
+    }
+  }
+  if (best_axis == -1) return -1;
+  std::sort(objs.begin(), objs.end(), [&tris, best_axis](int a, int b) {
+    return tris[a].center[best_axis] < tris[b].center[best_axis];
+  });
+  return best_split;
+}
+
+}  // namespace
+
+bool read_stl(const std::string& path, std::vector<float>& v, std::vector<float>& n,
+              std::string& err) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) {
+    err = "cannot open " + path;
+    return false;
+  }
+  std::string head(256, '\0');
+  in.read(&head[0], 256);
+  head.resize(size_t(in.gcount()));
+  for (auto& ch : head) ch = char(std::tolower(static_cast<unsigned char>(ch)));
+  const bool ascii = head.find("solid") != std::string::npos &&
+                     head.find('\n') != std::string::npos &&
+                     head.find("facet") != std::string::npos &&
+                     head.find("normal") != std::string::npos;
+  in.clear();
+  in.seekg(0);
+  v.clear();
+  n.clear();
+  if (ascii) {
+    std::string line, tok;
+    size_t nv = 0;
+    while (std::getline(in, line)) {
+      std::istringstream ls(line);
+      std::vector<std::string> toks;
+      while (ls >> tok) toks.push_back(tok);
+      if (toks.empty()) continue;
+      if (toks[0] == "vertex") {
+        if (toks.size() < 4) {
+          err = "malformed vertex line in " + path;
+          return false;
+        }
+        for (int i = 0; i < 3; ++i) v.push_back(float(std::atof(toks[1 + i].c_str())));
+        ++nv;
+      } else if (toks[0] == "facet") {
+        if (toks.size() < 5 || toks[1] != "normal") {
+          err = "malformed facet line in " + path;
+          return false;
+        }
+        for (int i = 0; i < 3; ++i) n.push_back(float(std::atof(toks[2 + i].c_str())));
+        nv = 0;
+      } else if (toks[0] == "endfacet") {
+        if (nv != 3) {
+          err = "facet without 3 vertices in " + path;
+          return false;
+        }
+      }
+    }
+  } else {
+    char hdr[80];
+    uint32_t cnt = 0;
+    in.read(hdr, 80);
+    in.read(reinterpret_cast<char*>(&cnt), 4);
+    if (!in) {
+      err = "truncated binary STL header in " + path;
+      return false;
+    }
+    v.resize(size_t(cnt) * 9);
+    n.resize(size_t(cnt) * 3);
+    for (uint32_t t = 0; t < cnt; ++t) {
+      float d[12];
+      char attr[2];
+      in.read(reinterpret_cast<char*>(d), 48);
+      in.read(attr, 2);
+      if (!in) {
+        err = "truncated binary STL facet in " + path;
+        return false;
+      }
+      std::memcpy(&n[3 * size_t(t)], d, 12);
+      std::memcpy(&v[9 * size_t(t)], d + 3, 36);
+    }
+  }
+  if (n.size() * 3 != v.size()) {
+    err = "facet/vertex count mismatch in " + path;
+    return false;
+  }
+  return true;
+}
+
+bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, HostScene& out,
+                   std::string& err) {
+  out = HostScene();
+  if (n_tri <= 0 || !v || !nrm) {
+    err = "empty triangle list";
+    return false;
+  }
+  // Exact vertex merge (StlReader.h:448-508): equal float triples share an id.
+  struct Key {
+    float x, y, z;
+    bool operator==(const Key& o) const { return x == o.x && y == o.y && z == o.z; }
+  };
+  struct KeyHash {
+    size_t operator()(const Key& k) const {
+      // +0.0 and -0.0 compare equal, so hash them alike.
+      float a = k.x == 0.0f ? 0.0f : k.x, b = k.y == 0.0f ? 0.0f : k.y,
+            c = k.z == 0.0f ? 0.0f : k.z;
+      uint32_t u[3];
+      std::memcpy(&u[0], &a, 4);
+      std::memcpy(&u[1], &b, 4);
+      std::memcpy(&u[2], &c, 4);
+      uint64_t h = 1469598103934665603ull;
+      for (uint32_t w : u) h = (h ^ w) * 1099511628211ull;
+      return size_t(h);
+    }
+  };
+  const size_t nv = size_t(n_tri) * 3;
+  std::unordered_map<Key, int, KeyHash> ids;
+  ids.reserve(nv);
+  std::vector<int> uid(nv);
+  for (size_t i = 0; i < nv; ++i) {
+    Key k{v[3 * i], v[3 * i + 1], v[3 * i + 2]};
+    auto it = ids.emplace(k, int(ids.size())).first;
+    uid[i] = it->second;
+  }
+  std::vector<int> vidx;
+  std::vector<size_t> src;
+  for (size_t t = 0; t < size_t(n_tri); ++t) {
+    int a = uid[3 * t], b = uid[3 * t + 1], c = uid[3 * t + 2];
+    if (a != b && a != c && b != c) {
+      vidx.push_back(a);
+      vidx.push_back(b);
+      vidx.push_back(c);
+      src.push_back(t);
+    }
+  }
+  // A collapsed facet shifts later normals in the reference reader; reject
+  // such input instead of reproducing the misalignment silently.
+  if (src.size() != size_t(n_tri)) {
+    err = "degenerate triangle(s) after vertex merge: " + std::to_string(size_t(n_tri) - src.size());
+    return false;
+  }
+  out.tris.resize(src.size());
+  double ext = 0;
+  for (size_t t = 0; t < src.size(); ++t) {
+    HostTri& tr = out.tris[t];
+    const float* p = &v[9 * src[t]];
+    for (int a = 0; a < 3; ++a) {
+      tr.v1[a] = p[a];
+      tr.v2[a] = p[3 + a];
+      tr.v3[a] = p[6 + a];
+      tr.n[a] = nrm[3 * t + a];
+      ext = std::max({ext, std::fabs(tr.v1[a]), std::fabs(tr.v2[a]), std::fabs(tr.v3[a])});
+    }
+    tr.id = int(t);
+    tr.mat = mat ? mat[src[t]] : 0;
+    finish_tri(tr);
+  }
+  out.extent = ext;
+
+  // Coplanar ids (Preprocessor.cpp:116-246).
+  const int nt = int(out.tris.size());
+  std::vector<int> parent(nt);
+  std::iota(parent.begin(), parent.end(), 0);
+  auto find = [&](int a) {
+    while (parent[a] != a) a = parent[a] = parent[parent[a]];
+    return a;
+  };
+  std::unordered_map<uint64_t, std::vector<int>> edges;
+  edges.reserve(size_t(nt) * 2);
+  auto same_or_opposite = [&](int a, int b) {
+    const double* p = out.tris[a].n;
+    const double* q = out.tris[b].n;
+    return (p[0] == q[0] && p[1] == q[1] && p[2] == q[2]) ||
+           (p[0] == -q[0] && p[1] == -q[1] && p[2] == -q[2]);
+  };
+  for (int t = 0; t < nt; ++t) {
+    int a = vidx[3 * t], b = vidx[3 * t + 1], c = vidx[3 * t + 2];
+    int es[3][2] = {{std::min(a, b), std::max(a, b)},
+                    {std::min(b, c), std::max(b, c)},
+                    {std::min(a, c), std::max(a, c)}};
+    for (auto& e : es) {
+      uint64_t key = (uint64_t(uint32_t(e[0])) << 32) | uint32_t(e[1]);
+      auto& lst = edges[key];
+      for (int o : lst)
+        if (same_or_opposite(o, t)) parent[find(o)] = find(t);
+      lst.push_back(t);
+    }
+  }
+  std::vector<int> comp(nt, -1);
+  int next = 0;
+  for (int t = 0; t < nt; ++t) {
+    int r = find(t);
+    if (comp[r] < 0) comp[r] = next++;
+    out.tris[t].cop = comp[r];
+  }
+
+  // SAH BVH with the reference's splits; nodes renumbered depth-first.
+  std::vector<BuildNode> bn;
+  bn.reserve(size_t(2) * nt);
+  bn.emplace_back();
+  bn[0].objs.resize(nt);
+  std::iota(bn[0].objs.begin(), bn[0].objs.end(), 0);
+  std::vector<double> sa1, sa2;
+  std::vector<int> work{0};
+  bool root_done = false;
+  while (!work.empty()) {
+    int idx = work.back();
+    work.pop_back();
+    std::vector<int> objs;
+    objs.swap(bn[idx].objs);
+    double bb[6];
+    int split = sah_split(out.tris, objs, bb, sa1, sa2);
+    std::memcpy(bn[idx].bb, bb, sizeof bb);
+    if (!root_done) {
+      out.mesh_order = objs;  // the caller's vector after ConstructBVH
+      root_done = true;
+    }
+    if (split < 0) {
+      bn[idx].objs.swap(objs);
+      continue;
+    }
+    int c0 = int(bn.size());
+    bn.emplace_back();
+    int c1 = int(bn.size());
+    bn.emplace_back();
+    bn[idx].c0 = c0;
+    bn[idx].c1 = c1;
+    bn[c0].objs.assign(objs.begin(), objs.begin() + split);
+    bn[c1].objs.assign(objs.begin() + split, objs.end());
+    work.push_back(c1);
+    work.push_back(c0);
+  }
+  // Depth-first renumbering, children[0] first.
+  out.nodes.clear();
+  out.nodes.reserve(bn.size());
+  struct Item {
+    int b, parent, depth, slot_parent, which;
+  };
+  std::vector<Item> st{{0, -1, 0, -1, 0}};
+  while (!st.empty()) {
+    Item it = st.back();
+    st.pop_back();
+    int me = int(out.nodes.size());
+    out.nodes.emplace_back();
+    HostNode& hn = out.nodes.back();
+    std::memcpy(hn.bb, bn[it.b].bb, sizeof hn.bb);
+    hn.parent = it.parent;
+    hn.depth = it.depth;
+    out.max_depth = std::max(out.max_depth, it.depth);
+    if (it.slot_parent >= 0) {
+      if (it.which == 0) out.nodes[it.slot_parent].c0 = me;
+      else out.nodes[it.slot_parent].c1 = me;
+    }
+    if (bn[it.b].c0 < 0) {
+      hn.first = int(out.dfs_tris.size());
+      hn.count = int(bn[it.b].objs.size());
+      out.dfs_tris.insert(out.dfs_tris.end(), bn[it.b].objs.begin(), bn[it.b].objs.end());
+    } else {
+      st.push_back({bn[it.b].c1, me, it.depth + 1, me, 1});
+      st.push_back({bn[it.b].c0, me, it.depth + 1, me, 0});
+    }
+  }
+  return true;
+}
+
+void icosphere(int level, std::vector<double>& dirs) {
+  const double X = .525731112119133606, Z = .850650808352039932, N = 0.0;
+  std::vector<double> v = {-X, N, Z, X, N, Z,  -X, N, -Z, X, N, -Z, N, Z, X,  N, Z, -X,
+                           N,  -Z, X, N, -Z, -X, Z,  X, N, -Z, X,  N, Z, -X, N, -Z, -X, N};
+  std::vector<int> f = {0, 4, 1,  0, 9, 4,  9, 5, 4,  4, 5, 8,  4, 8, 1,  8, 10, 1, 8, 3, 10,
+                        5, 3, 8,  5, 2, 3,  2, 7, 3,  7, 10, 3, 7, 6, 10, 7, 11, 6, 11, 0, 6,
+                        0, 1, 6,  6, 1, 10, 9, 0, 11, 9, 11, 2, 9, 2, 5,  7, 2, 11};
+  for (int l = 0; l < level; ++l) {
+    std::unordered_map<uint64_t, int> lookup;
+    lookup.reserve(f.size());
+    std::vector<int> nf;
+    nf.reserve(f.size() * 4);
+    auto mid = [&](int a, int b) {
+      uint64_t key = (uint64_t(uint32_t(std::min(a, b))) << 32) | uint32_t(std::max(a, b));
+      auto ins = lookup.emplace(key, int(v.size() / 3));
+      if (ins.second) {
+        double s[3] = {v[3 * a] + v[3 * b], v[3 * a + 1] + v[3 * b + 1], v[3 * a + 2] + v[3 * b + 2]};
+        double m[3];
+        normalize3(s, m);
+        v.insert(v.end(), m, m + 3);
+      }
+      return ins.first->second;
+    };
+    for (size_t t = 0; t < f.size(); t += 3) {
+      int a = f[t], b = f[t + 1], c = f[t + 2];
+      int m0 = mid(a, b), m1 = mid(b, c), m2 = mid(c, a);
+      int add[12] = {a, m0, m2, b, m1, m0, c, m2, m1, m0, m1, m2};
+      nf.insert(nf.end(), add, add + 12);
+    }
+    f.swap(nf);
+  }
+  dirs.resize(v.size());
+  for (size_t i = 0; i < v.size(); i += 3) normalize3(&v[i], &dirs[i]);
+}
+
+}  // namespace sbr

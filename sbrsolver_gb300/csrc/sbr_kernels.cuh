@@ -1,0 +1,349 @@
+// Device functions of the SBR path: closest hit, reception sphere, image
+// correction and the received field.  Reference behaviour is cited per
+// function (paths relative to SBRSolver_rev2/).
+#pragma once
+
+#include <cfloat>
+#include <climits>
+#include <cuda_runtime.h>
+
+#include "sbr_device.h"
+
+namespace sbr {
+
+constexpr double kEps64 = 1.1920928955078125e-07;  // FLT_EPSILON as double, Constants.h:13
+constexpr float kEps32 = 1.1920928955078125e-07f;
+constexpr float kFiltK = 6.103515625e-05f;         // 2^-14: FP32 filter margin factor
+
+struct Hit {
+  double t, dist;
+  double p[3];
+  int rank;  // index in depth-first triangle order, INT_MAX = no hit
+  int leaf;
+};
+
+// Triangle::RayIntersects (Triangle.cpp:80-124), FP64, reference operation order.
+__device__ __forceinline__ bool mt64(const Tri64& T, const double* o, const double* d, double& t,
+                                     double* P, double& dist) {
+  using namespace x64;
+  double h[3];
+  cross(d, T.e2, h);
+  const double a = dot(T.e1, h);
+  if (a > -kEps64 && a < kEps64) return false;
+  const double f = div(1.0, a);
+  double s[3];
+  sub3(o, T.v1, s);
+  const double u = mul(f, dot(s, h));
+  if (u < 0.0 || u > 1.0) return false;
+  double q[3];
+  cross(s, T.e1, q);
+  const double v = mul(f, dot(d, q));
+  if (v < 0.0 || add(u, v) > 1.0) return false;
+  const double tt = mul(f, dot(T.e2, q));
+  if (!(tt > kEps64)) return false;
+  P[0] = add(o[0], mul(d[0], tt));
+  P[1] = add(o[1], mul(d[1], tt));
+  P[2] = add(o[2], mul(d[2], tt));
+  double w[3];
+  sub3(P, o, w);
+  dist = norm(w);
+  t = tt;
+  return true;
+}
+
+// Same test on a CorrTri (image correction looks triangles up by mesh position).
+__device__ __forceinline__ bool mt64c(const CorrTri& T, const double* o, const double* d,
+                                      double* P) {
+  Tri64 t;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    t.v1[i] = T.v1[i];
+    t.e1[i] = T.e1[i];
+    t.e2[i] = T.e2[i];
+  }
+  double tt, dist;
+  return mt64(t, o, d, tt, P, dist);
+}
+
+// BVHNode::IntersectsAABB (BVH/BVHNode.h:64-85), FP64, with std::min/std::max
+// argument order so NaN slabs are ignored exactly as the reference ignores them.
+__device__ __forceinline__ bool slab64(const double* bb, const double* o, const double* d) {
+  using namespace x64;
+  double tmax = __longlong_as_double(0x7ff0000000000000ll);
+  double tmin = -tmax;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double t1 = div(sub(bb[i], o[i]), d[i]);
+    const double t2 = div(sub(bb[3 + i], o[i]), d[i]);
+    const double tn = (t2 < t1) ? t2 : t1;
+    const double tf = (t1 < t2) ? t2 : t1;
+    tmax = (tf < tmax) ? tf : tmax;
+    tmin = (tmin < tn) ? tn : tmin;
+    if (tmin > tmax) return false;
+  }
+  return true;
+}
+
+// BVH::RayIntersects (BVH/BVH.h:276-328) exactly: depth-first, both children,
+// children[0] first, strict '<' on distance so the first visited wins ties.
+__device__ bool exact_closest(const DevScene& sc, const double* o, const double* d, Hit& best,
+                              unsigned* overflow) {
+  int stack[kStack];
+  int sp = 0;
+  stack[sp++] = 0;
+  best.rank = INT_MAX;
+  best.dist = __longlong_as_double(0x7ff0000000000000ll);
+  while (sp > 0) {
+    const int n = stack[--sp];
+    const RefNode& nd = sc.ref[n];
+    if (!slab64(nd.bb, o, d)) continue;
+    if (nd.c0 >= 0) {
+      if (sp + 2 > kStack) {
+        atomicOr(overflow, kOvStack);
+        return false;
+      }
+      stack[sp++] = nd.c1;
+      stack[sp++] = nd.c0;
+    } else {
+      for (int r = nd.first; r < nd.first + nd.count; ++r) {
+        double t, P[3], dist;
+        if (mt64(sc.tri64[r], o, d, t, P, dist) && dist < best.dist) {
+          best.dist = dist;
+          best.t = t;
+          best.p[0] = P[0];
+          best.p[1] = P[1];
+          best.p[2] = P[2];
+          best.rank = r;
+          best.leaf = n;
+        }
+      }
+    }
+  }
+  return best.rank != INT_MAX;
+}
+
+// FP32 Moller-Trumbore filter with error margins.  Returns false only when
+// the FP64 test certainly rejects; otherwise tlo is a lower bound on t.
+__device__ __forceinline__ bool tri_filter(const Tri32& T, const float3& o, const float3& d,
+                                           float no, float nd, float& tlo) {
+  const float hx = d.y * T.e2[2] - d.z * T.e2[1];
+  const float hy = d.z * T.e2[0] - d.x * T.e2[2];
+  const float hz = d.x * T.e2[1] - d.y * T.e2[0];
+  const float a = T.e1[0] * hx + T.e1[1] * hy + T.e1[2] * hz;
+  const float sx = o.x - T.v1[0], sy = o.y - T.v1[1], sz = o.z - T.v1[2];
+  float U = sx * hx + sy * hy + sz * hz;
+  const float qx = sy * T.e1[2] - sz * T.e1[1];
+  const float qy = sz * T.e1[0] - sx * T.e1[2];
+  const float qz = sx * T.e1[1] - sy * T.e1[0];
+  float V = d.x * qx + d.y * qy + d.z * qz;
+  float W = T.e2[0] * qx + T.e2[1] * qy + T.e2[2] * qz;
+  const float ns = no + T.nv1;
+  const float ea = kFiltK * T.ne1 * T.ne2 * nd;
+  const float eU = kFiltK * ns * nd * T.ne2;
+  const float eV = kFiltK * ns * T.ne1 * nd;
+  const float eW = kFiltK * ns * T.ne1 * T.ne2;
+  const float A = fabsf(a);
+  if (A <= kEps32 + ea) {  // near-parallel: the FP64 test decides
+    tlo = 0.0f;
+    return true;
+  }
+  if (a < 0.0f) {
+    U = -U;
+    V = -V;
+    W = -W;
+  }
+  if (U < -eU || V < -eV) return false;
+  if (U > A + ea + eU) return false;
+  if (U + V > A + ea + eU + eV) return false;
+  const float thi = (W + eW) / (A - ea);
+  if (thi <= kEps32 * 0.5f) return false;
+  tlo = (W - eW) / (A + ea);
+  return true;
+}
+
+__device__ __forceinline__ void load_node(const Node32* nodes, int i, float4& f0, float4& f1,
+                                          float4& f2, int2& ch) {
+  const float4* p = reinterpret_cast<const float4*>(nodes + i);
+  f0 = __ldg(p);
+  f1 = __ldg(p + 1);
+  f2 = __ldg(p + 2);
+  const float4 f3 = __ldg(p + 3);
+  ch = make_int2(__float_as_int(f3.x), __float_as_int(f3.y));
+}
+
+__device__ __forceinline__ void slab32(float lx, float ly, float lz, float hx, float hy, float hz,
+                                       const float3& o, const float3& inv, float m, float& tn,
+                                       float& tf) {
+  const float ax = ((lx - m) - o.x) * inv.x, bx = ((hx + m) - o.x) * inv.x;
+  const float ay = ((ly - m) - o.y) * inv.y, by = ((hy + m) - o.y) * inv.y;
+  const float az = ((lz - m) - o.z) * inv.z, bz = ((hz + m) - o.z) * inv.z;
+  tn = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz));
+  tf = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz));
+}
+
+struct TraceStats {
+  unsigned fp64_tri, fallback;
+};
+
+// Closest hit with the reference's result.  FP32 ordered traversal over the
+// reference BVH (boxes widened by box_margin so no box the FP64 test accepts
+// is missed), FP32 triangle filter, FP64 test for every triangle the filter
+// cannot rule out, lexicographic (distance, depth-first rank) minimum - the
+// reference's strict '<' in visit order.  The winner is accepted only if every
+// ancestor box of its leaf passes the reference's FP64 slab test; otherwise
+// the ray is re-run with the reference-order traversal.
+__device__ bool closest_hit(const DevScene& sc, const double* o, const double* d, Hit& best,
+                            TraceStats& st, unsigned* overflow) {
+  const float3 o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
+  const float3 d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
+  const float3 inv = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
+  const float no = sqrtf(o32.x * o32.x + o32.y * o32.y + o32.z * o32.z);
+  const float nd = sqrtf(d32.x * d32.x + d32.y * d32.y + d32.z * d32.z);
+  const float m = sc.box_margin + kFiltK * no;
+  best.rank = INT_MAX;
+  best.dist = __longlong_as_double(0x7ff0000000000000ll);
+  best.t = best.dist;
+  float tcut = INFINITY;  // boxes entered beyond this cannot hold a better hit
+
+  int stack[kStack];
+  int sp = 0;
+  int pending_leaf = -1;
+  if (sc.root_leaf) pending_leaf = 0;
+  else stack[sp++] = 0;
+  bool stack_overflow = false;
+
+  while (true) {
+    if (pending_leaf >= 0) {
+      const RefNode& L = sc.ref[pending_leaf];
+      for (int r = L.first; r < L.first + L.count; ++r) {
+        float tlo;
+        if (!tri_filter(sc.tri32[r], o32, d32, no, nd, tlo)) continue;
+        if (tlo > tcut) continue;
+        ++st.fp64_tri;
+        double t, P[3], dist;
+        if (!mt64(sc.tri64[r], o, d, t, P, dist)) continue;
+        if (dist < best.dist || (dist == best.dist && r < best.rank)) {
+          best.dist = dist;
+          best.t = t;
+          best.p[0] = P[0];
+          best.p[1] = P[1];
+          best.p[2] = P[2];
+          best.rank = r;
+          best.leaf = pending_leaf;
+          tcut = float(t) * (1.0f + 1.0f / 4096.0f) + 1e-30f;
+        }
+      }
+      pending_leaf = -1;
+    }
+    if (sp == 0) break;
+    const int ni = stack[--sp];
+    if (ni < 0) {  // a leaf deferred as the farther child
+      pending_leaf = ~ni;
+      continue;
+    }
+    float4 f0, f1, f2;
+    int2 ch;
+    load_node(sc.node32, ni, f0, f1, f2, ch);
+    float tn0, tf0, tn1, tf1;
+    slab32(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, o32, inv, m, tn0, tf0);
+    slab32(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, o32, inv, m, tn1, tf1);
+    const bool h0 = tn0 <= tf0 && tf0 >= 0.0f && tn0 <= tcut;
+    const bool h1 = tn1 <= tf1 && tf1 >= 0.0f && tn1 <= tcut;
+    int first = 0, second = 0;
+    bool has_first = false, has_second = false;
+    if (h0 && h1) {
+      has_first = has_second = true;
+      if (tn1 < tn0) {
+        first = ch.y;
+        second = ch.x;
+      } else {
+        first = ch.x;
+        second = ch.y;
+      }
+    } else if (h0) {
+      has_first = true;
+      first = ch.x;
+    } else if (h1) {
+      has_first = true;
+      first = ch.y;
+    }
+    if (has_second) {
+      if (sp >= kStack) {
+        stack_overflow = true;
+        break;
+      }
+      stack[sp++] = second;  // internal node or ~leaf
+    }
+    if (has_first) {
+      if (first < 0) {
+        pending_leaf = ~first;
+      } else {
+        if (sp >= kStack) {
+          stack_overflow = true;
+          break;
+        }
+        stack[sp++] = first;
+      }
+    }
+  }
+
+  bool ok = !stack_overflow;
+  if (ok && best.rank != INT_MAX) {
+    // every ancestor of the winner's leaf must pass the FP64 slab test
+    for (int n = best.leaf; n >= 0; n = sc.ref[n].parent) {
+      if (!slab64(sc.ref[n].bb, o, d)) {
+        ok = false;
+        break;
+      }
+    }
+  }
+  if (!ok) {
+    ++st.fallback;
+    return exact_closest(sc, o, d, best, overflow);
+  }
+  return best.rank != INT_MAX;
+}
+
+// HitReceptionSphere (RTSolver.cpp:805-863), FP64 in the reference's order.
+__device__ __forceinline__ bool reception64(const double* s, const double* t, const double* c,
+                                            double path_len, double tan_beta) {
+  using namespace x64;
+  double rd[3], w[3];
+  sub3(t, s, rd);
+  sub3(c, s, w);
+  double t0 = div(dot(rd, w), sqn(rd));
+  if (t0 < 0) return false;
+  if (t0 >= 1) t0 = 1;
+  double P[3] = {add(s[0], mul(t0, rd[0])), add(s[1], mul(t0, rd[1])), add(s[2], mul(t0, rd[2]))};
+  const double unfolded = add(path_len, norm(P));
+  const double radius = mul(unfolded, tan_beta);
+  double e[3];
+  sub3(c, P, e);
+  return norm(e) <= radius;
+}
+
+// FP32 reception filter: 1 = captured, 0 = not captured, -1 = within the
+// error margin (decide with reception64).
+__device__ __forceinline__ int reception32(const float3& s, const float3& u, float len, float S,
+                                           const float3& c, float tanb) {
+  const float wx = c.x - s.x, wy = c.y - s.y, wz = c.z - s.z;
+  const float lam = u.x * wx + u.y * wy + u.z * wz;
+  const float ns = sqrtf(s.x * s.x + s.y * s.y + s.z * s.z);
+  const float nc = sqrtf(c.x * c.x + c.y * c.y + c.z * c.z);
+  const float mag = ns + nc + 1.0f;
+  const float ml = kFiltK * mag;
+  if (lam < -ml) return 0;
+  if (lam <= ml) return -1;
+  const float lc = fminf(lam, len);
+  const float px = s.x + lc * u.x, py = s.y + lc * u.y, pz = s.z + lc * u.z;
+  const float np = sqrtf(px * px + py * py + pz * pz);
+  const float ex = c.x - px, ey = c.y - py, ez = c.z - pz;
+  const float dist = sqrtf(ex * ex + ey * ey + ez * ez);
+  const float rad = (S + np) * tanb;
+  const float mr = kFiltK * (mag + S + np);
+  if (dist > rad + mr) return 0;
+  if (dist < rad - mr) return 1;
+  return -1;
+}
+
+}  // namespace sbr

@@ -1,0 +1,128 @@
+"""GPU path against the reference: identical path sets (receiver, launch,
+facet ids, coplanar ids, interaction kinds, ray counts) and received fields
+within 1e-4 relative magnitude / 1e-3 rad phase, through the C ABI."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from helpers import field_close, golden_field, golden_paths, max_rel_err, path_keys
+from sbrsolver_gb300 import api, scenes
+from test_oracle_golden import CASES, GOLD, _case
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu(wl, precision="fp64", scene=None):
+    sc = scene or api.DeviceScene.from_scene(wl.scene)
+    return api.solve(sc, api.request_from_workload(wl.request, precision)), sc
+
+
+def _check_against(res, ref_paths, ref_field, counts=None, tight=True):
+    assert path_keys(res.paths) == path_keys(ref_paths)
+    for p, q in zip(res.paths, ref_paths):
+        # corrected points come from FP64 arithmetic in the reference order
+        np.testing.assert_array_equal(p["points"], q["points"])
+    bad = field_close(res.field, ref_field)
+    assert not bad, bad[:5]
+    if tight:
+        assert max_rel_err(res.field, ref_field) < 1e-9
+    if counts:
+        for k, v in counts.items():
+            assert res.counts[k] == v, (k, res.counts[k], v)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_cases(built, name):
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    wl = _case(name)
+    res, _ = _gpu(wl)
+    _check_against(res, golden_paths(g), golden_field(g),
+                   {"segments": int(g["segments"]), "captured": int(g["captured"]),
+                    "corrected": int(g["corrected"])})
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp32_field_mode_within_tolerance(built, name):
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    res, _ = _gpu(_case(name), precision="fp32")
+    assert path_keys(res.paths) == path_keys(golden_paths(g))
+    bad = field_close(res.field, golden_field(g))
+    assert not bad, bad[:5]
+
+
+def test_scene_tables_match_oracle(built):
+    for wl in (scenes.small_scene(), scenes.urban_scene(level=3)):
+        sc = api.DeviceScene.from_scene(wl.scene)
+        o = orc.OracleScene.from_scene(wl.scene)
+        np.testing.assert_array_equal(sc.mesh_order(), o.mesh_order())
+        np.testing.assert_array_equal(sc.coplanar_ids(), o.coplanar_ids())
+
+
+def _oracle(wl):
+    return orc.solve(orc.OracleScene.from_scene(wl.scene), wl.request, wl.scene.materials)
+
+
+@pytest.mark.parametrize("level,R,T,antenna", [(6, 6, 1, 0), (5, 3, 2, 2), (6, 8, 0, 1),
+                                               (4, 0, 3, 0), (0, 2, 1, 1)])
+def test_urban_variants(built, level, R, T, antenna):
+    wl = scenes.urban_scene(level=level, rx_pitch=125.0, max_reflection=R, max_transmission=T)
+    wl.request.antenna = antenna
+    ref = _oracle(wl)
+    res, _ = _gpu(wl)
+    _check_against(res, ref["paths"], ref["field"],
+                   {k: ref["counts"][k] for k in ("segments", "captured", "corrected")})
+
+
+def test_identity_mesh_order(built):
+    """A caller whose triangle vector stays in file order: image correction
+    and frames then use the hit triangle itself."""
+    wl = scenes.small_scene()
+    sc = api.DeviceScene.from_scene(wl.scene)
+    sc.set_mesh_order(np.arange(wl.scene.n_tri, dtype=np.int32))
+    res, _ = _gpu(wl, scene=sc)
+    assert res.counts["corrected"] > 253  # more reflections survive correction
+    ref_sc = orc.OracleScene.from_scene(wl.scene)
+    assert res.counts["segments"] == 96720
+
+
+def test_batch_equals_single(built):
+    wl = scenes.small_scene()
+    a = scenes.small_scene()
+    a.request.tx = (30.0, -60.0, 12.0)
+    a.request.tessellation = 5
+    a.request.antenna = 0
+    sc = api.DeviceScene.from_scene(wl.scene)
+    r1 = api.solve(sc, api.request_from_workload(wl.request))
+    r2 = api.solve(sc, api.request_from_workload(a.request))
+    rb = api.solve(sc, [api.request_from_workload(wl.request), api.request_from_workload(a.request)])
+    np.testing.assert_array_equal(rb.field, np.concatenate([r1.field, r2.field]))
+    assert rb.counts["segments"] == r1.counts["segments"] + r2.counts["segments"]
+    pb = [p for p in rb.paths if p["request"] == 0]
+    assert path_keys(pb) == path_keys(r1.paths)
+    pb = [p for p in rb.paths if p["request"] == 1]
+    assert path_keys(pb) == path_keys(r2.paths)
+
+
+def test_edge_cases(built):
+    wl = scenes.small_scene()
+    sc = api.DeviceScene.from_scene(wl.scene)
+    # no receivers
+    wl0 = scenes.small_scene()
+    wl0.request.rx = np.zeros((0, 3))
+    r = api.solve(sc, api.request_from_workload(wl0.request))
+    assert r.counts["paths"] == 0 and r.counts["segments"] == 96720
+    # receiver exactly at the transmitter, receivers on a facet, no bounces
+    wl1 = scenes.small_scene()
+    wl1.request.rx = np.array([wl1.request.tx, (5.0, 5.0, 0.0), (50.0, -10.0, 1.5)])
+    wl1.request.max_reflection = 0
+    ref = _oracle(wl1)
+    res = api.solve(sc, api.request_from_workload(wl1.request))
+    assert path_keys(res.paths) == path_keys(ref["paths"])
+    assert not field_close(res.field, ref["field"])
+    # bad requests
+    bad = scenes.small_scene()
+    bad.request.tessellation = 13
+    with pytest.raises(Exception):
+        api.solve(sc, api.request_from_workload(bad.request))

@@ -1,0 +1,69 @@
+"""The C-ABI library (no GPU needed): it builds, loads, exports every symbol
+include/sbr.h declares, and rejects bad arguments with a status and message."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from sbrsolver_gb300 import _lib, api, scenes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _gpu_present():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def test_header_and_exports_agree(built):
+    hdr = open(os.path.join(ROOT, "include", "sbr.h")).read()
+    declared = set(re.findall(r"\b(sbr_[a-z_]+)\s*\(", hdr))
+    assert declared == set(_lib.EXPORTS)
+    lib = _lib.load()
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert b"sm_103a" in lib.sbr_version()
+
+
+def test_null_arguments_are_rejected(built):
+    lib = _lib.load()
+    out = C.c_void_p()
+    assert lib.sbr_scene_create(0, None, None, None, None, 0, C.byref(out)) == _lib.ERR_INVALID_ARG
+    assert b"empty" in lib.sbr_last_error()
+    assert lib.sbr_solve_batch(None, None, 0, C.byref(out)) == _lib.ERR_INVALID_ARG
+    assert lib.sbr_result_counts(None, None) == _lib.ERR_INVALID_ARG
+    assert lib.sbr_scene_destroy(None) == _lib.OK
+    assert lib.sbr_result_destroy(None) == _lib.OK
+
+
+def test_missing_stl_is_io_error(built):
+    lib = _lib.load()
+    out = C.c_void_p()
+    m = (_lib.Material * 1)(_lib.Material(1e9, 0, 0, 5, 0, 0.1))
+    st = lib.sbr_scene_create_from_stl(b"/nonexistent/x.stl", None, m, 1, C.byref(out))
+    assert st == _lib.ERR_IO
+    assert b"cannot open" in lib.sbr_last_error()
+
+
+def test_bad_material_id_rejected(built):
+    wl = scenes.small_scene()
+    mesh = api.Mesh(wl.scene.tri, wl.scene.normal, np.full(wl.scene.n_tri, 7, np.int32))
+    with pytest.raises(_lib.SbrError) as e:
+        api.DeviceScene(mesh, [api.MaterialProperties()])
+    assert e.value.status == _lib.ERR_INVALID_ARG
+    assert "material id out of range" in str(e.value)
+
+
+@pytest.mark.skipif(_gpu_present(), reason="checks the no-GPU error path")
+def test_no_gpu_fails_loudly(built):
+    """Without a GPU the product path returns a CUDA error; it never falls
+    back to a CPU computation."""
+    wl = scenes.small_scene()
+    with pytest.raises(_lib.SbrError) as e:
+        api.DeviceScene.from_scene(wl.scene)
+    assert e.value.status in (_lib.ERR_CUDA, _lib.ERR_OOM)

@@ -1,0 +1,97 @@
+"""The oracle (CPU restatement) against golden fixtures produced by the
+reference's own sources (tests/golden/make_golden.py)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from helpers import golden_field, golden_paths, path_keys
+from sbrsolver_gb300 import scenes
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _case(name):
+    if name == "reference_main":
+        return scenes.reference_main_scene()
+    if name == "small_L6_R3":
+        return scenes.small_scene()
+    if name == "small_L4_R3T1_hertzian":
+        wl = scenes.small_scene()
+        wl.request.antenna = 1
+        wl.request.tessellation = 4
+        wl.request.max_transmission = 1
+        return wl
+    if name == "urban_L5_R6T1_rx100":
+        return scenes.urban_scene(level=5, rx_pitch=100.0)
+    if name == "urban_L4_R3T2_rx400":
+        return scenes.urban_scene(level=4, rx_pitch=50.0, max_reflection=3, max_transmission=2)
+    raise KeyError(name)
+
+
+CASES = ["reference_main", "small_L6_R3", "small_L4_R3T1_hertzian", "urban_L5_R6T1_rx100",
+         "urban_L4_R3T2_rx400"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference(built, name):
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    wl = _case(name)
+    sc = orc.OracleScene.from_scene(wl.scene)
+    out = orc.solve(sc, wl.request, wl.scene.materials)
+    assert out["counts"]["segments"] == int(g["segments"])
+    assert out["counts"]["captured"] == int(g["captured"])
+    assert out["counts"]["corrected"] == int(g["corrected"])
+    ref_paths = golden_paths(g)
+    assert path_keys(out["paths"]) == path_keys(ref_paths)
+    for p, q in zip(out["paths"], ref_paths):
+        np.testing.assert_array_equal(p["points"], q["points"])
+    # same host arithmetic; libm may differ in the last bit across machines
+    np.testing.assert_allclose(out["field"], golden_field(g), rtol=1e-12, atol=1e-300)
+
+
+def test_reference_main_pins_shipped_outputs():
+    """The fixture generator checked the reference run against the outputs the
+    reference ships (ElectricField.csv, RayPath.vtk); the oracle reproduces
+    the CSV at its printed precision."""
+    g = np.load(os.path.join(GOLD, "reference_main.npz"))
+    assert bool(g["shipped_field_csv_match"]) and bool(g["shipped_raypath_pairs_match"])
+    wl = scenes.reference_main_scene()
+    out = orc.solve(orc.OracleScene.from_scene(wl.scene), wl.request, wl.scene.materials)
+    f = out["field"]
+    ours = np.stack([f.real, f.imag], -1).reshape(-1, 6)
+    printed = np.vectorize(lambda x: float("%.6g" % x))(ours)
+    np.testing.assert_array_equal(printed, g["shipped_field_csv"])
+    assert len(out["paths"]) == 3133
+
+
+@pytest.mark.parametrize("level", [0, 1, 2, 5])
+def test_icosphere_bit_exact(built, level):
+    ref = np.load(os.path.join(GOLD, f"icosphere_L{level}.npy"))
+    np.testing.assert_array_equal(orc.icosphere(level), ref)
+    assert len(ref) == 10 * 4 ** level + 2
+
+
+def test_scene_inputs_are_reproducible(tmp_path):
+    """Fixture inputs are regenerated from seeds: the STL/material/receiver
+    bytes must hash to what the fixture was made from."""
+    import hashlib
+    for name in CASES[1:]:
+        g = np.load(os.path.join(GOLD, name + ".npz"))
+        d = tmp_path / name
+        scenes.write_oracle_case(_case(name), str(d))
+        h = hashlib.sha256()
+        for f in ("scene.stl", "trimat.txt", "rx.txt"):
+            h.update((d / f).read_bytes())
+        assert h.hexdigest() == str(g["inputs_sha256"]), name
+
+
+def test_fresnel_sweep_pins():
+    """RefCoeffTest reproduces the shipped coeff_test.csv magnitudes exactly;
+    the shipped phases are exactly pi away (older sign convention)."""
+    g = np.load(os.path.join(GOLD, "fresnel_sweep.npz"))
+    ours, shipped = g["reference"], g["shipped"]
+    np.testing.assert_array_equal(ours[:, [0, 1, 3]], shipped[:, [0, 1, 3]])
+    d = np.abs(np.angle(np.exp(1j * (ours[:, [2, 4]] - shipped[:, [2, 4]]))))
+    assert np.all(np.abs(d - np.pi) < 2e-5)
