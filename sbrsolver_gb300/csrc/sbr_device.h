@@ -141,6 +141,7 @@ struct Counters {
   unsigned long long fp64_tri;   // exact triangle tests run
   unsigned long long fallback;   // rays that needed the reference-order traversal
   unsigned long long fp64_capture;
+  unsigned long long used_cls, used_cop, used_grp, used_dd;  // occupied hash slots
   unsigned int overflow;         // bit mask of capacity overflows
   unsigned int pad;
 };

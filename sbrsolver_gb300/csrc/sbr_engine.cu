@@ -108,15 +108,26 @@ __device__ __forceinline__ unsigned long long warp_reserve(unsigned long long* c
   return base + before;
 }
 
+// Open addressing with linear probing.  Tables are kept at most half full
+// (the host grows them between solves from the occupancy counters), so a
+// probe run longer than kMaxProbe means the table is too small: the insert
+// reports overflow and the solve is repeated with a larger table.
+constexpr uint32_t kMaxProbe = 4096;
+
 __device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long key, unsigned* ov,
-                                              unsigned bit) {
+                                              unsigned bit, unsigned long long* used) {
   uint32_t h = uint32_t(mix64(key)) & t.mask;
-  for (uint32_t i = 0; i <= t.mask; ++i) {
+  const uint32_t lim = min(kMaxProbe, t.mask + 1);
+  for (uint32_t i = 0; i < lim; ++i) {
     unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&t.keys[h]);
     if (k == key) return h;
     if (k == kEmptyKey) {
       unsigned long long old = atomicCAS(&t.keys[h], kEmptyKey, key);
-      if (old == kEmptyKey || old == key) return h;
+      if (old == kEmptyKey) {
+        atomicAdd(used, 1ull);
+        return h;
+      }
+      if (old == key) return h;
     }
     h = (h + 1) & t.mask;
   }
@@ -126,7 +137,8 @@ __device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long ke
 
 __device__ __forceinline__ uint32_t ht_find(HashTable t, unsigned long long key) {
   uint32_t h = uint32_t(mix64(key)) & t.mask;
-  for (uint32_t i = 0; i <= t.mask; ++i) {
+  const uint32_t lim = min(kMaxProbe, t.mask + 1);
+  for (uint32_t i = 0; i < lim; ++i) {
     unsigned long long k = t.keys[h];
     if (k == key) return h;
     if (k == kEmptyKey) return 0xFFFFFFFFu;
@@ -420,7 +432,7 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
       c.pad = 0;
       const int cop = A.tri_cop[h.rank];
       const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
-      const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop);
+      const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop);
       unsigned long long slot = base;
       if (do_t) {  // transmitted: same direction, heap 2h
         c.d[0] = r.d[0]; c.d[1] = r.d[1]; c.d[2] = r.d[2];
@@ -428,7 +440,7 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
         c.rc = r.rc;
         c.tc = r.tc + 1;
         const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
-        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass);
+        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls);
         c.cop = cop_cls;
         if (c.cls != 0xFFFFFFFFu) {
           A.cls_info[c.cls] = ClassInfo{r.cls, h.rank, cop_cls, uint8_t(2), uint8_t(A.depth + 1), 0, 0};
@@ -446,7 +458,7 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
         c.rc = r.rc + 1;
         c.tc = r.tc;
         const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1);
-        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass);
+        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls);
         c.cop = cop_cls;
         if (c.cls != 0xFFFFFFFFu) {
           A.cls_info[c.cls] = ClassInfo{r.cls, h.rank, cop_cls, uint8_t(1), uint8_t(A.depth + 1), 0, 0};
@@ -572,7 +584,7 @@ __global__ void __launch_bounds__(128) k_capture(CaptureArgs A) {
               if (sup) continue;
               ++events;
               const unsigned long long key = (unsigned long long)uint32_t(gi) << 32 | n.cls;
-              const uint32_t slot = ht_insert(A.grp, key, &A.ctr->overflow, kOvGroup);
+              const uint32_t slot = ht_insert(A.grp, key, &A.ctr->overflow, kOvGroup, &A.ctr->used_grp);
               if (slot != 0xFFFFFFFFu) {
                 const unsigned long long rank =
                     (unsigned long long)n.launch << kHeapBits | n.heap;
@@ -698,7 +710,7 @@ __global__ void k_correct(CorrectArgs A) {
     corrected += A.grp_count[s];
     const uint32_t cop = cls == kRootClass ? kRootClass : A.cls_info[cls].cop;
     const unsigned long long dk = (unsigned long long)gi << 32 | cop;
-    const uint32_t ds = ht_insert(A.dedup, dk, &A.ctr->overflow, kOvDedup);
+    const uint32_t ds = ht_insert(A.dedup, dk, &A.ctr->overflow, kOvDedup, &A.ctr->used_dd);
     if (ds != 0xFFFFFFFFu) atomicMin(&A.dedup_rank[ds], A.grp_rank[s]);
   }
   if (corrected) atomicAdd(&A.ctr->corrected, corrected);
@@ -889,8 +901,8 @@ struct SceneImpl {
   DBuf<int> path_nray, path_tri, path_cop, path_kind;
   DBuf<Counters> ctr;
   // capacities (grow on overflow)
-  unsigned long long cap_nodes = 1 << 20, cap_queue = 1 << 20, cap_surv = 1 << 16;
-  uint32_t cap_cls = 1 << 20, cap_cop = 1 << 18, cap_grp = 1 << 22, cap_dd = 1 << 20;
+  unsigned long long cap_nodes = 1 << 22, cap_queue = 1 << 21, cap_surv = 1 << 16;
+  uint32_t cap_cls = 1 << 21, cap_cop = 1 << 19, cap_grp = 1 << 24, cap_dd = 1 << 20;
   cudaEvent_t ev[8] = {};
 };
 
@@ -1254,6 +1266,14 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     CK(cudaMemcpyAsync(&c, S.ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (c.overflow & kOvStack) throw std::string("BVH deeper than the traversal stack");
+    // keep every hash table at most half full for the next solve
+    auto grow = [](uint32_t& cap, unsigned long long used) {
+      while (used * 2 > cap && cap < (1u << 30)) cap *= 2;
+    };
+    grow(S.cap_cls, c.used_cls);
+    grow(S.cap_cop, c.used_cop);
+    grow(S.cap_grp, c.used_grp);
+    grow(S.cap_dd, c.used_dd);
     if (c.overflow) {
       if (c.overflow & kOvNodes) S.cap_nodes = std::max(S.cap_nodes * 2, c.nodes + c.nodes / 8);
       if (c.overflow & kOvQueue) {
