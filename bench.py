@@ -160,6 +160,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--level", type=int, default=9,
+                    help="icosahedron level (9 = the benchmark; lower for profiling runs)")
     args = ap.parse_args()
     rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
     dist = None
@@ -181,7 +183,7 @@ def main():
     from sbrsolver_gb300.build import build_library
     build_library()
 
-    wl = scenes.urban_scene()
+    wl = scenes.urban_scene(level=args.level)
     scene = api.DeviceScene.from_scene(wl.scene)
     rx_dev = torch.tensor(wl.request.rx, dtype=torch.float64, device=f"cuda:{local}")
     torch.cuda.synchronize()

@@ -96,6 +96,8 @@ typedef struct sbr_counts {
   long long rays;          /* rays over all surviving paths */
   long long fp64_triangle_tests, fallback_rays, fp64_capture_tests;
   long long launches;
+  long long capture_candidates; /* receivers tested against a reception sphere */
+  long long ancestor_tests;     /* re-tests of ancestors for capture suppression */
 } sbr_counts;
 
 /* One surviving path; its rays are [ray_offset, ray_offset + n_rays) in the

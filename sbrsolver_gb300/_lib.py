@@ -51,7 +51,8 @@ class Request(C.Structure):
 class Counts(C.Structure):
     _fields_ = [(n, C.c_longlong) for n in ("segments", "captured", "corrected", "paths", "rays",
                                              "fp64_triangle_tests", "fallback_rays",
-                                             "fp64_capture_tests", "launches")]
+                                             "fp64_capture_tests", "launches",
+                                             "capture_candidates", "ancestor_tests")]
 
 
 class Path(C.Structure):

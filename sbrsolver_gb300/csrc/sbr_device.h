@@ -142,6 +142,8 @@ struct Counters {
   unsigned long long fallback;   // rays that needed the reference-order traversal
   unsigned long long fp64_capture;
   unsigned long long used_cls, used_cop, used_grp, used_dd;  // occupied hash slots
+  unsigned long long cand;       // receiver candidates tested by the capture stage
+  unsigned long long anc;        // ancestor re-tests for suppression
   unsigned int overflow;         // bit mask of capacity overflows
   unsigned int pad;
 };

@@ -225,7 +225,7 @@ __global__ void k_grid_shape(GridBuild* gb, RxGrid* grids, const TxParams* txp, 
       }
     float cell = 1.0f;
     if (k > 0) {
-      double target = fmax(1.0, txp[r].n_rx / 4.0);
+      double target = fmax(1.0, txp[r].n_rx / 2.0);
       cell = float(pow(vol / target, 1.0 / k));
     }
     if (cell <= 0) cell = 1.0f;
@@ -487,116 +487,197 @@ struct CaptureArgs {
   unsigned long long node_cap;
 };
 
-__device__ __forceinline__ int capture_test(const NodeRec& n, const float3& c32, const double* c64,
-                                            float tanb32, double tanb, unsigned& n64) {
-  const float3 s = make_float3(float(n.s[0]), float(n.s[1]), float(n.s[2]));
-  const float3 u = make_float3(n.u[0], n.u[1], n.u[2]);
-  int v = reception32(s, u, n.len, float(n.S), c32, tanb32);
+// Segment data of a node's ancestor, staged in shared memory once per node.
+struct AncRec {
+  float s[3], u[3], len, S;
+  uint32_t idx, pad;
+};
+
+__device__ __forceinline__ int capture_test_f(const float3& s, const float3& u, float len, float S,
+                                              uint32_t idx, const NodeRec* nodes,
+                                              const float3& c32, const double* c64, float tanb32,
+                                              double tanb, unsigned& n64) {
+  const int v = reception32(s, u, len, S, c32, tanb32);
   if (v >= 0) return v;
   ++n64;
+  const NodeRec& n = nodes[idx];
   return reception64(n.s, n.t, c64, n.S, tanb) ? 1 : 0;
 }
 
-__global__ void __launch_bounds__(128) k_capture(CaptureArgs A) {
+// One warp per tree node.  The receivers that can fall inside the node's
+// reception spheres lie within rb of its segment (rb bounds the sphere radius
+// (S + |P|) tan(beta), with |P| <= (cmax + S tan b) / (1 - tan b) for any
+// capturing point); the segment is clipped to that region, cut into chunks
+// (each receiver is owned by the chunk its projection falls in), and each
+// chunk's capsule is rasterised row by row over the receiver grid, where a
+// row of cells is one contiguous run of receivers for the lanes to stride.
+// A capture counts unless an ancestor of the node captures the same receiver
+// (RTSolver.cpp:277-284); ancestors come from shared memory.
+constexpr int kCapWarps = 4;
+
+__global__ void __launch_bounds__(32 * kCapWarps) k_capture(CaptureArgs A) {
+  __shared__ AncRec anc[kCapWarps][kMaxDepth];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned long long n_nodes = min(A.ctr->nodes, A.node_cap);
-  unsigned long long events = 0;
+  unsigned long long events = 0, cand = 0, anc_tests = 0;
   unsigned n64 = 0;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-       i < n_nodes; i += (unsigned long long)gridDim.x * blockDim.x) {
-    const NodeRec n = A.nodes[i];
-    const TxParams& P = A.txp[n.tx];
-    if (P.n_rx == 0) continue;
-    const RxGrid g = A.grids[n.tx];
-    const float tanb = float(P.tan_beta);
-    const float S = float(n.S);
-    // Upper bound of any capture radius on this segment: |P| is bounded by
-    // (cmax + S tan b) / (1 - tan b) for any point that can capture.
-    const float cmax = A.gb[n.tx].cmax;
-    const float pmax = (cmax + S * tanb) / fmaxf(1e-6f, 1.0f - tanb) * 1.0001f + 1.0f;
-    const float3 s = make_float3(float(n.s[0]), float(n.s[1]), float(n.s[2]));
-    const float3 u = make_float3(n.u[0], n.u[1], n.u[2]);
-    // parameter range with |s + l u| <= pmax
-    const float su = s.x * u.x + s.y * u.y + s.z * u.z;
-    const float ss = s.x * s.x + s.y * s.y + s.z * s.z;
-    const float disc = su * su - (ss - pmax * pmax);
-    if (disc < 0.0f) continue;
-    const float sq = sqrtf(disc);
-    float lo = fmaxf(0.0f, -su - sq), hi = fminf(n.len, -su + sq);
-    const float rb = (S + pmax) * tanb * 1.0001f + 1e-3f;
-    // clip to the receiver box grown by rb
-    for (int a = 0; a < 3 && lo <= hi; ++a) {
-      const float sa = a == 0 ? s.x : (a == 1 ? s.y : s.z);
-      const float ua = a == 0 ? u.x : (a == 1 ? u.y : u.z);
-      const float bl = g.bmin[a] - rb, bh = g.bmax[a] + rb;
-      if (fabsf(ua) < 1e-20f) {
-        if (sa < bl || sa > bh) hi = -1.0f;
-      } else {
-        float t1 = (bl - sa) / ua, t2 = (bh - sa) / ua;
-        lo = fmaxf(lo, fminf(t1, t2) - 1e-3f);
-        hi = fminf(hi, fmaxf(t1, t2) + 1e-3f);
+  const unsigned long long nw = (unsigned long long)gridDim.x * kCapWarps;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * kCapWarps + warp; i < n_nodes;
+       i += nw) {
+    const NodeRec& nref = A.nodes[i];
+    const uint32_t ntx = nref.tx;
+    const TxParams& P = A.txp[ntx];
+    const RxGrid& g = A.grids[ntx];
+    const float3 s = make_float3(float(nref.s[0]), float(nref.s[1]), float(nref.s[2]));
+    const float3 u = make_float3(nref.u[0], nref.u[1], nref.u[2]);
+    const float len = nref.len;
+    const float S = float(nref.S);
+    const uint32_t cls = nref.cls, launch = nref.launch, heap = nref.heap;
+    // stage the ancestor chain
+    int na = 0;
+    if (lane == 0) {
+      for (uint32_t p = nref.parent; p != 0xFFFFFFFFu && p < A.node_cap && na < kMaxDepth;) {
+        const NodeRec& a = A.nodes[p];
+        AncRec& r = anc[warp][na++];
+        r.s[0] = float(a.s[0]); r.s[1] = float(a.s[1]); r.s[2] = float(a.s[2]);
+        r.u[0] = a.u[0]; r.u[1] = a.u[1]; r.u[2] = a.u[2];
+        r.len = a.len;
+        r.S = float(a.S);
+        r.idx = p;
+        p = a.parent;
       }
     }
-    if (lo > hi) continue;
-    const float lc = fmaxf(g.cell, 2.0f * rb);
-    int nchunk = int(ceilf((hi - lo) / lc));
-    if (nchunk < 1) nchunk = 1;
-    if (nchunk > 4096) nchunk = 4096;
-    const float step = (hi - lo) / nchunk;
-    const float pad = rb + g.cell * 0.01f + 1e-3f;
-    for (int ch = 0; ch < nchunk; ++ch) {
-      const float a = lo + ch * step, b = (ch == nchunk - 1) ? hi : lo + (ch + 1) * step;
-      float bl[3], bh[3];
-      const float pa[3] = {s.x + a * u.x, s.y + a * u.y, s.z + a * u.z};
-      const float pb[3] = {s.x + b * u.x, s.y + b * u.y, s.z + b * u.z};
-      int c0[3], c1[3];
-      for (int k = 0; k < 3; ++k) {
-        bl[k] = fminf(pa[k], pb[k]) - pad;
-        bh[k] = fmaxf(pa[k], pb[k]) + pad;
-        c0[k] = max(0, int(floorf((bl[k] - g.org[k]) / g.cell)));
-        c1[k] = min(g.dim[k] - 1, int(floorf((bh[k] - g.org[k]) / g.cell)));
+    na = __shfl_sync(0xffffffffu, na, 0);
+    __syncwarp();
+    if (P.n_rx > 0) {
+      const float tanb = float(P.tan_beta);
+      const float cmax = A.gb[ntx].cmax;
+      const float pmax = (cmax + S * tanb) / fmaxf(1e-6f, 1.0f - tanb) * 1.0001f + 1.0f;
+      const float su = s.x * u.x + s.y * u.y + s.z * u.z;
+      const float ss = s.x * s.x + s.y * s.y + s.z * s.z;
+      const float disc = su * su - (ss - pmax * pmax);
+      float lo = 0.0f, hi = -1.0f;
+      if (disc >= 0.0f) {
+        const float sq = sqrtf(disc);
+        lo = fmaxf(0.0f, -su - sq);
+        hi = fminf(len, -su + sq);
       }
-      for (int iz = c0[2]; iz <= c1[2]; ++iz)
-        for (int iy = c0[1]; iy <= c1[1]; ++iy)
-          for (int ix = c0[0]; ix <= c1[0]; ++ix) {
-            const int cid = (iz * g.dim[1] + iy) * g.dim[0] + ix;
-            const int e = g.cell_start[cid + 1];
-            for (int j = g.cell_start[cid]; j < e; ++j) {
-              const float4 c4 = g.rx32[j];
-              const float3 c = make_float3(c4.x, c4.y, c4.z);
-              const float lam = u.x * (c.x - s.x) + u.y * (c.y - s.y) + u.z * (c.z - s.z);
-              // each receiver is owned by exactly one chunk
-              if (ch > 0 && lam < a) continue;
-              if (ch < nchunk - 1 && lam >= b) continue;
-              const int gi = __float_as_int(c4.w);
-              const double* c64 = A.rx + 3 * size_t(gi);
-              if (!capture_test(n, c, c64, tanb, P.tan_beta, n64)) continue;
-              // suppressed if an ancestor captured the same receiver
-              bool sup = false;
-              for (uint32_t p = n.parent; p != 0xFFFFFFFFu;) {
-                if (p >= A.node_cap) break;  // node pool overflowed: this pass is redone
-                const NodeRec an = A.nodes[p];
-                if (capture_test(an, c, c64, tanb, P.tan_beta, n64)) {
-                  sup = true;
-                  break;
-                }
-                p = an.parent;
+      const float rbg = (S + pmax) * tanb * 1.0001f + 1e-3f;  // bound over the whole segment
+      for (int a = 0; a < 3 && lo <= hi; ++a) {
+        const float sa = a == 0 ? s.x : (a == 1 ? s.y : s.z);
+        const float ua = a == 0 ? u.x : (a == 1 ? u.y : u.z);
+        const float bl = g.bmin[a] - rbg, bh = g.bmax[a] + rbg;
+        if (fabsf(ua) < 1e-20f) {
+          if (sa < bl || sa > bh) hi = -1.0f;
+        } else {
+          const float t1 = (bl - sa) / ua, t2 = (bh - sa) / ua;
+          lo = fmaxf(lo, fminf(t1, t2) - 1e-3f);
+          hi = fminf(hi, fmaxf(t1, t2) + 1e-3f);
+        }
+      }
+      if (lo <= hi) {
+        // chunk length: a few cells, or the local sphere radius if larger
+        const float r0 = (S + sqrtf(fmaxf(0.0f, ss + 2.0f * lo * su + lo * lo))) * tanb;
+        const float lc = fmaxf(4.0f * g.cell, r0);
+        int nchunk = int(ceilf((hi - lo) / lc));
+        nchunk = max(1, min(nchunk, 4096));
+        const float step = (hi - lo) / nchunk;
+        for (int ch = 0; ch < nchunk; ++ch) {
+          const float a = lo + ch * step, b = (ch == nchunk - 1) ? hi : lo + (ch + 1) * step;
+          const float pa[3] = {s.x + a * u.x, s.y + a * u.y, s.z + a * u.z};
+          const float pb[3] = {s.x + b * u.x, s.y + b * u.y, s.z + b * u.z};
+          const float npa = sqrtf(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]);
+          const float npb = sqrtf(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]);
+          // |P| is convex along the chunk: the larger end bounds it
+          const float rb = (S + fmaxf(npa, npb)) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f +
+                           kFiltK * (fmaxf(npa, npb) + S + 1.0f);
+          int c0[3], c1[3];
+          for (int k = 0; k < 3; ++k) {
+            c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - rb - g.org[k]) / g.cell)));
+            c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + rb - g.org[k]) / g.cell)));
+          }
+          for (int iz = c0[2]; iz <= c1[2]; ++iz) {
+            const float z0 = g.org[2] + iz * g.cell - rb, z1 = g.org[2] + (iz + 1) * g.cell + rb;
+            for (int iy = c0[1]; iy <= c1[1]; ++iy) {
+              const float y0 = g.org[1] + iy * g.cell - rb, y1 = g.org[1] + (iy + 1) * g.cell + rb;
+              // part of the chunk whose y and z are within rb of this row
+              float la = a, lb = b;
+              if (fabsf(u.y) > 1e-20f) {
+                const float t1 = (y0 - s.y) / u.y, t2 = (y1 - s.y) / u.y;
+                la = fmaxf(la, fminf(t1, t2));
+                lb = fminf(lb, fmaxf(t1, t2));
+              } else if (s.y < y0 || s.y > y1) {
+                continue;
               }
-              if (sup) continue;
-              ++events;
-              const unsigned long long key = (unsigned long long)uint32_t(gi) << 32 | n.cls;
-              const uint32_t slot = ht_insert(A.grp, key, &A.ctr->overflow, kOvGroup, &A.ctr->used_grp);
-              if (slot != 0xFFFFFFFFu) {
-                const unsigned long long rank =
-                    (unsigned long long)n.launch << kHeapBits | n.heap;
-                atomicMin(&A.grp_rank[slot], rank);
-                atomicAdd(&A.grp_count[slot], 1u);
+              if (fabsf(u.z) > 1e-20f) {
+                const float t1 = (z0 - s.z) / u.z, t2 = (z1 - s.z) / u.z;
+                la = fmaxf(la, fminf(t1, t2));
+                lb = fminf(lb, fmaxf(t1, t2));
+              } else if (s.z < z0 || s.z > z1) {
+                continue;
+              }
+              if (la > lb) continue;
+              const float xa = s.x + la * u.x, xb = s.x + lb * u.x;
+              const int x0 = max(c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) / g.cell)));
+              const int x1 = min(c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) / g.cell)));
+              if (x0 > x1) continue;
+              const int row = (iz * g.dim[1] + iy) * g.dim[0];
+              const int beg = g.cell_start[row + x0], end = g.cell_start[row + x1 + 1];
+              for (int j = beg + lane; j < end; j += 32) {
+                const float4 c4 = g.rx32[j];
+                const float3 c = make_float3(c4.x, c4.y, c4.z);
+                const float lam = u.x * (c.x - s.x) + u.y * (c.y - s.y) + u.z * (c.z - s.z);
+                if (ch > 0 && lam < a) continue;              // owned by an earlier chunk
+                if (ch < nchunk - 1 && lam >= b) continue;    // owned by a later chunk
+                const int gi = __float_as_int(c4.w);
+                const double* c64 = A.rx + 3 * size_t(gi);
+                ++cand;
+                if (!capture_test_f(s, u, len, S, uint32_t(i), A.nodes, c, c64, tanb,
+                                    P.tan_beta, n64))
+                  continue;
+                bool sup = false;
+                for (int q = 0; q < na; ++q) {
+                  const AncRec& r = anc[warp][q];
+                  ++anc_tests;
+                  if (capture_test_f(make_float3(r.s[0], r.s[1], r.s[2]),
+                                     make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, r.idx,
+                                     A.nodes, c, c64, tanb, P.tan_beta, n64)) {
+                    sup = true;
+                    break;
+                  }
+                }
+                if (sup) continue;
+                ++events;
+                const unsigned long long key = (unsigned long long)uint32_t(gi) << 32 | cls;
+                const uint32_t slot =
+                    ht_insert(A.grp, key, &A.ctr->overflow, kOvGroup, &A.ctr->used_grp);
+                if (slot != 0xFFFFFFFFu) {
+                  const unsigned long long rank = (unsigned long long)launch << kHeapBits | heap;
+                  // the stored minimum only decreases: skip the atomic when it cannot lower it
+                  if (*reinterpret_cast<volatile unsigned long long*>(&A.grp_rank[slot]) > rank)
+                    atomicMin(&A.grp_rank[slot], rank);
+                  if (A.grp_count) atomicAdd(&A.grp_count[slot], 1u);
+                }
               }
             }
           }
+        }
+      }
     }
+    __syncwarp();
   }
-  if (events) atomicAdd(&A.ctr->events, events);
-  if (n64) atomicAdd(&A.ctr->fp64_capture, (unsigned long long)n64);
+  for (int o = 16; o; o >>= 1) {
+    events += __shfl_xor_sync(0xffffffffu, events, o);
+    cand += __shfl_xor_sync(0xffffffffu, cand, o);
+    anc_tests += __shfl_xor_sync(0xffffffffu, anc_tests, o);
+    n64 += __shfl_xor_sync(0xffffffffu, n64, o);
+  }
+  if (lane == 0) {
+    if (events) atomicAdd(&A.ctr->events, events);
+    if (cand) atomicAdd(&A.ctr->cand, cand);
+    if (anc_tests) atomicAdd(&A.ctr->anc, anc_tests);
+    if (n64) atomicAdd(&A.ctr->fp64_capture, (unsigned long long)n64);
+  }
 }
 
 // ---- correction / dedup -----------------------------------------------------
@@ -1137,7 +1218,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
   }
   CK(cudaEventRecord(S.ev[1], st));
   // ---- receiver grid
-  const int max_cells = 1 << 20;
+  const int max_cells = 1 << 21;
   S.gb.ensure(n_req);
   {
     std::vector<GridBuild> g0(n_req);
@@ -1237,7 +1318,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     ca.grp_count = S.grp_count.p;
     ca.ctr = S.ctr.p;
     ca.node_cap = S.cap_nodes;
-    k_capture<<<152 * 16, 128, 0, st>>>(ca);
+    k_capture<<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
     CK(cudaGetLastError());
     CK(cudaEventRecord(S.ev[4], st));
     // ---- correct, dedup, select
@@ -1397,6 +1478,8 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     out.counts.fallback_rays = (long long)c.fallback;
     out.counts.fp64_capture_tests = (long long)c.fp64_capture;
     out.counts.launches = launches;
+    out.counts.capture_candidates = (long long)c.cand;
+    out.counts.ancestor_tests = (long long)c.anc;
     float ms[8] = {};
     for (int i = 1; i < 8; ++i) CK(cudaEventElapsedTime(&ms[i], S.ev[i - 1], S.ev[i]));
     out.timing.h2d_ms = ms[1];
