@@ -86,11 +86,14 @@ typedef struct sbr_request {
   int n_rx;
   const double* rx;        /* 3 doubles per receiver */
   int rx_on_device;        /* rx is a device pointer (already resident) */
+  int stage_counts;        /* also count captures before correction (sbr_counts.captured);
+                              costs time, results are identical either way */
 } sbr_request;
 
 typedef struct sbr_counts {
   long long segments;      /* executed ray segments = closest-hit queries (rays x bounces) */
-  long long captured;      /* receiver captures before image correction */
+  long long captured;      /* receiver captures before image correction (-1 unless
+                              the request set stage_counts) */
   long long corrected;     /* captures whose image correction succeeded */
   long long paths;         /* surviving paths after duplicate removal */
   long long rays;          /* rays over all surviving paths */
@@ -98,6 +101,9 @@ typedef struct sbr_counts {
   long long launches;
   long long capture_candidates; /* receivers tested against a reception sphere */
   long long ancestor_tests;     /* re-tests of ancestors for capture suppression */
+  long long classes;            /* distinct (facet, interaction) prefixes traced */
+  long long groups;             /* unused, -1 */
+  long long keys;               /* distinct (receiver, coplanar key) after correction */
 } sbr_counts;
 
 /* One surviving path; its rays are [ray_offset, ray_offset + n_rays) in the

@@ -45,14 +45,16 @@ class Request(C.Structure):
                 ("max_reflection", C.c_int), ("max_transmission", C.c_int),
                 ("frequency", C.c_double), ("pt", C.c_double), ("use_fresnel", C.c_int),
                 ("tessellation", C.c_int), ("antenna", C.c_int), ("field_precision", C.c_int),
-                ("n_rx", C.c_int), ("rx", C.POINTER(C.c_double)), ("rx_on_device", C.c_int)]
+                ("n_rx", C.c_int), ("rx", C.POINTER(C.c_double)), ("rx_on_device", C.c_int),
+                ("stage_counts", C.c_int)]
 
 
 class Counts(C.Structure):
     _fields_ = [(n, C.c_longlong) for n in ("segments", "captured", "corrected", "paths", "rays",
                                              "fp64_triangle_tests", "fallback_rays",
                                              "fp64_capture_tests", "launches",
-                                             "capture_candidates", "ancestor_tests")]
+                                             "capture_candidates", "ancestor_tests",
+                                             "classes", "groups", "keys")]
 
 
 class Path(C.Structure):

@@ -203,7 +203,7 @@ class Result:
 
 def make_request(tx, tx_coord_sys, max_reflection, max_transmission, frequency, pt, use_fresnel,
                  rx: np.ndarray, tessellation: int, antenna: int = 1,
-                 precision: str = "fp64") -> tuple:
+                 precision: str = "fp64", stage_counts: bool = False) -> tuple:
     rx = np.ascontiguousarray(rx, np.float64).reshape(-1, 3)
     q = _lib.Request()
     for i in range(3):
@@ -222,13 +222,15 @@ def make_request(tx, tx_coord_sys, max_reflection, max_transmission, frequency, 
     q.n_rx = int(rx.shape[0])
     q.rx = rx.ctypes.data_as(C.POINTER(C.c_double))
     q.rx_on_device = 0
+    q.stage_counts = 1 if stage_counts else 0
     return q, rx  # keep rx alive with the request
 
 
-def request_from_workload(req: WorkRequest, precision: str = "fp64") -> tuple:
+def request_from_workload(req: WorkRequest, precision: str = "fp64",
+                          stage_counts: bool = False) -> tuple:
     return make_request(req.tx, req.tx_coord_sys, req.max_reflection, req.max_transmission,
                         req.frequency, req.pt, req.use_fresnel, req.rx, req.tessellation,
-                        req.antenna, precision)
+                        req.antenna, precision, stage_counts)
 
 
 def solve(scene: DeviceScene, requests, with_paths: bool = True) -> Result:

@@ -19,7 +19,12 @@
 
 namespace sbr {
 
-constexpr uint32_t kRootClass = 0xFFFFFFFFu;  // class id of the empty path prefix
+constexpr uint32_t kRootClass = 0xFFFFFFFFu;  // coplanar class of the empty path prefix
+// Path classes (interned facet/interaction prefixes) of different requests
+// must not merge because each class carries its request's image source:
+// the empty prefix of request q is class kRootBase + q.
+constexpr uint32_t kRootBase = 0xFFFF0000u;
+__host__ __device__ __forceinline__ bool is_root_class(uint32_t c) { return c >= kRootBase; }
 constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kHeapBits = 17;                  // rank = launch << 17 | BFS heap index
 constexpr int kMaxDepth = 16;                  // max interactions per path (R + T)
@@ -68,6 +73,8 @@ struct DevScene {
   const Tri32* tri32;
   const Tri64* tri64;
   const CorrTri* corr;
+  const Tri32* corr32;     // FP32 filter copy of corr
+  const int* rank_to_id;   // triangle id of each depth-first rank
   const Material* mats;
   int n_tri, n_nodes, n_mats;
   int root_leaf;
@@ -125,11 +132,25 @@ struct HashTable {
   uint32_t mask;
 };
 
-struct ClassInfo {
+// One path class: the path's last ray starts on `tri` (depth-first rank),
+// reached by interaction `kind` (1 reflect, 2 transmit) from class `parent`.
+// img is the image source of that ray (GetImageSources, RTSolver.cpp:396-433,
+// FP64 in the reference's order), img32 its FP32 copy.
+struct __align__(16) ClassInfo {
+  double img[3];
+  float img32[3];
   uint32_t parent;
   int tri;
   uint32_t cop;
   uint8_t kind, depth, pad0, pad1;
+  uint32_t pad2;
+};
+
+// A capture whose image correction succeeded (one reference path before
+// duplicate removal).
+struct Corrected {
+  uint32_t rx, cls;
+  unsigned long long rank;
 };
 
 struct Counters {
@@ -141,7 +162,7 @@ struct Counters {
   unsigned long long fp64_tri;   // exact triangle tests run
   unsigned long long fallback;   // rays that needed the reference-order traversal
   unsigned long long fp64_capture;
-  unsigned long long used_cls, used_cop, used_grp, used_dd;  // occupied hash slots
+  unsigned long long used_cls, used_cop, used_dd;  // occupied hash slots
   unsigned long long cand;       // receiver candidates tested by the capture stage
   unsigned long long anc;        // ancestor re-tests for suppression
   unsigned int overflow;         // bit mask of capacity overflows
@@ -149,7 +170,7 @@ struct Counters {
 };
 
 enum OverflowBits : unsigned {
-  kOvNodes = 1, kOvQueue = 2, kOvClass = 4, kOvCop = 8, kOvGroup = 16, kOvDedup = 32,
+  kOvNodes = 1, kOvQueue = 2, kOvClass = 4, kOvCop = 8, kOvCorr = 16, kOvDedup = 32,
   kOvSurv = 64, kOvStack = 128
 };
 

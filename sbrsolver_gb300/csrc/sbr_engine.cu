@@ -353,6 +353,25 @@ __device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long 
   return lo;
 }
 
+// Every thread that interns a class writes the same values (they depend
+// only on the key), so concurrent writers agree.
+__device__ __forceinline__ void write_class(ClassInfo& ci, const double* img, uint32_t parent,
+                                            int tri, uint32_t cop, int kind, int depth) {
+  ci.img[0] = img[0];
+  ci.img[1] = img[1];
+  ci.img[2] = img[2];
+  ci.img32[0] = float(img[0]);
+  ci.img32[1] = float(img[1]);
+  ci.img32[2] = float(img[2]);
+  ci.parent = parent;
+  ci.tri = tri;
+  ci.cop = cop;
+  ci.kind = uint8_t(kind);
+  ci.depth = uint8_t(depth);
+  ci.pad0 = ci.pad1 = 0;
+  ci.pad2 = 0;
+}
+
 __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
   const long long n_in =
       A.depth == 0 ? A.n_root
@@ -371,7 +390,7 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
       r.total = 0.0;
       r.S = 0.0;
       r.parent = 0xFFFFFFFFu;
-      r.cls = kRootClass;
+      r.cls = kRootBase + uint32_t(q);
       r.cop = kRootClass;
       r.launch = uint32_t(li);
       r.heap = 1;
@@ -433,8 +452,10 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
       const int cop = A.tri_cop[h.rank];
       const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
       const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop);
+      // image source of the parent ray's class (the transmitter for a launch)
+      const double* pimg = is_root_class(r.cls) ? P.tx : A.cls_info[r.cls].img;
       unsigned long long slot = base;
-      if (do_t) {  // transmitted: same direction, heap 2h
+      if (do_t) {  // transmitted: same direction, heap 2h, same image source
         c.d[0] = r.d[0]; c.d[1] = r.d[1]; c.d[2] = r.d[2];
         c.heap = r.heap * 2;
         c.rc = r.rc;
@@ -442,9 +463,7 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
         const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
         c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls);
         c.cop = cop_cls;
-        if (c.cls != 0xFFFFFFFFu) {
-          A.cls_info[c.cls] = ClassInfo{r.cls, h.rank, cop_cls, uint8_t(2), uint8_t(A.depth + 1), 0, 0};
-        }
+        if (c.cls != 0xFFFFFFFFu) write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
         if (slot < A.out_cap) A.out[slot] = c;
         else atomicOr(&A.ctr->overflow, kOvQueue);
         ++slot;
@@ -461,7 +480,14 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
         c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls);
         c.cop = cop_cls;
         if (c.cls != 0xFFFFFFFFu) {
-          A.cls_info[c.cls] = ClassInfo{r.cls, h.rank, cop_cls, uint8_t(1), uint8_t(A.depth + 1), 0, 0};
+          // ImagePoint (RTSolver.cpp:910-924) across the triangle the
+          // reference finds at this id's position of its mesh vector
+          const CorrTri& M = A.sc.corr[A.sc.rank_to_id[h.rank]];
+          double w[3], img[3];
+          x64::sub3(pimg, M.v1, w);
+          const double dist = x64::dot(M.n, w);
+          for (int a = 0; a < 3; ++a) img[a] = x64::sub(pimg[a], x64::mul(x64::mul(2.0, dist), M.n[a]));
+          write_class(A.cls_info[c.cls], img, r.cls, h.rank, cop_cls, 1, A.depth + 1);
         }
         if (slot < A.out_cap) A.out[slot] = c;
         else atomicOr(&A.ctr->overflow, kOvQueue);
@@ -475,16 +501,19 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
 // ---- capture ----------------------------------------------------------------
 
 struct CaptureArgs {
+  DevScene sc;
   const NodeRec* nodes;
   const TxParams* txp;
   const RxGrid* grids;
   const GridBuild* gb;
   const double* rx;
-  HashTable grp;
-  unsigned long long* grp_rank;
-  unsigned* grp_count;
+  const ClassInfo* cls_info;
+  const unsigned char* direct_ok;
+  Corrected* corr_list;
+  unsigned long long corr_cap;
   Counters* ctr;
   unsigned long long node_cap;
+  int stage_counts;
 };
 
 // Segment data of a node's ancestor, staged in shared memory once per node.
@@ -502,6 +531,39 @@ __device__ __forceinline__ int capture_test_f(const float3& s, const float3& u, 
   ++n64;
   const NodeRec& n = nodes[idx];
   return reception64(n.s, n.t, c64, n.S, tanb) ? 1 : 0;
+}
+
+// MultiPathCorrection (RTSolver.cpp:330-373) for one capture, walking the
+// path class from the receiver back to the transmitter: the line from each
+// ray's image source to its current target must cross the triangle at that
+// id's mesh position.  FP32 filter first (nearly every correction fails at
+// its first test); the FP64 test in the reference's order decides the rest
+// and yields the exact intersection that becomes the next target.
+__device__ __forceinline__ bool correct_event(const DevScene& sc, const ClassInfo* info,
+                                             uint32_t cls, const float3& c32, const double* c64,
+                                             unsigned& n64) {
+  double tgt[3] = {c64[0], c64[1], c64[2]};
+  float3 t32 = c32;
+  for (uint32_t c = cls; !is_root_class(c);) {
+    const ClassInfo& ci = info[c];
+    const int mpos = sc.rank_to_id[ci.tri];
+    const float3 o = make_float3(ci.img32[0], ci.img32[1], ci.img32[2]);
+    const float3 d = make_float3(t32.x - o.x, t32.y - o.y, t32.z - o.z);
+    const float no = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
+    const float nd = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+    float tlo;
+    if (!tri_filter(sc.corr32[mpos], o, d, no, nd, tlo)) return false;
+    ++n64;
+    double dd[3], P3[3];
+    x64::sub3(tgt, ci.img, dd);
+    if (!mt64c(sc.corr[mpos], ci.img, dd, P3)) return false;
+    tgt[0] = P3[0];
+    tgt[1] = P3[1];
+    tgt[2] = P3[2];
+    t32 = make_float3(float(P3[0]), float(P3[1]), float(P3[2]));
+    c = ci.parent;
+  }
+  return true;
 }
 
 // One warp per tree node.  The receivers that can fall inside the node's
@@ -635,29 +697,34 @@ __global__ void __launch_bounds__(32 * kCapWarps) k_capture(CaptureArgs A) {
                 if (!capture_test_f(s, u, len, S, uint32_t(i), A.nodes, c, c64, tanb,
                                     P.tan_beta, n64))
                   continue;
-                bool sup = false;
-                for (int q = 0; q < na; ++q) {
-                  const AncRec& r = anc[warp][q];
-                  ++anc_tests;
-                  if (capture_test_f(make_float3(r.s[0], r.s[1], r.s[2]),
-                                     make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, r.idx,
-                                     A.nodes, c, c64, tanb, P.tan_beta, n64)) {
-                    sup = true;
-                    break;
+                // RayCapture deletes a captured node's subtree, so an ancestor
+                // capturing the same receiver suppresses this one.
+                auto suppressed = [&]() {
+                  for (int q = 0; q < na; ++q) {
+                    const AncRec& r = anc[warp][q];
+                    ++anc_tests;
+                    if (capture_test_f(make_float3(r.s[0], r.s[1], r.s[2]),
+                                       make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, r.idx,
+                                       A.nodes, c, c64, tanb, P.tan_beta, n64))
+                      return true;
                   }
+                  return false;
+                };
+                if (A.stage_counts) {
+                  if (suppressed()) continue;
+                  ++events;
                 }
-                if (sup) continue;
-                ++events;
-                const unsigned long long key = (unsigned long long)uint32_t(gi) << 32 | cls;
-                const uint32_t slot =
-                    ht_insert(A.grp, key, &A.ctr->overflow, kOvGroup, &A.ctr->used_grp);
-                if (slot != 0xFFFFFFFFu) {
-                  const unsigned long long rank = (unsigned long long)launch << kHeapBits | heap;
-                  // the stored minimum only decreases: skip the atomic when it cannot lower it
-                  if (*reinterpret_cast<volatile unsigned long long*>(&A.grp_rank[slot]) > rank)
-                    atomicMin(&A.grp_rank[slot], rank);
-                  if (A.grp_count) atomicAdd(&A.grp_count[slot], 1u);
-                }
+                const bool ok = is_root_class(cls)
+                                    ? A.direct_ok[gi] != 0
+                                    : correct_event(A.sc, A.cls_info, cls, c, c64, n64);
+                if (!ok) continue;
+                if (!A.stage_counts && suppressed()) continue;
+                const unsigned long long k = atomicAdd(&A.ctr->corrected, 1ull);
+                if (k < A.corr_cap)
+                  A.corr_list[k] =
+                      Corrected{uint32_t(gi), cls, (unsigned long long)launch << kHeapBits | heap};
+                else
+                  atomicOr(&A.ctr->overflow, kOvCorr);
               }
             }
           }
@@ -694,7 +761,7 @@ struct PathBuf {
 __device__ __forceinline__ bool class_path(const ClassInfo* info, uint32_t cls, PathBuf& pb) {
   int depth = 0;
   int tri_rev[kMaxDepth], kind_rev[kMaxDepth];
-  for (uint32_t c = cls; c != kRootClass; c = info[c].parent) {
+  for (uint32_t c = cls; !is_root_class(c); c = info[c].parent) {
     if (depth >= kMaxDepth) return false;
     tri_rev[depth] = info[c].tri;
     kind_rev[depth] = info[c].kind;
@@ -709,23 +776,6 @@ __device__ __forceinline__ bool class_path(const ClassInfo* info, uint32_t cls, 
   pb.tri[depth] = -1;
   return true;
 }
-
-struct CorrectArgs {
-  DevScene sc;
-  const TxParams* txp;
-  int n_tx;
-  const double* rx;
-  const int* rx_req;      // request of each receiver
-  HashTable grp;
-  const unsigned long long* grp_rank;
-  const unsigned* grp_count;
-  unsigned char* grp_ok;
-  const ClassInfo* cls_info;
-  HashTable dedup;
-  unsigned long long* dedup_rank;
-  const int* rank_to_id;  // triangle id of each rank
-  Counters* ctr;
-};
 
 // GetImageSources + MultiPathCorrection / DirectPathCorrection
 // (RTSolver.cpp:330-433).  Fills pb.pts with the corrected points.
@@ -775,47 +825,56 @@ __device__ bool correct_path(const DevScene& sc, const int* rank_to_id, const Tx
   return true;
 }
 
-__global__ void k_correct(CorrectArgs A) {
-  unsigned long long corrected = 0;
-  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= A.grp.mask;
-       s += gridDim.x * blockDim.x) {
-    const unsigned long long key = A.grp.keys[s];
-    if (key == kEmptyKey) continue;
-    const uint32_t gi = uint32_t(key >> 32), cls = uint32_t(key);
-    const TxParams& P = A.txp[A.rx_req[gi]];
-    PathBuf pb;
-    bool ok = class_path(A.cls_info, cls, pb) &&
-              correct_path(A.sc, A.rank_to_id, P, A.rx + 3 * size_t(gi), pb, &A.ctr->overflow);
-    A.grp_ok[s] = ok ? 1 : 0;
-    if (!ok) continue;
-    corrected += A.grp_count[s];
-    const uint32_t cop = cls == kRootClass ? kRootClass : A.cls_info[cls].cop;
-    const unsigned long long dk = (unsigned long long)gi << 32 | cop;
-    const uint32_t ds = ht_insert(A.dedup, dk, &A.ctr->overflow, kOvDedup, &A.ctr->used_dd);
-    if (ds != 0xFFFFFFFFu) atomicMin(&A.dedup_rank[ds], A.grp_rank[s]);
+// DirectPathCorrection (RTSolver.cpp:375-394) once per receiver: the direct
+// path survives iff the reference-order BVH query from the transmitter along
+// (rx - tx) finds nothing closer than the receiver.
+__global__ void k_direct(DevScene sc, const TxParams* txp, const double* rx, const int* rx_req,
+                         int n_rx, unsigned char* ok, Counters* ctr) {
+  for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < n_rx; gi += gridDim.x * blockDim.x) {
+    const double* tx = txp[rx_req[gi]].tx;
+    const double* c = rx + 3 * size_t(gi);
+    double d[3];
+    x64::sub3(c, tx, d);
+    Hit h;
+    const bool has = exact_closest(sc, tx, d, h, &ctr->overflow);
+    ok[gi] = (!has || x64::norm(d) < h.dist) ? 1 : 0;
   }
-  if (corrected) atomicAdd(&A.ctr->corrected, corrected);
+}
+
+// RemoveDuplicatePath (RTSolver.cpp:435-459): the first corrected path in
+// (launch, BFS) order wins each (receiver, coplanar key).
+__device__ __forceinline__ unsigned long long dedup_key(const ClassInfo* info, const Corrected& e) {
+  const uint32_t cop = is_root_class(e.cls) ? kRootClass : info[e.cls].cop;
+  return (unsigned long long)e.rx << 32 | cop;
+}
+
+__global__ void k_dedup(const Corrected* list, unsigned long long cap, const ClassInfo* info,
+                        HashTable dedup, unsigned long long* dedup_rank, Counters* ctr) {
+  const unsigned long long n = min(ctr->corrected, cap);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const Corrected e = list[i];
+    const uint32_t ds = ht_insert(dedup, dedup_key(info, e), &ctr->overflow, kOvDedup, &ctr->used_dd);
+    if (ds != 0xFFFFFFFFu) atomicMin(&dedup_rank[ds], e.rank);
+  }
 }
 
 struct Survivor {
-  uint32_t slot, rx;
+  uint32_t cls, rx;
   unsigned long long rank;
 };
 
-__global__ void k_select(HashTable grp, const unsigned long long* grp_rank,
-                         const unsigned char* grp_ok, const ClassInfo* cls_info, HashTable dedup,
-                         const unsigned long long* dedup_rank, Survivor* surv,
-                         unsigned long long cap, Counters* ctr) {
-  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= grp.mask;
-       s += gridDim.x * blockDim.x) {
-    const unsigned long long key = grp.keys[s];
-    if (key == kEmptyKey || !grp_ok[s]) continue;
-    const uint32_t gi = uint32_t(key >> 32), cls = uint32_t(key);
-    const uint32_t cop = cls == kRootClass ? kRootClass : cls_info[cls].cop;
-    const uint32_t ds = ht_find(dedup, (unsigned long long)gi << 32 | cop);
-    if (ds == 0xFFFFFFFFu || dedup_rank[ds] != grp_rank[s]) continue;
-    const unsigned long long i = atomicAdd(&ctr->survivors, 1ull);
-    if (i < cap) surv[i] = Survivor{s, gi, grp_rank[s]};
+__global__ void k_select(const Corrected* list, unsigned long long cap, const ClassInfo* info,
+                         HashTable dedup, const unsigned long long* dedup_rank, Survivor* surv,
+                         unsigned long long surv_cap, Counters* ctr) {
+  const unsigned long long n = min(ctr->corrected, cap);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const Corrected e = list[i];
+    const uint32_t ds = ht_find(dedup, dedup_key(info, e));
+    if (ds == 0xFFFFFFFFu || dedup_rank[ds] != e.rank) continue;
+    const unsigned long long k = atomicAdd(&ctr->survivors, 1ull);
+    if (k < surv_cap) surv[k] = Survivor{e.cls, e.rx, e.rank};
     else atomicOr(&ctr->overflow, kOvSurv);
   }
 }
@@ -827,7 +886,6 @@ struct FieldArgs {
   const TxParams* txp;
   const double* rx;
   const int* rx_req;
-  HashTable grp;
   const ClassInfo* cls_info;
   const int* rank_to_id;
   const Survivor* surv;
@@ -848,7 +906,7 @@ __global__ void k_field(FieldArgs A) {
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     const Survivor sv = A.surv[i];
-    const uint32_t cls = uint32_t(A.grp.keys[sv.slot]);
+    const uint32_t cls = sv.cls;
     const TxParams& P = A.txp[A.rx_req[sv.rx]];
     PathBuf pb;
     class_path(A.cls_info, cls, pb);
@@ -972,10 +1030,11 @@ struct SceneImpl {
   DBuf<float4> rx32;
   DBuf<RayRec> q0, q1;
   DBuf<NodeRec> nodes;
-  DBuf<unsigned long long> cls_keys, cop_keys, grp_keys, grp_rank, dd_keys, dd_rank;
+  DBuf<unsigned long long> cls_keys, cop_keys, dd_keys, dd_rank;
   DBuf<ClassInfo> cls_info;
-  DBuf<unsigned> grp_count;
-  DBuf<unsigned char> grp_ok;
+  DBuf<Corrected> corr_list;
+  DBuf<unsigned char> direct_ok;
+  DBuf<Tri32> corr32;
   DBuf<Survivor> surv;
   DBuf<int> s_counts, s_starts, s_cursor, s_order;
   DBuf<double> path_field, path_pts, field;
@@ -983,7 +1042,8 @@ struct SceneImpl {
   DBuf<Counters> ctr;
   // capacities (grow on overflow)
   unsigned long long cap_nodes = 1 << 22, cap_queue = 1 << 21, cap_surv = 1 << 16;
-  uint32_t cap_cls = 1 << 21, cap_cop = 1 << 19, cap_grp = 1 << 24, cap_dd = 1 << 20;
+  unsigned long long cap_corr = 1 << 20;
+  uint32_t cap_cls = 1 << 21, cap_cop = 1 << 19, cap_dd = 1 << 20;
   cudaEvent_t ev[8] = {};
 };
 
@@ -1084,6 +1144,7 @@ static void upload_scene(SceneImpl& S) {
   S.dev.tri32 = S.tri32.p;
   S.dev.tri64 = S.tri64.p;
   S.dev.mats = S.mats.p;
+  S.dev.rank_to_id = S.rank_to_id.p;
   S.dev.n_tri = nt;
   S.dev.n_nodes = nn;
   S.dev.n_mats = int(mats.size());
@@ -1113,8 +1174,23 @@ static void upload_mesh_order(SceneImpl& S, const std::vector<int>& order) {
     d.mat = t.mat;
     d.pad = 0;
   }
+  std::vector<Tri32> c32(nt);
+  for (int i = 0; i < nt; ++i) {
+    Tri32& f = c32[i];
+    for (int a = 0; a < 3; ++a) {
+      f.v1[a] = float(c[i].v1[a]);
+      f.e1[a] = float(c[i].e1[a]);
+      f.e2[a] = float(c[i].e2[a]);
+    }
+    auto n3 = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+    f.nv1 = float(n3(c[i].v1)) * 1.0001f;
+    f.ne1 = float(n3(c[i].e1)) * 1.0001f;
+    f.ne2 = float(n3(c[i].e2)) * 1.0001f;
+  }
   S.corr.upload(c.data(), c.size(), S.stream);
+  S.corr32.upload(c32.data(), c32.size(), S.stream);
   S.dev.corr = S.corr.p;
+  S.dev.corr32 = S.corr32.p;
   CK(cudaStreamSynchronize(S.stream));
 }
 
@@ -1200,11 +1276,14 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     max_depth = std::max(max_depth, q.max_reflection + q.max_transmission);
   }
   const int precision = reqs[0].field_precision == SBR_FIELD_FP32 ? 1 : 0;
+  const int stage_counts = reqs[0].stage_counts ? 1 : 0;
+  if (n_req >= int(0xFFFFFFFFu - kRootBase)) throw std::string("too many requests in one batch");
   auto t0 = std::chrono::steady_clock::now();
   CK(cudaEventRecord(S.ev[0], st));
   S.txp.upload(tp.data(), tp.size(), st);
   // receivers
   S.rx.ensure(std::max(1, 3 * rx_total));
+  S.direct_ok.ensure(std::max(1, rx_total));
   {
     std::vector<int> req_of(std::max(1, rx_total));
     for (int r = 0; r < n_req; ++r) {
@@ -1265,10 +1344,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     S.cls_keys.ensure(S.cap_cls);
     S.cls_info.ensure(S.cap_cls);
     S.cop_keys.ensure(S.cap_cop);
-    S.grp_keys.ensure(S.cap_grp);
-    S.grp_rank.ensure(S.cap_grp);
-    S.grp_count.ensure(S.cap_grp);
-    S.grp_ok.ensure(S.cap_grp);
+    S.corr_list.ensure(S.cap_corr);
     S.dd_keys.ensure(S.cap_dd);
     S.dd_rank.ensure(S.cap_dd);
     S.surv.ensure(S.cap_surv);
@@ -1276,11 +1352,8 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     const int fb = 256;
     k_fill_u64<<<grid_for(S.cap_cls, fb), fb, 0, st>>>(S.cls_keys.p, S.cap_cls, kEmptyKey);
     k_fill_u64<<<grid_for(S.cap_cop, fb), fb, 0, st>>>(S.cop_keys.p, S.cap_cop, kEmptyKey);
-    k_fill_u64<<<grid_for(S.cap_grp, fb), fb, 0, st>>>(S.grp_keys.p, S.cap_grp, kEmptyKey);
-    k_fill_u64<<<grid_for(S.cap_grp, fb), fb, 0, st>>>(S.grp_rank.p, S.cap_grp, kEmptyKey);
     k_fill_u64<<<grid_for(S.cap_dd, fb), fb, 0, st>>>(S.dd_keys.p, S.cap_dd, kEmptyKey);
     k_fill_u64<<<grid_for(S.cap_dd, fb), fb, 0, st>>>(S.dd_rank.p, S.cap_dd, kEmptyKey);
-    CK(cudaMemsetAsync(S.grp_count.p, 0, sizeof(unsigned) * S.cap_grp, st));
     CK(cudaEventRecord(S.ev[2], st));
     // ---- trace
     TraceArgs ta;
@@ -1308,39 +1381,32 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     CK(cudaEventRecord(S.ev[3], st));
     // ---- capture
     CaptureArgs ca;
+    ca.sc = S.dev;
     ca.nodes = S.nodes.p;
     ca.txp = S.txp.p;
     ca.grids = S.grids.p;
     ca.gb = S.gb.p;
     ca.rx = S.rx.p;
-    ca.grp = HashTable{S.grp_keys.p, S.cap_grp - 1};
-    ca.grp_rank = S.grp_rank.p;
-    ca.grp_count = S.grp_count.p;
+    ca.cls_info = S.cls_info.p;
+    ca.direct_ok = S.direct_ok.p;
+    ca.corr_list = S.corr_list.p;
+    ca.corr_cap = S.cap_corr;
     ca.ctr = S.ctr.p;
     ca.node_cap = S.cap_nodes;
+    ca.stage_counts = stage_counts;
+    if (rx_total)
+      k_direct<<<grid_for(rx_total, 64), 64, 0, st>>>(S.dev, S.txp.p, S.rx.p, S.rx_req.p, rx_total,
+                                                      S.direct_ok.p, S.ctr.p);
     k_capture<<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
     CK(cudaGetLastError());
     CK(cudaEventRecord(S.ev[4], st));
-    // ---- correct, dedup, select
-    CorrectArgs co;
-    co.sc = S.dev;
-    co.txp = S.txp.p;
-    co.n_tx = n_req;
-    co.rx = S.rx.p;
-    co.rx_req = S.rx_req.p;
-    co.grp = ca.grp;
-    co.grp_rank = S.grp_rank.p;
-    co.grp_count = S.grp_count.p;
-    co.grp_ok = S.grp_ok.p;
-    co.cls_info = S.cls_info.p;
-    co.dedup = HashTable{S.dd_keys.p, S.cap_dd - 1};
-    co.dedup_rank = S.dd_rank.p;
-    co.rank_to_id = S.rank_to_id.p;
-    co.ctr = S.ctr.p;
-    k_correct<<<grid_for(S.cap_grp, 128), 128, 0, st>>>(co);
-    k_select<<<grid_for(S.cap_grp, 256), 256, 0, st>>>(co.grp, S.grp_rank.p, S.grp_ok.p,
-                                                       S.cls_info.p, co.dedup, S.dd_rank.p,
-                                                       S.surv.p, S.cap_surv, S.ctr.p);
+    // ---- duplicate removal over the corrected captures
+    const HashTable dd{S.dd_keys.p, S.cap_dd - 1};
+    k_dedup<<<grid_for(S.cap_corr, 256), 256, 0, st>>>(S.corr_list.p, S.cap_corr, S.cls_info.p,
+                                                       dd, S.dd_rank.p, S.ctr.p);
+    k_select<<<grid_for(S.cap_corr, 256), 256, 0, st>>>(S.corr_list.p, S.cap_corr, S.cls_info.p,
+                                                        dd, S.dd_rank.p, S.surv.p, S.cap_surv,
+                                                        S.ctr.p);
     CK(cudaGetLastError());
     CK(cudaEventRecord(S.ev[5], st));
     Counters c;
@@ -1353,7 +1419,6 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     };
     grow(S.cap_cls, c.used_cls);
     grow(S.cap_cop, c.used_cop);
-    grow(S.cap_grp, c.used_grp);
     grow(S.cap_dd, c.used_dd);
     if (c.overflow) {
       if (c.overflow & kOvNodes) S.cap_nodes = std::max(S.cap_nodes * 2, c.nodes + c.nodes / 8);
@@ -1364,7 +1429,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
       }
       if (c.overflow & kOvClass) S.cap_cls *= 4;
       if (c.overflow & kOvCop) S.cap_cop *= 4;
-      if (c.overflow & kOvGroup) S.cap_grp *= 4;
+      if (c.overflow & kOvCorr) S.cap_corr = std::max(S.cap_corr * 2, c.corrected + c.corrected / 4);
       if (c.overflow & kOvDedup) S.cap_dd *= 4;
       if (c.overflow & kOvSurv) S.cap_surv = next_pow2(c.survivors + c.survivors / 4);
       continue;
@@ -1388,7 +1453,6 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     fa.txp = S.txp.p;
     fa.rx = S.rx.p;
     fa.rx_req = S.rx_req.p;
-    fa.grp = co.grp;
     fa.cls_info = S.cls_info.p;
     fa.rank_to_id = S.rank_to_id.p;
     fa.surv = S.surv.p;
@@ -1470,7 +1534,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     // paths are ordered by survivor order within a receiver; receivers ascend
     // because s_order is grouped by receiver index.
     out.counts.segments = (long long)c.nodes;
-    out.counts.captured = (long long)c.events;
+    out.counts.captured = stage_counts ? (long long)c.events : -1;
     out.counts.corrected = (long long)c.corrected;
     out.counts.paths = (long long)ns;
     out.counts.rays = (long long)out.tri.size();
@@ -1480,6 +1544,9 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     out.counts.launches = launches;
     out.counts.capture_candidates = (long long)c.cand;
     out.counts.ancestor_tests = (long long)c.anc;
+    out.counts.classes = (long long)c.used_cls;
+    out.counts.groups = -1;
+    out.counts.keys = (long long)c.used_dd;
     float ms[8] = {};
     for (int i = 1; i < 8; ++i) CK(cudaEventElapsedTime(&ms[i], S.ev[i - 1], S.ev[i]));
     out.timing.h2d_ms = ms[1];

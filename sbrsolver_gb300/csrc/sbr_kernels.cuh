@@ -185,6 +185,50 @@ struct TraceStats {
   unsigned fp64_tri, fallback;
 };
 
+// The reference's slab test (slab64) decided in FP32 where the error bounds
+// allow: 1 = accepted, 0 = rejected, -1 = within the error bounds (run
+// slab64).  Box bounds are float values (they come from float vertices), so
+// only the origin, direction and the arithmetic carry FP32 error; each
+// slab parameter t = (b - o) / d is within
+//   e = 2^-20 (|lo| + |hi| + 2|o|) / |d|
+// of its FP64 value.  A flat axis (lo == hi) gives one FP64 value t for both
+// planes, so the FP64 test accepts iff the other axes' intervals contain it.
+__device__ __forceinline__ int slab_certain(const double* bb, const float3& o, const float3& d) {
+  const float K = 9.5367431640625e-07f;  // 2^-20
+  float A_lo = -INFINITY, A_hi = -INFINITY, B_lo = INFINITY, B_hi = INFINITY;
+  float v = 0.0f, ev = 0.0f;
+  int flat = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float da = a == 0 ? d.x : (a == 1 ? d.y : d.z);
+    const float oa = a == 0 ? o.x : (a == 1 ? o.y : o.z);
+    if (da == 0.0f) return -1;
+    const float lo = float(bb[a]), hi = float(bb[3 + a]);
+    const float t1 = (lo - oa) / da, t2 = (hi - oa) / da;
+    const float e = K * (fabsf(lo) + fabsf(hi) + 2.0f * fabsf(oa)) / fabsf(da);
+    if (!isfinite(t1) || !isfinite(t2) || !isfinite(e)) return -1;
+    if (bb[a] == bb[3 + a]) {
+      if (flat++) return -1;
+      v = t1;
+      ev = e;
+      continue;
+    }
+    const float tn = fminf(t1, t2), tf = fmaxf(t1, t2);
+    A_lo = fmaxf(A_lo, tn - e);
+    A_hi = fmaxf(A_hi, tn + e);
+    B_lo = fminf(B_lo, tf - e);
+    B_hi = fminf(B_hi, tf + e);
+  }
+  if (flat) {
+    if (A_hi < v - ev && v + ev < B_lo) return 1;
+    if (v + ev < A_lo || v - ev > B_hi || A_lo > B_hi) return 0;
+    return -1;
+  }
+  if (A_hi < B_lo) return 1;
+  if (A_lo > B_hi) return 0;
+  return -1;
+}
+
 // Closest hit with the reference's result.  FP32 ordered traversal over the
 // reference BVH (boxes widened by box_margin so no box the FP64 test accepts
 // is missed), FP32 triangle filter, FP64 test for every triangle the filter
@@ -291,7 +335,9 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
   if (ok && best.rank != INT_MAX) {
     // every ancestor of the winner's leaf must pass the FP64 slab test
     for (int n = best.leaf; n >= 0; n = sc.ref[n].parent) {
-      if (!slab64(sc.ref[n].bb, o, d)) {
+      int v = slab_certain(sc.ref[n].bb, o32, d32);
+      if (v < 0) v = slab64(sc.ref[n].bb, o, d) ? 1 : 0;
+      if (!v) {
         ok = false;
         break;
       }

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 def _gpu(wl, precision="fp64", scene=None):
     sc = scene or api.DeviceScene.from_scene(wl.scene)
-    return api.solve(sc, api.request_from_workload(wl.request, precision)), sc
+    return api.solve(sc, api.request_from_workload(wl.request, precision, stage_counts=True)), sc
 
 
 def _check_against(res, ref_paths, ref_field, counts=None, tight=True):
