@@ -38,10 +38,13 @@ struct __align__(16) Node32 {
   int pad[2];
 };
 
-// FP64 reference node (depth-first numbering).
+// FP64 reference node (depth-first numbering), with its box also as floats
+// (exact: box bounds are float vertex coordinates) and a mask of its flat
+// axes (lo == hi), so FP32 tests need no FP64 conversions.
 struct RefNode {
   double bb[6];
-  int c0, c1, first, count, parent, pad;
+  float fb[6];
+  int c0, c1, first, count, parent, flat;
 };
 
 // Triangle, depth-first leaf order (index == closest-hit tie rank).

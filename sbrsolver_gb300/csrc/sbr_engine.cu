@@ -1074,12 +1074,19 @@ static void upload_scene(SceneImpl& S) {
     const HostNode& h = H.nodes[i];
     RefNode& r = ref[i];
     std::memcpy(r.bb, h.bb, sizeof r.bb);
+    r.flat = 0;
+    for (int a = 0; a < 6; ++a) r.fb[a] = float(h.bb[a]);
+    for (int a = 0; a < 3; ++a) {
+      // boxes of float vertices are floats; a non-float bound (empty box
+      // sentinel) disables the FP32 decision for that node
+      if (double(r.fb[a]) != h.bb[a] || double(r.fb[3 + a]) != h.bb[3 + a]) r.flat |= 8;
+      if (h.bb[a] == h.bb[3 + a]) r.flat |= 1 << a;
+    }
     r.c0 = h.c0;
     r.c1 = h.c1;
     r.first = h.first;
     r.count = h.count;
     r.parent = h.parent;
-    r.pad = 0;
     Node32& m = n32[i];
     std::memset(&m, 0, sizeof m);
     if (h.c0 >= 0) {

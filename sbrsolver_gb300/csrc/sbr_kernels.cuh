@@ -161,6 +161,47 @@ __device__ __forceinline__ bool tri_filter(const Tri32& T, const float3& o, cons
   return true;
 }
 
+// As tri_filter, also telling whether the FP64 test certainly hits (2) or
+// may go either way (1); 0 = certainly misses.  [tlo, thi] bounds t.
+__device__ __forceinline__ int tri_classify(const Tri32& T, const float3& o, const float3& d,
+                                            float no, float nd, float& tlo, float& thi) {
+  const float hx = d.y * T.e2[2] - d.z * T.e2[1];
+  const float hy = d.z * T.e2[0] - d.x * T.e2[2];
+  const float hz = d.x * T.e2[1] - d.y * T.e2[0];
+  const float a = T.e1[0] * hx + T.e1[1] * hy + T.e1[2] * hz;
+  const float sx = o.x - T.v1[0], sy = o.y - T.v1[1], sz = o.z - T.v1[2];
+  float U = sx * hx + sy * hy + sz * hz;
+  const float qx = sy * T.e1[2] - sz * T.e1[1];
+  const float qy = sz * T.e1[0] - sx * T.e1[2];
+  const float qz = sx * T.e1[1] - sy * T.e1[0];
+  float V = d.x * qx + d.y * qy + d.z * qz;
+  float W = T.e2[0] * qx + T.e2[1] * qy + T.e2[2] * qz;
+  const float ns = no + T.nv1;
+  const float ea = kFiltK * T.ne1 * T.ne2 * nd;
+  const float eU = kFiltK * ns * nd * T.ne2;
+  const float eV = kFiltK * ns * T.ne1 * nd;
+  const float eW = kFiltK * ns * T.ne1 * T.ne2;
+  const float A = fabsf(a);
+  if (A <= kEps32 + ea) {
+    tlo = 0.0f;
+    thi = INFINITY;
+    return 1;
+  }
+  if (a < 0.0f) {
+    U = -U;
+    V = -V;
+    W = -W;
+  }
+  if (U < -eU || V < -eV) return 0;
+  if (U > A + ea + eU) return 0;
+  if (U + V > A + ea + eU + eV) return 0;
+  thi = (W + eW) / (A - ea);
+  if (thi <= kEps32 * 0.5f) return 0;
+  tlo = (W - eW) / (A + ea);
+  const bool sure = U > eU && V > eV && U + V < A - ea - eU - eV && tlo > 2.0f * kEps32;
+  return sure ? 2 : 1;
+}
+
 __device__ __forceinline__ void load_node(const Node32* nodes, int i, float4& f0, float4& f1,
                                           float4& f2, int2& ch) {
   const float4* p = reinterpret_cast<const float4*>(nodes + i);
@@ -193,21 +234,23 @@ struct TraceStats {
 //   e = 2^-20 (|lo| + |hi| + 2|o|) / |d|
 // of its FP64 value.  A flat axis (lo == hi) gives one FP64 value t for both
 // planes, so the FP64 test accepts iff the other axes' intervals contain it.
-__device__ __forceinline__ int slab_certain(const double* bb, const float3& o, const float3& d) {
+__device__ __forceinline__ int slab_certain(const float* bb, int flatmask, const float3& o,
+                                            const float3& d) {
   const float K = 9.5367431640625e-07f;  // 2^-20
   float A_lo = -INFINITY, A_hi = -INFINITY, B_lo = INFINITY, B_hi = INFINITY;
   float v = 0.0f, ev = 0.0f;
   int flat = 0;
+  if (flatmask & 8) return -1;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const float da = a == 0 ? d.x : (a == 1 ? d.y : d.z);
     const float oa = a == 0 ? o.x : (a == 1 ? o.y : o.z);
     if (da == 0.0f) return -1;
-    const float lo = float(bb[a]), hi = float(bb[3 + a]);
+    const float lo = bb[a], hi = bb[3 + a];
     const float t1 = (lo - oa) / da, t2 = (hi - oa) / da;
     const float e = K * (fabsf(lo) + fabsf(hi) + 2.0f * fabsf(oa)) / fabsf(da);
     if (!isfinite(t1) || !isfinite(t2) || !isfinite(e)) return -1;
-    if (bb[a] == bb[3 + a]) {
+    if (flatmask & (1 << a)) {
       if (flat++) return -1;
       v = t1;
       ev = e;
@@ -252,6 +295,11 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
   int stack[kStack];
   int sp = 0;
   int pending_leaf = -1;
+  constexpr int kCand = 8;
+  int cand_r[kCand], cand_leaf[kCand];
+  float cand_t[kCand];
+  int ncand = 0;
+  bool overflowed = false;
   if (sc.root_leaf) pending_leaf = 0;
   else stack[sp++] = 0;
   bool stack_overflow = false;
@@ -260,21 +308,30 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
     if (pending_leaf >= 0) {
       const RefNode& L = sc.ref[pending_leaf];
       for (int r = L.first; r < L.first + L.count; ++r) {
-        float tlo;
-        if (!tri_filter(sc.tri32[r], o32, d32, no, nd, tlo)) continue;
-        if (tlo > tcut) continue;
-        ++st.fp64_tri;
-        double t, P[3], dist;
-        if (!mt64(sc.tri64[r], o, d, t, P, dist)) continue;
-        if (dist < best.dist || (dist == best.dist && r < best.rank)) {
-          best.dist = dist;
-          best.t = t;
-          best.p[0] = P[0];
-          best.p[1] = P[1];
-          best.p[2] = P[2];
-          best.rank = r;
-          best.leaf = pending_leaf;
-          tcut = float(t) * (1.0f + 1.0f / 4096.0f) + 1e-30f;
+        float tlo, thi;
+        const int k = tri_classify(sc.tri32[r], o32, d32, no, nd, tlo, thi);
+        if (k == 0 || tlo > tcut) continue;
+        if (ncand < kCand) {
+          cand_r[ncand] = r;
+          cand_leaf[ncand] = pending_leaf;
+          cand_t[ncand] = tlo;
+          ++ncand;
+          if (k == 2) tcut = fminf(tcut, thi * (1.0f + 1.0f / 4096.0f) + 1e-30f);
+        } else {
+          overflowed = true;  // too many contenders: resolve this one now
+          ++st.fp64_tri;
+          double t, P[3], dist;
+          if (mt64(sc.tri64[r], o, d, t, P, dist) &&
+              (dist < best.dist || (dist == best.dist && r < best.rank))) {
+            best.dist = dist;
+            best.t = t;
+            best.p[0] = P[0];
+            best.p[1] = P[1];
+            best.p[2] = P[2];
+            best.rank = r;
+            best.leaf = pending_leaf;
+            tcut = fminf(tcut, float(t) * (1.0f + 1.0f / 4096.0f) + 1e-30f);
+          }
         }
       }
       pending_leaf = -1;
@@ -331,11 +388,44 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
     }
   }
 
+  // Resolve the contenders exactly, nearest lower bound first, until none
+  // can reach the best exact distance.
+  for (int i = 1; i < ncand; ++i) {  // insertion sort by tlo (ncand <= kCand)
+    const float kt = cand_t[i];
+    const int kr = cand_r[i], kl = cand_leaf[i];
+    int j = i - 1;
+    while (j >= 0 && cand_t[j] > kt) {
+      cand_t[j + 1] = cand_t[j];
+      cand_r[j + 1] = cand_r[j];
+      cand_leaf[j + 1] = cand_leaf[j];
+      --j;
+    }
+    cand_t[j + 1] = kt;
+    cand_r[j + 1] = kr;
+    cand_leaf[j + 1] = kl;
+  }
+  for (int i = 0; i < ncand; ++i) {
+    if (best.rank != INT_MAX && cand_t[i] > float(best.t) * (1.0f + 1.0f / 4096.0f) + 1e-30f) break;
+    const int r = cand_r[i];
+    ++st.fp64_tri;
+    double t, P[3], dist;
+    if (mt64(sc.tri64[r], o, d, t, P, dist) &&
+        (dist < best.dist || (dist == best.dist && r < best.rank))) {
+      best.dist = dist;
+      best.t = t;
+      best.p[0] = P[0];
+      best.p[1] = P[1];
+      best.p[2] = P[2];
+      best.rank = r;
+      best.leaf = cand_leaf[i];
+    }
+  }
+  (void)overflowed;
   bool ok = !stack_overflow;
   if (ok && best.rank != INT_MAX) {
     // every ancestor of the winner's leaf must pass the FP64 slab test
     for (int n = best.leaf; n >= 0; n = sc.ref[n].parent) {
-      int v = slab_certain(sc.ref[n].bb, o32, d32);
+      int v = slab_certain(sc.ref[n].fb, sc.ref[n].flat, o32, d32);
       if (v < 0) v = slab64(sc.ref[n].bb, o, d) ? 1 : 0;
       if (!v) {
         ok = false;
