@@ -99,13 +99,18 @@ struct __align__(16) RayRec {
   uint32_t pad;
 };
 
-// One executed segment (tree node).
-struct __align__(16) NodeRec {
-  double s[3], t[3];
-  double S;
+// One executed segment (tree node), split in two arrays: the FP32 part the
+// capture stage reads for every node and ancestor, and the FP64 part it
+// reads only for the rare tests inside the FP32 error margin.
+struct __align__(16) NodeHot {
+  float s[3], S;    // source point, RayCapture's pathLength argument
+  float u[3], len;  // unit direction and segment length
   uint32_t parent, cls, launch, heap;
-  float u[3], len;  // FP32 unit direction and length for the capture filter
-  uint32_t tx, pad;
+  uint32_t tx, pad0, pad1, pad2;
+};
+struct __align__(16) NodeCold {
+  double s[3], t[3];  // source and target points (RTSolver.cpp:156-183, 228-255)
+  double S, pad;
 };
 
 // Per transmitter (one request of a batch).

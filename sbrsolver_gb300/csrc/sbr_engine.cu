@@ -333,7 +333,8 @@ struct TraceArgs {
   const RayRec* in;
   RayRec* out;
   unsigned long long out_cap;
-  NodeRec* nodes;
+  NodeHot* nodes;
+  NodeCold* nodes_cold;
   unsigned long long node_cap;
   HashTable cls_tab, cop_tab;
   ClassInfo* cls_info;
@@ -405,27 +406,32 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
     const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
     const bool root = A.depth == 0;
     if (ni < A.node_cap) {
-      NodeRec n;
+      NodeCold n;
+      NodeHot m;
       n.s[0] = r.o[0]; n.s[1] = r.o[1]; n.s[2] = r.o[2];
       if (hit) {
         n.t[0] = h.p[0]; n.t[1] = h.p[1]; n.t[2] = h.p[2];
-        n.len = float(h.dist);
+        m.len = float(h.dist);
       } else {
         const double sc = root ? 1E10 : 1E2;  // RTSolver.cpp:231,249
         n.t[0] = x64::add(r.o[0], x64::mul(r.d[0], sc));
         n.t[1] = x64::add(r.o[1], x64::mul(r.d[1], sc));
         n.t[2] = x64::add(r.o[2], x64::mul(r.d[2], sc));
-        n.len = float(sc);
+        m.len = float(sc);
       }
-      n.u[0] = float(r.d[0]); n.u[1] = float(r.d[1]); n.u[2] = float(r.d[2]);
       n.S = r.S;
-      n.parent = r.parent;
-      n.cls = r.cls;
-      n.launch = r.launch;
-      n.heap = r.heap;
-      n.tx = r.tx;
-      n.pad = 0;
-      A.nodes[ni] = n;
+      n.pad = 0.0;
+      m.s[0] = float(r.o[0]); m.s[1] = float(r.o[1]); m.s[2] = float(r.o[2]);
+      m.S = float(r.S);
+      m.u[0] = float(r.d[0]); m.u[1] = float(r.d[1]); m.u[2] = float(r.d[2]);
+      m.parent = r.parent;
+      m.cls = r.cls;
+      m.launch = r.launch;
+      m.heap = r.heap;
+      m.tx = r.tx;
+      m.pad0 = m.pad1 = m.pad2 = 0;
+      A.nodes_cold[ni] = n;
+      A.nodes[ni] = m;
     } else {
       atomicOr(&A.ctr->overflow, kOvNodes);
     }
@@ -502,7 +508,8 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
 
 struct CaptureArgs {
   DevScene sc;
-  const NodeRec* nodes;
+  const NodeHot* nodes;
+  const NodeCold* nodes_cold;
   const TxParams* txp;
   const RxGrid* grids;
   const GridBuild* gb;
@@ -515,23 +522,6 @@ struct CaptureArgs {
   unsigned long long node_cap;
   int stage_counts;
 };
-
-// Segment data of a node's ancestor, staged in shared memory once per node.
-struct AncRec {
-  float s[3], u[3], len, S;
-  uint32_t idx, pad;
-};
-
-__device__ __forceinline__ int capture_test_f(const float3& s, const float3& u, float len, float S,
-                                              uint32_t idx, const NodeRec* nodes,
-                                              const float3& c32, const double* c64, float tanb32,
-                                              double tanb, unsigned& n64) {
-  const int v = reception32(s, u, len, S, c32, tanb32);
-  if (v >= 0) return v;
-  ++n64;
-  const NodeRec& n = nodes[idx];
-  return reception64(n.s, n.t, c64, n.S, tanb) ? 1 : 0;
-}
 
 // MultiPathCorrection (RTSolver.cpp:330-373) for one capture, walking the
 // path class from the receiver back to the transmitter: the line from each
@@ -566,57 +556,68 @@ __device__ __forceinline__ bool correct_event(const DevScene& sc, const ClassInf
   return true;
 }
 
+// Exact decision for a test inside the FP32 margin (reception64 on the
+// node's FP64 record).
+__device__ __noinline__ int capture_exact(const NodeCold* cold, uint32_t idx, const double* c64,
+                                          double tanb) {
+  const NodeCold& n = cold[idx];
+  return reception64(n.s, n.t, c64, n.S, tanb) ? 1 : 0;
+}
+
 // One warp per tree node.  The receivers that can fall inside the node's
 // reception spheres lie within rb of its segment (rb bounds the sphere radius
 // (S + |P|) tan(beta), with |P| <= (cmax + S tan b) / (1 - tan b) for any
-// capturing point); the segment is clipped to that region, cut into chunks
-// (each receiver is owned by the chunk its projection falls in), and each
-// chunk's capsule is rasterised row by row over the receiver grid, where a
-// row of cells is one contiguous run of receivers for the lanes to stride.
-// A capture counts unless an ancestor of the node captures the same receiver
-// (RTSolver.cpp:277-284); ancestors come from shared memory.
+// capturing point); the segment is clipped to that region and cut into
+// chunks (each receiver is owned by the chunk its projection falls in).  Each
+// chunk's capsule is rasterised over the receiver grid one row of cells per
+// lane; a row is one contiguous run of receivers, and the lanes stride over
+// the concatenation of the rows' runs.  A capture counts unless an ancestor
+// of the node captures the same receiver (RTSolver.cpp:277-284); ancestors
+// come from shared memory.
 constexpr int kCapWarps = 4;
 
-__global__ void __launch_bounds__(32 * kCapWarps) k_capture(CaptureArgs A) {
+struct AncRec {
+  float s[3], S, u[3], len;
+  uint32_t idx, pad[3];
+};
+
+__global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
   __shared__ AncRec anc[kCapWarps][kMaxDepth];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
   const unsigned long long n_nodes = min(A.ctr->nodes, A.node_cap);
   unsigned long long events = 0, cand = 0, anc_tests = 0;
   unsigned n64 = 0;
   const unsigned long long nw = (unsigned long long)gridDim.x * kCapWarps;
   for (unsigned long long i = (unsigned long long)blockIdx.x * kCapWarps + warp; i < n_nodes;
        i += nw) {
-    const NodeRec& nref = A.nodes[i];
-    const uint32_t ntx = nref.tx;
-    const TxParams& P = A.txp[ntx];
-    const RxGrid& g = A.grids[ntx];
-    const float3 s = make_float3(float(nref.s[0]), float(nref.s[1]), float(nref.s[2]));
-    const float3 u = make_float3(nref.u[0], nref.u[1], nref.u[2]);
-    const float len = nref.len;
-    const float S = float(nref.S);
-    const uint32_t cls = nref.cls, launch = nref.launch, heap = nref.heap;
+    const NodeHot nd = A.nodes[i];
+    const TxParams& P = A.txp[nd.tx];
+    const RxGrid& g = A.grids[nd.tx];
+    const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
+    const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
+    const float len = nd.len, S = nd.S;
     // stage the ancestor chain
     int na = 0;
     if (lane == 0) {
-      for (uint32_t p = nref.parent; p != 0xFFFFFFFFu && p < A.node_cap && na < kMaxDepth;) {
-        const NodeRec& a = A.nodes[p];
+      for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap && na < kMaxDepth;) {
+        const NodeHot a = A.nodes[p];
         AncRec& r = anc[warp][na++];
-        r.s[0] = float(a.s[0]); r.s[1] = float(a.s[1]); r.s[2] = float(a.s[2]);
-        r.u[0] = a.u[0]; r.u[1] = a.u[1]; r.u[2] = a.u[2];
-        r.len = a.len;
-        r.S = float(a.S);
+        r.s[0] = a.s[0]; r.s[1] = a.s[1]; r.s[2] = a.s[2]; r.S = a.S;
+        r.u[0] = a.u[0]; r.u[1] = a.u[1]; r.u[2] = a.u[2]; r.len = a.len;
         r.idx = p;
         p = a.parent;
       }
     }
-    na = __shfl_sync(0xffffffffu, na, 0);
+    na = __shfl_sync(FULL, na, 0);
     __syncwarp();
     if (P.n_rx > 0) {
       const float tanb = float(P.tan_beta);
-      const float cmax = A.gb[ntx].cmax;
+      const float cmax = A.gb[nd.tx].cmax;
       const float pmax = (cmax + S * tanb) / fmaxf(1e-6f, 1.0f - tanb) * 1.0001f + 1.0f;
       const float su = s.x * u.x + s.y * u.y + s.z * u.z;
       const float ss = s.x * s.x + s.y * s.y + s.z * s.z;
+      const float ns = sqrtf(ss);
       const float disc = su * su - (ss - pmax * pmax);
       float lo = 0.0f, hi = -1.0f;
       if (disc >= 0.0f) {
@@ -638,94 +639,147 @@ __global__ void __launch_bounds__(32 * kCapWarps) k_capture(CaptureArgs A) {
         }
       }
       if (lo <= hi) {
-        // chunk length: a few cells, or the local sphere radius if larger
         const float r0 = (S + sqrtf(fmaxf(0.0f, ss + 2.0f * lo * su + lo * lo))) * tanb;
         const float lc = fmaxf(4.0f * g.cell, r0);
         int nchunk = int(ceilf((hi - lo) / lc));
         nchunk = max(1, min(nchunk, 4096));
         const float step = (hi - lo) / nchunk;
+        // error margins of the FP32 reception test, from per-node bounds
+        const float ml = kFiltK * (ns + cmax + 1.0f);
         for (int ch = 0; ch < nchunk; ++ch) {
           const float a = lo + ch * step, b = (ch == nchunk - 1) ? hi : lo + (ch + 1) * step;
           const float pa[3] = {s.x + a * u.x, s.y + a * u.y, s.z + a * u.z};
           const float pb[3] = {s.x + b * u.x, s.y + b * u.y, s.z + b * u.z};
-          const float npa = sqrtf(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]);
-          const float npb = sqrtf(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]);
+          const float npmax = fmaxf(sqrtf(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]),
+                                    sqrtf(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]));
+          const float mr = kFiltK * (ns + cmax + S + npmax + 1.0f);
           // |P| is convex along the chunk: the larger end bounds it
-          const float rb = (S + fmaxf(npa, npb)) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f +
-                           kFiltK * (fmaxf(npa, npb) + S + 1.0f);
+          const float rb = (S + npmax) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f + mr;
           int c0[3], c1[3];
           for (int k = 0; k < 3; ++k) {
             c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - rb - g.org[k]) / g.cell)));
             c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + rb - g.org[k]) / g.cell)));
           }
-          for (int iz = c0[2]; iz <= c1[2]; ++iz) {
-            const float z0 = g.org[2] + iz * g.cell - rb, z1 = g.org[2] + (iz + 1) * g.cell + rb;
-            for (int iy = c0[1]; iy <= c1[1]; ++iy) {
+          const int ny = c1[1] - c0[1] + 1, nz = c1[2] - c0[2] + 1;
+          const int nrows = (c0[0] <= c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
+          for (int rbase = 0; rbase < nrows; rbase += 32) {
+            // this lane's row: the part of the chunk within rb of its y/z band
+            int beg = 0, cnt = 0;
+            const int ridx = rbase + lane;
+            if (ridx < nrows) {
+              const int iy = c0[1] + ridx % ny, iz = c0[2] + ridx / ny;
               const float y0 = g.org[1] + iy * g.cell - rb, y1 = g.org[1] + (iy + 1) * g.cell + rb;
-              // part of the chunk whose y and z are within rb of this row
+              const float z0 = g.org[2] + iz * g.cell - rb, z1 = g.org[2] + (iz + 1) * g.cell + rb;
               float la = a, lb = b;
+              bool ok = true;
               if (fabsf(u.y) > 1e-20f) {
                 const float t1 = (y0 - s.y) / u.y, t2 = (y1 - s.y) / u.y;
                 la = fmaxf(la, fminf(t1, t2));
                 lb = fminf(lb, fmaxf(t1, t2));
               } else if (s.y < y0 || s.y > y1) {
-                continue;
+                ok = false;
               }
               if (fabsf(u.z) > 1e-20f) {
                 const float t1 = (z0 - s.z) / u.z, t2 = (z1 - s.z) / u.z;
                 la = fmaxf(la, fminf(t1, t2));
                 lb = fminf(lb, fmaxf(t1, t2));
               } else if (s.z < z0 || s.z > z1) {
-                continue;
+                ok = false;
               }
-              if (la > lb) continue;
-              const float xa = s.x + la * u.x, xb = s.x + lb * u.x;
-              const int x0 = max(c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) / g.cell)));
-              const int x1 = min(c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) / g.cell)));
-              if (x0 > x1) continue;
-              const int row = (iz * g.dim[1] + iy) * g.dim[0];
-              const int beg = g.cell_start[row + x0], end = g.cell_start[row + x1 + 1];
-              for (int j = beg + lane; j < end; j += 32) {
-                const float4 c4 = g.rx32[j];
-                const float3 c = make_float3(c4.x, c4.y, c4.z);
-                const float lam = u.x * (c.x - s.x) + u.y * (c.y - s.y) + u.z * (c.z - s.z);
-                if (ch > 0 && lam < a) continue;              // owned by an earlier chunk
-                if (ch < nchunk - 1 && lam >= b) continue;    // owned by a later chunk
-                const int gi = __float_as_int(c4.w);
-                const double* c64 = A.rx + 3 * size_t(gi);
-                ++cand;
-                if (!capture_test_f(s, u, len, S, uint32_t(i), A.nodes, c, c64, tanb,
-                                    P.tan_beta, n64))
-                  continue;
-                // RayCapture deletes a captured node's subtree, so an ancestor
-                // capturing the same receiver suppresses this one.
-                auto suppressed = [&]() {
-                  for (int q = 0; q < na; ++q) {
-                    const AncRec& r = anc[warp][q];
-                    ++anc_tests;
-                    if (capture_test_f(make_float3(r.s[0], r.s[1], r.s[2]),
-                                       make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, r.idx,
-                                       A.nodes, c, c64, tanb, P.tan_beta, n64))
-                      return true;
-                  }
-                  return false;
-                };
-                if (A.stage_counts) {
-                  if (suppressed()) continue;
-                  ++events;
+              if (ok && la <= lb) {
+                const float xa = s.x + la * u.x, xb = s.x + lb * u.x;
+                const int x0 = max(c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) / g.cell)));
+                const int x1 = min(c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) / g.cell)));
+                if (x0 <= x1) {
+                  const int row = (iz * g.dim[1] + iy) * g.dim[0];
+                  beg = g.cell_start[row + x0];
+                  cnt = g.cell_start[row + x1 + 1] - beg;
                 }
-                const bool ok = is_root_class(cls)
-                                    ? A.direct_ok[gi] != 0
-                                    : correct_event(A.sc, A.cls_info, cls, c, c64, n64);
-                if (!ok) continue;
-                if (!A.stage_counts && suppressed()) continue;
-                const unsigned long long k = atomicAdd(&A.ctr->corrected, 1ull);
-                if (k < A.corr_cap)
-                  A.corr_list[k] =
-                      Corrected{uint32_t(gi), cls, (unsigned long long)launch << kHeapBits | heap};
-                else
-                  atomicOr(&A.ctr->overflow, kOvCorr);
               }
+            }
+            // concatenate the 32 rows' receiver runs
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+              const int v = __shfl_up_sync(FULL, incl, o);
+              if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(FULL, incl, 31);
+            for (int kb = 0; kb < total; kb += 32) {
+              const int k = kb + lane;
+              // row holding item k: first lane whose inclusive count exceeds k
+              int rl = 0;
+              for (int step2 = 16; step2; step2 >>= 1) {
+                const int v = __shfl_sync(FULL, incl, rl + step2 - 1);
+                if (v <= k) rl += step2;
+              }
+              const int rincl = __shfl_sync(FULL, incl, rl);
+              const int rcnt = __shfl_sync(FULL, cnt, rl);
+              const int rbeg = __shfl_sync(FULL, beg, rl);
+              if (k >= total) continue;
+              const int j = rbeg + (k - (rincl - rcnt));
+              const float4 c4 = g.rx32[j];
+              const float3 c = make_float3(c4.x, c4.y, c4.z);
+              const float wx = c.x - s.x, wy = c.y - s.y, wz = c.z - s.z;
+              const float lam = u.x * wx + u.y * wy + u.z * wz;
+              if (ch > 0 && lam < a) continue;            // owned by an earlier chunk
+              if (ch < nchunk - 1 && lam >= b) continue;  // owned by a later chunk
+              const int gi = __float_as_int(c4.w);
+              const double* c64 = A.rx + 3 * size_t(gi);
+              ++cand;
+              int v;
+              if (lam < a || lam > b) {
+                // outside the chunk's own range: full-margin test
+                v = reception32(s, u, len, S, c, tanb);
+              } else if (lam < -ml) {
+                v = 0;
+              } else if (lam <= ml) {
+                v = -1;
+              } else {
+                const float lcl = fminf(lam, len);
+                const float px = s.x + lcl * u.x, py = s.y + lcl * u.y, pz = s.z + lcl * u.z;
+                const float np = sqrtf(px * px + py * py + pz * pz);
+                const float ex = c.x - px, ey = c.y - py, ez = c.z - pz;
+                const float d2 = ex * ex + ey * ey + ez * ez;
+                const float rad = (S + np) * tanb;
+                const float rh = rad + mr, rl2 = rad - mr;
+                v = d2 > rh * rh ? 0 : ((rl2 > 0.0f && d2 < rl2 * rl2) ? 1 : -1);
+              }
+              if (v < 0) {
+                ++n64;
+                v = capture_exact(A.nodes_cold, uint32_t(i), c64, P.tan_beta);
+              }
+              if (!v) continue;
+              // RayCapture deletes a captured node's subtree, so an ancestor
+              // capturing the same receiver suppresses this one.
+              auto suppressed = [&]() {
+                for (int q = 0; q < na; ++q) {
+                  const AncRec& r = anc[warp][q];
+                  ++anc_tests;
+                  int w = reception32(make_float3(r.s[0], r.s[1], r.s[2]),
+                                      make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, c, tanb);
+                  if (w < 0) {
+                    ++n64;
+                    w = capture_exact(A.nodes_cold, r.idx, c64, P.tan_beta);
+                  }
+                  if (w) return true;
+                }
+                return false;
+              };
+              if (A.stage_counts) {
+                if (suppressed()) continue;
+                ++events;
+              }
+              const bool ok = is_root_class(nd.cls)
+                                  ? A.direct_ok[gi] != 0
+                                  : correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
+              if (!ok) continue;
+              if (!A.stage_counts && suppressed()) continue;
+              const unsigned long long kk = atomicAdd(&A.ctr->corrected, 1ull);
+              if (kk < A.corr_cap)
+                A.corr_list[kk] = Corrected{uint32_t(gi), nd.cls,
+                                            (unsigned long long)nd.launch << kHeapBits | nd.heap};
+              else
+                atomicOr(&A.ctr->overflow, kOvCorr);
             }
           }
         }
@@ -734,10 +788,10 @@ __global__ void __launch_bounds__(32 * kCapWarps) k_capture(CaptureArgs A) {
     __syncwarp();
   }
   for (int o = 16; o; o >>= 1) {
-    events += __shfl_xor_sync(0xffffffffu, events, o);
-    cand += __shfl_xor_sync(0xffffffffu, cand, o);
-    anc_tests += __shfl_xor_sync(0xffffffffu, anc_tests, o);
-    n64 += __shfl_xor_sync(0xffffffffu, n64, o);
+    events += __shfl_xor_sync(FULL, events, o);
+    cand += __shfl_xor_sync(FULL, cand, o);
+    anc_tests += __shfl_xor_sync(FULL, anc_tests, o);
+    n64 += __shfl_xor_sync(FULL, n64, o);
   }
   if (lane == 0) {
     if (events) atomicAdd(&A.ctr->events, events);
@@ -1029,7 +1083,8 @@ struct SceneImpl {
   DBuf<int> cell_base, cell_counts, cell_starts, cell_cursor;
   DBuf<float4> rx32;
   DBuf<RayRec> q0, q1;
-  DBuf<NodeRec> nodes;
+  DBuf<NodeHot> nodes;
+  DBuf<NodeCold> nodes_cold;
   DBuf<unsigned long long> cls_keys, cop_keys, dd_keys, dd_rank;
   DBuf<ClassInfo> cls_info;
   DBuf<Corrected> corr_list;
@@ -1346,6 +1401,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     if (attempt > 6) throw std::string("capacity: tables kept overflowing");
     S.ctr.ensure(1);
     S.nodes.ensure(S.cap_nodes);
+    S.nodes_cold.ensure(S.cap_nodes);
     S.q0.ensure(S.cap_queue);
     S.q1.ensure(S.cap_queue);
     S.cls_keys.ensure(S.cap_cls);
@@ -1369,6 +1425,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     ta.n_tx = n_req;
     ta.dirs = S.dir_table.p;
     ta.nodes = S.nodes.p;
+    ta.nodes_cold = S.nodes_cold.p;
     ta.node_cap = S.cap_nodes;
     ta.out_cap = S.cap_queue;
     ta.cls_tab = HashTable{S.cls_keys.p, S.cap_cls - 1};
@@ -1390,6 +1447,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     CaptureArgs ca;
     ca.sc = S.dev;
     ca.nodes = S.nodes.p;
+    ca.nodes_cold = S.nodes_cold.p;
     ca.txp = S.txp.p;
     ca.grids = S.grids.p;
     ca.gb = S.gb.p;
