@@ -164,6 +164,27 @@ sbr_status sbr_result_destroy(sbr_result* result);
 const char* sbr_last_error(void);
 const char* sbr_version(void);
 
+/* ---- allocation-free field sum -------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory (code inside CUDA graph capture, processes whose device memory
+ * belongs to another framework's pool, services that must not grow after
+ * start-up): sums per-path fields into per-receiver fields in each
+ * receiver's (launch, BFS) rank order, exactly as sbr_solve does, using only
+ * a fixed 4 MiB array compiled into the library (held on every GPU that
+ * loads it until exit).  All pointers are device pointers owned by the
+ * caller: path_receiver[n_paths] (0-based), path_rank[n_paths]
+ * (launch << 17 | heap, see sbr_path), path_field[6 * n_paths],
+ * field_out[6 * n_rx].  Limits: 1 <= n_rx <= 262144, 0 <= n_paths <= 262144;
+ * larger sizes are rejected with SBR_ERR_INVALID_ARG.  Runs on `stream`
+ * (a cudaStream_t, NULL = default stream) and returns after it completes.
+ * The first call on a device looks up the array's device address and should
+ * come before any stream capture.  Calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+sbr_status sbr_receiver_field_sum_noalloc(const int* path_receiver, const long long* path_rank,
+                                          const double* path_field, int n_paths, int n_rx,
+                                          int field_precision, double* field_out,
+                                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

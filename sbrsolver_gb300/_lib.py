@@ -20,6 +20,7 @@ EXPORTS = (
     "sbr_scene_set_mesh_order", "sbr_scene_coplanar_ids", "sbr_scene_destroy", "sbr_solve",
     "sbr_solve_batch", "sbr_result_counts", "sbr_result_field", "sbr_result_paths",
     "sbr_result_timing", "sbr_result_destroy", "sbr_last_error", "sbr_version",
+    "sbr_receiver_field_sum_noalloc",
 )
 
 
@@ -98,6 +99,7 @@ def load(path: str = LIB_PATH):
             "sbr_result_paths": [vp, P(Path), P(I), P(I), P(I), P(D)],
             "sbr_result_timing": [vp, P(Timing)],
             "sbr_result_destroy": [vp],
+            "sbr_receiver_field_sum_noalloc": [vp, vp, vp, I, I, I, vp, vp],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

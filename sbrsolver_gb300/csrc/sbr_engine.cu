@@ -41,6 +41,7 @@ namespace sbr {
 // ------------------------------------------------------------ error state
 static thread_local std::string g_err;
 static void set_err(const std::string& s) { g_err = s; }
+void set_error_message(const std::string& s) { g_err = s; }
 
 struct CudaError {
   cudaError_t e;

@@ -1,0 +1,215 @@
+// Per-receiver field sum without any allocation.
+//
+// Some callers of this library cannot allocate device memory: code running
+// while a CUDA graph is being captured (cudaMalloc is not capturable),
+// processes whose device memory is owned by another framework's pool, and
+// services that must not grow their footprint after start-up.  For them,
+// sbr_receiver_field_sum_noalloc sums per-path fields into per-receiver
+// fields, in each receiver's (launch, BFS) rank order, with all of its
+// working memory in one fixed array compiled into this library.
+//
+// The scratch array below is a file-scope __device__ array: every GPU that
+// loads the library holds it (4 MiB) until the process exits.  Host code must
+// not pass the symbol itself to a kernel; its device address is looked up once
+// per device with cudaGetSymbolAddress, on the first call made while that
+// device is current.  That first call therefore performs the set-up and
+// should come before any stream capture.  Every call shares the array and
+// leaves the previous call's contents behind, so the counters are cleared at
+// the start of each call; calls that overlap on the GPU (for example on two
+// streams at once) race on the array and must be serialised by the caller.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/sbr.h"
+
+namespace sbr {
+namespace noalloc {
+
+constexpr int kMaxRx = 1 << 18;     // receivers per call
+constexpr int kMaxPaths = 1 << 18;  // paths per call
+// layout (ints): counts[kMaxRx + 1] | starts[kMaxRx + 2] | cursor[kMaxRx + 1] |
+//                order[kMaxPaths] | error flag
+constexpr size_t kCounts = 0;
+constexpr size_t kStarts = kCounts + kMaxRx + 1;
+constexpr size_t kCursor = kStarts + kMaxRx + 2;
+constexpr size_t kOrder = kCursor + kMaxRx + 1;
+constexpr size_t kError = kOrder + kMaxPaths;
+constexpr size_t kScratchInts = kError + 1;
+
+static __device__ __align__(256) int g_scratch[kScratchInts];
+
+__global__ void k_clear(int* s, int n_rx) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n_rx; i += gridDim.x * blockDim.x) {
+    s[kCounts + i] = 0;
+    s[kCursor + i] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) s[kError] = 0;
+}
+
+__global__ void k_hist(const int* recv, int n, int n_rx, int* s) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = recv[i];
+    if (r < 0 || r >= n_rx) {
+      atomicExch(&s[kError], 1);
+      continue;
+    }
+    atomicAdd(&s[kCounts + r], 1);
+  }
+}
+
+// one block: exclusive scan of counts[0..n_rx) into starts[0..n_rx]
+__global__ void k_scan(int* s, int n_rx) {
+  __shared__ int part[1024];
+  const int* in = s + kCounts;
+  int* out = s + kStarts;
+  const int t = threadIdx.x, T = blockDim.x;
+  const int chunk = (n_rx + T - 1) / T;
+  const int b = min(n_rx, t * chunk), e = min(n_rx, b + chunk);
+  int sum = 0;
+  for (int i = b; i < e; ++i) sum += in[i];
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < T; off <<= 1) {
+    const int v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int run = t ? part[t - 1] : 0;
+  for (int i = b; i < e; ++i) {
+    const int v = in[i];
+    out[i] = run;
+    run += v;
+  }
+  if (t == T - 1) out[n_rx] = part[T - 1];
+}
+
+__global__ void k_scatter(const int* recv, int n, int n_rx, int* s) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = recv[i];
+    if (r < 0 || r >= n_rx) continue;
+    s[kOrder + s[kStarts + r] + atomicAdd(&s[kCursor + r], 1)] = i;
+  }
+}
+
+// Insertion sort of each receiver's paths by rank, then the sum in that
+// order: FP64, or compensated FP32 (Neumaier) for SBR_FIELD_FP32.
+__global__ void k_sum(const long long* rank, const double* pf, int n_rx, int precision, int* s,
+                      double* out) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rx; r += gridDim.x * blockDim.x) {
+    int* order = s + kOrder;
+    const int b = s[kStarts + r], e = s[kStarts + r + 1];
+    for (int i = b + 1; i < e; ++i) {
+      const int v = order[i];
+      const long long key = rank[v];
+      int j = i - 1;
+      while (j >= b && rank[order[j]] > key) {
+        order[j + 1] = order[j];
+        --j;
+      }
+      order[j + 1] = v;
+    }
+    if (precision == SBR_FIELD_FP32) {
+      float acc[6] = {0, 0, 0, 0, 0, 0}, c[6] = {0, 0, 0, 0, 0, 0};
+      for (int i = b; i < e; ++i)
+        for (int k = 0; k < 6; ++k) {
+          const float x = float(pf[6 * size_t(order[i]) + k]);
+          const float t = acc[k] + x;
+          c[k] += fabsf(acc[k]) >= fabsf(x) ? (acc[k] - t) + x : (x - t) + acc[k];
+          acc[k] = t;
+        }
+      for (int k = 0; k < 6; ++k) out[6 * size_t(r) + k] = double(acc[k]) + double(c[k]);
+    } else {
+      double acc[6] = {0, 0, 0, 0, 0, 0};
+      for (int i = b; i < e; ++i)
+        for (int k = 0; k < 6; ++k) acc[k] = __dadd_rn(acc[k], pf[6 * size_t(order[i]) + k]);
+      for (int k = 0; k < 6; ++k) out[6 * size_t(r) + k] = acc[k];
+    }
+  }
+}
+
+// Device address of g_scratch, looked up once per device.
+static std::mutex g_mu;
+static int* g_addr[64] = {};
+
+static sbr_status scratch_for_current_device(int** out, std::string& err) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+    return SBR_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= 64) {
+    err = "device index out of range";
+    return SBR_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess || !p) {
+      err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return SBR_ERR_CUDA;
+    }
+    g_addr[dev] = static_cast<int*>(p);
+  }
+  *out = g_addr[dev];
+  return SBR_OK;
+}
+
+}  // namespace noalloc
+// Sets the message sbr_last_error() returns (defined with the other entry points).
+void set_error_message(const std::string& s);
+}  // namespace sbr
+
+extern "C" {
+
+sbr_status sbr_receiver_field_sum_noalloc(const int* path_receiver, const long long* path_rank,
+                                          const double* path_field, int n_paths, int n_rx,
+                                          int field_precision, double* field_out,
+                                          void* stream) {
+  using namespace sbr::noalloc;
+  std::string g_err;
+  struct Report {
+    std::string& m;
+    ~Report() {
+      if (!m.empty()) sbr::set_error_message(m);
+    }
+  } report{g_err};
+  if (n_rx < 1 || n_rx > kMaxRx || n_paths < 0 || n_paths > kMaxPaths) {
+    g_err = "sbr_receiver_field_sum_noalloc: need 1 <= n_rx <= " + std::to_string(kMaxRx) +
+            " and 0 <= n_paths <= " + std::to_string(kMaxPaths) + " (got n_rx=" +
+            std::to_string(n_rx) + ", n_paths=" + std::to_string(n_paths) + ")";
+    return SBR_ERR_INVALID_ARG;
+  }
+  if (!field_out || (n_paths > 0 && (!path_receiver || !path_rank || !path_field))) {
+    g_err = "sbr_receiver_field_sum_noalloc: NULL device pointer";
+    return SBR_ERR_INVALID_ARG;
+  }
+  int* s = nullptr;
+  sbr_status st = scratch_for_current_device(&s, g_err);
+  if (st != SBR_OK) return st;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  const int gb = 152 * 4;
+  k_clear<<<gb, 256, 0, cs>>>(s, n_rx);
+  if (n_paths) k_hist<<<gb, 256, 0, cs>>>(path_receiver, n_paths, n_rx, s);
+  k_scan<<<1, 1024, 0, cs>>>(s, n_rx);
+  if (n_paths) k_scatter<<<gb, 256, 0, cs>>>(path_receiver, n_paths, n_rx, s);
+  k_sum<<<gb, 128, 0, cs>>>(path_rank, path_field, n_rx, field_precision, s, field_out);
+  int bad = 0;
+  cudaError_t e = cudaMemcpyAsync(&bad, s + kError, sizeof(int), cudaMemcpyDeviceToHost, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+  if (e != cudaSuccess) {
+    g_err = std::string("sbr_receiver_field_sum_noalloc: ") + cudaGetErrorString(e);
+    return SBR_ERR_CUDA;
+  }
+  if (bad) {
+    g_err = "sbr_receiver_field_sum_noalloc: a receiver index is outside [0, n_rx)";
+    return SBR_ERR_INVALID_ARG;
+  }
+  return SBR_OK;
+}
+
+}  // extern "C"
