@@ -128,6 +128,120 @@ def cpu_baseline(wl, level: int = 5, threads: int = 0):
                       f"{len(req.rx)} receivers): {seg} segments in {dt:.2f} s"}
 
 
+def batched_workload(seed: int = 0x5B5 + 2, n_tx: int = 256):
+    """256 transmitters on the urban scene: seeded street-level positions,
+    levels U{6..9}, patterns U{Hertzian, half-wave, isotropic}, 5 reflections,
+    4,096 shared receivers on a 64 x 64 grid at 1.5 m."""
+    import numpy as np
+    from sbrsolver_gb300 import scenes
+    wl = scenes.urban_scene()
+    rng = np.random.default_rng(seed)
+    g = -500.0 + (1000.0 / 64) * (np.arange(64) + 0.5)
+    rx = np.array([(x, y, 1.5) for x in g for y in g], np.float64)
+    reqs = []
+    for _ in range(n_tx):
+        # street crossings of the 50 m lattice, 10-40 m high
+        tx = (float(rng.integers(-10, 10) * 50.0), float(rng.integers(-10, 10) * 50.0),
+              float(rng.uniform(10, 40)))
+        reqs.append(scenes.Request(tx=tx, rx=rx, max_reflection=5, max_transmission=0,
+                                   frequency=28e9, tessellation=int(rng.integers(6, 10)),
+                                   antenna=int(rng.integers(0, 3))))
+    return wl, reqs
+
+
+def serving_stream(scene_wls, n: int, seed: int = 0x5B5 + 4):
+    """Request mix on resident scenes: scene uniform, Tx uniform over the
+    scene (2-40 m above its floor), frequency log-uniform 0.9-60 GHz,
+    icosahedron level U{5..10}, receivers log-uniform 100-100k (1.5 m above
+    the floor), 2-8 bounces."""
+    import numpy as np
+    from sbrsolver_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        si = int(rng.integers(0, len(scene_wls)))
+        wl = scene_wls[si]
+        v = wl.scene.tri.reshape(-1, 3)
+        lo, hi = v.min(0), v.max(0)
+        floor = float(wl.request.rx[:, 2].min() - 1.5)
+        nrx = int(round(np.exp(rng.uniform(np.log(100), np.log(100000)))))
+        rx = np.column_stack([rng.uniform(lo[0], hi[0], nrx), rng.uniform(lo[1], hi[1], nrx),
+                              np.full(nrx, floor + 1.5)])
+        tx = (float(rng.uniform(lo[0], hi[0])), float(rng.uniform(lo[1], hi[1])),
+              floor + float(rng.uniform(2, 40)))
+        out.append((si, scenes.Request(
+            tx=tx, rx=rx, max_reflection=int(rng.integers(2, 9)), max_transmission=0,
+            frequency=float(np.exp(rng.uniform(np.log(0.9e9), np.log(60e9)))),
+            tessellation=int(rng.integers(5, 11)), antenna=int(rng.integers(0, 3)))))
+    return out
+
+
+def run_batched(precision: str):
+    from sbrsolver_gb300 import api
+    wl, reqs = batched_workload()
+    sc = api.DeviceScene.from_scene(wl.scene)
+    qs = [api.request_from_workload(r, precision) for r in reqs]
+    api.solve(sc, qs, with_paths=False)  # warm-up: sizes the buffers for the batch
+    t0 = time.perf_counter()
+    seg_plain = 0
+    for q in qs:
+        seg_plain += api.solve(sc, q, with_paths=False).counts["segments"]
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rb = api.solve(sc, qs, with_paths=False)
+    t_batch = time.perf_counter() - t0
+    sc.close()
+    return {"workload": "urban 256 Tx, levels 6-9, R5, 4096 shared receivers",
+            "requests": len(qs), "segments": rb.counts["segments"],
+            "batched": rb.counts["segments"] / t_batch, "plain": seg_plain / t_plain,
+            "unit": "segments/s", "batched_s": t_batch, "plain_s": t_plain,
+            "speedup": (rb.counts["segments"] / t_batch) / (seg_plain / t_plain)}
+
+
+def run_serving(precision: str, n_req: int = 48, rate: float = 20.0, slots: int = 4):
+    import numpy as np
+    from sbrsolver_gb300 import api, scenes
+    wls = [scenes.small_scene(), scenes.urban_scene(), scenes.large_scene()]
+    scs = [api.DeviceScene.from_scene(w.scene) for w in wls]
+    stream = serving_stream(wls, n_req)
+    qs = [(si, api.request_from_workload(r, precision)) for si, r in stream]
+    for si, q in qs[:3]:
+        api.solve(scs[si], q, with_paths=False)  # warm-up
+    # plain: one request at a time
+    t0 = time.perf_counter()
+    seg = 0
+    for si, q in qs:
+        seg += api.solve(scs[si], q, with_paths=False).counts["segments"]
+    plain = seg / (time.perf_counter() - t0)
+    # served: Poisson arrivals at `rate`, `slots` overlapping solves
+    rng = np.random.default_rng(99)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(qs)))
+    srv = api.Server(scs, slots=slots)
+    lat, seg_s, done = [], 0, 0
+    t0 = time.perf_counter()
+    nxt = 0
+    while done < len(qs):
+        now = time.perf_counter() - t0
+        while nxt < len(qs) and arrivals[nxt] <= now:
+            srv.submit(qs[nxt][0], qs[nxt][1], nxt)
+            nxt += 1
+        wait = 5 if nxt < len(qs) else 100
+        for c in srv.poll(timeout_ms=wait):
+            if c["status"] == 0:
+                lat.append(c["latency_ms"])
+                seg_s += c["counts"]["segments"]
+            done += 1
+    makespan = time.perf_counter() - t0
+    srv.close()
+    for sc in scs:
+        sc.close()
+    return {"workload": "config-4 mix on 3 resident scenes (small, urban, large)",
+            "requests": len(qs), "rate_req_s": rate, "slots": slots,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "served": seg_s / makespan, "plain": plain, "unit": "segments/s",
+            "speedup": (seg_s / makespan) / plain, "completed": len(lat)}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -162,6 +276,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--level", type=int, default=9,
                     help="icosahedron level (9 = the benchmark; lower for profiling runs)")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     args = ap.parse_args()
     rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
     dist = None
@@ -274,6 +390,10 @@ def main():
             "gpu_launches": launches_per_step * steps,
             "clocks": clocks,
         }
+        if not args.no_batched and args.level == 9:
+            line["batched"] = run_batched(args.precision)
+        if not args.no_serving and args.level == 9:
+            line["serving"] = run_serving(args.precision)
         if not args.no_cpu_baseline and world == 1:
             try:
                 line["cpu_baseline"] = cpu_baseline(wl)

@@ -164,6 +164,37 @@ sbr_status sbr_result_destroy(sbr_result* result);
 const char* sbr_last_error(void);
 const char* sbr_version(void);
 
+/* ---- request server ------------------------------------------------- */
+/* No reference counterpart (the reference's main() runs one solve).  A
+ * server runs `slots` solves at a time over resident scenes: submitted
+ * requests queue in arrival order and each starts as soon as a slot is free
+ * and its device-memory estimate fits in the HBM budget next to the requests
+ * already running (hbm_budget_bytes <= 0: 60% of free memory at creation).
+ * Requests admitted while others run overlap with them on the GPU (separate
+ * streams); each result equals sbr_solve of that request alone. */
+typedef struct sbr_server sbr_server;
+typedef struct sbr_completion {
+  long long tag;           /* the caller's tag from sbr_server_submit */
+  int status;              /* sbr_status of the solve */
+  int scene;
+  double queue_ms;         /* submit -> start */
+  double latency_ms;       /* submit -> result ready */
+  double device_ms;        /* sbr_timing.device_ms */
+  sbr_counts counts;
+  sbr_result* result;      /* caller destroys with sbr_result_destroy (NULL on error) */
+} sbr_completion;
+sbr_status sbr_server_create(sbr_scene* const* scenes, int n_scenes, int slots,
+                             long long hbm_budget_bytes, sbr_server** out);
+/* Copies the request and its receivers (host memory); returns at once. */
+sbr_status sbr_server_submit(sbr_server* server, int scene, const sbr_request* request,
+                             long long tag);
+/* Up to max finished requests; waits up to timeout_ms when none is ready. */
+sbr_status sbr_server_poll(sbr_server* server, sbr_completion* out, int max, int* n_out,
+                           int timeout_ms);
+sbr_status sbr_server_pending(sbr_server* server, int* queued, long long* in_flight_bytes);
+/* Finishes queued and running requests, then stops. */
+sbr_status sbr_server_destroy(sbr_server* server);
+
 /* ---- allocation-free field sum -------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory (code inside CUDA graph capture, processes whose device memory

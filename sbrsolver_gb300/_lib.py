@@ -20,7 +20,8 @@ EXPORTS = (
     "sbr_scene_set_mesh_order", "sbr_scene_coplanar_ids", "sbr_scene_destroy", "sbr_solve",
     "sbr_solve_batch", "sbr_result_counts", "sbr_result_field", "sbr_result_paths",
     "sbr_result_timing", "sbr_result_destroy", "sbr_last_error", "sbr_version",
-    "sbr_receiver_field_sum_noalloc",
+    "sbr_receiver_field_sum_noalloc", "sbr_server_create", "sbr_server_submit", "sbr_server_poll",
+    "sbr_server_pending", "sbr_server_destroy",
 )
 
 
@@ -64,6 +65,12 @@ class Path(C.Structure):
                 ("field", C.c_double * 6)]
 
 
+class Completion(C.Structure):
+    _fields_ = [("tag", C.c_longlong), ("status", C.c_int), ("scene", C.c_int),
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double), ("device_ms", C.c_double),
+                ("counts", Counts), ("result", C.c_void_p)]
+
+
 class Timing(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("total_ms", "trace_ms", "capture_ms", "correct_ms",
                                            "field_ms", "h2d_ms", "d2h_ms", "device_ms")]
@@ -100,6 +107,11 @@ def load(path: str = LIB_PATH):
             "sbr_result_timing": [vp, P(Timing)],
             "sbr_result_destroy": [vp],
             "sbr_receiver_field_sum_noalloc": [vp, vp, vp, I, I, I, vp, vp],
+            "sbr_server_create": [P(vp), I, I, C.c_longlong, P(vp)],
+            "sbr_server_submit": [vp, I, P(Request), C.c_longlong],
+            "sbr_server_poll": [vp, P(Completion), I, P(I), I],
+            "sbr_server_pending": [vp, P(I), P(C.c_longlong)],
+            "sbr_server_destroy": [vp],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

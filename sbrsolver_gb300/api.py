@@ -241,10 +241,15 @@ def solve(scene: DeviceScene, requests, with_paths: bool = True) -> Result:
     arr = (_lib.Request * len(requests))(*[r[0] for r in requests])
     h = C.c_void_p()
     _lib.check(lib.sbr_solve_batch(scene.handle, arr, len(requests), C.byref(h)))
+    return _collect(h, sum(r[0].n_rx for r in requests), with_paths)
+
+
+def _collect(h, n_rx: int, with_paths: bool) -> Result:
+    """Reads an sbr_result into a Result and destroys it."""
+    lib = _lib.load()
     try:
         cnt = _lib.Counts()
         _lib.check(lib.sbr_result_counts(h, C.byref(cnt)))
-        n_rx = sum(r[0].n_rx for r in requests)
         f = np.zeros(6 * n_rx, np.float64)
         if n_rx:
             _lib.check(lib.sbr_result_field(h, f.ctypes.data_as(C.POINTER(C.c_double))))
@@ -277,6 +282,51 @@ def solve(scene: DeviceScene, requests, with_paths: bool = True) -> Result:
         return Result(field_c, counts, timing, paths)
     finally:
         lib.sbr_result_destroy(h)
+
+
+class Server:
+    """Request server over resident scenes (sbr_server_*): `slots` solves at
+    a time, admitted in arrival order by an HBM budget, overlapping on the GPU."""
+
+    def __init__(self, scenes: Sequence[DeviceScene], slots: int = 4, hbm_budget: int = 0):
+        lib = _lib.load()
+        arr = (C.c_void_p * len(scenes))(*[s.handle.value for s in scenes])
+        h = C.c_void_p()
+        _lib.check(lib.sbr_server_create(arr, len(scenes), int(slots), int(hbm_budget), C.byref(h)))
+        self.handle = h
+        self._lib = lib
+        self._nrx = {}
+
+    def submit(self, scene: int, request: tuple, tag: int) -> None:
+        self._nrx[int(tag)] = request[0].n_rx
+        _lib.check(self._lib.sbr_server_submit(self.handle, int(scene), C.byref(request[0]), int(tag)))
+
+    def poll(self, max_items: int = 64, timeout_ms: int = 50, with_paths: bool = False) -> list:
+        buf = (_lib.Completion * max_items)()
+        n = C.c_int()
+        _lib.check(self._lib.sbr_server_poll(self.handle, buf, max_items, C.byref(n), int(timeout_ms)))
+        out = []
+        for c in buf[:n.value]:
+            item = {"tag": int(c.tag), "status": int(c.status), "scene": int(c.scene),
+                    "queue_ms": c.queue_ms, "latency_ms": c.latency_ms, "device_ms": c.device_ms,
+                    "counts": {k: int(getattr(c.counts, k)) for k, _ in _lib.Counts._fields_},
+                    "result": None}
+            if c.result:
+                item["result"] = _collect(C.c_void_p(c.result), self._nrx.get(int(c.tag), 0),
+                                          with_paths)
+            out.append(item)
+        return out
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.sbr_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class FieldCompute:

@@ -56,6 +56,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
          "-o", os.path.join(obj_dir, "sbr_host.o")],
         [nvcc, *ARCH, *common, "-lineinfo", "-c", os.path.join(CSRC, "sbr_noalloc.cu"),
          "-o", os.path.join(obj_dir, "sbr_noalloc.o")],
+        [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, "sbr_server.cpp"),
+         "-o", os.path.join(obj_dir, "sbr_server.o")],
     ]
     with ThreadPoolExecutor(len(jobs)) as ex:
         outs = list(ex.map(run, jobs))
@@ -63,7 +65,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         print("".join(outs))
     tmp = LIB + ".tmp"
     run([nvcc, *ARCH, "-shared", "-o", tmp, os.path.join(obj_dir, "sbr_engine.o"),
-         os.path.join(obj_dir, "sbr_host.o"), os.path.join(obj_dir, "sbr_noalloc.o")])
+         os.path.join(obj_dir, "sbr_host.o"), os.path.join(obj_dir, "sbr_noalloc.o"),
+         os.path.join(obj_dir, "sbr_server.o")])
     os.replace(tmp, LIB)
     return LIB
 

@@ -891,7 +891,8 @@ __global__ void k_direct(DevScene sc, const TxParams* txp, const double* rx, con
     double d[3];
     x64::sub3(c, tx, d);
     Hit h;
-    const bool has = exact_closest(sc, tx, d, h, &ctr->overflow);
+    TraceStats st{0, 0};
+    const bool has = closest_hit(sc, tx, d, h, st, &ctr->overflow);
     ok[gi] = (!has || x64::norm(d) < h.dist) ? 1 : 0;
   }
 }
@@ -1055,27 +1056,12 @@ __global__ void k_rx_sum(const Survivor* surv, const int* starts, int* order, in
 
 // ============================================================ host side
 
-struct SceneImpl {
-  HostScene host;
-  std::vector<sbr_material> materials;
-  int device = 0;
+// Buffers, stream and capacities of one solve in flight.  A scene keeps a
+// pool of these so that solves issued from several host threads run on
+// separate streams and overlap on the GPU.
+struct Workspace {
   cudaStream_t stream = nullptr;
-  DBuf<Node32> node32;
-  DBuf<RefNode> ref;
-  DBuf<Tri32> tri32;
-  DBuf<Tri64> tri64;
-  DBuf<CorrTri> corr;
-  DBuf<Material> mats;
-  DBuf<int> tri_cop;     // by rank
-  DBuf<int> rank_to_id;
-  DevScene dev{};
-  long long dev_bytes = 0;
-  int n_cop = 0;
-  // launch directions per icosahedron level (0..12), resident once built
-  std::vector<std::unique_ptr<DBuf<double>>> dirs;
-  DBuf<const double*> dir_table;
-  std::mutex mu;
-  // workspace
+  cudaEvent_t ev[8] = {};
   DBuf<TxParams> txp;
   DBuf<double> rx;
   DBuf<int> rx_req;
@@ -1090,18 +1076,59 @@ struct SceneImpl {
   DBuf<ClassInfo> cls_info;
   DBuf<Corrected> corr_list;
   DBuf<unsigned char> direct_ok;
-  DBuf<Tri32> corr32;
   DBuf<Survivor> surv;
   DBuf<int> s_counts, s_starts, s_cursor, s_order;
   DBuf<double> path_field, path_pts, field;
   DBuf<int> path_nray, path_tri, path_cop, path_kind;
   DBuf<Counters> ctr;
-  // capacities (grow on overflow)
-  unsigned long long cap_nodes = 1 << 22, cap_queue = 1 << 21, cap_surv = 1 << 16;
-  unsigned long long cap_corr = 1 << 20;
-  uint32_t cap_cls = 1 << 21, cap_cop = 1 << 19, cap_dd = 1 << 20;
-  cudaEvent_t ev[8] = {};
+  // capacities (grown from occupancy and on overflow)
+  unsigned long long cap_nodes = 1 << 20, cap_queue = 1 << 19, cap_surv = 1 << 14;
+  unsigned long long cap_corr = 1 << 16;
+  uint32_t cap_cls = 1 << 16, cap_cop = 1 << 14, cap_dd = 1 << 14;
+  // occupancy seen per executed segment in earlier solves, used to size the
+  // tables of the next solve before it runs
+  double r_cls = 0, r_cop = 0, r_corr = 0, r_dd = 0, r_surv = 0;
+  ~Workspace() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
 };
+
+struct SceneImpl {
+  HostScene host;
+  std::vector<sbr_material> materials;
+  int device = 0;
+  cudaStream_t stream = nullptr;  // scene uploads
+  DBuf<Node32> node32;
+  DBuf<RefNode> ref;
+  DBuf<Tri32> tri32;
+  DBuf<Tri64> tri64;
+  DBuf<CorrTri> corr;
+  DBuf<Tri32> corr32;
+  DBuf<Material> mats;
+  DBuf<int> tri_cop;     // by rank
+  DBuf<int> rank_to_id;
+  DevScene dev{};
+  long long dev_bytes = 0;
+  int n_cop = 0;
+  // launch directions per icosahedron level (0..12), resident once built
+  std::mutex dirs_mu;
+  std::vector<std::unique_ptr<DBuf<double>>> dirs;
+  DBuf<const double*> dir_table;  // 13 entries, allocated once
+  std::mutex pool_mu;  // held while the mesh order is replaced
+};
+
+// Process-wide pool of idle workspaces per device, shared by all scenes
+// (a workspace holds no scene data).
+struct WorkspacePool {
+  std::mutex mu;
+  std::vector<std::unique_ptr<Workspace>> idle[64];
+};
+static WorkspacePool& ws_pool() {
+  static WorkspacePool* p = new WorkspacePool();  // intentionally never destroyed
+  return *p;
+}
 
 }  // namespace sbr
 
@@ -1258,22 +1285,61 @@ static void upload_mesh_order(SceneImpl& S, const std::vector<int>& order) {
 }
 
 static void ensure_dirs(SceneImpl& S, int level) {
-  if (S.dirs.size() < 13) S.dirs.resize(13);
   if (level < 0 || level > 12) throw std::string("tessellation level must be 0..12");
+  std::lock_guard<std::mutex> lock(S.dirs_mu);
+  if (S.dirs.size() < 13) S.dirs.resize(13);
+  if (!S.dir_table.p) {
+    S.dir_table.ensure(13);
+    CK(cudaMemset(S.dir_table.p, 0, 13 * sizeof(const double*)));
+  }
   if (!S.dirs[level]) {
     std::vector<double> d;
     icosphere(level, d);
     auto b = std::make_unique<DBuf<double>>();
-    b->upload(d.data(), d.size(), S.stream);
+    b->ensure(d.size());
+    CK(cudaMemcpy(b->p, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+    const double* ptr = b->p;
+    CK(cudaMemcpy(S.dir_table.p + level, &ptr, sizeof ptr, cudaMemcpyHostToDevice));
     S.dirs[level] = std::move(b);
   }
-  std::vector<const double*> tab(13, nullptr);
-  for (int l = 0; l < 13; ++l)
-    if (S.dirs[l]) tab[l] = S.dirs[l]->p;
-  S.dir_table.upload(tab.data(), tab.size(), S.stream);
 }
 
 static long long n_launch_of(int level) { return 10LL * (1LL << (2 * level)) + 2; }
+
+// Bounds of one launch's ray tree (RTSolver.cpp:186-221): nodes with r
+// reflections and t transmissions exist for r <= R, t <= T, C(r+t, t) of each.
+static double tree_nodes(int R, int T) {
+  double n = 0;
+  for (int r = 0; r <= R; ++r) {
+    double c = 1;  // C(r + t, t), t = 0
+    for (int t = 0; t <= T; ++t) {
+      n += c;
+      c = c * double(r + t + 1) / double(t + 1);
+    }
+  }
+  return n;
+}
+// widest bounce depth: nodes with r + t = d
+static double tree_width(int R, int T) {
+  double w = 1;
+  for (int d = 0; d <= R + T; ++d) {
+    double n = 0, c = 1;  // C(d, t)
+    for (int t = 0; t <= std::min(d, T); ++t) {
+      if (d - t <= R) n += c;
+      c = c * double(d - t) / double(t + 1);
+    }
+    w = std::max(w, n);
+  }
+  return w;
+}
+// Device bytes a request may need (node records at the tree bound, queues,
+// receivers): used to split batches into passes and to size buffers.
+double request_bytes(const sbr_request& q) {
+  const double L = double(n_launch_of(std::min(std::max(q.tessellation, 0), 12)));
+  const int R = std::max(q.max_reflection, 0), T = std::max(q.max_transmission, 0);
+  return L * tree_nodes(R, T) * (sizeof(NodeHot) + sizeof(NodeCold)) +
+         L * tree_width(R, T) * 2 * sizeof(RayRec) + double(q.n_rx) * 256.0;
+}
 
 static int grid_for(long long n, int block) {
   int dev_sms = 152;
@@ -1295,12 +1361,15 @@ static FieldConsts field_consts() {
   return K;
 }
 
-static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_result& out) {
-  std::lock_guard<std::mutex> lock(S.mu);
-  cudaStream_t st = S.stream;
+static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int n_req,
+                       sbr_result& out) {
+  cudaStream_t st = W.stream;
+  if (S.host.mesh_order.empty()) throw std::string("scene is not initialised");
   CK(cudaSetDevice(S.device));
-  if (!S.ev[0])
-    for (auto& e : S.ev) CK(cudaEventCreate(&e));
+  if (!W.stream) CK(cudaStreamCreateWithFlags(&W.stream, cudaStreamNonBlocking));
+  if (!W.ev[0])
+    for (auto& e : W.ev) CK(cudaEventCreate(&e));
+  st = W.stream;
   // ---- request table
   std::vector<TxParams> tp(n_req);
   long long launches = 0;
@@ -1342,26 +1411,29 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
   const int stage_counts = reqs[0].stage_counts ? 1 : 0;
   if (n_req >= int(0xFFFFFFFFu - kRootBase)) throw std::string("too many requests in one batch");
   auto t0 = std::chrono::steady_clock::now();
-  CK(cudaEventRecord(S.ev[0], st));
-  S.txp.upload(tp.data(), tp.size(), st);
+  CK(cudaEventRecord(W.ev[0], st));
+  W.txp.upload(tp.data(), tp.size(), st);
   // receivers
-  S.rx.ensure(std::max(1, 3 * rx_total));
-  S.direct_ok.ensure(std::max(1, rx_total));
+  W.rx.ensure(std::max(1, 3 * rx_total));
+  W.direct_ok.ensure(std::max(1, rx_total));
   {
     std::vector<int> req_of(std::max(1, rx_total));
     for (int r = 0; r < n_req; ++r) {
       const sbr_request& q = reqs[r];
       if (q.n_rx)
-        CK(cudaMemcpyAsync(S.rx.p + 3 * size_t(tp[r].rx_first), q.rx, 3 * sizeof(double) * q.n_rx,
+        CK(cudaMemcpyAsync(W.rx.p + 3 * size_t(tp[r].rx_first), q.rx, 3 * sizeof(double) * q.n_rx,
                            q.rx_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
       for (int i = 0; i < q.n_rx; ++i) req_of[tp[r].rx_first + i] = r;
     }
-    S.rx_req.upload(req_of.data(), req_of.size(), st);
+    W.rx_req.upload(req_of.data(), req_of.size(), st);
   }
-  CK(cudaEventRecord(S.ev[1], st));
+  CK(cudaEventRecord(W.ev[1], st));
   // ---- receiver grid
-  const int max_cells = 1 << 21;
-  S.gb.ensure(n_req);
+  // cells per request: the grid aims at ~2 receivers per cell
+  int max_cells = 64;
+  for (auto& p : tp) max_cells = std::max(max_cells, 2 * p.n_rx + 64);
+  max_cells = std::min(max_cells, 1 << 21);
+  W.gb.ensure(n_req);
   {
     std::vector<GridBuild> g0(n_req);
     for (auto& g : g0) {
@@ -1373,183 +1445,226 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
       g.cmax = 0;
       g.ncell = 0;
     }
-    CK(cudaMemcpyAsync(S.gb.p, g0.data(), sizeof(GridBuild) * n_req, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(W.gb.p, g0.data(), sizeof(GridBuild) * n_req, cudaMemcpyHostToDevice, st));
   }
-  S.grids.ensure(n_req);
-  S.cell_base.ensure(n_req + 1);
+  W.grids.ensure(n_req);
+  W.cell_base.ensure(n_req + 1);
   const size_t cell_cap = size_t(n_req) * (max_cells + 1) + 1;
-  S.cell_counts.ensure(cell_cap);
-  S.cell_starts.ensure(cell_cap + 1);
-  S.cell_cursor.ensure(cell_cap);
-  S.rx32.ensure(std::max(1, rx_total));
-  CK(cudaMemsetAsync(S.cell_counts.p, 0, sizeof(int) * cell_cap, st));
-  CK(cudaMemsetAsync(S.cell_cursor.p, 0, sizeof(int) * cell_cap, st));
+  W.cell_counts.ensure(cell_cap);
+  W.cell_starts.ensure(cell_cap + 1);
+  W.cell_cursor.ensure(cell_cap);
+  W.rx32.ensure(std::max(1, rx_total));
+  CK(cudaMemsetAsync(W.cell_counts.p, 0, sizeof(int) * cell_cap, st));
+  CK(cudaMemsetAsync(W.cell_cursor.p, 0, sizeof(int) * cell_cap, st));
   int max_rx = 1;
   for (auto& p : tp) max_rx = std::max(max_rx, p.n_rx);
   dim3 rg(std::min(1024, (max_rx + 255) / 256), n_req);
-  k_rx_bounds<<<rg, 256, 0, st>>>(S.rx.p, S.txp.p, n_req, S.gb.p);
-  k_grid_shape<<<1, 1, 0, st>>>(S.gb.p, S.grids.p, S.txp.p, n_req, max_cells, S.cell_base.p);
-  k_rx_count<<<rg, 256, 0, st>>>(S.rx.p, S.txp.p, n_req, S.grids.p, S.cell_base.p, S.cell_counts.p);
-  k_scan_exclusive<<<1, 1024, 0, st>>>(S.cell_counts.p, S.cell_starts.p, int(cell_cap));
-  k_rx_scatter<<<rg, 256, 0, st>>>(S.rx.p, S.txp.p, n_req, S.grids.p, S.cell_base.p,
-                                   S.cell_starts.p, S.cell_cursor.p, S.rx32.p);
-  k_grid_finish<<<(n_req + 127) / 128, 128, 0, st>>>(S.grids.p, S.cell_starts.p, S.cell_base.p,
-                                                    S.rx32.p, n_req);
+  k_rx_bounds<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.gb.p);
+  k_grid_shape<<<1, 1, 0, st>>>(W.gb.p, W.grids.p, W.txp.p, n_req, max_cells, W.cell_base.p);
+  k_rx_count<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p, W.cell_counts.p);
+  k_scan_exclusive<<<1, 1024, 0, st>>>(W.cell_counts.p, W.cell_starts.p, int(cell_cap));
+  k_rx_scatter<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p,
+                                   W.cell_starts.p, W.cell_cursor.p, W.rx32.p);
+  k_grid_finish<<<(n_req + 127) / 128, 128, 0, st>>>(W.grids.p, W.cell_starts.p, W.cell_base.p,
+                                                    W.rx32.p, n_req);
   CK(cudaGetLastError());
 
   const FieldConsts K = field_consts();
+  {
+    // Size node pool and queues at the ray-tree bounds so a pass needs no
+    // re-run (the batch splitter keeps each pass within the memory budget).
+    double nodes = 0, width = 0;
+    for (int r = 0; r < n_req; ++r) {
+      const double L = double(tp[r].n_launch);
+      nodes += L * tree_nodes(tp[r].R, tp[r].T);
+      width += L * tree_width(tp[r].R, tp[r].T);
+    }
+    W.cap_nodes = std::max<unsigned long long>(W.cap_nodes, (unsigned long long)nodes + 1024);
+    W.cap_queue = std::max<unsigned long long>(W.cap_queue, (unsigned long long)width + 1024);
+    // Tables from the occupancy ratios learned so far (hash tables half
+    // full), each limited to 2% of free device memory: past that the solve
+    // grows the table on overflow instead.
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const double cap_bytes = 0.02 * double(free_b);
+    auto pow2 = [](double x, double entry_bytes, double limit) {
+      x = std::min(x, limit / entry_bytes);
+      uint32_t p = 1;
+      while (p < x && p < (1u << 30)) p <<= 1;
+      return p;
+    };
+    W.cap_cls = std::max(W.cap_cls, pow2(2.2 * W.r_cls * nodes, 8 + sizeof(ClassInfo), cap_bytes));
+    W.cap_cop = std::max(W.cap_cop, pow2(2.2 * W.r_cop * nodes, 8, cap_bytes));
+    W.cap_dd = std::max(W.cap_dd, pow2(2.2 * W.r_dd * nodes, 16, cap_bytes));
+    W.cap_corr = std::max<unsigned long long>(
+        W.cap_corr, (unsigned long long)std::min(1.2 * W.r_corr * nodes, cap_bytes / sizeof(Corrected)));
+    W.cap_surv = std::max<unsigned long long>(
+        W.cap_surv, (unsigned long long)std::min(1.2 * W.r_surv * nodes, cap_bytes / 640.0));
+  }
   for (int attempt = 0;; ++attempt) {
     if (attempt > 6) throw std::string("capacity: tables kept overflowing");
-    S.ctr.ensure(1);
-    S.nodes.ensure(S.cap_nodes);
-    S.nodes_cold.ensure(S.cap_nodes);
-    S.q0.ensure(S.cap_queue);
-    S.q1.ensure(S.cap_queue);
-    S.cls_keys.ensure(S.cap_cls);
-    S.cls_info.ensure(S.cap_cls);
-    S.cop_keys.ensure(S.cap_cop);
-    S.corr_list.ensure(S.cap_corr);
-    S.dd_keys.ensure(S.cap_dd);
-    S.dd_rank.ensure(S.cap_dd);
-    S.surv.ensure(S.cap_surv);
-    CK(cudaMemsetAsync(S.ctr.p, 0, sizeof(Counters), st));
+    W.ctr.ensure(1);
+    W.nodes.ensure(W.cap_nodes);
+    W.nodes_cold.ensure(W.cap_nodes);
+    W.q0.ensure(W.cap_queue);
+    W.q1.ensure(W.cap_queue);
+    W.cls_keys.ensure(W.cap_cls);
+    W.cls_info.ensure(W.cap_cls);
+    W.cop_keys.ensure(W.cap_cop);
+    W.corr_list.ensure(W.cap_corr);
+    W.dd_keys.ensure(W.cap_dd);
+    W.dd_rank.ensure(W.cap_dd);
+    W.surv.ensure(W.cap_surv);
+    CK(cudaMemsetAsync(W.ctr.p, 0, sizeof(Counters), st));
     const int fb = 256;
-    k_fill_u64<<<grid_for(S.cap_cls, fb), fb, 0, st>>>(S.cls_keys.p, S.cap_cls, kEmptyKey);
-    k_fill_u64<<<grid_for(S.cap_cop, fb), fb, 0, st>>>(S.cop_keys.p, S.cap_cop, kEmptyKey);
-    k_fill_u64<<<grid_for(S.cap_dd, fb), fb, 0, st>>>(S.dd_keys.p, S.cap_dd, kEmptyKey);
-    k_fill_u64<<<grid_for(S.cap_dd, fb), fb, 0, st>>>(S.dd_rank.p, S.cap_dd, kEmptyKey);
-    CK(cudaEventRecord(S.ev[2], st));
+    k_fill_u64<<<grid_for(W.cap_cls, fb), fb, 0, st>>>(W.cls_keys.p, W.cap_cls, kEmptyKey);
+    k_fill_u64<<<grid_for(W.cap_cop, fb), fb, 0, st>>>(W.cop_keys.p, W.cap_cop, kEmptyKey);
+    k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_keys.p, W.cap_dd, kEmptyKey);
+    k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_rank.p, W.cap_dd, kEmptyKey);
+    CK(cudaEventRecord(W.ev[2], st));
     // ---- trace
     TraceArgs ta;
     ta.sc = S.dev;
-    ta.txp = S.txp.p;
+    ta.txp = W.txp.p;
     ta.n_tx = n_req;
     ta.dirs = S.dir_table.p;
-    ta.nodes = S.nodes.p;
-    ta.nodes_cold = S.nodes_cold.p;
-    ta.node_cap = S.cap_nodes;
-    ta.out_cap = S.cap_queue;
-    ta.cls_tab = HashTable{S.cls_keys.p, S.cap_cls - 1};
-    ta.cop_tab = HashTable{S.cop_keys.p, S.cap_cop - 1};
-    ta.cls_info = S.cls_info.p;
+    ta.nodes = W.nodes.p;
+    ta.nodes_cold = W.nodes_cold.p;
+    ta.node_cap = W.cap_nodes;
+    ta.out_cap = W.cap_queue;
+    ta.cls_tab = HashTable{W.cls_keys.p, W.cap_cls - 1};
+    ta.cop_tab = HashTable{W.cop_keys.p, W.cap_cop - 1};
+    ta.cls_info = W.cls_info.p;
     ta.tri_cop = S.tri_cop.p;
-    ta.ctr = S.ctr.p;
+    ta.ctr = W.ctr.p;
     ta.n_root = launches;
     for (int d = 0; d <= max_depth; ++d) {
       ta.depth = d;
-      ta.in = (d % 2 == 0) ? S.q1.p : S.q0.p;
-      ta.out = (d % 2 == 0) ? S.q0.p : S.q1.p;
-      const long long width = d == 0 ? launches : (long long)std::min<unsigned long long>(S.cap_queue, 1ull << 40);
+      ta.in = (d % 2 == 0) ? W.q1.p : W.q0.p;
+      ta.out = (d % 2 == 0) ? W.q0.p : W.q1.p;
+      const long long width = d == 0 ? launches : (long long)std::min<unsigned long long>(W.cap_queue, 1ull << 40);
       k_trace<<<grid_for(width, 128), 128, 0, st>>>(ta);
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(S.ev[3], st));
+    CK(cudaEventRecord(W.ev[3], st));
     // ---- capture
     CaptureArgs ca;
     ca.sc = S.dev;
-    ca.nodes = S.nodes.p;
-    ca.nodes_cold = S.nodes_cold.p;
-    ca.txp = S.txp.p;
-    ca.grids = S.grids.p;
-    ca.gb = S.gb.p;
-    ca.rx = S.rx.p;
-    ca.cls_info = S.cls_info.p;
-    ca.direct_ok = S.direct_ok.p;
-    ca.corr_list = S.corr_list.p;
-    ca.corr_cap = S.cap_corr;
-    ca.ctr = S.ctr.p;
-    ca.node_cap = S.cap_nodes;
+    ca.nodes = W.nodes.p;
+    ca.nodes_cold = W.nodes_cold.p;
+    ca.txp = W.txp.p;
+    ca.grids = W.grids.p;
+    ca.gb = W.gb.p;
+    ca.rx = W.rx.p;
+    ca.cls_info = W.cls_info.p;
+    ca.direct_ok = W.direct_ok.p;
+    ca.corr_list = W.corr_list.p;
+    ca.corr_cap = W.cap_corr;
+    ca.ctr = W.ctr.p;
+    ca.node_cap = W.cap_nodes;
     ca.stage_counts = stage_counts;
     if (rx_total)
-      k_direct<<<grid_for(rx_total, 64), 64, 0, st>>>(S.dev, S.txp.p, S.rx.p, S.rx_req.p, rx_total,
-                                                      S.direct_ok.p, S.ctr.p);
+      k_direct<<<grid_for(rx_total, 64), 64, 0, st>>>(S.dev, W.txp.p, W.rx.p, W.rx_req.p, rx_total,
+                                                      W.direct_ok.p, W.ctr.p);
     k_capture<<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(S.ev[4], st));
+    CK(cudaEventRecord(W.ev[4], st));
     // ---- duplicate removal over the corrected captures
-    const HashTable dd{S.dd_keys.p, S.cap_dd - 1};
-    k_dedup<<<grid_for(S.cap_corr, 256), 256, 0, st>>>(S.corr_list.p, S.cap_corr, S.cls_info.p,
-                                                       dd, S.dd_rank.p, S.ctr.p);
-    k_select<<<grid_for(S.cap_corr, 256), 256, 0, st>>>(S.corr_list.p, S.cap_corr, S.cls_info.p,
-                                                        dd, S.dd_rank.p, S.surv.p, S.cap_surv,
-                                                        S.ctr.p);
+    const HashTable dd{W.dd_keys.p, W.cap_dd - 1};
+    k_dedup<<<grid_for(W.cap_corr, 256), 256, 0, st>>>(W.corr_list.p, W.cap_corr, W.cls_info.p,
+                                                       dd, W.dd_rank.p, W.ctr.p);
+    k_select<<<grid_for(W.cap_corr, 256), 256, 0, st>>>(W.corr_list.p, W.cap_corr, W.cls_info.p,
+                                                        dd, W.dd_rank.p, W.surv.p, W.cap_surv,
+                                                        W.ctr.p);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(S.ev[5], st));
+    CK(cudaEventRecord(W.ev[5], st));
     Counters c;
-    CK(cudaMemcpyAsync(&c, S.ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&c, W.ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (c.overflow & kOvStack) throw std::string("BVH deeper than the traversal stack");
     // keep every hash table at most half full for the next solve
     auto grow = [](uint32_t& cap, unsigned long long used) {
       while (used * 2 > cap && cap < (1u << 30)) cap *= 2;
     };
-    grow(S.cap_cls, c.used_cls);
-    grow(S.cap_cop, c.used_cop);
-    grow(S.cap_dd, c.used_dd);
+    grow(W.cap_cls, c.used_cls);
+    grow(W.cap_cop, c.used_cop);
+    grow(W.cap_dd, c.used_dd);
     if (c.overflow) {
-      if (c.overflow & kOvNodes) S.cap_nodes = std::max(S.cap_nodes * 2, c.nodes + c.nodes / 8);
+      if (c.overflow & kOvNodes) W.cap_nodes = std::max(W.cap_nodes * 2, c.nodes + c.nodes / 8);
       if (c.overflow & kOvQueue) {
         unsigned long long mx = 0;
         for (auto v : c.queue) mx = std::max(mx, v);
-        S.cap_queue = std::max(S.cap_queue * 2, mx + mx / 8);
+        W.cap_queue = std::max(W.cap_queue * 2, mx + mx / 8);
       }
-      if (c.overflow & kOvClass) S.cap_cls *= 4;
-      if (c.overflow & kOvCop) S.cap_cop *= 4;
-      if (c.overflow & kOvCorr) S.cap_corr = std::max(S.cap_corr * 2, c.corrected + c.corrected / 4);
-      if (c.overflow & kOvDedup) S.cap_dd *= 4;
-      if (c.overflow & kOvSurv) S.cap_surv = next_pow2(c.survivors + c.survivors / 4);
+      if (c.overflow & kOvClass) W.cap_cls *= 4;
+      if (c.overflow & kOvCop) W.cap_cop *= 4;
+      if (c.overflow & kOvCorr) W.cap_corr = std::max(W.cap_corr * 2, c.corrected + c.corrected / 4);
+      if (c.overflow & kOvDedup) W.cap_dd *= 4;
+      if (c.overflow & kOvSurv) W.cap_surv = next_pow2(c.survivors + c.survivors / 4);
       continue;
+    }
+    if (c.nodes) {
+      // ratios of this solve, per bound node (what the next pre-sizing multiplies)
+      double bound = 0;
+      for (int r = 0; r < n_req; ++r) bound += double(tp[r].n_launch) * tree_nodes(tp[r].R, tp[r].T);
+      const double n = std::max(1.0, bound);
+      auto upd = [](double& r, double v) { r = std::max(0.9 * r, v); };
+      upd(W.r_cls, c.used_cls / n);
+      upd(W.r_cop, c.used_cop / n);
+      upd(W.r_dd, c.used_dd / n);
+      upd(W.r_corr, c.corrected / n);
+      upd(W.r_surv, c.survivors / n);
     }
     // ---- field + ordered per-receiver sum
     const unsigned long long ns = c.survivors;
     const size_t nsa = std::max<size_t>(1, ns);
-    S.path_field.ensure(6 * nsa);
-    S.path_nray.ensure(nsa);
-    S.path_tri.ensure(nsa * (kMaxDepth + 1));
-    S.path_cop.ensure(nsa * (kMaxDepth + 1));
-    S.path_kind.ensure(nsa * (kMaxDepth + 1));
-    S.path_pts.ensure(nsa * (kMaxDepth + 2) * 3);
-    S.field.ensure(std::max(1, 6 * rx_total));
-    S.s_counts.ensure(rx_total + 1);
-    S.s_starts.ensure(rx_total + 2);
-    S.s_cursor.ensure(rx_total + 1);
-    S.s_order.ensure(nsa);
+    W.path_field.ensure(6 * nsa);
+    W.path_nray.ensure(nsa);
+    W.path_tri.ensure(nsa * (kMaxDepth + 1));
+    W.path_cop.ensure(nsa * (kMaxDepth + 1));
+    W.path_kind.ensure(nsa * (kMaxDepth + 1));
+    W.path_pts.ensure(nsa * (kMaxDepth + 2) * 3);
+    W.field.ensure(std::max(1, 6 * rx_total));
+    W.s_counts.ensure(rx_total + 1);
+    W.s_starts.ensure(rx_total + 2);
+    W.s_cursor.ensure(rx_total + 1);
+    W.s_order.ensure(nsa);
     FieldArgs fa;
     fa.sc = S.dev;
-    fa.txp = S.txp.p;
-    fa.rx = S.rx.p;
-    fa.rx_req = S.rx_req.p;
-    fa.cls_info = S.cls_info.p;
+    fa.txp = W.txp.p;
+    fa.rx = W.rx.p;
+    fa.rx_req = W.rx_req.p;
+    fa.cls_info = W.cls_info.p;
     fa.rank_to_id = S.rank_to_id.p;
-    fa.surv = S.surv.p;
-    fa.ctr = S.ctr.p;
-    fa.cap = S.cap_surv;
+    fa.surv = W.surv.p;
+    fa.ctr = W.ctr.p;
+    fa.cap = W.cap_surv;
     fa.K = K;
     fa.precision = precision;
-    fa.path_field = S.path_field.p;
-    fa.path_nray = S.path_nray.p;
-    fa.path_tri = S.path_tri.p;
-    fa.path_cop = S.path_cop.p;
-    fa.path_kind = S.path_kind.p;
-    fa.path_pts = S.path_pts.p;
+    fa.path_field = W.path_field.p;
+    fa.path_nray = W.path_nray.p;
+    fa.path_tri = W.path_tri.p;
+    fa.path_cop = W.path_cop.p;
+    fa.path_kind = W.path_kind.p;
+    fa.path_pts = W.path_pts.p;
     if (ns) k_field<<<grid_for(ns, 64), 64, 0, st>>>(fa);
-    CK(cudaMemsetAsync(S.s_counts.p, 0, sizeof(int) * (rx_total + 1), st));
-    CK(cudaMemsetAsync(S.s_cursor.p, 0, sizeof(int) * (rx_total + 1), st));
-    if (ns) k_surv_hist<<<grid_for(ns, 256), 256, 0, st>>>(S.surv.p, S.ctr.p, S.cap_surv, S.s_counts.p);
-    k_scan_exclusive<<<1, 1024, 0, st>>>(S.s_counts.p, S.s_starts.p, rx_total);
+    CK(cudaMemsetAsync(W.s_counts.p, 0, sizeof(int) * (rx_total + 1), st));
+    CK(cudaMemsetAsync(W.s_cursor.p, 0, sizeof(int) * (rx_total + 1), st));
+    if (ns) k_surv_hist<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv, W.s_counts.p);
+    k_scan_exclusive<<<1, 1024, 0, st>>>(W.s_counts.p, W.s_starts.p, rx_total);
     if (ns)
-      k_surv_scatter<<<grid_for(ns, 256), 256, 0, st>>>(S.surv.p, S.ctr.p, S.cap_surv,
-                                                        S.s_starts.p, S.s_cursor.p, S.s_order.p);
+      k_surv_scatter<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv,
+                                                        W.s_starts.p, W.s_cursor.p, W.s_order.p);
     if (rx_total)
-      k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(S.surv.p, S.s_starts.p, S.s_order.p,
-                                                        rx_total, S.path_field.p, precision,
-                                                        S.field.p);
+      k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
+                                                        rx_total, W.path_field.p, precision,
+                                                        W.field.p);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(S.ev[6], st));
+    CK(cudaEventRecord(W.ev[6], st));
     // ---- results to the host
     out.field.resize(6 * size_t(rx_total));
     if (rx_total)
-      CK(cudaMemcpyAsync(out.field.data(), S.field.p, sizeof(double) * 6 * rx_total,
+      CK(cudaMemcpyAsync(out.field.data(), W.field.p, sizeof(double) * 6 * rx_total,
                          cudaMemcpyDeviceToHost, st));
     std::vector<int> order(ns), nray(ns), starts(rx_total + 1);
     std::vector<Survivor> sv(ns);
@@ -1557,16 +1672,16 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     std::vector<int> ptri(ns * (kMaxDepth + 1)), pcop(ns * (kMaxDepth + 1)),
         pkind(ns * (kMaxDepth + 1));
     if (ns) {
-      CK(cudaMemcpyAsync(order.data(), S.s_order.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(nray.data(), S.path_nray.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(sv.data(), S.surv.p, sizeof(Survivor) * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pf.data(), S.path_field.p, sizeof(double) * 6 * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(ptri.data(), S.path_tri.p, sizeof(int) * ptri.size(), cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pcop.data(), S.path_cop.p, sizeof(int) * pcop.size(), cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pkind.data(), S.path_kind.p, sizeof(int) * pkind.size(), cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pts.data(), S.path_pts.p, sizeof(double) * pts.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(order.data(), W.s_order.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(nray.data(), W.path_nray.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(sv.data(), W.surv.p, sizeof(Survivor) * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pf.data(), W.path_field.p, sizeof(double) * 6 * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(ptri.data(), W.path_tri.p, sizeof(int) * ptri.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pcop.data(), W.path_cop.p, sizeof(int) * pcop.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pkind.data(), W.path_kind.p, sizeof(int) * pkind.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pts.data(), W.path_pts.p, sizeof(double) * pts.size(), cudaMemcpyDeviceToHost, st));
     }
-    CK(cudaEventRecord(S.ev[7], st));
+    CK(cudaEventRecord(W.ev[7], st));
     CK(cudaStreamSynchronize(st));
     // assemble paths in receiver order, then (launch, BFS) order
     std::vector<int> req_of(rx_total);
@@ -1614,7 +1729,7 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     out.counts.groups = -1;
     out.counts.keys = (long long)c.used_dd;
     float ms[8] = {};
-    for (int i = 1; i < 8; ++i) CK(cudaEventElapsedTime(&ms[i], S.ev[i - 1], S.ev[i]));
+    for (int i = 1; i < 8; ++i) CK(cudaEventElapsedTime(&ms[i], W.ev[i - 1], W.ev[i]));
     out.timing.h2d_ms = ms[1];
     out.timing.trace_ms = ms[3];
     out.timing.capture_ms = ms[4];
@@ -1622,8 +1737,8 @@ static void solve_impl(SceneImpl& S, const sbr_request* reqs, int n_req, sbr_res
     out.timing.field_ms = ms[6];
     out.timing.d2h_ms = ms[7];
     float all = 0, dev = 0;
-    CK(cudaEventElapsedTime(&all, S.ev[0], S.ev[7]));
-    CK(cudaEventElapsedTime(&dev, S.ev[1], S.ev[6]));
+    CK(cudaEventElapsedTime(&all, W.ev[0], W.ev[7]));
+    CK(cudaEventElapsedTime(&dev, W.ev[1], W.ev[6]));
     out.timing.total_ms = all;
     out.timing.device_ms = dev;
     (void)t0;
@@ -1751,7 +1866,8 @@ sbr_status sbr_scene_set_mesh_order(sbr_scene* scene, const int* order) {
     }
   }
   ABI_GUARD({
-    std::lock_guard<std::mutex> lock(scene->impl.mu);
+    // not to be called while solves on this scene are in flight
+    std::lock_guard<std::mutex> lock(scene->impl.pool_mu);
     scene->impl.host.mesh_order = o;
     upload_mesh_order(scene->impl, o);
     return SBR_OK;
@@ -1769,9 +1885,9 @@ sbr_status sbr_scene_coplanar_ids(const sbr_scene* scene, int* out) {
 
 sbr_status sbr_scene_destroy(sbr_scene* scene) {
   if (!scene) return SBR_OK;
+  // solves hold a workspace until they return; destroying a scene while a
+  // solve on it is running is the caller's error
   if (scene->impl.stream) cudaStreamSynchronize(scene->impl.stream);
-  for (auto& e : scene->impl.ev)
-    if (e) cudaEventDestroy(e);
   cudaStream_t st = scene->impl.stream;
   delete scene;
   if (st) cudaStreamDestroy(st);
@@ -1786,8 +1902,66 @@ sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_
   }
   *out = nullptr;
   ABI_GUARD({
+    SceneImpl& S = scene->impl;
+    CK(cudaSetDevice(S.device));
+    WorkspacePool& pool = ws_pool();
+    const int dev = S.device & 63;
+    std::unique_ptr<Workspace> W;
+    {
+      std::lock_guard<std::mutex> lock(pool.mu);
+      if (!pool.idle[dev].empty()) {
+        W = std::move(pool.idle[dev].back());
+        pool.idle[dev].pop_back();
+      }
+    }
+    if (!W) W = std::make_unique<Workspace>();
+    struct Return {
+      WorkspacePool& pool;
+      int dev;
+      std::unique_ptr<Workspace>& W;
+      ~Return() {
+        std::lock_guard<std::mutex> lock(pool.mu);
+        pool.idle[dev].push_back(std::move(W));
+      }
+    } give_back{pool, dev, W};
+    // Split the batch into device passes whose estimated footprint (node
+    // records, queues, receivers) fits in 60% of the free device memory.
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const double budget = std::max(2e9, 0.45 * double(free_b));
+    auto est = [](const sbr_request& q) { return request_bytes(q); };
     auto res = std::make_unique<sbr_result>();
-    solve_impl(scene->impl, requests, n_requests, *res);
+    int first = 0;
+    while (first < n_requests) {
+      int last = first + 1;
+      double acc = est(requests[first]);
+      while (last < n_requests && acc + est(requests[last]) <= budget) acc += est(requests[last++]);
+      if (first == 0 && last == n_requests) {
+        solve_impl(S, *W, requests, n_requests, *res);
+        break;
+      }
+      sbr_result part;
+      solve_impl(S, *W, requests + first, last - first, part);
+      const long long ray_base = (long long)res->tri.size();
+      for (sbr_path p : part.paths) {
+        p.request += first;
+        p.ray_offset += ray_base;
+        res->paths.push_back(p);
+      }
+      res->field.insert(res->field.end(), part.field.begin(), part.field.end());
+      res->tri.insert(res->tri.end(), part.tri.begin(), part.tri.end());
+      res->cop.insert(res->cop.end(), part.cop.begin(), part.cop.end());
+      res->kind.insert(res->kind.end(), part.kind.begin(), part.kind.end());
+      res->points.insert(res->points.end(), part.points.begin(), part.points.end());
+      long long* a = &res->counts.segments;
+      const long long* b = &part.counts.segments;
+      for (size_t k = 0; k < sizeof(sbr_counts) / sizeof(long long); ++k)
+        a[k] = (first == 0 || a[k] < 0 || b[k] < 0) ? (first == 0 ? b[k] : -1) : a[k] + b[k];
+      double* ta = &res->timing.total_ms;
+      const double* tb = &part.timing.total_ms;
+      for (size_t k = 0; k < sizeof(sbr_timing) / sizeof(double); ++k) ta[k] += tb[k];
+      first = last;
+    }
     *out = res.release();
     return SBR_OK;
   })

@@ -1,0 +1,215 @@
+// Request server: continuous admission of propagation solves on resident
+// scenes (no reference counterpart; the reference solves one transmitter per
+// call from main()).
+//
+// A server owns `slots` worker threads.  Submitted requests (copied, with
+// their receivers) wait in one FIFO queue.  A worker takes the head request
+// as soon as (a) the worker is free and (b) the request's device-memory
+// estimate fits in the HBM budget next to the requests already running.  It
+// then runs sbr_solve, which checks a workspace (buffers + CUDA stream) out
+// of the process-wide pool, so requests admitted while others are on the GPU
+// run on their own streams and overlap with them on the device.  Each
+// result is exactly what sbr_solve returns for that request alone: requests
+// share only read-only scene data.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sbr.h"
+
+namespace sbr {
+void set_error_message(const std::string& s);
+double request_bytes(const sbr_request& q);  // device bytes a request may need
+}
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Job {
+  long long tag;
+  int scene;
+  sbr_request req;
+  std::vector<double> rx;
+  long long est_bytes;
+  Clock::time_point submitted;
+};
+
+// Device memory one request may need (node records at the ray-tree bound,
+// queues, receivers, plus tables); it only gates admission.
+long long estimate_bytes(const sbr_request& q) {
+  return (long long)sbr::request_bytes(q) + (64LL << 20);
+}
+
+}  // namespace
+
+struct sbr_server {
+  std::vector<sbr_scene*> scenes;
+  long long budget = 0;
+  long long in_flight = 0;
+  bool stopping = false;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Job> queue;
+  std::deque<sbr_completion> done;
+  std::vector<std::thread> workers;
+  int device = 0;
+
+  void worker() {
+    cudaSetDevice(device);
+    for (;;) {
+      Job job;
+      {
+        std::unique_lock<std::mutex> lock(mu);
+        cv_work.wait(lock, [&] {
+          if (stopping && queue.empty()) return true;
+          if (queue.empty()) return false;
+          const long long need = std::min(queue.front().est_bytes, budget);
+          return in_flight == 0 || in_flight + need <= budget;
+        });
+        if (queue.empty()) return;
+        job = std::move(queue.front());
+        queue.pop_front();
+        in_flight += std::min(job.est_bytes, budget);
+      }
+      cv_work.notify_all();
+      const Clock::time_point start = Clock::now();
+      job.req.rx = job.rx.empty() ? nullptr : job.rx.data();
+      job.req.rx_on_device = 0;
+      sbr_result* res = nullptr;
+      const sbr_status st = sbr_solve(scenes[job.scene], &job.req, &res);
+      const Clock::time_point end = Clock::now();
+      sbr_completion c;
+      std::memset(&c, 0, sizeof c);
+      c.tag = job.tag;
+      c.scene = job.scene;
+      c.status = st;
+      c.queue_ms = std::chrono::duration<double, std::milli>(start - job.submitted).count();
+      c.latency_ms = std::chrono::duration<double, std::milli>(end - job.submitted).count();
+      c.result = res;
+      if (res) {
+        sbr_timing t;
+        sbr_result_timing(res, &t);
+        c.device_ms = t.device_ms;
+        sbr_result_counts(res, &c.counts);
+      }
+      {
+        std::lock_guard<std::mutex> lock(mu);
+        in_flight -= std::min(job.est_bytes, budget);
+        done.push_back(c);
+      }
+      cv_work.notify_all();
+      cv_done.notify_all();
+    }
+  }
+};
+
+extern "C" {
+
+sbr_status sbr_server_create(sbr_scene* const* scenes, int n_scenes, int slots,
+                             long long hbm_budget_bytes, sbr_server** out) {
+  if (!scenes || n_scenes <= 0 || slots <= 0 || slots > 64 || !out) {
+    sbr::set_error_message("sbr_server_create: need scenes, 1..64 slots and an output pointer");
+    return SBR_ERR_INVALID_ARG;
+  }
+  for (int i = 0; i < n_scenes; ++i)
+    if (!scenes[i]) {
+      sbr::set_error_message("sbr_server_create: NULL scene");
+      return SBR_ERR_INVALID_ARG;
+    }
+  auto srv = std::make_unique<sbr_server>();
+  srv->scenes.assign(scenes, scenes + n_scenes);
+  cudaGetDevice(&srv->device);
+  if (hbm_budget_bytes <= 0) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      sbr::set_error_message("sbr_server_create: cudaMemGetInfo failed");
+      return SBR_ERR_CUDA;
+    }
+    hbm_budget_bytes = (long long)(0.6 * double(free_b));
+  }
+  srv->budget = hbm_budget_bytes;
+  for (int i = 0; i < slots; ++i) srv->workers.emplace_back(&sbr_server::worker, srv.get());
+  *out = srv.release();
+  return SBR_OK;
+}
+
+sbr_status sbr_server_submit(sbr_server* srv, int scene, const sbr_request* req, long long tag) {
+  if (!srv || !req || scene < 0 || scene >= int(srv->scenes.size()) || req->n_rx < 0 ||
+      (req->n_rx > 0 && !req->rx) || req->rx_on_device) {
+    sbr::set_error_message("sbr_server_submit: bad arguments (receivers must be host memory)");
+    return SBR_ERR_INVALID_ARG;
+  }
+  Job job;
+  job.tag = tag;
+  job.scene = scene;
+  job.req = *req;
+  job.rx.assign(req->rx, req->rx + 3 * size_t(req->n_rx));
+  job.est_bytes = estimate_bytes(*req);
+  job.submitted = Clock::now();
+  {
+    std::lock_guard<std::mutex> lock(srv->mu);
+    if (srv->stopping) {
+      sbr::set_error_message("sbr_server_submit: server is shutting down");
+      return SBR_ERR_NOT_READY;
+    }
+    srv->queue.push_back(std::move(job));
+  }
+  srv->cv_work.notify_one();
+  return SBR_OK;
+}
+
+sbr_status sbr_server_poll(sbr_server* srv, sbr_completion* out, int max, int* n_out,
+                           int timeout_ms) {
+  if (!srv || !out || max <= 0 || !n_out) {
+    sbr::set_error_message("sbr_server_poll: bad arguments");
+    return SBR_ERR_INVALID_ARG;
+  }
+  std::unique_lock<std::mutex> lock(srv->mu);
+  if (srv->done.empty() && timeout_ms > 0)
+    srv->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms),
+                          [&] { return !srv->done.empty(); });
+  int n = 0;
+  while (n < max && !srv->done.empty()) {
+    out[n++] = srv->done.front();
+    srv->done.pop_front();
+  }
+  *n_out = n;
+  return SBR_OK;
+}
+
+sbr_status sbr_server_pending(sbr_server* srv, int* queued, long long* in_flight_bytes) {
+  if (!srv) {
+    sbr::set_error_message("sbr_server_pending: NULL server");
+    return SBR_ERR_INVALID_ARG;
+  }
+  std::lock_guard<std::mutex> lock(srv->mu);
+  if (queued) *queued = int(srv->queue.size());
+  if (in_flight_bytes) *in_flight_bytes = srv->in_flight;
+  return SBR_OK;
+}
+
+sbr_status sbr_server_destroy(sbr_server* srv) {
+  if (!srv) return SBR_OK;
+  {
+    std::lock_guard<std::mutex> lock(srv->mu);
+    srv->stopping = true;
+  }
+  srv->cv_work.notify_all();
+  for (auto& t : srv->workers) t.join();
+  for (auto& c : srv->done)
+    if (c.result) sbr_result_destroy(c.result);
+  delete srv;
+  return SBR_OK;
+}
+
+}  // extern "C"

@@ -309,3 +309,124 @@ def write_oracle_case(wl: Workload, directory: str, antenna: int | None = None) 
         fh.write(f"tess {rq.tessellation}\nantenna {rq.antenna if antenna is None else antenna}\n")
         fh.write("freq %.17g\npt %.17g\nfresnel %d\n" % (rq.frequency, rq.pt, int(rq.use_fresnel)))
     return case
+
+
+def _diamond_square(n: int, rng: np.random.Generator, roughness: float = 0.55) -> np.ndarray:
+    """(n+1) x (n+1) fractal height field (diamond-square, Fournier et al. 1982),
+    n a power of two, values scaled to [-1, 1]."""
+    h = np.zeros((n + 1, n + 1), np.float64)
+    h[0, 0], h[0, n], h[n, 0], h[n, n] = rng.uniform(-1, 1, 4)
+    step, amp = n, 1.0
+    while step > 1:
+        half = step // 2
+        # diamond: centres of squares
+        c = (h[0:-1:step, 0:-1:step] + h[step::step, 0:-1:step] + h[0:-1:step, step::step] +
+             h[step::step, step::step]) / 4.0
+        h[half::step, half::step] = c + rng.uniform(-amp, amp, c.shape)
+        # square: edge midpoints (average of available neighbours)
+        for (i0, j0) in ((0, half), (half, 0)):
+            ii, jj = np.meshgrid(np.arange(i0, n + 1, step), np.arange(j0, n + 1, step), indexing="ij")
+            acc = np.zeros(ii.shape)
+            cnt = np.zeros(ii.shape)
+            for di, dj in ((-half, 0), (half, 0), (0, -half), (0, half)):
+                a, b = ii + di, jj + dj
+                m = (a >= 0) & (a <= n) & (b >= 0) & (b <= n)
+                acc[m] += h[a[m], b[m]]
+                cnt[m] += 1
+            h[ii, jj] = acc / cnt + rng.uniform(-amp, amp, ii.shape)
+        step, amp = half, amp * roughness
+    h -= h.min()
+    h /= max(h.max(), 1e-12)
+    return 2.0 * h - 1.0
+
+
+def large_scene(seed: int = 0x5B5 + 3, level: int = 10, n_rx: int = 50000,
+                max_reflection: int = 8, cells: int = 512, spacing: float = 2.0,
+                n_poly: int = 2000) -> Workload:
+    """Large scene for the precision study: a cells x cells fractal terrain
+    (diamond-square, +/-20 m relief, `spacing` m grid: 2*cells^2 triangles)
+    plus n_poly extruded convex polygons (4-12 sides, circumradius U(5,15) m,
+    heights lognormal(mu=3, sigma=0.5) m) standing on it; half-wave Tx at
+    3.5 GHz 30 m above the centre, level-10 icosahedron (10,485,762 rays),
+    8 reflections, n_rx receivers 1.5 m above the terrain at seeded
+    positions.  With the defaults: 524,288 + the polygons' triangles."""
+    rng = np.random.default_rng(seed)
+    f = 3.5e9
+    H = 20.0 * _diamond_square(cells, rng)
+    half = cells * spacing / 2.0
+    xs = -half + spacing * np.arange(cells + 1)
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    V = np.stack([X, Y, H], -1).astype(np.float32)
+
+    def height(x, y):
+        gx = np.clip((x + half) / spacing, 0, cells - 1e-6)
+        gy = np.clip((y + half) / spacing, 0, cells - 1e-6)
+        i, j = np.floor(gx).astype(int), np.floor(gy).astype(int)
+        fx, fy = gx - i, gy - j
+        return ((1 - fx) * (1 - fy) * H[i, j] + fx * (1 - fy) * H[i + 1, j] +
+                (1 - fx) * fy * H[i, j + 1] + fx * fy * H[i + 1, j + 1])
+
+    # terrain: two triangles per cell, normals from the float vertices
+    a = V[:-1, :-1].reshape(-1, 3)
+    b = V[1:, :-1].reshape(-1, 3)
+    c = V[1:, 1:].reshape(-1, 3)
+    d = V[:-1, 1:].reshape(-1, 3)
+    t1 = np.stack([a, b, c], 1)
+    t2 = np.stack([a, c, d], 1)
+    tri = np.concatenate([t1, t2], 0).astype(np.float32)
+
+    def normals(t):
+        t = t.astype(np.float64)
+        nrm = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+        nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-30)
+        return nrm.astype(np.float32)
+
+    tris, nrms, mats = [tri], [normals(tri)], [np.zeros(len(tri), np.int32)]
+    tx = (0.0, 0.0, float(height(np.array(0.0), np.array(0.0))) + 30.0)
+    mb = _MeshBuilder()
+    for _ in range(n_poly):
+        while True:
+            cx, cy = rng.uniform(-half + 20, half - 20, 2)
+            if (cx - tx[0]) ** 2 + (cy - tx[1]) ** 2 > 30.0 ** 2:
+                break
+        k = int(rng.integers(4, 13))
+        r = rng.uniform(5.0, 15.0)
+        ang = np.sort(rng.uniform(0, 2 * np.pi, k))
+        px, py = cx + r * np.cos(ang), cy + r * np.sin(ang)
+        hgt = float(np.exp(rng.normal(3.0, 0.5)))
+        z0 = float(min(height(px, py).min(), height(np.array(cx), np.array(cy)))) - 0.5
+        z1 = z0 + hgt
+        P = [(float(np.float32(x)), float(np.float32(y))) for x, y in zip(px, py)]
+        z0, z1 = float(np.float32(z0)), float(np.float32(z1))
+        mat = 1 + int(rng.integers(0, 2))
+        for i in range(k):
+            (x0, y0), (x1, y1) = P[i], P[(i + 1) % k]
+            nx, ny = (y1 - y0), -(x1 - x0)
+            ln = max((nx * nx + ny * ny) ** 0.5, 1e-12)
+            mb.quad((x0, y0, z0), (x1, y1, z0), (x1, y1, z1), (x0, y0, z1), (nx / ln, ny / ln, 0.0), mat)
+        for i in range(1, k - 1):  # fans: top (+z) and bottom (-z)
+            mb.tri((P[0][0], P[0][1], z1), (P[i][0], P[i][1], z1), (P[i + 1][0], P[i + 1][1], z1), (0, 0, 1), mat)
+            mb.tri((P[0][0], P[0][1], z0), (P[i + 1][0], P[i + 1][1], z0), (P[i][0], P[i][1], z0), (0, 0, -1), mat)
+    if mb.tris:
+        tris.append(np.asarray(mb.tris, np.float64).astype(np.float32))
+        nrms.append(np.asarray(mb.normals, np.float64).astype(np.float32))
+        mats.append(np.asarray(mb.mats, np.int32))
+    tri = np.concatenate(tris, 0)
+    nrm = np.concatenate(nrms, 0)
+    mat = np.concatenate(mats, 0)
+    # drop facets whose float corners coincide (degenerate); keep the rest in order
+    e1 = tri[:, 1].astype(np.float64) - tri[:, 0]
+    e2 = tri[:, 2].astype(np.float64) - tri[:, 0]
+    good = (np.linalg.norm(np.cross(e1, e2), axis=1) > 0) & \
+        ~np.all(tri[:, 0] == tri[:, 1], 1) & ~np.all(tri[:, 0] == tri[:, 2], 1) & \
+        ~np.all(tri[:, 1] == tri[:, 2], 1)
+    tri, nrm, mat = tri[good], nrm[good], mat[good]
+    ground = (f, 0.0, 0.0, 15.0, 0.0, 0.035)  # medium-dry ground
+    concrete = (f, 0.0, 0.0, 5.31, 0.0, round(p2040_sigma(0.0326, 0.8095, f), 6))
+    glass = (f, 0.0, 0.0, 6.27, 0.0, round(p2040_sigma(0.0043, 1.1925, f), 6))
+    scene = Scene("large", tri, nrm, mat, [ground, concrete, glass])
+    rx_xy = rng.uniform(-half + 1.0, half - 1.0, (n_rx, 2))
+    rx = np.column_stack([rx_xy, height(rx_xy[:, 0], rx_xy[:, 1]) + 1.5]).astype(np.float64)
+    req = Request(tx=tx, rx=rx, max_reflection=max_reflection, max_transmission=0,
+                  frequency=f, tessellation=level, antenna=2)
+    return Workload(f"large_L{level}_R{max_reflection}", scene, req, {"seed": seed})
