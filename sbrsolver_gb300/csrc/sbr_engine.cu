@@ -341,6 +341,7 @@ struct TraceArgs {
   ClassInfo* cls_info;
   const int* tri_cop;  // coplanar id by rank
   Counters* ctr;
+  unsigned long long* seg_per_tx;  // executed segments per request
   int depth;
   long long n_root;    // total launches (depth 0)
 };
@@ -405,6 +406,11 @@ __global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
     Hit h;
     const bool hit = closest_hit(A.sc, r.o, r.d, h, st, &A.ctr->overflow);
     const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
+    {  // per-request segment count, one atomic per request present in the warp
+      const unsigned peers = __match_any_sync(__activemask(), r.tx);
+      if (int(lane_id()) == __ffs(peers) - 1)
+        atomicAdd(&A.seg_per_tx[r.tx], (unsigned long long)__popc(peers));
+    }
     const bool root = A.depth == 0;
     if (ni < A.node_cap) {
       NodeCold n;
@@ -1081,6 +1087,7 @@ struct Workspace {
   DBuf<double> path_field, path_pts, field;
   DBuf<int> path_nray, path_tri, path_cop, path_kind;
   DBuf<Counters> ctr;
+  DBuf<unsigned long long> seg_tx;
   // capacities (grown from occupancy and on overflow)
   unsigned long long cap_nodes = 1 << 20, cap_queue = 1 << 19, cap_surv = 1 << 14;
   unsigned long long cap_corr = 1 << 16;
@@ -1143,6 +1150,9 @@ struct sbr_result {
   std::vector<double> points;
   sbr_counts counts{};
   sbr_timing timing{};
+  std::vector<long long> segments_per_request;
+  std::vector<long long> launches_per_request;
+  std::vector<int> rx_per_request;
 };
 
 namespace sbr {
@@ -1516,6 +1526,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.dd_rank.ensure(W.cap_dd);
     W.surv.ensure(W.cap_surv);
     CK(cudaMemsetAsync(W.ctr.p, 0, sizeof(Counters), st));
+    W.seg_tx.ensure(n_req);
+    CK(cudaMemsetAsync(W.seg_tx.p, 0, sizeof(unsigned long long) * n_req, st));
     const int fb = 256;
     k_fill_u64<<<grid_for(W.cap_cls, fb), fb, 0, st>>>(W.cls_keys.p, W.cap_cls, kEmptyKey);
     k_fill_u64<<<grid_for(W.cap_cop, fb), fb, 0, st>>>(W.cop_keys.p, W.cap_cop, kEmptyKey);
@@ -1537,6 +1549,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ta.cls_info = W.cls_info.p;
     ta.tri_cop = S.tri_cop.p;
     ta.ctr = W.ctr.p;
+    ta.seg_per_tx = W.seg_tx.p;
     ta.n_root = launches;
     for (int d = 0; d <= max_depth; ++d) {
       ta.depth = d;
@@ -1715,6 +1728,18 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     // paths are ordered by survivor order within a receiver; receivers ascend
     // because s_order is grouped by receiver index.
     out.counts.segments = (long long)c.nodes;
+    {
+      std::vector<unsigned long long> spt(n_req);
+      CK(cudaMemcpy(spt.data(), W.seg_tx.p, sizeof(unsigned long long) * n_req,
+                    cudaMemcpyDeviceToHost));
+      out.segments_per_request.assign(spt.begin(), spt.end());
+      out.rx_per_request.resize(n_req);
+      out.launches_per_request.resize(n_req);
+      for (int r = 0; r < n_req; ++r) {
+        out.rx_per_request[r] = tp[r].n_rx;
+        out.launches_per_request[r] = tp[r].n_launch;
+      }
+    }
     out.counts.captured = stage_counts ? (long long)c.events : -1;
     out.counts.corrected = (long long)c.corrected;
     out.counts.paths = (long long)ns;
@@ -1746,6 +1771,45 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
   }
 }
 
+}  // namespace sbr
+
+namespace sbr {
+// One result per request of a batch result (request order); fields, paths and
+// segment counts are the request's own, stage counters the batch's.
+std::vector<sbr_result*> split_result(const sbr_result& b) {
+  std::vector<sbr_result*> out;
+  const int n = int(b.rx_per_request.size());
+  size_t f0 = 0;
+  for (int r = 0; r < n; ++r) {
+    auto* x = new sbr_result();
+    const size_t nf = 6 * size_t(b.rx_per_request[r]);
+    x->field.assign(b.field.begin() + f0, b.field.begin() + f0 + nf);
+    f0 += nf;
+    for (const sbr_path& p : b.paths) {
+      if (p.request != r) continue;
+      sbr_path q = p;
+      q.request = 0;
+      q.ray_offset = (long long)x->tri.size();
+      const size_t o = size_t(p.ray_offset), m = size_t(p.n_rays);
+      x->tri.insert(x->tri.end(), b.tri.begin() + o, b.tri.begin() + o + m);
+      x->cop.insert(x->cop.end(), b.cop.begin() + o, b.cop.begin() + o + m);
+      x->kind.insert(x->kind.end(), b.kind.begin() + o, b.kind.begin() + o + m);
+      x->points.insert(x->points.end(), b.points.begin() + 6 * o, b.points.begin() + 6 * (o + m));
+      x->paths.push_back(q);
+    }
+    x->counts = b.counts;
+    x->counts.segments = r < int(b.segments_per_request.size()) ? b.segments_per_request[r] : -1;
+    x->counts.paths = (long long)x->paths.size();
+    x->counts.rays = (long long)x->tri.size();
+    x->timing = b.timing;
+    x->counts.launches = r < int(b.launches_per_request.size()) ? b.launches_per_request[r] : -1;
+    x->segments_per_request = {x->counts.segments};
+    x->launches_per_request = {x->counts.launches};
+    x->rx_per_request = {b.rx_per_request[r]};
+    out.push_back(x);
+  }
+  return out;
+}
 }  // namespace sbr
 
 // ============================================================ C ABI
@@ -1948,6 +2012,14 @@ sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_
         p.ray_offset += ray_base;
         res->paths.push_back(p);
       }
+      res->segments_per_request.insert(res->segments_per_request.end(),
+                                       part.segments_per_request.begin(),
+                                       part.segments_per_request.end());
+      res->rx_per_request.insert(res->rx_per_request.end(), part.rx_per_request.begin(),
+                                 part.rx_per_request.end());
+      res->launches_per_request.insert(res->launches_per_request.end(),
+                                       part.launches_per_request.begin(),
+                                       part.launches_per_request.end());
       res->field.insert(res->field.end(), part.field.begin(), part.field.end());
       res->tri.insert(res->tri.end(), part.tri.begin(), part.tri.end());
       res->cop.insert(res->cop.end(), part.cop.begin(), part.cop.end());

@@ -1,16 +1,19 @@
-// Request server: continuous admission of propagation solves on resident
+// Request server: continuous batching of propagation solves on resident
 // scenes (no reference counterpart; the reference solves one transmitter per
 // call from main()).
 //
 // A server owns `slots` worker threads.  Submitted requests (copied, with
 // their receivers) wait in one FIFO queue.  A worker takes the head request
 // as soon as (a) the worker is free and (b) the request's device-memory
-// estimate fits in the HBM budget next to the requests already running.  It
-// then runs sbr_solve, which checks a workspace (buffers + CUDA stream) out
-// of the process-wide pool, so requests admitted while others are on the GPU
-// run on their own streams and overlap with them on the device.  Each
-// result is exactly what sbr_solve returns for that request alone: requests
-// share only read-only scene data.
+// estimate fits in the HBM budget next to the requests already running.  If
+// the head is small, the worker also takes the queued small requests on the
+// same scene (up to kMaxBatch, within the budget) and solves them together in
+// one device pass (sbr_solve_batch), which fills the GPU far better than
+// small requests one by one.  Every solve checks a workspace (buffers + CUDA
+// stream) out of the process-wide pool, so work admitted while other work is
+// on the GPU runs on its own stream and overlaps with it.  Each result is
+// exactly what sbr_solve returns for that request alone: requests share only
+// read-only scene data, and batch results are split per request.
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -28,7 +31,11 @@
 namespace sbr {
 void set_error_message(const std::string& s);
 double request_bytes(const sbr_request& q);  // device bytes a request may need
+std::vector<sbr_result*> split_result(const sbr_result& batch);
 }
+// The result type is defined with the solver; the server only needs a
+// reference to hand to split_result.
+struct sbr_result;
 
 namespace {
 
@@ -49,6 +56,10 @@ long long estimate_bytes(const sbr_request& q) {
   return (long long)sbr::request_bytes(q) + (64LL << 20);
 }
 
+constexpr size_t kMaxBatch = 64;
+// Requests at most this large (device-memory estimate) are batched together.
+constexpr long long kSmallBytes = 512LL << 20;
+
 }  // namespace
 
 struct sbr_server {
@@ -66,7 +77,8 @@ struct sbr_server {
   void worker() {
     cudaSetDevice(device);
     for (;;) {
-      Job job;
+      std::vector<Job> batch;
+      long long est = 0;
       {
         std::unique_lock<std::mutex> lock(mu);
         cv_work.wait(lock, [&] {
@@ -76,35 +88,65 @@ struct sbr_server {
           return in_flight == 0 || in_flight + need <= budget;
         });
         if (queue.empty()) return;
-        job = std::move(queue.front());
+        batch.push_back(std::move(queue.front()));
         queue.pop_front();
-        in_flight += std::min(job.est_bytes, budget);
+        est = std::min(batch[0].est_bytes, budget);
+        if (batch[0].est_bytes <= kSmallBytes) {
+          for (auto it = queue.begin(); it != queue.end() && batch.size() < kMaxBatch;) {
+            if (it->scene == batch[0].scene && it->est_bytes <= kSmallBytes &&
+                in_flight + est + it->est_bytes <= budget) {
+              est += it->est_bytes;
+              batch.push_back(std::move(*it));
+              it = queue.erase(it);
+            } else {
+              ++it;
+            }
+          }
+        }
+        in_flight += est;
       }
       cv_work.notify_all();
       const Clock::time_point start = Clock::now();
-      job.req.rx = job.rx.empty() ? nullptr : job.rx.data();
-      job.req.rx_on_device = 0;
+      std::vector<sbr_request> reqs(batch.size());
+      for (size_t i = 0; i < batch.size(); ++i) {
+        reqs[i] = batch[i].req;
+        reqs[i].rx = batch[i].rx.empty() ? nullptr : batch[i].rx.data();
+        reqs[i].rx_on_device = 0;
+      }
       sbr_result* res = nullptr;
-      const sbr_status st = sbr_solve(scenes[job.scene], &job.req, &res);
+      const sbr_status st =
+          sbr_solve_batch(scenes[batch[0].scene], reqs.data(), int(reqs.size()), &res);
       const Clock::time_point end = Clock::now();
-      sbr_completion c;
-      std::memset(&c, 0, sizeof c);
-      c.tag = job.tag;
-      c.scene = job.scene;
-      c.status = st;
-      c.queue_ms = std::chrono::duration<double, std::milli>(start - job.submitted).count();
-      c.latency_ms = std::chrono::duration<double, std::milli>(end - job.submitted).count();
-      c.result = res;
-      if (res) {
-        sbr_timing t;
-        sbr_result_timing(res, &t);
-        c.device_ms = t.device_ms;
-        sbr_result_counts(res, &c.counts);
+      std::vector<sbr_result*> parts;
+      if (res && batch.size() > 1) {
+        parts = sbr::split_result(*res);
+        sbr_result_destroy(res);
+      } else {
+        parts.assign(batch.size(), nullptr);
+        if (res) parts[0] = res;
+      }
+      std::vector<sbr_completion> out;
+      for (size_t i = 0; i < batch.size(); ++i) {
+        sbr_completion c;
+        std::memset(&c, 0, sizeof c);
+        c.tag = batch[i].tag;
+        c.scene = batch[i].scene;
+        c.status = st;
+        c.queue_ms = std::chrono::duration<double, std::milli>(start - batch[i].submitted).count();
+        c.latency_ms = std::chrono::duration<double, std::milli>(end - batch[i].submitted).count();
+        c.result = i < parts.size() ? parts[i] : nullptr;
+        if (c.result) {
+          sbr_timing t;
+          sbr_result_timing(c.result, &t);
+          c.device_ms = t.device_ms;
+          sbr_result_counts(c.result, &c.counts);
+        }
+        out.push_back(c);
       }
       {
         std::lock_guard<std::mutex> lock(mu);
-        in_flight -= std::min(job.est_bytes, budget);
-        done.push_back(c);
+        in_flight -= est;
+        for (auto& c : out) done.push_back(c);
       }
       cv_work.notify_all();
       cv_done.notify_all();

@@ -53,6 +53,7 @@ def test_results_identical_alone_and_in_the_mix(built):
         res = got[tag]["result"]
         np.testing.assert_array_equal(res.field, ref.field)
         assert path_keys(res.paths) == path_keys(ref.paths)
+        assert res.counts["segments"] == ref.counts["segments"]
         assert got[tag]["latency_ms"] >= got[tag]["queue_ms"] >= 0
 
 
