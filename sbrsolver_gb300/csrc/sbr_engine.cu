@@ -375,7 +375,7 @@ __device__ __forceinline__ void write_class(ClassInfo& ci, const double* img, ui
   ci.pad2 = 0;
 }
 
-__global__ void __launch_bounds__(128) k_trace(TraceArgs A) {
+__global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
   const long long n_in =
       A.depth == 0 ? A.n_root
                    : (long long)min(A.ctr->queue[A.depth], (unsigned long long)A.out_cap);
@@ -588,7 +588,7 @@ struct AncRec {
   uint32_t idx, pad[3];
 };
 
-__global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
+__global__ void __launch_bounds__(32 * kCapWarps, 5) k_capture(CaptureArgs A) {
   __shared__ AncRec anc[kCapWarps][kMaxDepth];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
@@ -604,9 +604,11 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
     const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
     const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
     const float len = nd.len, S = nd.S;
-    // stage the ancestor chain
+    // Stage the ancestor chain when every capture is checked against it
+    // (stage counts); otherwise only corrected captures (~0.1% of captures)
+    // need it and they walk the chain themselves.
     int na = 0;
-    if (lane == 0) {
+    if (A.stage_counts && lane == 0) {
       for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap && na < kMaxDepth;) {
         const NodeHot a = A.nodes[p];
         AncRec& r = anc[warp][na++];
@@ -759,16 +761,31 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
               // RayCapture deletes a captured node's subtree, so an ancestor
               // capturing the same receiver suppresses this one.
               auto suppressed = [&]() {
-                for (int q = 0; q < na; ++q) {
-                  const AncRec& r = anc[warp][q];
+                if (A.stage_counts) {
+                  for (int q = 0; q < na; ++q) {
+                    const AncRec& r = anc[warp][q];
+                    ++anc_tests;
+                    int w = reception32(make_float3(r.s[0], r.s[1], r.s[2]),
+                                        make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, c, tanb);
+                    if (w < 0) {
+                      ++n64;
+                      w = capture_exact(A.nodes_cold, r.idx, c64, P.tan_beta);
+                    }
+                    if (w) return true;
+                  }
+                  return false;
+                }
+                for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
+                  const NodeHot a = A.nodes[p];
                   ++anc_tests;
-                  int w = reception32(make_float3(r.s[0], r.s[1], r.s[2]),
-                                      make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, c, tanb);
+                  int w = reception32(make_float3(a.s[0], a.s[1], a.s[2]),
+                                      make_float3(a.u[0], a.u[1], a.u[2]), a.len, a.S, c, tanb);
                   if (w < 0) {
                     ++n64;
-                    w = capture_exact(A.nodes_cold, r.idx, c64, P.tan_beta);
+                    w = capture_exact(A.nodes_cold, p, c64, P.tan_beta);
                   }
                   if (w) return true;
+                  p = a.parent;
                 }
                 return false;
               };
