@@ -190,12 +190,18 @@ def run_batched(precision: str):
     t0 = time.perf_counter()
     rb = api.solve(sc, qs, with_paths=False)
     t_batch = time.perf_counter() - t0
+    err = None
+    if precision != "fp64":  # untimed: the batch's field error against FP64
+        qc = [api.request_from_workload(r, precision, field_check=True) for r in reqs]
+        rc = api.solve(sc, qc, with_paths=False)
+        err = api.field_error_stats(rc.field, rc.field_fp64)
     sc.close()
     return {"workload": "urban 256 Tx, levels 6-9, R5, 4096 shared receivers",
             "requests": len(qs), "segments": rb.counts["segments"],
             "batched": rb.counts["segments"] / t_batch, "plain": seg_plain / t_plain,
             "unit": "segments/s", "batched_s": t_batch, "plain_s": t_plain,
-            "speedup": (rb.counts["segments"] / t_batch) / (seg_plain / t_plain)}
+            "speedup": (rb.counts["segments"] / t_batch) / (seg_plain / t_plain),
+            "field_error_vs_fp64": err}
 
 
 def run_serving(precision: str, n_req: int = 48, rates=(10.0, 50.0, 500.0), slots: int = 4):
@@ -248,6 +254,44 @@ def run_serving(precision: str, n_req: int = 48, rates=(10.0, 50.0, 500.0), slot
             "p99_ms": top["p99_ms"], "speedup": top["served"] / plain}
 
 
+def run_precision(level: int = 10, n_rx: int = 50000):
+    """Precision study on the large terrain scene: the same solve with the
+    field in FP64, in FP32 (Fresnel and rotations FP32, path length and phase
+    FP64, compensated FP32 receiver sums) and in FP32 with an FP32 phase.
+    Reports throughput per mode, whether the path sets are identical, and
+    each FP32 mode's field error against the FP64 field (which the parity
+    tests pin to the CPU oracle)."""
+    import numpy as np
+    from sbrsolver_gb300 import api, scenes
+    t0 = time.perf_counter()
+    wl = scenes.large_scene(level=level, n_rx=n_rx)
+    gen_s = time.perf_counter() - t0
+    sc = api.DeviceScene.from_scene(wl.scene)
+    res = {}
+    modes = {}
+    for mode in ("fp64", "fp32", "fp32_phase"):
+        q = api.request_from_workload(wl.request, mode, field_check=(mode != "fp64"))
+        api.solve(sc, q, with_paths=False)  # warm-up (sizes the workspace)
+        r = api.solve(sc, q, with_paths="arrays")
+        res[mode] = r
+        modes[mode] = {"device_ms": r.timing["device_ms"], "field_ms": r.timing["field_ms"],
+                       "segments_per_s": r.counts["segments"] / (r.timing["device_ms"] / 1e3)}
+    sc.close()
+    ref = res["fp64"]
+    for mode in ("fp32", "fp32_phase"):
+        r = res[mode]
+        modes[mode]["same_path_set"] = api.same_path_set(r.paths, ref.paths)
+        modes[mode]["shadow_fp64_equals_fp64_run"] = bool(np.array_equal(r.field_fp64, ref.field))
+        modes[mode]["error_vs_fp64"] = api.field_error_stats(r.field, ref.field)
+        modes[mode]["device_reported"] = r.field_error
+    c = ref.counts
+    return {"workload": f"large terrain: {wl.scene.n_tri} tris, icosahedron level {level} "
+                        f"({c['launches']} rays), R8 T0, {n_rx} receivers, half-wave 3.5 GHz",
+            "segments": c["segments"], "paths": c["paths"], "rays": c["rays"],
+            "scene_generation_s": gen_s, "modes": modes,
+            "tolerance": {"rel_mag": 1e-4, "phase_rad": 1e-3}}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -284,6 +328,7 @@ def main():
                     help="icosahedron level (9 = the benchmark; lower for profiling runs)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-precision", action="store_true")
     args = ap.parse_args()
     rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
     dist = None
@@ -317,6 +362,13 @@ def main():
 
     for _ in range(args.warmup):
         api.solve(scene, req_dev, with_paths=False)
+    # stage counts and the field error of this precision (untimed)
+    q_chk = api.request_from_workload(wl.request, args.precision, stage_counts=True,
+                                      field_check=args.precision != "fp64")
+    r_chk = api.solve(scene, q_chk, with_paths=False)
+    captured = r_chk.counts["captured"]
+    field_error = (api.field_error_stats(r_chk.field, r_chk.field_fp64)
+                   if r_chk.field_fp64 is not None else None)
     # ---- device-resident timing
     if dist:
         dist.barrier()
@@ -366,7 +418,7 @@ def main():
         tr_ms = stage["trace_ms"] / steps
         if cap_ms >= tr_ms:
             kern, ms = "k_capture", cap_ms
-            alg = n_nodes * NODE_BYTES + counts["captured"] * EVENT_BYTES
+            alg = n_nodes * NODE_BYTES + captured * EVENT_BYTES
         else:
             kern, ms = "k_trace", tr_ms / (depth + 1)
             alg = n_nodes * SEGMENT_BYTES / (depth + 1)
@@ -384,7 +436,8 @@ def main():
                        "field_precision": args.precision,
                        "parallelism": f"replicas{world}",
                        "l2": "working set (node pool) larger than L2 each step"},
-            "counts": counts,
+            "counts": dict(counts, captured=captured),
+            "field_error_vs_fp64": field_error,
             "stages_ms": {k: v / steps for k, v in stage.items()},
             "e2e": {"value": tot_e2e / max_e2e, "unit": "segments/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -400,6 +453,8 @@ def main():
             line["batched"] = run_batched(args.precision)
         if not args.no_serving and args.level == 9:
             line["serving"] = run_serving(args.precision)
+        if not args.no_precision and args.level == 9:
+            line["precision"] = run_precision()
         if not args.no_cpu_baseline and world == 1:
             try:
                 line["cpu_baseline"] = cpu_baseline(wl)

@@ -60,8 +60,10 @@ typedef struct sbr_material {
 enum { SBR_ANTENNA_ISOTROPIC = 0, SBR_ANTENNA_HERTZIAN = 1, SBR_ANTENNA_HALF_WAVE = 2 };
 
 /* Field precision: FP64 everywhere, or FP32 Fresnel/rotation arithmetic
- * with FP64 path length and phase and a compensated FP32 per-receiver sum. */
-enum { SBR_FIELD_FP64 = 0, SBR_FIELD_FP32 = 1 };
+ * with FP64 path length and phase and a compensated FP32 per-receiver sum.
+ * SBR_FIELD_FP32_PHASE also takes path length and phase k*L in FP32; it
+ * exists to measure the phase error that FP64 length/phase avoids. */
+enum { SBR_FIELD_FP64 = 0, SBR_FIELD_FP32 = 1, SBR_FIELD_FP32_PHASE = 2 };
 
 typedef struct sbr_scene sbr_scene;
 typedef struct sbr_result sbr_result;
@@ -88,6 +90,8 @@ typedef struct sbr_request {
   int rx_on_device;        /* rx is a device pointer (already resident) */
   int stage_counts;        /* also count captures before correction (sbr_counts.captured);
                               costs time, results are identical either way */
+  int field_check;         /* FP32 field precisions: also compute the FP64 field on the
+                              GPU so sbr_result_field_error can state the error */
 } sbr_request;
 
 typedef struct sbr_counts {
@@ -118,6 +122,17 @@ typedef struct sbr_path {
 /* Stage times from CUDA events on the engine's stream.  device_ms spans
  * everything after the receivers are on the device (grid, trace, capture,
  * correction, field) and before results are copied back. */
+/* Error of an FP32-precision field against the FP64 field of the same path
+ * set (requests with field_check).  Components compared: those whose FP64
+ * magnitude exceeds 1e-6 of the receiver's largest component. */
+typedef struct sbr_field_error {
+  long long components;      /* receiver field components compared */
+  long long over_tolerance;  /* of those, outside 1e-4 relative magnitude or 1e-3 rad */
+  double max_rel_mag;        /* max | |E| - |E64| | / |E64| */
+  double max_phase_rad;      /* max |arg(E / E64)| */
+  double max_rel_vec;        /* max |E - E64| / |E64| */
+} sbr_field_error;
+
 typedef struct sbr_timing {
   double total_ms, trace_ms, capture_ms, correct_ms, field_ms, h2d_ms, d2h_ms, device_ms;
 } sbr_timing;
@@ -152,6 +167,11 @@ sbr_status sbr_result_counts(const sbr_result* result, sbr_counts* out);
 /* 6 doubles per receiver (Ex re, Ex im, Ey re, Ey im, Ez re, Ez im), requests
  * concatenated in order. */
 sbr_status sbr_result_field(const sbr_result* result, double* out);
+/* Field error of an FP32-precision result against FP64 (request field_check);
+ * SBR_ERR_NOT_READY when the result carries no FP64 field. */
+sbr_status sbr_result_field_error(const sbr_result* result, sbr_field_error* out);
+/* The FP64 field of a field_check result, in sbr_result_field's layout. */
+sbr_status sbr_result_field_fp64(const sbr_result* result, double* out);
 /* paths: counts.paths entries; tri/cop/kind: counts.rays entries
  * (kind 0 = launch, 1 = reflected, 2 = transmitted; tri/cop -1 on the last
  * ray); points: 6 doubles per ray (corrected source, target).  Any output

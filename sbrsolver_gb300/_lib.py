@@ -21,7 +21,7 @@ EXPORTS = (
     "sbr_solve_batch", "sbr_result_counts", "sbr_result_field", "sbr_result_paths",
     "sbr_result_timing", "sbr_result_destroy", "sbr_last_error", "sbr_version",
     "sbr_receiver_field_sum_noalloc", "sbr_server_create", "sbr_server_submit", "sbr_server_poll",
-    "sbr_server_pending", "sbr_server_destroy",
+    "sbr_server_pending", "sbr_server_destroy", "sbr_result_field_error", "sbr_result_field_fp64",
 )
 
 
@@ -48,7 +48,13 @@ class Request(C.Structure):
                 ("frequency", C.c_double), ("pt", C.c_double), ("use_fresnel", C.c_int),
                 ("tessellation", C.c_int), ("antenna", C.c_int), ("field_precision", C.c_int),
                 ("n_rx", C.c_int), ("rx", C.POINTER(C.c_double)), ("rx_on_device", C.c_int),
-                ("stage_counts", C.c_int)]
+                ("stage_counts", C.c_int), ("field_check", C.c_int)]
+
+
+class FieldError(C.Structure):
+    _fields_ = [("components", C.c_longlong), ("over_tolerance", C.c_longlong),
+                ("max_rel_mag", C.c_double), ("max_phase_rad", C.c_double),
+                ("max_rel_vec", C.c_double)]
 
 
 class Counts(C.Structure):
@@ -103,6 +109,8 @@ def load(path: str = LIB_PATH):
             "sbr_solve_batch": [vp, P(Request), I, P(vp)],
             "sbr_result_counts": [vp, P(Counts)],
             "sbr_result_field": [vp, P(D)],
+            "sbr_result_field_fp64": [vp, P(D)],
+            "sbr_result_field_error": [vp, P(FieldError)],
             "sbr_result_paths": [vp, P(Path), P(I), P(I), P(I), P(D)],
             "sbr_result_timing": [vp, P(Timing)],
             "sbr_result_destroy": [vp],

@@ -198,12 +198,16 @@ class Result:
     field: np.ndarray          # (n_rx, 3) complex128
     counts: dict
     timing: dict
-    paths: List[dict] = field(default_factory=list)
+    paths: object = field(default_factory=list)  # list of dicts, or dict of arrays
+    # requests with field_check: FP64 field of the same paths and the error of `field`
+    field_fp64: Optional[np.ndarray] = None
+    field_error: Optional[dict] = None
 
 
 def make_request(tx, tx_coord_sys, max_reflection, max_transmission, frequency, pt, use_fresnel,
                  rx: np.ndarray, tessellation: int, antenna: int = 1,
-                 precision: str = "fp64", stage_counts: bool = False) -> tuple:
+                 precision: str = "fp64", stage_counts: bool = False,
+                 field_check: bool = False) -> tuple:
     rx = np.ascontiguousarray(rx, np.float64).reshape(-1, 3)
     q = _lib.Request()
     for i in range(3):
@@ -218,23 +222,27 @@ def make_request(tx, tx_coord_sys, max_reflection, max_transmission, frequency, 
     q.use_fresnel = 1 if use_fresnel else 0
     q.tessellation = int(tessellation)
     q.antenna = int(antenna)
-    q.field_precision = 1 if precision == "fp32" else 0
+    q.field_precision = {"fp64": 0, "fp32": 1, "fp32_phase": 2}[precision]
     q.n_rx = int(rx.shape[0])
     q.rx = rx.ctypes.data_as(C.POINTER(C.c_double))
     q.rx_on_device = 0
     q.stage_counts = 1 if stage_counts else 0
+    q.field_check = 1 if field_check else 0
     return q, rx  # keep rx alive with the request
 
 
 def request_from_workload(req: WorkRequest, precision: str = "fp64",
-                          stage_counts: bool = False) -> tuple:
+                          stage_counts: bool = False, field_check: bool = False) -> tuple:
     return make_request(req.tx, req.tx_coord_sys, req.max_reflection, req.max_transmission,
                         req.frequency, req.pt, req.use_fresnel, req.rx, req.tessellation,
-                        req.antenna, precision, stage_counts)
+                        req.antenna, precision, stage_counts, field_check)
 
 
-def solve(scene: DeviceScene, requests, with_paths: bool = True) -> Result:
-    """Runs one or more requests (a batch) and returns fields, counts and paths."""
+def solve(scene: DeviceScene, requests, with_paths=True) -> Result:
+    """Runs one or more requests (a batch) and returns fields, counts and paths
+    (a list of per-path dicts, or with with_paths="arrays" one dict of flat
+    arrays: per-path request/receiver/launch/heap/ray_offset/n_rays and
+    per-ray tri/cop/kind/points)."""
     lib = _lib.load()
     if isinstance(requests, tuple) and len(requests) == 2 and isinstance(requests[0], _lib.Request):
         requests = [requests]  # one (request, receiver array) pair
@@ -269,6 +277,14 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
             _lib.check(lib.sbr_result_paths(h, P, tri.ctypes.data_as(ip), cop.ctypes.data_as(ip),
                                             kind.ctypes.data_as(ip),
                                             pts.ctypes.data_as(C.POINTER(C.c_double))))
+            if with_paths == "arrays":
+                # the whole path set as flat arrays (cheap at 1e5-1e6 paths)
+                A = np.ctypeslib.as_array(P)
+                paths = {k: np.array(A[k]) for k in ("request", "receiver", "launch", "heap",
+                                                     "ray_offset", "n_rays", "field")}
+                paths.update(tri=tri[:cnt.rays], cop=cop[:cnt.rays], kind=kind[:cnt.rays],
+                             points=pts[:6 * cnt.rays].reshape(-1, 6))
+                P = ()
             for p in P:
                 o, n = int(p.ray_offset), int(p.n_rays)
                 paths.append({
@@ -279,9 +295,57 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
                     "field": np.array(p.field[:], np.float64)})
         fc = f.reshape(-1, 3, 2)
         field_c = fc[..., 0] + 1j * fc[..., 1]
-        return Result(field_c, counts, timing, paths)
+        res = Result(field_c, counts, timing, paths)
+        fe = _lib.FieldError()
+        if lib.sbr_result_field_error(h, C.byref(fe)) == 0:
+            res.field_error = {k: getattr(fe, k) for k, _ in _lib.FieldError._fields_}
+            f64 = np.zeros(6 * n_rx, np.float64)
+            if n_rx:
+                _lib.check(lib.sbr_result_field_fp64(h, f64.ctypes.data_as(C.POINTER(C.c_double))))
+            g = f64.reshape(-1, 3, 2)
+            res.field_fp64 = g[..., 0] + 1j * g[..., 1]
+        return res
     finally:
         lib.sbr_result_destroy(h)
+
+
+def field_error_stats(field: np.ndarray, reference: np.ndarray, floor: float = 1e-6,
+                      rel_tol: float = 1e-4, phase_tol: float = 1e-3) -> dict:
+    """Error of a received field against a reference field (both (n_rx, 3)
+    complex), over the components whose reference magnitude exceeds `floor`
+    times the receiver's largest component (the ones that carry a phase):
+    relative magnitude error ||E|-|E_ref||/|E_ref|, phase error |arg(E/E_ref)|
+    and relative vector error |E-E_ref|/|E_ref| (max, median, 99th percentile),
+    plus how many components fall outside rel_tol / phase_tol."""
+    a = np.asarray(field).reshape(-1, 3)
+    b = np.asarray(reference).reshape(-1, 3)
+    mb = np.abs(b)
+    scale = mb.max(axis=1, keepdims=True) if len(b) else np.zeros((0, 1))
+    m = (mb > floor * scale) & (scale > 0)
+    x, y, my = a[m], b[m], mb[m]
+    out = {"components": int(m.sum()), "receivers": int(len(b)),
+           "receivers_with_field": int((scale[:, 0] > 0).sum()) if len(b) else 0}
+    if not len(y):
+        return out
+    rel_mag = np.abs(np.abs(x) - my) / my
+    phase = np.abs(np.angle(x * np.conj(y)))
+    rel_vec = np.abs(x - y) / my
+    for name, v in (("rel_mag", rel_mag), ("phase_rad", phase), ("rel_vec", rel_vec)):
+        out[f"max_{name}"] = float(v.max())
+        out[f"median_{name}"] = float(np.median(v))
+        out[f"p99_{name}"] = float(np.percentile(v, 99))
+    out["over_tolerance"] = int(((rel_mag > rel_tol) | (phase > phase_tol)).sum())
+    return out
+
+
+def same_path_set(a: dict, b: dict) -> bool:
+    """Two path sets (solve(..., with_paths="arrays")) are identical: same
+    receivers, launches, BFS positions, ray counts and facet / coplanar /
+    interaction sequences, in the same order."""
+    keys = ("request", "receiver", "launch", "heap", "n_rays", "tri", "cop", "kind")
+    if isinstance(a, list) or isinstance(b, list):
+        return (not a) and (not b)
+    return all(np.array_equal(a[k], b[k]) for k in keys)
 
 
 class Server:

@@ -998,7 +998,10 @@ __global__ void k_field(FieldArgs A) {
       if (r + 1 < pb.n) mat[r + 1] = A.sc.tri64[pb.tri[r]].mat;
     }
     Cx<double> e[3];
-    if (A.precision == 1)
+    if (A.precision == 2)
+      path_field<float, true>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq,
+                              P.pt, P.antenna, P.fresnel != 0, A.K, e);
+    else if (A.precision == 1)
       path_field<float>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
                         P.antenna, P.fresnel != 0, A.K, e);
     else
@@ -1058,7 +1061,7 @@ __global__ void k_rx_sum(const Survivor* surv, const int* starts, int* order, in
       }
       order[j + 1] = v;
     }
-    if (precision == 1) {
+    if (precision != 0) {  // both FP32 modes: compensated FP32 sum
       float s[6] = {0, 0, 0, 0, 0, 0}, c[6] = {0, 0, 0, 0, 0, 0};
       for (int i = b; i < e; ++i)
         for (int k = 0; k < 6; ++k) {
@@ -1102,6 +1105,7 @@ struct Workspace {
   DBuf<Survivor> surv;
   DBuf<int> s_counts, s_starts, s_cursor, s_order;
   DBuf<double> path_field, path_pts, field;
+  DBuf<double> path_field64, field64;  // FP64 shadow of an FP32 field (field_check)
   DBuf<int> path_nray, path_tri, path_cop, path_kind;
   DBuf<Counters> ctr;
   DBuf<unsigned long long> seg_tx;
@@ -1162,6 +1166,7 @@ struct sbr_scene {
 
 struct sbr_result {
   std::vector<double> field;
+  std::vector<double> field64;  // FP64 shadow field (field_check requests), else empty
   std::vector<sbr_path> paths;
   std::vector<int> tri, cop, kind;
   std::vector<double> points;
@@ -1434,8 +1439,13 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     rx_total += q.n_rx;
     max_depth = std::max(max_depth, q.max_reflection + q.max_transmission);
   }
-  const int precision = reqs[0].field_precision == SBR_FIELD_FP32 ? 1 : 0;
+  const int precision = reqs[0].field_precision == SBR_FIELD_FP32
+                            ? 1
+                            : (reqs[0].field_precision == SBR_FIELD_FP32_PHASE ? 2 : 0);
   const int stage_counts = reqs[0].stage_counts ? 1 : 0;
+  bool field_check = false;
+  for (int r = 0; r < n_req; ++r) field_check |= reqs[r].field_check != 0;
+  field_check &= precision != 0;
   if (n_req >= int(0xFFFFFFFFu - kRootBase)) throw std::string("too many requests in one batch");
   auto t0 = std::chrono::steady_clock::now();
   CK(cudaEventRecord(W.ev[0], st));
@@ -1691,11 +1701,31 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
                                                         W.field.p);
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[6], st));
+    if (field_check) {  // FP64 shadow of the same paths, outside the timed stages
+      W.path_field64.ensure(nsa * 6);
+      W.field64.ensure(std::max(1, 6 * rx_total));
+      FieldArgs f64 = fa;
+      f64.precision = 0;
+      f64.path_field = W.path_field64.p;
+      if (ns) k_field<<<grid_for(ns, 64), 64, 0, st>>>(f64);
+      if (rx_total)
+        k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
+                                                          rx_total, W.path_field64.p, 0,
+                                                          W.field64.p);
+      CK(cudaGetLastError());
+    }
     // ---- results to the host
     out.field.resize(6 * size_t(rx_total));
     if (rx_total)
       CK(cudaMemcpyAsync(out.field.data(), W.field.p, sizeof(double) * 6 * rx_total,
                          cudaMemcpyDeviceToHost, st));
+    out.field64.clear();
+    if (field_check) {
+      out.field64.resize(6 * size_t(rx_total));
+      if (rx_total)
+        CK(cudaMemcpyAsync(out.field64.data(), W.field64.p, sizeof(double) * 6 * rx_total,
+                           cudaMemcpyDeviceToHost, st));
+    }
     std::vector<int> order(ns), nray(ns), starts(rx_total + 1);
     std::vector<Survivor> sv(ns);
     std::vector<double> pf(6 * ns), pts(ns * (kMaxDepth + 2) * 3);
@@ -1801,6 +1831,7 @@ std::vector<sbr_result*> split_result(const sbr_result& b) {
     auto* x = new sbr_result();
     const size_t nf = 6 * size_t(b.rx_per_request[r]);
     x->field.assign(b.field.begin() + f0, b.field.begin() + f0 + nf);
+    if (!b.field64.empty()) x->field64.assign(b.field64.begin() + f0, b.field64.begin() + f0 + nf);
     f0 += nf;
     for (const sbr_path& p : b.paths) {
       if (p.request != r) continue;
@@ -2075,6 +2106,56 @@ sbr_status sbr_result_field(const sbr_result* r, double* out) {
     return SBR_ERR_INVALID_ARG;
   }
   std::copy(r->field.begin(), r->field.end(), out);
+  return SBR_OK;
+}
+
+sbr_status sbr_result_field_fp64(const sbr_result* r, double* out) {
+  if (!r || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  if (r->field64.size() != r->field.size()) {
+    set_err("sbr_result_field_fp64: the request did not set field_check with an FP32 precision");
+    return SBR_ERR_NOT_READY;
+  }
+  std::copy(r->field64.begin(), r->field64.end(), out);
+  return SBR_OK;
+}
+
+sbr_status sbr_result_field_error(const sbr_result* r, sbr_field_error* out) {
+  if (!r || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  if (r->field64.size() != r->field.size()) {
+    set_err("sbr_result_field_error: the request did not set field_check with an FP32 precision");
+    return SBR_ERR_NOT_READY;
+  }
+  sbr_field_error e{};
+  const size_t n_rx = r->field.size() / 6;
+  for (size_t k = 0; k < n_rx; ++k) {
+    const double* a = &r->field[6 * k];
+    const double* b = &r->field64[6 * k];
+    double scale = 0;
+    for (int j = 0; j < 3; ++j) scale = std::max(scale, std::hypot(b[2 * j], b[2 * j + 1]));
+    if (scale == 0) continue;
+    for (int j = 0; j < 3; ++j) {
+      const double ar = a[2 * j], ai = a[2 * j + 1], br = b[2 * j], bi = b[2 * j + 1];
+      const double mb = std::hypot(br, bi);
+      if (!(mb > 1e-6 * scale)) continue;
+      const double ma = std::hypot(ar, ai);
+      const double rel_mag = std::fabs(ma - mb) / mb;
+      // arg(a * conj(b))
+      const double ph = std::fabs(std::atan2(ai * br - ar * bi, ar * br + ai * bi));
+      const double rel_vec = std::hypot(ar - br, ai - bi) / mb;
+      ++e.components;
+      if (rel_mag > 1e-4 || ph > 1e-3) ++e.over_tolerance;
+      e.max_rel_mag = std::max(e.max_rel_mag, rel_mag);
+      e.max_phase_rad = std::max(e.max_phase_rad, ph);
+      e.max_rel_vec = std::max(e.max_rel_vec, rel_vec);
+    }
+  }
+  *out = e;
   return SBR_OK;
 }
 

@@ -167,7 +167,9 @@ __device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, R lam, bool i
 // One corrected path: n rays with endpoints pts[i] -> pts[i+1], the hit
 // triangle frame of ray i's end (or none for the last ray), and the kind /
 // material of each ray's start.  Returns E (3 complex, global Cartesian).
-template <class R>
+// R: real type of the rotation/Fresnel arithmetic.  fp32_phase: also take the
+// path length and the phase k*L in FP32 (only to measure what FP64 phase buys).
+template <class R, bool fp32_phase = false>
 __device__ void path_field(int n, const double (*pts)[3], const double* const* frames,
                            const int* kind, const int* mat, const Material* mats,
                            const double* txcs, double freq, double pt, int antenna,
@@ -251,6 +253,22 @@ __device__ void path_field(int n, const double (*pts)[3], const double* const* f
     mtv(cur, c, tot);   // back to global: current^T
   }
   // E * exp(-j k L) / L with k L in FP64 and reduced mod 2 pi before sin/cos
+  if (fp32_phase) {
+    const float k32 = float((2.0 * K.pi_hi) / lam64);
+    float L32 = 0.0f;
+    for (int i = 0; i < n; ++i) {
+      const float dx = float(pts[i + 1][0] - pts[i][0]), dy = float(pts[i + 1][1] - pts[i][1]),
+                  dz = float(pts[i + 1][2] - pts[i][2]);
+      L32 += sqrtf(dx * dx + dy * dy + dz * dz);
+    }
+    const float kl = k32 * L32;
+    const float s = sinf(-kl), c = cosf(-kl);
+    for (int j = 0; j < 3; ++j) {
+      const float re = float(tot[j].re), im = float(tot[j].im);
+      out[j] = Cx<double>{double((re * c - im * s) / L32), double((re * s + im * c) / L32)};
+    }
+    return;
+  }
   const double k = (2.0 * K.pi_hi) / lam64;
   const double kl = k * L;
   const double s = sin(-kl), c = cos(-kl);

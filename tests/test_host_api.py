@@ -1,5 +1,6 @@
 """Host-side mirror of the reference interface (no GPU)."""
 import numpy as np
+import pytest
 
 from sbrsolver_gb300 import api, scenes
 
@@ -48,3 +49,29 @@ def test_pcg32_reference_values():
     # PCG32 demo stream: seed 42, sequence 54 (O'Neill's pcg32-demo output)
     g = scenes.PCG32(42, 54)
     assert [g.next_u32() for _ in range(3)] == [0xa15c02b7, 0x7b47f409, 0xba1d3330]
+
+
+def test_field_error_stats_definitions():
+    from sbrsolver_gb300 import api
+    ref = np.array([[1 + 0j, 1e-9 + 0j, 0j], [0j, 0j, 0j], [2j, 1 + 1j, 0.5 + 0j]])
+    a = ref.copy()
+    a[0, 0] = 1.00005 * np.exp(2e-3j)   # 5e-5 magnitude, 2e-3 rad phase
+    a[2, 1] = (1 + 1j) * 1.0002         # 2e-4 magnitude
+    st = api.field_error_stats(a, ref)
+    # components above 1e-6 of their receiver's largest: 1 + 3; empty receiver skipped
+    assert st["components"] == 4 and st["receivers_with_field"] == 2
+    assert st["max_rel_mag"] == pytest.approx(2e-4, rel=1e-6)
+    assert st["max_phase_rad"] == pytest.approx(2e-3, rel=1e-6)
+    assert st["over_tolerance"] == 2
+    assert api.field_error_stats(ref, ref)["max_rel_vec"] == 0.0
+
+
+def test_same_path_set():
+    from sbrsolver_gb300 import api
+    a = {k: np.arange(4) for k in ("request", "receiver", "launch", "heap", "n_rays")}
+    a.update(tri=np.arange(7), cop=np.arange(7), kind=np.zeros(7))
+    b = {k: v.copy() for k, v in a.items()}
+    assert api.same_path_set(a, b)
+    b["tri"][3] = 99
+    assert not api.same_path_set(a, b)
+    assert api.same_path_set([], [])

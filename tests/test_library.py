@@ -22,12 +22,43 @@ def _gpu_present():
 
 def test_header_and_exports_agree(built):
     hdr = open(os.path.join(ROOT, "include", "sbr.h")).read()
-    declared = set(re.findall(r"\b(sbr_[a-z_]+)\s*\(", hdr))
+    declared = set(re.findall(r"\b(sbr_[a-z0-9_]+)\s*\(", hdr))
     assert declared == set(_lib.EXPORTS)
     lib = _lib.load()
     for name in declared:
         assert hasattr(lib, name), name
     assert b"sm_103a" in lib.sbr_version()
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes structures have the header's sizes and field offsets (a C
+    program compiled against include/sbr.h prints them)."""
+    checks = {"sbr_request": (_lib.Request, ["n_rx", "rx", "stage_counts", "field_check"]),
+              "sbr_counts": (_lib.Counts, ["keys"]),
+              "sbr_path": (_lib.Path, ["launch", "field"]),
+              "sbr_timing": (_lib.Timing, ["device_ms"]),
+              "sbr_field_error": (_lib.FieldError, ["max_rel_vec"]),
+              "sbr_completion": (_lib.Completion, ["counts", "result"]),
+              "sbr_material": (_lib.Material, ["rel_conductivity"]),
+              "sbr_scene_info": (_lib.SceneInfo, ["device_bytes"])}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "sbr.h"', "int main(void) {"]
+    for t, (_, fields) in checks.items():
+        lines.append(f'  printf("{t} %zu\\n", sizeof({t}));')
+        for f in fields:
+            lines.append(f'  printf("{t}.{f} %zu\\n", offsetof({t}, {f}));')
+    lines.append("  return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    import subprocess
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                 check=True).stdout.splitlines())
+    for t, (cls, fields) in checks.items():
+        assert int(got[t]) == C.sizeof(cls), t
+        for f in fields:
+            assert int(got[f"{t}.{f}"]) == getattr(cls, f).offset, (t, f)
 
 
 def test_null_arguments_are_rejected(built):
