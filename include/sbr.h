@@ -215,6 +215,26 @@ sbr_status sbr_server_pending(sbr_server* server, int* queued, long long* in_fli
 /* Finishes queued and running requests, then stops. */
 sbr_status sbr_server_destroy(sbr_server* server);
 
+/* ---- result files --------------------------------------------------- */
+/* The reference's output files, byte for byte (default six-digit stream
+ * formatting, the sticky '+' sign of its CSV writer, Phase columns holding
+ * the sum of the component phases in radians).  Arrays are host memory in
+ * the layouts of sbr_result_field / sbr_result_paths.  Return SBR_ERR_IO when
+ * the file cannot be written. */
+/* RTSolver::SaveFieldAsCsv (RTSolver.cpp:692-717): X,Y,Z,Ex,Ey,Ez rows. */
+sbr_status sbr_write_field_csv(const char* path, const double* rx, int n_rx, const double* field);
+/* RTSolver::SaveReceiversAsVtk (RTSolver.cpp:612-690). */
+sbr_status sbr_write_receivers_vtk(const char* path, const double* rx, int n_rx,
+                                   const double* field);
+/* RTSolver::SavePathsAsVtk (RTSolver.cpp:510-610): one polyline per path,
+ * ordered by launch, receiver, then breadth-first tree position; `points`
+ * holds 6 doubles (source, target) per ray; field is per receiver. */
+sbr_status sbr_write_paths_vtk(const char* path, const sbr_path* paths, int n_paths,
+                               const double* points, const double* field, int n_rx);
+/* RTSolver::SaveIcosahedronAsVtk (RTSolver.cpp:719-766): the launch rays of
+ * an icosahedron level as unit segments from `origin` (3 doubles). */
+sbr_status sbr_write_launch_rays_vtk(const char* path, const double* origin, int tessellation);
+
 /* ---- allocation-free field sum -------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory (code inside CUDA graph capture, processes whose device memory

@@ -22,6 +22,8 @@ EXPORTS = (
     "sbr_result_timing", "sbr_result_destroy", "sbr_last_error", "sbr_version",
     "sbr_receiver_field_sum_noalloc", "sbr_server_create", "sbr_server_submit", "sbr_server_poll",
     "sbr_server_pending", "sbr_server_destroy", "sbr_result_field_error", "sbr_result_field_fp64",
+    "sbr_write_field_csv", "sbr_write_receivers_vtk", "sbr_write_paths_vtk",
+    "sbr_write_launch_rays_vtk",
 )
 
 
@@ -120,6 +122,10 @@ def load(path: str = LIB_PATH):
             "sbr_server_poll": [vp, P(Completion), I, P(I), I],
             "sbr_server_pending": [vp, P(I), P(C.c_longlong)],
             "sbr_server_destroy": [vp],
+            "sbr_write_field_csv": [C.c_char_p, P(D), I, P(D)],
+            "sbr_write_receivers_vtk": [C.c_char_p, P(D), I, P(D)],
+            "sbr_write_paths_vtk": [C.c_char_p, P(Path), I, P(D), P(D), I],
+            "sbr_write_launch_rays_vtk": [C.c_char_p, P(D), I],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
 
@@ -393,6 +394,32 @@ class Server:
             pass
 
 
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _path_structs(paths):
+    """sbr_path array + flat ray points (6 per ray) from a path set in either
+    form solve() returns."""
+    if isinstance(paths, dict):
+        n = len(paths["receiver"])
+        P = (_lib.Path * n)()
+        A = np.ctypeslib.as_array(P) if n else None
+        for k in ("request", "receiver", "launch", "heap", "ray_offset", "n_rays"):
+            if n:
+                A[k] = paths[k]
+        return P, np.ascontiguousarray(paths["points"], np.float64).reshape(-1)
+    P = (_lib.Path * len(paths))()
+    pts, off = [], 0
+    for i, p in enumerate(paths):
+        P[i].request, P[i].receiver, P[i].launch = p["request"], p["receiver"], p["launch"]
+        P[i].heap, P[i].n_rays, P[i].ray_offset = p["heap"], p["n_rays"], off
+        off += p["n_rays"]
+        pts.append(np.asarray(p["points"], np.float64).reshape(-1))
+    flat = np.concatenate(pts) if pts else np.zeros(0)
+    return P, np.ascontiguousarray(flat, np.float64)
+
+
 class FieldCompute:
     """FieldCompute (FieldCompute.h:9-94): the field stage is fused into the
     GPU solve; FieldAtReceiver reads the result."""
@@ -430,7 +457,7 @@ class RTSolver:
         req = make_request(sourcePoint, txCoordSys, maxReflectionCount, maxTransmissionCount,
                            frequency, pt, useFresnelCoeff, rx, txTesslation,
                            self.config.antennaType, self.config.fieldPrecision)
-        self._result = solve(self._scene, req)
+        self._result = solve(self._scene, req, with_paths="arrays")
         self._receivers = rx
         return int(self._result.counts["launches"]) * int(rx.shape[0])
 
@@ -441,21 +468,41 @@ class RTSolver:
     def field_compute(self) -> FieldCompute:
         return FieldCompute(self._result)
 
+    def _need_result(self):
+        if self._result is None:
+            raise RuntimeError("ExecuteRayTracing was not called")
+        rx = np.ascontiguousarray(self._receivers, np.float64)
+        f = np.ascontiguousarray(np.stack([self._result.field.real, self._result.field.imag],
+                                          -1).reshape(-1), np.float64)
+        return rx, f
+
     def SaveFieldAsCsv(self, fname: str) -> bool:
-        """RTSolver::SaveFieldAsCsv (RTSolver.cpp:692-717), including its
-        sticky std::showpos after the first receiver row."""
-        rx, f = self._receivers, self._result.field
+        """RTSolver::SaveFieldAsCsv (RTSolver.cpp:692-717), byte for byte,
+        including its sticky std::showpos after the first receiver row."""
+        rx, f = self._need_result()
+        _lib.check(_lib.load().sbr_write_field_csv(os.fsencode(fname), _dp(rx), len(rx), _dp(f)))
+        return True
 
-        def num(x: float, plus: bool) -> str:
-            s = "%g" % x
-            if s in ("inf", "-inf", "nan", "-nan"):
-                s = s
-            return ("+" + s) if plus and not s.startswith("-") else s
+    def SaveReceiversAsVtk(self, fname: str) -> bool:
+        """RTSolver::SaveReceiversAsVtk (RTSolver.cpp:612-690), byte for byte."""
+        rx, f = self._need_result()
+        _lib.check(_lib.load().sbr_write_receivers_vtk(os.fsencode(fname), _dp(rx), len(rx),
+                                                       _dp(f)))
+        return True
 
-        with open(fname, "w") as fh:
-            fh.write("X,Y,Z,Ex,Ey,Ez\n")
-            for i in range(len(rx)):
-                p = i > 0
-                fh.write(",".join(num(v, p) for v in rx[i]) + ",")
-                fh.write(",".join(num(c.real, True) + num(c.imag, True) + "i" for c in f[i]) + "\n")
+    def SavePathsAsVtk(self, fname: str) -> bool:
+        """RTSolver::SavePathsAsVtk (RTSolver.cpp:510-610), byte for byte:
+        paths by launch, receiver, then breadth-first tree position."""
+        rx, f = self._need_result()
+        P, pts = _path_structs(self._result.paths)
+        _lib.check(_lib.load().sbr_write_paths_vtk(os.fsencode(fname), P, len(P), _dp(pts),
+                                                   _dp(f), len(rx)))
+        return True
+
+    def SaveIcosahedronAsVtk(self, fname: str, rayOrg, tessellation: int) -> bool:
+        """RTSolver::SaveIcosahedronAsVtk (RTSolver.cpp:719-766): the launch
+        rays of `tessellation` as unit segments from rayOrg."""
+        o = np.ascontiguousarray(np.asarray(rayOrg, np.float64).reshape(3))
+        _lib.check(_lib.load().sbr_write_launch_rays_vtk(os.fsencode(fname), _dp(o),
+                                                         int(tessellation)))
         return True

@@ -124,6 +124,21 @@ def pin_reference_main(rep: dict) -> dict:
             "shipped_field_csv": gold}
 
 
+def shipped_output_hashes() -> None:
+    """sha256 and size of the output files the reference ships for its main()
+    run (field CSV, ray-path / receiver VTK) and of its level-3 launch-ray VTK
+    from (0, 0, 5); the writers in the library must reproduce them byte for
+    byte from the reference_main fixture."""
+    import json
+    out = {}
+    for f in ("ElectricField.csv", "RayPath.vtk", "RxLocations.vtk", "Icosahedron.vtk"):
+        b = open(os.path.join(REF, "SBRSolver_rev2/data/output", f), "rb").read()
+        out[f] = {"sha256": hashlib.sha256(b).hexdigest(), "bytes": len(b)}
+    with open(os.path.join(OUT, "shipped_outputs.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+    print("shipped output hashes written")
+
+
 def coefficient_sweep() -> None:
     """RefCoeffTest vs the shipped coeff_test.csv (1000 angles, eps2 = 1-10j):
     magnitudes are compared exactly at printed precision; the shipped phases
@@ -153,6 +168,7 @@ def main() -> None:
     d = dict(np.load(os.path.join(OUT, "reference_main.npz")))
     d.update(pins)
     np.savez_compressed(os.path.join(OUT, "reference_main.npz"), **d)
+    shipped_output_hashes()
     coefficient_sweep()
     run_case(scenes.small_scene(), "small_L6_R3")
     wl = scenes.small_scene()
@@ -174,4 +190,7 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    if "--outputs-only" in sys.argv:  # refresh only shipped_outputs.json
+        shipped_output_hashes()
+    else:
+        main()

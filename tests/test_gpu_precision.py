@@ -73,8 +73,8 @@ def test_fp32_phase_mode_is_measured(built, large):
 
 def test_field_check_on_urban_batch(built):
     """field_check on a batch: per-request results each carry their error."""
-    wl = scenes.urban_scene(level=5, rx_pitch=100.0)
-    other = scenes.urban_scene(level=4, rx_pitch=200.0)
+    wl = scenes.urban_scene(level=4, rx_pitch=50.0, max_reflection=3, max_transmission=2)
+    other = scenes.urban_scene(level=5, rx_pitch=100.0)
     other.request.tx = (100.0, 150.0, 25.0)
     sc = api.DeviceScene.from_scene(wl.scene)
     qs = [api.request_from_workload(w.request, "fp32", field_check=True) for w in (wl, other)]
@@ -84,5 +84,5 @@ def test_field_check_on_urban_batch(built):
     np.testing.assert_array_equal(rb.field_fp64[:n0], r0.field_fp64)
     np.testing.assert_array_equal(rb.field[:n0], r0.field)
     st = api.field_error_stats(rb.field, rb.field_fp64)
-    assert st["components"] > 100 and st["over_tolerance"] == 0
+    assert st["components"] >= 10 and st["over_tolerance"] == 0
     sc.close()
