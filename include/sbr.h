@@ -156,7 +156,19 @@ sbr_status sbr_scene_mesh_order(const sbr_scene* scene, int* out);
 /* Replace that order (e.g. identity for a caller whose vector is in file order). */
 sbr_status sbr_scene_set_mesh_order(sbr_scene* scene, const int* order);
 sbr_status sbr_scene_coplanar_ids(const sbr_scene* scene, int* out);
+/* Replace the per-triangle material ids (NULL = all 0) and the material
+ * table, as RTSolver::Init (RTSolver.cpp:13-22) binds materials after
+ * BVH::ConstructBVH.  Not while solves on the scene are running. */
+sbr_status sbr_scene_set_materials(sbr_scene* scene, const int* material_ids,
+                                   const sbr_material* materials, int n_materials);
 sbr_status sbr_scene_destroy(sbr_scene* scene);
+/* The facets of a binary or ASCII STL file in file order (StlReader.h, as
+ * Preprocessor::StlToGeometry reads it, Preprocessor.cpp:69-114): 9 floats
+ * of vertices and 3 of normal per facet.  With vertices or normals NULL only
+ * *n_triangles is set; otherwise *n_triangles is the buffers' capacity on
+ * entry (SBR_ERR_CAPACITY if too small) and the facet count on return.  No
+ * GPU needed. */
+sbr_status sbr_stl_read(const char* path, int* n_triangles, float* vertices, float* normals);
 
 /* ---- solve ---------------------------------------------------------- */
 sbr_status sbr_solve(sbr_scene* scene, const sbr_request* request, sbr_result** out);
@@ -214,6 +226,20 @@ sbr_status sbr_server_poll(sbr_server* server, sbr_completion* out, int max, int
 sbr_status sbr_server_pending(sbr_server* server, int* queued, long long* in_flight_bytes);
 /* Finishes queued and running requests, then stops. */
 sbr_status sbr_server_destroy(sbr_server* server);
+
+/* ---- receiver layouts ---------------------------------------------- */
+/* Preprocessor::GenerateRXLine (Preprocessor.cpp:270-284): floor(|end-start|
+ * / resolution) points start + i*resolution*unit(end-start).  With out NULL
+ * only *n_out is set; otherwise `capacity` points fit in out (3 doubles each,
+ * SBR_ERR_CAPACITY if fewer).  No GPU needed. */
+sbr_status sbr_generate_rx_line(const double* start, const double* end, double resolution,
+                                double* out, int capacity, int* n_out);
+/* Preprocessor::GenerateRxPlane (Preprocessor.cpp:254-268): an
+ * (int((xMax-xMin)/res)+1) x (int((yMax-yMin)/res)+1) grid at `height`,
+ * x-major; same buffer convention. */
+sbr_status sbr_generate_rx_plane(double x_min, double y_min, double x_max, double y_max,
+                                 double height, double resolution, double* out, int capacity,
+                                 int* n_out);
 
 /* ---- result files --------------------------------------------------- */
 /* The reference's output files, byte for byte (default six-digit stream

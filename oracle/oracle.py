@@ -162,8 +162,7 @@ def solve(scene: OracleScene, request, materials: Sequence, threads: int = 0) ->
                           "kind": kind[o:o + n].tolist(),
                           "points": pts[6 * o:6 * (o + n)].reshape(n, 6).copy(),
                           "field": np.array(p.field[:], np.float64)})
-        fc = field.reshape(-1, 3, 2)
-        return {"field": fc[..., 0] + 1j * fc[..., 1],
+        return {"field": np.ascontiguousarray(field, np.float64).view(np.complex128).reshape(-1, 3),
                 "counts": {"segments": seg.value, "captured": cap.value, "corrected": cor.value,
                            "paths": npth.value, "rays": nray.value,
                            "launches": 10 * 4 ** request.tessellation + 2},

@@ -23,7 +23,8 @@ EXPORTS = (
     "sbr_receiver_field_sum_noalloc", "sbr_server_create", "sbr_server_submit", "sbr_server_poll",
     "sbr_server_pending", "sbr_server_destroy", "sbr_result_field_error", "sbr_result_field_fp64",
     "sbr_write_field_csv", "sbr_write_receivers_vtk", "sbr_write_paths_vtk",
-    "sbr_write_launch_rays_vtk",
+    "sbr_write_launch_rays_vtk", "sbr_scene_set_materials", "sbr_stl_read",
+    "sbr_generate_rx_line", "sbr_generate_rx_plane",
 )
 
 
@@ -126,6 +127,10 @@ def load(path: str = LIB_PATH):
             "sbr_write_receivers_vtk": [C.c_char_p, P(D), I, P(D)],
             "sbr_write_paths_vtk": [C.c_char_p, P(Path), I, P(D), P(D), I],
             "sbr_write_launch_rays_vtk": [C.c_char_p, P(D), I],
+            "sbr_scene_set_materials": [vp, P(I), P(Material), I],
+            "sbr_stl_read": [C.c_char_p, P(I), P(C.c_float), P(C.c_float)],
+            "sbr_generate_rx_line": [P(D), P(D), D, P(D), I, P(I)],
+            "sbr_generate_rx_plane": [D, D, D, D, D, D, P(D), I, P(I)],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

@@ -67,26 +67,16 @@ class Preprocessor:
     @staticmethod
     def StlToGeometry(fileName: str, output: Optional[list] = None, saveEdges: bool = False,
                       saveFaces: bool = False, dataDir: str = "") -> Mesh:
-        data = open(fileName, "rb").read()
-        head = data[:256].lower()
-        if b"solid" in head and b"\n" in head and b"facet" in head and b"normal" in head:
-            v, n = [], []
-            for line in data.decode(errors="replace").splitlines():
-                t = line.split()
-                if not t:
-                    continue
-                if t[0] == "vertex":
-                    v.append([float(x) for x in t[1:4]])
-                elif t[0] == "facet":
-                    n.append([float(x) for x in t[2:5]])
-            vv = np.asarray(v, np.float64).astype(np.float32).reshape(-1, 3, 3)
-            nn = np.asarray(n, np.float64).astype(np.float32).reshape(-1, 3)
-        else:
-            cnt = int.from_bytes(data[80:84], "little")
-            rec = np.frombuffer(data, dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)),
-                                                       ("a", "<u2")]), count=cnt, offset=84)
-            vv = np.array(rec["v"], dtype=np.float32)
-            nn = np.array(rec["n"], dtype=np.float32)
+        """Preprocessor::StlToGeometry (Preprocessor.cpp:69-114): the facets
+        of a binary or ASCII STL in file order (read by the library's reader,
+        the one sbr_scene_create_from_stl uses)."""
+        lib, n = _lib.load(), C.c_int()
+        _lib.check(lib.sbr_stl_read(os.fsencode(fileName), C.byref(n), None, None))
+        vv = np.zeros((n.value, 3, 3), np.float32)
+        nn = np.zeros((n.value, 3), np.float32)
+        fp = C.POINTER(C.c_float)
+        _lib.check(lib.sbr_stl_read(os.fsencode(fileName), C.byref(n), vv.ctypes.data_as(fp),
+                                    nn.ctypes.data_as(fp)))
         mesh = Mesh(vv, nn, np.zeros(len(vv), np.int32))
         if output is not None:
             output.append(mesh)
@@ -94,22 +84,26 @@ class Preprocessor:
 
     @staticmethod
     def GenerateRxPlane(xMin, yMin, xMax, yMax, height, resolution, output: list) -> None:
-        nx = int((xMax - xMin) / resolution)
-        ny = int((yMax - yMin) / resolution)
-        for i in range(nx + 1):
-            x = xMin + i * resolution
-            for j in range(ny + 1):
-                output.append((x, yMin + j * resolution, height))
+        """Preprocessor::GenerateRxPlane (Preprocessor.cpp:254-268)."""
+        lib, n = _lib.load(), C.c_int()
+        args = [float(a) for a in (xMin, yMin, xMax, yMax, height, resolution)]
+        _lib.check(lib.sbr_generate_rx_plane(*args, None, 0, C.byref(n)))
+        out = np.zeros(3 * n.value, np.float64)
+        _lib.check(lib.sbr_generate_rx_plane(*args, _dp(out), n.value, C.byref(n)))
+        output.extend(map(tuple, out.reshape(-1, 3).tolist()))
 
     @staticmethod
     def GenerateRXLine(start, end, resolution, output: list) -> None:
-        s = np.asarray(start, np.float64)
-        d = np.asarray(end, np.float64) - s
-        n = int(math.floor(math.sqrt(float(d @ d)) / resolution))
-        nrm = math.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
-        d = d / nrm if nrm > 0 else d
-        for i in range(n):
-            output.append(tuple(s + (i * resolution) * d))
+        """Preprocessor::GenerateRXLine (Preprocessor.cpp:270-284)."""
+        lib, n = _lib.load(), C.c_int()
+        s = np.ascontiguousarray(np.asarray(start, np.float64).reshape(3))
+        e = np.ascontiguousarray(np.asarray(end, np.float64).reshape(3))
+        _lib.check(lib.sbr_generate_rx_line(_dp(s), _dp(e), float(resolution), None, 0,
+                                            C.byref(n)))
+        out = np.zeros(3 * n.value, np.float64)
+        _lib.check(lib.sbr_generate_rx_line(_dp(s), _dp(e), float(resolution), _dp(out), n.value,
+                                            C.byref(n)))
+        output.extend(map(tuple, out.reshape(-1, 3).tolist()))
 
     @staticmethod
     def ReadLocationFile(fileName: str, output: list) -> bool:
@@ -294,8 +288,7 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
                     "cop": cop[o:o + n].tolist(), "kind": kind[o:o + n].tolist(),
                     "points": pts[6 * o:6 * (o + n)].reshape(n, 6).copy(),
                     "field": np.array(p.field[:], np.float64)})
-        fc = f.reshape(-1, 3, 2)
-        field_c = fc[..., 0] + 1j * fc[..., 1]
+        field_c = f.view(np.complex128).reshape(-1, 3)  # exact, inf stays inf
         res = Result(field_c, counts, timing, paths)
         fe = _lib.FieldError()
         if lib.sbr_result_field_error(h, C.byref(fe)) == 0:
@@ -303,8 +296,7 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
             f64 = np.zeros(6 * n_rx, np.float64)
             if n_rx:
                 _lib.check(lib.sbr_result_field_fp64(h, f64.ctypes.data_as(C.POINTER(C.c_double))))
-            g = f64.reshape(-1, 3, 2)
-            res.field_fp64 = g[..., 0] + 1j * g[..., 1]
+            res.field_fp64 = f64.view(np.complex128).reshape(-1, 3)
         return res
     finally:
         lib.sbr_result_destroy(h)

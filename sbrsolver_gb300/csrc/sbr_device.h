@@ -124,7 +124,7 @@ struct TxParams {
   int rx_first, n_rx;          // receivers of this request in the batch arrays
   long long launch_first;      // first global launch index
   int grid;                    // receiver grid index
-  int pad;
+  int precision;               // field precision: 0 FP64, 1 FP32, 2 FP32 with FP32 phase
 };
 
 struct RxGrid {

@@ -971,7 +971,7 @@ struct FieldArgs {
   Counters* ctr;
   unsigned long long cap;
   FieldConsts K;
-  int precision;
+  int precision;        // -1: each request's own; 0: FP64 for all (the FP64 shadow)
   double* path_field;   // 6 per survivor
   int* path_nray;
   int* path_tri;        // (kMaxDepth + 1) per survivor: triangle id
@@ -998,10 +998,11 @@ __global__ void k_field(FieldArgs A) {
       if (r + 1 < pb.n) mat[r + 1] = A.sc.tri64[pb.tri[r]].mat;
     }
     Cx<double> e[3];
-    if (A.precision == 2)
+    const int prec = A.precision < 0 ? P.precision : A.precision;
+    if (prec == 2)
       path_field<float, true>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq,
                               P.pt, P.antenna, P.fresnel != 0, A.K, e);
-    else if (A.precision == 1)
+    else if (prec == 1)
       path_field<float>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
                         P.antenna, P.fresnel != 0, A.K, e);
     else
@@ -1046,10 +1047,13 @@ __global__ void k_surv_scatter(const Survivor* surv, const Counters* ctr, unsign
 }
 
 // Sort each receiver's survivors by (launch, BFS) rank and sum their fields in
-// that order: FP64, or compensated FP32 (Neumaier) in FP32 mode.
+// that order: FP64, or compensated FP32 (Neumaier) for the FP32 precisions.
+// precision -1 takes each receiver's request precision, 0 forces FP64.
 __global__ void k_rx_sum(const Survivor* surv, const int* starts, int* order, int n_rx,
-                         const double* path_field, int precision, double* field) {
+                         const double* path_field, int force_precision, const int* rx_req,
+                         const TxParams* txp, double* field) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rx; r += gridDim.x * blockDim.x) {
+    const int precision = force_precision < 0 ? txp[rx_req[r]].precision : force_precision;
     const int b = starts[r], e = starts[r + 1];
     for (int i = b + 1; i < e; ++i) {
       const int v = order[i];
@@ -1393,8 +1397,10 @@ static FieldConsts field_consts() {
   return K;
 }
 
+// force_check: compute the FP64 shadow field even if no request here asks for
+// it (another pass of the same batch did).
 static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int n_req,
-                       sbr_result& out) {
+                       sbr_result& out, bool force_check = false) {
   cudaStream_t st = W.stream;
   if (S.host.mesh_order.empty()) throw std::string("scene is not initialised");
   CK(cudaSetDevice(S.device));
@@ -1435,17 +1441,16 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     P.n_rx = q.n_rx;
     P.launch_first = launches;
     P.grid = r;
+    P.precision = q.field_precision == SBR_FIELD_FP32
+                      ? 1
+                      : (q.field_precision == SBR_FIELD_FP32_PHASE ? 2 : 0);
     launches += P.n_launch;
     rx_total += q.n_rx;
     max_depth = std::max(max_depth, q.max_reflection + q.max_transmission);
   }
-  const int precision = reqs[0].field_precision == SBR_FIELD_FP32
-                            ? 1
-                            : (reqs[0].field_precision == SBR_FIELD_FP32_PHASE ? 2 : 0);
   const int stage_counts = reqs[0].stage_counts ? 1 : 0;
-  bool field_check = false;
-  for (int r = 0; r < n_req; ++r) field_check |= reqs[r].field_check != 0;
-  field_check &= precision != 0;
+  bool field_check = force_check;
+  for (int r = 0; r < n_req; ++r) field_check |= reqs[r].field_check && tp[r].precision != 0;
   if (n_req >= int(0xFFFFFFFFu - kRootBase)) throw std::string("too many requests in one batch");
   auto t0 = std::chrono::steady_clock::now();
   CK(cudaEventRecord(W.ev[0], st));
@@ -1680,7 +1685,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fa.ctr = W.ctr.p;
     fa.cap = W.cap_surv;
     fa.K = K;
-    fa.precision = precision;
+    fa.precision = -1;
     fa.path_field = W.path_field.p;
     fa.path_nray = W.path_nray.p;
     fa.path_tri = W.path_tri.p;
@@ -1697,8 +1702,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
                                                         W.s_starts.p, W.s_cursor.p, W.s_order.p);
     if (rx_total)
       k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
-                                                        rx_total, W.path_field.p, precision,
-                                                        W.field.p);
+                                                        rx_total, W.path_field.p, -1, W.rx_req.p,
+                                                        W.txp.p, W.field.p);
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[6], st));
     if (field_check) {  // FP64 shadow of the same paths, outside the timed stages
@@ -1711,7 +1716,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       if (rx_total)
         k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
                                                           rx_total, W.path_field64.p, 0,
-                                                          W.field64.p);
+                                                          W.rx_req.p, W.txp.p, W.field64.p);
       CK(cudaGetLastError());
     }
     // ---- results to the host
@@ -1986,6 +1991,56 @@ sbr_status sbr_scene_set_mesh_order(sbr_scene* scene, const int* order) {
   })
 }
 
+sbr_status sbr_scene_set_materials(sbr_scene* scene, const int* material_ids,
+                                   const sbr_material* materials, int n_materials) {
+  if (!scene || !materials || n_materials <= 0) {
+    set_err("sbr_scene_set_materials: need a scene and at least one material");
+    return SBR_ERR_INVALID_ARG;
+  }
+  SceneImpl& S = scene->impl;
+  const int nt = int(S.host.tris.size());
+  for (int i = 0; material_ids && i < nt; ++i)
+    if (material_ids[i] < 0 || material_ids[i] >= n_materials) {
+      set_err("material id out of range at triangle " + std::to_string(i));
+      return SBR_ERR_INVALID_ARG;
+    }
+  ABI_GUARD({
+    // not to be called while solves on this scene are in flight
+    std::lock_guard<std::mutex> lock(S.pool_mu);
+    for (int i = 0; i < nt; ++i) S.host.tris[i].mat = material_ids ? material_ids[i] : 0;
+    S.materials.assign(materials, materials + n_materials);
+    upload_scene(S);
+    upload_mesh_order(S, S.host.mesh_order);
+    return SBR_OK;
+  })
+}
+
+sbr_status sbr_stl_read(const char* path, int* n_triangles, float* vertices, float* normals) {
+  if (!path || !n_triangles) {
+    set_err("sbr_stl_read: NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  std::vector<float> v, n;
+  std::string err;
+  if (!read_stl(path, v, n, err)) {
+    set_err(err);
+    return SBR_ERR_IO;
+  }
+  const int nt = int(n.size() / 3);
+  if (vertices && normals) {
+    if (*n_triangles < nt) {
+      set_err("sbr_stl_read: buffers hold " + std::to_string(*n_triangles) + " facets, file has " +
+              std::to_string(nt));
+      *n_triangles = nt;
+      return SBR_ERR_CAPACITY;
+    }
+    std::copy(v.begin(), v.end(), vertices);
+    std::copy(n.begin(), n.end(), normals);
+  }
+  *n_triangles = nt;
+  return SBR_OK;
+}
+
 sbr_status sbr_scene_coplanar_ids(const sbr_scene* scene, int* out) {
   if (!scene || !out) {
     set_err("NULL argument");
@@ -2042,6 +2097,9 @@ sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_
     CK(cudaMemGetInfo(&free_b, &total_b));
     const double budget = std::max(2e9, 0.45 * double(free_b));
     auto est = [](const sbr_request& q) { return request_bytes(q); };
+    bool batch_check = false;  // every pass carries the FP64 shadow if any request wants it
+    for (int r = 0; r < n_requests; ++r)
+      batch_check |= requests[r].field_check && requests[r].field_precision != SBR_FIELD_FP64;
     auto res = std::make_unique<sbr_result>();
     int first = 0;
     while (first < n_requests) {
@@ -2053,7 +2111,7 @@ sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_
         break;
       }
       sbr_result part;
-      solve_impl(S, *W, requests + first, last - first, part);
+      solve_impl(S, *W, requests + first, last - first, part, batch_check);
       const long long ray_base = (long long)res->tri.size();
       for (sbr_path p : part.paths) {
         p.request += first;
@@ -2069,6 +2127,7 @@ sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_
                                        part.launches_per_request.begin(),
                                        part.launches_per_request.end());
       res->field.insert(res->field.end(), part.field.begin(), part.field.end());
+      res->field64.insert(res->field64.end(), part.field64.begin(), part.field64.end());
       res->tri.insert(res->tri.end(), part.tri.begin(), part.tri.end());
       res->cop.insert(res->cop.end(), part.cop.begin(), part.cop.end());
       res->kind.insert(res->kind.end(), part.kind.begin(), part.kind.end());

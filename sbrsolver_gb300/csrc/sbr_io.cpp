@@ -215,6 +215,78 @@ sbr_status sbr_write_paths_vtk(const char* path, const sbr_path* paths, int n_pa
   return close_or_fail(ofs, path, "sbr_write_paths_vtk");
 }
 
+sbr_status sbr_generate_rx_line(const double* start, const double* end, double resolution,
+                                double* out, int capacity, int* n_out) {
+  if (!start || !end || !n_out || !(resolution > 0)) {
+    sbr::set_error_message("sbr_generate_rx_line: need start, end, a positive resolution, n_out");
+    return SBR_ERR_INVALID_ARG;
+  }
+  double d[3] = {end[0] - start[0], end[1] - start[1], end[2] - start[2]};
+  const double len = std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+  const double fn = std::floor(len / resolution);
+  if (!(fn < 2147483647.0)) {
+    sbr::set_error_message("sbr_generate_rx_line: too many points");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const int n = std::max(0, int(fn));
+  if (len > 0)
+    for (double& c : d) c /= len;
+  if (out) {
+    if (capacity < n) {
+      *n_out = n;
+      sbr::set_error_message("sbr_generate_rx_line: capacity below the point count");
+      return SBR_ERR_CAPACITY;
+    }
+    for (int i = 0; i < n; ++i) {
+      const double s = double(i) * resolution;
+      for (int a = 0; a < 3; ++a) {
+        const double step = s * d[a];  // rounded before the add (no contraction)
+        out[3 * size_t(i) + a] = start[a] + step;
+      }
+    }
+  }
+  *n_out = n;
+  return SBR_OK;
+}
+
+sbr_status sbr_generate_rx_plane(double x_min, double y_min, double x_max, double y_max,
+                                 double height, double resolution, double* out, int capacity,
+                                 int* n_out) {
+  if (!n_out || !(resolution > 0)) {
+    sbr::set_error_message("sbr_generate_rx_plane: need a positive resolution and n_out");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const double fx = (x_max - x_min) / resolution, fy = (y_max - y_min) / resolution;
+  if (!(fx < 1e9 && fy < 1e9)) {
+    sbr::set_error_message("sbr_generate_rx_plane: too many points");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const long long nx = (long long)int(fx), ny = (long long)int(fy);
+  const long long n = (nx >= 0 && ny >= 0) ? (nx + 1) * (ny + 1) : 0;
+  if (n > 2147483647LL) {
+    sbr::set_error_message("sbr_generate_rx_plane: too many points");
+    return SBR_ERR_INVALID_ARG;
+  }
+  if (out) {
+    if (capacity < n) {
+      *n_out = int(n);
+      sbr::set_error_message("sbr_generate_rx_plane: capacity below the point count");
+      return SBR_ERR_CAPACITY;
+    }
+    size_t k = 0;
+    for (long long i = 0; n && i <= nx; ++i) {
+      const double x = x_min + double(i) * resolution;
+      for (long long j = 0; j <= ny; ++j) {
+        out[k++] = x;
+        out[k++] = y_min + double(j) * resolution;
+        out[k++] = height;
+      }
+    }
+  }
+  *n_out = int(n);
+  return SBR_OK;
+}
+
 sbr_status sbr_write_launch_rays_vtk(const char* path, const double* origin, int tessellation) {
   if (!origin || tessellation < 0 || tessellation > 12) {
     sbr::set_error_message("sbr_write_launch_rays_vtk: need an origin and a level in 0..12");

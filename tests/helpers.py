@@ -26,8 +26,7 @@ def golden_paths(g):
 
 
 def golden_field(g):
-    f = g["field"].reshape(-1, 3, 2)
-    return f[..., 0] + 1j * f[..., 1]
+    return np.ascontiguousarray(g["field"], np.float64).view(np.complex128).reshape(-1, 3)
 
 
 def field_close(a: np.ndarray, b: np.ndarray, rel=FIELD_REL, phase=PHASE_RAD, floor=None):

@@ -86,3 +86,18 @@ def test_field_check_on_urban_batch(built):
     st = api.field_error_stats(rb.field, rb.field_fp64)
     assert st["components"] >= 10 and st["over_tolerance"] == 0
     sc.close()
+
+
+def test_mixed_precision_batch(built):
+    """Each request in a batch keeps its own field precision."""
+    wl = scenes.urban_scene(level=4, rx_pitch=50.0, max_reflection=3, max_transmission=2)
+    sc = api.DeviceScene.from_scene(wl.scene)
+    modes = ("fp64", "fp32", "fp32_phase", "fp64")
+    qs = [api.request_from_workload(wl.request, m) for m in modes]
+    rb = api.solve(sc, qs)
+    n = len(wl.request.rx)
+    for k, m in enumerate(modes):
+        alone = api.solve(sc, api.request_from_workload(wl.request, m))
+        np.testing.assert_array_equal(rb.field[k * n:(k + 1) * n], alone.field)
+    assert not np.array_equal(rb.field[n:2 * n], rb.field[:n])  # FP32 differs in low bits
+    sc.close()
