@@ -177,19 +177,37 @@ def serving_stream(scene_wls, n: int, seed: int = 0x5B5 + 4):
 
 
 def run_batched(precision: str):
+    """256 transmitters as one batched call against 256 plain calls, overall
+    and per icosahedron level (each level's requests batched on their own)."""
     from sbrsolver_gb300 import api
     wl, reqs = batched_workload()
     sc = api.DeviceScene.from_scene(wl.scene)
     qs = [api.request_from_workload(r, precision) for r in reqs]
     api.solve(sc, qs, with_paths=False)  # warm-up: sizes the buffers for the batch
+    t_req, seg_req = [], []
     t0 = time.perf_counter()
-    seg_plain = 0
     for q in qs:
-        seg_plain += api.solve(sc, q, with_paths=False).counts["segments"]
+        t1 = time.perf_counter()
+        seg_req.append(api.solve(sc, q, with_paths=False).counts["segments"])
+        t_req.append(time.perf_counter() - t1)
     t_plain = time.perf_counter() - t0
+    seg_plain = sum(seg_req)
     t0 = time.perf_counter()
     rb = api.solve(sc, qs, with_paths=False)
     t_batch = time.perf_counter() - t0
+    by_level = {}
+    for lvl in sorted({r.tessellation for r in reqs}):
+        idx = [i for i, r in enumerate(reqs) if r.tessellation == lvl]
+        sub = [qs[i] for i in idx]
+        t0 = time.perf_counter()
+        rs = api.solve(sc, sub, with_paths=False)
+        tb = time.perf_counter() - t0
+        tp = sum(t_req[i] for i in idx)
+        by_level[str(lvl)] = {"requests": len(idx), "segments": rs.counts["segments"],
+                              "plain": sum(seg_req[i] for i in idx) / tp,
+                              "batched": rs.counts["segments"] / tb,
+                              "speedup": (rs.counts["segments"] / tb) /
+                                         (sum(seg_req[i] for i in idx) / tp)}
     err = None
     if precision != "fp64":  # untimed: the batch's field error against FP64
         qc = [api.request_from_workload(r, precision, field_check=True) for r in reqs]
@@ -201,6 +219,7 @@ def run_batched(precision: str):
             "batched": rb.counts["segments"] / t_batch, "plain": seg_plain / t_plain,
             "unit": "segments/s", "batched_s": t_batch, "plain_s": t_plain,
             "speedup": (rb.counts["segments"] / t_batch) / (seg_plain / t_plain),
+            "by_level": by_level, "field_precision": precision,
             "field_error_vs_fp64": err}
 
 
@@ -216,16 +235,24 @@ def run_serving(precision: str, n_req: int = 48, rates=(10.0, 50.0, 500.0), slot
     qs = [(si, api.request_from_workload(r, precision)) for si, r in stream]
     for si, q in qs:
         api.solve(scs[si], q, with_paths=False)  # warm-up: sizes every workspace
-    # plain: one request at a time
+    # plain: one request at a time (service time of each, wall clock)
     t0 = time.perf_counter()
-    seg = 0
+    seg, service = 0, []
     for si, q in qs:
+        t1 = time.perf_counter()
         seg += api.solve(scs[si], q, with_paths=False).counts["segments"]
+        service.append(time.perf_counter() - t1)
     plain = seg / (time.perf_counter() - t0)
     sweep = []
     for rate in rates:
         rng = np.random.default_rng(99)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, len(qs)))
+        # the plain path under the same arrivals: one request at a time in
+        # arrival order, each taking its measured service time
+        free, plain_lat = 0.0, []
+        for a, sv in zip(arrivals, service):
+            free = max(free, a) + sv
+            plain_lat.append(1e3 * (free - a))
         srv = api.Server(scs, slots=slots)
         lat, seg_s, done = [], 0, 0
         t0 = time.perf_counter()
@@ -244,12 +271,20 @@ def run_serving(precision: str, n_req: int = 48, rates=(10.0, 50.0, 500.0), slot
         srv.close()
         sweep.append({"rate_req_s": rate, "p50_ms": float(np.percentile(lat, 50)),
                       "p99_ms": float(np.percentile(lat, 99)), "served": seg_s / makespan,
-                      "completed": len(lat), "makespan_s": makespan})
+                      "completed": len(lat), "makespan_s": makespan,
+                      "plain_p50_ms": float(np.percentile(plain_lat, 50)),
+                      "plain_p99_ms": float(np.percentile(plain_lat, 99)),
+                      "plain_served": seg / max(free, 1e-9)})
     for sc in scs:
         sc.close()
     top = sweep[-1]
+    levels = [r.tessellation for _, r in stream]
     return {"workload": "config-4 mix on 3 resident scenes (small, urban, large)",
             "requests": len(qs), "slots": slots, "unit": "segments/s", "plain": plain,
+            "request_levels": {str(l): levels.count(l) for l in sorted(set(levels))},
+            "service_ms": {"p50": float(np.percentile(service, 50)) * 1e3,
+                           "max": float(max(service)) * 1e3},
+            "field_precision": precision,
             "sweep": sweep, "served": top["served"], "p50_ms": top["p50_ms"],
             "p99_ms": top["p99_ms"], "speedup": top["served"] / plain}
 
@@ -322,7 +357,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "fp32_phase"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--level", type=int, default=9,
                     help="icosahedron level (9 = the benchmark; lower for profiling runs)")
@@ -362,13 +397,14 @@ def main():
 
     for _ in range(args.warmup):
         api.solve(scene, req_dev, with_paths=False)
-    # stage counts and the field error of this precision (untimed)
-    q_chk = api.request_from_workload(wl.request, args.precision, stage_counts=True,
-                                      field_check=args.precision != "fp64")
-    r_chk = api.solve(scene, q_chk, with_paths=False)
-    captured = r_chk.counts["captured"]
-    field_error = (api.field_error_stats(r_chk.field, r_chk.field_fp64)
-                   if r_chk.field_fp64 is not None else None)
+    # stage counts, and the FP32 field modes' error on this workload (untimed)
+    q_chk = api.request_from_workload(wl.request, args.precision, stage_counts=True)
+    captured = api.solve(scene, q_chk, with_paths=False).counts["captured"]
+    fp32_error = {}
+    for mode in ("fp32", "fp32_phase"):
+        r_chk = api.solve(scene, api.request_from_workload(wl.request, mode, field_check=True),
+                          with_paths=False)
+        fp32_error[mode] = api.field_error_stats(r_chk.field, r_chk.field_fp64)
     # ---- device-resident timing
     if dist:
         dist.barrier()
@@ -437,7 +473,9 @@ def main():
                        "parallelism": f"replicas{world}",
                        "l2": "working set (node pool) larger than L2 each step"},
             "counts": dict(counts, captured=captured),
-            "field_error_vs_fp64": field_error,
+            "field_error": ("FP64 field: the reference's arithmetic; parity tests hold it "
+                            "within 1e-9 of the oracle" if args.precision == "fp64" else
+                            fp32_error[args.precision]),
             "stages_ms": {k: v / steps for k, v in stage.items()},
             "e2e": {"value": tot_e2e / max_e2e, "unit": "segments/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -455,6 +493,7 @@ def main():
             line["serving"] = run_serving(args.precision)
         if not args.no_precision and args.level == 9:
             line["precision"] = run_precision()
+            line["precision"]["urban_L9"] = fp32_error
         if not args.no_cpu_baseline and world == 1:
             try:
                 line["cpu_baseline"] = cpu_baseline(wl)

@@ -108,6 +108,8 @@ typedef struct sbr_counts {
   long long classes;            /* distinct (facet, interaction) prefixes traced */
   long long groups;             /* unused, -1 */
   long long keys;               /* distinct (receiver, coplanar key) after correction */
+  long long near_edge_paths;    /* surviving paths with an interaction point within 1e-6
+                                   (barycentric) of its triangle's edge */
 } sbr_counts;
 
 /* One surviving path; its rays are [ray_offset, ray_offset + n_rays) in the
@@ -117,6 +119,9 @@ typedef struct sbr_path {
   long long launch;
   long long ray_offset;
   double field[6];                      /* this path's contribution (Ex re, im, Ey, Ez) */
+  int near_edge;                        /* 1: an interaction point lies within 1e-6
+                                           (barycentric) of its triangle's edge */
+  int reserved;
 } sbr_path;
 
 /* Stage times from CUDA events on the engine's stream.  device_ms spans

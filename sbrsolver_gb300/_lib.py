@@ -65,13 +65,14 @@ class Counts(C.Structure):
                                              "fp64_triangle_tests", "fallback_rays",
                                              "fp64_capture_tests", "launches",
                                              "capture_candidates", "ancestor_tests",
-                                             "classes", "groups", "keys")]
+                                             "classes", "groups", "keys",
+                                             "near_edge_paths")]
 
 
 class Path(C.Structure):
     _fields_ = [("request", C.c_int), ("receiver", C.c_int), ("n_rays", C.c_int),
                 ("heap", C.c_int), ("launch", C.c_longlong), ("ray_offset", C.c_longlong),
-                ("field", C.c_double * 6)]
+                ("field", C.c_double * 6), ("near_edge", C.c_int), ("reserved", C.c_int)]
 
 
 class Completion(C.Structure):

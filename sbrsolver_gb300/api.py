@@ -276,7 +276,8 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
                 # the whole path set as flat arrays (cheap at 1e5-1e6 paths)
                 A = np.ctypeslib.as_array(P)
                 paths = {k: np.array(A[k]) for k in ("request", "receiver", "launch", "heap",
-                                                     "ray_offset", "n_rays", "field")}
+                                                     "ray_offset", "n_rays", "field",
+                                                     "near_edge")}
                 paths.update(tri=tri[:cnt.rays], cop=cop[:cnt.rays], kind=kind[:cnt.rays],
                              points=pts[:6 * cnt.rays].reshape(-1, 6))
                 P = ()
@@ -287,7 +288,7 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
                     "heap": p.heap, "n_rays": n, "tri": tri[o:o + n].tolist(),
                     "cop": cop[o:o + n].tolist(), "kind": kind[o:o + n].tolist(),
                     "points": pts[6 * o:6 * (o + n)].reshape(n, 6).copy(),
-                    "field": np.array(p.field[:], np.float64)})
+                    "field": np.array(p.field[:], np.float64), "near_edge": p.near_edge})
         field_c = f.view(np.complex128).reshape(-1, 3)  # exact, inf stays inf
         res = Result(field_c, counts, timing, paths)
         fe = _lib.FieldError()

@@ -977,8 +977,24 @@ struct FieldArgs {
   int* path_tri;        // (kMaxDepth + 1) per survivor: triangle id
   int* path_cop;
   int* path_kind;
+  int* path_near_edge;  // 1 if an interaction point is within 1e-6 of its triangle's edge
   double* path_pts;     // (kMaxDepth + 2) * 3 per survivor
 };
+
+// Barycentric distance of a point (on the triangle's plane) from the
+// triangle's edges is below tol: min(u, v, 1-u-v) < tol.
+__device__ __forceinline__ int near_edge(const CorrTri& T, const double* p, double tol) {
+  double w[3] = {p[0] - T.v1[0], p[1] - T.v1[1], p[2] - T.v1[2]};
+  const double d00 = T.e1[0] * T.e1[0] + T.e1[1] * T.e1[1] + T.e1[2] * T.e1[2];
+  const double d01 = T.e1[0] * T.e2[0] + T.e1[1] * T.e2[1] + T.e1[2] * T.e2[2];
+  const double d11 = T.e2[0] * T.e2[0] + T.e2[1] * T.e2[1] + T.e2[2] * T.e2[2];
+  const double d20 = w[0] * T.e1[0] + w[1] * T.e1[1] + w[2] * T.e1[2];
+  const double d21 = w[0] * T.e2[0] + w[1] * T.e2[1] + w[2] * T.e2[2];
+  const double den = d00 * d11 - d01 * d01;
+  if (!(den > 0)) return 1;
+  const double u = (d11 * d20 - d01 * d21) / den, v = (d00 * d21 - d01 * d20) / den;
+  return fmin(fmin(u, v), 1.0 - u - v) < tol ? 1 : 0;
+}
 
 __global__ void k_field(FieldArgs A) {
   const unsigned long long ns = min(A.ctr->survivors, A.cap);
@@ -1023,6 +1039,11 @@ __global__ void k_field(FieldArgs A) {
     const size_t bp = size_t(i) * (kMaxDepth + 2) * 3;
     for (int r = 0; r <= pb.n; ++r)
       for (int a = 0; a < 3; ++a) A.path_pts[bp + 3 * r + a] = pb.pts[r][a];
+    // interaction point r+1 lies on the triangle the correction intersected
+    int near = 0;
+    for (int r = 0; r + 1 < pb.n; ++r)
+      near |= near_edge(A.sc.corr[A.rank_to_id[pb.tri[r]]], pb.pts[r + 1], 1e-6);
+    A.path_near_edge[i] = near;
   }
 }
 
@@ -1110,7 +1131,7 @@ struct Workspace {
   DBuf<int> s_counts, s_starts, s_cursor, s_order;
   DBuf<double> path_field, path_pts, field;
   DBuf<double> path_field64, field64;  // FP64 shadow of an FP32 field (field_check)
-  DBuf<int> path_nray, path_tri, path_cop, path_kind;
+  DBuf<int> path_nray, path_tri, path_cop, path_kind, path_near;
   DBuf<Counters> ctr;
   DBuf<unsigned long long> seg_tx;
   // capacities (grown from occupancy and on overflow)
@@ -1668,6 +1689,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.path_tri.ensure(nsa * (kMaxDepth + 1));
     W.path_cop.ensure(nsa * (kMaxDepth + 1));
     W.path_kind.ensure(nsa * (kMaxDepth + 1));
+    W.path_near.ensure(nsa);
     W.path_pts.ensure(nsa * (kMaxDepth + 2) * 3);
     W.field.ensure(std::max(1, 6 * rx_total));
     W.s_counts.ensure(rx_total + 1);
@@ -1691,6 +1713,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fa.path_tri = W.path_tri.p;
     fa.path_cop = W.path_cop.p;
     fa.path_kind = W.path_kind.p;
+    fa.path_near_edge = W.path_near.p;
     fa.path_pts = W.path_pts.p;
     if (ns) k_field<<<grid_for(ns, 64), 64, 0, st>>>(fa);
     CK(cudaMemsetAsync(W.s_counts.p, 0, sizeof(int) * (rx_total + 1), st));
@@ -1731,7 +1754,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         CK(cudaMemcpyAsync(out.field64.data(), W.field64.p, sizeof(double) * 6 * rx_total,
                            cudaMemcpyDeviceToHost, st));
     }
-    std::vector<int> order(ns), nray(ns), starts(rx_total + 1);
+    std::vector<int> order(ns), nray(ns), starts(rx_total + 1), pnear(ns);
     std::vector<Survivor> sv(ns);
     std::vector<double> pf(6 * ns), pts(ns * (kMaxDepth + 2) * 3);
     std::vector<int> ptri(ns * (kMaxDepth + 1)), pcop(ns * (kMaxDepth + 1)),
@@ -1739,6 +1762,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     if (ns) {
       CK(cudaMemcpyAsync(order.data(), W.s_order.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
       CK(cudaMemcpyAsync(nray.data(), W.path_nray.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pnear.data(), W.path_near.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
       CK(cudaMemcpyAsync(sv.data(), W.surv.p, sizeof(Survivor) * ns, cudaMemcpyDeviceToHost, st));
       CK(cudaMemcpyAsync(pf.data(), W.path_field.p, sizeof(double) * 6 * ns, cudaMemcpyDeviceToHost, st));
       CK(cudaMemcpyAsync(ptri.data(), W.path_tri.p, sizeof(int) * ptri.size(), cudaMemcpyDeviceToHost, st));
@@ -1767,6 +1791,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       p.heap = int(sv[i].rank & ((1u << kHeapBits) - 1));
       p.ray_offset = (long long)out.tri.size();
       for (int j = 0; j < 6; ++j) p.field[j] = pf[6 * size_t(i) + j];
+      p.near_edge = pnear[i];
+      p.reserved = 0;
       for (int r = 0; r < p.n_rays; ++r) {
         const size_t b = size_t(i) * (kMaxDepth + 1) + r;
         out.tri.push_back(ptri[b]);
@@ -1805,6 +1831,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     out.counts.classes = (long long)c.used_cls;
     out.counts.groups = -1;
     out.counts.keys = (long long)c.used_dd;
+    out.counts.near_edge_paths = 0;
+    for (const sbr_path& p : out.paths) out.counts.near_edge_paths += p.near_edge;
     float ms[8] = {};
     for (int i = 1; i < 8; ++i) CK(cudaEventElapsedTime(&ms[i], W.ev[i - 1], W.ev[i]));
     out.timing.h2d_ms = ms[1];
@@ -1853,6 +1881,8 @@ std::vector<sbr_result*> split_result(const sbr_result& b) {
     x->counts = b.counts;
     x->counts.segments = r < int(b.segments_per_request.size()) ? b.segments_per_request[r] : -1;
     x->counts.paths = (long long)x->paths.size();
+    x->counts.near_edge_paths = 0;
+    for (const sbr_path& p : x->paths) x->counts.near_edge_paths += p.near_edge;
     x->counts.rays = (long long)x->tri.size();
     x->timing = b.timing;
     x->counts.launches = r < int(b.launches_per_request.size()) ? b.launches_per_request[r] : -1;
