@@ -79,6 +79,10 @@ struct DevScene {
   const Tri32* corr32;     // FP32 filter copy of corr
   const int* rank_to_id;   // triangle id of each depth-first rank
   const Material* mats;
+  // search BVH of the FP32 candidate search (child < 0: ~(first << 3 | count))
+  const Node32* snode;
+  const Tri32* stri;    // triangles in search leaf order
+  const int* srank;     // their depth-first ranks
   int n_tri, n_nodes, n_mats;
   int root_leaf;
   float box_margin;  // absolute FP32 box expansion (metres)

@@ -344,6 +344,9 @@ struct TraceArgs {
   unsigned long long* seg_per_tx;  // executed segments per request
   int depth;
   long long n_root;    // total launches (depth 0)
+  long long lo, hi;    // this launch covers rays [lo, hi) of the depth
+  const uint2* cand;   // contenders of those rays (k_find)
+  const unsigned char* ncand;
 };
 
 __device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long long g) {
@@ -375,21 +378,202 @@ __device__ __forceinline__ void write_class(ClassInfo& ci, const double* img, ui
   ci.pad2 = 0;
 }
 
+// Number of rays entering bounce depth `depth` (known on the device only).
+__device__ __forceinline__ long long rays_at_depth(const Counters* ctr, int depth, long long n_root,
+                                                   unsigned long long cap) {
+  return depth == 0 ? n_root : (long long)min(ctr->queue[depth], cap);
+}
+
+// Launch ray g of the batch: origin and direction (FP64).
+__device__ __forceinline__ void root_ray(const TxParams* txp, int n_tx, const double* const* dirs,
+                                         long long g, double* o, double* d, int& q, long long& li) {
+  q = find_request(txp, n_tx, g);
+  const TxParams& P = txp[q];
+  li = g - P.launch_first;
+  const double* dd = dirs[P.level] + 3 * li;
+  for (int a = 0; a < 3; ++a) {
+    o[a] = P.tx[a];
+    d[a] = dd[a];
+  }
+}
+
+// ---- FP32 candidate search (persistent, rays refilled per warp) ----------
+//
+// Each lane traverses one ray at a time.  Lanes whose ray is finished take a
+// new one from the chunk's work counter (one atomic per warp, when at least
+// a quarter of the warp is idle or nobody is busy), so warps stay full while
+// rays of very different lengths finish at different times.
+struct FindArgs {
+  DevScene sc;
+  const TxParams* txp;
+  int n_tx;
+  const double* const* dirs;
+  const RayRec* in;
+  const Counters* ctr;
+  unsigned long long in_cap;
+  long long n_root;
+  int depth;
+  long long lo, hi;            // this launch covers rays [lo, hi) of the depth
+  unsigned long long* work;    // rays of the chunk handed out (zero at launch)
+  uint2* cand;                 // kCand per ray of the chunk
+  unsigned char* ncand;        // contenders per ray, kFindFallback = exact traversal
+};
+
+constexpr int kFindSteps = 16;  // traversal steps between refills
+
+__global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
+  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.in_cap);
+  const long long n = min(n_all, A.hi) - A.lo;
+  if (n <= 0) return;
+  const unsigned lane = lane_id();
+  long long ray = -1;
+  bool exhausted = false;
+  float3 o32 = make_float3(0, 0, 0), d32 = o32, inv = o32;
+  float no = 0.0f, nd = 0.0f, m = 0.0f, tcut = INFINITY;
+  int stack[kStack];
+  int sp = 0, pending = -1, nc = 0;
+  bool fail = false;
+  uint2* out = nullptr;
+  while (true) {
+    const bool idle = ray < 0 && !exhausted;
+    const unsigned im = __ballot_sync(0xffffffffu, idle);
+    const unsigned busy = __ballot_sync(0xffffffffu, ray >= 0);
+    if (im && (__popc(im) >= 8 || busy == 0)) {
+      const int leader = __ffs(im) - 1;
+      unsigned long long base = 0;
+      if (int(lane) == leader) base = atomicAdd(A.work, (unsigned long long)__popc(im));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (idle) {
+        const long long k = (long long)base + __popc(im & ((1u << lane) - 1u));
+        if (k < n) {
+          ray = k;
+          double o[3], d[3];
+          if (A.depth == 0) {
+            int q;
+            long long li;
+            root_ray(A.txp, A.n_tx, A.dirs, A.lo + k, o, d, q, li);
+          } else {
+            const RayRec& r = A.in[A.lo + k];
+            for (int a = 0; a < 3; ++a) {
+              o[a] = r.o[a];
+              d[a] = r.d[a];
+            }
+          }
+          o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
+          d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
+          inv = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
+          no = sqrtf(o32.x * o32.x + o32.y * o32.y + o32.z * o32.z);
+          nd = sqrtf(d32.x * d32.x + d32.y * d32.y + d32.z * d32.z);
+          m = A.sc.box_margin + kFiltK * no;
+          tcut = INFINITY;
+          sp = 0;
+          pending = -1;
+          nc = 0;
+          fail = false;
+          stack[sp++] = 0;  // the search root is always a node
+          out = A.cand + size_t(k) * kCand;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, ray >= 0) == 0) {
+      if (__all_sync(0xffffffffu, exhausted)) break;
+      continue;
+    }
+    if (ray < 0) continue;
+    bool done = false;
+    for (int it = 0; it < kFindSteps && !done; ++it) {
+      if (pending >= 0) {
+        const int first = pending >> 3, last = first + (pending & 7);
+        for (int j = first; j < last; ++j) {
+          float tlo, thi;
+          const int k = tri_classify(A.sc.stri[j], o32, d32, no, nd, tlo, thi);
+          if (k == 0 || tlo > tcut) continue;
+          if (nc == kCand) {
+            fail = true;
+            break;
+          }
+          out[nc++] = make_uint2(unsigned(__ldg(A.sc.srank + j)), __float_as_uint(tlo));
+          if (k == 2) tcut = fminf(tcut, thi * (1.0f + 1.0f / 4096.0f) + 1e-30f);
+        }
+        pending = -1;
+        if (fail) done = true;
+        continue;
+      }
+      if (sp == 0) {
+        done = true;
+        break;
+      }
+      const int ni = stack[--sp];
+      if (ni < 0) {  // a leaf deferred as the farther child
+        pending = ~ni;
+        continue;
+      }
+      float4 f0, f1, f2;
+      int2 ch;
+      load_node(A.sc.snode, ni, f0, f1, f2, ch);
+      float tn0, tf0, tn1, tf1;
+      slab32(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, o32, inv, m, tn0, tf0);
+      slab32(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, o32, inv, m, tn1, tf1);
+      const bool h0 = tn0 <= tf0 && tf0 >= 0.0f && tn0 <= tcut;
+      const bool h1 = tn1 <= tf1 && tf1 >= 0.0f && tn1 <= tcut;
+      int first = 0, second = 0;
+      bool has_first = false, has_second = false;
+      if (h0 && h1) {
+        has_first = has_second = true;
+        if (tn1 < tn0) {
+          first = ch.y;
+          second = ch.x;
+        } else {
+          first = ch.x;
+          second = ch.y;
+        }
+      } else if (h0) {
+        has_first = true;
+        first = ch.x;
+      } else if (h1) {
+        has_first = true;
+        first = ch.y;
+      }
+      if (has_second) {
+        if (sp >= kStack) {
+          fail = done = true;
+          break;
+        }
+        stack[sp++] = second;  // node, or ~leaf code
+      }
+      if (has_first) {
+        if (first < 0) {
+          pending = ~first;
+        } else {
+          if (sp >= kStack) {
+            fail = done = true;
+            break;
+          }
+          stack[sp++] = first;
+        }
+      }
+    }
+    if (done) {
+      A.ncand[ray] = fail ? kFindFallback : (unsigned char)nc;
+      ray = -1;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
-  const long long n_in =
-      A.depth == 0 ? A.n_root
-                   : (long long)min(A.ctr->queue[A.depth], (unsigned long long)A.out_cap);
+  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
+  const long long n_in = min(n_all, A.hi);
   TraceStats st{0, 0};
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in; i += stride) {
+  for (long long i = A.lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in;
+       i += stride) {
     RayRec r;
     if (A.depth == 0) {
-      const int q = find_request(A.txp, A.n_tx, i);
-      const TxParams& P = A.txp[q];
-      const long long li = i - P.launch_first;
-      const double* d = A.dirs[P.level] + 3 * li;
-      r.o[0] = P.tx[0]; r.o[1] = P.tx[1]; r.o[2] = P.tx[2];
-      r.d[0] = d[0]; r.d[1] = d[1]; r.d[2] = d[2];
+      int q;
+      long long li;
+      root_ray(A.txp, A.n_tx, A.dirs, i, r.o, r.d, q, li);
       r.total = 0.0;
       r.S = 0.0;
       r.parent = 0xFFFFFFFFu;
@@ -404,7 +588,9 @@ __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
     }
     const TxParams& P = A.txp[r.tx];
     Hit h;
-    const bool hit = closest_hit(A.sc, r.o, r.d, h, st, &A.ctr->overflow);
+    const long long c = i - A.lo;
+    const bool hit = resolve_hit(A.sc, r.o, r.d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
+                                 &A.ctr->overflow);
     const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
     {  // per-request segment count, one atomic per request present in the warp
       const unsigned peers = __match_any_sync(__activemask(), r.tx);
@@ -1134,6 +1320,9 @@ struct Workspace {
   DBuf<int> path_nray, path_tri, path_cop, path_kind, path_near;
   DBuf<Counters> ctr;
   DBuf<unsigned long long> seg_tx;
+  DBuf<uint2> cand;                    // FP32 search contenders, kCand per ray of a chunk
+  DBuf<unsigned char> ncand;
+  DBuf<unsigned long long> find_work;  // work counter of the running search launch
   // capacities (grown from occupancy and on overflow)
   unsigned long long cap_nodes = 1 << 20, cap_queue = 1 << 19, cap_surv = 1 << 14;
   unsigned long long cap_corr = 1 << 16;
@@ -1157,6 +1346,9 @@ struct SceneImpl {
   DBuf<RefNode> ref;
   DBuf<Tri32> tri32;
   DBuf<Tri64> tri64;
+  DBuf<Node32> snode;
+  DBuf<Tri32> stri;
+  DBuf<int> srank;
   DBuf<CorrTri> corr;
   DBuf<Tri32> corr32;
   DBuf<Material> mats;
@@ -1284,6 +1476,31 @@ static void upload_scene(SceneImpl& S) {
   S.tri32.upload(t32.data(), t32.size(), st);
   S.tri64.upload(t64.data(), t64.size(), st);
   S.mats.upload(mats.data(), mats.size(), st);
+  {  // search BVH
+    const SearchBVH& B = H.search;
+    std::vector<Node32> sn(B.nodes.size());
+    for (size_t i = 0; i < B.nodes.size(); ++i) {
+      Node32& m = sn[i];
+      std::memset(&m, 0, sizeof m);
+      for (int a = 0; a < 3; ++a) {
+        m.lo0[a] = B.nodes[i].lo[0][a];
+        m.hi0[a] = B.nodes[i].hi[0][a];
+        m.lo1[a] = B.nodes[i].lo[1][a];
+        m.hi1[a] = B.nodes[i].hi[1][a];
+      }
+      m.child[0] = B.nodes[i].child[0];
+      m.child[1] = B.nodes[i].child[1];
+    }
+    std::vector<Tri32> st32(B.order.size());
+    for (size_t j = 0; j < B.order.size(); ++j) st32[j] = t32[B.order[j]];
+    S.snode.upload(sn.data(), sn.size(), st);
+    S.stri.upload(st32.data(), st32.size(), st);
+    S.srank.upload(B.order.data(), B.order.size(), st);
+    S.dev.snode = S.snode.p;
+    S.dev.stri = S.stri.p;
+    S.dev.srank = S.srank.p;
+    CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
+  }
   S.tri_cop.upload(cop.data(), cop.size(), st);
   S.rank_to_id.upload(r2i.data(), r2i.size(), st);
   S.dev.node32 = S.node32.p;
@@ -1396,6 +1613,18 @@ double request_bytes(const sbr_request& q) {
   const int R = std::max(q.max_reflection, 0), T = std::max(q.max_transmission, 0);
   return L * tree_nodes(R, T) * (sizeof(NodeHot) + sizeof(NodeCold)) +
          L * tree_width(R, T) * 2 * sizeof(RayRec) + double(q.n_rx) * 256.0;
+}
+
+// Persistent grid of the FP32 search: as many blocks as fit on the device.
+static int find_grid() {
+  static int g = [] {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find, 128, 0);
+    return std::max(1, sms) * std::max(1, per_sm);
+  }();
+  return g;
 }
 
 static int grid_for(long long n, int block) {
@@ -1604,12 +1833,41 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ta.ctr = W.ctr.p;
     ta.seg_per_tx = W.seg_tx.p;
     ta.n_root = launches;
+    // Each depth runs in chunks of at most kTraceChunk rays: the FP32
+    // search (k_find) stores the chunk's contenders, then k_trace resolves
+    // them in FP64 and spawns the next depth.  The ray count of a depth > 0
+    // is on the device; chunks past it return at once.
+    constexpr long long kTraceChunk = 1LL << 24;
+    const long long max_width = std::max<long long>(launches, (long long)W.cap_queue);
+    const long long chunk = std::max<long long>(1, std::min(kTraceChunk, max_width));
+    W.cand.ensure(size_t(chunk) * kCand);
+    W.ncand.ensure(size_t(chunk));
+    W.find_work.ensure(1);
+    FindArgs fnd;
+    fnd.sc = S.dev;
+    fnd.txp = W.txp.p;
+    fnd.n_tx = n_req;
+    fnd.dirs = S.dir_table.p;
+    fnd.ctr = W.ctr.p;
+    fnd.in_cap = W.cap_queue;
+    fnd.n_root = launches;
+    fnd.work = W.find_work.p;
+    fnd.cand = W.cand.p;
+    fnd.ncand = W.ncand.p;
+    ta.cand = W.cand.p;
+    ta.ncand = W.ncand.p;
     for (int d = 0; d <= max_depth; ++d) {
-      ta.depth = d;
-      ta.in = (d % 2 == 0) ? W.q1.p : W.q0.p;
+      ta.depth = fnd.depth = d;
+      ta.in = fnd.in = (d % 2 == 0) ? W.q1.p : W.q0.p;
       ta.out = (d % 2 == 0) ? W.q0.p : W.q1.p;
-      const long long width = d == 0 ? launches : (long long)std::min<unsigned long long>(W.cap_queue, 1ull << 40);
-      k_trace<<<grid_for(width, 128), 128, 0, st>>>(ta);
+      const long long bound = d == 0 ? launches : (long long)W.cap_queue;
+      for (long long lo = 0; lo < bound; lo += chunk) {
+        ta.lo = fnd.lo = lo;
+        ta.hi = fnd.hi = std::min(bound, lo + chunk);
+        CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
+        k_find<<<find_grid(), 128, 0, st>>>(fnd);
+        k_trace<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
+      }
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[3], st));

@@ -380,7 +380,163 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
       st.push_back({bn[it.b].c0, me, it.depth + 1, me, 0});
     }
   }
+  build_search_bvh(out);
   return true;
+}
+
+namespace {
+
+struct FBox {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  void add(const float* l, const float* h) {
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], l[a]);
+      hi[a] = std::max(hi[a], h[a]);
+    }
+  }
+  void add_point(const float* p) { add(p, p); }
+  float area() const {
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return dx < 0 ? 0.0f : 2.0f * (dx * dy + dy * dz + dz * dx);
+  }
+};
+
+struct SearchBuild {
+  std::vector<float> blo, bhi, cen;  // per rank
+  SearchBVH* out;
+  int max_depth = 0;
+
+  int leaf(int b, int n) { return ~((b << 3) | n); }
+
+  // Builds [b, e) of out->order; returns the child ref and its box.
+  int build(int b, int e, int depth, FBox& box) {
+    std::vector<int>& ord = out->order;
+    FBox cb;
+    box = FBox();
+    for (int i = b; i < e; ++i) {
+      const int p = ord[i];
+      box.add(&blo[3 * p], &bhi[3 * p]);
+      cb.add_point(&cen[3 * p]);
+    }
+    max_depth = std::max(max_depth, depth);
+    const int n = e - b;
+    if (n <= 2) return leaf(b, n);
+    int ax = 0;
+    for (int a = 1; a < 3; ++a)
+      if (cb.hi[a] - cb.lo[a] > cb.hi[ax] - cb.lo[ax]) ax = a;
+    const float ext = cb.hi[ax] - cb.lo[ax];
+    int mid = -1;
+    if (ext > 0) {
+      constexpr int kBins = 32;
+      FBox bins[kBins];
+      int cnt[kBins] = {0};
+      const float k = kBins / ext;
+      auto bin_of = [&](int p) {
+        return std::min(kBins - 1, std::max(0, int((cen[3 * p + ax] - cb.lo[ax]) * k)));
+      };
+      for (int i = b; i < e; ++i) {
+        const int p = ord[i], q = bin_of(p);
+        ++cnt[q];
+        bins[q].add(&blo[3 * p], &bhi[3 * p]);
+      }
+      float right_area[kBins];
+      int right_cnt[kBins];
+      FBox acc;
+      int c = 0;
+      for (int i = kBins - 1; i > 0; --i) {
+        acc.add(bins[i].lo, bins[i].hi);
+        c += cnt[i];
+        right_area[i] = acc.area();
+        right_cnt[i] = c;
+      }
+      FBox lacc;
+      int lc = 0, best = -1;
+      float best_cost = INFINITY;
+      for (int i = 0; i < kBins - 1; ++i) {
+        lacc.add(bins[i].lo, bins[i].hi);
+        lc += cnt[i];
+        if (lc == 0 || right_cnt[i + 1] == 0) continue;
+        const float cost = lacc.area() * lc + right_area[i + 1] * right_cnt[i + 1];
+        if (cost < best_cost) {
+          best_cost = cost;
+          best = i;
+        }
+      }
+      // cost of a node relative to its leaf: one box test per triangle saved
+      const float leaf_cost = box.area() * n;
+      if (best >= 0 && (n > 7 || best_cost + box.area() < leaf_cost)) {
+        mid = int(std::partition(ord.begin() + b, ord.begin() + e,
+                                 [&](int p) { return bin_of(p) <= best; }) -
+                  ord.begin());
+      } else if (n <= 7) {
+        return leaf(b, n);
+      }
+    } else if (n <= 7) {
+      return leaf(b, n);
+    }
+    if (depth > 48) mid = -1;  // keep the tree shallow enough for the traversal stack
+    if (mid <= b || mid >= e) {  // no usable SAH split: median along the axis
+      mid = b + n / 2;
+      std::nth_element(ord.begin() + b, ord.begin() + mid, ord.begin() + e,
+                       [&](int x, int y) { return cen[3 * x + ax] < cen[3 * y + ax]; });
+    }
+    const int me = int(out->nodes.size());
+    out->nodes.emplace_back();
+    FBox lb, rb;
+    const int l = build(b, mid, depth + 1, lb);
+    const int r = build(mid, e, depth + 1, rb);
+    SearchNode& nd = out->nodes[me];
+    for (int a = 0; a < 3; ++a) {
+      nd.lo[0][a] = lb.lo[a];
+      nd.hi[0][a] = lb.hi[a];
+      nd.lo[1][a] = rb.lo[a];
+      nd.hi[1][a] = rb.hi[a];
+    }
+    nd.child[0] = l;
+    nd.child[1] = r;
+    return me;
+  }
+};
+
+}  // namespace
+
+void build_search_bvh(HostScene& H) {
+  const int n = int(H.dfs_tris.size());
+  SearchBuild sb;
+  sb.out = &H.search;
+  H.search.nodes.clear();
+  H.search.order.resize(n);
+  sb.blo.resize(3 * size_t(n));
+  sb.bhi.resize(3 * size_t(n));
+  sb.cen.resize(3 * size_t(n));
+  for (int r = 0; r < n; ++r) {
+    const HostTri& t = H.tris[H.dfs_tris[r]];
+    for (int a = 0; a < 3; ++a) {
+      // vertices are float values, so the float box is exact
+      const float x = float(t.v1[a]), y = float(t.v2[a]), z = float(t.v3[a]);
+      sb.blo[3 * r + a] = std::min({x, y, z});
+      sb.bhi[3 * r + a] = std::max({x, y, z});
+      sb.cen[3 * r + a] = 0.5f * (sb.blo[3 * r + a] + sb.bhi[3 * r + a]);
+    }
+    H.search.order[r] = r;
+  }
+  H.search.nodes.reserve(size_t(n) / 2 + 2);
+  H.search.nodes.emplace_back();  // root
+  FBox box;
+  const int ref = sb.build(0, n, 1, box);
+  SearchNode& root = H.search.nodes[0];
+  if (ref >= 0) {  // the root's children become node 0's children
+    root = H.search.nodes[size_t(ref)];
+    // node `ref` stays as an unreachable copy
+  } else {  // the whole scene is one leaf: one child, the other an empty leaf
+    for (int a = 0; a < 3; ++a) {
+      root.lo[0][a] = root.lo[1][a] = box.lo[a];
+      root.hi[0][a] = root.hi[1][a] = box.hi[a];
+    }
+    root.child[0] = ref;
+    root.child[1] = ~0;  // first 0, count 0
+  }
+  H.search.max_depth = sb.max_depth;
 }
 
 void icosphere(int level, std::vector<double>& dirs) {

@@ -35,6 +35,21 @@ struct HostNode {
   int depth = 0;
 };
 
+// Search BVH of the FP32 candidate search: a binned-SAH binary BVH over the
+// triangles (any topology finds the same candidates; the reference BVH
+// above still decides ties and reachability), leaves of at most 7
+// triangles.  Node child ref: >= 0 node index, < 0 ~(first << 3 | count)
+// into `order` (depth-first ranks in leaf order).
+struct SearchNode {
+  float lo[2][3], hi[2][3];
+  int child[2];
+};
+struct SearchBVH {
+  std::vector<SearchNode> nodes;  // node 0 is the root
+  std::vector<int> order;
+  int max_depth = 0;
+};
+
 struct HostScene {
   std::vector<HostTri> tris;    // by triangle id (file order after merge)
   std::vector<int> mesh_order;  // reference caller vector after ConstructBVH: position -> id
@@ -42,6 +57,7 @@ struct HostScene {
   std::vector<int> dfs_tris;    // triangle ids in depth-first leaf order
   int max_depth = 0;
   double extent = 0;            // max |coordinate| of any vertex
+  SearchBVH search;
 };
 
 // Binary or ASCII STL (format chosen as StlReader.h:703-718 does).  Returns
@@ -53,6 +69,9 @@ bool read_stl(const std::string& path, std::vector<float>& v, std::vector<float>
 // facets whose vertices collapse, exactly like the reference reader.
 bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, HostScene& out,
                    std::string& err);
+
+// Builds H.search from the triangles in depth-first rank order.
+void build_search_bvh(HostScene& H);
 
 // Icosahedron launch directions at a subdivision level, in the reference's
 // vertex order (Icosahedron.cpp:3-109), 3 doubles per direction.

@@ -440,6 +440,71 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
   return best.rank != INT_MAX;
 }
 
+// ---- split closest hit: FP32 candidate search, then FP64 resolution -------
+//
+// The same decision as closest_hit, cut in two so that the FP32 traversal
+// (divergent: rays visit very different numbers of nodes) and the FP64
+// resolution (dense FP64 work) run in separate kernels.  The search keeps up
+// to kCand contender triangles per ray (depth-first rank, FP32 lower bound on
+// t); more contenders, or a stack overflow, send the ray to the
+// reference-order FP64 traversal.
+constexpr int kCand = 8;
+constexpr unsigned char kFindFallback = 0xFF;
+
+// Resolution of a ray's contenders (rank, FP32 t lower bound as bits).
+__device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d,
+                            const uint2* cand, int nc, Hit& best, TraceStats& st,
+                            unsigned* overflow) {
+  if (nc == kFindFallback)  // more contenders than kept, or a deep stack: one-pass search
+    return closest_hit(sc, o, d, best, st, overflow);
+  int cr[kCand];
+  float ct[kCand];
+  for (int i = 0; i < nc; ++i) {
+    const uint2 c = cand[i];
+    const float t = __uint_as_float(c.y);
+    int j = i - 1;
+    while (j >= 0 && ct[j] > t) {  // insertion by lower bound (stable)
+      ct[j + 1] = ct[j];
+      cr[j + 1] = cr[j];
+      --j;
+    }
+    ct[j + 1] = t;
+    cr[j + 1] = int(c.x);
+  }
+  best.rank = INT_MAX;
+  best.dist = __longlong_as_double(0x7ff0000000000000ll);
+  best.t = best.dist;
+  for (int i = 0; i < nc; ++i) {
+    if (best.rank != INT_MAX && ct[i] > float(best.t) * (1.0f + 1.0f / 4096.0f) + 1e-30f) break;
+    const int r = cr[i];
+    ++st.fp64_tri;
+    double t, P[3], dist;
+    if (mt64(sc.tri64[r], o, d, t, P, dist) &&
+        (dist < best.dist || (dist == best.dist && r < best.rank))) {
+      best.dist = dist;
+      best.t = t;
+      best.p[0] = P[0];
+      best.p[1] = P[1];
+      best.p[2] = P[2];
+      best.rank = r;
+    }
+  }
+  if (best.rank == INT_MAX) return false;
+  best.leaf = sc.tri64[best.rank].node;
+  // every ancestor of the winner's leaf must pass the reference's slab test
+  const float3 o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
+  const float3 d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
+  for (int n = best.leaf; n >= 0; n = sc.ref[n].parent) {
+    int v = slab_certain(sc.ref[n].fb, sc.ref[n].flat, o32, d32);
+    if (v < 0) v = slab64(sc.ref[n].bb, o, d) ? 1 : 0;
+    if (!v) {
+      ++st.fallback;
+      return exact_closest(sc, o, d, best, overflow);
+    }
+  }
+  return true;
+}
+
 // HitReceptionSphere (RTSolver.cpp:805-863), FP64 in the reference's order.
 __device__ __forceinline__ bool reception64(const double* s, const double* t, const double* c,
                                             double path_len, double tan_beta) {
