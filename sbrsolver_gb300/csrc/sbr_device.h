@@ -175,6 +175,8 @@ struct Counters {
   unsigned long long fallback;   // rays that needed the reference-order traversal
   unsigned long long fp64_capture;
   unsigned long long used_cls, used_cop, used_dd;  // occupied hash slots
+  unsigned long long lost_cls, lost_cop, lost_dd;  // inserts refused by a full table
+  unsigned long long pairs;      // (node, receiver) pairs handed to the FP64 capture pass
   unsigned long long cand;       // receiver candidates tested by the capture stage
   unsigned long long anc;        // ancestor re-tests for suppression
   unsigned int overflow;         // bit mask of capacity overflows
@@ -183,8 +185,11 @@ struct Counters {
 
 enum OverflowBits : unsigned {
   kOvNodes = 1, kOvQueue = 2, kOvClass = 4, kOvCop = 8, kOvCorr = 16, kOvDedup = 32,
-  kOvSurv = 64, kOvStack = 128
+  kOvSurv = 64, kOvStack = 128, kOvPairs = 256
 };
+// Overflows of the trace stage: the solve will be repeated, so the stages
+// after it skip their work.
+constexpr unsigned kOvTrace = kOvNodes | kOvQueue | kOvClass | kOvCop;
 
 // ------------------------------------------------------------------ FP64
 namespace x64 {

@@ -113,10 +113,11 @@ __device__ __forceinline__ unsigned long long warp_reserve(unsigned long long* c
 // (the host grows them between solves from the occupancy counters), so a
 // probe run longer than kMaxProbe means the table is too small: the insert
 // reports overflow and the solve is repeated with a larger table.
-constexpr uint32_t kMaxProbe = 4096;
+constexpr uint32_t kMaxProbe = 256;
 
 __device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long key, unsigned* ov,
-                                              unsigned bit, unsigned long long* used) {
+                                              unsigned bit, unsigned long long* used,
+                                              unsigned long long* lost) {
   uint32_t h = uint32_t(mix64(key)) & t.mask;
   const uint32_t lim = min(kMaxProbe, t.mask + 1);
   for (uint32_t i = 0; i < lim; ++i) {
@@ -133,6 +134,7 @@ __device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long ke
     h = (h + 1) & t.mask;
   }
   atomicOr(ov, bit);
+  atomicAdd(lost, 1ull);
   return 0xFFFFFFFFu;
 }
 
@@ -422,6 +424,7 @@ struct FindArgs {
 constexpr int kFindSteps = 16;  // traversal steps between refills
 
 __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
+  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
   const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.in_cap);
   const long long n = min(n_all, A.hi) - A.lo;
   if (n <= 0) return;
@@ -563,6 +566,7 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
 }
 
 __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
+  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
   const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
   const long long n_in = min(n_all, A.hi);
   TraceStats st{0, 0};
@@ -650,7 +654,8 @@ __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
       c.pad = 0;
       const int cop = A.tri_cop[h.rank];
       const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
-      const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop);
+      const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop,
+                                           &A.ctr->lost_cop);
       // image source of the parent ray's class (the transmitter for a launch)
       const double* pimg = is_root_class(r.cls) ? P.tx : A.cls_info[r.cls].img;
       unsigned long long slot = base;
@@ -660,7 +665,8 @@ __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
         c.rc = r.rc;
         c.tc = r.tc + 1;
         const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
-        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls);
+        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
+                          &A.ctr->lost_cls);
         c.cop = cop_cls;
         if (c.cls != 0xFFFFFFFFu) write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
         if (slot < A.out_cap) A.out[slot] = c;
@@ -676,7 +682,8 @@ __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
         c.rc = r.rc + 1;
         c.tc = r.tc;
         const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1);
-        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls);
+        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
+                          &A.ctr->lost_cls);
         c.cop = cop_cls;
         if (c.cls != 0xFFFFFFFFu) {
           // ImagePoint (RTSolver.cpp:910-924) across the triangle the
@@ -714,6 +721,8 @@ struct CaptureArgs {
   Counters* ctr;
   unsigned long long node_cap;
   int stage_counts;
+  uint2* pairs;                // (node, receiver | unsure << 31) for k_capture_finish
+  unsigned long long pair_cap;
 };
 
 // MultiPathCorrection (RTSolver.cpp:330-373) for one capture, walking the
@@ -774,10 +783,11 @@ struct AncRec {
   uint32_t idx, pad[3];
 };
 
-__global__ void __launch_bounds__(32 * kCapWarps, 5) k_capture(CaptureArgs A) {
+__global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
   __shared__ AncRec anc[kCapWarps][kMaxDepth];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
+  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
   const unsigned long long n_nodes = min(A.ctr->nodes, A.node_cap);
   unsigned long long events = 0, cand = 0, anc_tests = 0;
   unsigned n64 = 0;
@@ -806,6 +816,21 @@ __global__ void __launch_bounds__(32 * kCapWarps, 5) k_capture(CaptureArgs A) {
     }
     na = __shfl_sync(FULL, na, 0);
     __syncwarp();
+    // Image correction of this node's class must first cross the triangle
+    // the last ray reflected or passed on (MultiPathCorrection's last step):
+    // an FP32 filter from the class's image source towards each receiver
+    // rejects ~99.9% of receivers before the reception test.  Stage counts
+    // need every capture, so they keep the reception test first.
+    const bool root = is_root_class(nd.cls);
+    Tri32 Tl;
+    TriFrom Fl;
+    float3 img = make_float3(0.0f, 0.0f, 0.0f);
+    if (!root) {
+      const ClassInfo& ci = A.cls_info[nd.cls];
+      img = make_float3(ci.img32[0], ci.img32[1], ci.img32[2]);
+      Tl = A.sc.corr32[A.sc.rank_to_id[ci.tri]];
+      Fl = tri_from(Tl, img, sqrtf(img.x * img.x + img.y * img.y + img.z * img.z));
+    }
     if (P.n_rx > 0) {
       const float tanb = float(P.tan_beta);
       const float cmax = A.gb[nd.tx].cmax;
@@ -921,6 +946,16 @@ __global__ void __launch_bounds__(32 * kCapWarps, 5) k_capture(CaptureArgs A) {
               const int gi = __float_as_int(c4.w);
               const double* c64 = A.rx + 3 * size_t(gi);
               ++cand;
+              if (!A.stage_counts) {
+                if (root) {
+                  if (!A.direct_ok[gi]) continue;
+                } else {
+                  const float3 dd = make_float3(c.x - img.x, c.y - img.y, c.z - img.z);
+                  if (!tri_filter_from(Tl, Fl, dd,
+                                       sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z)))
+                    continue;
+                }
+              }
               int v;
               if (lam < a || lam > b) {
                 // outside the chunk's own range: full-margin test
@@ -938,6 +973,18 @@ __global__ void __launch_bounds__(32 * kCapWarps, 5) k_capture(CaptureArgs A) {
                 const float rad = (S + np) * tanb;
                 const float rh = rad + mr, rl2 = rad - mr;
                 v = d2 > rh * rh ? 0 : ((rl2 > 0.0f && d2 < rl2 * rl2) ? 1 : -1);
+              }
+              if (!A.stage_counts) {
+                // everything after the FP32 tests (exact reception test,
+                // image correction, ancestor suppression) runs densely in
+                // k_capture_finish
+                if (v == 0) continue;
+                const unsigned long long slot = atomicAdd(&A.ctr->pairs, 1ull);
+                if (slot < A.pair_cap)
+                  A.pairs[slot] = make_uint2(uint32_t(i), uint32_t(gi) | (v < 0 ? 0x80000000u : 0u));
+                else
+                  atomicOr(&A.ctr->overflow, kOvPairs);
+                continue;
               }
               if (v < 0) {
                 ++n64;
@@ -1006,6 +1053,67 @@ __global__ void __launch_bounds__(32 * kCapWarps, 5) k_capture(CaptureArgs A) {
   if (lane == 0) {
     if (events) atomicAdd(&A.ctr->events, events);
     if (cand) atomicAdd(&A.ctr->cand, cand);
+    if (anc_tests) atomicAdd(&A.ctr->anc, anc_tests);
+    if (n64) atomicAdd(&A.ctr->fp64_capture, (unsigned long long)n64);
+  }
+}
+
+// The FP64 part of capture for the pairs k_capture could not settle in FP32:
+// the exact reception test where the FP32 one was unsure, then image
+// correction (MultiPathCorrection / DirectPathCorrection) and suppression by
+// an ancestor capturing the same receiver (RTSolver.cpp:277-284), as in
+// k_capture.  One thread per pair keeps the FP64 pipe busy with full warps.
+__global__ void __launch_bounds__(128) k_capture_finish(CaptureArgs A) {
+  if (A.ctr->overflow & (kOvTrace | kOvPairs)) return;  // this solve will be repeated
+  const unsigned long long n = min(A.ctr->pairs, A.pair_cap);
+  unsigned n64 = 0;
+  unsigned long long anc_tests = 0;
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint2 pr = A.pairs[k];
+    const uint32_t i = pr.x;
+    const int gi = int(pr.y & 0x7fffffffu);
+    const NodeHot nd = A.nodes[i];
+    const TxParams& P = A.txp[nd.tx];
+    const double* c64 = A.rx + 3 * size_t(gi);
+    if (pr.y >> 31) {
+      ++n64;
+      if (!capture_exact(A.nodes_cold, i, c64, P.tan_beta)) continue;
+    }
+    const float3 c = make_float3(float(c64[0]), float(c64[1]), float(c64[2]));
+    const bool ok = is_root_class(nd.cls) ? A.direct_ok[gi] != 0
+                                          : correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
+    if (!ok) continue;
+    const float tanb = float(P.tan_beta);
+    bool sup = false;
+    for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
+      const NodeHot a = A.nodes[p];
+      ++anc_tests;
+      int w = reception32(make_float3(a.s[0], a.s[1], a.s[2]), make_float3(a.u[0], a.u[1], a.u[2]),
+                          a.len, a.S, c, tanb);
+      if (w < 0) {
+        ++n64;
+        w = capture_exact(A.nodes_cold, p, c64, P.tan_beta);
+      }
+      if (w) {
+        sup = true;
+        break;
+      }
+      p = a.parent;
+    }
+    if (sup) continue;
+    const unsigned long long kk = atomicAdd(&A.ctr->corrected, 1ull);
+    if (kk < A.corr_cap)
+      A.corr_list[kk] =
+          Corrected{uint32_t(gi), nd.cls, (unsigned long long)nd.launch << kHeapBits | nd.heap};
+    else
+      atomicOr(&A.ctr->overflow, kOvCorr);
+  }
+  for (int o = 16; o; o >>= 1) {
+    anc_tests += __shfl_xor_sync(0xffffffffu, anc_tests, o);
+    n64 += __shfl_xor_sync(0xffffffffu, n64, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
     if (anc_tests) atomicAdd(&A.ctr->anc, anc_tests);
     if (n64) atomicAdd(&A.ctr->fp64_capture, (unsigned long long)n64);
   }
@@ -1119,7 +1227,8 @@ __global__ void k_dedup(const Corrected* list, unsigned long long cap, const Cla
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     const Corrected e = list[i];
-    const uint32_t ds = ht_insert(dedup, dedup_key(info, e), &ctr->overflow, kOvDedup, &ctr->used_dd);
+    const uint32_t ds = ht_insert(dedup, dedup_key(info, e), &ctr->overflow, kOvDedup, &ctr->used_dd,
+                                &ctr->lost_dd);
     if (ds != 0xFFFFFFFFu) atomicMin(&dedup_rank[ds], e.rank);
   }
 }
@@ -1312,6 +1421,7 @@ struct Workspace {
   DBuf<unsigned long long> cls_keys, cop_keys, dd_keys, dd_rank;
   DBuf<ClassInfo> cls_info;
   DBuf<Corrected> corr_list;
+  DBuf<uint2> pairs;  // capture pairs left to the FP64 pass
   DBuf<unsigned char> direct_ok;
   DBuf<Survivor> surv;
   DBuf<int> s_counts, s_starts, s_cursor, s_order;
@@ -1325,11 +1435,11 @@ struct Workspace {
   DBuf<unsigned long long> find_work;  // work counter of the running search launch
   // capacities (grown from occupancy and on overflow)
   unsigned long long cap_nodes = 1 << 20, cap_queue = 1 << 19, cap_surv = 1 << 14;
-  unsigned long long cap_corr = 1 << 16;
+  unsigned long long cap_corr = 1 << 16, cap_pairs = 1 << 20;
   uint32_t cap_cls = 1 << 16, cap_cop = 1 << 14, cap_dd = 1 << 14;
   // occupancy seen per executed segment in earlier solves, used to size the
   // tables of the next solve before it runs
-  double r_cls = 0, r_cop = 0, r_corr = 0, r_dd = 0, r_surv = 0;
+  double r_cls = 0, r_cop = 0, r_corr = 0, r_dd = 0, r_surv = 0, r_pairs = 0;
   ~Workspace() {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
@@ -1792,6 +1902,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         W.cap_corr, (unsigned long long)std::min(1.2 * W.r_corr * nodes, cap_bytes / sizeof(Corrected)));
     W.cap_surv = std::max<unsigned long long>(
         W.cap_surv, (unsigned long long)std::min(1.2 * W.r_surv * nodes, cap_bytes / 640.0));
+    W.cap_pairs = std::max<unsigned long long>(
+        W.cap_pairs, (unsigned long long)std::min(1.3 * W.r_pairs * nodes, cap_bytes / sizeof(uint2)));
   }
   for (int attempt = 0;; ++attempt) {
     if (attempt > 6) throw std::string("capacity: tables kept overflowing");
@@ -1804,6 +1916,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.cls_info.ensure(W.cap_cls);
     W.cop_keys.ensure(W.cap_cop);
     W.corr_list.ensure(W.cap_corr);
+    W.pairs.ensure(W.cap_pairs);
     W.dd_keys.ensure(W.cap_dd);
     W.dd_rank.ensure(W.cap_dd);
     W.surv.ensure(W.cap_surv);
@@ -1887,10 +2000,13 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ca.ctr = W.ctr.p;
     ca.node_cap = W.cap_nodes;
     ca.stage_counts = stage_counts;
+    ca.pairs = W.pairs.p;
+    ca.pair_cap = W.cap_pairs;
     if (rx_total)
       k_direct<<<grid_for(rx_total, 64), 64, 0, st>>>(S.dev, W.txp.p, W.rx.p, W.rx_req.p, rx_total,
                                                       W.direct_ok.p, W.ctr.p);
     k_capture<<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
+    if (!stage_counts) k_capture_finish<<<152 * 16, 128, 0, st>>>(ca);
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[4], st));
     // ---- duplicate removal over the corrected captures
@@ -1920,11 +2036,18 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         for (auto v : c.queue) mx = std::max(mx, v);
         W.cap_queue = std::max(W.cap_queue * 2, mx + mx / 8);
       }
-      if (c.overflow & kOvClass) W.cap_cls *= 4;
-      if (c.overflow & kOvCop) W.cap_cop *= 4;
+      // at least 4x, and twice what the refused inserts say was needed (the
+      // trace stops at the overflow, so later depths are not counted)
+      auto regrow = [](uint32_t& cap, unsigned long long used, unsigned long long lost) {
+        const unsigned long long need = std::max<unsigned long long>(4ull * cap, 2 * (used + lost));
+        while (cap < need && cap < (1u << 30)) cap *= 2;
+      };
+      if (c.overflow & kOvClass) regrow(W.cap_cls, c.used_cls, c.lost_cls);
+      if (c.overflow & kOvCop) regrow(W.cap_cop, c.used_cop, c.lost_cop);
       if (c.overflow & kOvCorr) W.cap_corr = std::max(W.cap_corr * 2, c.corrected + c.corrected / 4);
-      if (c.overflow & kOvDedup) W.cap_dd *= 4;
+      if (c.overflow & kOvDedup) regrow(W.cap_dd, c.used_dd, c.lost_dd);
       if (c.overflow & kOvSurv) W.cap_surv = next_pow2(c.survivors + c.survivors / 4);
+      if (c.overflow & kOvPairs) W.cap_pairs = std::max(W.cap_pairs * 2, c.pairs + c.pairs / 4);
       continue;
     }
     if (c.nodes) {
@@ -1938,6 +2061,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       upd(W.r_dd, c.used_dd / n);
       upd(W.r_corr, c.corrected / n);
       upd(W.r_surv, c.survivors / n);
+      upd(W.r_pairs, c.pairs / n);
     }
     // ---- field + ordered per-receiver sum
     const unsigned long long ns = c.survivors;

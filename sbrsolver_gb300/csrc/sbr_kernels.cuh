@@ -161,6 +161,56 @@ __device__ __forceinline__ bool tri_filter(const Tri32& T, const float3& o, cons
   return true;
 }
 
+// tri_filter for many rays from one origin o (an image source towards many
+// receivers): the terms that depend only on o and the triangle are formed
+// once.  Same arithmetic and margins as tri_filter.
+struct TriFrom {
+  float sx, sy, sz;  // o - v1
+  float qx, qy, qz;  // (o - v1) x e1
+  float W;           // e2 . q
+  float ns;          // |o| + |v1|
+};
+
+__device__ __forceinline__ TriFrom tri_from(const Tri32& T, const float3& o, float no) {
+  TriFrom F;
+  F.sx = o.x - T.v1[0];
+  F.sy = o.y - T.v1[1];
+  F.sz = o.z - T.v1[2];
+  F.qx = F.sy * T.e1[2] - F.sz * T.e1[1];
+  F.qy = F.sz * T.e1[0] - F.sx * T.e1[2];
+  F.qz = F.sx * T.e1[1] - F.sy * T.e1[0];
+  F.W = T.e2[0] * F.qx + T.e2[1] * F.qy + T.e2[2] * F.qz;
+  F.ns = no + T.nv1;
+  return F;
+}
+
+__device__ __forceinline__ bool tri_filter_from(const Tri32& T, const TriFrom& F,
+                                                const float3& d, float nd) {
+  const float hx = d.y * T.e2[2] - d.z * T.e2[1];
+  const float hy = d.z * T.e2[0] - d.x * T.e2[2];
+  const float hz = d.x * T.e2[1] - d.y * T.e2[0];
+  const float a = T.e1[0] * hx + T.e1[1] * hy + T.e1[2] * hz;
+  float U = F.sx * hx + F.sy * hy + F.sz * hz;
+  float V = d.x * F.qx + d.y * F.qy + d.z * F.qz;
+  float W = F.W;
+  const float ea = kFiltK * T.ne1 * T.ne2 * nd;
+  const float eU = kFiltK * F.ns * nd * T.ne2;
+  const float eV = kFiltK * F.ns * T.ne1 * nd;
+  const float eW = kFiltK * F.ns * T.ne1 * T.ne2;
+  const float A = fabsf(a);
+  if (A <= kEps32 + ea) return true;  // near-parallel: the FP64 test decides
+  if (a < 0.0f) {
+    U = -U;
+    V = -V;
+    W = -W;
+  }
+  if (U < -eU || V < -eV) return false;
+  if (U > A + ea + eU) return false;
+  if (U + V > A + ea + eU + eV) return false;
+  const float thi = (W + eW) / (A - ea);
+  return thi > kEps32 * 0.5f;
+}
+
 // As tri_filter, also telling whether the FP64 test certainly hits (2) or
 // may go either way (1); 0 = certainly misses.  [tlo, thi] bounds t.
 __device__ __forceinline__ int tri_classify(const Tri32& T, const float3& o, const float3& d,
