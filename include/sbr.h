@@ -110,6 +110,7 @@ typedef struct sbr_counts {
   long long keys;               /* distinct (receiver, coplanar key) after correction */
   long long near_edge_paths;    /* surviving paths with an interaction point within 1e-6
                                    (barycentric) of its triangle's edge */
+  long long gpu_kernels;        /* kernel launches of the solve (a batch's, for its parts) */
 } sbr_counts;
 
 /* One surviving path; its rays are [ray_offset, ray_offset + n_rays) in the

@@ -66,7 +66,7 @@ class Counts(C.Structure):
                                              "fp64_capture_tests", "launches",
                                              "capture_candidates", "ancestor_tests",
                                              "classes", "groups", "keys",
-                                             "near_edge_paths")]
+                                             "near_edge_paths", "gpu_kernels")]
 
 
 class Path(C.Structure):

@@ -778,13 +778,80 @@ __device__ __noinline__ int capture_exact(const NodeCold* cold, uint32_t idx, co
 // come from shared memory.
 constexpr int kCapWarps = 4;
 
+// The cone of points c for which the line from the image source img towards
+// c crosses triangle T (MultiPathCorrection's first test for a capture at
+// c; RTSolver.cpp:356): three planes through img and the triangle's edges,
+// n_k . p >= off_k, each loosened by 2 m_k, m_k bounding the FP32 error of
+// the test for |p| <= cmax (2^-12 relative, four times the FP32 filter margin).
+// The reference's FP64 test accepts only points inside the exact cone, so
+// receivers outside the loosened one are skipped without changing a result.
+// Returns false when the cone is ill-conditioned (then no cell is culled).
+__device__ __forceinline__ bool correction_cone(const Tri32& T, const float3& img, float nimg,
+                                                float cmax, float* out) {
+  const float v[3][3] = {{T.v1[0], T.v1[1], T.v1[2]},
+                         {T.v1[0] + T.e1[0], T.v1[1] + T.e1[1], T.v1[2] + T.e1[2]},
+                         {T.v1[0] + T.e2[0], T.v1[1] + T.e2[1], T.v1[2] + T.e2[2]}};
+  const float g[3] = {(v[0][0] + v[1][0] + v[2][0]) / 3.0f, (v[0][1] + v[1][1] + v[2][1]) / 3.0f,
+                      (v[0][2] + v[1][2] + v[2][2]) / 3.0f};
+  const float im[3] = {img.x, img.y, img.z};
+  const float mag = cmax + nimg + T.nv1 + T.ne1 + T.ne2 + 1.0f;
+  for (int k = 0; k < 3; ++k) {
+    const float* p = v[k];
+    const float* q = v[(k + 1) % 3];
+    const float a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
+    const float b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
+    float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    const float nn = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const float m = 2.44140625e-04f * nn * mag;  // 2^-12 |n| (|p| + |img| + |T| + 1)
+    // orient towards the triangle's centroid, which lies inside the cone
+    const float gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
+    if (!(fabsf(gc) > 4.0f * m) || !isfinite(m)) return false;
+    const float sg = gc > 0.0f ? 1.0f : -1.0f;
+    out[4 * k + 0] = sg * n[0];
+    out[4 * k + 1] = sg * n[1];
+    out[4 * k + 2] = sg * n[2];
+    // n.p >= n.img - 2m
+    out[4 * k + 3] = sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]) - 2.0f * m;
+  }
+  return true;
+}
+
+// Narrows the cell range [x0, x1] of grid row (iy, iz) to the cells whose
+// box can hold a point inside the cone; an empty row gets x0 > x1.
+__device__ __forceinline__ void cone_cells(const float* cone, const RxGrid& g, float inv_cell,
+                                           int iy, int iz, int& x0, int& x1) {
+  const float y0 = g.org[1] + iy * g.cell, y1 = y0 + g.cell;
+  const float z0 = g.org[2] + iz * g.cell, z1 = z0 + g.cell;
+  for (int k = 0; k < 3; ++k) {
+    const float nx = cone[4 * k], ny = cone[4 * k + 1], nz = cone[4 * k + 2], off = cone[4 * k + 3];
+    // need nx*x >= off - max over the row's y/z band of (ny*y + nz*z)
+    const float r = off - fmaxf(ny * y0, ny * y1) - fmaxf(nz * z0, nz * z1);
+    const float slack = 1e-3f * g.cell;
+    if (nx > 0.0f) {
+      const float xl = r / nx;  // x >= xl
+      if (isfinite(xl)) x0 = max(x0, int(floorf((xl - g.org[0] - slack) * inv_cell)));
+    } else if (nx < 0.0f) {
+      const float xh = r / nx;  // x <= xh
+      if (isfinite(xh)) x1 = min(x1, int(floorf((xh - g.org[0] + slack) * inv_cell)));
+    } else if (r > 0.0f) {
+      x1 = x0 - 1;
+    }
+  }
+}
+
 struct AncRec {
   float s[3], S, u[3], len;
   uint32_t idx, pad[3];
 };
 
-__global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
+// kStage: stage counts requested (every capture counted, the plain order of
+// tests); otherwise the fast path with the correction prefilter and the
+// deferred FP64 pass.
+template <bool kStage>
+__global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(CaptureArgs A) {
   __shared__ AncRec anc[kCapWarps][kMaxDepth];
+  // per warp: the correction cone of the node's class (3 planes n.p >= off)
+  __shared__ float cone[kCapWarps][12];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
@@ -800,11 +867,15 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
     const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
     const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
     const float len = nd.len, S = nd.S;
+    // Reciprocals for the cell-range arithmetic below.  Every range there is
+    // widened by at least 2e-3 m + cell/100, far more than the few ulps a
+    // product with a reciprocal differs from the quotient.
+    const float inv_uy = 1.0f / u.y, inv_uz = 1.0f / u.z, inv_cell = 1.0f / g.cell;
     // Stage the ancestor chain when every capture is checked against it
     // (stage counts); otherwise only corrected captures (~0.1% of captures)
     // need it and they walk the chain themselves.
     int na = 0;
-    if (A.stage_counts && lane == 0) {
+    if (kStage && lane == 0) {
       for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap && na < kMaxDepth;) {
         const NodeHot a = A.nodes[p];
         AncRec& r = anc[warp][na++];
@@ -825,11 +896,17 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
     Tri32 Tl;
     TriFrom Fl;
     float3 img = make_float3(0.0f, 0.0f, 0.0f);
+    bool use_cone = false;
     if (!root) {
       const ClassInfo& ci = A.cls_info[nd.cls];
       img = make_float3(ci.img32[0], ci.img32[1], ci.img32[2]);
       Tl = A.sc.corr32[A.sc.rank_to_id[ci.tri]];
-      Fl = tri_from(Tl, img, sqrtf(img.x * img.x + img.y * img.y + img.z * img.z));
+      const float nimg = sqrtf(img.x * img.x + img.y * img.y + img.z * img.z);
+      Fl = tri_from(Tl, img, nimg);
+      if (!kStage && lane == 0)
+        use_cone = correction_cone(Tl, img, nimg, A.gb[nd.tx].cmax, cone[warp]);
+      use_cone = __shfl_sync(FULL, use_cone, 0);
+      __syncwarp();
     }
     if (P.n_rx > 0) {
       const float tanb = float(P.tan_beta);
@@ -877,8 +954,8 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
           const float rb = (S + npmax) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f + mr;
           int c0[3], c1[3];
           for (int k = 0; k < 3; ++k) {
-            c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - rb - g.org[k]) / g.cell)));
-            c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + rb - g.org[k]) / g.cell)));
+            c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - rb - g.org[k]) * inv_cell)));
+            c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + rb - g.org[k]) * inv_cell)));
           }
           const int ny = c1[1] - c0[1] + 1, nz = c1[2] - c0[2] + 1;
           const int nrows = (c0[0] <= c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
@@ -893,14 +970,14 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
               float la = a, lb = b;
               bool ok = true;
               if (fabsf(u.y) > 1e-20f) {
-                const float t1 = (y0 - s.y) / u.y, t2 = (y1 - s.y) / u.y;
+                const float t1 = (y0 - s.y) * inv_uy, t2 = (y1 - s.y) * inv_uy;
                 la = fmaxf(la, fminf(t1, t2));
                 lb = fminf(lb, fmaxf(t1, t2));
               } else if (s.y < y0 || s.y > y1) {
                 ok = false;
               }
               if (fabsf(u.z) > 1e-20f) {
-                const float t1 = (z0 - s.z) / u.z, t2 = (z1 - s.z) / u.z;
+                const float t1 = (z0 - s.z) * inv_uz, t2 = (z1 - s.z) * inv_uz;
                 la = fmaxf(la, fminf(t1, t2));
                 lb = fminf(lb, fmaxf(t1, t2));
               } else if (s.z < z0 || s.z > z1) {
@@ -908,8 +985,10 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
               }
               if (ok && la <= lb) {
                 const float xa = s.x + la * u.x, xb = s.x + lb * u.x;
-                const int x0 = max(c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) / g.cell)));
-                const int x1 = min(c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) / g.cell)));
+                int x0 = max(c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) * inv_cell)));
+                int x1 = min(c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) * inv_cell)));
+                if (use_cone && x0 <= x1)
+                  cone_cells(cone[warp], g, inv_cell, iy, iz, x0, x1);
                 if (x0 <= x1) {
                   const int row = (iz * g.dim[1] + iy) * g.dim[0];
                   beg = g.cell_start[row + x0];
@@ -946,7 +1025,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
               const int gi = __float_as_int(c4.w);
               const double* c64 = A.rx + 3 * size_t(gi);
               ++cand;
-              if (!A.stage_counts) {
+              if (!kStage) {
                 if (root) {
                   if (!A.direct_ok[gi]) continue;
                 } else {
@@ -974,7 +1053,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
                 const float rh = rad + mr, rl2 = rad - mr;
                 v = d2 > rh * rh ? 0 : ((rl2 > 0.0f && d2 < rl2 * rl2) ? 1 : -1);
               }
-              if (!A.stage_counts) {
+              if (!kStage) {
                 // everything after the FP32 tests (exact reception test,
                 // image correction, ancestor suppression) runs densely in
                 // k_capture_finish
@@ -994,7 +1073,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
               // RayCapture deletes a captured node's subtree, so an ancestor
               // capturing the same receiver suppresses this one.
               auto suppressed = [&]() {
-                if (A.stage_counts) {
+                if (kStage) {
                   for (int q = 0; q < na; ++q) {
                     const AncRec& r = anc[warp][q];
                     ++anc_tests;
@@ -1022,7 +1101,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
                 }
                 return false;
               };
-              if (A.stage_counts) {
+              if (kStage) {
                 if (suppressed()) continue;
                 ++events;
               }
@@ -1030,7 +1109,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, 4) k_capture(CaptureArgs A) {
                                   ? A.direct_ok[gi] != 0
                                   : correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
               if (!ok) continue;
-              if (!A.stage_counts && suppressed()) continue;
+              if (!kStage && suppressed()) continue;
               const unsigned long long kk = atomicAdd(&A.ctr->corrected, 1ull);
               if (kk < A.corr_cap)
                 A.corr_list[kk] = Corrected{uint32_t(gi), nd.cls,
@@ -1439,7 +1518,9 @@ struct Workspace {
   uint32_t cap_cls = 1 << 16, cap_cop = 1 << 14, cap_dd = 1 << 14;
   // occupancy seen per executed segment in earlier solves, used to size the
   // tables of the next solve before it runs
-  double r_cls = 0, r_cop = 0, r_corr = 0, r_dd = 0, r_surv = 0, r_pairs = 0;
+  // (first solve: values typical of the urban canyon, so most first solves
+  // need no retry)
+  double r_cls = 0.01, r_cop = 0.004, r_corr = 0.01, r_dd = 5e-4, r_surv = 5e-4, r_pairs = 0.1;
   ~Workspace() {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
@@ -1761,6 +1842,7 @@ static FieldConsts field_consts() {
 // it (another pass of the same batch did).
 static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int n_req,
                        sbr_result& out, bool force_check = false) {
+  long long nl = 0;  // kernel launches of this solve (all attempts)
   cudaStream_t st = W.stream;
   if (S.host.mesh_order.empty()) throw std::string("scene is not initialised");
   CK(cudaSetDevice(S.device));
@@ -1861,13 +1943,13 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
   int max_rx = 1;
   for (auto& p : tp) max_rx = std::max(max_rx, p.n_rx);
   dim3 rg(std::min(1024, (max_rx + 255) / 256), n_req);
-  k_rx_bounds<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.gb.p);
-  k_grid_shape<<<1, 1, 0, st>>>(W.gb.p, W.grids.p, W.txp.p, n_req, max_cells, W.cell_base.p);
-  k_rx_count<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p, W.cell_counts.p);
-  k_scan_exclusive<<<1, 1024, 0, st>>>(W.cell_counts.p, W.cell_starts.p, int(cell_cap));
-  k_rx_scatter<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p,
+  ++nl, k_rx_bounds<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.gb.p);
+  ++nl, k_grid_shape<<<1, 1, 0, st>>>(W.gb.p, W.grids.p, W.txp.p, n_req, max_cells, W.cell_base.p);
+  ++nl, k_rx_count<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p, W.cell_counts.p);
+  ++nl, k_scan_exclusive<<<1, 1024, 0, st>>>(W.cell_counts.p, W.cell_starts.p, int(cell_cap));
+  ++nl, k_rx_scatter<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p,
                                    W.cell_starts.p, W.cell_cursor.p, W.rx32.p);
-  k_grid_finish<<<(n_req + 127) / 128, 128, 0, st>>>(W.grids.p, W.cell_starts.p, W.cell_base.p,
+  ++nl, k_grid_finish<<<(n_req + 127) / 128, 128, 0, st>>>(W.grids.p, W.cell_starts.p, W.cell_base.p,
                                                     W.rx32.p, n_req);
   CK(cudaGetLastError());
 
@@ -1924,10 +2006,10 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.seg_tx.ensure(n_req);
     CK(cudaMemsetAsync(W.seg_tx.p, 0, sizeof(unsigned long long) * n_req, st));
     const int fb = 256;
-    k_fill_u64<<<grid_for(W.cap_cls, fb), fb, 0, st>>>(W.cls_keys.p, W.cap_cls, kEmptyKey);
-    k_fill_u64<<<grid_for(W.cap_cop, fb), fb, 0, st>>>(W.cop_keys.p, W.cap_cop, kEmptyKey);
-    k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_keys.p, W.cap_dd, kEmptyKey);
-    k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_rank.p, W.cap_dd, kEmptyKey);
+    ++nl, k_fill_u64<<<grid_for(W.cap_cls, fb), fb, 0, st>>>(W.cls_keys.p, W.cap_cls, kEmptyKey);
+    ++nl, k_fill_u64<<<grid_for(W.cap_cop, fb), fb, 0, st>>>(W.cop_keys.p, W.cap_cop, kEmptyKey);
+    ++nl, k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_keys.p, W.cap_dd, kEmptyKey);
+    ++nl, k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_rank.p, W.cap_dd, kEmptyKey);
     CK(cudaEventRecord(W.ev[2], st));
     // ---- trace
     TraceArgs ta;
@@ -1978,8 +2060,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         ta.lo = fnd.lo = lo;
         ta.hi = fnd.hi = std::min(bound, lo + chunk);
         CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
-        k_find<<<find_grid(), 128, 0, st>>>(fnd);
-        k_trace<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
+        ++nl, k_find<<<find_grid(), 128, 0, st>>>(fnd);
+        ++nl, k_trace<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
       }
     }
     CK(cudaGetLastError());
@@ -2003,17 +2085,21 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ca.pairs = W.pairs.p;
     ca.pair_cap = W.cap_pairs;
     if (rx_total)
-      k_direct<<<grid_for(rx_total, 64), 64, 0, st>>>(S.dev, W.txp.p, W.rx.p, W.rx_req.p, rx_total,
+      ++nl, k_direct<<<grid_for(rx_total, 64), 64, 0, st>>>(S.dev, W.txp.p, W.rx.p, W.rx_req.p, rx_total,
                                                       W.direct_ok.p, W.ctr.p);
-    k_capture<<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
-    if (!stage_counts) k_capture_finish<<<152 * 16, 128, 0, st>>>(ca);
+    if (stage_counts) {
+      ++nl, k_capture<true><<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
+    } else {
+      ++nl, k_capture<false><<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
+      ++nl, k_capture_finish<<<152 * 16, 128, 0, st>>>(ca);
+    }
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[4], st));
     // ---- duplicate removal over the corrected captures
     const HashTable dd{W.dd_keys.p, W.cap_dd - 1};
-    k_dedup<<<grid_for(W.cap_corr, 256), 256, 0, st>>>(W.corr_list.p, W.cap_corr, W.cls_info.p,
+    ++nl, k_dedup<<<grid_for(W.cap_corr, 256), 256, 0, st>>>(W.corr_list.p, W.cap_corr, W.cls_info.p,
                                                        dd, W.dd_rank.p, W.ctr.p);
-    k_select<<<grid_for(W.cap_corr, 256), 256, 0, st>>>(W.corr_list.p, W.cap_corr, W.cls_info.p,
+    ++nl, k_select<<<grid_for(W.cap_corr, 256), 256, 0, st>>>(W.corr_list.p, W.cap_corr, W.cls_info.p,
                                                         dd, W.dd_rank.p, W.surv.p, W.cap_surv,
                                                         W.ctr.p);
     CK(cudaGetLastError());
@@ -2097,16 +2183,16 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fa.path_kind = W.path_kind.p;
     fa.path_near_edge = W.path_near.p;
     fa.path_pts = W.path_pts.p;
-    if (ns) k_field<<<grid_for(ns, 64), 64, 0, st>>>(fa);
+    if (ns) ++nl, k_field<<<grid_for(ns, 64), 64, 0, st>>>(fa);
     CK(cudaMemsetAsync(W.s_counts.p, 0, sizeof(int) * (rx_total + 1), st));
     CK(cudaMemsetAsync(W.s_cursor.p, 0, sizeof(int) * (rx_total + 1), st));
-    if (ns) k_surv_hist<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv, W.s_counts.p);
-    k_scan_exclusive<<<1, 1024, 0, st>>>(W.s_counts.p, W.s_starts.p, rx_total);
+    if (ns) ++nl, k_surv_hist<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv, W.s_counts.p);
+    ++nl, k_scan_exclusive<<<1, 1024, 0, st>>>(W.s_counts.p, W.s_starts.p, rx_total);
     if (ns)
-      k_surv_scatter<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv,
+      ++nl, k_surv_scatter<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv,
                                                         W.s_starts.p, W.s_cursor.p, W.s_order.p);
     if (rx_total)
-      k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
+      ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
                                                         rx_total, W.path_field.p, -1, W.rx_req.p,
                                                         W.txp.p, W.field.p);
     CK(cudaGetLastError());
@@ -2117,9 +2203,9 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       FieldArgs f64 = fa;
       f64.precision = 0;
       f64.path_field = W.path_field64.p;
-      if (ns) k_field<<<grid_for(ns, 64), 64, 0, st>>>(f64);
+      if (ns) ++nl, k_field<<<grid_for(ns, 64), 64, 0, st>>>(f64);
       if (rx_total)
-        k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
+        ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
                                                           rx_total, W.path_field64.p, 0,
                                                           W.rx_req.p, W.txp.p, W.field64.p);
       CK(cudaGetLastError());
@@ -2215,6 +2301,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     out.counts.keys = (long long)c.used_dd;
     out.counts.near_edge_paths = 0;
     for (const sbr_path& p : out.paths) out.counts.near_edge_paths += p.near_edge;
+    out.counts.gpu_kernels = nl;
     float ms[8] = {};
     for (int i = 1; i < 8; ++i) CK(cudaEventElapsedTime(&ms[i], W.ev[i - 1], W.ev[i]));
     out.timing.h2d_ms = ms[1];

@@ -126,3 +126,22 @@ def test_edge_cases(built):
     bad.request.tessellation = 13
     with pytest.raises(Exception):
         api.solve(sc, api.request_from_workload(bad.request))
+
+
+@pytest.mark.parametrize("which", ["urban", "large"])
+def test_fast_capture_equals_plain_capture_at_scale(built, which):
+    """At sizes the oracle cannot reach, the capture stage's fast path (image-
+    correction prefilter, correction-cone cell culling, deferred FP64 pass)
+    must give exactly what its plain path gives (reception test first, every
+    decision inline; used when stage counts are requested)."""
+    wl = (scenes.urban_scene(level=8) if which == "urban"
+          else scenes.large_scene(level=8, n_rx=20000))
+    sc = api.DeviceScene.from_scene(wl.scene)
+    fast = api.solve(sc, api.request_from_workload(wl.request, "fp64"), with_paths="arrays")
+    plain = api.solve(sc, api.request_from_workload(wl.request, "fp64", stage_counts=True),
+                      with_paths="arrays")
+    assert fast.counts["corrected"] == plain.counts["corrected"] > 0
+    assert fast.counts["paths"] == plain.counts["paths"] > 0
+    assert api.same_path_set(fast.paths, plain.paths)
+    np.testing.assert_array_equal(fast.field, plain.field)
+    sc.close()

@@ -34,7 +34,7 @@ def test_struct_layouts_match_header(tmp_path):
     """The ctypes structures have the header's sizes and field offsets (a C
     program compiled against include/sbr.h prints them)."""
     checks = {"sbr_request": (_lib.Request, ["n_rx", "rx", "stage_counts", "field_check"]),
-              "sbr_counts": (_lib.Counts, ["keys", "near_edge_paths"]),
+              "sbr_counts": (_lib.Counts, ["keys", "near_edge_paths", "gpu_kernels"]),
               "sbr_path": (_lib.Path, ["launch", "field", "near_edge"]),
               "sbr_timing": (_lib.Timing, ["device_ms"]),
               "sbr_field_error": (_lib.FieldError, ["max_rel_vec"]),
