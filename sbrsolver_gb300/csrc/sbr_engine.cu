@@ -786,32 +786,46 @@ constexpr int kCapWarps = 4;
 // The reference's FP64 test accepts only points inside the exact cone, so
 // receivers outside the loosened one are skipped without changing a result.
 // Returns false when the cone is ill-conditioned (then no cell is culled).
-__device__ __forceinline__ bool correction_cone(const Tri32& T, const float3& img, float nimg,
-                                                float cmax, float* out) {
-  const float v[3][3] = {{T.v1[0], T.v1[1], T.v1[2]},
-                         {T.v1[0] + T.e1[0], T.v1[1] + T.e1[1], T.v1[2] + T.e1[2]},
-                         {T.v1[0] + T.e2[0], T.v1[1] + T.e2[1], T.v1[2] + T.e2[2]}};
+__device__ __forceinline__ bool correction_cone_plane(const Tri32& T, const float3& img, float nimg,
+                                                      float cmax, int k, float* out) {
+  float v[3][3];
+  for (int a = 0; a < 3; ++a) {
+    v[0][a] = T.v1[a];
+    v[1][a] = T.v1[a] + T.e1[a];
+    v[2][a] = T.v1[a] + T.e2[a];
+  }
   const float g[3] = {(v[0][0] + v[1][0] + v[2][0]) / 3.0f, (v[0][1] + v[1][1] + v[2][1]) / 3.0f,
                       (v[0][2] + v[1][2] + v[2][2]) / 3.0f};
   const float im[3] = {img.x, img.y, img.z};
   const float mag = cmax + nimg + T.nv1 + T.ne1 + T.ne2 + 1.0f;
+  const float* p = v[k];
+  const float* q = v[k == 2 ? 0 : k + 1];
+  const float a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
+  const float b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
+  const float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+  const float nn = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  const float m = 2.44140625e-04f * nn * mag;  // 2^-12 |n| (|p| + |img| + |T| + 1)
+  // orient towards the triangle's centroid, which lies inside the cone
+  const float gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
+  if (!(fabsf(gc) > 4.0f * m) || !isfinite(m)) return false;
+  const float sg = gc > 0.0f ? 1.0f : -1.0f;
+  out[4 * k + 0] = sg * n[0];
+  out[4 * k + 1] = sg * n[1];
+  out[4 * k + 2] = sg * n[2];
+  // n.p >= n.img - 2m
+  out[4 * k + 3] = sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]) - 2.0f * m;
+  return true;
+}
+
+// Whether the box [lo, hi] may hold a point of the cone.
+__device__ __forceinline__ bool cone_meets_box(const float* cone, const float* lo, const float* hi) {
   for (int k = 0; k < 3; ++k) {
-    const float* p = v[k];
-    const float* q = v[(k + 1) % 3];
-    const float a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
-    const float b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
-    float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-    const float nn = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    const float m = 2.44140625e-04f * nn * mag;  // 2^-12 |n| (|p| + |img| + |T| + 1)
-    // orient towards the triangle's centroid, which lies inside the cone
-    const float gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
-    if (!(fabsf(gc) > 4.0f * m) || !isfinite(m)) return false;
-    const float sg = gc > 0.0f ? 1.0f : -1.0f;
-    out[4 * k + 0] = sg * n[0];
-    out[4 * k + 1] = sg * n[1];
-    out[4 * k + 2] = sg * n[2];
-    // n.p >= n.img - 2m
-    out[4 * k + 3] = sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]) - 2.0f * m;
+    float mx = 0.0f, mag = fabsf(cone[4 * k + 3]) + 1.0f;
+    for (int a = 0; a < 3; ++a) {
+      mx += fmaxf(cone[4 * k + a] * lo[a], cone[4 * k + a] * hi[a]);
+      mag += fabsf(cone[4 * k + a]) * fmaxf(fabsf(lo[a]), fabsf(hi[a]));
+    }
+    if (mx < cone[4 * k + 3] - 1e-3f * mag) return false;  // slack >> FP32 error of mx
   }
   return true;
 }
@@ -903,9 +917,10 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
       Tl = A.sc.corr32[A.sc.rank_to_id[ci.tri]];
       const float nimg = sqrtf(img.x * img.x + img.y * img.y + img.z * img.z);
       Fl = tri_from(Tl, img, nimg);
-      if (!kStage && lane == 0)
-        use_cone = correction_cone(Tl, img, nimg, A.gb[nd.tx].cmax, cone[warp]);
-      use_cone = __shfl_sync(FULL, use_cone, 0);
+      bool ok_plane = true;
+      if (!kStage && lane < 3)
+        ok_plane = correction_cone_plane(Tl, img, nimg, A.gb[nd.tx].cmax, lane, cone[warp]);
+      use_cone = !kStage && __all_sync(FULL, ok_plane);
       __syncwarp();
     }
     if (P.n_rx > 0) {
@@ -958,7 +973,15 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
             c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + rb - g.org[k]) * inv_cell)));
           }
           const int ny = c1[1] - c0[1] + 1, nz = c1[2] - c0[2] + 1;
-          const int nrows = (c0[0] <= c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
+          int nrows = (c0[0] <= c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
+          if (use_cone && nrows) {  // the chunk's cells all outside the cone: skip it
+            float blo[3], bhi[3];
+            for (int k = 0; k < 3; ++k) {
+              blo[k] = g.org[k] + c0[k] * g.cell;
+              bhi[k] = g.org[k] + (c1[k] + 1) * g.cell;
+            }
+            if (!cone_meets_box(cone[warp], blo, bhi)) nrows = 0;
+          }
           for (int rbase = 0; rbase < nrows; rbase += 32) {
             // this lane's row: the part of the chunk within rb of its y/z band
             int beg = 0, cnt = 0;
