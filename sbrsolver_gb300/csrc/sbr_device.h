@@ -158,6 +158,22 @@ struct __align__(16) ClassInfo {
   uint32_t pad2;
 };
 
+// What the capture stage needs of a class, formed once when the class is
+// interned: the FP32 image source, the FP32 image-correction filter terms
+// from it to the class's last triangle (mesh position tpos), and that
+// triangle's correction cone without the request-dependent margin (see
+// k_capture).
+struct __align__(16) ClassCap {
+  float img[3];
+  int tpos;        // corr32 index of the last triangle
+  float F[8];      // TriFrom: o - v1, (o - v1) x e1, e2 . q, |o| + |v1|
+  float n[3][4];   // cone plane k: oriented normal, n . img
+  float nn[3];     // |n_k|
+  float w[3];      // |n_k| (|img| + |T| + 1)
+  float gc[3];     // |n_k . (centroid - img)|
+  float inv_nx[3]; // 1 / n_k.x
+};
+
 // A capture whose image correction succeeded (one reference path before
 // duplicate removal).
 struct Corrected {

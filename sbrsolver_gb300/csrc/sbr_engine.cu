@@ -117,7 +117,7 @@ constexpr uint32_t kMaxProbe = 256;
 
 __device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long key, unsigned* ov,
                                               unsigned bit, unsigned long long* used,
-                                              unsigned long long* lost) {
+                                              unsigned long long* lost, bool* fresh = nullptr) {
   uint32_t h = uint32_t(mix64(key)) & t.mask;
   const uint32_t lim = min(kMaxProbe, t.mask + 1);
   for (uint32_t i = 0; i < lim; ++i) {
@@ -127,6 +127,7 @@ __device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long ke
       unsigned long long old = atomicCAS(&t.keys[h], kEmptyKey, key);
       if (old == kEmptyKey) {
         atomicAdd(used, 1ull);
+        if (fresh) *fresh = true;
         return h;
       }
       if (old == key) return h;
@@ -341,6 +342,7 @@ struct TraceArgs {
   unsigned long long node_cap;
   HashTable cls_tab, cop_tab;
   ClassInfo* cls_info;
+  ClassCap* cls_cap;
   const int* tri_cop;  // coplanar id by rank
   Counters* ctr;
   unsigned long long* seg_per_tx;  // executed segments per request
@@ -359,6 +361,50 @@ __device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long 
     else hi = mid - 1;
   }
   return lo;
+}
+
+// The capture-stage record of a class with image source img (FP64) whose
+// last ray starts on the triangle at mesh position tpos.
+__device__ void write_class_cap(const DevScene& sc, const double* img, int tpos, ClassCap& cc) {
+  const Tri32 T = sc.corr32[tpos];
+  const float3 o = make_float3(float(img[0]), float(img[1]), float(img[2]));
+  const float no = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
+  const TriFrom F = tri_from(T, o, no);
+  cc.img[0] = o.x;
+  cc.img[1] = o.y;
+  cc.img[2] = o.z;
+  cc.tpos = tpos;
+  cc.F[0] = F.sx; cc.F[1] = F.sy; cc.F[2] = F.sz;
+  cc.F[3] = F.qx; cc.F[4] = F.qy; cc.F[5] = F.qz;
+  cc.F[6] = F.W; cc.F[7] = F.ns;
+  float v[3][3];
+  for (int a = 0; a < 3; ++a) {
+    v[0][a] = T.v1[a];
+    v[1][a] = T.v1[a] + T.e1[a];
+    v[2][a] = T.v1[a] + T.e2[a];
+  }
+  const float im[3] = {o.x, o.y, o.z};
+  const float g[3] = {(v[0][0] + v[1][0] + v[2][0]) / 3.0f, (v[0][1] + v[1][1] + v[2][1]) / 3.0f,
+                      (v[0][2] + v[1][2] + v[2][2]) / 3.0f};
+  const float tmag = no + T.nv1 + T.ne1 + T.ne2 + 1.0f;
+  for (int k = 0; k < 3; ++k) {
+    const float* p = v[k];
+    const float* q = v[k == 2 ? 0 : k + 1];
+    const float a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
+    const float b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
+    const float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                        a[0] * b[1] - a[1] * b[0]};
+    const float nn = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    // orient towards the triangle's centroid, which lies inside the cone
+    const float gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
+    const float sg = gc > 0.0f ? 1.0f : -1.0f;
+    for (int c = 0; c < 3; ++c) cc.n[k][c] = sg * n[c];
+    cc.n[k][3] = sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]);
+    cc.nn[k] = nn;
+    cc.w[k] = nn * tmag;
+    cc.gc[k] = fabsf(gc);
+    cc.inv_nx[k] = 1.0f / (sg * n[0]);
+  }
 }
 
 // Every thread that interns a class writes the same values (they depend
@@ -665,10 +711,14 @@ __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
         c.rc = r.rc;
         c.tc = r.tc + 1;
         const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
+        bool fresh = false;
         c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
-                          &A.ctr->lost_cls);
+                          &A.ctr->lost_cls, &fresh);
         c.cop = cop_cls;
-        if (c.cls != 0xFFFFFFFFu) write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
+        if (fresh) {  // only the thread that interned the class writes its records
+          write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
+          write_class_cap(A.sc, pimg, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
+        }
         if (slot < A.out_cap) A.out[slot] = c;
         else atomicOr(&A.ctr->overflow, kOvQueue);
         ++slot;
@@ -682,10 +732,11 @@ __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
         c.rc = r.rc + 1;
         c.tc = r.tc;
         const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1);
+        bool fresh = false;
         c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
-                          &A.ctr->lost_cls);
+                          &A.ctr->lost_cls, &fresh);
         c.cop = cop_cls;
-        if (c.cls != 0xFFFFFFFFu) {
+        if (fresh) {  // only the thread that interned the class writes its records
           // ImagePoint (RTSolver.cpp:910-924) across the triangle the
           // reference finds at this id's position of its mesh vector
           const CorrTri& M = A.sc.corr[A.sc.rank_to_id[h.rank]];
@@ -694,6 +745,7 @@ __global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
           const double dist = x64::dot(M.n, w);
           for (int a = 0; a < 3; ++a) img[a] = x64::sub(pimg[a], x64::mul(x64::mul(2.0, dist), M.n[a]));
           write_class(A.cls_info[c.cls], img, r.cls, h.rank, cop_cls, 1, A.depth + 1);
+          write_class_cap(A.sc, img, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
         }
         if (slot < A.out_cap) A.out[slot] = c;
         else atomicOr(&A.ctr->overflow, kOvQueue);
@@ -715,6 +767,7 @@ struct CaptureArgs {
   const GridBuild* gb;
   const double* rx;
   const ClassInfo* cls_info;
+  const ClassCap* cls_cap;
   const unsigned char* direct_ok;
   Corrected* corr_list;
   unsigned long long corr_cap;
@@ -777,45 +830,22 @@ __device__ __noinline__ int capture_exact(const NodeCold* cold, uint32_t idx, co
 // of the node captures the same receiver (RTSolver.cpp:277-284); ancestors
 // come from shared memory.
 constexpr int kCapWarps = 4;
+// Minimum chunk length along a segment, in receiver-grid cells.
+#ifndef SBR_CAP_CHUNK_CELLS
+#define SBR_CAP_CHUNK_CELLS 16
+#endif
+constexpr float kCapChunkCells = SBR_CAP_CHUNK_CELLS;
 
-// The cone of points c for which the line from the image source img towards
-// c crosses triangle T (MultiPathCorrection's first test for a capture at
-// c; RTSolver.cpp:356): three planes through img and the triangle's edges,
-// n_k . p >= off_k, each loosened by 2 m_k, m_k bounding the FP32 error of
-// the test for |p| <= cmax (2^-12 relative, four times the FP32 filter margin).
-// The reference's FP64 test accepts only points inside the exact cone, so
-// receivers outside the loosened one are skipped without changing a result.
-// Returns false when the cone is ill-conditioned (then no cell is culled).
-__device__ __forceinline__ bool correction_cone_plane(const Tri32& T, const float3& img, float nimg,
-                                                      float cmax, int k, float* out) {
-  float v[3][3];
-  for (int a = 0; a < 3; ++a) {
-    v[0][a] = T.v1[a];
-    v[1][a] = T.v1[a] + T.e1[a];
-    v[2][a] = T.v1[a] + T.e2[a];
-  }
-  const float g[3] = {(v[0][0] + v[1][0] + v[2][0]) / 3.0f, (v[0][1] + v[1][1] + v[2][1]) / 3.0f,
-                      (v[0][2] + v[1][2] + v[2][2]) / 3.0f};
-  const float im[3] = {img.x, img.y, img.z};
-  const float mag = cmax + nimg + T.nv1 + T.ne1 + T.ne2 + 1.0f;
-  const float* p = v[k];
-  const float* q = v[k == 2 ? 0 : k + 1];
-  const float a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
-  const float b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
-  const float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-  const float nn = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-  const float m = 2.44140625e-04f * nn * mag;  // 2^-12 |n| (|p| + |img| + |T| + 1)
-  // orient towards the triangle's centroid, which lies inside the cone
-  const float gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
-  if (!(fabsf(gc) > 4.0f * m) || !isfinite(m)) return false;
-  const float sg = gc > 0.0f ? 1.0f : -1.0f;
-  out[4 * k + 0] = sg * n[0];
-  out[4 * k + 1] = sg * n[1];
-  out[4 * k + 2] = sg * n[2];
-  // n.p >= n.img - 2m
-  out[4 * k + 3] = sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]) - 2.0f * m;
-  return true;
-}
+// Correction cone of a class: the points c for which the line from the
+// image source img towards c crosses the class's last triangle T
+// (MultiPathCorrection's first test for a capture at c; RTSolver.cpp:356).
+// Three planes through img and T's edges, n_k . p >= n_k . img, formed once
+// per class (write_class_cap); k_capture loosens each by 2 m_k, m_k =
+// 2^-12 |n_k| (cmax + |img| + |T| + 1) bounding the FP32 error of the test
+// for receivers |p| <= cmax (four times the FP32 filter margin), and uses
+// no cone when a plane is ill-conditioned.  The reference's FP64 test accepts
+// only points inside the exact cone, so receivers outside the loosened one
+// are skipped without changing a result.
 
 // Whether the box [lo, hi] may hold a point of the cone.
 __device__ __forceinline__ bool cone_meets_box(const float* cone, const float* lo, const float* hi) {
@@ -842,10 +872,10 @@ __device__ __forceinline__ void cone_cells(const float* cone, const RxGrid& g, f
     const float r = off - fmaxf(ny * y0, ny * y1) - fmaxf(nz * z0, nz * z1);
     const float slack = 1e-3f * g.cell;
     if (nx > 0.0f) {
-      const float xl = r / nx;  // x >= xl
+      const float xl = r * cone[12 + k];  // x >= xl
       if (isfinite(xl)) x0 = max(x0, int(floorf((xl - g.org[0] - slack) * inv_cell)));
     } else if (nx < 0.0f) {
-      const float xh = r / nx;  // x <= xh
+      const float xh = r * cone[12 + k];  // x <= xh
       if (isfinite(xh)) x1 = min(x1, int(floorf((xh - g.org[0] + slack) * inv_cell)));
     } else if (r > 0.0f) {
       x1 = x0 - 1;
@@ -865,7 +895,7 @@ template <bool kStage>
 __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(CaptureArgs A) {
   __shared__ AncRec anc[kCapWarps][kMaxDepth];
   // per warp: the correction cone of the node's class (3 planes n.p >= off)
-  __shared__ float cone[kCapWarps][12];
+  __shared__ float cone[kCapWarps][16];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
@@ -884,7 +914,8 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
     // Reciprocals for the cell-range arithmetic below.  Every range there is
     // widened by at least 2e-3 m + cell/100, far more than the few ulps a
     // product with a reciprocal differs from the quotient.
-    const float inv_uy = 1.0f / u.y, inv_uz = 1.0f / u.z, inv_cell = 1.0f / g.cell;
+    const float inv_ux = 1.0f / u.x, inv_uy = 1.0f / u.y, inv_uz = 1.0f / u.z;
+    const float inv_cell = 1.0f / g.cell;
     // Stage the ancestor chain when every capture is checked against it
     // (stage counts); otherwise only corrected captures (~0.1% of captures)
     // need it and they walk the chain themselves.
@@ -912,14 +943,23 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
     float3 img = make_float3(0.0f, 0.0f, 0.0f);
     bool use_cone = false;
     if (!root) {
-      const ClassInfo& ci = A.cls_info[nd.cls];
-      img = make_float3(ci.img32[0], ci.img32[1], ci.img32[2]);
-      Tl = A.sc.corr32[A.sc.rank_to_id[ci.tri]];
-      const float nimg = sqrtf(img.x * img.x + img.y * img.y + img.z * img.z);
-      Fl = tri_from(Tl, img, nimg);
+      const ClassCap& cc = A.cls_cap[nd.cls];
+      img = make_float3(cc.img[0], cc.img[1], cc.img[2]);
+      Tl = A.sc.corr32[cc.tpos];
+      Fl = TriFrom{cc.F[0], cc.F[1], cc.F[2], cc.F[3], cc.F[4], cc.F[5], cc.F[6], cc.F[7]};
       bool ok_plane = true;
-      if (!kStage && lane < 3)
-        ok_plane = correction_cone_plane(Tl, img, nimg, A.gb[nd.tx].cmax, lane, cone[warp]);
+      if (!kStage && lane < 3) {
+        // the cone's planes loosened by 2 m, m = 2^-12 |n| (cmax + |img| + |T| + 1)
+        const int k = lane;
+        const float m = 2.44140625e-04f * (cc.nn[k] * A.gb[nd.tx].cmax + cc.w[k]);
+        ok_plane = cc.gc[k] > 4.0f * m && isfinite(m);
+        float* o = cone[warp];
+        o[4 * k + 0] = cc.n[k][0];
+        o[4 * k + 1] = cc.n[k][1];
+        o[4 * k + 2] = cc.n[k][2];
+        o[4 * k + 3] = cc.n[k][3] - 2.0f * m;
+        o[12 + k] = cc.inv_nx[k];
+      }
       use_cone = !kStage && __all_sync(FULL, ok_plane);
       __syncwarp();
     }
@@ -941,18 +981,21 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
       for (int a = 0; a < 3 && lo <= hi; ++a) {
         const float sa = a == 0 ? s.x : (a == 1 ? s.y : s.z);
         const float ua = a == 0 ? u.x : (a == 1 ? u.y : u.z);
+        const float ia = a == 0 ? inv_ux : (a == 1 ? inv_uy : inv_uz);
         const float bl = g.bmin[a] - rbg, bh = g.bmax[a] + rbg;
         if (fabsf(ua) < 1e-20f) {
           if (sa < bl || sa > bh) hi = -1.0f;
         } else {
-          const float t1 = (bl - sa) / ua, t2 = (bh - sa) / ua;
-          lo = fmaxf(lo, fminf(t1, t2) - 1e-3f);
-          hi = fminf(hi, fmaxf(t1, t2) + 1e-3f);
+          // slack: 1 mm plus 2^-20 relative, beyond the reciprocal's rounding
+          const float t1 = (bl - sa) * ia, t2 = (bh - sa) * ia;
+          const float tn = fminf(t1, t2), tf = fmaxf(t1, t2);
+          lo = fmaxf(lo, tn - 1e-3f - 9.5367431640625e-07f * fabsf(tn));
+          hi = fminf(hi, tf + 1e-3f + 9.5367431640625e-07f * fabsf(tf));
         }
       }
       if (lo <= hi) {
         const float r0 = (S + sqrtf(fmaxf(0.0f, ss + 2.0f * lo * su + lo * lo))) * tanb;
-        const float lc = fmaxf(4.0f * g.cell, r0);
+        const float lc = fmaxf(kCapChunkCells * g.cell, r0);
         int nchunk = int(ceilf((hi - lo) / lc));
         nchunk = max(1, min(nchunk, 4096));
         const float step = (hi - lo) / nchunk;
@@ -1522,6 +1565,7 @@ struct Workspace {
   DBuf<NodeCold> nodes_cold;
   DBuf<unsigned long long> cls_keys, cop_keys, dd_keys, dd_rank;
   DBuf<ClassInfo> cls_info;
+  DBuf<ClassCap> cls_cap;
   DBuf<Corrected> corr_list;
   DBuf<uint2> pairs;  // capture pairs left to the FP64 pass
   DBuf<unsigned char> direct_ok;
@@ -2000,7 +2044,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       while (p < x && p < (1u << 30)) p <<= 1;
       return p;
     };
-    W.cap_cls = std::max(W.cap_cls, pow2(2.2 * W.r_cls * nodes, 8 + sizeof(ClassInfo), cap_bytes));
+    W.cap_cls = std::max(W.cap_cls, pow2(2.2 * W.r_cls * nodes, 8 + sizeof(ClassInfo) + sizeof(ClassCap), cap_bytes));
     W.cap_cop = std::max(W.cap_cop, pow2(2.2 * W.r_cop * nodes, 8, cap_bytes));
     W.cap_dd = std::max(W.cap_dd, pow2(2.2 * W.r_dd * nodes, 16, cap_bytes));
     W.cap_corr = std::max<unsigned long long>(
@@ -2019,6 +2063,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.q1.ensure(W.cap_queue);
     W.cls_keys.ensure(W.cap_cls);
     W.cls_info.ensure(W.cap_cls);
+    W.cls_cap.ensure(W.cap_cls);
     W.cop_keys.ensure(W.cap_cop);
     W.corr_list.ensure(W.cap_corr);
     W.pairs.ensure(W.cap_pairs);
@@ -2047,6 +2092,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ta.cls_tab = HashTable{W.cls_keys.p, W.cap_cls - 1};
     ta.cop_tab = HashTable{W.cop_keys.p, W.cap_cop - 1};
     ta.cls_info = W.cls_info.p;
+    ta.cls_cap = W.cls_cap.p;
     ta.tri_cop = S.tri_cop.p;
     ta.ctr = W.ctr.p;
     ta.seg_per_tx = W.seg_tx.p;
@@ -2099,6 +2145,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ca.gb = W.gb.p;
     ca.rx = W.rx.p;
     ca.cls_info = W.cls_info.p;
+    ca.cls_cap = W.cls_cap.p;
     ca.direct_ok = W.direct_ok.p;
     ca.corr_list = W.corr_list.p;
     ca.corr_cap = W.cap_corr;

@@ -207,8 +207,8 @@ __device__ __forceinline__ bool tri_filter_from(const Tri32& T, const TriFrom& F
   if (U < -eU || V < -eV) return false;
   if (U > A + ea + eU) return false;
   if (U + V > A + ea + eU + eV) return false;
-  const float thi = (W + eW) / (A - ea);
-  return thi > kEps32 * 0.5f;
+  // thi = (W + eW) / (A - ea) > eps/2 with A - ea > 0, without the division
+  return W + eW > (kEps32 * 0.5f) * (A - ea);
 }
 
 // As tri_filter, also telling whether the FP64 test certainly hits (2) or
@@ -284,8 +284,10 @@ struct TraceStats {
 //   e = 2^-20 (|lo| + |hi| + 2|o|) / |d|
 // of its FP64 value.  A flat axis (lo == hi) gives one FP64 value t for both
 // planes, so the FP64 test accepts iff the other axes' intervals contain it.
+// inv = 1/d in FP32: a product with it differs from the quotient by a few
+// ulps, far inside e.
 __device__ __forceinline__ int slab_certain(const float* bb, int flatmask, const float3& o,
-                                            const float3& d) {
+                                            const float3& d, const float3& inv) {
   const float K = 9.5367431640625e-07f;  // 2^-20
   float A_lo = -INFINITY, A_hi = -INFINITY, B_lo = INFINITY, B_hi = INFINITY;
   float v = 0.0f, ev = 0.0f;
@@ -295,10 +297,11 @@ __device__ __forceinline__ int slab_certain(const float* bb, int flatmask, const
   for (int a = 0; a < 3; ++a) {
     const float da = a == 0 ? d.x : (a == 1 ? d.y : d.z);
     const float oa = a == 0 ? o.x : (a == 1 ? o.y : o.z);
+    const float ia = a == 0 ? inv.x : (a == 1 ? inv.y : inv.z);
     if (da == 0.0f) return -1;
     const float lo = bb[a], hi = bb[3 + a];
-    const float t1 = (lo - oa) / da, t2 = (hi - oa) / da;
-    const float e = K * (fabsf(lo) + fabsf(hi) + 2.0f * fabsf(oa)) / fabsf(da);
+    const float t1 = (lo - oa) * ia, t2 = (hi - oa) * ia;
+    const float e = K * (fabsf(lo) + fabsf(hi) + 2.0f * fabsf(oa)) * fabsf(ia);
     if (!isfinite(t1) || !isfinite(t2) || !isfinite(e)) return -1;
     if (flatmask & (1 << a)) {
       if (flat++) return -1;
@@ -475,7 +478,7 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
   if (ok && best.rank != INT_MAX) {
     // every ancestor of the winner's leaf must pass the FP64 slab test
     for (int n = best.leaf; n >= 0; n = sc.ref[n].parent) {
-      int v = slab_certain(sc.ref[n].fb, sc.ref[n].flat, o32, d32);
+      int v = slab_certain(sc.ref[n].fb, sc.ref[n].flat, o32, d32, inv);
       if (v < 0) v = slab64(sc.ref[n].bb, o, d) ? 1 : 0;
       if (!v) {
         ok = false;
@@ -544,8 +547,9 @@ __device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d
   // every ancestor of the winner's leaf must pass the reference's slab test
   const float3 o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
   const float3 d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
+  const float3 i32 = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
   for (int n = best.leaf; n >= 0; n = sc.ref[n].parent) {
-    int v = slab_certain(sc.ref[n].fb, sc.ref[n].flat, o32, d32);
+    int v = slab_certain(sc.ref[n].fb, sc.ref[n].flat, o32, d32, i32);
     if (v < 0) v = slab64(sc.ref[n].bb, o, d) ? 1 : 0;
     if (!v) {
       ++st.fallback;
