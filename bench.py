@@ -223,7 +223,7 @@ def run_batched(precision: str):
             "field_error_vs_fp64": err}
 
 
-def run_serving(precision: str, n_req: int = 48, rates=(10.0, 50.0, 500.0), slots: int = 4):
+def run_serving(precision: str, n_req: int = 96, rates=(10.0, 50.0, 500.0), slots: int = 4):
     """The config-4 mix through the server at Poisson arrival rates `rates`
     (req/s), against the same requests solved one at a time.  At the highest
     rate the queue saturates, so its throughput is the sustained capacity."""

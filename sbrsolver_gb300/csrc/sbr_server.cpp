@@ -3,10 +3,13 @@
 // call from main()).
 //
 // A server owns `slots` worker threads.  Submitted requests (copied, with
-// their receivers) wait in one FIFO queue.  A worker takes the head request
-// as soon as (a) the worker is free and (b) the request's device-memory
-// estimate fits in the HBM budget next to the requests already running.  If
-// the head is small, the worker also takes the queued small requests on the
+// their receivers) wait in one queue.  A free worker takes the queued request
+// with the least remaining priority cost that fits in the HBM budget next to
+// the requests already running: cost = its device-memory estimate (which
+// scales with its ray-tree bound, i.e. its work) minus kAgingBytesPerSec per
+// second it has waited, so short requests go first and every request is
+// served within about a second of becoming the oldest.  If the chosen
+// request is small, the worker also takes the queued small requests on the
 // same scene (up to kMaxBatch, within the budget) and solves them together in
 // one device pass (sbr_solve_batch), which fills the GPU far better than
 // small requests one by one.  Every solve checks a workspace (buffers + CUDA
@@ -57,6 +60,9 @@ long long estimate_bytes(const sbr_request& q) {
 }
 
 constexpr size_t kMaxBatch = 64;
+// Waiting time converted to priority: a request that has waited one second
+// ranks like one whose estimate is 16 GB smaller.
+constexpr double kAgingBytesPerSec = 16e9;
 // Requests at most this large (device-memory estimate) are batched together.
 constexpr long long kSmallBytes = 512LL << 20;
 
@@ -74,6 +80,26 @@ struct sbr_server {
   std::vector<std::thread> workers;
   int device = 0;
 
+  // Index of the queued request to run next (least aged cost among those
+  // that fit the budget), or -1.  Caller holds mu.
+  long pick() const {
+    const Clock::time_point now = Clock::now();
+    long best = -1;
+    double best_cost = 0;
+    for (size_t k = 0; k < queue.size(); ++k) {
+      const Job& j = queue[k];
+      const long long need = std::min(j.est_bytes, budget);
+      if (!(in_flight == 0 || in_flight + need <= budget)) continue;
+      const double waited = std::chrono::duration<double>(now - j.submitted).count();
+      const double cost = double(j.est_bytes) - kAgingBytesPerSec * waited;
+      if (best < 0 || cost < best_cost) {
+        best = long(k);
+        best_cost = cost;
+      }
+    }
+    return best;
+  }
+
   void worker() {
     cudaSetDevice(device);
     for (;;) {
@@ -81,15 +107,15 @@ struct sbr_server {
       long long est = 0;
       {
         std::unique_lock<std::mutex> lock(mu);
+        long sel = -1;
         cv_work.wait(lock, [&] {
           if (stopping && queue.empty()) return true;
-          if (queue.empty()) return false;
-          const long long need = std::min(queue.front().est_bytes, budget);
-          return in_flight == 0 || in_flight + need <= budget;
+          sel = pick();
+          return sel >= 0;
         });
         if (queue.empty()) return;
-        batch.push_back(std::move(queue.front()));
-        queue.pop_front();
+        batch.push_back(std::move(queue[size_t(sel)]));
+        queue.erase(queue.begin() + sel);
         est = std::min(batch[0].est_bytes, budget);
         if (batch[0].est_bytes <= kSmallBytes) {
           for (auto it = queue.begin(); it != queue.end() && batch.size() < kMaxBatch;) {
