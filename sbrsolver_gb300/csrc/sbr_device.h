@@ -47,6 +47,15 @@ struct RefNode {
   int c0, c1, first, count, parent, flat;
 };
 
+// One box on a reference leaf's path to the root (leaf first), stored
+// contiguously per leaf so the reachability check of a hit reads one run
+// instead of chasing parent links.  node < 0 ends a leaf's run.
+struct __align__(16) AncBox {
+  float fb[6];
+  int flat;  // RefNode::flat
+  int node;  // RefNode index (its FP64 box decides cases the FP32 test cannot)
+};
+
 // Triangle, depth-first leaf order (index == closest-hit tie rank).
 struct __align__(16) Tri32 {
   float v1[3], nv1;  // |v1|
@@ -83,6 +92,8 @@ struct DevScene {
   const Node32* snode;
   const Tri32* stri;    // triangles in search leaf order
   const int* srank;     // their depth-first ranks
+  const AncBox* anc;    // per reference leaf: its boxes up to the root
+  const int* anc_off;   // start of a leaf's run in anc (by node index)
   int n_tri, n_nodes, n_mats;
   int root_leaf;
   float box_margin;  // absolute FP32 box expansion (metres)

@@ -1607,6 +1607,8 @@ struct SceneImpl {
   DBuf<Node32> snode;
   DBuf<Tri32> stri;
   DBuf<int> srank;
+  DBuf<AncBox> anc;
+  DBuf<int> anc_off;
   DBuf<CorrTri> corr;
   DBuf<Tri32> corr32;
   DBuf<Material> mats;
@@ -1759,6 +1761,30 @@ static void upload_scene(SceneImpl& S) {
     S.dev.srank = S.srank.p;
     CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
   }
+  {  // every reference leaf's boxes up to the root, one run per leaf
+    std::vector<AncBox> ab;
+    std::vector<int> off(nn, -1);
+    for (int i = 0; i < nn; ++i) {
+      if (H.nodes[i].c0 >= 0) continue;
+      off[i] = int(ab.size());
+      for (int n = i; n >= 0; n = H.nodes[n].parent) {
+        AncBox b;
+        std::memcpy(b.fb, ref[n].fb, sizeof b.fb);
+        b.flat = ref[n].flat;
+        b.node = n;
+        ab.push_back(b);
+      }
+      AncBox end;
+      std::memset(&end, 0, sizeof end);
+      end.node = -1;
+      ab.push_back(end);
+    }
+    S.anc.upload(ab.data(), ab.size(), st);
+    S.anc_off.upload(off.data(), off.size(), st);
+    S.dev.anc = S.anc.p;
+    S.dev.anc_off = S.anc_off.p;
+    CK(cudaStreamSynchronize(st));
+  }
   S.tri_cop.upload(cop.data(), cop.size(), st);
   S.rank_to_id.upload(r2i.data(), r2i.size(), st);
   S.dev.node32 = S.node32.p;
@@ -1774,7 +1800,10 @@ static void upload_scene(SceneImpl& S) {
   S.dev.box_margin = float(margin_m);
   S.dev_bytes = (long long)(n32.size() * sizeof(Node32) + ref.size() * sizeof(RefNode) +
                             t32.size() * sizeof(Tri32) + t64.size() * sizeof(Tri64) +
-                            2 * nt * sizeof(int) + nt * sizeof(CorrTri));
+                            2 * nt * sizeof(int) + nt * sizeof(CorrTri) +
+                            S.snode.n * sizeof(Node32) + S.stri.n * sizeof(Tri32) +
+                            S.srank.n * sizeof(int) + S.anc.n * sizeof(AncBox) +
+                            S.anc_off.n * sizeof(int));
   CK(cudaStreamSynchronize(st));
 }
 

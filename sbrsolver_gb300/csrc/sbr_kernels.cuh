@@ -548,9 +548,11 @@ __device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d
   const float3 o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
   const float3 d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
   const float3 i32 = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
-  for (int n = best.leaf; n >= 0; n = sc.ref[n].parent) {
-    int v = slab_certain(sc.ref[n].fb, sc.ref[n].flat, o32, d32, i32);
-    if (v < 0) v = slab64(sc.ref[n].bb, o, d) ? 1 : 0;
+  for (const AncBox* a = sc.anc + sc.anc_off[best.leaf];; ++a) {
+    const AncBox b = *a;
+    if (b.node < 0) break;
+    int v = slab_certain(b.fb, b.flat, o32, d32, i32);
+    if (v < 0) v = slab64(sc.ref[b.node].bb, o, d) ? 1 : 0;
     if (!v) {
       ++st.fallback;
       return exact_closest(sc, o, d, best, overflow);
