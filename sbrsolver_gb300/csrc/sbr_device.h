@@ -144,7 +144,8 @@ struct TxParams {
 
 struct RxGrid {
   float org[3], cell;
-  int dim[3], pad;
+  int dim[3];
+  float inv_cell;  // 1 / cell
   const int* cell_start;  // ncell + 1
   const float4* rx32;     // sorted by cell: xyz, w = receiver index (int bits)
   float bmin[3], bmax[3];

@@ -251,6 +251,7 @@ __global__ void k_grid_shape(GridBuild* gb, RxGrid* grids, const TxParams* txp, 
       g.bmax[a] = hi[a];
     }
     g.cell = cell;
+    g.inv_cell = 1.0f / cell;
     gb[r].ncell = int(tot);
     gb[r].cmax = o2f(gb[r].cmax_o);
     cell_base[r] = base;
@@ -611,7 +612,11 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
   }
 }
 
-__global__ void __launch_bounds__(128, 4) k_trace(TraceArgs A) {
+// Resident blocks of k_trace per SM (register budget 65536 / (128 x this)).
+#ifndef SBR_TRACE_BLOCKS
+#define SBR_TRACE_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
   const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
   const long long n_in = min(n_all, A.hi);
@@ -836,6 +841,15 @@ constexpr int kCapWarps = 4;
 #endif
 constexpr float kCapChunkCells = SBR_CAP_CHUNK_CELLS;
 
+// Upper bound on sqrt(x) from the hardware reciprocal square root (relative
+// error below 2^-21), for the capture stage's conservative ranges and
+// margins, which all carry slack far beyond that.
+__device__ __forceinline__ float sqrt_up(float x) {
+  if (!(x > 0.0f)) return 0.0f;
+  if (isinf(x)) return x;
+  return x * rsqrtf(x) * 1.00000095367431640625f;  // 1 + 2^-20
+}
+
 // Correction cone of a class: the points c for which the line from the
 // image source img towards c crosses the class's last triangle T
 // (MultiPathCorrection's first test for a capture at c; RTSolver.cpp:356).
@@ -888,14 +902,70 @@ struct AncRec {
   uint32_t idx, pad[3];
 };
 
+// A node's segment clipped to the region that can hold a capture of this
+// request's receivers, cut into chunks (nchunk = 0: nothing to test).
+struct NodeSpan {
+  float lo, hi, step, ns;  // ns = |segment start|
+  int nchunk, use_cone;
+};
+
+// The receivers that can fall inside the node's reception spheres lie within
+// rb of its segment (rb bounds the sphere radius (S + |P|) tan(beta), with
+// |P| <= (cmax + S tan b) / (1 - tan b) for any capturing point).  All
+// ranges are widened well beyond their FP32 rounding.
+__device__ __forceinline__ NodeSpan node_span(const NodeHot& nd, const TxParams& P,
+                                              const RxGrid& g, float cmax, int use_cone) {
+  NodeSpan sp{0.0f, -1.0f, 0.0f, 0.0f, 0, use_cone};
+  if (P.n_rx <= 0) return sp;
+  const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
+  const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
+  const float len = nd.len, S = nd.S;
+  const float tanb = float(P.tan_beta);
+  const float pmax = __fdividef(cmax + S * tanb, fmaxf(1e-6f, 1.0f - tanb)) * 1.0001f + 1.0f;
+  const float su = s.x * u.x + s.y * u.y + s.z * u.z;
+  const float ss = s.x * s.x + s.y * s.y + s.z * s.z;
+  sp.ns = sqrt_up(ss);
+  const float disc = su * su - (ss - pmax * pmax);
+  float lo = 0.0f, hi = -1.0f;
+  if (disc >= 0.0f) {
+    const float sq = sqrt_up(disc);
+    lo = fmaxf(0.0f, -su - sq);
+    hi = fminf(len, -su + sq);
+  }
+  const float rbg = (S + pmax) * tanb * 1.0001f + 1e-3f;  // bound over the whole segment
+  for (int a = 0; a < 3 && lo <= hi; ++a) {
+    const float sa = a == 0 ? s.x : (a == 1 ? s.y : s.z);
+    const float ua = a == 0 ? u.x : (a == 1 ? u.y : u.z);
+    const float bl = g.bmin[a] - rbg, bh = g.bmax[a] + rbg;
+    if (fabsf(ua) < 1e-20f) {
+      if (sa < bl || sa > bh) hi = -1.0f;
+    } else {
+      // slack: 1 mm plus 2^-20 relative, beyond the reciprocal's rounding
+      const float ia = __frcp_rn(ua);
+      const float t1 = (bl - sa) * ia, t2 = (bh - sa) * ia;
+      const float tn = fminf(t1, t2), tf = fmaxf(t1, t2);
+      lo = fmaxf(lo, tn - 1e-3f - 9.5367431640625e-07f * fabsf(tn));
+      hi = fminf(hi, tf + 1e-3f + 9.5367431640625e-07f * fabsf(tf));
+    }
+  }
+  if (!(lo <= hi)) return sp;
+  const float r0 = (S + sqrt_up(ss + 2.0f * lo * su + lo * lo)) * tanb;
+  const float lc = fmaxf(kCapChunkCells * g.cell, r0);
+  int nchunk = int(ceilf(__fdividef(hi - lo, lc)));
+  nchunk = max(1, min(nchunk, 4096));
+  sp.lo = lo;
+  sp.hi = hi;
+  sp.nchunk = nchunk;
+  sp.step = __fdividef(hi - lo, float(nchunk));
+  return sp;
+}
+
 // kStage: stage counts requested (every capture counted, the plain order of
 // tests); otherwise the fast path with the correction prefilter and the
 // deferred FP64 pass.
 template <bool kStage>
 __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(CaptureArgs A) {
   __shared__ AncRec anc[kCapWarps][kMaxDepth];
-  // per warp: the correction cone of the node's class (3 planes n.p >= off)
-  __shared__ float cone[kCapWarps][16];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
@@ -903,291 +973,292 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
   unsigned long long events = 0, cand = 0, anc_tests = 0;
   unsigned n64 = 0;
   const unsigned long long nw = (unsigned long long)gridDim.x * kCapWarps;
-  for (unsigned long long i = (unsigned long long)blockIdx.x * kCapWarps + warp; i < n_nodes;
-       i += nw) {
-    const NodeHot nd = A.nodes[i];
-    const TxParams& P = A.txp[nd.tx];
-    const RxGrid& g = A.grids[nd.tx];
-    const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
-    const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
-    const float len = nd.len, S = nd.S;
-    // Reciprocals for the cell-range arithmetic below.  Every range there is
-    // widened by at least 2e-3 m + cell/100, far more than the few ulps a
-    // product with a reciprocal differs from the quotient.
-    const float inv_ux = 1.0f / u.x, inv_uy = 1.0f / u.y, inv_uz = 1.0f / u.z;
-    const float inv_cell = 1.0f / g.cell;
-    // Stage the ancestor chain when every capture is checked against it
-    // (stage counts); otherwise only corrected captures (~0.1% of captures)
-    // need it and they walk the chain themselves.
-    int na = 0;
-    if (kStage && lane == 0) {
-      for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap && na < kMaxDepth;) {
-        const NodeHot a = A.nodes[p];
-        AncRec& r = anc[warp][na++];
-        r.s[0] = a.s[0]; r.s[1] = a.s[1]; r.s[2] = a.s[2]; r.S = a.S;
-        r.u[0] = a.u[0]; r.u[1] = a.u[1]; r.u[2] = a.u[2]; r.len = a.len;
-        r.idx = p;
-        p = a.parent;
+  // Nodes are taken 32 at a time: each lane loads one node's record, its
+  // class record and last triangle, so the three dependent loads are paid
+  // once per 32 nodes; the warp then works through the 32 from shared memory.
+  __shared__ NodeHot s_nh[kCapWarps][32];
+  __shared__ Tri32 s_tl[kCapWarps][32];      // the class's last triangle
+  __shared__ float s_fl[kCapWarps][32][12];  // image source + correction filter terms
+  __shared__ float s_cn[kCapWarps][32][16];  // loosened correction cone
+  __shared__ NodeSpan s_sp[kCapWarps][32];   // clipped span and chunking
+  for (unsigned long long base = ((unsigned long long)blockIdx.x * kCapWarps + warp) * 32;
+       base < n_nodes; base += nw * 32) {
+    {
+      const unsigned long long my = base + lane;
+      if (my < n_nodes) {
+        const NodeHot h = A.nodes[my];
+        s_nh[warp][lane] = h;
+        const float cmax = A.gb[h.tx].cmax;
+        int cone_ok = 0;
+        if (!is_root_class(h.cls)) {
+          const ClassCap c = A.cls_cap[h.cls];
+          s_tl[warp][lane] = A.sc.corr32[c.tpos];
+          float* fl = s_fl[warp][lane];
+          for (int q = 0; q < 3; ++q) fl[q] = c.img[q];
+          for (int q = 0; q < 8; ++q) fl[3 + q] = c.F[q];
+          // the cone's planes loosened by 2 m, m = 2^-12 |n| (cmax + |img| + |T| + 1)
+          float* cn = s_cn[warp][lane];
+          cone_ok = !kStage;
+          for (int k = 0; k < 3; ++k) {
+            const float m = 2.44140625e-04f * (c.nn[k] * cmax + c.w[k]);
+            cone_ok &= (c.gc[k] > 4.0f * m && isfinite(m)) ? 1 : 0;
+            cn[4 * k + 0] = c.n[k][0];
+            cn[4 * k + 1] = c.n[k][1];
+            cn[4 * k + 2] = c.n[k][2];
+            cn[4 * k + 3] = c.n[k][3] - 2.0f * m;
+            cn[12 + k] = c.inv_nx[k];
+          }
+        }
+        s_sp[warp][lane] = node_span(h, A.txp[h.tx], A.grids[h.tx], cmax, cone_ok);
       }
-    }
-    na = __shfl_sync(FULL, na, 0);
-    __syncwarp();
-    // Image correction of this node's class must first cross the triangle
-    // the last ray reflected or passed on (MultiPathCorrection's last step):
-    // an FP32 filter from the class's image source towards each receiver
-    // rejects ~99.9% of receivers before the reception test.  Stage counts
-    // need every capture, so they keep the reception test first.
-    const bool root = is_root_class(nd.cls);
-    Tri32 Tl;
-    TriFrom Fl;
-    float3 img = make_float3(0.0f, 0.0f, 0.0f);
-    bool use_cone = false;
-    if (!root) {
-      const ClassCap& cc = A.cls_cap[nd.cls];
-      img = make_float3(cc.img[0], cc.img[1], cc.img[2]);
-      Tl = A.sc.corr32[cc.tpos];
-      Fl = TriFrom{cc.F[0], cc.F[1], cc.F[2], cc.F[3], cc.F[4], cc.F[5], cc.F[6], cc.F[7]};
-      bool ok_plane = true;
-      if (!kStage && lane < 3) {
-        // the cone's planes loosened by 2 m, m = 2^-12 |n| (cmax + |img| + |T| + 1)
-        const int k = lane;
-        const float m = 2.44140625e-04f * (cc.nn[k] * A.gb[nd.tx].cmax + cc.w[k]);
-        ok_plane = cc.gc[k] > 4.0f * m && isfinite(m);
-        float* o = cone[warp];
-        o[4 * k + 0] = cc.n[k][0];
-        o[4 * k + 1] = cc.n[k][1];
-        o[4 * k + 2] = cc.n[k][2];
-        o[4 * k + 3] = cc.n[k][3] - 2.0f * m;
-        o[12 + k] = cc.inv_nx[k];
-      }
-      use_cone = !kStage && __all_sync(FULL, ok_plane);
       __syncwarp();
     }
-    if (P.n_rx > 0) {
-      const float tanb = float(P.tan_beta);
-      const float cmax = A.gb[nd.tx].cmax;
-      const float pmax = (cmax + S * tanb) / fmaxf(1e-6f, 1.0f - tanb) * 1.0001f + 1.0f;
-      const float su = s.x * u.x + s.y * u.y + s.z * u.z;
-      const float ss = s.x * s.x + s.y * s.y + s.z * s.z;
-      const float ns = sqrtf(ss);
-      const float disc = su * su - (ss - pmax * pmax);
-      float lo = 0.0f, hi = -1.0f;
-      if (disc >= 0.0f) {
-        const float sq = sqrtf(disc);
-        lo = fmaxf(0.0f, -su - sq);
-        hi = fminf(len, -su + sq);
-      }
-      const float rbg = (S + pmax) * tanb * 1.0001f + 1e-3f;  // bound over the whole segment
-      for (int a = 0; a < 3 && lo <= hi; ++a) {
-        const float sa = a == 0 ? s.x : (a == 1 ? s.y : s.z);
-        const float ua = a == 0 ? u.x : (a == 1 ? u.y : u.z);
-        const float ia = a == 0 ? inv_ux : (a == 1 ? inv_uy : inv_uz);
-        const float bl = g.bmin[a] - rbg, bh = g.bmax[a] + rbg;
-        if (fabsf(ua) < 1e-20f) {
-          if (sa < bl || sa > bh) hi = -1.0f;
-        } else {
-          // slack: 1 mm plus 2^-20 relative, beyond the reciprocal's rounding
-          const float t1 = (bl - sa) * ia, t2 = (bh - sa) * ia;
-          const float tn = fminf(t1, t2), tf = fmaxf(t1, t2);
-          lo = fmaxf(lo, tn - 1e-3f - 9.5367431640625e-07f * fabsf(tn));
-          hi = fminf(hi, tf + 1e-3f + 9.5367431640625e-07f * fabsf(tf));
+    const int n_here = int(min(32ull, n_nodes - base));
+    for (int jj = 0; jj < n_here; ++jj) {
+      const unsigned long long i = base + jj;
+      const NodeHot nd = s_nh[warp][jj];
+      const TxParams& P = A.txp[nd.tx];
+      const RxGrid& g = A.grids[nd.tx];
+      const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
+      const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
+      const float len = nd.len, S = nd.S;
+      // Reciprocals for the cell-range arithmetic below.  Every range there is
+      // widened by at least 2e-3 m + cell/100, far more than the few ulps a
+      // product with a reciprocal differs from the quotient.
+      const float inv_uy = __frcp_rn(u.y), inv_uz = __frcp_rn(u.z);
+      const float inv_cell = g.inv_cell;
+      // Stage the ancestor chain when every capture is checked against it
+      // (stage counts); otherwise only corrected captures (~0.1% of captures)
+      // need it and they walk the chain themselves.
+      int na = 0;
+      if (kStage && lane == 0) {
+        for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap && na < kMaxDepth;) {
+          const NodeHot a = A.nodes[p];
+          AncRec& r = anc[warp][na++];
+          r.s[0] = a.s[0]; r.s[1] = a.s[1]; r.s[2] = a.s[2]; r.S = a.S;
+          r.u[0] = a.u[0]; r.u[1] = a.u[1]; r.u[2] = a.u[2]; r.len = a.len;
+          r.idx = p;
+          p = a.parent;
         }
       }
-      if (lo <= hi) {
-        const float r0 = (S + sqrtf(fmaxf(0.0f, ss + 2.0f * lo * su + lo * lo))) * tanb;
-        const float lc = fmaxf(kCapChunkCells * g.cell, r0);
-        int nchunk = int(ceilf((hi - lo) / lc));
-        nchunk = max(1, min(nchunk, 4096));
-        const float step = (hi - lo) / nchunk;
+      na = __shfl_sync(FULL, na, 0);
+      __syncwarp();
+      // Image correction of this node's class must first cross the triangle
+      // the last ray reflected or passed on (MultiPathCorrection's last step):
+      // an FP32 filter from the class's image source towards each receiver
+      // rejects ~99.9% of receivers before the reception test.  Stage counts
+      // need every capture, so they keep the reception test first.
+      const bool root = is_root_class(nd.cls);
+      Tri32 Tl;
+      TriFrom Fl;
+      float3 img = make_float3(0.0f, 0.0f, 0.0f);
+      const NodeSpan sp = s_sp[warp][jj];
+      const bool use_cone = sp.use_cone != 0;
+      const float* cone_w = s_cn[warp][jj];
+      if (!root) {
+        const float* fl = s_fl[warp][jj];
+        img = make_float3(fl[0], fl[1], fl[2]);
+        Tl = s_tl[warp][jj];
+        Fl = TriFrom{fl[3], fl[4], fl[5], fl[6], fl[7], fl[8], fl[9], fl[10]};
+      }
+      if (sp.nchunk > 0) {
+        const float tanb = float(P.tan_beta);
+        const float cmax = A.gb[nd.tx].cmax;
+        const float lo = sp.lo, hi = sp.hi, ns = sp.ns;
+        const int nchunk = sp.nchunk;
+        const float step = sp.step;
         // error margins of the FP32 reception test, from per-node bounds
         const float ml = kFiltK * (ns + cmax + 1.0f);
-        for (int ch = 0; ch < nchunk; ++ch) {
-          const float a = lo + ch * step, b = (ch == nchunk - 1) ? hi : lo + (ch + 1) * step;
-          const float pa[3] = {s.x + a * u.x, s.y + a * u.y, s.z + a * u.z};
-          const float pb[3] = {s.x + b * u.x, s.y + b * u.y, s.z + b * u.z};
-          const float npmax = fmaxf(sqrtf(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]),
-                                    sqrtf(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]));
-          const float mr = kFiltK * (ns + cmax + S + npmax + 1.0f);
-          // |P| is convex along the chunk: the larger end bounds it
-          const float rb = (S + npmax) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f + mr;
-          int c0[3], c1[3];
-          for (int k = 0; k < 3; ++k) {
-            c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - rb - g.org[k]) * inv_cell)));
-            c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + rb - g.org[k]) * inv_cell)));
-          }
-          const int ny = c1[1] - c0[1] + 1, nz = c1[2] - c0[2] + 1;
-          int nrows = (c0[0] <= c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
-          if (use_cone && nrows) {  // the chunk's cells all outside the cone: skip it
-            float blo[3], bhi[3];
+        {
+          for (int ch = 0; ch < nchunk; ++ch) {
+            const float a = lo + ch * step, b = (ch == nchunk - 1) ? hi : lo + (ch + 1) * step;
+            const float pa[3] = {s.x + a * u.x, s.y + a * u.y, s.z + a * u.z};
+            const float pb[3] = {s.x + b * u.x, s.y + b * u.y, s.z + b * u.z};
+            const float npmax = fmaxf(sqrt_up(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]),
+                                      sqrt_up(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]));
+            const float mr = kFiltK * (ns + cmax + S + npmax + 1.0f);
+            // |P| is convex along the chunk: the larger end bounds it
+            const float rb = (S + npmax) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f + mr;
+            int c0[3], c1[3];
             for (int k = 0; k < 3; ++k) {
-              blo[k] = g.org[k] + c0[k] * g.cell;
-              bhi[k] = g.org[k] + (c1[k] + 1) * g.cell;
+              c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - rb - g.org[k]) * inv_cell)));
+              c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + rb - g.org[k]) * inv_cell)));
             }
-            if (!cone_meets_box(cone[warp], blo, bhi)) nrows = 0;
-          }
-          for (int rbase = 0; rbase < nrows; rbase += 32) {
-            // this lane's row: the part of the chunk within rb of its y/z band
-            int beg = 0, cnt = 0;
-            const int ridx = rbase + lane;
-            if (ridx < nrows) {
-              const int iy = c0[1] + ridx % ny, iz = c0[2] + ridx / ny;
-              const float y0 = g.org[1] + iy * g.cell - rb, y1 = g.org[1] + (iy + 1) * g.cell + rb;
-              const float z0 = g.org[2] + iz * g.cell - rb, z1 = g.org[2] + (iz + 1) * g.cell + rb;
-              float la = a, lb = b;
-              bool ok = true;
-              if (fabsf(u.y) > 1e-20f) {
-                const float t1 = (y0 - s.y) * inv_uy, t2 = (y1 - s.y) * inv_uy;
-                la = fmaxf(la, fminf(t1, t2));
-                lb = fminf(lb, fmaxf(t1, t2));
-              } else if (s.y < y0 || s.y > y1) {
-                ok = false;
+            const int ny = c1[1] - c0[1] + 1, nz = c1[2] - c0[2] + 1;
+            int nrows = (c0[0] <= c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
+            if (use_cone && nrows) {  // the chunk's cells all outside the cone: skip it
+              float blo[3], bhi[3];
+              for (int k = 0; k < 3; ++k) {
+                blo[k] = g.org[k] + c0[k] * g.cell;
+                bhi[k] = g.org[k] + (c1[k] + 1) * g.cell;
               }
-              if (fabsf(u.z) > 1e-20f) {
-                const float t1 = (z0 - s.z) * inv_uz, t2 = (z1 - s.z) * inv_uz;
-                la = fmaxf(la, fminf(t1, t2));
-                lb = fminf(lb, fmaxf(t1, t2));
-              } else if (s.z < z0 || s.z > z1) {
-                ok = false;
-              }
-              if (ok && la <= lb) {
-                const float xa = s.x + la * u.x, xb = s.x + lb * u.x;
-                int x0 = max(c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) * inv_cell)));
-                int x1 = min(c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) * inv_cell)));
-                if (use_cone && x0 <= x1)
-                  cone_cells(cone[warp], g, inv_cell, iy, iz, x0, x1);
-                if (x0 <= x1) {
-                  const int row = (iz * g.dim[1] + iy) * g.dim[0];
-                  beg = g.cell_start[row + x0];
-                  cnt = g.cell_start[row + x1 + 1] - beg;
+              if (!cone_meets_box(cone_w, blo, bhi)) nrows = 0;
+            }
+            for (int rbase = 0; rbase < nrows; rbase += 32) {
+              // this lane's row: the part of the chunk within rb of its y/z band
+              int beg = 0, cnt = 0;
+              const int ridx = rbase + lane;
+              if (ridx < nrows) {
+                const int iy = c0[1] + ridx % ny, iz = c0[2] + ridx / ny;
+                const float y0 = g.org[1] + iy * g.cell - rb, y1 = g.org[1] + (iy + 1) * g.cell + rb;
+                const float z0 = g.org[2] + iz * g.cell - rb, z1 = g.org[2] + (iz + 1) * g.cell + rb;
+                float la = a, lb = b;
+                bool ok = true;
+                if (fabsf(u.y) > 1e-20f) {
+                  const float t1 = (y0 - s.y) * inv_uy, t2 = (y1 - s.y) * inv_uy;
+                  la = fmaxf(la, fminf(t1, t2));
+                  lb = fminf(lb, fmaxf(t1, t2));
+                } else if (s.y < y0 || s.y > y1) {
+                  ok = false;
+                }
+                if (fabsf(u.z) > 1e-20f) {
+                  const float t1 = (z0 - s.z) * inv_uz, t2 = (z1 - s.z) * inv_uz;
+                  la = fmaxf(la, fminf(t1, t2));
+                  lb = fminf(lb, fmaxf(t1, t2));
+                } else if (s.z < z0 || s.z > z1) {
+                  ok = false;
+                }
+                if (ok && la <= lb) {
+                  const float xa = s.x + la * u.x, xb = s.x + lb * u.x;
+                  int x0 = max(c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) * inv_cell)));
+                  int x1 = min(c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) * inv_cell)));
+                  if (use_cone && x0 <= x1)
+                    cone_cells(cone_w, g, inv_cell, iy, iz, x0, x1);
+                  if (x0 <= x1) {
+                    const int row = (iz * g.dim[1] + iy) * g.dim[0];
+                    beg = g.cell_start[row + x0];
+                    cnt = g.cell_start[row + x1 + 1] - beg;
+                  }
                 }
               }
-            }
-            // concatenate the 32 rows' receiver runs
-            int incl = cnt;
-            for (int o = 1; o < 32; o <<= 1) {
-              const int v = __shfl_up_sync(FULL, incl, o);
-              if (lane >= o) incl += v;
-            }
-            const int total = __shfl_sync(FULL, incl, 31);
-            for (int kb = 0; kb < total; kb += 32) {
-              const int k = kb + lane;
-              // row holding item k: first lane whose inclusive count exceeds k
-              int rl = 0;
-              for (int step2 = 16; step2; step2 >>= 1) {
-                const int v = __shfl_sync(FULL, incl, rl + step2 - 1);
-                if (v <= k) rl += step2;
+              // concatenate the 32 rows' receiver runs
+              int incl = cnt;
+              for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += v;
               }
-              const int rincl = __shfl_sync(FULL, incl, rl);
-              const int rcnt = __shfl_sync(FULL, cnt, rl);
-              const int rbeg = __shfl_sync(FULL, beg, rl);
-              if (k >= total) continue;
-              const int j = rbeg + (k - (rincl - rcnt));
-              const float4 c4 = g.rx32[j];
-              const float3 c = make_float3(c4.x, c4.y, c4.z);
-              const float wx = c.x - s.x, wy = c.y - s.y, wz = c.z - s.z;
-              const float lam = u.x * wx + u.y * wy + u.z * wz;
-              if (ch > 0 && lam < a) continue;            // owned by an earlier chunk
-              if (ch < nchunk - 1 && lam >= b) continue;  // owned by a later chunk
-              const int gi = __float_as_int(c4.w);
-              const double* c64 = A.rx + 3 * size_t(gi);
-              ++cand;
-              if (!kStage) {
-                if (root) {
-                  if (!A.direct_ok[gi]) continue;
+              const int total = __shfl_sync(FULL, incl, 31);
+              for (int kb = 0; kb < total; kb += 32) {
+                const int k = kb + lane;
+                // row holding item k: first lane whose inclusive count exceeds k
+                int rl = 0;
+                for (int step2 = 16; step2; step2 >>= 1) {
+                  const int v = __shfl_sync(FULL, incl, rl + step2 - 1);
+                  if (v <= k) rl += step2;
+                }
+                const int rincl = __shfl_sync(FULL, incl, rl);
+                const int rcnt = __shfl_sync(FULL, cnt, rl);
+                const int rbeg = __shfl_sync(FULL, beg, rl);
+                if (k >= total) continue;
+                const int j = rbeg + (k - (rincl - rcnt));
+                const float4 c4 = g.rx32[j];
+                const float3 c = make_float3(c4.x, c4.y, c4.z);
+                const float wx = c.x - s.x, wy = c.y - s.y, wz = c.z - s.z;
+                const float lam = u.x * wx + u.y * wy + u.z * wz;
+                if (ch > 0 && lam < a) continue;            // owned by an earlier chunk
+                if (ch < nchunk - 1 && lam >= b) continue;  // owned by a later chunk
+                const int gi = __float_as_int(c4.w);
+                const double* c64 = A.rx + 3 * size_t(gi);
+                ++cand;
+                if (!kStage) {
+                  if (root) {
+                    if (!A.direct_ok[gi]) continue;
+                  } else {
+                    const float3 dd = make_float3(c.x - img.x, c.y - img.y, c.z - img.z);
+                    if (!tri_filter_from(Tl, Fl, dd,
+                                         sqrt_up(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z)))
+                      continue;
+                  }
+                }
+                int v;
+                if (lam < a || lam > b) {
+                  // outside the chunk's own range: full-margin test
+                  v = reception32(s, u, len, S, c, tanb);
+                } else if (lam < -ml) {
+                  v = 0;
+                } else if (lam <= ml) {
+                  v = -1;
                 } else {
-                  const float3 dd = make_float3(c.x - img.x, c.y - img.y, c.z - img.z);
-                  if (!tri_filter_from(Tl, Fl, dd,
-                                       sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z)))
-                    continue;
+                  const float lcl = fminf(lam, len);
+                  const float px = s.x + lcl * u.x, py = s.y + lcl * u.y, pz = s.z + lcl * u.z;
+                  const float np = sqrt_up(px * px + py * py + pz * pz);
+                  const float ex = c.x - px, ey = c.y - py, ez = c.z - pz;
+                  const float d2 = ex * ex + ey * ey + ez * ez;
+                  const float rad = (S + np) * tanb;
+                  const float rh = rad + mr, rl2 = rad - mr;
+                  v = d2 > rh * rh ? 0 : ((rl2 > 0.0f && d2 < rl2 * rl2) ? 1 : -1);
                 }
-              }
-              int v;
-              if (lam < a || lam > b) {
-                // outside the chunk's own range: full-margin test
-                v = reception32(s, u, len, S, c, tanb);
-              } else if (lam < -ml) {
-                v = 0;
-              } else if (lam <= ml) {
-                v = -1;
-              } else {
-                const float lcl = fminf(lam, len);
-                const float px = s.x + lcl * u.x, py = s.y + lcl * u.y, pz = s.z + lcl * u.z;
-                const float np = sqrtf(px * px + py * py + pz * pz);
-                const float ex = c.x - px, ey = c.y - py, ez = c.z - pz;
-                const float d2 = ex * ex + ey * ey + ez * ez;
-                const float rad = (S + np) * tanb;
-                const float rh = rad + mr, rl2 = rad - mr;
-                v = d2 > rh * rh ? 0 : ((rl2 > 0.0f && d2 < rl2 * rl2) ? 1 : -1);
-              }
-              if (!kStage) {
-                // everything after the FP32 tests (exact reception test,
-                // image correction, ancestor suppression) runs densely in
-                // k_capture_finish
-                if (v == 0) continue;
-                const unsigned long long slot = atomicAdd(&A.ctr->pairs, 1ull);
-                if (slot < A.pair_cap)
-                  A.pairs[slot] = make_uint2(uint32_t(i), uint32_t(gi) | (v < 0 ? 0x80000000u : 0u));
-                else
-                  atomicOr(&A.ctr->overflow, kOvPairs);
-                continue;
-              }
-              if (v < 0) {
-                ++n64;
-                v = capture_exact(A.nodes_cold, uint32_t(i), c64, P.tan_beta);
-              }
-              if (!v) continue;
-              // RayCapture deletes a captured node's subtree, so an ancestor
-              // capturing the same receiver suppresses this one.
-              auto suppressed = [&]() {
-                if (kStage) {
-                  for (int q = 0; q < na; ++q) {
-                    const AncRec& r = anc[warp][q];
+                if (!kStage) {
+                  // everything after the FP32 tests (exact reception test,
+                  // image correction, ancestor suppression) runs densely in
+                  // k_capture_finish
+                  if (v == 0) continue;
+                  const unsigned long long slot = atomicAdd(&A.ctr->pairs, 1ull);
+                  if (slot < A.pair_cap)
+                    A.pairs[slot] = make_uint2(uint32_t(i), uint32_t(gi) | (v < 0 ? 0x80000000u : 0u));
+                  else
+                    atomicOr(&A.ctr->overflow, kOvPairs);
+                  continue;
+                }
+                if (v < 0) {
+                  ++n64;
+                  v = capture_exact(A.nodes_cold, uint32_t(i), c64, P.tan_beta);
+                }
+                if (!v) continue;
+                // RayCapture deletes a captured node's subtree, so an ancestor
+                // capturing the same receiver suppresses this one.
+                auto suppressed = [&]() {
+                  if (kStage) {
+                    for (int q = 0; q < na; ++q) {
+                      const AncRec& r = anc[warp][q];
+                      ++anc_tests;
+                      int w = reception32(make_float3(r.s[0], r.s[1], r.s[2]),
+                                          make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, c, tanb);
+                      if (w < 0) {
+                        ++n64;
+                        w = capture_exact(A.nodes_cold, r.idx, c64, P.tan_beta);
+                      }
+                      if (w) return true;
+                    }
+                    return false;
+                  }
+                  for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
+                    const NodeHot a = A.nodes[p];
                     ++anc_tests;
-                    int w = reception32(make_float3(r.s[0], r.s[1], r.s[2]),
-                                        make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, c, tanb);
+                    int w = reception32(make_float3(a.s[0], a.s[1], a.s[2]),
+                                        make_float3(a.u[0], a.u[1], a.u[2]), a.len, a.S, c, tanb);
                     if (w < 0) {
                       ++n64;
-                      w = capture_exact(A.nodes_cold, r.idx, c64, P.tan_beta);
+                      w = capture_exact(A.nodes_cold, p, c64, P.tan_beta);
                     }
                     if (w) return true;
+                    p = a.parent;
                   }
                   return false;
+                };
+                if (kStage) {
+                  if (suppressed()) continue;
+                  ++events;
                 }
-                for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
-                  const NodeHot a = A.nodes[p];
-                  ++anc_tests;
-                  int w = reception32(make_float3(a.s[0], a.s[1], a.s[2]),
-                                      make_float3(a.u[0], a.u[1], a.u[2]), a.len, a.S, c, tanb);
-                  if (w < 0) {
-                    ++n64;
-                    w = capture_exact(A.nodes_cold, p, c64, P.tan_beta);
-                  }
-                  if (w) return true;
-                  p = a.parent;
-                }
-                return false;
-              };
-              if (kStage) {
-                if (suppressed()) continue;
-                ++events;
+                const bool ok = is_root_class(nd.cls)
+                                    ? A.direct_ok[gi] != 0
+                                    : correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
+                if (!ok) continue;
+                if (!kStage && suppressed()) continue;
+                const unsigned long long kk = atomicAdd(&A.ctr->corrected, 1ull);
+                if (kk < A.corr_cap)
+                  A.corr_list[kk] = Corrected{uint32_t(gi), nd.cls,
+                                              (unsigned long long)nd.launch << kHeapBits | nd.heap};
+                else
+                  atomicOr(&A.ctr->overflow, kOvCorr);
               }
-              const bool ok = is_root_class(nd.cls)
-                                  ? A.direct_ok[gi] != 0
-                                  : correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
-              if (!ok) continue;
-              if (!kStage && suppressed()) continue;
-              const unsigned long long kk = atomicAdd(&A.ctr->corrected, 1ull);
-              if (kk < A.corr_cap)
-                A.corr_list[kk] = Corrected{uint32_t(gi), nd.cls,
-                                            (unsigned long long)nd.launch << kHeapBits | nd.heap};
-              else
-                atomicOr(&A.ctr->overflow, kOvCorr);
             }
           }
         }
       }
+      __syncwarp();
     }
-    __syncwarp();
+    __syncwarp();  // the next batch overwrites the staged records
   }
   for (int o = 16; o; o >>= 1) {
     events += __shfl_xor_sync(FULL, events, o);
