@@ -352,6 +352,7 @@ struct TraceArgs {
   long long lo, hi;    // this launch covers rays [lo, hi) of the depth
   const uint2* cand;   // contenders of those rays (k_find)
   const unsigned char* ncand;
+  Hit* hits;           // their closest hits (k_resolve), INT_MAX rank = none
 };
 
 __device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long long g) {
@@ -612,9 +613,43 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
   }
 }
 
+// FP64 resolution of each ray's contenders (resolve_hit): the closest hit
+// the reference finds, stored per ray of the chunk for k_trace.  A separate
+// kernel so the FP64 work runs at higher occupancy than the spawning.
+__global__ void __launch_bounds__(128, 5) k_resolve(TraceArgs A) {
+  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
+  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
+  const long long n_in = min(n_all, A.hi);
+  TraceStats st{0, 0};
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = A.lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in;
+       i += stride) {
+    double o[3], d[3];
+    if (A.depth == 0) {
+      int q;
+      long long li;
+      root_ray(A.txp, A.n_tx, A.dirs, i, o, d, q, li);
+    } else {
+      const RayRec& r = A.in[i];
+      for (int a = 0; a < 3; ++a) {
+        o[a] = r.o[a];
+        d[a] = r.d[a];
+      }
+    }
+    const long long c = i - A.lo;
+    Hit h;
+    if (!resolve_hit(A.sc, o, d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
+                     &A.ctr->overflow))
+      h.rank = INT_MAX;
+    A.hits[c] = h;
+  }
+  if (st.fp64_tri) atomicAdd(&A.ctr->fp64_tri, (unsigned long long)st.fp64_tri);
+  if (st.fallback) atomicAdd(&A.ctr->fallback, (unsigned long long)st.fallback);
+}
+
 // Resident blocks of k_trace per SM (register budget 65536 / (128 x this)).
 #ifndef SBR_TRACE_BLOCKS
-#define SBR_TRACE_BLOCKS 4
+#define SBR_TRACE_BLOCKS 6
 #endif
 __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
@@ -642,10 +677,8 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
       r = A.in[i];
     }
     const TxParams& P = A.txp[r.tx];
-    Hit h;
-    const long long c = i - A.lo;
-    const bool hit = resolve_hit(A.sc, r.o, r.d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
-                                 &A.ctr->overflow);
+    const Hit h = A.hits[i - A.lo];
+    const bool hit = h.rank != INT_MAX;
     const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
     {  // per-request segment count, one atomic per request present in the warp
       const unsigned peers = __match_any_sync(__activemask(), r.tx);
@@ -960,6 +993,49 @@ __device__ __forceinline__ NodeSpan node_span(const NodeHot& nd, const TxParams&
   return sp;
 }
 
+// Chunk ch of a node's span: its parameter range [a, b], the radius rb
+// around it that can hold a capture, the reception test's error margin mr,
+// and the receiver-grid cell box around it (nrows = 0: nothing to test,
+// including a box wholly outside the correction cone).
+struct ChunkBox {
+  float a, b, rb, mr;
+  int c0[3], c1[3];
+  int nrows;
+};
+
+__device__ __forceinline__ ChunkBox chunk_box(const NodeHot& nd, const RxGrid& g,
+                                              const NodeSpan& sp, int ch, float cmax, float tanb,
+                                              bool use_cone, const float* cone) {
+  ChunkBox cb;
+  const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
+  const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
+  const float S = nd.S;
+  cb.a = sp.lo + ch * sp.step;
+  cb.b = (ch == sp.nchunk - 1) ? sp.hi : sp.lo + (ch + 1) * sp.step;
+  const float pa[3] = {s.x + cb.a * u.x, s.y + cb.a * u.y, s.z + cb.a * u.z};
+  const float pb[3] = {s.x + cb.b * u.x, s.y + cb.b * u.y, s.z + cb.b * u.z};
+  const float npmax = fmaxf(sqrt_up(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]),
+                            sqrt_up(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]));
+  cb.mr = kFiltK * (sp.ns + cmax + S + npmax + 1.0f);
+  // |P| is convex along the chunk: the larger end bounds it
+  cb.rb = (S + npmax) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f + cb.mr;
+  for (int k = 0; k < 3; ++k) {
+    cb.c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - cb.rb - g.org[k]) * g.inv_cell)));
+    cb.c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + cb.rb - g.org[k]) * g.inv_cell)));
+  }
+  const int ny = cb.c1[1] - cb.c0[1] + 1, nz = cb.c1[2] - cb.c0[2] + 1;
+  cb.nrows = (cb.c0[0] <= cb.c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
+  if (use_cone && cb.nrows) {  // the chunk's cells all outside the cone: skip it
+    float blo[3], bhi[3];
+    for (int k = 0; k < 3; ++k) {
+      blo[k] = g.org[k] + cb.c0[k] * g.cell;
+      bhi[k] = g.org[k] + (cb.c1[k] + 1) * g.cell;
+    }
+    if (!cone_meets_box(cone, blo, bhi)) cb.nrows = 0;
+  }
+  return cb;
+}
+
 // kStage: stage counts requested (every capture counted, the plain order of
 // tests); otherwise the fast path with the correction prefilter and the
 // deferred FP64 pass.
@@ -981,6 +1057,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
   __shared__ float s_fl[kCapWarps][32][12];  // image source + correction filter terms
   __shared__ float s_cn[kCapWarps][32][16];  // loosened correction cone
   __shared__ NodeSpan s_sp[kCapWarps][32];   // clipped span and chunking
+  __shared__ ChunkBox s_ck[kCapWarps][32];   // the span's first chunk
   for (unsigned long long base = ((unsigned long long)blockIdx.x * kCapWarps + warp) * 32;
        base < n_nodes; base += nw * 32) {
     {
@@ -1009,7 +1086,11 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
             cn[12 + k] = c.inv_nx[k];
           }
         }
-        s_sp[warp][lane] = node_span(h, A.txp[h.tx], A.grids[h.tx], cmax, cone_ok);
+        const NodeSpan sp = node_span(h, A.txp[h.tx], A.grids[h.tx], cmax, cone_ok);
+        s_sp[warp][lane] = sp;
+        if (sp.nchunk > 0)
+          s_ck[warp][lane] = chunk_box(h, A.grids[h.tx], sp, 0, cmax, float(A.txp[h.tx].tan_beta),
+                                       cone_ok != 0, s_cn[warp][lane]);
       }
       __syncwarp();
     }
@@ -1071,29 +1152,13 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
         const float ml = kFiltK * (ns + cmax + 1.0f);
         {
           for (int ch = 0; ch < nchunk; ++ch) {
-            const float a = lo + ch * step, b = (ch == nchunk - 1) ? hi : lo + (ch + 1) * step;
-            const float pa[3] = {s.x + a * u.x, s.y + a * u.y, s.z + a * u.z};
-            const float pb[3] = {s.x + b * u.x, s.y + b * u.y, s.z + b * u.z};
-            const float npmax = fmaxf(sqrt_up(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]),
-                                      sqrt_up(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]));
-            const float mr = kFiltK * (ns + cmax + S + npmax + 1.0f);
-            // |P| is convex along the chunk: the larger end bounds it
-            const float rb = (S + npmax) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f + mr;
-            int c0[3], c1[3];
-            for (int k = 0; k < 3; ++k) {
-              c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - rb - g.org[k]) * inv_cell)));
-              c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + rb - g.org[k]) * inv_cell)));
-            }
-            const int ny = c1[1] - c0[1] + 1, nz = c1[2] - c0[2] + 1;
-            int nrows = (c0[0] <= c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
-            if (use_cone && nrows) {  // the chunk's cells all outside the cone: skip it
-              float blo[3], bhi[3];
-              for (int k = 0; k < 3; ++k) {
-                blo[k] = g.org[k] + c0[k] * g.cell;
-                bhi[k] = g.org[k] + (c1[k] + 1) * g.cell;
-              }
-              if (!cone_meets_box(cone_w, blo, bhi)) nrows = 0;
-            }
+            const ChunkBox cb = ch == 0 ? s_ck[warp][jj]
+                                        : chunk_box(nd, g, sp, ch, cmax, tanb, use_cone, cone_w);
+            const float a = cb.a, b = cb.b, rb = cb.rb, mr = cb.mr;
+            const int c0[3] = {cb.c0[0], cb.c0[1], cb.c0[2]};
+            const int c1[3] = {cb.c1[0], cb.c1[1], cb.c1[2]};
+            const int ny = c1[1] - c0[1] + 1;
+            const int nrows = cb.nrows;
             for (int rbase = 0; rbase < nrows; rbase += 32) {
               // this lane's row: the part of the chunk within rb of its y/z band
               int beg = 0, cnt = 0;
@@ -1648,6 +1713,7 @@ struct Workspace {
   DBuf<Counters> ctr;
   DBuf<unsigned long long> seg_tx;
   DBuf<uint2> cand;                    // FP32 search contenders, kCand per ray of a chunk
+  DBuf<Hit> hits;                      // closest hit per ray of a chunk
   DBuf<unsigned char> ncand;
   DBuf<unsigned long long> find_work;  // work counter of the running search launch
   // capacities (grown from occupancy and on overflow)
@@ -2206,6 +2272,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     const long long chunk = std::max<long long>(1, std::min(kTraceChunk, max_width));
     W.cand.ensure(size_t(chunk) * kCand);
     W.ncand.ensure(size_t(chunk));
+    W.hits.ensure(size_t(chunk));
     W.find_work.ensure(1);
     FindArgs fnd;
     fnd.sc = S.dev;
@@ -2220,6 +2287,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fnd.ncand = W.ncand.p;
     ta.cand = W.cand.p;
     ta.ncand = W.ncand.p;
+    ta.hits = W.hits.p;
     for (int d = 0; d <= max_depth; ++d) {
       ta.depth = fnd.depth = d;
       ta.in = fnd.in = (d % 2 == 0) ? W.q1.p : W.q0.p;
@@ -2230,6 +2298,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         ta.hi = fnd.hi = std::min(bound, lo + chunk);
         CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
         ++nl, k_find<<<find_grid(), 128, 0, st>>>(fnd);
+        ++nl, k_resolve<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
         ++nl, k_trace<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
       }
     }
