@@ -352,7 +352,6 @@ struct TraceArgs {
   long long lo, hi;    // this launch covers rays [lo, hi) of the depth
   const uint2* cand;   // contenders of those rays (k_find)
   const unsigned char* ncand;
-  Hit* hits;           // their closest hits (k_resolve), INT_MAX rank = none
 };
 
 __device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long long g) {
@@ -613,43 +612,9 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
   }
 }
 
-// FP64 resolution of each ray's contenders (resolve_hit): the closest hit
-// the reference finds, stored per ray of the chunk for k_trace.  A separate
-// kernel so the FP64 work runs at higher occupancy than the spawning.
-__global__ void __launch_bounds__(128, 5) k_resolve(TraceArgs A) {
-  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
-  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
-  const long long n_in = min(n_all, A.hi);
-  TraceStats st{0, 0};
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = A.lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in;
-       i += stride) {
-    double o[3], d[3];
-    if (A.depth == 0) {
-      int q;
-      long long li;
-      root_ray(A.txp, A.n_tx, A.dirs, i, o, d, q, li);
-    } else {
-      const RayRec& r = A.in[i];
-      for (int a = 0; a < 3; ++a) {
-        o[a] = r.o[a];
-        d[a] = r.d[a];
-      }
-    }
-    const long long c = i - A.lo;
-    Hit h;
-    if (!resolve_hit(A.sc, o, d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
-                     &A.ctr->overflow))
-      h.rank = INT_MAX;
-    A.hits[c] = h;
-  }
-  if (st.fp64_tri) atomicAdd(&A.ctr->fp64_tri, (unsigned long long)st.fp64_tri);
-  if (st.fallback) atomicAdd(&A.ctr->fallback, (unsigned long long)st.fallback);
-}
-
 // Resident blocks of k_trace per SM (register budget 65536 / (128 x this)).
 #ifndef SBR_TRACE_BLOCKS
-#define SBR_TRACE_BLOCKS 6
+#define SBR_TRACE_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
@@ -677,8 +642,10 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
       r = A.in[i];
     }
     const TxParams& P = A.txp[r.tx];
-    const Hit h = A.hits[i - A.lo];
-    const bool hit = h.rank != INT_MAX;
+    Hit h;
+    const long long c = i - A.lo;
+    const bool hit = resolve_hit(A.sc, r.o, r.d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
+                                 &A.ctr->overflow);
     const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
     {  // per-request segment count, one atomic per request present in the warp
       const unsigned peers = __match_any_sync(__activemask(), r.tx);
@@ -1713,7 +1680,6 @@ struct Workspace {
   DBuf<Counters> ctr;
   DBuf<unsigned long long> seg_tx;
   DBuf<uint2> cand;                    // FP32 search contenders, kCand per ray of a chunk
-  DBuf<Hit> hits;                      // closest hit per ray of a chunk
   DBuf<unsigned char> ncand;
   DBuf<unsigned long long> find_work;  // work counter of the running search launch
   // capacities (grown from occupancy and on overflow)
@@ -2272,7 +2238,6 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     const long long chunk = std::max<long long>(1, std::min(kTraceChunk, max_width));
     W.cand.ensure(size_t(chunk) * kCand);
     W.ncand.ensure(size_t(chunk));
-    W.hits.ensure(size_t(chunk));
     W.find_work.ensure(1);
     FindArgs fnd;
     fnd.sc = S.dev;
@@ -2287,7 +2252,6 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fnd.ncand = W.ncand.p;
     ta.cand = W.cand.p;
     ta.ncand = W.ncand.p;
-    ta.hits = W.hits.p;
     for (int d = 0; d <= max_depth; ++d) {
       ta.depth = fnd.depth = d;
       ta.in = fnd.in = (d % 2 == 0) ? W.q1.p : W.q0.p;
@@ -2298,7 +2262,6 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         ta.hi = fnd.hi = std::min(bound, lo + chunk);
         CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
         ++nl, k_find<<<find_grid(), 128, 0, st>>>(fnd);
-        ++nl, k_resolve<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
         ++nl, k_trace<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
       }
     }
