@@ -327,6 +327,21 @@ def run_precision(level: int = 10, n_rx: int = 50000):
             "tolerance": {"rel_mag": 1e-4, "phase_rad": 1e-3}}
 
 
+def replica_totals(dist, world: int, segments: float, seconds: float, e2e_segments: float,
+                   e2e_seconds: float):
+    """Whole-job totals of independent replicas: segments summed over ranks,
+    time = the slowest rank's (device and end to end).  dist is
+    torch.distributed (any backend) or None for one process."""
+    if not dist:
+        return segments, seconds, e2e_segments, e2e_seconds
+    import torch
+    t = torch.tensor([segments, seconds, e2e_segments, e2e_seconds], dtype=torch.float64)
+    g = [torch.zeros_like(t) for _ in range(world)]
+    dist.all_gather(g, t)
+    return (sum(x[0].item() for x in g), max(x[1].item() for x in g),
+            sum(x[2].item() for x in g), max(x[3].item() for x in g))
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -446,15 +461,8 @@ def main():
     t_e2e = time.perf_counter() - t0
     h2d = 8 * 3 * len(wl.request.rx) + 160
     # ---- aggregate over ranks (replicas)
-    tot_seg, max_t, max_e2e, tot_e2e = sum(seg), t_dev, t_e2e, e2e_seg
-    if dist:
-        t = torch.tensor([float(sum(seg)), t_dev, t_e2e, float(e2e_seg)], dtype=torch.float64)
-        g = [torch.zeros_like(t) for _ in range(world)]
-        dist.all_gather(g, t)
-        tot_seg = sum(x[0].item() for x in g)
-        max_t = max(x[1].item() for x in g)
-        max_e2e = max(x[2].item() for x in g)
-        tot_e2e = sum(x[3].item() for x in g)
+    tot_seg, max_t, tot_e2e, max_e2e = replica_totals(dist, world, float(sum(seg)), t_dev,
+                                                      float(e2e_seg), t_e2e)
     if rank == 0:
         peak, peak_kind = peaks()
         steps = args.steps
