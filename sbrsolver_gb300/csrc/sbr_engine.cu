@@ -1131,7 +1131,10 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
               int beg = 0, cnt = 0;
               const int ridx = rbase + lane;
               if (ridx < nrows) {
-                const int iy = c0[1] + ridx % ny, iz = c0[2] + ridx / ny;
+                // one layer of cells (receivers on a plane) needs no division
+                const bool flat = c1[2] == c0[2];
+                const int iy = c0[1] + (flat ? ridx : ridx % ny);
+                const int iz = c0[2] + (flat ? 0 : ridx / ny);
                 const float y0 = g.org[1] + iy * g.cell - rb, y1 = g.org[1] + (iy + 1) * g.cell + rb;
                 const float z0 = g.org[2] + iz * g.cell - rb, z1 = g.org[2] + (iz + 1) * g.cell + rb;
                 float la = a, lb = b;
@@ -1225,7 +1228,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
                   // image correction, ancestor suppression) runs densely in
                   // k_capture_finish
                   if (v == 0) continue;
-                  const unsigned long long slot = atomicAdd(&A.ctr->pairs, 1ull);
+                  const unsigned long long slot = warp_reserve(&A.ctr->pairs, 1);
                   if (slot < A.pair_cap)
                     A.pairs[slot] = make_uint2(uint32_t(i), uint32_t(gi) | (v < 0 ? 0x80000000u : 0u));
                   else
