@@ -57,7 +57,9 @@ typedef struct sbr_material {
 
 /* Antenna patterns of FieldCompute::GetAnalyticEfieldPattern
  * (FieldCompute.cpp:153-183); the reference always uses SBR_ANTENNA_HERTZIAN. */
-enum { SBR_ANTENNA_ISOTROPIC = 0, SBR_ANTENNA_HERTZIAN = 1, SBR_ANTENNA_HALF_WAVE = 2 };
+enum { SBR_ANTENNA_ISOTROPIC = 0, SBR_ANTENNA_HERTZIAN = 1, SBR_ANTENNA_HALF_WAVE = 2,
+       SBR_ANTENNA_TABULATED = 3 /* sbr_request.pattern: see sbr_pattern_create */ };
+typedef struct sbr_pattern sbr_pattern;
 
 /* Field precision: FP64 everywhere, or FP32 Fresnel/rotation arithmetic
  * with FP64 path length and phase and a compensated FP32 per-receiver sum.
@@ -92,6 +94,7 @@ typedef struct sbr_request {
                               costs time, results are identical either way */
   int field_check;         /* FP32 field precisions: also compute the FP64 field on the
                               GPU so sbr_result_field_error can state the error */
+  const sbr_pattern* pattern; /* antenna SBR_ANTENNA_TABULATED; must outlive the solve */
 } sbr_request;
 
 typedef struct sbr_counts {
@@ -232,6 +235,26 @@ sbr_status sbr_server_poll(sbr_server* server, sbr_completion* out, int max, int
 sbr_status sbr_server_pending(sbr_server* server, int* queued, long long* in_flight_bytes);
 /* Finishes queued and running requests, then stops. */
 sbr_status sbr_server_destroy(sbr_server* server);
+
+/* ---- tabulated antenna patterns -------------------------------------- */
+/* The reference ships data/TXPattern.dat and reads it with
+ * Preprocessor::ReadPatternFile (Preprocessor.cpp:3-35) into a GainMap, but
+ * never applies it.  Antenna SBR_ANTENNA_TABULATED applies such a table to
+ * the launch direction (theta, phi in the txCoordSys frame, as the analytic
+ * patterns): E_theta = sqrt(60 Pt) 10^(g_theta/20) e^(j arg_theta), E_phi
+ * likewise, gains in dB, phases in degrees, bilinear on the grid.
+ * gain_phase: 4 floats per grid point (g_theta, arg_theta, g_phi, arg_phi),
+ * theta-major, theta = i * d_theta (i < n_theta, at most 180 degrees), phi =
+ * j * d_phi with n_phi * d_phi = 360.  The table is copied to the current
+ * device. */
+sbr_status sbr_pattern_create(int n_theta, int n_phi, double d_theta, double d_phi,
+                              const float* gain_phase, sbr_pattern** out);
+/* TXPattern.dat: lines of six numbers (theta phi g_theta arg_theta g_phi
+ * arg_phi) on a regular grid from (0, 0); other lines are skipped. */
+sbr_status sbr_pattern_read(const char* path, sbr_pattern** out);
+sbr_status sbr_pattern_info(const sbr_pattern* pattern, int* n_theta, int* n_phi,
+                            double* d_theta, double* d_phi);
+sbr_status sbr_pattern_destroy(sbr_pattern* pattern);
 
 /* ---- receiver layouts ---------------------------------------------- */
 /* Preprocessor::GenerateRXLine (Preprocessor.cpp:270-284): floor(|end-start|

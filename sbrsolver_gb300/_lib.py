@@ -24,7 +24,8 @@ EXPORTS = (
     "sbr_server_pending", "sbr_server_destroy", "sbr_result_field_error", "sbr_result_field_fp64",
     "sbr_write_field_csv", "sbr_write_receivers_vtk", "sbr_write_paths_vtk",
     "sbr_write_launch_rays_vtk", "sbr_scene_set_materials", "sbr_stl_read",
-    "sbr_generate_rx_line", "sbr_generate_rx_plane",
+    "sbr_generate_rx_line", "sbr_generate_rx_plane", "sbr_pattern_create", "sbr_pattern_read",
+    "sbr_pattern_info", "sbr_pattern_destroy",
 )
 
 
@@ -51,7 +52,7 @@ class Request(C.Structure):
                 ("frequency", C.c_double), ("pt", C.c_double), ("use_fresnel", C.c_int),
                 ("tessellation", C.c_int), ("antenna", C.c_int), ("field_precision", C.c_int),
                 ("n_rx", C.c_int), ("rx", C.POINTER(C.c_double)), ("rx_on_device", C.c_int),
-                ("stage_counts", C.c_int), ("field_check", C.c_int)]
+                ("stage_counts", C.c_int), ("field_check", C.c_int), ("pattern", C.c_void_p)]
 
 
 class FieldError(C.Structure):
@@ -132,6 +133,10 @@ def load(path: str = LIB_PATH):
             "sbr_stl_read": [C.c_char_p, P(I), P(C.c_float), P(C.c_float)],
             "sbr_generate_rx_line": [P(D), P(D), D, P(D), I, P(I)],
             "sbr_generate_rx_plane": [D, D, D, D, D, D, P(D), I, P(I)],
+            "sbr_pattern_create": [I, I, D, D, P(C.c_float), P(vp)],
+            "sbr_pattern_read": [C.c_char_p, P(vp)],
+            "sbr_pattern_info": [vp, P(I), P(I), P(D), P(D)],
+            "sbr_pattern_destroy": [vp],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

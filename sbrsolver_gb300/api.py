@@ -45,6 +45,7 @@ class GlobalConfig:
 
     antennaType: int = 1
     fieldPrecision: str = "fp64"
+    pattern: Optional["AntennaPattern"] = None  # antennaType 3 (tabulated)
 
 
 @dataclass
@@ -104,6 +105,26 @@ class Preprocessor:
         _lib.check(lib.sbr_generate_rx_line(_dp(s), _dp(e), float(resolution), _dp(out), n.value,
                                             C.byref(n)))
         output.extend(map(tuple, out.reshape(-1, 3).tolist()))
+
+    @staticmethod
+    def ReadPatternFile(fileName: str, output: dict) -> bool:
+        """Preprocessor::ReadPatternFile (Preprocessor.cpp:3-35): every line of
+        six numbers becomes output[(theta, phi)] = (g_theta, arg_theta, g_phi,
+        arg_phi) as float32 values; other lines are skipped."""
+        try:
+            with open(fileName) as fh:
+                for line in fh:
+                    t = line.split()
+                    if len(t) != 6:
+                        continue
+                    try:
+                        v = [float(np.float32(x)) for x in t]
+                    except ValueError:
+                        continue
+                    output[(v[0], v[1])] = tuple(v[2:])
+            return True
+        except OSError:
+            return False
 
     @staticmethod
     def ReadLocationFile(fileName: str, output: list) -> bool:
@@ -202,7 +223,7 @@ class Result:
 def make_request(tx, tx_coord_sys, max_reflection, max_transmission, frequency, pt, use_fresnel,
                  rx: np.ndarray, tessellation: int, antenna: int = 1,
                  precision: str = "fp64", stage_counts: bool = False,
-                 field_check: bool = False) -> tuple:
+                 field_check: bool = False, pattern: Optional[AntennaPattern] = None) -> tuple:
     rx = np.ascontiguousarray(rx, np.float64).reshape(-1, 3)
     q = _lib.Request()
     for i in range(3):
@@ -223,7 +244,8 @@ def make_request(tx, tx_coord_sys, max_reflection, max_transmission, frequency, 
     q.rx_on_device = 0
     q.stage_counts = 1 if stage_counts else 0
     q.field_check = 1 if field_check else 0
-    return q, rx  # keep rx alive with the request
+    q.pattern = pattern.handle.value if pattern is not None else None
+    return (q, rx, pattern) if pattern is not None else (q, rx)  # keep rx alive with the request
 
 
 def request_from_workload(req: WorkRequest, precision: str = "fp64",
@@ -239,8 +261,8 @@ def solve(scene: DeviceScene, requests, with_paths=True) -> Result:
     arrays: per-path request/receiver/launch/heap/ray_offset/n_rays and
     per-ray tri/cop/kind/points)."""
     lib = _lib.load()
-    if isinstance(requests, tuple) and len(requests) == 2 and isinstance(requests[0], _lib.Request):
-        requests = [requests]  # one (request, receiver array) pair
+    if isinstance(requests, tuple) and isinstance(requests[0], _lib.Request):
+        requests = [requests]  # one (request, receiver array[, pattern]) tuple
     arr = (_lib.Request * len(requests))(*[r[0] for r in requests])
     h = C.c_void_p()
     _lib.check(lib.sbr_solve_batch(scene.handle, arr, len(requests), C.byref(h)))
@@ -387,6 +409,63 @@ class Server:
             pass
 
 
+class AntennaPattern:
+    """Tabulated antenna pattern (sbr_pattern_*): the TXPattern.dat grid the
+    reference reads with Preprocessor::ReadPatternFile, applied by antenna
+    type 3 as E_theta, E_phi = sqrt(60 Pt) 10^(g/20) e^(j arg) (g in dB, arg
+    in degrees, bilinear on the grid).  The table lives on the current GPU."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    @classmethod
+    def read(cls, path: str) -> "AntennaPattern":
+        h = C.c_void_p()
+        _lib.check(_lib.load().sbr_pattern_read(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_table(cls, gain_phase: np.ndarray, d_theta: float, d_phi: float) -> "AntennaPattern":
+        """gain_phase: (n_theta, n_phi, 4) of g_theta, arg_theta, g_phi, arg_phi."""
+        t = np.ascontiguousarray(gain_phase, np.float32)
+        h = C.c_void_p()
+        _lib.check(_lib.load().sbr_pattern_create(t.shape[0], t.shape[1], float(d_theta),
+                                                  float(d_phi),
+                                                  t.ctypes.data_as(C.POINTER(C.c_float)),
+                                                  C.byref(h)))
+        return cls(h)
+
+    def info(self) -> tuple:
+        nt, npp, dt, dp = C.c_int(), C.c_int(), C.c_double(), C.c_double()
+        _lib.check(_lib.load().sbr_pattern_info(self.handle, C.byref(nt), C.byref(npp),
+                                                C.byref(dt), C.byref(dp)))
+        return nt.value, npp.value, dt.value, dp.value
+
+    def close(self) -> None:
+        if self.handle:
+            _lib.load().sbr_pattern_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def write_pattern_file(path: str, gain_phase: np.ndarray, d_theta: float, d_phi: float) -> None:
+    """Writes a table in the TXPattern.dat layout (data/TXPattern.dat: a title
+    line, the grid line, then theta phi g_theta arg_theta g_phi arg_phi)."""
+    t = np.asarray(gain_phase, np.float64)
+    with open(path, "w") as fh:
+        fh.write("Transmitter (theta, phi, g_theta, arg_theta, g_phi, arg_phi)\n")
+        fh.write(f"{t.shape[0]} {t.shape[1]} {d_theta:g} {d_phi:g}\n")
+        for i in range(t.shape[0]):
+            for j in range(t.shape[1]):
+                g = t[i, j]
+                fh.write(f"{i * d_theta:g} {j * d_phi:g} {g[0]:.6g} {g[1]:.6g} {g[2]:.6g} {g[3]:.6g}\n")
+
+
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
@@ -449,7 +528,8 @@ class RTSolver:
         rx = np.asarray(receivers, np.float64).reshape(-1, 3)
         req = make_request(sourcePoint, txCoordSys, maxReflectionCount, maxTransmissionCount,
                            frequency, pt, useFresnelCoeff, rx, txTesslation,
-                           self.config.antennaType, self.config.fieldPrecision)
+                           self.config.antennaType, self.config.fieldPrecision,
+                           pattern=self.config.pattern)
         self._result = solve(self._scene, req, with_paths="arrays")
         self._receivers = rx
         return int(self._result.counts["launches"]) * int(rx.shape[0])

@@ -60,6 +60,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
          "-o", os.path.join(obj_dir, "sbr_server.o")],
         [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, "sbr_io.cpp"),
          "-o", os.path.join(obj_dir, "sbr_io.o")],
+        [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, "sbr_pattern.cpp"),
+         "-o", os.path.join(obj_dir, "sbr_pattern.o")],
     ]
     with ThreadPoolExecutor(len(jobs)) as ex:
         outs = list(ex.map(run, jobs))
@@ -68,7 +70,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + ".tmp"
     run([nvcc, *ARCH, "-shared", "-o", tmp, os.path.join(obj_dir, "sbr_engine.o"),
          os.path.join(obj_dir, "sbr_host.o"), os.path.join(obj_dir, "sbr_noalloc.o"),
-         os.path.join(obj_dir, "sbr_server.o"), os.path.join(obj_dir, "sbr_io.o")])
+         os.path.join(obj_dir, "sbr_server.o"), os.path.join(obj_dir, "sbr_io.o"),
+         os.path.join(obj_dir, "sbr_pattern.o")])
     os.replace(tmp, LIB)
     return LIB
 

@@ -840,6 +840,11 @@ constexpr int kCapWarps = 4;
 #define SBR_CAP_CHUNK_CELLS 16
 #endif
 constexpr float kCapChunkCells = SBR_CAP_CHUNK_CELLS;
+// Nodes staged per warp at a time (at most 32: one per lane).
+#ifndef SBR_CAP_BATCH
+#define SBR_CAP_BATCH 32
+#endif
+constexpr int kCapBatch = SBR_CAP_BATCH;
 
 // Upper bound on sqrt(x) from the hardware reciprocal square root (relative
 // error below 2^-21), for the capture stage's conservative ranges and
@@ -1019,17 +1024,18 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
   // Nodes are taken 32 at a time: each lane loads one node's record, its
   // class record and last triangle, so the three dependent loads are paid
   // once per 32 nodes; the warp then works through the 32 from shared memory.
-  __shared__ NodeHot s_nh[kCapWarps][32];
-  __shared__ Tri32 s_tl[kCapWarps][32];      // the class's last triangle
-  __shared__ float s_fl[kCapWarps][32][12];  // image source + correction filter terms
-  __shared__ float s_cn[kCapWarps][32][16];  // loosened correction cone
-  __shared__ NodeSpan s_sp[kCapWarps][32];   // clipped span and chunking
-  __shared__ ChunkBox s_ck[kCapWarps][32];   // the span's first chunk
-  for (unsigned long long base = ((unsigned long long)blockIdx.x * kCapWarps + warp) * 32;
-       base < n_nodes; base += nw * 32) {
+  constexpr int B = kCapBatch;
+  __shared__ NodeHot s_nh[kCapWarps][B];
+  __shared__ Tri32 s_tl[kCapWarps][B];      // the class's last triangle
+  __shared__ float s_fl[kCapWarps][B][12];  // image source + correction filter terms
+  __shared__ float s_cn[kCapWarps][B][16];  // loosened correction cone
+  __shared__ NodeSpan s_sp[kCapWarps][B];   // clipped span and chunking
+  __shared__ ChunkBox s_ck[kCapWarps][B];   // the span's first chunk
+  for (unsigned long long base = ((unsigned long long)blockIdx.x * kCapWarps + warp) * B;
+       base < n_nodes; base += nw * B) {
     {
       const unsigned long long my = base + lane;
-      if (my < n_nodes) {
+      if (lane < B && my < n_nodes) {
         const NodeHot h = A.nodes[my];
         s_nh[warp][lane] = h;
         const float cmax = A.gb[h.tx].cmax;
@@ -1061,7 +1067,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
       }
       __syncwarp();
     }
-    const int n_here = int(min(32ull, n_nodes - base));
+    const int n_here = int(min((unsigned long long)B, n_nodes - base));
     for (int jj = 0; jj < n_here; ++jj) {
       const unsigned long long i = base + jj;
       const NodeHot nd = s_nh[warp][jj];
@@ -1560,16 +1566,17 @@ __global__ void k_field(FieldArgs A) {
       if (r + 1 < pb.n) mat[r + 1] = A.sc.tri64[pb.tri[r]].mat;
     }
     Cx<double> e[3];
+    const PatternTab pat{P.pat, P.pat_nt, P.pat_np, P.pat_dt, P.pat_dp};
     const int prec = A.precision < 0 ? P.precision : A.precision;
     if (prec == 2)
       path_field<float, true>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq,
-                              P.pt, P.antenna, P.fresnel != 0, A.K, e);
+                              P.pt, P.antenna, P.fresnel != 0, A.K, e, &pat);
     else if (prec == 1)
       path_field<float>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
-                        P.antenna, P.fresnel != 0, A.K, e);
+                        P.antenna, P.fresnel != 0, A.K, e, &pat);
     else
       path_field<double>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
-                         P.antenna, P.fresnel != 0, A.K, e);
+                         P.antenna, P.fresnel != 0, A.K, e, &pat);
     for (int j = 0; j < 3; ++j) {
       A.path_field[6 * i + 2 * j] = e[j].re;
       A.path_field[6 * i + 2 * j + 1] = e[j].im;
@@ -1761,6 +1768,17 @@ struct sbr_result {
 };
 
 namespace sbr {
+
+void pattern_fields(const sbr_pattern* p, const float** dev, int* nt, int* np, double* dt,
+                    double* dp, int* device);  // sbr_pattern.cpp
+
+static void pattern_params(const sbr_pattern* p, int scene_device, TxParams& P) {
+  const float* dev = nullptr;
+  int device = -1;
+  pattern_fields(p, &dev, &P.pat_nt, &P.pat_np, &P.pat_dt, &P.pat_dp, &device);
+  if (device != scene_device) throw std::string("the pattern was created on another device");
+  P.pat = reinterpret_cast<const float4*>(dev);
+}
 
 static void upload_scene(SceneImpl& S) {
   const HostScene& H = S.host;
@@ -2064,7 +2082,9 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       throw std::string("max_reflection + max_transmission must be 0..16");
     if (q.tessellation < 0 || q.tessellation > 12) throw std::string("tessellation must be 0..12");
     if (!(q.frequency > 0)) throw std::string("frequency must be > 0");
-    if (q.antenna < 0 || q.antenna > 2) throw std::string("antenna must be 0, 1 or 2");
+    if (q.antenna < 0 || q.antenna > 3) throw std::string("antenna must be 0, 1, 2 or 3");
+    if (q.antenna == SBR_ANTENNA_TABULATED && !q.pattern)
+      throw std::string("antenna 3 (tabulated) needs a pattern");
     ensure_dirs(S, q.tessellation);
     TxParams& P = tp[r];
     std::memset(&P, 0, sizeof P);
@@ -2078,6 +2098,10 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     P.R = q.max_reflection;
     P.T = q.max_transmission;
     P.antenna = q.antenna;
+    P.pat = nullptr;
+    P.pat_nt = P.pat_np = 0;
+    P.pat_dt = P.pat_dp = 1.0;
+    if (q.antenna == SBR_ANTENNA_TABULATED) pattern_params(q.pattern, S.device, P);
     P.fresnel = q.use_fresnel ? 1 : 0;
     P.level = q.tessellation;
     P.n_launch = int(n_launch_of(q.tessellation));

@@ -129,6 +129,40 @@ __device__ __forceinline__ M3<R> sph_frame(R th, R ph) {
   return M3<R>{{st * cp, ct * cp, -sp, st * sp, ct * sp, cp, ct, -st, R(0)}};
 }
 
+// Tabulated antenna pattern (the TXPattern.dat grid of data/TXPattern.dat,
+// which Preprocessor::ReadPatternFile loads, Preprocessor.cpp:3-35): complex
+// relative amplitudes of E_theta and E_phi on a regular (theta, phi) grid in
+// degrees, phi periodic.  E = sqrt(60 Pt) * amplitude, as the analytic
+// patterns scale with sqrt(60 Pt G).
+struct PatternTab {
+  const float4* a;  // nt * np entries, theta-major
+  int nt, np;
+  double dt, dp;
+};
+
+// Bilinear interpolation of the grid at (theta, phi) degrees; theta clamped
+// to the grid, phi wrapped.  out = (re, im) of E_theta then E_phi.
+__device__ __forceinline__ void pattern_at(const PatternTab& p, double th, double ph, double* out) {
+  double ft = th / p.dt;
+  ft = fmin(fmax(ft, 0.0), double(p.nt - 1));
+  int t0 = min(int(ft), p.nt - 2 >= 0 ? p.nt - 2 : 0);
+  const double wt = p.nt > 1 ? ft - t0 : 0.0;
+  const int t1 = p.nt > 1 ? t0 + 1 : t0;
+  double fp = ph / p.dp;
+  fp -= floor(fp / p.np) * p.np;
+  int p0 = int(fp);
+  if (p0 >= p.np) p0 = p.np - 1;
+  const double wp = fp - p0;
+  const int p1 = (p0 + 1) % p.np;
+  const float4 a00 = p.a[t0 * p.np + p0], a01 = p.a[t0 * p.np + p1];
+  const float4 a10 = p.a[t1 * p.np + p0], a11 = p.a[t1 * p.np + p1];
+  const double w00 = (1 - wt) * (1 - wp), w01 = (1 - wt) * wp, w10 = wt * (1 - wp), w11 = wt * wp;
+  out[0] = w00 * a00.x + w01 * a01.x + w10 * a10.x + w11 * a11.x;
+  out[1] = w00 * a00.y + w01 * a01.y + w10 * a10.y + w11 * a11.y;
+  out[2] = w00 * a00.z + w01 * a01.z + w10 * a10.z + w11 * a11.z;
+  out[3] = w00 * a00.w + w01 * a01.w + w10 * a10.w + w11 * a11.w;
+}
+
 struct FieldConsts {
   double e0, eta0, pi_hi, pi_lo;  // reference constants (computed on the host)
 };
@@ -173,7 +207,8 @@ template <class R, bool fp32_phase = false>
 __device__ void path_field(int n, const double (*pts)[3], const double* const* frames,
                            const int* kind, const int* mat, const Material* mats,
                            const double* txcs, double freq, double pt, int antenna,
-                           bool fresnel, const FieldConsts& K, Cx<double>* out) {
+                           bool fresnel, const FieldConsts& K, Cx<double>* out,
+                           const PatternTab* pat = nullptr) {
   const double lam64 = 2.99792458e8 / freq;
   const R lam = R(lam64);
   M3<R> cur, next;
@@ -214,6 +249,13 @@ __device__ void path_field(int n, const double (*pts)[3], const double* const* f
       if (antenna == 1) inc[1] = cx(R(0), R(sqrt(60.0 * pt * 1.5)) * sin(th));
       else if (antenna == 2)
         inc[1] = cx(R(0), R(sqrt(60.0 * pt)) * (cos(R(K.pi_hi) * cos(th) / R(2)) / sin(th)));
+      else if (antenna == 3 && pat) {
+        double a[4];
+        pattern_at(*pat, double(th) * (180.0 / K.pi_hi), double(ph) * (180.0 / K.pi_hi), a);
+        const double amp = sqrt(60.0 * pt);
+        inc[1] = cx(R(amp * a[0]), R(amp * a[1]));
+        inc[2] = cx(R(amp * a[2]), R(amp * a[3]));
+      }
     } else {
       Cx<R> g[3];
       mtv(cur, tot, g);   // RotateToNewCoordSys(E, current, global) = current^T E

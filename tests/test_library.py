@@ -33,7 +33,7 @@ def test_header_and_exports_agree(built):
 def test_struct_layouts_match_header(tmp_path):
     """The ctypes structures have the header's sizes and field offsets (a C
     program compiled against include/sbr.h prints them)."""
-    checks = {"sbr_request": (_lib.Request, ["n_rx", "rx", "stage_counts", "field_check"]),
+    checks = {"sbr_request": (_lib.Request, ["n_rx", "rx", "stage_counts", "field_check", "pattern"]),
               "sbr_counts": (_lib.Counts, ["keys", "near_edge_paths", "gpu_kernels"]),
               "sbr_path": (_lib.Path, ["launch", "field", "near_edge"]),
               "sbr_timing": (_lib.Timing, ["device_ms"]),
