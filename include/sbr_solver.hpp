@@ -8,6 +8,7 @@
 //   Preprocessor::GenerateRxPlane Preprocessor.cpp:254-268
 //   Preprocessor::GenerateRXLine  Preprocessor.cpp:270-284
 //   Preprocessor::ReadLocationFile Preprocessor.h:21
+//   Preprocessor::ReadPatternFile Preprocessor.cpp:3-35 (+ AntennaPattern, antenna type 3)
 //   BVH<Triangle>::ConstructBVH   BVH/BVH.h:25,135-230
 //   RTSolver::Init / ExecuteRayTracing / Save*   RTSolver.h:18-45
 //   FieldCompute::FieldAtReceiver FieldCompute.h:39
@@ -34,6 +35,7 @@
 #include <cstdio>
 #include <fstream>
 #include <initializer_list>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -114,7 +116,28 @@ struct Triangle {
 struct GlobalConfig {
   int antennaType = SBR_ANTENNA_HERTZIAN;
   int fieldPrecision = SBR_FIELD_FP64;
-  bool fieldCheck = false;  // FP32 precisions: also state the error against FP64
+  bool fieldCheck = false;                // FP32 precisions: also state the error against FP64
+  const sbr_pattern* pattern = nullptr;  // antennaType SBR_ANTENNA_TABULATED
+};
+
+// DataStructures.h:32-37: antenna gain table keyed by (theta, phi) degrees.
+struct GainInfo {
+  float data[4];  // theta gain, theta phase, phi gain, phi phase
+};
+using ThetaPhiAngle = std::pair<float, float>;
+using GainMap = std::map<ThetaPhiAngle, GainInfo>;
+
+// A TXPattern.dat table on the device (sbr_pattern_read), for antenna type 3.
+class AntennaPattern {
+ public:
+  explicit AntennaPattern(const std::string& fileName) { check(sbr_pattern_read(fileName.c_str(), &p_)); }
+  AntennaPattern(const AntennaPattern&) = delete;
+  AntennaPattern& operator=(const AntennaPattern&) = delete;
+  ~AntennaPattern() { sbr_pattern_destroy(p_); }
+  const sbr_pattern* get() const { return p_; }
+
+ private:
+  sbr_pattern* p_ = nullptr;
 };
 
 // ---------------------------------------------------------- preprocessing
@@ -163,6 +186,23 @@ inline void GenerateRXLine(Vec3 start, Vec3 end, double resolution, VecVec3& out
   std::vector<double> p(3 * size_t(n));
   check(sbr_generate_rx_line(start.data(), end.data(), resolution, p.data(), n, &n));
   for (int i = 0; i < n; ++i) output.emplace_back(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+}
+
+// Preprocessor.cpp:3-35: lines of six numbers (theta phi g_theta arg_theta
+// g_phi arg_phi) into the map; other lines are skipped.
+inline bool ReadPatternFile(std::string fileName, GainMap& output) {
+  std::ifstream in(fileName);
+  if (!in) return false;
+  std::string line;
+  while (std::getline(in, line)) {
+    float v[6];
+    char extra;
+    if (std::sscanf(line.c_str(), " %f %f %f %f %f %f %c", &v[0], &v[1], &v[2], &v[3], &v[4],
+                    &v[5], &extra) != 6)
+      continue;
+    output[{v[0], v[1]}] = GainInfo{{v[2], v[3], v[4], v[5]}};
+  }
+  return true;
 }
 
 // Whitespace-separated x y z per line; lines that do not parse are skipped.
@@ -315,6 +355,7 @@ class RTSolver {
     q.antenna = config_.antennaType;
     q.field_precision = config_.fieldPrecision;
     q.field_check = config_.fieldCheck ? 1 : 0;
+    q.pattern = config_.pattern;
     q.n_rx = int(receivers.size());
     q.rx = receivers_.data();
     if (result_) sbr_result_destroy(result_);
