@@ -840,9 +840,10 @@ constexpr int kCapWarps = 4;
 #define SBR_CAP_CHUNK_CELLS 16
 #endif
 constexpr float kCapChunkCells = SBR_CAP_CHUNK_CELLS;
-// Nodes staged per warp at a time (at most 32: one per lane).
+// Nodes staged per warp at a time (at most 32: one per lane; 16 leaves more
+// of the SM's shared memory to L1 for the receiver grid).
 #ifndef SBR_CAP_BATCH
-#define SBR_CAP_BATCH 32
+#define SBR_CAP_BATCH 16
 #endif
 constexpr int kCapBatch = SBR_CAP_BATCH;
 
