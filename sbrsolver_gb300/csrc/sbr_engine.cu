@@ -1,22 +1,21 @@
-// GB300 SBR engine: device-resident scene, wavefront ray tracing, reception
-// capture, image correction, duplicate removal and the received field, behind
-// the C ABI declared in include/sbr.h.
-//
-// Pipeline per solve (one CUDA stream, no host round trip between stages):
-//   grid     receivers -> uniform grid (bbox, count, scan, scatter)
-//   trace    one kernel per bounce depth over a compacted wavefront queue;
-//            each ray runs the closest-hit query, writes its tree node and
-//            spawns its reflected / transmitted children (RTSolver.cpp:128-257)
-//   capture  every node tests the receivers near its segment against its
-//            reception sphere (RTSolver.cpp:805-863); a capture counts unless an
-//            ancestor captured the same receiver (RayCapture deletes the
-//            subtree, RTSolver.cpp:277-284).  Captures are grouped by
-//            (receiver, path class) with the minimum (launch, BFS) rank
-//   correct  one image-method correction per group (RTSolver.cpp:299-433)
-//   dedup    minimum rank per (receiver, coplanar key) over corrected groups
-//            (RTSolver.cpp:435-459); the minimum is the reference's survivor
-//   field    per survivor (FieldCompute.cpp:71-151), summed per receiver in
-//            (launch, BFS) order (FieldCompute.cpp:11-25)
+// GB300 SBR engine: device-resident scenes, workspaces and the solve behind
+// the C ABI declared in include/sbr.h.  The kernels live in
+//   sbr_grid.cuh     receivers -> uniform grid (bbox, count, scan, scatter)
+//   sbr_trace.cuh    RayLaunch (RTSolver.cpp:128-257) as a wavefront: per bounce
+//                    depth an FP32 candidate search (k_find) and the FP64
+//                    closest hit, tree node and children (k_trace)
+//   sbr_capture.cuh  RayCapture (RTSolver.cpp:259-297, 805-863) with image
+//                    correction's first step as a prefilter (k_capture), FP64
+//                    decisions, MultiPathCorrection and ancestor suppression
+//                    (k_capture_finish)
+//   sbr_paths.cuh    DirectPathCorrection per receiver (k_direct), duplicate
+//                    removal (RTSolver.cpp:435-459), the survivors'
+//                    geometry and field (FieldCompute.cpp:71-151) and the
+//                    per-receiver sum in (launch, BFS) order
+//                    (FieldCompute.cpp:11-25)
+// One CUDA stream per workspace; the host synchronises once per solve, after
+// the capacity counters (a solve whose tables overflowed is repeated with
+// larger ones).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,6 +34,12 @@
 #include "sbr_field.cuh"
 #include "sbr_host.h"
 #include "sbr_kernels.cuh"
+
+#include "sbr_common.cuh"
+#include "sbr_grid.cuh"
+#include "sbr_trace.cuh"
+#include "sbr_capture.cuh"
+#include "sbr_paths.cuh"
 
 namespace sbr {
 
@@ -87,1576 +92,6 @@ static uint32_t next_pow2(uint64_t x) {
   uint64_t p = 1;
   while (p < x) p <<= 1;
   return uint32_t(std::min<uint64_t>(p, 1ull << 31));
-}
-
-// ============================================================ kernels
-
-__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
-
-// Warp-aggregated slot reservation: every active lane asks for `cnt` (0..2)
-// entries; one atomicAdd per warp.
-__device__ __forceinline__ unsigned long long warp_reserve(unsigned long long* ctr, unsigned cnt) {
-  const unsigned mask = __activemask();
-  const unsigned b1 = __ballot_sync(mask, cnt >= 1);
-  const unsigned b2 = __ballot_sync(mask, cnt >= 2);
-  const unsigned lt = (1u << lane_id()) - 1u;
-  const unsigned before = __popc(b1 & lt) + __popc(b2 & lt);
-  const unsigned total = __popc(b1) + __popc(b2);
-  const int leader = __ffs(mask) - 1;
-  unsigned long long base = 0;
-  if (lane_id() == unsigned(leader) && total) base = atomicAdd(ctr, (unsigned long long)total);
-  base = __shfl_sync(mask, base, leader);
-  return base + before;
-}
-
-// Open addressing with linear probing.  Tables are kept at most half full
-// (the host grows them between solves from the occupancy counters), so a
-// probe run longer than kMaxProbe means the table is too small: the insert
-// reports overflow and the solve is repeated with a larger table.
-constexpr uint32_t kMaxProbe = 256;
-
-__device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long key, unsigned* ov,
-                                              unsigned bit, unsigned long long* used,
-                                              unsigned long long* lost, bool* fresh = nullptr) {
-  uint32_t h = uint32_t(mix64(key)) & t.mask;
-  const uint32_t lim = min(kMaxProbe, t.mask + 1);
-  for (uint32_t i = 0; i < lim; ++i) {
-    unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&t.keys[h]);
-    if (k == key) return h;
-    if (k == kEmptyKey) {
-      unsigned long long old = atomicCAS(&t.keys[h], kEmptyKey, key);
-      if (old == kEmptyKey) {
-        atomicAdd(used, 1ull);
-        if (fresh) *fresh = true;
-        return h;
-      }
-      if (old == key) return h;
-    }
-    h = (h + 1) & t.mask;
-  }
-  atomicOr(ov, bit);
-  atomicAdd(lost, 1ull);
-  return 0xFFFFFFFFu;
-}
-
-__device__ __forceinline__ uint32_t ht_find(HashTable t, unsigned long long key) {
-  uint32_t h = uint32_t(mix64(key)) & t.mask;
-  const uint32_t lim = min(kMaxProbe, t.mask + 1);
-  for (uint32_t i = 0; i < lim; ++i) {
-    unsigned long long k = t.keys[h];
-    if (k == key) return h;
-    if (k == kEmptyKey) return 0xFFFFFFFFu;
-    h = (h + 1) & t.mask;
-  }
-  return 0xFFFFFFFFu;
-}
-
-__global__ void k_fill_u64(unsigned long long* p, size_t n, unsigned long long v) {
-  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
-       i += size_t(gridDim.x) * blockDim.x)
-    p[i] = v;
-}
-
-// ---- receiver grid ------------------------------------------------------
-
-// Order-preserving float <-> int mapping for atomicMin/Max on floats.
-__device__ __forceinline__ int f2o(float f) {
-  int i = __float_as_int(f);
-  return i >= 0 ? i : i ^ 0x7FFFFFFF;
-}
-__device__ __forceinline__ float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
-
-struct GridBuild {
-  int bmin[3], bmax[3];  // ordered ints
-  float cmax;            // max |rx| (as float, atomicMax on ordered int below)
-  int cmax_o;
-  int ncell;
-};
-
-__global__ void k_rx_bounds(const double* rx, const TxParams* txp, int n_tx, GridBuild* gb) {
-  const int r = blockIdx.y;  // request
-  if (r >= n_tx) return;
-  const TxParams& P = txp[r];
-  int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN}, cm = INT_MIN;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_rx; i += gridDim.x * blockDim.x) {
-    const double* c = rx + 3 * size_t(P.rx_first + i);
-    float c32[3] = {float(c[0]), float(c[1]), float(c[2])};
-    for (int a = 0; a < 3; ++a) {
-      mn[a] = min(mn[a], f2o(c32[a]));
-      mx[a] = max(mx[a], f2o(c32[a]));
-    }
-    cm = max(cm, f2o(float(sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]))));
-  }
-  for (int a = 0; a < 3; ++a) {
-    for (int o = 16; o; o >>= 1) {
-      mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-      mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-    }
-  }
-  for (int o = 16; o; o >>= 1) cm = max(cm, __shfl_xor_sync(0xffffffffu, cm, o));
-  if (lane_id() == 0) {
-    for (int a = 0; a < 3; ++a) {
-      atomicMin(&gb[r].bmin[a], mn[a]);
-      atomicMax(&gb[r].bmax[a], mx[a]);
-    }
-    atomicMax(&gb[r].cmax_o, cm);
-  }
-}
-
-// Grid shape: cells of equal size sized for ~4 receivers per cell over the
-// axes with extent, at most max_cells cells.
-__global__ void k_grid_shape(GridBuild* gb, RxGrid* grids, const TxParams* txp, int n_tx,
-                             int max_cells, int* cell_base) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int base = 0;
-  for (int r = 0; r < n_tx; ++r) {
-    RxGrid& g = grids[r];
-    float lo[3], hi[3], ext[3];
-    float emax = 0;
-    for (int a = 0; a < 3; ++a) {
-      lo[a] = o2f(gb[r].bmin[a]);
-      hi[a] = o2f(gb[r].bmax[a]);
-      if (txp[r].n_rx == 0) lo[a] = hi[a] = 0;
-      ext[a] = hi[a] - lo[a];
-      emax = fmaxf(emax, ext[a]);
-    }
-    int k = 0;
-    double vol = 1;
-    for (int a = 0; a < 3; ++a)
-      if (ext[a] > 1e-6f * emax && ext[a] > 0) {
-        ++k;
-        vol *= ext[a];
-      }
-    float cell = 1.0f;
-    if (k > 0) {
-      double target = fmax(1.0, txp[r].n_rx / 2.0);
-      cell = float(pow(vol / target, 1.0 / k));
-    }
-    if (cell <= 0) cell = 1.0f;
-    int dim[3];
-    long long tot;
-    for (;;) {
-      tot = 1;
-      for (int a = 0; a < 3; ++a) {
-        dim[a] = max(1, min(1 << 20, int(ext[a] / cell) + 1));
-        tot *= dim[a];
-      }
-      if (tot <= max_cells) break;
-      cell *= 1.25f;
-    }
-    for (int a = 0; a < 3; ++a) {
-      g.org[a] = lo[a];
-      g.dim[a] = dim[a];
-      g.bmin[a] = lo[a];
-      g.bmax[a] = hi[a];
-    }
-    g.cell = cell;
-    g.inv_cell = 1.0f / cell;
-    gb[r].ncell = int(tot);
-    gb[r].cmax = o2f(gb[r].cmax_o);
-    cell_base[r] = base;
-    base += int(tot) + 1;
-  }
-  cell_base[n_tx] = base;
-}
-
-__device__ __forceinline__ int cell_of(const RxGrid& g, float x, float y, float z) {
-  int ix = min(g.dim[0] - 1, max(0, int((x - g.org[0]) / g.cell)));
-  int iy = min(g.dim[1] - 1, max(0, int((y - g.org[1]) / g.cell)));
-  int iz = min(g.dim[2] - 1, max(0, int((z - g.org[2]) / g.cell)));
-  return (iz * g.dim[1] + iy) * g.dim[0] + ix;
-}
-
-__global__ void k_rx_count(const double* rx, const TxParams* txp, int n_tx, const RxGrid* grids,
-                           const int* cell_base, int* counts) {
-  const int r = blockIdx.y;
-  if (r >= n_tx) return;
-  const RxGrid g = grids[r];
-  const TxParams& P = txp[r];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_rx; i += gridDim.x * blockDim.x) {
-    const double* c = rx + 3 * size_t(P.rx_first + i);
-    atomicAdd(&counts[cell_base[r] + cell_of(g, float(c[0]), float(c[1]), float(c[2]))], 1);
-  }
-}
-
-// Single-block exclusive scan (n up to a few million): each thread scans a
-// contiguous chunk, then the chunk totals are scanned across the block.
-__global__ void k_scan_exclusive(const int* in, int* out, int n) {
-  __shared__ int part[1024];
-  const int t = threadIdx.x, T = blockDim.x;
-  const int chunk = (n + T - 1) / T;
-  const int b = min(n, t * chunk), e = min(n, b + chunk);
-  int s = 0;
-  for (int i = b; i < e; ++i) s += in[i];
-  part[t] = s;
-  __syncthreads();
-  for (int off = 1; off < T; off <<= 1) {
-    int v = t >= off ? part[t - off] : 0;
-    __syncthreads();
-    part[t] += v;
-    __syncthreads();
-  }
-  int run = t ? part[t - 1] : 0;
-  for (int i = b; i < e; ++i) {
-    int v = in[i];
-    out[i] = run;
-    run += v;
-  }
-  if (t == T - 1) out[n] = part[T - 1];
-}
-
-__global__ void k_rx_scatter(const double* rx, const TxParams* txp, int n_tx, const RxGrid* grids,
-                             const int* cell_base, const int* starts, int* cursor, float4* rx32) {
-  const int r = blockIdx.y;
-  if (r >= n_tx) return;
-  const RxGrid g = grids[r];
-  const TxParams& P = txp[r];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_rx; i += gridDim.x * blockDim.x) {
-    const int gi = P.rx_first + i;
-    const double* c = rx + 3 * size_t(gi);
-    const int cid = cell_base[r] + cell_of(g, float(c[0]), float(c[1]), float(c[2]));
-    const int pos = starts[cid] + atomicAdd(&cursor[cid], 1);
-    rx32[pos] = make_float4(float(c[0]), float(c[1]), float(c[2]), __int_as_float(gi));
-  }
-}
-
-__global__ void k_grid_finish(RxGrid* grids, const int* starts, const int* cell_base,
-                              const float4* rx32, int n_tx) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_tx) return;
-  grids[r].cell_start = starts + cell_base[r];
-  grids[r].rx32 = rx32;
-}
-
-// ---- trace ------------------------------------------------------------------
-
-struct TraceArgs {
-  DevScene sc;
-  const TxParams* txp;
-  int n_tx;
-  const double* const* dirs;  // per level
-  const RayRec* in;
-  RayRec* out;
-  unsigned long long out_cap;
-  NodeHot* nodes;
-  NodeCold* nodes_cold;
-  unsigned long long node_cap;
-  HashTable cls_tab, cop_tab;
-  ClassInfo* cls_info;
-  ClassCap* cls_cap;
-  const int* tri_cop;  // coplanar id by rank
-  Counters* ctr;
-  unsigned long long* seg_per_tx;  // executed segments per request
-  int depth;
-  long long n_root;    // total launches (depth 0)
-  long long lo, hi;    // this launch covers rays [lo, hi) of the depth
-  const uint2* cand;   // contenders of those rays (k_find)
-  const unsigned char* ncand;
-};
-
-__device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long long g) {
-  int lo = 0, hi = n_tx - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (txp[mid].launch_first <= g) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
-// The capture-stage record of a class with image source img (FP64) whose
-// last ray starts on the triangle at mesh position tpos.
-__device__ void write_class_cap(const DevScene& sc, const double* img, int tpos, ClassCap& cc) {
-  const Tri32 T = sc.corr32[tpos];
-  const float3 o = make_float3(float(img[0]), float(img[1]), float(img[2]));
-  const float no = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
-  const TriFrom F = tri_from(T, o, no);
-  cc.img[0] = o.x;
-  cc.img[1] = o.y;
-  cc.img[2] = o.z;
-  cc.tpos = tpos;
-  cc.F[0] = F.sx; cc.F[1] = F.sy; cc.F[2] = F.sz;
-  cc.F[3] = F.qx; cc.F[4] = F.qy; cc.F[5] = F.qz;
-  cc.F[6] = F.W; cc.F[7] = F.ns;
-  float v[3][3];
-  for (int a = 0; a < 3; ++a) {
-    v[0][a] = T.v1[a];
-    v[1][a] = T.v1[a] + T.e1[a];
-    v[2][a] = T.v1[a] + T.e2[a];
-  }
-  const float im[3] = {o.x, o.y, o.z};
-  const float g[3] = {(v[0][0] + v[1][0] + v[2][0]) / 3.0f, (v[0][1] + v[1][1] + v[2][1]) / 3.0f,
-                      (v[0][2] + v[1][2] + v[2][2]) / 3.0f};
-  const float tmag = no + T.nv1 + T.ne1 + T.ne2 + 1.0f;
-  for (int k = 0; k < 3; ++k) {
-    const float* p = v[k];
-    const float* q = v[k == 2 ? 0 : k + 1];
-    const float a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
-    const float b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
-    const float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
-                        a[0] * b[1] - a[1] * b[0]};
-    const float nn = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    // orient towards the triangle's centroid, which lies inside the cone
-    const float gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
-    const float sg = gc > 0.0f ? 1.0f : -1.0f;
-    for (int c = 0; c < 3; ++c) cc.n[k][c] = sg * n[c];
-    cc.n[k][3] = sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]);
-    cc.nn[k] = nn;
-    cc.w[k] = nn * tmag;
-    cc.gc[k] = fabsf(gc);
-    cc.inv_nx[k] = 1.0f / (sg * n[0]);
-  }
-}
-
-// Every thread that interns a class writes the same values (they depend
-// only on the key), so concurrent writers agree.
-__device__ __forceinline__ void write_class(ClassInfo& ci, const double* img, uint32_t parent,
-                                            int tri, uint32_t cop, int kind, int depth) {
-  ci.img[0] = img[0];
-  ci.img[1] = img[1];
-  ci.img[2] = img[2];
-  ci.img32[0] = float(img[0]);
-  ci.img32[1] = float(img[1]);
-  ci.img32[2] = float(img[2]);
-  ci.parent = parent;
-  ci.tri = tri;
-  ci.cop = cop;
-  ci.kind = uint8_t(kind);
-  ci.depth = uint8_t(depth);
-  ci.pad0 = ci.pad1 = 0;
-  ci.pad2 = 0;
-}
-
-// Number of rays entering bounce depth `depth` (known on the device only).
-__device__ __forceinline__ long long rays_at_depth(const Counters* ctr, int depth, long long n_root,
-                                                   unsigned long long cap) {
-  return depth == 0 ? n_root : (long long)min(ctr->queue[depth], cap);
-}
-
-// Launch ray g of the batch: origin and direction (FP64).
-__device__ __forceinline__ void root_ray(const TxParams* txp, int n_tx, const double* const* dirs,
-                                         long long g, double* o, double* d, int& q, long long& li) {
-  q = find_request(txp, n_tx, g);
-  const TxParams& P = txp[q];
-  li = g - P.launch_first;
-  const double* dd = dirs[P.level] + 3 * li;
-  for (int a = 0; a < 3; ++a) {
-    o[a] = P.tx[a];
-    d[a] = dd[a];
-  }
-}
-
-// ---- FP32 candidate search (persistent, rays refilled per warp) ----------
-//
-// Each lane traverses one ray at a time.  Lanes whose ray is finished take a
-// new one from the chunk's work counter (one atomic per warp, when at least
-// a quarter of the warp is idle or nobody is busy), so warps stay full while
-// rays of very different lengths finish at different times.
-struct FindArgs {
-  DevScene sc;
-  const TxParams* txp;
-  int n_tx;
-  const double* const* dirs;
-  const RayRec* in;
-  const Counters* ctr;
-  unsigned long long in_cap;
-  long long n_root;
-  int depth;
-  long long lo, hi;            // this launch covers rays [lo, hi) of the depth
-  unsigned long long* work;    // rays of the chunk handed out (zero at launch)
-  uint2* cand;                 // kCand per ray of the chunk
-  unsigned char* ncand;        // contenders per ray, kFindFallback = exact traversal
-};
-
-constexpr int kFindSteps = 16;  // traversal steps between refills
-
-__global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
-  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
-  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.in_cap);
-  const long long n = min(n_all, A.hi) - A.lo;
-  if (n <= 0) return;
-  const unsigned lane = lane_id();
-  long long ray = -1;
-  bool exhausted = false;
-  float3 o32 = make_float3(0, 0, 0), d32 = o32, inv = o32;
-  float no = 0.0f, nd = 0.0f, m = 0.0f, tcut = INFINITY;
-  int stack[kStack];
-  int sp = 0, pending = -1, nc = 0;
-  bool fail = false;
-  uint2* out = nullptr;
-  while (true) {
-    const bool idle = ray < 0 && !exhausted;
-    const unsigned im = __ballot_sync(0xffffffffu, idle);
-    const unsigned busy = __ballot_sync(0xffffffffu, ray >= 0);
-    if (im && (__popc(im) >= 8 || busy == 0)) {
-      const int leader = __ffs(im) - 1;
-      unsigned long long base = 0;
-      if (int(lane) == leader) base = atomicAdd(A.work, (unsigned long long)__popc(im));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (idle) {
-        const long long k = (long long)base + __popc(im & ((1u << lane) - 1u));
-        if (k < n) {
-          ray = k;
-          double o[3], d[3];
-          if (A.depth == 0) {
-            int q;
-            long long li;
-            root_ray(A.txp, A.n_tx, A.dirs, A.lo + k, o, d, q, li);
-          } else {
-            const RayRec& r = A.in[A.lo + k];
-            for (int a = 0; a < 3; ++a) {
-              o[a] = r.o[a];
-              d[a] = r.d[a];
-            }
-          }
-          o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
-          d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
-          inv = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
-          no = sqrtf(o32.x * o32.x + o32.y * o32.y + o32.z * o32.z);
-          nd = sqrtf(d32.x * d32.x + d32.y * d32.y + d32.z * d32.z);
-          m = A.sc.box_margin + kFiltK * no;
-          tcut = INFINITY;
-          sp = 0;
-          pending = -1;
-          nc = 0;
-          fail = false;
-          stack[sp++] = 0;  // the search root is always a node
-          out = A.cand + size_t(k) * kCand;
-        } else {
-          exhausted = true;
-        }
-      }
-    }
-    if (__ballot_sync(0xffffffffu, ray >= 0) == 0) {
-      if (__all_sync(0xffffffffu, exhausted)) break;
-      continue;
-    }
-    if (ray < 0) continue;
-    bool done = false;
-    for (int it = 0; it < kFindSteps && !done; ++it) {
-      if (pending >= 0) {
-        const int first = pending >> 3, last = first + (pending & 7);
-        for (int j = first; j < last; ++j) {
-          float tlo, thi;
-          const int k = tri_classify(A.sc.stri[j], o32, d32, no, nd, tlo, thi);
-          if (k == 0 || tlo > tcut) continue;
-          if (nc == kCand) {
-            fail = true;
-            break;
-          }
-          out[nc++] = make_uint2(unsigned(__ldg(A.sc.srank + j)), __float_as_uint(tlo));
-          if (k == 2) tcut = fminf(tcut, thi * (1.0f + 1.0f / 4096.0f) + 1e-30f);
-        }
-        pending = -1;
-        if (fail) done = true;
-        continue;
-      }
-      if (sp == 0) {
-        done = true;
-        break;
-      }
-      const int ni = stack[--sp];
-      if (ni < 0) {  // a leaf deferred as the farther child
-        pending = ~ni;
-        continue;
-      }
-      float4 f0, f1, f2;
-      int2 ch;
-      load_node(A.sc.snode, ni, f0, f1, f2, ch);
-      float tn0, tf0, tn1, tf1;
-      slab32(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, o32, inv, m, tn0, tf0);
-      slab32(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, o32, inv, m, tn1, tf1);
-      const bool h0 = tn0 <= tf0 && tf0 >= 0.0f && tn0 <= tcut;
-      const bool h1 = tn1 <= tf1 && tf1 >= 0.0f && tn1 <= tcut;
-      int first = 0, second = 0;
-      bool has_first = false, has_second = false;
-      if (h0 && h1) {
-        has_first = has_second = true;
-        if (tn1 < tn0) {
-          first = ch.y;
-          second = ch.x;
-        } else {
-          first = ch.x;
-          second = ch.y;
-        }
-      } else if (h0) {
-        has_first = true;
-        first = ch.x;
-      } else if (h1) {
-        has_first = true;
-        first = ch.y;
-      }
-      if (has_second) {
-        if (sp >= kStack) {
-          fail = done = true;
-          break;
-        }
-        stack[sp++] = second;  // node, or ~leaf code
-      }
-      if (has_first) {
-        if (first < 0) {
-          pending = ~first;
-        } else {
-          if (sp >= kStack) {
-            fail = done = true;
-            break;
-          }
-          stack[sp++] = first;
-        }
-      }
-    }
-    if (done) {
-      A.ncand[ray] = fail ? kFindFallback : (unsigned char)nc;
-      ray = -1;
-    }
-  }
-}
-
-// Resident blocks of k_trace per SM (register budget 65536 / (128 x this)).
-#ifndef SBR_TRACE_BLOCKS
-#define SBR_TRACE_BLOCKS 4
-#endif
-__global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
-  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
-  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
-  const long long n_in = min(n_all, A.hi);
-  TraceStats st{0, 0};
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = A.lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in;
-       i += stride) {
-    RayRec r;
-    if (A.depth == 0) {
-      int q;
-      long long li;
-      root_ray(A.txp, A.n_tx, A.dirs, i, r.o, r.d, q, li);
-      r.total = 0.0;
-      r.S = 0.0;
-      r.parent = 0xFFFFFFFFu;
-      r.cls = kRootBase + uint32_t(q);
-      r.cop = kRootClass;
-      r.launch = uint32_t(li);
-      r.heap = 1;
-      r.rc = r.tc = 0;
-      r.tx = uint32_t(q);
-    } else {
-      r = A.in[i];
-    }
-    const TxParams& P = A.txp[r.tx];
-    Hit h;
-    const long long c = i - A.lo;
-    const bool hit = resolve_hit(A.sc, r.o, r.d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
-                                 &A.ctr->overflow);
-    const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
-    {  // per-request segment count, one atomic per request present in the warp
-      const unsigned peers = __match_any_sync(__activemask(), r.tx);
-      if (int(lane_id()) == __ffs(peers) - 1)
-        atomicAdd(&A.seg_per_tx[r.tx], (unsigned long long)__popc(peers));
-    }
-    const bool root = A.depth == 0;
-    if (ni < A.node_cap) {
-      NodeCold n;
-      NodeHot m;
-      n.s[0] = r.o[0]; n.s[1] = r.o[1]; n.s[2] = r.o[2];
-      if (hit) {
-        n.t[0] = h.p[0]; n.t[1] = h.p[1]; n.t[2] = h.p[2];
-        m.len = float(h.dist);
-      } else {
-        const double sc = root ? 1E10 : 1E2;  // RTSolver.cpp:231,249
-        n.t[0] = x64::add(r.o[0], x64::mul(r.d[0], sc));
-        n.t[1] = x64::add(r.o[1], x64::mul(r.d[1], sc));
-        n.t[2] = x64::add(r.o[2], x64::mul(r.d[2], sc));
-        m.len = float(sc);
-      }
-      n.S = r.S;
-      n.pad = 0.0;
-      m.s[0] = float(r.o[0]); m.s[1] = float(r.o[1]); m.s[2] = float(r.o[2]);
-      m.S = float(r.S);
-      m.u[0] = float(r.d[0]); m.u[1] = float(r.d[1]); m.u[2] = float(r.d[2]);
-      m.parent = r.parent;
-      m.cls = r.cls;
-      m.launch = r.launch;
-      m.heap = r.heap;
-      m.tx = r.tx;
-      m.pad0 = m.pad1 = m.pad2 = 0;
-      A.nodes_cold[ni] = n;
-      A.nodes[ni] = m;
-    } else {
-      atomicOr(&A.ctr->overflow, kOvNodes);
-    }
-    // children (RTSolver.cpp:186-221)
-    unsigned nch = 0;
-    bool do_r = false, do_t = false;
-    if (hit) {
-      do_r = r.rc < P.R;
-      do_t = r.tc < P.T;
-      nch = unsigned(do_r) + unsigned(do_t);
-    }
-    const unsigned long long base = warp_reserve(&A.ctr->queue[A.depth + 1], nch);
-    if (nch) {
-      const Tri64& T = A.sc.tri64[h.rank];
-      const double cum = x64::add(r.total, h.dist);  // node pathLength
-      RayRec c;
-      c.o[0] = h.p[0]; c.o[1] = h.p[1]; c.o[2] = h.p[2];
-      c.total = cum;
-      c.S = x64::add(r.S, cum);
-      c.parent = uint32_t(ni);
-      c.launch = r.launch;
-      c.tx = r.tx;
-      c.pad = 0;
-      const int cop = A.tri_cop[h.rank];
-      const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
-      const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop,
-                                           &A.ctr->lost_cop);
-      // image source of the parent ray's class (the transmitter for a launch)
-      const double* pimg = is_root_class(r.cls) ? P.tx : A.cls_info[r.cls].img;
-      unsigned long long slot = base;
-      if (do_t) {  // transmitted: same direction, heap 2h, same image source
-        c.d[0] = r.d[0]; c.d[1] = r.d[1]; c.d[2] = r.d[2];
-        c.heap = r.heap * 2;
-        c.rc = r.rc;
-        c.tc = r.tc + 1;
-        const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
-        bool fresh = false;
-        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
-                          &A.ctr->lost_cls, &fresh);
-        c.cop = cop_cls;
-        if (fresh) {  // only the thread that interned the class writes its records
-          write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
-          write_class_cap(A.sc, pimg, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
-        }
-        if (slot < A.out_cap) A.out[slot] = c;
-        else atomicOr(&A.ctr->overflow, kOvQueue);
-        ++slot;
-      }
-      if (do_r) {  // reflected: Reflect(d, n).normalized(), heap 2h+1
-        const double dn = x64::dot(T.n, r.d);
-        double v[3];
-        for (int a = 0; a < 3; ++a) v[a] = x64::sub(r.d[a], x64::mul(x64::mul(2.0, T.n[a]), dn));
-        x64::normalize(v, c.d);
-        c.heap = r.heap * 2 + 1;
-        c.rc = r.rc + 1;
-        c.tc = r.tc;
-        const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1);
-        bool fresh = false;
-        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
-                          &A.ctr->lost_cls, &fresh);
-        c.cop = cop_cls;
-        if (fresh) {  // only the thread that interned the class writes its records
-          // ImagePoint (RTSolver.cpp:910-924) across the triangle the
-          // reference finds at this id's position of its mesh vector
-          const CorrTri& M = A.sc.corr[A.sc.rank_to_id[h.rank]];
-          double w[3], img[3];
-          x64::sub3(pimg, M.v1, w);
-          const double dist = x64::dot(M.n, w);
-          for (int a = 0; a < 3; ++a) img[a] = x64::sub(pimg[a], x64::mul(x64::mul(2.0, dist), M.n[a]));
-          write_class(A.cls_info[c.cls], img, r.cls, h.rank, cop_cls, 1, A.depth + 1);
-          write_class_cap(A.sc, img, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
-        }
-        if (slot < A.out_cap) A.out[slot] = c;
-        else atomicOr(&A.ctr->overflow, kOvQueue);
-      }
-    }
-  }
-  if (st.fp64_tri) atomicAdd(&A.ctr->fp64_tri, (unsigned long long)st.fp64_tri);
-  if (st.fallback) atomicAdd(&A.ctr->fallback, (unsigned long long)st.fallback);
-}
-
-// ---- capture ----------------------------------------------------------------
-
-struct CaptureArgs {
-  DevScene sc;
-  const NodeHot* nodes;
-  const NodeCold* nodes_cold;
-  const TxParams* txp;
-  const RxGrid* grids;
-  const GridBuild* gb;
-  const double* rx;
-  const ClassInfo* cls_info;
-  const ClassCap* cls_cap;
-  const unsigned char* direct_ok;
-  Corrected* corr_list;
-  unsigned long long corr_cap;
-  Counters* ctr;
-  unsigned long long node_cap;
-  int stage_counts;
-  uint2* pairs;                // (node, receiver | unsure << 31) for k_capture_finish
-  unsigned long long pair_cap;
-};
-
-// MultiPathCorrection (RTSolver.cpp:330-373) for one capture, walking the
-// path class from the receiver back to the transmitter: the line from each
-// ray's image source to its current target must cross the triangle at that
-// id's mesh position.  FP32 filter first (nearly every correction fails at
-// its first test); the FP64 test in the reference's order decides the rest
-// and yields the exact intersection that becomes the next target.
-__device__ __forceinline__ bool correct_event(const DevScene& sc, const ClassInfo* info,
-                                             uint32_t cls, const float3& c32, const double* c64,
-                                             unsigned& n64) {
-  double tgt[3] = {c64[0], c64[1], c64[2]};
-  float3 t32 = c32;
-  for (uint32_t c = cls; !is_root_class(c);) {
-    const ClassInfo& ci = info[c];
-    const int mpos = sc.rank_to_id[ci.tri];
-    const float3 o = make_float3(ci.img32[0], ci.img32[1], ci.img32[2]);
-    const float3 d = make_float3(t32.x - o.x, t32.y - o.y, t32.z - o.z);
-    const float no = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
-    const float nd = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
-    float tlo;
-    if (!tri_filter(sc.corr32[mpos], o, d, no, nd, tlo)) return false;
-    ++n64;
-    double dd[3], P3[3];
-    x64::sub3(tgt, ci.img, dd);
-    if (!mt64c(sc.corr[mpos], ci.img, dd, P3)) return false;
-    tgt[0] = P3[0];
-    tgt[1] = P3[1];
-    tgt[2] = P3[2];
-    t32 = make_float3(float(P3[0]), float(P3[1]), float(P3[2]));
-    c = ci.parent;
-  }
-  return true;
-}
-
-// Exact decision for a test inside the FP32 margin (reception64 on the
-// node's FP64 record).
-__device__ __noinline__ int capture_exact(const NodeCold* cold, uint32_t idx, const double* c64,
-                                          double tanb) {
-  const NodeCold& n = cold[idx];
-  return reception64(n.s, n.t, c64, n.S, tanb) ? 1 : 0;
-}
-
-// One warp per tree node.  The receivers that can fall inside the node's
-// reception spheres lie within rb of its segment (rb bounds the sphere radius
-// (S + |P|) tan(beta), with |P| <= (cmax + S tan b) / (1 - tan b) for any
-// capturing point); the segment is clipped to that region and cut into
-// chunks (each receiver is owned by the chunk its projection falls in).  Each
-// chunk's capsule is rasterised over the receiver grid one row of cells per
-// lane; a row is one contiguous run of receivers, and the lanes stride over
-// the concatenation of the rows' runs.  A capture counts unless an ancestor
-// of the node captures the same receiver (RTSolver.cpp:277-284); ancestors
-// come from shared memory.
-constexpr int kCapWarps = 4;
-// Minimum chunk length along a segment, in receiver-grid cells.
-#ifndef SBR_CAP_CHUNK_CELLS
-#define SBR_CAP_CHUNK_CELLS 16
-#endif
-constexpr float kCapChunkCells = SBR_CAP_CHUNK_CELLS;
-// Nodes staged per warp at a time (at most 32: one per lane; 16 leaves more
-// of the SM's shared memory to L1 for the receiver grid).
-#ifndef SBR_CAP_BATCH
-#define SBR_CAP_BATCH 16
-#endif
-constexpr int kCapBatch = SBR_CAP_BATCH;
-
-// Upper bound on sqrt(x) from the hardware reciprocal square root (relative
-// error below 2^-21), for the capture stage's conservative ranges and
-// margins, which all carry slack far beyond that.
-__device__ __forceinline__ float sqrt_up(float x) {
-  if (!(x > 0.0f)) return 0.0f;
-  if (isinf(x)) return x;
-  return x * rsqrtf(x) * 1.00000095367431640625f;  // 1 + 2^-20
-}
-
-// Correction cone of a class: the points c for which the line from the
-// image source img towards c crosses the class's last triangle T
-// (MultiPathCorrection's first test for a capture at c; RTSolver.cpp:356).
-// Three planes through img and T's edges, n_k . p >= n_k . img, formed once
-// per class (write_class_cap); k_capture loosens each by 2 m_k, m_k =
-// 2^-12 |n_k| (cmax + |img| + |T| + 1) bounding the FP32 error of the test
-// for receivers |p| <= cmax (four times the FP32 filter margin), and uses
-// no cone when a plane is ill-conditioned.  The reference's FP64 test accepts
-// only points inside the exact cone, so receivers outside the loosened one
-// are skipped without changing a result.
-
-// Whether the box [lo, hi] may hold a point of the cone.
-__device__ __forceinline__ bool cone_meets_box(const float* cone, const float* lo, const float* hi) {
-  for (int k = 0; k < 3; ++k) {
-    float mx = 0.0f, mag = fabsf(cone[4 * k + 3]) + 1.0f;
-    for (int a = 0; a < 3; ++a) {
-      mx += fmaxf(cone[4 * k + a] * lo[a], cone[4 * k + a] * hi[a]);
-      mag += fabsf(cone[4 * k + a]) * fmaxf(fabsf(lo[a]), fabsf(hi[a]));
-    }
-    if (mx < cone[4 * k + 3] - 1e-3f * mag) return false;  // slack >> FP32 error of mx
-  }
-  return true;
-}
-
-// Narrows the cell range [x0, x1] of grid row (iy, iz) to the cells whose
-// box can hold a point inside the cone; an empty row gets x0 > x1.
-__device__ __forceinline__ void cone_cells(const float* cone, const RxGrid& g, float inv_cell,
-                                           int iy, int iz, int& x0, int& x1) {
-  const float y0 = g.org[1] + iy * g.cell, y1 = y0 + g.cell;
-  const float z0 = g.org[2] + iz * g.cell, z1 = z0 + g.cell;
-  for (int k = 0; k < 3; ++k) {
-    const float nx = cone[4 * k], ny = cone[4 * k + 1], nz = cone[4 * k + 2], off = cone[4 * k + 3];
-    // need nx*x >= off - max over the row's y/z band of (ny*y + nz*z)
-    const float r = off - fmaxf(ny * y0, ny * y1) - fmaxf(nz * z0, nz * z1);
-    const float slack = 1e-3f * g.cell;
-    if (nx > 0.0f) {
-      const float xl = r * cone[12 + k];  // x >= xl
-      if (isfinite(xl)) x0 = max(x0, int(floorf((xl - g.org[0] - slack) * inv_cell)));
-    } else if (nx < 0.0f) {
-      const float xh = r * cone[12 + k];  // x <= xh
-      if (isfinite(xh)) x1 = min(x1, int(floorf((xh - g.org[0] + slack) * inv_cell)));
-    } else if (r > 0.0f) {
-      x1 = x0 - 1;
-    }
-  }
-}
-
-struct AncRec {
-  float s[3], S, u[3], len;
-  uint32_t idx, pad[3];
-};
-
-// A node's segment clipped to the region that can hold a capture of this
-// request's receivers, cut into chunks (nchunk = 0: nothing to test).
-struct NodeSpan {
-  float lo, hi, step, ns;  // ns = |segment start|
-  int nchunk, use_cone;
-};
-
-// The receivers that can fall inside the node's reception spheres lie within
-// rb of its segment (rb bounds the sphere radius (S + |P|) tan(beta), with
-// |P| <= (cmax + S tan b) / (1 - tan b) for any capturing point).  All
-// ranges are widened well beyond their FP32 rounding.
-__device__ __forceinline__ NodeSpan node_span(const NodeHot& nd, const TxParams& P,
-                                              const RxGrid& g, float cmax, int use_cone) {
-  NodeSpan sp{0.0f, -1.0f, 0.0f, 0.0f, 0, use_cone};
-  if (P.n_rx <= 0) return sp;
-  const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
-  const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
-  const float len = nd.len, S = nd.S;
-  const float tanb = float(P.tan_beta);
-  const float pmax = __fdividef(cmax + S * tanb, fmaxf(1e-6f, 1.0f - tanb)) * 1.0001f + 1.0f;
-  const float su = s.x * u.x + s.y * u.y + s.z * u.z;
-  const float ss = s.x * s.x + s.y * s.y + s.z * s.z;
-  sp.ns = sqrt_up(ss);
-  const float disc = su * su - (ss - pmax * pmax);
-  float lo = 0.0f, hi = -1.0f;
-  if (disc >= 0.0f) {
-    const float sq = sqrt_up(disc);
-    lo = fmaxf(0.0f, -su - sq);
-    hi = fminf(len, -su + sq);
-  }
-  const float rbg = (S + pmax) * tanb * 1.0001f + 1e-3f;  // bound over the whole segment
-  for (int a = 0; a < 3 && lo <= hi; ++a) {
-    const float sa = a == 0 ? s.x : (a == 1 ? s.y : s.z);
-    const float ua = a == 0 ? u.x : (a == 1 ? u.y : u.z);
-    const float bl = g.bmin[a] - rbg, bh = g.bmax[a] + rbg;
-    if (fabsf(ua) < 1e-20f) {
-      if (sa < bl || sa > bh) hi = -1.0f;
-    } else {
-      // slack: 1 mm plus 2^-20 relative, beyond the reciprocal's rounding
-      const float ia = __frcp_rn(ua);
-      const float t1 = (bl - sa) * ia, t2 = (bh - sa) * ia;
-      const float tn = fminf(t1, t2), tf = fmaxf(t1, t2);
-      lo = fmaxf(lo, tn - 1e-3f - 9.5367431640625e-07f * fabsf(tn));
-      hi = fminf(hi, tf + 1e-3f + 9.5367431640625e-07f * fabsf(tf));
-    }
-  }
-  if (!(lo <= hi)) return sp;
-  const float r0 = (S + sqrt_up(ss + 2.0f * lo * su + lo * lo)) * tanb;
-  const float lc = fmaxf(kCapChunkCells * g.cell, r0);
-  int nchunk = int(ceilf(__fdividef(hi - lo, lc)));
-  nchunk = max(1, min(nchunk, 4096));
-  sp.lo = lo;
-  sp.hi = hi;
-  sp.nchunk = nchunk;
-  sp.step = __fdividef(hi - lo, float(nchunk));
-  return sp;
-}
-
-// Chunk ch of a node's span: its parameter range [a, b], the radius rb
-// around it that can hold a capture, the reception test's error margin mr,
-// and the receiver-grid cell box around it (nrows = 0: nothing to test,
-// including a box wholly outside the correction cone).
-struct ChunkBox {
-  float a, b, rb, mr;
-  int c0[3], c1[3];
-  int nrows;
-};
-
-__device__ __forceinline__ ChunkBox chunk_box(const NodeHot& nd, const RxGrid& g,
-                                              const NodeSpan& sp, int ch, float cmax, float tanb,
-                                              bool use_cone, const float* cone) {
-  ChunkBox cb;
-  const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
-  const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
-  const float S = nd.S;
-  cb.a = sp.lo + ch * sp.step;
-  cb.b = (ch == sp.nchunk - 1) ? sp.hi : sp.lo + (ch + 1) * sp.step;
-  const float pa[3] = {s.x + cb.a * u.x, s.y + cb.a * u.y, s.z + cb.a * u.z};
-  const float pb[3] = {s.x + cb.b * u.x, s.y + cb.b * u.y, s.z + cb.b * u.z};
-  const float npmax = fmaxf(sqrt_up(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]),
-                            sqrt_up(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]));
-  cb.mr = kFiltK * (sp.ns + cmax + S + npmax + 1.0f);
-  // |P| is convex along the chunk: the larger end bounds it
-  cb.rb = (S + npmax) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f + cb.mr;
-  for (int k = 0; k < 3; ++k) {
-    cb.c0[k] = max(0, int(floorf((fminf(pa[k], pb[k]) - cb.rb - g.org[k]) * g.inv_cell)));
-    cb.c1[k] = min(g.dim[k] - 1, int(floorf((fmaxf(pa[k], pb[k]) + cb.rb - g.org[k]) * g.inv_cell)));
-  }
-  const int ny = cb.c1[1] - cb.c0[1] + 1, nz = cb.c1[2] - cb.c0[2] + 1;
-  cb.nrows = (cb.c0[0] <= cb.c1[0] && ny > 0 && nz > 0) ? ny * nz : 0;
-  if (use_cone && cb.nrows) {  // the chunk's cells all outside the cone: skip it
-    float blo[3], bhi[3];
-    for (int k = 0; k < 3; ++k) {
-      blo[k] = g.org[k] + cb.c0[k] * g.cell;
-      bhi[k] = g.org[k] + (cb.c1[k] + 1) * g.cell;
-    }
-    if (!cone_meets_box(cone, blo, bhi)) cb.nrows = 0;
-  }
-  return cb;
-}
-
-// kStage: stage counts requested (every capture counted, the plain order of
-// tests); otherwise the fast path with the correction prefilter and the
-// deferred FP64 pass.
-template <bool kStage>
-__global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(CaptureArgs A) {
-  __shared__ AncRec anc[kCapWarps][kMaxDepth];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const unsigned FULL = 0xffffffffu;
-  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
-  const unsigned long long n_nodes = min(A.ctr->nodes, A.node_cap);
-  unsigned long long events = 0, cand = 0, anc_tests = 0;
-  unsigned n64 = 0;
-  const unsigned long long nw = (unsigned long long)gridDim.x * kCapWarps;
-  // Nodes are taken 32 at a time: each lane loads one node's record, its
-  // class record and last triangle, so the three dependent loads are paid
-  // once per 32 nodes; the warp then works through the 32 from shared memory.
-  constexpr int B = kCapBatch;
-  __shared__ NodeHot s_nh[kCapWarps][B];
-  __shared__ Tri32 s_tl[kCapWarps][B];      // the class's last triangle
-  __shared__ float s_fl[kCapWarps][B][12];  // image source + correction filter terms
-  __shared__ float s_cn[kCapWarps][B][16];  // loosened correction cone
-  __shared__ NodeSpan s_sp[kCapWarps][B];   // clipped span and chunking
-  __shared__ ChunkBox s_ck[kCapWarps][B];   // the span's first chunk
-  for (unsigned long long base = ((unsigned long long)blockIdx.x * kCapWarps + warp) * B;
-       base < n_nodes; base += nw * B) {
-    {
-      const unsigned long long my = base + lane;
-      if (lane < B && my < n_nodes) {
-        const NodeHot h = A.nodes[my];
-        s_nh[warp][lane] = h;
-        const float cmax = A.gb[h.tx].cmax;
-        int cone_ok = 0;
-        if (!is_root_class(h.cls)) {
-          const ClassCap c = A.cls_cap[h.cls];
-          s_tl[warp][lane] = A.sc.corr32[c.tpos];
-          float* fl = s_fl[warp][lane];
-          for (int q = 0; q < 3; ++q) fl[q] = c.img[q];
-          for (int q = 0; q < 8; ++q) fl[3 + q] = c.F[q];
-          // the cone's planes loosened by 2 m, m = 2^-12 |n| (cmax + |img| + |T| + 1)
-          float* cn = s_cn[warp][lane];
-          cone_ok = !kStage;
-          for (int k = 0; k < 3; ++k) {
-            const float m = 2.44140625e-04f * (c.nn[k] * cmax + c.w[k]);
-            cone_ok &= (c.gc[k] > 4.0f * m && isfinite(m)) ? 1 : 0;
-            cn[4 * k + 0] = c.n[k][0];
-            cn[4 * k + 1] = c.n[k][1];
-            cn[4 * k + 2] = c.n[k][2];
-            cn[4 * k + 3] = c.n[k][3] - 2.0f * m;
-            cn[12 + k] = c.inv_nx[k];
-          }
-        }
-        const NodeSpan sp = node_span(h, A.txp[h.tx], A.grids[h.tx], cmax, cone_ok);
-        s_sp[warp][lane] = sp;
-        if (sp.nchunk > 0)
-          s_ck[warp][lane] = chunk_box(h, A.grids[h.tx], sp, 0, cmax, float(A.txp[h.tx].tan_beta),
-                                       cone_ok != 0, s_cn[warp][lane]);
-      }
-      __syncwarp();
-    }
-    const int n_here = int(min((unsigned long long)B, n_nodes - base));
-    for (int jj = 0; jj < n_here; ++jj) {
-      const unsigned long long i = base + jj;
-      const NodeHot nd = s_nh[warp][jj];
-      const TxParams& P = A.txp[nd.tx];
-      const RxGrid& g = A.grids[nd.tx];
-      const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
-      const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
-      const float len = nd.len, S = nd.S;
-      // Reciprocals for the cell-range arithmetic below.  Every range there is
-      // widened by at least 2e-3 m + cell/100, far more than the few ulps a
-      // product with a reciprocal differs from the quotient.
-      const float inv_uy = __frcp_rn(u.y), inv_uz = __frcp_rn(u.z);
-      const float inv_cell = g.inv_cell;
-      // Stage the ancestor chain when every capture is checked against it
-      // (stage counts); otherwise only corrected captures (~0.1% of captures)
-      // need it and they walk the chain themselves.
-      int na = 0;
-      if (kStage && lane == 0) {
-        for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap && na < kMaxDepth;) {
-          const NodeHot a = A.nodes[p];
-          AncRec& r = anc[warp][na++];
-          r.s[0] = a.s[0]; r.s[1] = a.s[1]; r.s[2] = a.s[2]; r.S = a.S;
-          r.u[0] = a.u[0]; r.u[1] = a.u[1]; r.u[2] = a.u[2]; r.len = a.len;
-          r.idx = p;
-          p = a.parent;
-        }
-      }
-      na = __shfl_sync(FULL, na, 0);
-      __syncwarp();
-      // Image correction of this node's class must first cross the triangle
-      // the last ray reflected or passed on (MultiPathCorrection's last step):
-      // an FP32 filter from the class's image source towards each receiver
-      // rejects ~99.9% of receivers before the reception test.  Stage counts
-      // need every capture, so they keep the reception test first.
-      const bool root = is_root_class(nd.cls);
-      Tri32 Tl;
-      TriFrom Fl;
-      float3 img = make_float3(0.0f, 0.0f, 0.0f);
-      const NodeSpan sp = s_sp[warp][jj];
-      const bool use_cone = sp.use_cone != 0;
-      const float* cone_w = s_cn[warp][jj];
-      if (!root) {
-        const float* fl = s_fl[warp][jj];
-        img = make_float3(fl[0], fl[1], fl[2]);
-        Tl = s_tl[warp][jj];
-        Fl = TriFrom{fl[3], fl[4], fl[5], fl[6], fl[7], fl[8], fl[9], fl[10]};
-      }
-      if (sp.nchunk > 0) {
-        const float tanb = float(P.tan_beta);
-        const float cmax = A.gb[nd.tx].cmax;
-        const float lo = sp.lo, hi = sp.hi, ns = sp.ns;
-        const int nchunk = sp.nchunk;
-        const float step = sp.step;
-        // error margins of the FP32 reception test, from per-node bounds
-        const float ml = kFiltK * (ns + cmax + 1.0f);
-        {
-          for (int ch = 0; ch < nchunk; ++ch) {
-            const ChunkBox cb = ch == 0 ? s_ck[warp][jj]
-                                        : chunk_box(nd, g, sp, ch, cmax, tanb, use_cone, cone_w);
-            const float a = cb.a, b = cb.b, rb = cb.rb, mr = cb.mr;
-            const int c0[3] = {cb.c0[0], cb.c0[1], cb.c0[2]};
-            const int c1[3] = {cb.c1[0], cb.c1[1], cb.c1[2]};
-            const int ny = c1[1] - c0[1] + 1;
-            const int nrows = cb.nrows;
-            for (int rbase = 0; rbase < nrows; rbase += 32) {
-              // this lane's row: the part of the chunk within rb of its y/z band
-              int beg = 0, cnt = 0;
-              const int ridx = rbase + lane;
-              if (ridx < nrows) {
-                // one layer of cells (receivers on a plane) needs no division
-                const bool flat = c1[2] == c0[2];
-                const int iy = c0[1] + (flat ? ridx : ridx % ny);
-                const int iz = c0[2] + (flat ? 0 : ridx / ny);
-                const float y0 = g.org[1] + iy * g.cell - rb, y1 = g.org[1] + (iy + 1) * g.cell + rb;
-                const float z0 = g.org[2] + iz * g.cell - rb, z1 = g.org[2] + (iz + 1) * g.cell + rb;
-                float la = a, lb = b;
-                bool ok = true;
-                if (fabsf(u.y) > 1e-20f) {
-                  const float t1 = (y0 - s.y) * inv_uy, t2 = (y1 - s.y) * inv_uy;
-                  la = fmaxf(la, fminf(t1, t2));
-                  lb = fminf(lb, fmaxf(t1, t2));
-                } else if (s.y < y0 || s.y > y1) {
-                  ok = false;
-                }
-                if (fabsf(u.z) > 1e-20f) {
-                  const float t1 = (z0 - s.z) * inv_uz, t2 = (z1 - s.z) * inv_uz;
-                  la = fmaxf(la, fminf(t1, t2));
-                  lb = fminf(lb, fmaxf(t1, t2));
-                } else if (s.z < z0 || s.z > z1) {
-                  ok = false;
-                }
-                if (ok && la <= lb) {
-                  const float xa = s.x + la * u.x, xb = s.x + lb * u.x;
-                  int x0 = max(c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) * inv_cell)));
-                  int x1 = min(c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) * inv_cell)));
-                  if (use_cone && x0 <= x1)
-                    cone_cells(cone_w, g, inv_cell, iy, iz, x0, x1);
-                  if (x0 <= x1) {
-                    const int row = (iz * g.dim[1] + iy) * g.dim[0];
-                    beg = g.cell_start[row + x0];
-                    cnt = g.cell_start[row + x1 + 1] - beg;
-                  }
-                }
-              }
-              // concatenate the 32 rows' receiver runs
-              int incl = cnt;
-              for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o) incl += v;
-              }
-              const int total = __shfl_sync(FULL, incl, 31);
-              for (int kb = 0; kb < total; kb += 32) {
-                const int k = kb + lane;
-                // row holding item k: first lane whose inclusive count exceeds k
-                int rl = 0;
-                for (int step2 = 16; step2; step2 >>= 1) {
-                  const int v = __shfl_sync(FULL, incl, rl + step2 - 1);
-                  if (v <= k) rl += step2;
-                }
-                const int rincl = __shfl_sync(FULL, incl, rl);
-                const int rcnt = __shfl_sync(FULL, cnt, rl);
-                const int rbeg = __shfl_sync(FULL, beg, rl);
-                if (k >= total) continue;
-                const int j = rbeg + (k - (rincl - rcnt));
-                const float4 c4 = g.rx32[j];
-                const float3 c = make_float3(c4.x, c4.y, c4.z);
-                const float wx = c.x - s.x, wy = c.y - s.y, wz = c.z - s.z;
-                const float lam = u.x * wx + u.y * wy + u.z * wz;
-                if (ch > 0 && lam < a) continue;            // owned by an earlier chunk
-                if (ch < nchunk - 1 && lam >= b) continue;  // owned by a later chunk
-                const int gi = __float_as_int(c4.w);
-                const double* c64 = A.rx + 3 * size_t(gi);
-                ++cand;
-                if (!kStage) {
-                  if (root) {
-                    if (!A.direct_ok[gi]) continue;
-                  } else {
-                    const float3 dd = make_float3(c.x - img.x, c.y - img.y, c.z - img.z);
-                    if (!tri_filter_from(Tl, Fl, dd,
-                                         sqrt_up(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z)))
-                      continue;
-                  }
-                }
-                int v;
-                if (lam < a || lam > b) {
-                  // outside the chunk's own range: full-margin test
-                  v = reception32(s, u, len, S, c, tanb);
-                } else if (lam < -ml) {
-                  v = 0;
-                } else if (lam <= ml) {
-                  v = -1;
-                } else {
-                  const float lcl = fminf(lam, len);
-                  const float px = s.x + lcl * u.x, py = s.y + lcl * u.y, pz = s.z + lcl * u.z;
-                  const float np = sqrt_up(px * px + py * py + pz * pz);
-                  const float ex = c.x - px, ey = c.y - py, ez = c.z - pz;
-                  const float d2 = ex * ex + ey * ey + ez * ez;
-                  const float rad = (S + np) * tanb;
-                  const float rh = rad + mr, rl2 = rad - mr;
-                  v = d2 > rh * rh ? 0 : ((rl2 > 0.0f && d2 < rl2 * rl2) ? 1 : -1);
-                }
-                if (!kStage) {
-                  // everything after the FP32 tests (exact reception test,
-                  // image correction, ancestor suppression) runs densely in
-                  // k_capture_finish
-                  if (v == 0) continue;
-                  const unsigned long long slot = warp_reserve(&A.ctr->pairs, 1);
-                  if (slot < A.pair_cap)
-                    A.pairs[slot] = make_uint2(uint32_t(i), uint32_t(gi) | (v < 0 ? 0x80000000u : 0u));
-                  else
-                    atomicOr(&A.ctr->overflow, kOvPairs);
-                  continue;
-                }
-                if (v < 0) {
-                  ++n64;
-                  v = capture_exact(A.nodes_cold, uint32_t(i), c64, P.tan_beta);
-                }
-                if (!v) continue;
-                // RayCapture deletes a captured node's subtree, so an ancestor
-                // capturing the same receiver suppresses this one.
-                auto suppressed = [&]() {
-                  if (kStage) {
-                    for (int q = 0; q < na; ++q) {
-                      const AncRec& r = anc[warp][q];
-                      ++anc_tests;
-                      int w = reception32(make_float3(r.s[0], r.s[1], r.s[2]),
-                                          make_float3(r.u[0], r.u[1], r.u[2]), r.len, r.S, c, tanb);
-                      if (w < 0) {
-                        ++n64;
-                        w = capture_exact(A.nodes_cold, r.idx, c64, P.tan_beta);
-                      }
-                      if (w) return true;
-                    }
-                    return false;
-                  }
-                  for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
-                    const NodeHot a = A.nodes[p];
-                    ++anc_tests;
-                    int w = reception32(make_float3(a.s[0], a.s[1], a.s[2]),
-                                        make_float3(a.u[0], a.u[1], a.u[2]), a.len, a.S, c, tanb);
-                    if (w < 0) {
-                      ++n64;
-                      w = capture_exact(A.nodes_cold, p, c64, P.tan_beta);
-                    }
-                    if (w) return true;
-                    p = a.parent;
-                  }
-                  return false;
-                };
-                if (kStage) {
-                  if (suppressed()) continue;
-                  ++events;
-                }
-                const bool ok = is_root_class(nd.cls)
-                                    ? A.direct_ok[gi] != 0
-                                    : correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
-                if (!ok) continue;
-                if (!kStage && suppressed()) continue;
-                const unsigned long long kk = atomicAdd(&A.ctr->corrected, 1ull);
-                if (kk < A.corr_cap)
-                  A.corr_list[kk] = Corrected{uint32_t(gi), nd.cls,
-                                              (unsigned long long)nd.launch << kHeapBits | nd.heap};
-                else
-                  atomicOr(&A.ctr->overflow, kOvCorr);
-              }
-            }
-          }
-        }
-      }
-      __syncwarp();
-    }
-    __syncwarp();  // the next batch overwrites the staged records
-  }
-  for (int o = 16; o; o >>= 1) {
-    events += __shfl_xor_sync(FULL, events, o);
-    cand += __shfl_xor_sync(FULL, cand, o);
-    anc_tests += __shfl_xor_sync(FULL, anc_tests, o);
-    n64 += __shfl_xor_sync(FULL, n64, o);
-  }
-  if (lane == 0) {
-    if (events) atomicAdd(&A.ctr->events, events);
-    if (cand) atomicAdd(&A.ctr->cand, cand);
-    if (anc_tests) atomicAdd(&A.ctr->anc, anc_tests);
-    if (n64) atomicAdd(&A.ctr->fp64_capture, (unsigned long long)n64);
-  }
-}
-
-// The FP64 part of capture for the pairs k_capture could not settle in FP32:
-// the exact reception test where the FP32 one was unsure, then image
-// correction (MultiPathCorrection / DirectPathCorrection) and suppression by
-// an ancestor capturing the same receiver (RTSolver.cpp:277-284), as in
-// k_capture.  One thread per pair keeps the FP64 pipe busy with full warps.
-__global__ void __launch_bounds__(128) k_capture_finish(CaptureArgs A) {
-  if (A.ctr->overflow & (kOvTrace | kOvPairs)) return;  // this solve will be repeated
-  const unsigned long long n = min(A.ctr->pairs, A.pair_cap);
-  unsigned n64 = 0;
-  unsigned long long anc_tests = 0;
-  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
-       k += (unsigned long long)gridDim.x * blockDim.x) {
-    const uint2 pr = A.pairs[k];
-    const uint32_t i = pr.x;
-    const int gi = int(pr.y & 0x7fffffffu);
-    const NodeHot nd = A.nodes[i];
-    const TxParams& P = A.txp[nd.tx];
-    const double* c64 = A.rx + 3 * size_t(gi);
-    if (pr.y >> 31) {
-      ++n64;
-      if (!capture_exact(A.nodes_cold, i, c64, P.tan_beta)) continue;
-    }
-    const float3 c = make_float3(float(c64[0]), float(c64[1]), float(c64[2]));
-    const bool ok = is_root_class(nd.cls) ? A.direct_ok[gi] != 0
-                                          : correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
-    if (!ok) continue;
-    const float tanb = float(P.tan_beta);
-    bool sup = false;
-    for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
-      const NodeHot a = A.nodes[p];
-      ++anc_tests;
-      int w = reception32(make_float3(a.s[0], a.s[1], a.s[2]), make_float3(a.u[0], a.u[1], a.u[2]),
-                          a.len, a.S, c, tanb);
-      if (w < 0) {
-        ++n64;
-        w = capture_exact(A.nodes_cold, p, c64, P.tan_beta);
-      }
-      if (w) {
-        sup = true;
-        break;
-      }
-      p = a.parent;
-    }
-    if (sup) continue;
-    const unsigned long long kk = atomicAdd(&A.ctr->corrected, 1ull);
-    if (kk < A.corr_cap)
-      A.corr_list[kk] =
-          Corrected{uint32_t(gi), nd.cls, (unsigned long long)nd.launch << kHeapBits | nd.heap};
-    else
-      atomicOr(&A.ctr->overflow, kOvCorr);
-  }
-  for (int o = 16; o; o >>= 1) {
-    anc_tests += __shfl_xor_sync(0xffffffffu, anc_tests, o);
-    n64 += __shfl_xor_sync(0xffffffffu, n64, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (anc_tests) atomicAdd(&A.ctr->anc, anc_tests);
-    if (n64) atomicAdd(&A.ctr->fp64_capture, (unsigned long long)n64);
-  }
-}
-
-// ---- correction / dedup -----------------------------------------------------
-
-struct PathBuf {
-  int n;            // rays
-  int tri[kMaxDepth + 1];
-  int kind[kMaxDepth + 1];
-  double pts[kMaxDepth + 2][3];
-};
-
-// Path of a class: tri of each ray (ray i ends on tri[i]; the last ray ends at
-// the receiver) and kind of each ray's start.
-__device__ __forceinline__ bool class_path(const ClassInfo* info, uint32_t cls, PathBuf& pb) {
-  int depth = 0;
-  int tri_rev[kMaxDepth], kind_rev[kMaxDepth];
-  for (uint32_t c = cls; !is_root_class(c); c = info[c].parent) {
-    if (depth >= kMaxDepth) return false;
-    tri_rev[depth] = info[c].tri;
-    kind_rev[depth] = info[c].kind;
-    ++depth;
-  }
-  pb.n = depth + 1;
-  pb.kind[0] = 0;
-  for (int i = 0; i < depth; ++i) {
-    pb.tri[i] = tri_rev[depth - 1 - i];   // rank of the triangle hit by ray i
-    pb.kind[i + 1] = kind_rev[depth - 1 - i];
-  }
-  pb.tri[depth] = -1;
-  return true;
-}
-
-// GetImageSources + MultiPathCorrection / DirectPathCorrection
-// (RTSolver.cpp:330-433).  Fills pb.pts with the corrected points.
-__device__ bool correct_path(const DevScene& sc, const int* rank_to_id, const TxParams& P,
-                             const double* rxp, PathBuf& pb, unsigned* overflow) {
-  using namespace x64;
-  const double* tx = P.tx;
-  if (pb.n == 1) {
-    double d[3];
-    sub3(rxp, tx, d);
-    Hit h;
-    const bool has = exact_closest(sc, tx, d, h, overflow);
-    if (has && !(norm(d) < h.dist)) return false;
-    for (int a = 0; a < 3; ++a) {
-      pb.pts[0][a] = tx[a];
-      pb.pts[1][a] = rxp[a];
-    }
-    return true;
-  }
-  const int n = pb.n;
-  double img[kMaxDepth + 1][3];
-  for (int a = 0; a < 3; ++a) img[0][a] = tx[a];
-  for (int i = 0; i + 1 < n; ++i) {
-    const CorrTri& T = sc.corr[rank_to_id[pb.tri[i]]];
-    if (pb.kind[i + 1] == 1) {  // ImagePoint (RTSolver.cpp:910-924)
-      double w[3];
-      sub3(img[i], T.v1, w);
-      const double dist = dot(T.n, w);
-      for (int a = 0; a < 3; ++a) img[i + 1][a] = sub(img[i][a], mul(mul(2.0, dist), T.n[a]));
-    } else {
-      for (int a = 0; a < 3; ++a) img[i + 1][a] = img[i][a];
-    }
-  }
-  double target[3] = {rxp[0], rxp[1], rxp[2]};
-  for (int a = 0; a < 3; ++a) pb.pts[n][a] = rxp[a];
-  for (int i = n - 1; i >= 1; --i) {
-    const CorrTri& T = sc.corr[rank_to_id[pb.tri[i - 1]]];
-    double d[3], P3[3];
-    sub3(target, img[i], d);
-    if (!mt64c(T, img[i], d, P3)) return false;
-    for (int a = 0; a < 3; ++a) {
-      pb.pts[i][a] = P3[a];
-      target[a] = P3[a];
-    }
-  }
-  for (int a = 0; a < 3; ++a) pb.pts[0][a] = tx[a];
-  return true;
-}
-
-// DirectPathCorrection (RTSolver.cpp:375-394) once per receiver: the direct
-// path survives iff the reference-order BVH query from the transmitter along
-// (rx - tx) finds nothing closer than the receiver.
-__global__ void k_direct(DevScene sc, const TxParams* txp, const double* rx, const int* rx_req,
-                         int n_rx, unsigned char* ok, Counters* ctr) {
-  for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < n_rx; gi += gridDim.x * blockDim.x) {
-    const double* tx = txp[rx_req[gi]].tx;
-    const double* c = rx + 3 * size_t(gi);
-    double d[3];
-    x64::sub3(c, tx, d);
-    Hit h;
-    TraceStats st{0, 0};
-    const bool has = closest_hit(sc, tx, d, h, st, &ctr->overflow);
-    ok[gi] = (!has || x64::norm(d) < h.dist) ? 1 : 0;
-  }
-}
-
-// RemoveDuplicatePath (RTSolver.cpp:435-459): the first corrected path in
-// (launch, BFS) order wins each (receiver, coplanar key).
-__device__ __forceinline__ unsigned long long dedup_key(const ClassInfo* info, const Corrected& e) {
-  const uint32_t cop = is_root_class(e.cls) ? kRootClass : info[e.cls].cop;
-  return (unsigned long long)e.rx << 32 | cop;
-}
-
-__global__ void k_dedup(const Corrected* list, unsigned long long cap, const ClassInfo* info,
-                        HashTable dedup, unsigned long long* dedup_rank, Counters* ctr) {
-  const unsigned long long n = min(ctr->corrected, cap);
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    const Corrected e = list[i];
-    const uint32_t ds = ht_insert(dedup, dedup_key(info, e), &ctr->overflow, kOvDedup, &ctr->used_dd,
-                                &ctr->lost_dd);
-    if (ds != 0xFFFFFFFFu) atomicMin(&dedup_rank[ds], e.rank);
-  }
-}
-
-struct Survivor {
-  uint32_t cls, rx;
-  unsigned long long rank;
-};
-
-__global__ void k_select(const Corrected* list, unsigned long long cap, const ClassInfo* info,
-                         HashTable dedup, const unsigned long long* dedup_rank, Survivor* surv,
-                         unsigned long long surv_cap, Counters* ctr) {
-  const unsigned long long n = min(ctr->corrected, cap);
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    const Corrected e = list[i];
-    const uint32_t ds = ht_find(dedup, dedup_key(info, e));
-    if (ds == 0xFFFFFFFFu || dedup_rank[ds] != e.rank) continue;
-    const unsigned long long k = atomicAdd(&ctr->survivors, 1ull);
-    if (k < surv_cap) surv[k] = Survivor{e.cls, e.rx, e.rank};
-    else atomicOr(&ctr->overflow, kOvSurv);
-  }
-}
-
-// ---- field ---------------------------------------------------------------
-
-struct FieldArgs {
-  DevScene sc;
-  const TxParams* txp;
-  const double* rx;
-  const int* rx_req;
-  const ClassInfo* cls_info;
-  const int* rank_to_id;
-  const Survivor* surv;
-  Counters* ctr;
-  unsigned long long cap;
-  FieldConsts K;
-  int precision;        // -1: each request's own; 0: FP64 for all (the FP64 shadow)
-  double* path_field;   // 6 per survivor
-  int* path_nray;
-  int* path_tri;        // (kMaxDepth + 1) per survivor: triangle id
-  int* path_cop;
-  int* path_kind;
-  int* path_near_edge;  // 1 if an interaction point is within 1e-6 of its triangle's edge
-  double* path_pts;     // (kMaxDepth + 2) * 3 per survivor
-};
-
-// Barycentric distance of a point (on the triangle's plane) from the
-// triangle's edges is below tol: min(u, v, 1-u-v) < tol.
-__device__ __forceinline__ int near_edge(const CorrTri& T, const double* p, double tol) {
-  double w[3] = {p[0] - T.v1[0], p[1] - T.v1[1], p[2] - T.v1[2]};
-  const double d00 = T.e1[0] * T.e1[0] + T.e1[1] * T.e1[1] + T.e1[2] * T.e1[2];
-  const double d01 = T.e1[0] * T.e2[0] + T.e1[1] * T.e2[1] + T.e1[2] * T.e2[2];
-  const double d11 = T.e2[0] * T.e2[0] + T.e2[1] * T.e2[1] + T.e2[2] * T.e2[2];
-  const double d20 = w[0] * T.e1[0] + w[1] * T.e1[1] + w[2] * T.e1[2];
-  const double d21 = w[0] * T.e2[0] + w[1] * T.e2[1] + w[2] * T.e2[2];
-  const double den = d00 * d11 - d01 * d01;
-  if (!(den > 0)) return 1;
-  const double u = (d11 * d20 - d01 * d21) / den, v = (d00 * d21 - d01 * d20) / den;
-  return fmin(fmin(u, v), 1.0 - u - v) < tol ? 1 : 0;
-}
-
-__global__ void k_field(FieldArgs A) {
-  const unsigned long long ns = min(A.ctr->survivors, A.cap);
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    const Survivor sv = A.surv[i];
-    const uint32_t cls = sv.cls;
-    const TxParams& P = A.txp[A.rx_req[sv.rx]];
-    PathBuf pb;
-    class_path(A.cls_info, cls, pb);
-    correct_path(A.sc, A.rank_to_id, P, A.rx + 3 * size_t(sv.rx), pb, &A.ctr->overflow);
-    const double* frames[kMaxDepth + 1];
-    int mat[kMaxDepth + 1];
-    mat[0] = 0;
-    for (int r = 0; r < pb.n; ++r) {
-      frames[r] = pb.tri[r] >= 0 ? A.sc.corr[A.rank_to_id[pb.tri[r]]].cs : nullptr;
-      if (r + 1 < pb.n) mat[r + 1] = A.sc.tri64[pb.tri[r]].mat;
-    }
-    Cx<double> e[3];
-    const PatternTab pat{P.pat, P.pat_nt, P.pat_np, P.pat_dt, P.pat_dp};
-    const int prec = A.precision < 0 ? P.precision : A.precision;
-    if (prec == 2)
-      path_field<float, true>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq,
-                              P.pt, P.antenna, P.fresnel != 0, A.K, e, &pat);
-    else if (prec == 1)
-      path_field<float>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
-                        P.antenna, P.fresnel != 0, A.K, e, &pat);
-    else
-      path_field<double>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
-                         P.antenna, P.fresnel != 0, A.K, e, &pat);
-    for (int j = 0; j < 3; ++j) {
-      A.path_field[6 * i + 2 * j] = e[j].re;
-      A.path_field[6 * i + 2 * j + 1] = e[j].im;
-    }
-    A.path_nray[i] = pb.n;
-    const size_t b = size_t(i) * (kMaxDepth + 1);
-    for (int r = 0; r < pb.n; ++r) {
-      const int t = pb.tri[r];
-      A.path_tri[b + r] = t >= 0 ? A.rank_to_id[t] : -1;
-      A.path_cop[b + r] = t >= 0 ? A.sc.tri64[t].cop : -1;
-      A.path_kind[b + r] = pb.kind[r];
-    }
-    const size_t bp = size_t(i) * (kMaxDepth + 2) * 3;
-    for (int r = 0; r <= pb.n; ++r)
-      for (int a = 0; a < 3; ++a) A.path_pts[bp + 3 * r + a] = pb.pts[r][a];
-    // interaction point r+1 lies on the triangle the correction intersected
-    int near = 0;
-    for (int r = 0; r + 1 < pb.n; ++r)
-      near |= near_edge(A.sc.corr[A.rank_to_id[pb.tri[r]]], pb.pts[r + 1], 1e-6);
-    A.path_near_edge[i] = near;
-  }
-}
-
-// ---- per-receiver ordered sum -------------------------------------------
-
-__global__ void k_surv_hist(const Survivor* surv, const Counters* ctr, unsigned long long cap,
-                            int* counts) {
-  const unsigned long long ns = min(ctr->survivors, cap);
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
-       i += (unsigned long long)gridDim.x * blockDim.x)
-    atomicAdd(&counts[surv[i].rx], 1);
-}
-
-__global__ void k_surv_scatter(const Survivor* surv, const Counters* ctr, unsigned long long cap,
-                               const int* starts, int* cursor, int* order) {
-  const unsigned long long ns = min(ctr->survivors, cap);
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    const uint32_t r = surv[i].rx;
-    order[starts[r] + atomicAdd(&cursor[r], 1)] = int(i);
-  }
-}
-
-// Sort each receiver's survivors by (launch, BFS) rank and sum their fields in
-// that order: FP64, or compensated FP32 (Neumaier) for the FP32 precisions.
-// precision -1 takes each receiver's request precision, 0 forces FP64.
-__global__ void k_rx_sum(const Survivor* surv, const int* starts, int* order, int n_rx,
-                         const double* path_field, int force_precision, const int* rx_req,
-                         const TxParams* txp, double* field) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rx; r += gridDim.x * blockDim.x) {
-    const int precision = force_precision < 0 ? txp[rx_req[r]].precision : force_precision;
-    const int b = starts[r], e = starts[r + 1];
-    for (int i = b + 1; i < e; ++i) {
-      const int v = order[i];
-      const unsigned long long key = surv[v].rank;
-      int j = i - 1;
-      while (j >= b && surv[order[j]].rank > key) {
-        order[j + 1] = order[j];
-        --j;
-      }
-      order[j + 1] = v;
-    }
-    if (precision != 0) {  // both FP32 modes: compensated FP32 sum
-      float s[6] = {0, 0, 0, 0, 0, 0}, c[6] = {0, 0, 0, 0, 0, 0};
-      for (int i = b; i < e; ++i)
-        for (int k = 0; k < 6; ++k) {
-          const float x = float(path_field[6 * size_t(order[i]) + k]);
-          const float t = s[k] + x;
-          c[k] += fabsf(s[k]) >= fabsf(x) ? (s[k] - t) + x : (x - t) + s[k];
-          s[k] = t;
-        }
-      for (int k = 0; k < 6; ++k) field[6 * size_t(r) + k] = double(s[k]) + double(c[k]);
-    } else {
-      double s[6] = {0, 0, 0, 0, 0, 0};
-      for (int i = b; i < e; ++i)
-        for (int k = 0; k < 6; ++k) s[k] = __dadd_rn(s[k], path_field[6 * size_t(order[i]) + k]);
-      for (int k = 0; k < 6; ++k) field[6 * size_t(r) + k] = s[k];
-    }
-  }
 }
 
 // ============================================================ host side

@@ -1,0 +1,452 @@
+// Trace stage: the reference's RayLaunch (RTSolver.cpp:128-257) as a
+// wavefront, one bounce depth per launch pair: k_find (FP32 candidate search
+// on the search BVH) and k_trace (FP64 resolution against the reference BVH,
+// tree node, children, path-class interning).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+
+#include "sbr_device.h"
+#include "sbr_field.cuh"
+#include "sbr_kernels.cuh"
+#include "sbr_common.cuh"
+
+namespace sbr {
+
+// ---- trace ------------------------------------------------------------------
+
+struct TraceArgs {
+  DevScene sc;
+  const TxParams* txp;
+  int n_tx;
+  const double* const* dirs;  // per level
+  const RayRec* in;
+  RayRec* out;
+  unsigned long long out_cap;
+  NodeHot* nodes;
+  NodeCold* nodes_cold;
+  unsigned long long node_cap;
+  HashTable cls_tab, cop_tab;
+  ClassInfo* cls_info;
+  ClassCap* cls_cap;
+  const int* tri_cop;  // coplanar id by rank
+  Counters* ctr;
+  unsigned long long* seg_per_tx;  // executed segments per request
+  int depth;
+  long long n_root;    // total launches (depth 0)
+  long long lo, hi;    // this launch covers rays [lo, hi) of the depth
+  const uint2* cand;   // contenders of those rays (k_find)
+  const unsigned char* ncand;
+};
+
+__device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long long g) {
+  int lo = 0, hi = n_tx - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (txp[mid].launch_first <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// The capture-stage record of a class with image source img (FP64) whose
+// last ray starts on the triangle at mesh position tpos.
+__device__ void write_class_cap(const DevScene& sc, const double* img, int tpos, ClassCap& cc) {
+  const Tri32 T = sc.corr32[tpos];
+  const float3 o = make_float3(float(img[0]), float(img[1]), float(img[2]));
+  const float no = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
+  const TriFrom F = tri_from(T, o, no);
+  cc.img[0] = o.x;
+  cc.img[1] = o.y;
+  cc.img[2] = o.z;
+  cc.tpos = tpos;
+  cc.F[0] = F.sx; cc.F[1] = F.sy; cc.F[2] = F.sz;
+  cc.F[3] = F.qx; cc.F[4] = F.qy; cc.F[5] = F.qz;
+  cc.F[6] = F.W; cc.F[7] = F.ns;
+  float v[3][3];
+  for (int a = 0; a < 3; ++a) {
+    v[0][a] = T.v1[a];
+    v[1][a] = T.v1[a] + T.e1[a];
+    v[2][a] = T.v1[a] + T.e2[a];
+  }
+  const float im[3] = {o.x, o.y, o.z};
+  const float g[3] = {(v[0][0] + v[1][0] + v[2][0]) / 3.0f, (v[0][1] + v[1][1] + v[2][1]) / 3.0f,
+                      (v[0][2] + v[1][2] + v[2][2]) / 3.0f};
+  const float tmag = no + T.nv1 + T.ne1 + T.ne2 + 1.0f;
+  for (int k = 0; k < 3; ++k) {
+    const float* p = v[k];
+    const float* q = v[k == 2 ? 0 : k + 1];
+    const float a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
+    const float b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
+    const float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                        a[0] * b[1] - a[1] * b[0]};
+    const float nn = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    // orient towards the triangle's centroid, which lies inside the cone
+    const float gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
+    const float sg = gc > 0.0f ? 1.0f : -1.0f;
+    for (int c = 0; c < 3; ++c) cc.n[k][c] = sg * n[c];
+    cc.n[k][3] = sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]);
+    cc.nn[k] = nn;
+    cc.w[k] = nn * tmag;
+    cc.gc[k] = fabsf(gc);
+    cc.inv_nx[k] = 1.0f / (sg * n[0]);
+  }
+}
+
+// Every thread that interns a class writes the same values (they depend
+// only on the key), so concurrent writers agree.
+__device__ __forceinline__ void write_class(ClassInfo& ci, const double* img, uint32_t parent,
+                                            int tri, uint32_t cop, int kind, int depth) {
+  ci.img[0] = img[0];
+  ci.img[1] = img[1];
+  ci.img[2] = img[2];
+  ci.img32[0] = float(img[0]);
+  ci.img32[1] = float(img[1]);
+  ci.img32[2] = float(img[2]);
+  ci.parent = parent;
+  ci.tri = tri;
+  ci.cop = cop;
+  ci.kind = uint8_t(kind);
+  ci.depth = uint8_t(depth);
+  ci.pad0 = ci.pad1 = 0;
+  ci.pad2 = 0;
+}
+
+// Number of rays entering bounce depth `depth` (known on the device only).
+__device__ __forceinline__ long long rays_at_depth(const Counters* ctr, int depth, long long n_root,
+                                                   unsigned long long cap) {
+  return depth == 0 ? n_root : (long long)min(ctr->queue[depth], cap);
+}
+
+// Launch ray g of the batch: origin and direction (FP64).
+__device__ __forceinline__ void root_ray(const TxParams* txp, int n_tx, const double* const* dirs,
+                                         long long g, double* o, double* d, int& q, long long& li) {
+  q = find_request(txp, n_tx, g);
+  const TxParams& P = txp[q];
+  li = g - P.launch_first;
+  const double* dd = dirs[P.level] + 3 * li;
+  for (int a = 0; a < 3; ++a) {
+    o[a] = P.tx[a];
+    d[a] = dd[a];
+  }
+}
+
+// ---- FP32 candidate search (persistent, rays refilled per warp) ----------
+//
+// Each lane traverses one ray at a time.  Lanes whose ray is finished take a
+// new one from the chunk's work counter (one atomic per warp, when at least
+// a quarter of the warp is idle or nobody is busy), so warps stay full while
+// rays of very different lengths finish at different times.
+struct FindArgs {
+  DevScene sc;
+  const TxParams* txp;
+  int n_tx;
+  const double* const* dirs;
+  const RayRec* in;
+  const Counters* ctr;
+  unsigned long long in_cap;
+  long long n_root;
+  int depth;
+  long long lo, hi;            // this launch covers rays [lo, hi) of the depth
+  unsigned long long* work;    // rays of the chunk handed out (zero at launch)
+  uint2* cand;                 // kCand per ray of the chunk
+  unsigned char* ncand;        // contenders per ray, kFindFallback = exact traversal
+};
+
+constexpr int kFindSteps = 16;  // traversal steps between refills
+
+__global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
+  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
+  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.in_cap);
+  const long long n = min(n_all, A.hi) - A.lo;
+  if (n <= 0) return;
+  const unsigned lane = lane_id();
+  long long ray = -1;
+  bool exhausted = false;
+  float3 o32 = make_float3(0, 0, 0), d32 = o32, inv = o32;
+  float no = 0.0f, nd = 0.0f, m = 0.0f, tcut = INFINITY;
+  int stack[kStack];
+  int sp = 0, pending = -1, nc = 0;
+  bool fail = false;
+  uint2* out = nullptr;
+  while (true) {
+    const bool idle = ray < 0 && !exhausted;
+    const unsigned im = __ballot_sync(0xffffffffu, idle);
+    const unsigned busy = __ballot_sync(0xffffffffu, ray >= 0);
+    if (im && (__popc(im) >= 8 || busy == 0)) {
+      const int leader = __ffs(im) - 1;
+      unsigned long long base = 0;
+      if (int(lane) == leader) base = atomicAdd(A.work, (unsigned long long)__popc(im));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (idle) {
+        const long long k = (long long)base + __popc(im & ((1u << lane) - 1u));
+        if (k < n) {
+          ray = k;
+          double o[3], d[3];
+          if (A.depth == 0) {
+            int q;
+            long long li;
+            root_ray(A.txp, A.n_tx, A.dirs, A.lo + k, o, d, q, li);
+          } else {
+            const RayRec& r = A.in[A.lo + k];
+            for (int a = 0; a < 3; ++a) {
+              o[a] = r.o[a];
+              d[a] = r.d[a];
+            }
+          }
+          o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
+          d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
+          inv = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
+          no = sqrtf(o32.x * o32.x + o32.y * o32.y + o32.z * o32.z);
+          nd = sqrtf(d32.x * d32.x + d32.y * d32.y + d32.z * d32.z);
+          m = A.sc.box_margin + kFiltK * no;
+          tcut = INFINITY;
+          sp = 0;
+          pending = -1;
+          nc = 0;
+          fail = false;
+          stack[sp++] = 0;  // the search root is always a node
+          out = A.cand + size_t(k) * kCand;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, ray >= 0) == 0) {
+      if (__all_sync(0xffffffffu, exhausted)) break;
+      continue;
+    }
+    if (ray < 0) continue;
+    bool done = false;
+    for (int it = 0; it < kFindSteps && !done; ++it) {
+      if (pending >= 0) {
+        const int first = pending >> 3, last = first + (pending & 7);
+        for (int j = first; j < last; ++j) {
+          float tlo, thi;
+          const int k = tri_classify(A.sc.stri[j], o32, d32, no, nd, tlo, thi);
+          if (k == 0 || tlo > tcut) continue;
+          if (nc == kCand) {
+            fail = true;
+            break;
+          }
+          out[nc++] = make_uint2(unsigned(__ldg(A.sc.srank + j)), __float_as_uint(tlo));
+          if (k == 2) tcut = fminf(tcut, thi * (1.0f + 1.0f / 4096.0f) + 1e-30f);
+        }
+        pending = -1;
+        if (fail) done = true;
+        continue;
+      }
+      if (sp == 0) {
+        done = true;
+        break;
+      }
+      const int ni = stack[--sp];
+      if (ni < 0) {  // a leaf deferred as the farther child
+        pending = ~ni;
+        continue;
+      }
+      float4 f0, f1, f2;
+      int2 ch;
+      load_node(A.sc.snode, ni, f0, f1, f2, ch);
+      float tn0, tf0, tn1, tf1;
+      slab32(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, o32, inv, m, tn0, tf0);
+      slab32(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, o32, inv, m, tn1, tf1);
+      const bool h0 = tn0 <= tf0 && tf0 >= 0.0f && tn0 <= tcut;
+      const bool h1 = tn1 <= tf1 && tf1 >= 0.0f && tn1 <= tcut;
+      int first = 0, second = 0;
+      bool has_first = false, has_second = false;
+      if (h0 && h1) {
+        has_first = has_second = true;
+        if (tn1 < tn0) {
+          first = ch.y;
+          second = ch.x;
+        } else {
+          first = ch.x;
+          second = ch.y;
+        }
+      } else if (h0) {
+        has_first = true;
+        first = ch.x;
+      } else if (h1) {
+        has_first = true;
+        first = ch.y;
+      }
+      if (has_second) {
+        if (sp >= kStack) {
+          fail = done = true;
+          break;
+        }
+        stack[sp++] = second;  // node, or ~leaf code
+      }
+      if (has_first) {
+        if (first < 0) {
+          pending = ~first;
+        } else {
+          if (sp >= kStack) {
+            fail = done = true;
+            break;
+          }
+          stack[sp++] = first;
+        }
+      }
+    }
+    if (done) {
+      A.ncand[ray] = fail ? kFindFallback : (unsigned char)nc;
+      ray = -1;
+    }
+  }
+}
+
+// Resident blocks of k_trace per SM (register budget 65536 / (128 x this)).
+#ifndef SBR_TRACE_BLOCKS
+#define SBR_TRACE_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
+  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
+  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
+  const long long n_in = min(n_all, A.hi);
+  TraceStats st{0, 0};
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = A.lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in;
+       i += stride) {
+    RayRec r;
+    if (A.depth == 0) {
+      int q;
+      long long li;
+      root_ray(A.txp, A.n_tx, A.dirs, i, r.o, r.d, q, li);
+      r.total = 0.0;
+      r.S = 0.0;
+      r.parent = 0xFFFFFFFFu;
+      r.cls = kRootBase + uint32_t(q);
+      r.cop = kRootClass;
+      r.launch = uint32_t(li);
+      r.heap = 1;
+      r.rc = r.tc = 0;
+      r.tx = uint32_t(q);
+    } else {
+      r = A.in[i];
+    }
+    const TxParams& P = A.txp[r.tx];
+    Hit h;
+    const long long c = i - A.lo;
+    const bool hit = resolve_hit(A.sc, r.o, r.d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
+                                 &A.ctr->overflow);
+    const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
+    {  // per-request segment count, one atomic per request present in the warp
+      const unsigned peers = __match_any_sync(__activemask(), r.tx);
+      if (int(lane_id()) == __ffs(peers) - 1)
+        atomicAdd(&A.seg_per_tx[r.tx], (unsigned long long)__popc(peers));
+    }
+    const bool root = A.depth == 0;
+    if (ni < A.node_cap) {
+      NodeCold n;
+      NodeHot m;
+      n.s[0] = r.o[0]; n.s[1] = r.o[1]; n.s[2] = r.o[2];
+      if (hit) {
+        n.t[0] = h.p[0]; n.t[1] = h.p[1]; n.t[2] = h.p[2];
+        m.len = float(h.dist);
+      } else {
+        const double sc = root ? 1E10 : 1E2;  // RTSolver.cpp:231,249
+        n.t[0] = x64::add(r.o[0], x64::mul(r.d[0], sc));
+        n.t[1] = x64::add(r.o[1], x64::mul(r.d[1], sc));
+        n.t[2] = x64::add(r.o[2], x64::mul(r.d[2], sc));
+        m.len = float(sc);
+      }
+      n.S = r.S;
+      n.pad = 0.0;
+      m.s[0] = float(r.o[0]); m.s[1] = float(r.o[1]); m.s[2] = float(r.o[2]);
+      m.S = float(r.S);
+      m.u[0] = float(r.d[0]); m.u[1] = float(r.d[1]); m.u[2] = float(r.d[2]);
+      m.parent = r.parent;
+      m.cls = r.cls;
+      m.launch = r.launch;
+      m.heap = r.heap;
+      m.tx = r.tx;
+      m.pad0 = m.pad1 = m.pad2 = 0;
+      A.nodes_cold[ni] = n;
+      A.nodes[ni] = m;
+    } else {
+      atomicOr(&A.ctr->overflow, kOvNodes);
+    }
+    // children (RTSolver.cpp:186-221)
+    unsigned nch = 0;
+    bool do_r = false, do_t = false;
+    if (hit) {
+      do_r = r.rc < P.R;
+      do_t = r.tc < P.T;
+      nch = unsigned(do_r) + unsigned(do_t);
+    }
+    const unsigned long long base = warp_reserve(&A.ctr->queue[A.depth + 1], nch);
+    if (nch) {
+      const Tri64& T = A.sc.tri64[h.rank];
+      const double cum = x64::add(r.total, h.dist);  // node pathLength
+      RayRec c;
+      c.o[0] = h.p[0]; c.o[1] = h.p[1]; c.o[2] = h.p[2];
+      c.total = cum;
+      c.S = x64::add(r.S, cum);
+      c.parent = uint32_t(ni);
+      c.launch = r.launch;
+      c.tx = r.tx;
+      c.pad = 0;
+      const int cop = A.tri_cop[h.rank];
+      const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
+      const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop,
+                                           &A.ctr->lost_cop);
+      // image source of the parent ray's class (the transmitter for a launch)
+      const double* pimg = is_root_class(r.cls) ? P.tx : A.cls_info[r.cls].img;
+      unsigned long long slot = base;
+      if (do_t) {  // transmitted: same direction, heap 2h, same image source
+        c.d[0] = r.d[0]; c.d[1] = r.d[1]; c.d[2] = r.d[2];
+        c.heap = r.heap * 2;
+        c.rc = r.rc;
+        c.tc = r.tc + 1;
+        const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
+        bool fresh = false;
+        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
+                          &A.ctr->lost_cls, &fresh);
+        c.cop = cop_cls;
+        if (fresh) {  // only the thread that interned the class writes its records
+          write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
+          write_class_cap(A.sc, pimg, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
+        }
+        if (slot < A.out_cap) A.out[slot] = c;
+        else atomicOr(&A.ctr->overflow, kOvQueue);
+        ++slot;
+      }
+      if (do_r) {  // reflected: Reflect(d, n).normalized(), heap 2h+1
+        const double dn = x64::dot(T.n, r.d);
+        double v[3];
+        for (int a = 0; a < 3; ++a) v[a] = x64::sub(r.d[a], x64::mul(x64::mul(2.0, T.n[a]), dn));
+        x64::normalize(v, c.d);
+        c.heap = r.heap * 2 + 1;
+        c.rc = r.rc + 1;
+        c.tc = r.tc;
+        const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1);
+        bool fresh = false;
+        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
+                          &A.ctr->lost_cls, &fresh);
+        c.cop = cop_cls;
+        if (fresh) {  // only the thread that interned the class writes its records
+          // ImagePoint (RTSolver.cpp:910-924) across the triangle the
+          // reference finds at this id's position of its mesh vector
+          const CorrTri& M = A.sc.corr[A.sc.rank_to_id[h.rank]];
+          double w[3], img[3];
+          x64::sub3(pimg, M.v1, w);
+          const double dist = x64::dot(M.n, w);
+          for (int a = 0; a < 3; ++a) img[a] = x64::sub(pimg[a], x64::mul(x64::mul(2.0, dist), M.n[a]));
+          write_class(A.cls_info[c.cls], img, r.cls, h.rank, cop_cls, 1, A.depth + 1);
+          write_class_cap(A.sc, img, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
+        }
+        if (slot < A.out_cap) A.out[slot] = c;
+        else atomicOr(&A.ctr->overflow, kOvQueue);
+      }
+    }
+  }
+  if (st.fp64_tri) atomicAdd(&A.ctr->fp64_tri, (unsigned long long)st.fp64_tri);
+  if (st.fallback) atomicAdd(&A.ctr->fallback, (unsigned long long)st.fallback);
+}
+
+}  // namespace sbr
