@@ -38,6 +38,7 @@ struct CaptureArgs {
   int stage_counts;
   uint2* pairs;                // (node, receiver | unsure << 31) for k_capture_finish
   unsigned long long pair_cap;
+  unsigned long long* work;    // nodes handed out to warps (zero at launch)
 };
 
 // MultiPathCorrection (RTSolver.cpp:330-373) for one capture, walking the
@@ -266,6 +267,14 @@ __device__ __forceinline__ ChunkBox chunk_box(const NodeHot& nd, const RxGrid& g
   return cb;
 }
 
+// Next batch of `b` nodes for the calling warp (all lanes get the same base).
+__device__ __forceinline__ unsigned long long next_batch(unsigned long long* work, int lane,
+                                                         int b) {
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(work, (unsigned long long)b);
+  return __shfl_sync(0xffffffffu, base, 0);
+}
+
 // kStage: stage counts requested (every capture counted, the plain order of
 // tests); otherwise the fast path with the correction prefilter and the
 // deferred FP64 pass.
@@ -278,7 +287,6 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
   const unsigned long long n_nodes = min(A.ctr->nodes, A.node_cap);
   unsigned long long events = 0, cand = 0, anc_tests = 0;
   unsigned n64 = 0;
-  const unsigned long long nw = (unsigned long long)gridDim.x * kCapWarps;
   // Nodes are taken 32 at a time: each lane loads one node's record, its
   // class record and last triangle, so the three dependent loads are paid
   // once per 32 nodes; the warp then works through the 32 from shared memory.
@@ -289,8 +297,10 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(Capt
   __shared__ float s_cn[kCapWarps][B][16];  // loosened correction cone
   __shared__ NodeSpan s_sp[kCapWarps][B];   // clipped span and chunking
   __shared__ ChunkBox s_ck[kCapWarps][B];   // the span's first chunk
-  for (unsigned long long base = ((unsigned long long)blockIdx.x * kCapWarps + warp) * B;
-       base < n_nodes; base += nw * B) {
+  // Batches of B nodes are handed out by a work counter, one atomic per warp
+  // and batch, so warps that drew short segments take more batches.
+  for (unsigned long long base = next_batch(A.work, lane, B); base < n_nodes;
+       base = next_batch(A.work, lane, B)) {
     {
       const unsigned long long my = base + lane;
       if (lane < B && my < n_nodes) {

@@ -474,6 +474,18 @@ static int find_grid() {
   return g;
 }
 
+// Capture grid: every block resident at once (the work counter balances).
+static int capture_grid() {
+  static int g = [] {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_capture<false>, 32 * kCapWarps, 0);
+    return std::max(1, sms) * std::max(1, per_sm);
+  }();
+  return g;
+}
+
 static int grid_for(long long n, int block) {
   int dev_sms = 152;
   long long g = (n + block - 1) / block;
@@ -749,13 +761,15 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ca.stage_counts = stage_counts;
     ca.pairs = W.pairs.p;
     ca.pair_cap = W.cap_pairs;
+    ca.work = W.find_work.p;  // the trace is done with it
+    CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
     if (rx_total)
       ++nl, k_direct<<<grid_for(rx_total, 64), 64, 0, st>>>(S.dev, W.txp.p, W.rx.p, W.rx_req.p, rx_total,
                                                       W.direct_ok.p, W.ctr.p);
     if (stage_counts) {
-      ++nl, k_capture<true><<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
+      ++nl, k_capture<true><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
     } else {
-      ++nl, k_capture<false><<<152 * 32, 32 * kCapWarps, 0, st>>>(ca);
+      ++nl, k_capture<false><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
       ++nl, k_capture_finish<<<152 * 16, 128, 0, st>>>(ca);
     }
     CK(cudaGetLastError());
