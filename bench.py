@@ -34,6 +34,9 @@ NODE_BYTES = 96      # NodeRec
 RAY_BYTES = 96       # RayRec
 SEGMENT_BYTES = 84   # algorithmic bytes per executed segment (trace)
 EVENT_BYTES = 16     # per capture event (group-table rank + count update)
+# DRAM bytes (read + write) per segment of the level-9 urban solve, measured
+# with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass, timed solve)
+TRAFFIC_PER_SEGMENT = {"k_capture": 2183.7e6 / 29924326, "k_trace": 11014.8e6 / 29924326}
 
 
 def _env_int(k, d):
@@ -473,9 +476,13 @@ def main():
         if cap_ms >= tr_ms:
             kern, ms = "k_capture", cap_ms
             alg = n_nodes * NODE_BYTES + captured * EVENT_BYTES
+            traffic = TRAFFIC_PER_SEGMENT["k_capture"] * n_nodes
         else:
             kern, ms = "k_trace", tr_ms / (depth + 1)
             alg = n_nodes * SEGMENT_BYTES / (depth + 1)
+            traffic = TRAFFIC_PER_SEGMENT["k_trace"] * n_nodes / (depth + 1)
+        if wl.name != "urban_L9_R6T1":
+            traffic = None  # measured for the level-9 workload only
         achieved = alg / (ms / 1e3) / 1e9
         launches_per_step = counts["gpu_kernels"]  # counted by the library
         line = {
@@ -500,7 +507,8 @@ def main():
                     "ms_per_step": 1e3 * max_e2e / steps},
             "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "algorithmic_bytes_per_launch": alg,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": alg,
+                         "traffic_frac": (traffic / (ms / 1e3) / 1e9 / peak) if traffic else None,
                          "launch_ms": ms},
             "gpu_launches": launches_per_step * steps,
             "clocks": clocks,
