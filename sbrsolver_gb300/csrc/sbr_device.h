@@ -111,7 +111,7 @@ struct __align__(16) RayRec {
   uint32_t heap;   // BFS heap index (root 1, transmit child 2h, reflect child 2h+1)
   uint16_t rc, tc;
   uint32_t tx;     // transmitter (request) index
-  uint32_t pad;
+  int orank;       // depth-first rank of the triangle the ray starts on, -1 for a launch
 };
 
 // One executed segment (tree node), split in two arrays: the FP32 part the

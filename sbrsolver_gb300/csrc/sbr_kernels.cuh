@@ -505,9 +505,27 @@ constexpr int kCand = 8;
 constexpr unsigned char kFindFallback = 0xFF;
 
 // Resolution of a ray's contenders (rank, FP32 t lower bound as bits).
+// Whether the reference's test of the triangle a ray starts on certainly
+// fails (so its FP64 test can be skipped).  The ray's origin is the hit
+// point the parent ray's FP64 test produced on that triangle, within about
+// 1e-15 |P| of its plane; leaving at |cos| >= 1e-2 the reference's t for it
+// is then below 1e-10 for |P| < 1e5, far under the t > FLT_EPSILON it
+// requires (Triangle.cpp:113).
+__device__ __forceinline__ bool origin_rejected(const Tri32& T, const double* o, const double* d) {
+  const float ox = float(o[0]), oy = float(o[1]), oz = float(o[2]);
+  if (!(fabsf(ox) < 1e5f && fabsf(oy) < 1e5f && fabsf(oz) < 1e5f)) return false;
+  const float nx = T.e1[1] * T.e2[2] - T.e1[2] * T.e2[1];
+  const float ny = T.e1[2] * T.e2[0] - T.e1[0] * T.e2[2];
+  const float nz = T.e1[0] * T.e2[1] - T.e1[1] * T.e2[0];
+  const float dx = float(d[0]), dy = float(d[1]), dz = float(d[2]);
+  const float dn = dx * nx + dy * ny + dz * nz;
+  const float nn = sqrtf(nx * nx + ny * ny + nz * nz), dd = sqrtf(dx * dx + dy * dy + dz * dz);
+  return fabsf(dn) >= 1e-2f * nn * dd;
+}
+
 __device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d,
                             const uint2* cand, int nc, Hit& best, TraceStats& st,
-                            unsigned* overflow) {
+                            unsigned* overflow, int orank = -1) {
   if (nc == kFindFallback)  // more contenders than kept, or a deep stack: one-pass search
     return closest_hit(sc, o, d, best, st, overflow);
   int cr[kCand];
@@ -530,6 +548,7 @@ __device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d
   for (int i = 0; i < nc; ++i) {
     if (best.rank != INT_MAX && ct[i] > float(best.t) * (1.0f + 1.0f / 4096.0f) + 1e-30f) break;
     const int r = cr[i];
+    if (r == orank && origin_rejected(sc.tri32[r], o, d)) continue;
     ++st.fp64_tri;
     double t, P[3], dist;
     if (mt64(sc.tri64[r], o, d, t, P, dist) &&

@@ -320,6 +320,7 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
       r.total = 0.0;
       r.S = 0.0;
       r.parent = 0xFFFFFFFFu;
+      r.orank = -1;
       r.cls = kRootBase + uint32_t(q);
       r.cop = kRootClass;
       r.launch = uint32_t(li);
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
     Hit h;
     const long long c = i - A.lo;
     const bool hit = resolve_hit(A.sc, r.o, r.d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
-                                 &A.ctr->overflow);
+                                 &A.ctr->overflow, r.orank);
     const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
     {  // per-request segment count, one atomic per request present in the warp
       const unsigned peers = __match_any_sync(__activemask(), r.tx);
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
       c.parent = uint32_t(ni);
       c.launch = r.launch;
       c.tx = r.tx;
-      c.pad = 0;
+      c.orank = h.rank;
       const int cop = A.tri_cop[h.rank];
       const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
       const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop,
