@@ -278,8 +278,12 @@ __device__ __forceinline__ unsigned long long next_batch(unsigned long long* wor
 // kStage: stage counts requested (every capture counted, the plain order of
 // tests); otherwise the fast path with the correction prefilter and the
 // deferred FP64 pass.
+// Resident blocks per SM of the fast path (register budget 65536 / (128 x this)).
+#ifndef SBR_CAP_BLOCKS
+#define SBR_CAP_BLOCKS 6
+#endif
 template <bool kStage>
-__global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : 5) k_capture(CaptureArgs A) {
+__global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k_capture(CaptureArgs A) {
   __shared__ AncRec anc[kCapWarps][kMaxDepth];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
