@@ -82,16 +82,13 @@ __device__ __noinline__ int capture_exact(const NodeCold* cold, uint32_t idx, co
   return reception64(n.s, n.t, c64, n.S, tanb) ? 1 : 0;
 }
 
-// One warp per tree node.  The receivers that can fall inside the node's
-// reception spheres lie within rb of its segment (rb bounds the sphere radius
-// (S + |P|) tan(beta), with |P| <= (cmax + S tan b) / (1 - tan b) for any
-// capturing point); the segment is clipped to that region and cut into
-// chunks (each receiver is owned by the chunk its projection falls in).  Each
-// chunk's capsule is rasterised over the receiver grid one row of cells per
-// lane; a row is one contiguous run of receivers, and the lanes stride over
-// the concatenation of the rows' runs.  A capture counts unless an ancestor
-// of the node captures the same receiver (RTSolver.cpp:277-284); ancestors
-// come from shared memory.
+// A warp works through batches of nodes.  Each node's segment is clipped to
+// the region that can hold its captures and cut into chunks (each receiver is
+// owned by the chunk its projection falls in); each chunk's capsule is
+// rasterised over the receiver grid one row of cells per lane; a row is one
+// contiguous run of receivers, and the lanes stride over the concatenation of
+// the rows' runs.  A capture counts unless an ancestor of the node captures
+// the same receiver (RTSolver.cpp:277-284).
 constexpr int kCapWarps = 4;
 // Minimum chunk length along a segment, in receiver-grid cells.
 #ifndef SBR_CAP_CHUNK_CELLS
