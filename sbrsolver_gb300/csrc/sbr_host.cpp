@@ -5,16 +5,20 @@
 #include "sbr_host.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <limits>
 #include <numeric>
 #include <sstream>
+#include <thread>
 #include <unordered_map>
+#include <utility>
 
 namespace sbr {
 namespace {
@@ -91,10 +95,19 @@ int sah_split(const std::vector<HostTri>& tris, std::vector<int>& objs, double* 
   const double sa_root = surface_area(bb);
   sa1.assign(size_t(n) + 1, std::numeric_limits<double>::max());
   sa2.assign(size_t(n) + 1, std::numeric_limits<double>::max());
+  // std::sort's result depends only on the outcomes of its comparisons, so
+  // sorting (key, id) pairs by key leaves the ids in exactly the order the
+  // reference's sort of ids by tris[id].center[axis] does, with the keys at
+  // hand instead of behind an indirection.
+  std::vector<std::pair<double, int>> kv(objs.size());
+  auto sort_axis = [&](int axis) {
+    for (size_t i = 0; i < objs.size(); ++i) kv[i] = {tris[objs[i]].center[axis], objs[i]};
+    std::sort(kv.begin(), kv.end(), [](const std::pair<double, int>& a,
+                                       const std::pair<double, int>& b) { return a.first < b.first; });
+    for (size_t i = 0; i < objs.size(); ++i) objs[i] = kv[i].second;
+  };
   for (int axis = 0; axis < 3; ++axis) {
-    std::sort(objs.begin(), objs.end(), [&tris, axis](int a, int b) {
-      return tris[a].center[axis] < tris[b].center[axis];
-    });
+    sort_axis(axis);
     double b1[6];
     empty_box(b1);
     sa1[0] = surface_area(b1);
@@ -120,9 +133,7 @@ int sah_split(const std::vector<HostTri>& tris, std::vector<int>& objs, double* 
     }
   }
   if (best_axis == -1) return -1;
-  std::sort(objs.begin(), objs.end(), [&tris, best_axis](int a, int b) {
-    return tris[a].center[best_axis] < tris[b].center[best_axis];
-  });
+  sort_axis(best_axis);
   return best_split;
 }
 
@@ -314,41 +325,110 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
     out.tris[t].cop = comp[r];
   }
 
-  // SAH BVH with the reference's splits; nodes renumbered depth-first.
+  // SAH BVH with the reference's splits; nodes renumbered depth-first.  Every
+  // node's split depends only on its own object list, so the tree does not
+  // depend on the order nodes are split in: nodes above a size threshold are
+  // split here, the subtrees below it in parallel, then merged.
   std::vector<BuildNode> bn;
   bn.reserve(size_t(2) * nt);
   bn.emplace_back();
   bn[0].objs.resize(nt);
   std::iota(bn[0].objs.begin(), bn[0].objs.end(), 0);
-  std::vector<double> sa1, sa2;
-  std::vector<int> work{0};
-  bool root_done = false;
-  while (!work.empty()) {
-    int idx = work.back();
-    work.pop_back();
-    std::vector<int> objs;
-    objs.swap(bn[idx].objs);
-    double bb[6];
-    int split = sah_split(out.tris, objs, bb, sa1, sa2);
-    std::memcpy(bn[idx].bb, bb, sizeof bb);
-    if (!root_done) {
-      out.mesh_order = objs;  // the caller's vector after ConstructBVH
-      root_done = true;
+  const size_t big = std::max<size_t>(4096, size_t(nt) / 64);
+  const unsigned nthreads =
+      std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
+  // runs f(0..n-1) on up to nthreads threads
+  auto parallel_for = [nthreads](size_t n, const std::function<void(size_t)>& f) {
+    std::atomic<size_t> next{0};
+    auto run = [&]() {
+      for (size_t k = next++; k < n; k = next++) f(k);
+    };
+    std::vector<std::thread> pool;
+    for (unsigned i = 1; i < nthreads && i < n; ++i) pool.emplace_back(run);
+    run();
+    for (auto& t : pool) t.join();
+  };
+  std::vector<int> subtrees;  // roots left to the parallel subtree phase
+  {
+    // the large nodes level by level, the nodes of a level split in parallel
+    std::vector<int> frontier{0};
+    while (!frontier.empty()) {
+      std::vector<int> split(frontier.size());
+      parallel_for(frontier.size(), [&](size_t k) {
+        std::vector<double> sa1, sa2;
+        BuildNode& b = bn[frontier[k]];
+        split[k] = sah_split(out.tris, b.objs, b.bb, sa1, sa2);
+      });
+      if (frontier[0] == 0) out.mesh_order = bn[0].objs;  // the caller's vector after ConstructBVH
+      std::vector<int> next;
+      for (size_t k = 0; k < frontier.size(); ++k) {
+        const int idx = frontier[k];
+        if (split[k] < 0) continue;  // a leaf keeps its objects
+        int c0 = int(bn.size());
+        bn.emplace_back();
+        int c1 = int(bn.size());
+        bn.emplace_back();
+        bn[idx].c0 = c0;
+        bn[idx].c1 = c1;
+        std::vector<int>& objs = bn[idx].objs;
+        bn[c0].objs.assign(objs.begin(), objs.begin() + split[k]);
+        bn[c1].objs.assign(objs.begin() + split[k], objs.end());
+        std::vector<int>().swap(objs);
+        for (int c : {c0, c1}) (bn[c].objs.size() >= big ? next : subtrees).push_back(c);
+      }
+      frontier.swap(next);
     }
-    if (split < 0) {
-      bn[idx].objs.swap(objs);
-      continue;
+  }
+  {
+    // each subtree into its own node list (local index 0 = the subtree root)
+    std::vector<std::vector<BuildNode>> local(subtrees.size());
+    parallel_for(subtrees.size(), [&](size_t k) {
+      std::vector<double> sa1, sa2;
+      {
+        std::vector<BuildNode>& ln = local[k];
+        ln.emplace_back();
+        ln[0].objs.swap(bn[subtrees[k]].objs);
+        std::vector<int> work{0};
+        while (!work.empty()) {
+          int idx = work.back();
+          work.pop_back();
+          std::vector<int> objs;
+          objs.swap(ln[idx].objs);
+          double bb[6];
+          int split = sah_split(out.tris, objs, bb, sa1, sa2);
+          std::memcpy(ln[idx].bb, bb, sizeof bb);
+          if (split < 0) {
+            ln[idx].objs.swap(objs);
+            continue;
+          }
+          int c0 = int(ln.size());
+          ln.emplace_back();
+          int c1 = int(ln.size());
+          ln.emplace_back();
+          ln[idx].c0 = c0;
+          ln[idx].c1 = c1;
+          ln[c0].objs.assign(objs.begin(), objs.begin() + split);
+          ln[c1].objs.assign(objs.begin() + split, objs.end());
+          work.push_back(c1);
+          work.push_back(c0);
+        }
+      }
+    });
+    for (size_t k = 0; k < subtrees.size(); ++k) {
+      std::vector<BuildNode>& ln = local[k];
+      const int off = int(bn.size()) - 1;  // local j >= 1 goes to bn[off + j]
+      auto map = [&](int c) { return c < 0 ? -1 : (c == 0 ? subtrees[k] : off + c); };
+      for (size_t j = 1; j < ln.size(); ++j) {
+        ln[j].c0 = map(ln[j].c0);
+        ln[j].c1 = map(ln[j].c1);
+        bn.push_back(std::move(ln[j]));
+      }
+      BuildNode& r = bn[subtrees[k]];
+      std::memcpy(r.bb, ln[0].bb, sizeof r.bb);
+      r.c0 = map(ln[0].c0);
+      r.c1 = map(ln[0].c1);
+      r.objs.swap(ln[0].objs);
     }
-    int c0 = int(bn.size());
-    bn.emplace_back();
-    int c1 = int(bn.size());
-    bn.emplace_back();
-    bn[idx].c0 = c0;
-    bn[idx].c1 = c1;
-    bn[c0].objs.assign(objs.begin(), objs.begin() + split);
-    bn[c1].objs.assign(objs.begin() + split, objs.end());
-    work.push_back(c1);
-    work.push_back(c0);
   }
   // Depth-first renumbering, children[0] first.
   out.nodes.clear();
