@@ -304,7 +304,9 @@ def run_precision(level: int = 10, n_rx: int = 50000):
     t0 = time.perf_counter()
     wl = scenes.large_scene(level=level, n_rx=n_rx)
     gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
     sc = api.DeviceScene.from_scene(wl.scene)
+    create_s = time.perf_counter() - t0
     res = {}
     modes = {}
     for mode in ("fp64", "fp32", "fp32_phase"):
@@ -326,7 +328,7 @@ def run_precision(level: int = 10, n_rx: int = 50000):
     return {"workload": f"large terrain: {wl.scene.n_tri} tris, icosahedron level {level} "
                         f"({c['launches']} rays), R8 T0, {n_rx} receivers, half-wave 3.5 GHz",
             "segments": c["segments"], "paths": c["paths"], "rays": c["rays"],
-            "scene_generation_s": gen_s, "modes": modes,
+            "scene_generation_s": gen_s, "scene_create_s": create_s, "modes": modes,
             "tolerance": {"rel_mag": 1e-4, "phase_rad": 1e-3}}
 
 
@@ -411,7 +413,9 @@ def main():
     build_library()
 
     wl = scenes.urban_scene(level=args.level)
+    t_scene = time.perf_counter()
     scene = api.DeviceScene.from_scene(wl.scene)
+    scene_ms = 1e3 * (time.perf_counter() - t_scene)
     rx_dev = torch.tensor(wl.request.rx, dtype=torch.float64, device=f"cuda:{local}")
     torch.cuda.synchronize()
     q_dev, _keep = api.request_from_workload(wl.request, args.precision)
@@ -498,6 +502,7 @@ def main():
                        "parallelism": f"replicas{world}",
                        "l2": "working set (node pool) larger than L2 each step"},
             "counts": dict(counts, captured=captured),
+            "scene_create_ms": scene_ms,
             "field_error": ("FP64 field: the reference's arithmetic; parity tests hold it "
                             "within 1e-9 of the oracle" if args.precision == "fp64" else
                             fp32_error[args.precision]),
