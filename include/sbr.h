@@ -49,10 +49,15 @@ typedef enum sbr_status {
 
 /* MaterialProperties (common/DataStructures.h:20-28), same field order.
  * The field uses rel_permittivity_re and rel_conductivity only, like the
- * reference (FieldCompute.cpp:185-235). */
+ * reference (FieldCompute.cpp:185-235).
+ * width: wall thickness in metres for the slab coefficients
+ * (FieldCompute.cpp:255-262,284-291), used when use_fresnel is 0.  The
+ * reference always passes 0 (FieldCompute.cpp:131,138), which gives
+ * reflection 0 and transmission 1; width 0 reproduces that. */
 typedef struct sbr_material {
   double frequency, transmission_loss, reflection_loss;
   double rel_permittivity_re, rel_permittivity_im, rel_conductivity;
+  double width;
 } sbr_material;
 
 /* Antenna patterns of FieldCompute::GetAnalyticEfieldPattern

@@ -101,6 +101,9 @@ struct MaterialProperties {
   double relPermittivityRe = 1;
   double relPermittivityIm = 0;
   double relConductivity = 0;
+  // Not in the reference: wall thickness (m) for the slab coefficients used
+  // when useFresnelCoeff is false; 0 is what the reference always passes.
+  double width = 0;
 };
 
 // Triangle.h:8-46: the fields a caller reads or sets.
@@ -257,7 +260,7 @@ class BVH<Triangle> {
       if (t.materialId >= n_mat) n_mat = t.materialId + 1;
     }
     // placeholder materials until RTSolver::Init binds the real table
-    std::vector<sbr_material> placeholder(size_t(n_mat), sbr_material{0, 0, 0, 1, 0, 0});
+    std::vector<sbr_material> placeholder(size_t(n_mat), sbr_material{0, 0, 0, 1, 0, 0, 0});
     sbr_scene_destroy(scene_);
     scene_ = nullptr;
     check(sbr_scene_create(n, v.data(), nr.data(), mat.data(), placeholder.data(), n_mat,
@@ -313,7 +316,8 @@ class RTSolver {
     for (int i = 0; i < materialPropertiesCount; ++i) {
       const MaterialProperties& p = materialProperties[i];
       m[size_t(i)] = sbr_material{p.frequency,         p.transmissionLoss,  p.reflectionLoss,
-                                  p.relPermittivityRe, p.relPermittivityIm, p.relConductivity};
+                                  p.relPermittivityRe, p.relPermittivityIm, p.relConductivity,
+                                  p.width};
     }
     const auto& tris = triangles.triangles_by_id();
     std::vector<int> ids(tris.size());

@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 class _Mat(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("frequency", "transmissionLoss", "reflectionLoss",
                                            "relPermittivityRe", "relPermittivityIm",
-                                           "relConductivity")]
+                                           "relConductivity", "width")]
 
 
 class _Req(C.Structure):

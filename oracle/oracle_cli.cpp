@@ -26,6 +26,10 @@ int main(int argc, char** argv) {
       int n; in >> n; mats.resize(n);
       for (auto& m : mats) in >> m.frequency >> m.transmissionLoss >> m.reflectionLoss >>
           m.relPermittivityRe >> m.relPermittivityIm >> m.relConductivity;
+    } else if (key == "widths") {
+      int n; in >> n;
+      if (n != int(mats.size())) { std::fprintf(stderr, "widths: need one per material\n"); return 2; }
+      for (auto& m : mats) in >> m.width;
     } else if (key == "tx") in >> rq.tx[0] >> rq.tx[1] >> rq.tx[2];
     else if (key == "txcs") for (double& v : txcs) in >> v;
     else if (key == "refl") in >> rq.max_reflection;

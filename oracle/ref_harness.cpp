@@ -57,6 +57,7 @@ namespace {
 struct Case {
   std::string stl, trimat, rx, out;
   std::vector<MaterialProperties> mats;
+  std::vector<double> widths;  // per material; the reference passes 0
   Vec3 tx{0, 0, 0};
   Mat3 txcs = Mat3::Identity();
   int refl = 1, trans = 0, tess = 2, antenna = 1;
@@ -80,6 +81,11 @@ bool read_case(const char* path, Case& c) {
       for (auto& m : c.mats)
         in >> m.frequency >> m.transmissionLoss >> m.reflectionLoss >> m.relPermittivityRe >>
             m.relPermittivityIm >> m.relConductivity;
+    } else if (key == "widths") {
+      int n;
+      in >> n;
+      c.widths.resize(n);
+      for (double& w : c.widths) in >> w;
     } else if (key == "tx") in >> c.tx(0) >> c.tx(1) >> c.tx(2);
     else if (key == "txcs") {
       for (int i = 0; i < 3; ++i)
@@ -109,8 +115,12 @@ bool read_points(const std::string& path, VecVec3& out) {
   return true;
 }
 
-// FieldCompute.cpp:71-151 with the pattern type as a parameter.
-Vec3c field_for_path(FieldCompute& fc, const std::vector<Ray>& path, int antenna) {
+// FieldCompute.cpp:71-151 with the pattern type and the per-material wall
+// thickness passed to ComputeRefcField/ComputeTransField as parameters (the
+// reference passes width 0 at FieldCompute.cpp:131,138).
+Vec3c field_for_path(FieldCompute& fc, const std::vector<Ray>& path, int antenna,
+                     const std::vector<double>& widths) {
+  auto width_of = [&](int m) { return m < int(widths.size()) ? widths[m] : 0.0; };
   double lamda = SPEED_OF_LIGHT / fc._frequency;
   double k = (2 * PI) / lamda;
   Mat3 globalCoordSys = Mat3::Identity();
@@ -141,14 +151,16 @@ Vec3c field_for_path(FieldCompute& fc, const std::vector<Ray>& path, int antenna
       double relPerm = fc._materials[ray.reflectionMaterialId].relPermittivityRe;
       double sigma = fc._materials[ray.reflectionMaterialId].relConductivity;
       totalField = fc.ComputeRefcField(incidentField, relPerm, sigma, fc._frequency,
-                                       incidentAngle, 0, fc._useFresnelCoeff);
+                                       incidentAngle, width_of(ray.reflectionMaterialId),
+                                       fc._useFresnelCoeff);
     } else if (ray.penetrationMaterialId >= 0) {
       double incidentAngle =
           AngleBetween(vecGlobal, currentCoordSys(2, Eigen::indexing::all), false, true);
       double relPerm = fc._materials[ray.penetrationMaterialId].relPermittivityRe;
       double sigma = fc._materials[ray.penetrationMaterialId].relConductivity;
       totalField = fc.ComputeTransField(incidentField, relPerm, sigma, fc._frequency,
-                                        incidentAngle, 0, fc._useFresnelCoeff);
+                                        incidentAngle, width_of(ray.penetrationMaterialId),
+                                        fc._useFresnelCoeff);
     } else {
       totalField = incidentField;
     }
@@ -198,12 +210,16 @@ int run_case(const Case& c) {
   std::fprintf(f, "segments %ld\nlaunches %d\nreceivers %d\ntriangles %zu\n", segments,
                solver->_pathsCount, solver->_receiverCount, mesh.size());
   int loop_mismatch = 0;
+  bool zero_width = true;
+  for (double w : c.widths) zero_width = zero_width && w == 0.0;
+  const std::vector<double> no_width;
   for (int k = 0; k < solver->_receiverCount; ++k) {
     Vec3c total{cdouble(0, 0), cdouble(0, 0), cdouble(0, 0)};
     for (int i = 0; i < solver->_pathsCount; ++i) {
       for (const auto& path : solver->_rayPaths[i][k].rayPaths) {
-        Vec3c e = field_for_path(fc, path, c.antenna);
-        if (!same_bits(field_for_path(fc, path, 1), fc.FieldForPath(path))) ++loop_mismatch;
+        Vec3c e = field_for_path(fc, path, c.antenna, c.widths);
+        if (!same_bits(field_for_path(fc, path, 1, no_width), fc.FieldForPath(path)))
+          ++loop_mismatch;
         total += e;
         std::fprintf(f, "path %d %d %zu %.17g %.17g %.17g %.17g %.17g %.17g\n", k, i, path.size(),
                      e(0).real(), e(0).imag(), e(1).real(), e(1).imag(), e(2).real(),
@@ -216,7 +232,7 @@ int run_case(const Case& c) {
       }
     }
     const Vec3c& ref = solver->_efield->at(k);
-    if (c.antenna == 1 && !same_bits(ref, total)) ++loop_mismatch;
+    if (c.antenna == 1 && zero_width && !same_bits(ref, total)) ++loop_mismatch;
     std::fprintf(f, "field %d %.17g %.17g %.17g %.17g %.17g %.17g\n", k, total(0).real(),
                  total(0).imag(), total(1).real(), total(1).imag(), total(2).real(),
                  total(2).imag());

@@ -626,7 +626,7 @@ void fresnel(bool te, cd ti, cd tt, cd ei, cd et, double lam, double width, bool
   }
 }
 C3 interact(bool reflect, const C3& e, double rel_perm, double sigma, double freq, double ti,
-            bool inf_wall) {  // FieldCompute.cpp:185-235
+            double width, bool inf_wall) {  // FieldCompute.cpp:185-235
   cd et;
   et.real(rel_perm);
   et.imag(-1 * sigma / (kE0 * 2 * kPi * freq));
@@ -634,8 +634,8 @@ C3 interact(bool reflect, const C3& e, double rel_perm, double sigma, double fre
   cd ei(1, 0);
   cd tt = ctrans_angle(ti, ei, et);
   cd rte, rtm, tte, ttm;
-  fresnel(false, ti, tt, ei, et, lam, 0, inf_wall, rtm, ttm);
-  fresnel(true, ti, tt, ei, et, lam, 0, inf_wall, rte, tte);
+  fresnel(false, ti, tt, ei, et, lam, width, inf_wall, rtm, ttm);
+  fresnel(true, ti, tt, ei, et, lam, width, inf_wall, rte, tte);
   C3 r;
   r.v[0] = e.v[0];
   r.v[1] = e.v[1] * (reflect ? rtm : ttm);
@@ -689,7 +689,8 @@ C3 field_for_path(const FieldCtx& c, const std::vector<PathRay>& path) {
     if (r.kind != 0) {
       double ang = angle_between(vg, cur.row(2));
       const MaterialProperties_c& m = (*c.mats)[r.mat];
-      tot = interact(r.kind == 1, inc, m.relPermittivityRe, m.relConductivity, c.freq, ang, c.fresnel);
+      tot = interact(r.kind == 1, inc, m.relPermittivityRe, m.relConductivity, c.freq, ang,
+                     m.width, c.fresnel);
     } else {
       tot = inc;
     }

@@ -7,10 +7,12 @@
 extern "C" {
 #endif
 
-/* MaterialProperties field order (SBRSolver_rev2/common/DataStructures.h:20-28). */
+/* MaterialProperties field order (SBRSolver_rev2/common/DataStructures.h:20-28),
+ * then the wall thickness passed to the slab coefficients (the reference
+ * passes 0, FieldCompute.cpp:131,138). */
 typedef struct {
   double frequency, transmissionLoss, reflectionLoss, relPermittivityRe, relPermittivityIm,
-      relConductivity;
+      relConductivity, width;
 } MaterialProperties_c;
 
 /* Arguments of RTSolver::ExecuteRayTracing (SBRSolver_rev2/RTSolver.h:25-37)

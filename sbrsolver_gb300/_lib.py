@@ -38,7 +38,7 @@ class SbrError(RuntimeError):
 class Material(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("frequency", "transmission_loss", "reflection_loss",
                                            "rel_permittivity_re", "rel_permittivity_im",
-                                           "rel_conductivity")]
+                                           "rel_conductivity", "width")]
 
 
 class SceneInfo(C.Structure):

@@ -30,10 +30,15 @@ class MaterialProperties:
     relPermittivityRe: float = 1.0
     relPermittivityIm: float = 0.0
     relConductivity: float = 0.0
+    # Wall thickness (m) for the slab coefficients used when useFresnelCoeff
+    # is false (FieldCompute.cpp:255-262,284-291).  The reference always
+    # passes 0 (FieldCompute.cpp:131,138): reflection 0, transmission 1.
+    width: float = 0.0
 
     def as_c(self) -> _lib.Material:
         return _lib.Material(self.frequency, self.transmissionLoss, self.reflectionLoss,
-                             self.relPermittivityRe, self.relPermittivityIm, self.relConductivity)
+                             self.relPermittivityRe, self.relPermittivityIm, self.relConductivity,
+                             self.width)
 
 
 @dataclass

@@ -76,7 +76,7 @@ struct CorrTri {
 };
 
 struct Material {
-  double eps_re, sigma;
+  double eps_re, sigma, width;  // width: slab thickness (m), 0 in the reference
 };
 
 struct DevScene {

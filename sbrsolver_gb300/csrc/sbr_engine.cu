@@ -289,7 +289,8 @@ static void upload_scene(SceneImpl& S) {
   for (auto& t : H.tris) S.n_cop = std::max(S.n_cop, t.cop + 1);
   std::vector<Material> mats(S.materials.size());
   for (size_t i = 0; i < mats.size(); ++i)
-    mats[i] = Material{S.materials[i].rel_permittivity_re, S.materials[i].rel_conductivity};
+    mats[i] = Material{S.materials[i].rel_permittivity_re, S.materials[i].rel_conductivity,
+                       S.materials[i].width};
   cudaStream_t st = S.stream;
   S.node32.upload(n32.data(), n32.size(), st);
   S.ref.upload(ref.data(), ref.size(), st);
@@ -1066,12 +1067,22 @@ extern "C" {
 const char* sbr_last_error(void) { return g_err.c_str(); }
 const char* sbr_version(void) { return "sbr-gb300 0.1 (sm_103a)"; }
 
+// Wall thicknesses must be finite and non-negative; empty string when valid.
+static std::string material_error(const sbr_material* m, int n) {
+  for (int i = 0; i < n; ++i)
+    if (!(m[i].width >= 0.0) || !std::isfinite(m[i].width))
+      return "material " + std::to_string(i) + ": width must be finite and >= 0";
+  return std::string();
+}
+
 static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, const int* mat_ids,
                                const sbr_material* materials, int n_materials, sbr_scene** out) {
   ABI_GUARD({
     if (!out) throw std::string("out is NULL");
     *out = nullptr;
     if (n_materials <= 0 || !materials) throw std::string("at least one material is required");
+    if (!material_error(materials, n_materials).empty())
+      throw material_error(materials, n_materials);
     const int nt = int(n.size() / 3);
     if (mat_ids)
       for (int i = 0; i < nt; ++i)
@@ -1173,6 +1184,10 @@ sbr_status sbr_scene_set_materials(sbr_scene* scene, const int* material_ids,
                                    const sbr_material* materials, int n_materials) {
   if (!scene || !materials || n_materials <= 0) {
     set_err("sbr_scene_set_materials: need a scene and at least one material");
+    return SBR_ERR_INVALID_ARG;
+  }
+  if (!material_error(materials, n_materials).empty()) {
+    set_err("sbr_scene_set_materials: " + material_error(materials, n_materials));
     return SBR_ERR_INVALID_ARG;
   }
   SceneImpl& S = scene->impl;

@@ -167,16 +167,30 @@ struct FieldConsts {
   double e0, eta0, pi_hi, pi_lo;  // reference constants (computed on the host)
 };
 
+// The slab's round-trip phase factor ph = e^(-j 2q), q = (2 pi width / lam)
+// sqrt(n_t - sin^2 theta_i) (FieldCompute.cpp:257-258,286-287; the square root
+// takes the refractive index n_t, as the reference's does).  Taken in FP64 for
+// every field precision: 2q reaches hundreds of radians for walls many
+// wavelengths thick.  Width 0 (what the reference always passes) gives q = 0
+// and ph = 1 exactly.
+__device__ __forceinline__ Cx<double> slab_phase(double theta_i, Cx<double> eps_t, double lam,
+                                                 double width, double two_pi) {
+  if (width == 0.0) return cx(1.0, 0.0);
+  const Cx<double> nt = csqrt(eps_t), si = csin_(cx(theta_i));
+  const Cx<double> q = ((two_pi * width) / lam) * csqrt(nt - si * si);
+  return cexp_(cx(0.0, -2.0) * q);
+}
+
 // GetTransAngle + GetTMCoeff/GetTECoeff for air -> eps_t; returns the
-// coefficient pair (TM, TE) applied to E_theta, E_phi.
+// coefficient pair (TM, TE) applied to E_theta, E_phi.  ph: slab_phase.
 template <class R>
-__device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, R lam, bool inf_wall,
+__device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, Cx<R> ph, bool inf_wall,
                              R eta0, Cx<R>& c_tm, Cx<R>& c_te) {
   const Cx<R> ni = cx(R(1)), nt = csqrt(eps_t);
   const Cx<R> ti = cx(theta_i);
   const Cx<R> tt = casin_((ni / nt) * csin_(ti));
   const Cx<R> etai = eta0 / ni, etat = eta0 / nt;
-  const Cx<R> ci = ccos_(ti), ct = ccos_(tt), si = csin_(ti);
+  const Cx<R> ci = ccos_(ti), ct = ccos_(tt);
   const Cx<R> g_te = -((etat / ct) - (etai / ci)) / ((etat / ct) + (etai / ci));
   const Cx<R> g_tm = (-(etat * ct) + etai * ci) / (etat * ct + etai * ci);
   if (inf_wall) {
@@ -184,9 +198,8 @@ __device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, R lam, bool i
     c_te = reflect ? g_te : cx(R(0));
     return;
   }
-  // Slab form with zero width (the reference always passes width 0).
-  const Cx<R> q = (R(0) / lam) * csqrt(nt - si * si);
-  const Cx<R> ph = cexp_(cx(R(0), R(-2)) * q);
+  // Slab of thickness width (FieldCompute.cpp:255-262,284-291); width 0
+  // gives reflection 0 and transmission 1.
   const Cx<R> one = cx(R(1));
   const Cx<R> den_tm = one - g_tm * g_tm * ph, den_te = one - g_te * g_te * ph;
   if (reflect) {
@@ -210,7 +223,6 @@ __device__ void path_field(int n, const double (*pts)[3], const double* const* f
                            bool fresnel, const FieldConsts& K, Cx<double>* out,
                            const PatternTab* pat = nullptr) {
   const double lam64 = 2.99792458e8 / freq;
-  const R lam = R(lam64);
   M3<R> cur, next;
   for (int i = 0; i < 9; ++i) next.m[i] = R(txcs[i]);
   Cx<R> tot[3] = {cx(R(0)), cx(R(0)), cx(R(0))};
@@ -220,15 +232,20 @@ __device__ void path_field(int n, const double (*pts)[3], const double* const* f
     R vg[3] = {R(vg64[0]), R(vg64[1]), R(vg64[2])};
     R vl[3];
     mv(next, vg, vl);
-    // CartesianToSpherical (VecMatDef.h:132-155); r is kept in FP64.
-    double vl64[3];
-    {
-      double nx[9];
-      for (int j = 0; j < 9; ++j) nx[j] = double(next.m[j]);
+    // CartesianToSpherical (VecMatDef.h:132-155); r is kept in FP64.  In FP64
+    // it is the length of the rotated vector, as in the reference.  With FP32
+    // frames it is the length of the global vector: a frame rounded to FP32 is
+    // orthonormal only to ~1e-7, which would move r by ~1e-7 r (1e-3 rad of
+    // phase for a 50 m segment at 28 GHz).
+    double r;
+    if constexpr (sizeof(R) == sizeof(double)) {
+      double vl64[3];
       for (int j = 0; j < 3; ++j)
-        vl64[j] = (nx[3 * j] * vg64[0] + nx[3 * j + 1] * vg64[1]) + nx[3 * j + 2] * vg64[2];
+        vl64[j] = (next.m[3 * j] * vg64[0] + next.m[3 * j + 1] * vg64[1]) + next.m[3 * j + 2] * vg64[2];
+      r = sqrt((vl64[0] * vl64[0] + vl64[1] * vl64[1]) + vl64[2] * vl64[2]);
+    } else {
+      r = sqrt((vg64[0] * vg64[0] + vg64[1] * vg64[1]) + vg64[2] * vg64[2]);
     }
-    const double r = sqrt((vl64[0] * vl64[0] + vl64[1] * vl64[1]) + vl64[2] * vl64[2]);
     R th, ph;
     if (vl[0] == R(0) && vl[1] == R(0) && vl[2] == R(0)) th = R(K.pi_hi * 0.5);
     else th = atan2(sqrt(vl[0] * vl[0] + vl[1] * vl[1]), vl[2]);
@@ -279,9 +296,15 @@ __device__ void path_field(int n, const double (*pts)[3], const double* const* f
         ang = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
       }
       const Material& m = mats[mat[i]];
-      const Cx<R> eps_t = cx(R(m.eps_re), R(-1.0 * m.sigma / (K.e0 * 2.0 * K.pi_hi * freq)));
+      const Cx<double> eps64 = cx(m.eps_re, -1.0 * m.sigma / (K.e0 * 2.0 * K.pi_hi * freq));
+      const Cx<R> eps_t = cx(R(eps64.re), R(eps64.im));
+      Cx<R> ph = cx(R(1));
+      if (!fresnel) {
+        const Cx<double> p64 = slab_phase(double(ang), eps64, lam64, m.width, 2.0 * K.pi_hi);
+        ph = cx(R(p64.re), R(p64.im));
+      }
       Cx<R> ctm, cte;
-      fresnel_pair<R>(kind[i] == 1, ang, eps_t, lam, fresnel, R(K.eta0), ctm, cte);
+      fresnel_pair<R>(kind[i] == 1, ang, eps_t, ph, fresnel, R(K.eta0), ctm, cte);
       tot[0] = inc[0];
       tot[1] = inc[1] * ctm;
       tot[2] = inc[2] * cte;

@@ -65,8 +65,9 @@ def p2040_sigma(c: float, d: float, f_hz: float) -> float:
 
 # (frequency, transmissionLoss, reflectionLoss, relPermittivityRe,
 #  relPermittivityIm, relConductivity): MaterialProperties field order,
-#  SBRSolver_rev2/common/DataStructures.h:20-28.
-Material = Tuple[float, float, float, float, float, float]
+#  SBRSolver_rev2/common/DataStructures.h:20-28, optionally followed by a wall
+#  thickness in metres (slab coefficients; the reference's is always 0).
+Material = Tuple[float, ...]
 
 
 @dataclass
@@ -223,6 +224,17 @@ def small_scene(seed: int = 0x5B5) -> Workload:
     return Workload("small_L6_R3", scene, req, {"seed": seed})
 
 
+def slab_walls(wl: Workload, widths: Sequence[float]) -> Workload:
+    """The same workload with finite-thickness walls: material i gets
+    thickness widths[i] (m) and the request switches to the slab
+    coefficients (use_fresnel False, FieldCompute.cpp:255-262,284-291)."""
+    mats = [tuple(m[:6]) + (float(w),) for m, w in zip(wl.scene.materials, widths)]
+    wl.scene.materials = mats
+    wl.request.use_fresnel = False
+    wl.name = wl.name + "_slab"
+    return wl
+
+
 def urban_scene(seed: int = 0x5B5 + 1, level: int = 9, rx_pitch: float = 10.0,
                 max_reflection: int = 6, max_transmission: int = 1) -> Workload:
     """Synthetic urban canyon: 1 km x 1 km ground plus 400 boxes on a 50 m
@@ -302,7 +314,10 @@ def write_oracle_case(wl: Workload, directory: str, antenna: int | None = None) 
         fh.write(f"stl {stl}\ntrimat {tm}\nrx {rxp}\nout {os.path.join(directory, 'out.txt')}\n")
         fh.write(f"materials {len(sc.materials)}\n")
         for m in sc.materials:
-            fh.write(" ".join("%.17g" % v for v in m) + "\n")
+            fh.write(" ".join("%.17g" % v for v in m[:6]) + "\n")
+        widths = [m[6] if len(m) > 6 else 0.0 for m in sc.materials]
+        if any(w != 0.0 for w in widths):
+            fh.write(f"widths {len(widths)} " + " ".join("%.17g" % w for w in widths) + "\n")
         fh.write("tx %.17g %.17g %.17g\n" % tuple(rq.tx))
         fh.write("txcs " + " ".join("%.17g" % v for v in rq.tx_coord_sys) + "\n")
         fh.write(f"refl {rq.max_reflection}\ntrans {rq.max_transmission}\n")

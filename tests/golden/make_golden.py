@@ -179,6 +179,11 @@ def main() -> None:
     run_case(scenes.urban_scene(level=5, rx_pitch=100.0), "urban_L5_R6T1_rx100")
     run_case(scenes.urban_scene(level=4, rx_pitch=50.0, max_reflection=3, max_transmission=2),
              "urban_L4_R3T2_rx400")
+    # finite-thickness walls: the reference's own ComputeRefcField /
+    # ComputeTransField with a non-zero width (its main() always passes 0)
+    run_case(scenes.slab_walls(scenes.urban_scene(level=5, rx_pitch=25.0, max_reflection=3,
+                                                  max_transmission=2), (0.5, 0.2, 0.01)),
+             "urban_L5_R3T2_rx1600_slab")
     # icosahedron launch directions, bit-exact
     for lvl in (0, 1, 2, 5):
         with tempfile.TemporaryDirectory(dir=os.path.join(ROOT, "_work")) as d:

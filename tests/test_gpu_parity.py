@@ -75,6 +75,20 @@ def test_urban_variants(built, level, R, T, antenna):
                    {k: ref["counts"][k] for k in ("segments", "captured", "corrected")})
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_slab_walls_against_oracle(built, precision):
+    """Finite-thickness walls (slab coefficients with width > 0): same path
+    set as the oracle, fields within tolerance; FP64 fields tight."""
+    wl = scenes.urban_scene(level=6, rx_pitch=25.0, max_reflection=4, max_transmission=2)
+    wl = scenes.slab_walls(wl, (0.3, 0.15, 0.006))
+    ref = _oracle(wl)
+    assert any(k == 2 for p in ref["paths"] for k in p["kind"])
+    res, _ = _gpu(wl, precision=precision)
+    _check_against(res, ref["paths"], ref["field"],
+                   {k: ref["counts"][k] for k in ("segments", "captured", "corrected")},
+                   tight=precision == "fp64")
+
+
 def test_identity_mesh_order(built):
     """A caller whose triangle vector stays in file order: image correction
     and frames then use the hit triangle itself."""

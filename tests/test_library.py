@@ -39,7 +39,7 @@ def test_struct_layouts_match_header(tmp_path):
               "sbr_timing": (_lib.Timing, ["device_ms"]),
               "sbr_field_error": (_lib.FieldError, ["max_rel_vec"]),
               "sbr_completion": (_lib.Completion, ["counts", "result"]),
-              "sbr_material": (_lib.Material, ["rel_conductivity"]),
+              "sbr_material": (_lib.Material, ["rel_conductivity", "width"]),
               "sbr_scene_info": (_lib.SceneInfo, ["device_bytes"])}
     lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "sbr.h"', "int main(void) {"]
     for t, (_, fields) in checks.items():
@@ -88,6 +88,18 @@ def test_bad_material_id_rejected(built):
         api.DeviceScene(mesh, [api.MaterialProperties()])
     assert e.value.status == _lib.ERR_INVALID_ARG
     assert "material id out of range" in str(e.value)
+
+
+@pytest.mark.parametrize("width", [-0.1, float("nan"), float("inf")])
+def test_bad_wall_width_rejected(built, width):
+    wl = scenes.small_scene()
+    mesh = api.Mesh(wl.scene.tri, wl.scene.normal, wl.scene.material_id)
+    mats = [api.MaterialProperties(*m) for m in wl.scene.materials]
+    mats[1].width = width
+    with pytest.raises(_lib.SbrError) as e:
+        api.DeviceScene(mesh, mats)
+    assert e.value.status == _lib.ERR_INVALID_ARG
+    assert "width" in str(e.value)
 
 
 @pytest.mark.skipif(_gpu_present(), reason="checks the no-GPU error path")

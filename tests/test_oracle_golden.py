@@ -23,6 +23,9 @@ def _case(name):
         wl.request.tessellation = 4
         wl.request.max_transmission = 1
         return wl
+    if name == "urban_L5_R3T2_rx1600_slab":
+        return scenes.slab_walls(scenes.urban_scene(level=5, rx_pitch=25.0, max_reflection=3,
+                                                    max_transmission=2), SLAB_WIDTHS)
     if name == "urban_L5_R6T1_rx100":
         return scenes.urban_scene(level=5, rx_pitch=100.0)
     if name == "urban_L4_R3T2_rx400":
@@ -31,7 +34,10 @@ def _case(name):
 
 
 CASES = ["reference_main", "small_L6_R3", "small_L4_R3T1_hertzian", "urban_L5_R6T1_rx100",
-         "urban_L4_R3T2_rx400"]
+         "urban_L4_R3T2_rx400", "urban_L5_R3T2_rx1600_slab"]
+# slab coefficients instead of infinite walls: ground 0.5 m, concrete walls
+# 0.2 m, glass 0.01 m thick
+SLAB_WIDTHS = (0.5, 0.2, 0.01)
 
 
 @pytest.mark.parametrize("name", CASES)
