@@ -90,11 +90,6 @@ __device__ __noinline__ int capture_exact(const NodeCold* cold, uint32_t idx, co
 // the rows' runs.  A capture counts unless an ancestor of the node captures
 // the same receiver (RTSolver.cpp:277-284).
 constexpr int kCapWarps = 4;
-// Minimum chunk length along a segment, in receiver-grid cells.
-#ifndef SBR_CAP_CHUNK_CELLS
-#define SBR_CAP_CHUNK_CELLS 16
-#endif
-constexpr float kCapChunkCells = SBR_CAP_CHUNK_CELLS;
 // Nodes staged per warp at a time (at most 32: one per lane; 16 leaves more
 // of the SM's shared memory to L1 for the receiver grid).
 #ifndef SBR_CAP_BATCH
@@ -211,7 +206,7 @@ __device__ __forceinline__ NodeSpan node_span(const NodeHot& nd, const TxParams&
   }
   if (!(lo <= hi)) return sp;
   const float r0 = (S + sqrt_up(ss + 2.0f * lo * su + lo * lo)) * tanb;
-  const float lc = fmaxf(kCapChunkCells * g.cell, r0);
+  const float lc = fmaxf(g.chunk_len, r0);
   int nchunk = int(ceilf(__fdividef(hi - lo, lc)));
   nchunk = max(1, min(nchunk, 4096));
   sp.lo = lo;

@@ -151,6 +151,7 @@ struct RxGrid {
   float org[3], cell;
   int dim[3];
   float inv_cell;  // 1 / cell
+  float chunk_len; // minimum chunk length along a node's segment in capture (m)
   const int* cell_start;  // ncell + 1
   const float4* rx32;     // sorted by cell: xyz, w = receiver index (int bits)
   float bmin[3], bmax[3];

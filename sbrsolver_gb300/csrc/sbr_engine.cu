@@ -590,7 +590,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
   // ---- receiver grid
   // cells per request: the grid aims at ~2 receivers per cell
   int max_cells = 64;
-  for (auto& p : tp) max_cells = std::max(max_cells, 2 * p.n_rx + 64);
+  for (auto& p : tp)
+    max_cells = std::max(max_cells, int(std::min(4.0 * p.n_rx / kMinRxPerCell, 4e6)) + 64);
   max_cells = std::min(max_cells, 1 << 21);
   W.gb.ensure(n_req);
   {

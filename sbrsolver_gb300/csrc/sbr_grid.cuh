@@ -61,8 +61,28 @@ __global__ void k_rx_bounds(const double* rx, const TxParams* txp, int n_tx, Gri
   }
 }
 
-// Grid shape: cells of equal size sized for ~4 receivers per cell over the
-// axes with extent, at most max_cells cells.
+// Receivers per cell the grid is sized for, and the minimum chunk length of a
+// node's segment in capture, in cells.  Smaller cells hug a node's capture
+// tube more closely (fewer candidates per node) but give more rows and chunks
+// per node; for receivers on a plane (one layer of cells) a row costs less,
+// and smaller cells pay.
+#ifndef SBR_GRID_RX_PER_CELL
+#define SBR_GRID_RX_PER_CELL 2.0
+#endif
+#ifndef SBR_GRID_RX_PER_CELL_FLAT
+#define SBR_GRID_RX_PER_CELL_FLAT 0.5
+#endif
+#ifndef SBR_CAP_CHUNK_CELLS
+#define SBR_CAP_CHUNK_CELLS 16
+#endif
+#ifndef SBR_CAP_CHUNK_CELLS_FLAT
+#define SBR_CAP_CHUNK_CELLS_FLAT 24
+#endif
+constexpr double kMinRxPerCell =
+    SBR_GRID_RX_PER_CELL < SBR_GRID_RX_PER_CELL_FLAT ? SBR_GRID_RX_PER_CELL : SBR_GRID_RX_PER_CELL_FLAT;
+
+// Grid shape: cells of equal size over the axes with extent, sized for the
+// receivers per cell above, at most max_cells cells.
 __global__ void k_grid_shape(GridBuild* gb, RxGrid* grids, const TxParams* txp, int n_tx,
                              int max_cells, int* cell_base) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -87,7 +107,8 @@ __global__ void k_grid_shape(GridBuild* gb, RxGrid* grids, const TxParams* txp, 
       }
     float cell = 1.0f;
     if (k > 0) {
-      double target = fmax(1.0, txp[r].n_rx / 2.0);
+      const double rpc = k < 3 ? SBR_GRID_RX_PER_CELL_FLAT : SBR_GRID_RX_PER_CELL;
+      double target = fmax(1.0, txp[r].n_rx / rpc);
       cell = float(pow(vol / target, 1.0 / k));
     }
     if (cell <= 0) cell = 1.0f;
@@ -110,6 +131,7 @@ __global__ void k_grid_shape(GridBuild* gb, RxGrid* grids, const TxParams* txp, 
     }
     g.cell = cell;
     g.inv_cell = 1.0f / cell;
+    g.chunk_len = float(k < 3 ? SBR_CAP_CHUNK_CELLS_FLAT : SBR_CAP_CHUNK_CELLS) * cell;
     gb[r].ncell = int(tot);
     gb[r].cmax = o2f(gb[r].cmax_o);
     cell_base[r] = base;
