@@ -138,8 +138,10 @@ __device__ __forceinline__ void root_ray(const TxParams* txp, int n_tx, const do
 //
 // Each lane traverses one ray at a time.  Lanes whose ray is finished take a
 // new one from the chunk's work counter (one atomic per warp, when at least
-// a quarter of the warp is idle or nobody is busy), so warps stay full while
-// rays of very different lengths finish at different times.
+// half the warp is idle or nobody is busy), so warps stay full while rays of
+// very different lengths finish at different times.  A step is one node
+// visit or one triangle test, so lanes in a leaf and lanes between nodes
+// advance at the same pace.
 struct FindArgs {
   DevScene sc;
   const TxParams* txp;
@@ -156,7 +158,15 @@ struct FindArgs {
   unsigned char* ncand;        // contenders per ray, kFindFallback = exact traversal
 };
 
-constexpr int kFindSteps = 16;  // traversal steps between refills
+// Traversal steps between refills, and the idle lanes that trigger one.
+#ifndef SBR_FIND_STEPS
+#define SBR_FIND_STEPS 32
+#endif
+#ifndef SBR_FIND_REFILL
+#define SBR_FIND_REFILL 16
+#endif
+constexpr int kFindSteps = SBR_FIND_STEPS;
+constexpr int kFindRefill = SBR_FIND_REFILL;
 
 __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
@@ -176,7 +186,7 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
     const bool idle = ray < 0 && !exhausted;
     const unsigned im = __ballot_sync(0xffffffffu, idle);
     const unsigned busy = __ballot_sync(0xffffffffu, ray >= 0);
-    if (im && (__popc(im) >= 8 || busy == 0)) {
+    if (im && (__popc(im) >= kFindRefill || busy == 0)) {
       const int leader = __ffs(im) - 1;
       unsigned long long base = 0;
       if (int(lane) == leader) base = atomicAdd(A.work, (unsigned long long)__popc(im));
@@ -223,20 +233,19 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
     bool done = false;
     for (int it = 0; it < kFindSteps && !done; ++it) {
       if (pending >= 0) {
-        const int first = pending >> 3, last = first + (pending & 7);
-        for (int j = first; j < last; ++j) {
-          float tlo, thi;
-          const int k = tri_classify(A.sc.stri[j], o32, d32, no, nd, tlo, thi);
-          if (k == 0 || tlo > tcut) continue;
-          if (nc == kCand) {
-            fail = true;
-            break;
-          }
-          out[nc++] = make_uint2(unsigned(__ldg(A.sc.srank + j)), __float_as_uint(tlo));
-          if (k == 2) tcut = fminf(tcut, thi * (1.0f + 1.0f / 4096.0f) + 1e-30f);
+        // one triangle of the pending leaf per step, so lanes testing
+        // triangles and lanes stepping through nodes cost one step each
+        const int j = pending >> 3, left = (pending & 7) - 1;
+        pending = left > 0 ? ((j + 1) << 3 | left) : -1;
+        float tlo, thi;
+        const int k = tri_classify(A.sc.stri[j], o32, d32, no, nd, tlo, thi);
+        if (k == 0 || tlo > tcut) continue;
+        if (nc == kCand) {
+          fail = done = true;
+          break;
         }
-        pending = -1;
-        if (fail) done = true;
+        out[nc++] = make_uint2(unsigned(__ldg(A.sc.srank + j)), __float_as_uint(tlo));
+        if (k == 2) tcut = fminf(tcut, thi * (1.0f + 1.0f / 4096.0f) + 1e-30f);
         continue;
       }
       if (sp == 0) {
