@@ -218,6 +218,10 @@ bool read_stl(const std::string& path, std::vector<float>& v, std::vector<float>
   return true;
 }
 
+namespace {
+void build_search_bvh_ids(const float* v, int n_tri, SearchBVH& out);
+}  // namespace
+
 bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, HostScene& out,
                    std::string& err) {
   out = HostScene();
@@ -225,6 +229,17 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
     err = "empty triangle list";
     return false;
   }
+  // The search BVH depends only on the triangles' float boxes, so it is built
+  // over triangle ids on its own thread while the reference BVH is built, and
+  // its leaves are mapped to depth-first ranks at the end.
+  SearchBVH search;
+  std::thread search_thread([&] { build_search_bvh_ids(v, n_tri, search); });
+  struct Joiner {
+    std::thread& t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } joiner{search_thread};
   // Exact vertex merge (StlReader.h:448-508): equal float triples share an id.
   struct Key {
     float x, y, z;
@@ -271,22 +286,36 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
     return false;
   }
   out.tris.resize(src.size());
-  double ext = 0;
-  for (size_t t = 0; t < src.size(); ++t) {
-    HostTri& tr = out.tris[t];
-    const float* p = &v[9 * src[t]];
-    for (int a = 0; a < 3; ++a) {
-      tr.v1[a] = p[a];
-      tr.v2[a] = p[3 + a];
-      tr.v3[a] = p[6 + a];
-      tr.n[a] = nrm[3 * t + a];
-      ext = std::max({ext, std::fabs(tr.v1[a]), std::fabs(tr.v2[a]), std::fabs(tr.v3[a])});
-    }
-    tr.id = int(t);
-    tr.mat = mat ? mat[src[t]] : 0;
-    finish_tri(tr);
+  // triangle records (frames, boxes) in parallel slices
+  const unsigned n_slices =
+      std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
+  std::vector<double> slice_ext(n_slices, 0.0);
+  {
+    auto fill = [&](unsigned k) {
+      const size_t b = src.size() * k / n_slices, e = src.size() * (k + 1) / n_slices;
+      double ext = 0;
+      for (size_t t = b; t < e; ++t) {
+        HostTri& tr = out.tris[t];
+        const float* p = &v[9 * src[t]];
+        for (int a = 0; a < 3; ++a) {
+          tr.v1[a] = p[a];
+          tr.v2[a] = p[3 + a];
+          tr.v3[a] = p[6 + a];
+          tr.n[a] = nrm[3 * t + a];
+          ext = std::max({ext, std::fabs(tr.v1[a]), std::fabs(tr.v2[a]), std::fabs(tr.v3[a])});
+        }
+        tr.id = int(t);
+        tr.mat = mat ? mat[src[t]] : 0;
+        finish_tri(tr);
+      }
+      slice_ext[k] = ext;
+    };
+    std::vector<std::thread> pool;
+    for (unsigned k = 1; k < n_slices; ++k) pool.emplace_back(fill, k);
+    fill(0);
+    for (auto& th : pool) th.join();
   }
-  out.extent = ext;
+  out.extent = *std::max_element(slice_ext.begin(), slice_ext.end());
 
   // Coplanar ids (Preprocessor.cpp:116-246).
   const int nt = int(out.tris.size());
@@ -296,26 +325,33 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
     while (parent[a] != a) a = parent[a] = parent[parent[a]];
     return a;
   };
-  std::unordered_map<uint64_t, std::vector<int>> edges;
-  edges.reserve(size_t(nt) * 2);
   auto same_or_opposite = [&](int a, int b) {
     const double* p = out.tris[a].n;
     const double* q = out.tris[b].n;
     return (p[0] == q[0] && p[1] == q[1] && p[2] == q[2]) ||
            (p[0] == -q[0] && p[1] == -q[1] && p[2] == -q[2]);
   };
+  // Triangles sharing an edge (of merged vertex ids) are adjacent when their
+  // facet normals are equal or opposite; the components do not depend on the
+  // order the pairs are joined in, so the edges are grouped by sorting.
+  std::vector<std::pair<uint64_t, int>> edges;
+  edges.reserve(3 * size_t(nt));
   for (int t = 0; t < nt; ++t) {
     int a = vidx[3 * t], b = vidx[3 * t + 1], c = vidx[3 * t + 2];
     int es[3][2] = {{std::min(a, b), std::max(a, b)},
                     {std::min(b, c), std::max(b, c)},
                     {std::min(a, c), std::max(a, c)}};
-    for (auto& e : es) {
-      uint64_t key = (uint64_t(uint32_t(e[0])) << 32) | uint32_t(e[1]);
-      auto& lst = edges[key];
-      for (int o : lst)
-        if (same_or_opposite(o, t)) parent[find(o)] = find(t);
-      lst.push_back(t);
-    }
+    for (auto& e : es) edges.push_back({(uint64_t(uint32_t(e[0])) << 32) | uint32_t(e[1]), t});
+  }
+  std::sort(edges.begin(), edges.end());
+  for (size_t i = 0; i < edges.size();) {
+    size_t j = i + 1;
+    while (j < edges.size() && edges[j].first == edges[i].first) ++j;
+    for (size_t x = i; x < j; ++x)
+      for (size_t y = x + 1; y < j; ++y)
+        if (same_or_opposite(edges[x].second, edges[y].second))
+          parent[find(edges[x].second)] = find(edges[y].second);
+    i = j;
   }
   std::vector<int> comp(nt, -1);
   int next = 0;
@@ -460,7 +496,11 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
       st.push_back({bn[it.b].c0, me, it.depth + 1, me, 0});
     }
   }
-  build_search_bvh(out);
+  search_thread.join();
+  out.search = std::move(search);
+  std::vector<int> rank_of(out.tris.size());
+  for (size_t r = 0; r < out.dfs_tris.size(); ++r) rank_of[size_t(out.dfs_tris[r])] = int(r);
+  for (int& o : out.search.order) o = rank_of[size_t(o)];
   return true;
 }
 
@@ -482,7 +522,7 @@ struct FBox {
 };
 
 struct SearchBuild {
-  std::vector<float> blo, bhi, cen;  // per rank
+  std::vector<float> blo, bhi, cen;  // per triangle
   SearchBVH* out;
   int max_depth = 0;
 
@@ -578,35 +618,34 @@ struct SearchBuild {
   }
 };
 
-}  // namespace
-
-void build_search_bvh(HostScene& H) {
-  const int n = int(H.dfs_tris.size());
+// Builds `out` over triangles 0..n_tri-1 with vertices v (9 floats each);
+// out.order holds triangle ids.
+void build_search_bvh_ids(const float* v, int n_tri, SearchBVH& out) {
+  const int n = n_tri;
   SearchBuild sb;
-  sb.out = &H.search;
-  H.search.nodes.clear();
-  H.search.order.resize(n);
+  sb.out = &out;
+  out.nodes.clear();
+  out.order.resize(n);
   sb.blo.resize(3 * size_t(n));
   sb.bhi.resize(3 * size_t(n));
   sb.cen.resize(3 * size_t(n));
-  for (int r = 0; r < n; ++r) {
-    const HostTri& t = H.tris[H.dfs_tris[r]];
+  for (int t = 0; t < n; ++t) {
+    const float* p = v + 9 * size_t(t);
     for (int a = 0; a < 3; ++a) {
-      // vertices are float values, so the float box is exact
-      const float x = float(t.v1[a]), y = float(t.v2[a]), z = float(t.v3[a]);
-      sb.blo[3 * r + a] = std::min({x, y, z});
-      sb.bhi[3 * r + a] = std::max({x, y, z});
-      sb.cen[3 * r + a] = 0.5f * (sb.blo[3 * r + a] + sb.bhi[3 * r + a]);
+      const float x = p[a], y = p[3 + a], z = p[6 + a];
+      sb.blo[3 * t + a] = std::min({x, y, z});
+      sb.bhi[3 * t + a] = std::max({x, y, z});
+      sb.cen[3 * t + a] = 0.5f * (sb.blo[3 * t + a] + sb.bhi[3 * t + a]);
     }
-    H.search.order[r] = r;
+    out.order[t] = t;
   }
-  H.search.nodes.reserve(size_t(n) / 2 + 2);
-  H.search.nodes.emplace_back();  // root
+  out.nodes.reserve(size_t(n) / 2 + 2);
+  out.nodes.emplace_back();  // root
   FBox box;
   const int ref = sb.build(0, n, 1, box);
-  SearchNode& root = H.search.nodes[0];
+  SearchNode& root = out.nodes[0];
   if (ref >= 0) {  // the root's children become node 0's children
-    root = H.search.nodes[size_t(ref)];
+    root = out.nodes[size_t(ref)];
     // node `ref` stays as an unreachable copy
   } else {  // the whole scene is one leaf: one child, the other an empty leaf
     for (int a = 0; a < 3; ++a) {
@@ -616,7 +655,24 @@ void build_search_bvh(HostScene& H) {
     root.child[0] = ref;
     root.child[1] = ~0;  // first 0, count 0
   }
-  H.search.max_depth = sb.max_depth;
+  out.max_depth = sb.max_depth;
+}
+
+}  // namespace
+
+void build_search_bvh(HostScene& H) {
+  std::vector<float> v(9 * H.tris.size());
+  for (size_t t = 0; t < H.tris.size(); ++t)
+    for (int a = 0; a < 3; ++a) {
+      // vertices are float values, so the float copies are exact
+      v[9 * t + a] = float(H.tris[t].v1[a]);
+      v[9 * t + 3 + a] = float(H.tris[t].v2[a]);
+      v[9 * t + 6 + a] = float(H.tris[t].v3[a]);
+    }
+  build_search_bvh_ids(v.data(), int(H.tris.size()), H.search);
+  std::vector<int> rank_of(H.tris.size());
+  for (size_t r = 0; r < H.dfs_tris.size(); ++r) rank_of[size_t(H.dfs_tris[r])] = int(r);
+  for (int& o : H.search.order) o = rank_of[size_t(o)];
 }
 
 void icosphere(int level, std::vector<double>& dirs) {
