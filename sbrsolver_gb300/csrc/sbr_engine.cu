@@ -101,7 +101,9 @@ static uint32_t next_pow2(uint64_t x) {
 // separate streams and overlap on the GPU.
 struct Workspace {
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // the direct-path test, concurrent with the trace
   cudaEvent_t ev[8] = {};
+  cudaEvent_t fork = nullptr, join = nullptr;
   DBuf<TxParams> txp;
   DBuf<double> rx;
   DBuf<int> rx_req;
@@ -121,6 +123,8 @@ struct Workspace {
   DBuf<Survivor> surv;
   DBuf<int> s_counts, s_starts, s_cursor, s_order;
   DBuf<double> path_field, path_pts, field;
+  DBuf<SegTerms> seg;                  // field terms per path segment
+  DBuf<int> path_mat;                  // material of each ray's start per path
   DBuf<double> path_field64, field64;  // FP64 shadow of an FP32 field (field_check)
   DBuf<int> path_nray, path_tri, path_cop, path_kind, path_near;
   DBuf<Counters> ctr;
@@ -140,7 +144,10 @@ struct Workspace {
   ~Workspace() {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
     if (stream) cudaStreamDestroy(stream);
+    if (side) cudaStreamDestroy(side);
   }
 };
 
@@ -516,8 +523,11 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
   if (S.host.mesh_order.empty()) throw std::string("scene is not initialised");
   CK(cudaSetDevice(S.device));
   if (!W.stream) CK(cudaStreamCreateWithFlags(&W.stream, cudaStreamNonBlocking));
+  if (!W.side) CK(cudaStreamCreateWithFlags(&W.side, cudaStreamNonBlocking));
   if (!W.ev[0])
     for (auto& e : W.ev) CK(cudaEventCreate(&e));
+  if (!W.fork) CK(cudaEventCreateWithFlags(&W.fork, cudaEventDisableTiming));
+  if (!W.join) CK(cudaEventCreateWithFlags(&W.join, cudaEventDisableTiming));
   st = W.stream;
   // ---- request table
   std::vector<TxParams> tp(n_req);
@@ -688,6 +698,15 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ++nl, k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_keys.p, W.cap_dd, kEmptyKey);
     ++nl, k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_rank.p, W.cap_dd, kEmptyKey);
     CK(cudaEventRecord(W.ev[2], st));
+    // The direct-path test of every receiver (DirectPathCorrection) needs
+    // only the scene and the receivers: it runs on the side stream while the
+    // trace runs, and the capture stage waits for it.
+    CK(cudaEventRecord(W.fork, st));
+    CK(cudaStreamWaitEvent(W.side, W.fork, 0));
+    if (rx_total)
+      ++nl, k_direct<<<grid_for(rx_total, 64), 64, 0, W.side>>>(S.dev, W.txp.p, W.rx.p, W.rx_req.p,
+                                                             rx_total, W.direct_ok.p, W.ctr.p);
+    CK(cudaEventRecord(W.join, W.side));
     // ---- trace
     TraceArgs ta;
     ta.sc = S.dev;
@@ -765,9 +784,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ca.pair_cap = W.cap_pairs;
     ca.work = W.find_work.p;  // the trace is done with it
     CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
-    if (rx_total)
-      ++nl, k_direct<<<grid_for(rx_total, 64), 64, 0, st>>>(S.dev, W.txp.p, W.rx.p, W.rx_req.p, rx_total,
-                                                      W.direct_ok.p, W.ctr.p);
+    CK(cudaStreamWaitEvent(st, W.join, 0));
     if (stage_counts) {
       ++nl, k_capture<true><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
     } else {
@@ -840,6 +857,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.path_kind.ensure(nsa * (kMaxDepth + 1));
     W.path_near.ensure(nsa);
     W.path_pts.ensure(nsa * (kMaxDepth + 2) * 3);
+    W.seg.ensure(nsa * (kMaxDepth + 1));
+    W.path_mat.ensure(nsa * (kMaxDepth + 1));
     W.field.ensure(std::max(1, 6 * rx_total));
     W.s_counts.ensure(rx_total + 1);
     W.s_starts.ensure(rx_total + 2);
@@ -864,7 +883,13 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fa.path_kind = W.path_kind.p;
     fa.path_near_edge = W.path_near.p;
     fa.path_pts = W.path_pts.p;
-    if (ns) ++nl, k_field<<<grid_for(ns, 64), 64, 0, st>>>(fa);
+    fa.seg = W.seg.p;
+    fa.path_mat = W.path_mat.p;
+    if (ns) {
+      ++nl, k_path<<<grid_for(ns, 64), 64, 0, st>>>(fa);
+      ++nl, k_seg<<<grid_for(ns * (kMaxDepth + 1), 64), 64, 0, st>>>(fa);
+      ++nl, k_combine<<<grid_for(ns, 64), 64, 0, st>>>(fa);
+    }
     CK(cudaMemsetAsync(W.s_counts.p, 0, sizeof(int) * (rx_total + 1), st));
     CK(cudaMemsetAsync(W.s_cursor.p, 0, sizeof(int) * (rx_total + 1), st));
     if (ns) ++nl, k_surv_hist<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv, W.s_counts.p);
@@ -884,7 +909,10 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       FieldArgs f64 = fa;
       f64.precision = 0;
       f64.path_field = W.path_field64.p;
-      if (ns) ++nl, k_field<<<grid_for(ns, 64), 64, 0, st>>>(f64);
+      if (ns) {
+        ++nl, k_seg<<<grid_for(ns * (kMaxDepth + 1), 64), 64, 0, st>>>(f64);
+        ++nl, k_combine<<<grid_for(ns, 64), 64, 0, st>>>(f64);
+      }
       if (rx_total)
         ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
                                                           rx_total, W.path_field64.p, 0,

@@ -122,13 +122,6 @@ __device__ __forceinline__ void mcv(const M3<R>& a, const Cx<R>* v, Cx<R>* r) { 
     r[i] = (a.m[3 * i] * v[0] + a.m[3 * i + 1] * v[1]) + a.m[3 * i + 2] * v[2];
 }
 
-// TransformationMatrix(theta, phi, sph2Cart=true), VecMatDef.h:85-99
-template <class R>
-__device__ __forceinline__ M3<R> sph_frame(R th, R ph) {
-  R st = sin(th), sp = sin(ph), ct = cos(th), cp = cos(ph);
-  return M3<R>{{st * cp, ct * cp, -sp, st * sp, ct * sp, cp, ct, -st, R(0)}};
-}
-
 // Tabulated antenna pattern (the TXPattern.dat grid of data/TXPattern.dat,
 // which Preprocessor::ReadPatternFile loads, Preprocessor.cpp:3-35): complex
 // relative amplitudes of E_theta and E_phi on a regular (theta, phi) grid in
@@ -211,103 +204,157 @@ __device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, Cx<R> ph, boo
   }
 }
 
-// One corrected path: n rays with endpoints pts[i] -> pts[i+1], the hit
-// triangle frame of ray i's end (or none for the last ray), and the kind /
-// material of each ray's start.  Returns E (3 complex, global Cartesian).
-// R: real type of the rotation/Fresnel arithmetic.  fp32_phase: also take the
-// path length and the phase k*L in FP32 (only to measure what FP64 phase buys).
-template <class R, bool fp32_phase = false>
-__device__ void path_field(int n, const double (*pts)[3], const double* const* frames,
-                           const int* kind, const int* mat, const Material* mats,
-                           const double* txcs, double freq, double pt, int antenna,
-                           bool fresnel, const FieldConsts& K, Cx<double>* out,
-                           const PatternTab* pat = nullptr) {
+// FieldForPath (FieldCompute.cpp:71-151) in two parts.  Everything a segment
+// contributes except the field it carries depends only on the path's geometry:
+// its length, the spherical angles of its direction in the frame it starts in,
+// the coefficients of the interaction at its start and, for the launch
+// segment, the antenna pattern.  seg_terms computes those for one segment (one
+// thread per segment, so the long FP64 chains of the transcendental functions
+// run side by side); path_combine then carries the field along the path with
+// the same operations, in the same order, as one sequential pass would.
+// R: real type of the rotation/Fresnel arithmetic.  Values of type R are
+// stored as doubles, which holds floats exactly.
+struct SegTerms {
+  double r;               // segment length (FP64)
+  double st, ct, sp, cp;  // sin / cos of the direction's theta and phi
+  double ctm[2], cte[2];  // TM / TE coefficients of the interaction at the start
+  double inc[6];          // launch segment: the pattern's field (r, theta, phi)
+};
+
+// The frame a segment starts in: the transmitter's for the launch segment,
+// else the frame of the triangle the previous segment ended on (none: global).
+template <class R>
+__device__ __forceinline__ M3<R> start_frame(int i, const double* const* frames,
+                                             const double* txcs) {
+  M3<R> f;
+  const double* src = i == 0 ? txcs : frames[i - 1];
+  if (src == nullptr) {
+    for (int j = 0; j < 9; ++j) f.m[j] = (j % 4 == 0) ? R(1) : R(0);
+  } else {
+    for (int j = 0; j < 9; ++j) f.m[j] = R(src[j]);
+  }
+  return f;
+}
+
+// Segment i of a path with points pts (i -> i+1), triangle frames frames[k]
+// of the triangle ray k ends on (null = none), and the kind / material of
+// each ray's start.
+template <class R>
+__device__ void seg_terms(int i, const double (*pts)[3], const double* const* frames,
+                          const int* kind, const int* mat, const Material* mats,
+                          const double* txcs, double freq, double pt, int antenna, bool fresnel,
+                          const FieldConsts& K, SegTerms& out, const PatternTab* pat = nullptr) {
   const double lam64 = 2.99792458e8 / freq;
-  M3<R> cur, next;
-  for (int i = 0; i < 9; ++i) next.m[i] = R(txcs[i]);
+  const M3<R> cur = start_frame<R>(i, frames, txcs);
+  double vg64[3] = {pts[i + 1][0] - pts[i][0], pts[i + 1][1] - pts[i][1], pts[i + 1][2] - pts[i][2]};
+  R vg[3] = {R(vg64[0]), R(vg64[1]), R(vg64[2])};
+  R vl[3];
+  mv(cur, vg, vl);
+  // CartesianToSpherical (VecMatDef.h:132-155); r is kept in FP64.  In FP64
+  // it is the length of the rotated vector, as in the reference.  With FP32
+  // frames it is the length of the global vector: a frame rounded to FP32 is
+  // orthonormal only to ~1e-7, which would move r by ~1e-7 r (1e-3 rad of
+  // phase for a 50 m segment at 28 GHz).
+  if constexpr (sizeof(R) == sizeof(double)) {
+    double vl64[3];
+    for (int j = 0; j < 3; ++j)
+      vl64[j] = (cur.m[3 * j] * vg64[0] + cur.m[3 * j + 1] * vg64[1]) + cur.m[3 * j + 2] * vg64[2];
+    out.r = sqrt((vl64[0] * vl64[0] + vl64[1] * vl64[1]) + vl64[2] * vl64[2]);
+  } else {
+    out.r = sqrt((vg64[0] * vg64[0] + vg64[1] * vg64[1]) + vg64[2] * vg64[2]);
+  }
+  R th, ph;
+  if (vl[0] == R(0) && vl[1] == R(0) && vl[2] == R(0)) th = R(K.pi_hi * 0.5);
+  else th = atan2(sqrt(vl[0] * vl[0] + vl[1] * vl[1]), vl[2]);
+  ph = atan2(vl[1], vl[0]);
+  if (ph < R(0)) ph = R((double(ph) + 2.0 * K.pi_hi) + 2.0 * K.pi_lo);
+  out.st = double(sin(th));
+  out.ct = double(cos(th));
+  out.sp = double(sin(ph));
+  out.cp = double(cos(ph));
+  for (int j = 0; j < 6; ++j) out.inc[j] = 0.0;
+  if (i == 0) {
+    Cx<R> inc[3] = {cx(R(0)), cx(R(0)), cx(R(0))};
+    if (antenna == 0) inc[0] = cx(R(0), R(sqrt(60.0 * pt)));
+    if (antenna == 1) inc[1] = cx(R(0), R(sqrt(60.0 * pt * 1.5)) * sin(th));
+    else if (antenna == 2)
+      inc[1] = cx(R(0), R(sqrt(60.0 * pt)) * (cos(R(K.pi_hi) * cos(th) / R(2)) / sin(th)));
+    else if (antenna == 3 && pat) {
+      double a[4];
+      pattern_at(*pat, double(th) * (180.0 / K.pi_hi), double(ph) * (180.0 / K.pi_hi), a);
+      const double amp = sqrt(60.0 * pt);
+      inc[1] = cx(R(amp * a[0]), R(amp * a[1]));
+      inc[2] = cx(R(amp * a[2]), R(amp * a[3]));
+    }
+    for (int j = 0; j < 3; ++j) {
+      out.inc[2 * j] = double(inc[j].re);
+      out.inc[2 * j + 1] = double(inc[j].im);
+    }
+  }
+  Cx<R> ctm = cx(R(1)), cte = cx(R(1));
+  if (kind[i] != 0) {
+    // AngleBetween(vecGlobal, current row 2) in radians (VecMatDef.h:56-77)
+    R a[3] = {vg[0], vg[1], vg[2]}, b[3] = {cur.m[6], cur.m[7], cur.m[8]};
+    R za = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
+    if (za > R(0)) { R s = sqrt(za); a[0] /= s; a[1] /= s; a[2] /= s; }
+    R zb = (b[0] * b[0] + b[1] * b[1]) + b[2] * b[2];
+    if (zb > R(0)) { R s = sqrt(zb); b[0] /= s; b[1] /= s; b[2] /= s; }
+    R ratio = (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+    R ang;
+    if (ratio < R(0)) {
+      R e0 = -a[0] - b[0], e1 = -a[1] - b[1], e2 = -a[2] - b[2];
+      R y = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
+      ang = R((K.pi_hi - double(y)) + K.pi_lo);
+    } else {
+      R e0 = a[0] - b[0], e1 = a[1] - b[1], e2 = a[2] - b[2];
+      ang = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
+    }
+    const Material& m = mats[mat[i]];
+    const Cx<double> eps64 = cx(m.eps_re, -1.0 * m.sigma / (K.e0 * 2.0 * K.pi_hi * freq));
+    const Cx<R> eps_t = cx(R(eps64.re), R(eps64.im));
+    Cx<R> sph = cx(R(1));
+    if (!fresnel) {
+      const Cx<double> p64 = slab_phase(double(ang), eps64, lam64, m.width, 2.0 * K.pi_hi);
+      sph = cx(R(p64.re), R(p64.im));
+    }
+    fresnel_pair<R>(kind[i] == 1, ang, eps_t, sph, fresnel, R(K.eta0), ctm, cte);
+  }
+  out.ctm[0] = double(ctm.re);
+  out.ctm[1] = double(ctm.im);
+  out.cte[0] = double(cte.re);
+  out.cte[1] = double(cte.im);
+}
+
+// The field at the end of an n-ray path from its segments' terms
+// (FieldCompute.cpp:99-148): E * exp(-j k L) / L, k L in FP64.
+// fp32_phase: take the path length and the phase k*L in FP32 (only to measure
+// what FP64 phase buys).
+template <class R, bool fp32_phase = false>
+__device__ void path_combine(int n, const SegTerms* seg, const double (*pts)[3],
+                             const double* const* frames, const int* kind, const double* txcs,
+                             double freq, const FieldConsts& K, Cx<double>* out) {
+  const double lam64 = 2.99792458e8 / freq;
   Cx<R> tot[3] = {cx(R(0)), cx(R(0)), cx(R(0))};
   double L = 0.0;
   for (int i = 0; i < n; ++i) {
-    double vg64[3] = {pts[i + 1][0] - pts[i][0], pts[i + 1][1] - pts[i][1], pts[i + 1][2] - pts[i][2]};
-    R vg[3] = {R(vg64[0]), R(vg64[1]), R(vg64[2])};
-    R vl[3];
-    mv(next, vg, vl);
-    // CartesianToSpherical (VecMatDef.h:132-155); r is kept in FP64.  In FP64
-    // it is the length of the rotated vector, as in the reference.  With FP32
-    // frames it is the length of the global vector: a frame rounded to FP32 is
-    // orthonormal only to ~1e-7, which would move r by ~1e-7 r (1e-3 rad of
-    // phase for a 50 m segment at 28 GHz).
-    double r;
-    if constexpr (sizeof(R) == sizeof(double)) {
-      double vl64[3];
-      for (int j = 0; j < 3; ++j)
-        vl64[j] = (next.m[3 * j] * vg64[0] + next.m[3 * j + 1] * vg64[1]) + next.m[3 * j + 2] * vg64[2];
-      r = sqrt((vl64[0] * vl64[0] + vl64[1] * vl64[1]) + vl64[2] * vl64[2]);
-    } else {
-      r = sqrt((vg64[0] * vg64[0] + vg64[1] * vg64[1]) + vg64[2] * vg64[2]);
-    }
-    R th, ph;
-    if (vl[0] == R(0) && vl[1] == R(0) && vl[2] == R(0)) th = R(K.pi_hi * 0.5);
-    else th = atan2(sqrt(vl[0] * vl[0] + vl[1] * vl[1]), vl[2]);
-    ph = atan2(vl[1], vl[0]);
-    if (ph < R(0)) ph = R((double(ph) + 2.0 * K.pi_hi) + 2.0 * K.pi_lo);
-    L += r;
-    cur = next;
-    if (frames[i] == nullptr) {
-      for (int j = 0; j < 9; ++j) next.m[j] = (j % 4 == 0) ? R(1) : R(0);
-    } else {
-      for (int j = 0; j < 9; ++j) next.m[j] = R(frames[i][j]);
-    }
+    const SegTerms& t = seg[i];
+    const M3<R> cur = start_frame<R>(i, frames, txcs);
+    L += t.r;
+    const R st = R(t.st), ct = R(t.ct), sp = R(t.sp), cp = R(t.cp);
+    // TransformationMatrix(theta, phi, sph2Cart=true), VecMatDef.h:85-99
+    const M3<R> T{{st * cp, ct * cp, -sp, st * sp, ct * sp, cp, ct, -st, R(0)}};
     Cx<R> inc[3];
-    const M3<R> T = sph_frame(th, ph);
     if (i == 0) {
-      inc[0] = inc[1] = inc[2] = cx(R(0));
-      if (antenna == 0) inc[0] = cx(R(0), R(sqrt(60.0 * pt)));
-      if (antenna == 1) inc[1] = cx(R(0), R(sqrt(60.0 * pt * 1.5)) * sin(th));
-      else if (antenna == 2)
-        inc[1] = cx(R(0), R(sqrt(60.0 * pt)) * (cos(R(K.pi_hi) * cos(th) / R(2)) / sin(th)));
-      else if (antenna == 3 && pat) {
-        double a[4];
-        pattern_at(*pat, double(th) * (180.0 / K.pi_hi), double(ph) * (180.0 / K.pi_hi), a);
-        const double amp = sqrt(60.0 * pt);
-        inc[1] = cx(R(amp * a[0]), R(amp * a[1]));
-        inc[2] = cx(R(amp * a[2]), R(amp * a[3]));
-      }
+      for (int j = 0; j < 3; ++j) inc[j] = cx(R(t.inc[2 * j]), R(t.inc[2 * j + 1]));
     } else {
       Cx<R> g[3];
       mtv(cur, tot, g);   // RotateToNewCoordSys(E, current, global) = current^T E
       mtv(T, g, inc);     // CartesianToSphericalVector = T^T
     }
     if (kind[i] != 0) {
-      // AngleBetween(vecGlobal, current row 2) in radians (VecMatDef.h:56-77)
-      R a[3] = {vg[0], vg[1], vg[2]}, b[3] = {cur.m[6], cur.m[7], cur.m[8]};
-      R za = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
-      if (za > R(0)) { R s = sqrt(za); a[0] /= s; a[1] /= s; a[2] /= s; }
-      R zb = (b[0] * b[0] + b[1] * b[1]) + b[2] * b[2];
-      if (zb > R(0)) { R s = sqrt(zb); b[0] /= s; b[1] /= s; b[2] /= s; }
-      R ratio = (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
-      R ang;
-      if (ratio < R(0)) {
-        R e0 = -a[0] - b[0], e1 = -a[1] - b[1], e2 = -a[2] - b[2];
-        R y = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
-        ang = R((K.pi_hi - double(y)) + K.pi_lo);
-      } else {
-        R e0 = a[0] - b[0], e1 = a[1] - b[1], e2 = a[2] - b[2];
-        ang = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
-      }
-      const Material& m = mats[mat[i]];
-      const Cx<double> eps64 = cx(m.eps_re, -1.0 * m.sigma / (K.e0 * 2.0 * K.pi_hi * freq));
-      const Cx<R> eps_t = cx(R(eps64.re), R(eps64.im));
-      Cx<R> ph = cx(R(1));
-      if (!fresnel) {
-        const Cx<double> p64 = slab_phase(double(ang), eps64, lam64, m.width, 2.0 * K.pi_hi);
-        ph = cx(R(p64.re), R(p64.im));
-      }
-      Cx<R> ctm, cte;
-      fresnel_pair<R>(kind[i] == 1, ang, eps_t, ph, fresnel, R(K.eta0), ctm, cte);
       tot[0] = inc[0];
-      tot[1] = inc[1] * ctm;
-      tot[2] = inc[2] * cte;
+      tot[1] = inc[1] * cx(R(t.ctm[0]), R(t.ctm[1]));
+      tot[2] = inc[2] * cx(R(t.cte[0]), R(t.cte[1]));
     } else {
       tot[0] = inc[0];
       tot[1] = inc[1];

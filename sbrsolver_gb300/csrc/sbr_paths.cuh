@@ -48,17 +48,14 @@ __device__ __forceinline__ bool class_path(const ClassInfo* info, uint32_t cls, 
 }
 
 // GetImageSources + MultiPathCorrection / DirectPathCorrection
-// (RTSolver.cpp:330-433).  Fills pb.pts with the corrected points.
+// (RTSolver.cpp:330-433) for a path whose correction succeeded when it was
+// captured (correct_event; k_direct for the direct path): fills pb.pts with
+// the corrected points.
 __device__ bool correct_path(const DevScene& sc, const int* rank_to_id, const TxParams& P,
-                             const double* rxp, PathBuf& pb, unsigned* overflow) {
+                             const double* rxp, PathBuf& pb) {
   using namespace x64;
   const double* tx = P.tx;
-  if (pb.n == 1) {
-    double d[3];
-    sub3(rxp, tx, d);
-    Hit h;
-    const bool has = exact_closest(sc, tx, d, h, overflow);
-    if (has && !(norm(d) < h.dist)) return false;
+  if (pb.n == 1) {  // the exact segment Tx -> Rx (RTSolver.cpp:385-387)
     for (int a = 0; a < 3; ++a) {
       pb.pts[0][a] = tx[a];
       pb.pts[1][a] = rxp[a];
@@ -172,6 +169,8 @@ struct FieldArgs {
   int* path_kind;
   int* path_near_edge;  // 1 if an interaction point is within 1e-6 of its triangle's edge
   double* path_pts;     // (kMaxDepth + 2) * 3 per survivor
+  SegTerms* seg;        // (kMaxDepth + 1) per survivor
+  int* path_mat;        // (kMaxDepth + 1) per survivor: material of each ray's start
 };
 
 // Barycentric distance of a point (on the triangle's plane) from the
@@ -189,39 +188,19 @@ __device__ __forceinline__ int near_edge(const CorrTri& T, const double* p, doub
   return fmin(fmin(u, v), 1.0 - u - v) < tol ? 1 : 0;
 }
 
-__global__ void k_field(FieldArgs A) {
+// Field stage, one kernel per part: k_path corrects each survivor's path
+// (FP64 image correction, sequential along the path) and writes its points,
+// triangles and kinds; k_seg computes every segment's terms (one thread per
+// segment); k_combine carries each path's field along it.
+__global__ void k_path(FieldArgs A) {
   const unsigned long long ns = min(A.ctr->survivors, A.cap);
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     const Survivor sv = A.surv[i];
-    const uint32_t cls = sv.cls;
     const TxParams& P = A.txp[A.rx_req[sv.rx]];
     PathBuf pb;
-    class_path(A.cls_info, cls, pb);
-    correct_path(A.sc, A.rank_to_id, P, A.rx + 3 * size_t(sv.rx), pb, &A.ctr->overflow);
-    const double* frames[kMaxDepth + 1];
-    int mat[kMaxDepth + 1];
-    mat[0] = 0;
-    for (int r = 0; r < pb.n; ++r) {
-      frames[r] = pb.tri[r] >= 0 ? A.sc.corr[A.rank_to_id[pb.tri[r]]].cs : nullptr;
-      if (r + 1 < pb.n) mat[r + 1] = A.sc.tri64[pb.tri[r]].mat;
-    }
-    Cx<double> e[3];
-    const PatternTab pat{P.pat, P.pat_nt, P.pat_np, P.pat_dt, P.pat_dp};
-    const int prec = A.precision < 0 ? P.precision : A.precision;
-    if (prec == 2)
-      path_field<float, true>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq,
-                              P.pt, P.antenna, P.fresnel != 0, A.K, e, &pat);
-    else if (prec == 1)
-      path_field<float>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
-                        P.antenna, P.fresnel != 0, A.K, e, &pat);
-    else
-      path_field<double>(pb.n, pb.pts, frames, pb.kind, mat, A.sc.mats, P.txcs, P.freq, P.pt,
-                         P.antenna, P.fresnel != 0, A.K, e, &pat);
-    for (int j = 0; j < 3; ++j) {
-      A.path_field[6 * i + 2 * j] = e[j].re;
-      A.path_field[6 * i + 2 * j + 1] = e[j].im;
-    }
+    class_path(A.cls_info, sv.cls, pb);
+    correct_path(A.sc, A.rank_to_id, P, A.rx + 3 * size_t(sv.rx), pb);
     A.path_nray[i] = pb.n;
     const size_t b = size_t(i) * (kMaxDepth + 1);
     for (int r = 0; r < pb.n; ++r) {
@@ -229,6 +208,8 @@ __global__ void k_field(FieldArgs A) {
       A.path_tri[b + r] = t >= 0 ? A.rank_to_id[t] : -1;
       A.path_cop[b + r] = t >= 0 ? A.sc.tri64[t].cop : -1;
       A.path_kind[b + r] = pb.kind[r];
+      // the hit triangle's own material (the ray's hit record carries it)
+      A.path_mat[b + r] = r > 0 ? A.sc.tri64[pb.tri[r - 1]].mat : 0;
     }
     const size_t bp = size_t(i) * (kMaxDepth + 2) * 3;
     for (int r = 0; r <= pb.n; ++r)
@@ -238,6 +219,79 @@ __global__ void k_field(FieldArgs A) {
     for (int r = 0; r + 1 < pb.n; ++r)
       near |= near_edge(A.sc.corr[A.rank_to_id[pb.tri[r]]], pb.pts[r + 1], 1e-6);
     A.path_near_edge[i] = near;
+  }
+}
+
+// The path inputs of path i for the field functions: points, frames of the
+// triangles each ray ends on, kinds and materials of each ray's start.
+struct PathView {
+  int n;
+  const double (*pts)[3];
+  const double* frames[kMaxDepth + 1];
+  int kind[kMaxDepth + 1];
+  int mat[kMaxDepth + 1];
+};
+
+__device__ __forceinline__ void path_view(const FieldArgs& A, unsigned long long i, PathView& v) {
+  v.n = A.path_nray[i];
+  v.pts = reinterpret_cast<const double(*)[3]>(A.path_pts + size_t(i) * (kMaxDepth + 2) * 3);
+  const size_t b = size_t(i) * (kMaxDepth + 1);
+  for (int r = 0; r < v.n; ++r) {
+    // frames by the id's position in the caller's mesh vector, as the
+    // reference looks them up (FieldCompute.cpp:107)
+    const int id = A.path_tri[b + r];
+    v.frames[r] = id >= 0 ? A.sc.corr[id].cs : nullptr;
+    v.kind[r] = A.path_kind[b + r];
+    v.mat[r] = A.path_mat[b + r];
+  }
+}
+
+__global__ void k_seg(FieldArgs A) {
+  const unsigned long long ns = min(A.ctr->survivors, A.cap);
+  const unsigned long long n_slots = ns * (kMaxDepth + 1);
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+       k < n_slots; k += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long i = k / (kMaxDepth + 1);
+    const int r = int(k % (kMaxDepth + 1));
+    if (r >= A.path_nray[i]) continue;
+    const Survivor sv = A.surv[i];
+    const TxParams& P = A.txp[A.rx_req[sv.rx]];
+    PathView v;
+    path_view(A, i, v);
+    const PatternTab pat{P.pat, P.pat_nt, P.pat_np, P.pat_dt, P.pat_dp};
+    const int prec = A.precision < 0 ? P.precision : A.precision;
+    SegTerms t;
+    if (prec != 0)
+      seg_terms<float>(r, v.pts, v.frames, v.kind, v.mat, A.sc.mats, P.txcs, P.freq, P.pt,
+                       P.antenna, P.fresnel != 0, A.K, t, &pat);
+    else
+      seg_terms<double>(r, v.pts, v.frames, v.kind, v.mat, A.sc.mats, P.txcs, P.freq, P.pt,
+                        P.antenna, P.fresnel != 0, A.K, t, &pat);
+    A.seg[k] = t;
+  }
+}
+
+__global__ void k_combine(FieldArgs A) {
+  const unsigned long long ns = min(A.ctr->survivors, A.cap);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const Survivor sv = A.surv[i];
+    const TxParams& P = A.txp[A.rx_req[sv.rx]];
+    PathView v;
+    path_view(A, i, v);
+    const SegTerms* seg = A.seg + size_t(i) * (kMaxDepth + 1);
+    Cx<double> e[3];
+    const int prec = A.precision < 0 ? P.precision : A.precision;
+    if (prec == 2)
+      path_combine<float, true>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e);
+    else if (prec == 1)
+      path_combine<float>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e);
+    else
+      path_combine<double>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e);
+    for (int j = 0; j < 3; ++j) {
+      A.path_field[6 * i + 2 * j] = e[j].re;
+      A.path_field[6 * i + 2 * j + 1] = e[j].im;
+    }
   }
 }
 
