@@ -14,6 +14,15 @@ namespace sbr {
 constexpr double kEps64 = 1.1920928955078125e-07;  // FLT_EPSILON as double, Constants.h:13
 constexpr float kEps32 = 1.1920928955078125e-07f;
 constexpr float kFiltK = 6.103515625e-05f;         // 2^-14: FP32 filter margin factor
+// Relative slack when a bound on a contender's t is compared with another
+// hit's t: a contender whose lower bound exceeds t * (1 + kTieSlack) lies
+// farther along the ray, so its FP64 distance is larger (distances of one ray
+// are t |d| to within a few FP64 ulps); the slack covers that and the FP32
+// rounding of the product.
+#ifndef SBR_TIE_SLACK
+#define SBR_TIE_SLACK 9.5367431640625e-07f  // 2^-20
+#endif
+constexpr float kTieSlack = SBR_TIE_SLACK;
 
 struct Hit {
   double t, dist;
@@ -369,7 +378,7 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
           cand_leaf[ncand] = pending_leaf;
           cand_t[ncand] = tlo;
           ++ncand;
-          if (k == 2) tcut = fminf(tcut, thi * (1.0f + 1.0f / 4096.0f) + 1e-30f);
+          if (k == 2) tcut = fminf(tcut, thi * (1.0f + kTieSlack) + 1e-30f);
         } else {
           overflowed = true;  // too many contenders: resolve this one now
           ++st.fp64_tri;
@@ -383,7 +392,7 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
             best.p[2] = P[2];
             best.rank = r;
             best.leaf = pending_leaf;
-            tcut = fminf(tcut, float(t) * (1.0f + 1.0f / 4096.0f) + 1e-30f);
+            tcut = fminf(tcut, float(t) * (1.0f + kTieSlack) + 1e-30f);
           }
         }
       }
@@ -458,7 +467,7 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
     cand_leaf[j + 1] = kl;
   }
   for (int i = 0; i < ncand; ++i) {
-    if (best.rank != INT_MAX && cand_t[i] > float(best.t) * (1.0f + 1.0f / 4096.0f) + 1e-30f) break;
+    if (best.rank != INT_MAX && cand_t[i] > float(best.t) * (1.0f + kTieSlack) + 1e-30f) break;
     const int r = cand_r[i];
     ++st.fp64_tri;
     double t, P[3], dist;
@@ -546,7 +555,7 @@ __device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d
   best.dist = __longlong_as_double(0x7ff0000000000000ll);
   best.t = best.dist;
   for (int i = 0; i < nc; ++i) {
-    if (best.rank != INT_MAX && ct[i] > float(best.t) * (1.0f + 1.0f / 4096.0f) + 1e-30f) break;
+    if (best.rank != INT_MAX && ct[i] > float(best.t) * (1.0f + kTieSlack) + 1e-30f) break;
     const int r = cr[i];
     if (r == orank && origin_rejected(sc.tri32[r], o, d)) continue;
     ++st.fp64_tri;

@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
           break;
         }
         out[nc++] = make_uint2(unsigned(__ldg(A.sc.srank + j)), __float_as_uint(tlo));
-        if (k == 2) tcut = fminf(tcut, thi * (1.0f + 1.0f / 4096.0f) + 1e-30f);
+        if (k == 2) tcut = fminf(tcut, thi * (1.0f + kTieSlack) + 1e-30f);
         continue;
       }
       if (sp == 0) {
