@@ -62,7 +62,10 @@ long long estimate_bytes(const sbr_request& q) {
 constexpr size_t kMaxBatch = 64;
 // Waiting time converted to priority: a request that has waited one second
 // ranks like one whose estimate is 16 GB smaller.
-constexpr double kAgingBytesPerSec = 16e9;
+#ifndef SBR_SERVER_AGING
+#define SBR_SERVER_AGING 16e9
+#endif
+constexpr double kAgingBytesPerSec = SBR_SERVER_AGING;
 // Requests at most this large (device-memory estimate) are batched together.
 constexpr long long kSmallBytes = 512LL << 20;
 
