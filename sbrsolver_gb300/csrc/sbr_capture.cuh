@@ -239,7 +239,7 @@ __device__ __forceinline__ ChunkBox chunk_box(const NodeHot& nd, const RxGrid& g
   const float pb[3] = {s.x + cb.b * u.x, s.y + cb.b * u.y, s.z + cb.b * u.z};
   const float npmax = fmaxf(sqrt_up(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]),
                             sqrt_up(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]));
-  cb.mr = kFiltK * (sp.ns + cmax + S + npmax + 1.0f);
+  cb.mr = kRecK * (sp.ns + cmax + S + npmax + 1.0f);
   // |P| is convex along the chunk: the larger end bounds it
   cb.rb = (S + npmax) * tanb * 1.0002f + g.cell * 0.01f + 2e-3f + cb.mr;
   for (int k = 0; k < 3; ++k) {
@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k
         const int nchunk = sp.nchunk;
         const float step = sp.step;
         // error margins of the FP32 reception test, from per-node bounds
-        const float ml = kFiltK * (ns + cmax + 1.0f);
+        const float ml = kRecK * (ns + cmax + 1.0f);
         {
           for (int ch = 0; ch < nchunk; ++ch) {
             const ChunkBox cb = ch == 0 ? s_ck[warp][jj]

@@ -14,6 +14,15 @@ namespace sbr {
 constexpr double kEps64 = 1.1920928955078125e-07;  // FLT_EPSILON as double, Constants.h:13
 constexpr float kEps32 = 1.1920928955078125e-07f;
 constexpr float kFiltK = 6.103515625e-05f;         // 2^-14: FP32 filter margin factor
+// Margin factor of the FP32 reception test: |dist - radius| and the
+// projection are decided in FP32 only when they clear this times the
+// magnitudes involved (|segment start| + |receiver| + 1 + unfolded length).
+// Bounding every rounding of the FP32 evaluation and of its rounded inputs
+// against the FP64 test gives under 30 * 2^-24 of the same magnitudes.
+#ifndef SBR_REC_K
+#define SBR_REC_K 1.52587890625e-05f  // 2^-16
+#endif
+constexpr float kRecK = SBR_REC_K;
 // Relative slack when a bound on a contender's t is compared with another
 // hit's t: a contender whose lower bound exceeds t * (1 + kTieSlack) lies
 // farther along the ray, so its FP64 distance is larger (distances of one ray
@@ -616,7 +625,7 @@ __device__ __forceinline__ int reception32(const float3& s, const float3& u, flo
   const float ns = sqrtf(s.x * s.x + s.y * s.y + s.z * s.z);
   const float nc = sqrtf(c.x * c.x + c.y * c.y + c.z * c.z);
   const float mag = ns + nc + 1.0f;
-  const float ml = kFiltK * mag;
+  const float ml = kRecK * mag;
   if (lam < -ml) return 0;
   if (lam <= ml) return -1;
   const float lc = fminf(lam, len);
@@ -625,7 +634,7 @@ __device__ __forceinline__ int reception32(const float3& s, const float3& u, flo
   const float ex = c.x - px, ey = c.y - py, ez = c.z - pz;
   const float dist = sqrtf(ex * ex + ey * ey + ez * ez);
   const float rad = (S + np) * tanb;
-  const float mr = kFiltK * (mag + S + np);
+  const float mr = kRecK * (mag + S + np);
   if (dist > rad + mr) return 0;
   if (dist < rad - mr) return 1;
   return -1;
