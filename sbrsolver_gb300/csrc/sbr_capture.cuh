@@ -38,6 +38,8 @@ struct CaptureArgs {
   int stage_counts;
   uint2* pairs;                // (node, receiver | unsure << 31) for k_capture_finish
   unsigned long long pair_cap;
+  HashTable corr_cache;        // (class, receiver) -> its image correction's outcome
+  unsigned char* corr_val;     // per slot: 0 not known yet, 1 fails, 2 succeeds
   unsigned long long* work;    // nodes handed out to warps (zero at launch)
 };
 
@@ -602,8 +604,30 @@ __global__ void __launch_bounds__(128) k_capture_finish(CaptureArgs A) {
       if (!capture_exact(A.nodes_cold, i, c64, P.tan_beta)) continue;
     }
     const float3 c = make_float3(float(c64[0]), float(c64[1]), float(c64[2]));
-    const bool ok = is_root_class(nd.cls) ? A.direct_ok[gi] != 0
-                                          : correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
+    bool ok;
+    if (is_root_class(nd.cls)) {
+      ok = A.direct_ok[gi] != 0;
+    } else {
+      // The correction depends only on the class and the receiver, and the
+      // reception spheres are wide (beta = acos(-1/sqrt 5) / (3 (L + 1))), so
+      // many nodes of one class capture the same receiver: the outcome is
+      // kept per (class, receiver) and each is computed about once.
+      const unsigned long long key = (unsigned long long)nd.cls << 32 | uint32_t(gi);
+      bool fresh = false;
+      const uint32_t slot = ht_claim(A.corr_cache, key, 32, fresh);
+      unsigned char known = 0;
+      if (slot != 0xFFFFFFFFu && !fresh)
+        known = *reinterpret_cast<volatile unsigned char*>(&A.corr_val[slot]);
+      if (known) {
+        ok = known == 2;
+      } else {
+        ok = correct_event(A.sc, A.cls_info, nd.cls, c, c64, n64);
+        if (slot != 0xFFFFFFFFu) {
+          A.corr_val[slot] = ok ? 2 : 1;
+          if (fresh) atomicAdd(&A.ctr->used_cc, 1ull);
+        }
+      }
+    }
     if (!ok) continue;
     const float tanb = float(P.tan_beta);
     bool sup = false;

@@ -60,6 +60,30 @@ __device__ __forceinline__ uint32_t ht_insert(HashTable t, unsigned long long ke
   return 0xFFFFFFFFu;
 }
 
+// Find or claim key's slot in a table that may fill up: the slot, or
+// 0xFFFFFFFF when a probe run of `limit` slots finds neither (the caller then
+// works without the table).  fresh: this call claimed the slot.
+__device__ __forceinline__ uint32_t ht_claim(HashTable t, unsigned long long key, uint32_t limit,
+                                             bool& fresh) {
+  fresh = false;
+  uint32_t h = uint32_t(mix64(key)) & t.mask;
+  const uint32_t lim = min(limit, t.mask + 1);
+  for (uint32_t i = 0; i < lim; ++i) {
+    unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&t.keys[h]);
+    if (k == key) return h;
+    if (k == kEmptyKey) {
+      const unsigned long long old = atomicCAS(&t.keys[h], kEmptyKey, key);
+      if (old == kEmptyKey) {
+        fresh = true;
+        return h;
+      }
+      if (old == key) return h;
+    }
+    h = (h + 1) & t.mask;
+  }
+  return 0xFFFFFFFFu;
+}
+
 __device__ __forceinline__ uint32_t ht_find(HashTable t, unsigned long long key) {
   uint32_t h = uint32_t(mix64(key)) & t.mask;
   const uint32_t lim = min(kMaxProbe, t.mask + 1);

@@ -213,6 +213,7 @@ struct Counters {
   unsigned long long pairs;      // (node, receiver) pairs handed to the FP64 capture pass
   unsigned long long cand;       // receiver candidates tested by the capture stage
   unsigned long long anc;        // ancestor re-tests for suppression
+  unsigned long long used_cc;    // (class, receiver) corrections cached
   unsigned int overflow;         // bit mask of capacity overflows
   unsigned int pad;
 };

@@ -115,6 +115,8 @@ struct Workspace {
   DBuf<NodeHot> nodes;
   DBuf<NodeCold> nodes_cold;
   DBuf<unsigned long long> cls_keys, cop_keys, dd_keys, dd_rank;
+  DBuf<unsigned long long> cc_keys;    // (class, receiver) correction cache
+  DBuf<unsigned char> cc_val;
   DBuf<ClassInfo> cls_info;
   DBuf<ClassCap> cls_cap;
   DBuf<Corrected> corr_list;
@@ -135,12 +137,13 @@ struct Workspace {
   // capacities (grown from occupancy and on overflow)
   unsigned long long cap_nodes = 1 << 20, cap_queue = 1 << 19, cap_surv = 1 << 14;
   unsigned long long cap_corr = 1 << 16, cap_pairs = 1 << 20;
-  uint32_t cap_cls = 1 << 16, cap_cop = 1 << 14, cap_dd = 1 << 14;
+  uint32_t cap_cls = 1 << 16, cap_cop = 1 << 14, cap_dd = 1 << 14, cap_cc = 1 << 14;
   // occupancy seen per executed segment in earlier solves, used to size the
   // tables of the next solve before it runs
   // (first solve: values typical of the urban canyon, so most first solves
   // need no retry)
-  double r_cls = 0.01, r_cop = 0.004, r_corr = 0.01, r_dd = 5e-4, r_surv = 5e-4, r_pairs = 0.1;
+  double r_cls = 0.01, r_cop = 0.004, r_corr = 0.01, r_dd = 5e-4, r_surv = 5e-4, r_pairs = 0.1,
+         r_cc = 0.01;
   ~Workspace() {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
@@ -666,6 +669,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.cap_cls = std::max(W.cap_cls, pow2(2.2 * W.r_cls * nodes, 8 + sizeof(ClassInfo) + sizeof(ClassCap), cap_bytes));
     W.cap_cop = std::max(W.cap_cop, pow2(2.2 * W.r_cop * nodes, 8, cap_bytes));
     W.cap_dd = std::max(W.cap_dd, pow2(2.2 * W.r_dd * nodes, 16, cap_bytes));
+    W.cap_cc = std::max(W.cap_cc, pow2(2.2 * W.r_cc * nodes, 9, cap_bytes));
     W.cap_corr = std::max<unsigned long long>(
         W.cap_corr, (unsigned long long)std::min(1.2 * W.r_corr * nodes, cap_bytes / sizeof(Corrected)));
     W.cap_surv = std::max<unsigned long long>(
@@ -687,6 +691,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.corr_list.ensure(W.cap_corr);
     W.pairs.ensure(W.cap_pairs);
     W.dd_keys.ensure(W.cap_dd);
+    W.cc_keys.ensure(W.cap_cc);
+    W.cc_val.ensure(W.cap_cc);
     W.dd_rank.ensure(W.cap_dd);
     W.surv.ensure(W.cap_surv);
     CK(cudaMemsetAsync(W.ctr.p, 0, sizeof(Counters), st));
@@ -697,6 +703,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ++nl, k_fill_u64<<<grid_for(W.cap_cop, fb), fb, 0, st>>>(W.cop_keys.p, W.cap_cop, kEmptyKey);
     ++nl, k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_keys.p, W.cap_dd, kEmptyKey);
     ++nl, k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_rank.p, W.cap_dd, kEmptyKey);
+    ++nl, k_fill_u64<<<grid_for(W.cap_cc, fb), fb, 0, st>>>(W.cc_keys.p, W.cap_cc, kEmptyKey);
+    CK(cudaMemsetAsync(W.cc_val.p, 0, W.cap_cc, st));
     CK(cudaEventRecord(W.ev[2], st));
     // The direct-path test of every receiver (DirectPathCorrection) needs
     // only the scene and the receivers: it runs on the side stream while the
@@ -782,6 +790,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ca.stage_counts = stage_counts;
     ca.pairs = W.pairs.p;
     ca.pair_cap = W.cap_pairs;
+    ca.corr_cache = HashTable{W.cc_keys.p, W.cap_cc - 1};
+    ca.corr_val = W.cc_val.p;
     ca.work = W.find_work.p;  // the trace is done with it
     CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
     CK(cudaStreamWaitEvent(st, W.join, 0));
@@ -813,6 +823,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     grow(W.cap_cls, c.used_cls);
     grow(W.cap_cop, c.used_cop);
     grow(W.cap_dd, c.used_dd);
+    grow(W.cap_cc, c.used_cc);  // a full cache only costs recomputation
     if (c.overflow) {
       if (c.overflow & kOvNodes) W.cap_nodes = std::max(W.cap_nodes * 2, c.nodes + c.nodes / 8);
       if (c.overflow & kOvQueue) {
@@ -843,6 +854,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       upd(W.r_cls, c.used_cls / n);
       upd(W.r_cop, c.used_cop / n);
       upd(W.r_dd, c.used_dd / n);
+      upd(W.r_cc, c.used_cc / n);
       upd(W.r_corr, c.corrected / n);
       upd(W.r_surv, c.survivors / n);
       upd(W.r_pairs, c.pairs / n);
