@@ -133,9 +133,6 @@ typedef struct sbr_path {
   int reserved;
 } sbr_path;
 
-/* Stage times from CUDA events on the engine's stream.  device_ms spans
- * everything after the receivers are on the device (grid, trace, capture,
- * correction, field) and before results are copied back. */
 /* Error of an FP32-precision field against the FP64 field of the same path
  * set (requests with field_check).  Components compared: those whose FP64
  * magnitude exceeds 1e-6 of the receiver's largest component. */
@@ -147,8 +144,13 @@ typedef struct sbr_field_error {
   double max_rel_vec;        /* max |E - E64| / |E64| */
 } sbr_field_error;
 
+/* Stage times from CUDA events on the engine's stream.  device_ms spans
+ * everything after the receivers are on the device (grid, trace, capture,
+ * correction, field) and before results are copied back; capture_kernel_ms
+ * is the capture kernel alone (inside capture_ms). */
 typedef struct sbr_timing {
   double total_ms, trace_ms, capture_ms, correct_ms, field_ms, h2d_ms, d2h_ms, device_ms;
+  double capture_kernel_ms;
 } sbr_timing;
 
 /* ---- scene ---------------------------------------------------------- */

@@ -104,6 +104,7 @@ struct Workspace {
   cudaStream_t side = nullptr;  // the direct-path test, concurrent with the trace
   cudaEvent_t ev[8] = {};
   cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t cap_ev[2] = {};  // around the capture kernel
   DBuf<TxParams> txp;
   DBuf<double> rx;
   DBuf<int> rx_req;
@@ -148,6 +149,8 @@ struct Workspace {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (fork) cudaEventDestroy(fork);
+    for (auto& e : cap_ev)
+      if (e) cudaEventDestroy(e);
     if (join) cudaEventDestroy(join);
     if (stream) cudaStreamDestroy(stream);
     if (side) cudaStreamDestroy(side);
@@ -530,6 +533,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
   if (!W.ev[0])
     for (auto& e : W.ev) CK(cudaEventCreate(&e));
   if (!W.fork) CK(cudaEventCreateWithFlags(&W.fork, cudaEventDisableTiming));
+  if (!W.cap_ev[0])
+    for (auto& e : W.cap_ev) CK(cudaEventCreate(&e));
   if (!W.join) CK(cudaEventCreateWithFlags(&W.join, cudaEventDisableTiming));
   st = W.stream;
   // ---- request table
@@ -795,10 +800,13 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ca.work = W.find_work.p;  // the trace is done with it
     CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
     CK(cudaStreamWaitEvent(st, W.join, 0));
+    CK(cudaEventRecord(W.cap_ev[0], st));
     if (stage_counts) {
       ++nl, k_capture<true><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
+      CK(cudaEventRecord(W.cap_ev[1], st));
     } else {
       ++nl, k_capture<false><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
+      CK(cudaEventRecord(W.cap_ev[1], st));
       ++nl, k_capture_finish<<<152 * 16, 128, 0, st>>>(ca);
     }
     CK(cudaGetLastError());
@@ -1031,6 +1039,9 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     out.timing.correct_ms = ms[5];
     out.timing.field_ms = ms[6];
     out.timing.d2h_ms = ms[7];
+    float cap_k = 0;
+    CK(cudaEventElapsedTime(&cap_k, W.cap_ev[0], W.cap_ev[1]));
+    out.timing.capture_kernel_ms = cap_k;
     float all = 0, dev = 0;
     CK(cudaEventElapsedTime(&all, W.ev[0], W.ev[7]));
     CK(cudaEventElapsedTime(&dev, W.ev[1], W.ev[6]));
