@@ -112,10 +112,12 @@ __device__ __forceinline__ float sqrt_up(float x) {
 // image source img towards c crosses the class's last triangle T
 // (MultiPathCorrection's first test for a capture at c; RTSolver.cpp:356).
 // Three planes through img and T's edges, n_k . p >= n_k . img, formed once
-// per class (write_class_cap); k_capture loosens each by 2 m_k, m_k =
-// 2^-12 |n_k| (cmax + |img| + |T| + 1) bounding the FP32 error of the test
-// for receivers |p| <= cmax (four times the FP32 filter margin), and uses
-// no cone when a plane is ill-conditioned.  The reference's FP64 test accepts
+// per class in FP64 and rounded to FP32 (k_class_cones); k_capture loosens
+// each by 2 m_k, m_k = 2^-19 |n_k| (cmax + |img| + |T| + 1).  The FP32 test
+// of a point p (|p| <= cmax) or of a cell corner errs by under
+// 10 * 2^-24 |n_k| (cmax + |img| + |T|): the plane's rounding, the rounding
+// of p, and the dot product.  No cone is used when a plane is
+// ill-conditioned (the centroid within 4 m_k of it).  The reference's FP64 test accepts
 // only points inside the exact cone, so receivers outside the loosened one
 // are skipped without changing a result.
 
@@ -312,11 +314,11 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k
           float* fl = s_fl[warp][lane];
           for (int q = 0; q < 3; ++q) fl[q] = c.img[q];
           for (int q = 0; q < 8; ++q) fl[3 + q] = c.F[q];
-          // the cone's planes loosened by 2 m, m = 2^-12 |n| (cmax + |img| + |T| + 1)
+          // the cone's planes loosened by 2 m, m = 2^-19 |n| (cmax + |img| + |T| + 1)
           float* cn = s_cn[warp][lane];
           cone_ok = !kStage;
           for (int k = 0; k < 3; ++k) {
-            const float m = 2.44140625e-04f * (c.nn[k] * cmax + c.w[k]);
+            const float m = 1.9073486328125e-06f * (c.nn[k] * cmax + c.w[k]);
             cone_ok &= (c.gc[k] > 4.0f * m && isfinite(m)) ? 1 : 0;
             cn[4 * k + 0] = c.n[k][0];
             cn[4 * k + 1] = c.n[k][1];

@@ -214,6 +214,7 @@ struct Counters {
   unsigned long long cand;       // receiver candidates tested by the capture stage
   unsigned long long anc;        // ancestor re-tests for suppression
   unsigned long long used_cc;    // (class, receiver) corrections cached
+  unsigned long long cls_listed; // classes listed for their correction cones
   unsigned int overflow;         // bit mask of capacity overflows
   unsigned int pad;
 };

@@ -117,6 +117,7 @@ struct Workspace {
   DBuf<NodeCold> nodes_cold;
   DBuf<unsigned long long> cls_keys, cop_keys, dd_keys, dd_rank;
   DBuf<unsigned long long> cc_keys;    // (class, receiver) correction cache
+  DBuf<uint32_t> cls_list;             // interned classes, for their correction cones
   DBuf<unsigned char> cc_val;
   DBuf<ClassInfo> cls_info;
   DBuf<ClassCap> cls_cap;
@@ -692,6 +693,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.cls_keys.ensure(W.cap_cls);
     W.cls_info.ensure(W.cap_cls);
     W.cls_cap.ensure(W.cap_cls);
+    W.cls_list.ensure(W.cap_cls);
     W.cop_keys.ensure(W.cap_cop);
     W.corr_list.ensure(W.cap_corr);
     W.pairs.ensure(W.cap_pairs);
@@ -734,6 +736,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ta.cop_tab = HashTable{W.cop_keys.p, W.cap_cop - 1};
     ta.cls_info = W.cls_info.p;
     ta.cls_cap = W.cls_cap.p;
+    ta.cls_list = W.cls_list.p;
     ta.tri_cop = S.tri_cop.p;
     ta.ctr = W.ctr.p;
     ta.seg_per_tx = W.seg_tx.p;
@@ -774,6 +777,9 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         ++nl, k_trace<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
       }
     }
+    // correction cones of the classes the trace interned
+    ++nl, k_class_cones<<<grid_for(W.cap_cls / 2, 128), 128, 0, st>>>(
+        W.cls_list.p, W.ctr.p, W.cap_cls, W.cls_info.p, S.dev, W.cls_cap.p);
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[3], st));
     // ---- capture

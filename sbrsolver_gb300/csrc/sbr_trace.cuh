@@ -32,6 +32,7 @@ struct TraceArgs {
   HashTable cls_tab, cop_tab;
   ClassInfo* cls_info;
   ClassCap* cls_cap;
+  uint32_t* cls_list;  // slots of the classes interned, in interning order
   const int* tri_cop;  // coplanar id by rank
   Counters* ctr;
   unsigned long long* seg_per_tx;  // executed segments per request
@@ -66,34 +67,60 @@ __device__ void write_class_cap(const DevScene& sc, const double* img, int tpos,
   cc.F[0] = F.sx; cc.F[1] = F.sy; cc.F[2] = F.sz;
   cc.F[3] = F.qx; cc.F[4] = F.qy; cc.F[5] = F.qz;
   cc.F[6] = F.W; cc.F[7] = F.ns;
-  float v[3][3];
-  for (int a = 0; a < 3; ++a) {
-    v[0][a] = T.v1[a];
-    v[1][a] = T.v1[a] + T.e1[a];
-    v[2][a] = T.v1[a] + T.e2[a];
+}
+
+// Correction cones of the interned classes (one thread per class-table
+// slot, after the trace): three planes through the image source and the
+// last triangle's edges, formed in FP64 and rounded to FP32, so a plane's
+// error is its FP32 rounding alone.
+__global__ void k_class_cones(const uint32_t* list, const Counters* ctr, uint32_t cap,
+                              const ClassInfo* info, DevScene sc, ClassCap* caps) {
+  if (ctr->overflow & kOvTrace) return;  // this solve will be repeated
+  const unsigned long long n = min(ctr->cls_listed, (unsigned long long)cap);
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint32_t s = list[k];
+    const ClassInfo& ci = info[s];
+    const CorrTri& T = sc.corr[sc.rank_to_id[ci.tri]];
+    ClassCap& cc = caps[s];
+    double v[3][3];
+    for (int a = 0; a < 3; ++a) {
+      v[0][a] = T.v1[a];
+      v[1][a] = T.v1[a] + T.e1[a];
+      v[2][a] = T.v1[a] + T.e2[a];
+    }
+    const double* im = ci.img;
+    const double g[3] = {(v[0][0] + v[1][0] + v[2][0]) / 3.0, (v[0][1] + v[1][1] + v[2][1]) / 3.0,
+                         (v[0][2] + v[1][2] + v[2][2]) / 3.0};
+    auto norm3 = [](const double* x) { return sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]); };
+    const float tmag =
+        float((norm3(im) + norm3(T.v1) + norm3(T.e1) + norm3(T.e2)) * (1.0 + 1e-6)) + 1.0f;
+    for (int k = 0; k < 3; ++k) {
+      const double* p = v[k];
+      const double* q = v[k == 2 ? 0 : k + 1];
+      const double a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
+      const double b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
+      const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                           a[0] * b[1] - a[1] * b[0]};
+      const double nn = norm3(n);
+      // orient towards the triangle's centroid, which lies inside the cone
+      const double gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
+      const double sg = gc > 0.0 ? 1.0 : -1.0;
+      for (int c = 0; c < 3; ++c) cc.n[k][c] = float(sg * n[c]);
+      cc.n[k][3] = float(sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]));
+      cc.nn[k] = float(nn * (1.0 + 1e-6));
+      cc.w[k] = cc.nn[k] * tmag;
+      cc.gc[k] = float(fabs(gc));
+      cc.inv_nx[k] = 1.0f / cc.n[k][0];
+    }
   }
-  const float im[3] = {o.x, o.y, o.z};
-  const float g[3] = {(v[0][0] + v[1][0] + v[2][0]) / 3.0f, (v[0][1] + v[1][1] + v[2][1]) / 3.0f,
-                      (v[0][2] + v[1][2] + v[2][2]) / 3.0f};
-  const float tmag = no + T.nv1 + T.ne1 + T.ne2 + 1.0f;
-  for (int k = 0; k < 3; ++k) {
-    const float* p = v[k];
-    const float* q = v[k == 2 ? 0 : k + 1];
-    const float a[3] = {p[0] - im[0], p[1] - im[1], p[2] - im[2]};
-    const float b[3] = {q[0] - im[0], q[1] - im[1], q[2] - im[2]};
-    const float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
-                        a[0] * b[1] - a[1] * b[0]};
-    const float nn = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    // orient towards the triangle's centroid, which lies inside the cone
-    const float gc = n[0] * (g[0] - im[0]) + n[1] * (g[1] - im[1]) + n[2] * (g[2] - im[2]);
-    const float sg = gc > 0.0f ? 1.0f : -1.0f;
-    for (int c = 0; c < 3; ++c) cc.n[k][c] = sg * n[c];
-    cc.n[k][3] = sg * (n[0] * im[0] + n[1] * im[1] + n[2] * im[2]);
-    cc.nn[k] = nn;
-    cc.w[k] = nn * tmag;
-    cc.gc[k] = fabsf(gc);
-    cc.inv_nx[k] = 1.0f / (sg * n[0]);
-  }
+}
+
+// Records an interned class's slot for k_class_cones (the list has the class
+// table's capacity, which bounds the classes).
+__device__ __forceinline__ void list_class(const TraceArgs& A, uint32_t cls) {
+  const unsigned long long k = atomicAdd(&A.ctr->cls_listed, 1ull);
+  if (k <= A.cls_tab.mask) A.cls_list[k] = cls;
 }
 
 // Every thread that interns a class writes the same values (they depend
@@ -421,6 +448,7 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
         if (fresh) {  // only the thread that interned the class writes its records
           write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
           write_class_cap(A.sc, pimg, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
+          list_class(A, c.cls);
         }
         if (slot < A.out_cap) A.out[slot] = c;
         else atomicOr(&A.ctr->overflow, kOvQueue);
@@ -449,6 +477,7 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
           for (int a = 0; a < 3; ++a) img[a] = x64::sub(pimg[a], x64::mul(x64::mul(2.0, dist), M.n[a]));
           write_class(A.cls_info[c.cls], img, r.cls, h.rank, cop_cls, 1, A.depth + 1);
           write_class_cap(A.sc, img, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
+          list_class(A, c.cls);
         }
         if (slot < A.out_cap) A.out[slot] = c;
         else atomicOr(&A.ctr->overflow, kOvQueue);
