@@ -174,7 +174,7 @@ struct FindArgs {
   const TxParams* txp;
   int n_tx;
   const double* const* dirs;
-  const RayRec* in;
+  RayRec* in;  // reflected rays get their direction normalised here
   const Counters* ctr;
   unsigned long long in_cap;
   long long n_root;
@@ -228,10 +228,18 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
             long long li;
             root_ray(A.txp, A.n_tx, A.dirs, A.lo + k, o, d, q, li);
           } else {
-            const RayRec& r = A.in[A.lo + k];
+            RayRec& r = A.in[A.lo + k];
             for (int a = 0; a < 3; ++a) {
               o[a] = r.o[a];
               d[a] = r.d[a];
+            }
+            if (r.heap & 1) {
+              // a reflected ray (heap 2h+1) arrives with Reflect(d, n) not yet
+              // normalised: normalise it here, where a refill runs on at least
+              // half the warp's lanes, and store it for k_trace
+              double v[3] = {d[0], d[1], d[2]};
+              x64::normalize(v, d);
+              for (int a = 0; a < 3; ++a) r.d[a] = d[a];
             }
           }
           o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
@@ -454,11 +462,9 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
         else atomicOr(&A.ctr->overflow, kOvQueue);
         ++slot;
       }
-      if (do_r) {  // reflected: Reflect(d, n).normalized(), heap 2h+1
+      if (do_r) {  // reflected: Reflect(d, n), heap 2h+1; k_find normalises it
         const double dn = x64::dot(T.n, r.d);
-        double v[3];
-        for (int a = 0; a < 3; ++a) v[a] = x64::sub(r.d[a], x64::mul(x64::mul(2.0, T.n[a]), dn));
-        x64::normalize(v, c.d);
+        for (int a = 0; a < 3; ++a) c.d[a] = x64::sub(r.d[a], x64::mul(x64::mul(2.0, T.n[a]), dn));
         c.heap = r.heap * 2 + 1;
         c.rc = r.rc + 1;
         c.tc = r.tc;
