@@ -36,7 +36,7 @@ SEGMENT_BYTES = 84   # algorithmic bytes per executed segment (trace)
 EVENT_BYTES = 16     # per capture event (group-table rank + count update)
 # DRAM bytes (read + write) per segment of the level-9 urban solve, measured
 # with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass, timed solve)
-K_TRACE_SHARE = 16.98 / (16.98 + 5.54)
+K_TRACE_SHARE = 15.17 / (15.17 + 5.81)
 TRAFFIC_PER_SEGMENT = {"k_capture": 2186.0e6 / 29924326, "k_trace": 11016.0e6 / 29924326}
 
 
