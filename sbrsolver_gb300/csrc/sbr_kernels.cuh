@@ -529,21 +529,24 @@ constexpr unsigned char kFindFallback = 0xFF;
 // 1e-15 |P| of its plane; leaving at |cos| >= 1e-2 the reference's t for it
 // is then below 1e-10 for |P| < 1e5, far under the t > FLT_EPSILON it
 // requires (Triangle.cpp:113).
-__device__ __forceinline__ bool origin_rejected(const Tri32& T, const double* o, const double* d) {
-  const float ox = float(o[0]), oy = float(o[1]), oz = float(o[2]);
+// o32, d32: the ray's origin and direction rounded to FP32 (conversions from
+// FP64 occupy the FP64 pipe like an FP64 add, so a ray's are made once).
+__device__ __forceinline__ bool origin_rejected(const Tri32& T, const float3& o32,
+                                                const float3& d32) {
+  const float ox = o32.x, oy = o32.y, oz = o32.z;
   if (!(fabsf(ox) < 1e5f && fabsf(oy) < 1e5f && fabsf(oz) < 1e5f)) return false;
   const float nx = T.e1[1] * T.e2[2] - T.e1[2] * T.e2[1];
   const float ny = T.e1[2] * T.e2[0] - T.e1[0] * T.e2[2];
   const float nz = T.e1[0] * T.e2[1] - T.e1[1] * T.e2[0];
-  const float dx = float(d[0]), dy = float(d[1]), dz = float(d[2]);
+  const float dx = d32.x, dy = d32.y, dz = d32.z;
   const float dn = dx * nx + dy * ny + dz * nz;
   const float nn = sqrtf(nx * nx + ny * ny + nz * nz), dd = sqrtf(dx * dx + dy * dy + dz * dz);
   return fabsf(dn) >= 1e-2f * nn * dd;
 }
 
 __device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d,
-                            const uint2* cand, int nc, Hit& best, TraceStats& st,
-                            unsigned* overflow, int orank = -1) {
+                            const float3& o32, const float3& d32, const uint2* cand, int nc,
+                            Hit& best, TraceStats& st, unsigned* overflow, int orank = -1) {
   if (nc == kFindFallback)  // more contenders than kept, or a deep stack: one-pass search
     return closest_hit(sc, o, d, best, st, overflow);
   int cr[kCand];
@@ -566,7 +569,7 @@ __device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d
   for (int i = 0; i < nc; ++i) {
     if (best.rank != INT_MAX && ct[i] > float(best.t) * (1.0f + kTieSlack) + 1e-30f) break;
     const int r = cr[i];
-    if (r == orank && origin_rejected(sc.tri32[r], o, d)) continue;
+    if (r == orank && origin_rejected(sc.tri32[r], o32, d32)) continue;
     ++st.fp64_tri;
     double t, P[3], dist;
     if (mt64(sc.tri64[r], o, d, t, P, dist) &&
@@ -582,8 +585,6 @@ __device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d
   if (best.rank == INT_MAX) return false;
   best.leaf = sc.tri64[best.rank].node;
   // every ancestor of the winner's leaf must pass the reference's slab test
-  const float3 o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
-  const float3 d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
   const float3 i32 = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
   for (const AncBox* a = sc.anc + sc.anc_off[best.leaf];; ++a) {
     const AncBox b = *a;

@@ -377,8 +377,11 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
     const TxParams& P = A.txp[r.tx];
     Hit h;
     const long long c = i - A.lo;
-    const bool hit = resolve_hit(A.sc, r.o, r.d, A.cand + size_t(c) * kCand, A.ncand[c], h, st,
-                                 &A.ctr->overflow, r.orank);
+    // the ray in FP32, converted once (each conversion costs an FP64 pipe slot)
+    const float3 o32 = make_float3(float(r.o[0]), float(r.o[1]), float(r.o[2]));
+    const float3 d32 = make_float3(float(r.d[0]), float(r.d[1]), float(r.d[2]));
+    const bool hit = resolve_hit(A.sc, r.o, r.d, o32, d32, A.cand + size_t(c) * kCand,
+                                 A.ncand[c], h, st, &A.ctr->overflow, r.orank);
     const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
     {  // per-request segment count, one atomic per request present in the warp
       const unsigned peers = __match_any_sync(__activemask(), r.tx);
@@ -402,9 +405,9 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
       }
       n.S = r.S;
       n.pad = 0.0;
-      m.s[0] = float(r.o[0]); m.s[1] = float(r.o[1]); m.s[2] = float(r.o[2]);
+      m.s[0] = o32.x; m.s[1] = o32.y; m.s[2] = o32.z;
       m.S = float(r.S);
-      m.u[0] = float(r.d[0]); m.u[1] = float(r.d[1]); m.u[2] = float(r.d[2]);
+      m.u[0] = d32.x; m.u[1] = d32.y; m.u[2] = d32.z;
       m.parent = r.parent;
       m.cls = r.cls;
       m.launch = r.launch;
