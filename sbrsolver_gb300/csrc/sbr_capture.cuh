@@ -180,7 +180,7 @@ __device__ __forceinline__ NodeSpan node_span(const NodeHot& nd, const TxParams&
   const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
   const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
   const float len = nd.len, S = nd.S;
-  const float tanb = float(P.tan_beta);
+  const float tanb = P.tan_beta32;
   const float pmax = __fdividef(cmax + S * tanb, fmaxf(1e-6f, 1.0f - tanb)) * 1.0001f + 1.0f;
   const float su = s.x * u.x + s.y * u.y + s.z * u.z;
   const float ss = s.x * s.x + s.y * s.y + s.z * s.z;
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k
         const NodeSpan sp = node_span(h, A.txp[h.tx], A.grids[h.tx], cmax, cone_ok);
         s_sp[warp][lane] = sp;
         if (sp.nchunk > 0)
-          s_ck[warp][lane] = chunk_box(h, A.grids[h.tx], sp, 0, cmax, float(A.txp[h.tx].tan_beta),
+          s_ck[warp][lane] = chunk_box(h, A.grids[h.tx], sp, 0, cmax, A.txp[h.tx].tan_beta32,
                                        cone_ok != 0, s_cn[warp][lane]);
       }
       __syncwarp();
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k
         Fl = TriFrom{fl[3], fl[4], fl[5], fl[6], fl[7], fl[8], fl[9], fl[10]};
       }
       if (sp.nchunk > 0) {
-        const float tanb = float(P.tan_beta);
+        const float tanb = P.tan_beta32;
         const float cmax = A.gb[nd.tx].cmax;
         const float lo = sp.lo, hi = sp.hi, ns = sp.ns;
         const int nchunk = sp.nchunk;
@@ -631,7 +631,7 @@ __global__ void __launch_bounds__(128) k_capture_finish(CaptureArgs A) {
       }
     }
     if (!ok) continue;
-    const float tanb = float(P.tan_beta);
+    const float tanb = P.tan_beta32;
     bool sup = false;
     for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
       const NodeHot a = A.nodes[p];

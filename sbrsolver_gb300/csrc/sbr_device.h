@@ -140,6 +140,8 @@ struct TxParams {
   long long launch_first;      // first global launch index
   int grid;                    // receiver grid index
   int precision;               // field precision: 0 FP64, 1 FP32, 2 FP32 with FP32 phase
+  float tan_beta32;            // tan_beta rounded to FP32 on the host (a device
+                               // conversion would take an FP64 pipe slot per use)
   // tabulated pattern (antenna 3): per (theta, phi) grid point the complex
   // relative amplitudes of E_theta and E_phi (re, im, re, im)
   const float4* pat;

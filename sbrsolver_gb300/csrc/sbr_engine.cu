@@ -563,6 +563,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     const int tess = q.tessellation + 1;  // RTSolver.cpp:70
     const double beta = 1.0 / (3.0 * tess) * std::acos(-1.0 / std::sqrt(5.0));  // RTSolver.cpp:839
     P.tan_beta = std::tan(beta);
+    P.tan_beta32 = float(P.tan_beta);
     P.R = q.max_reflection;
     P.T = q.max_transmission;
     P.antenna = q.antenna;
