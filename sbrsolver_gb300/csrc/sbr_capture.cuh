@@ -386,9 +386,8 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k
       if (sp.nchunk > 0) {
         const float tanb = P.tan_beta32;
         const float cmax = A.gb[nd.tx].cmax;
-        const float lo = sp.lo, hi = sp.hi, ns = sp.ns;
+        const float ns = sp.ns;
         const int nchunk = sp.nchunk;
-        const float step = sp.step;
         // error margins of the FP32 reception test, from per-node bounds
         const float ml = kRecK * (ns + cmax + 1.0f);
         {
@@ -517,7 +516,7 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k
                 // RayCapture deletes a captured node's subtree, so an ancestor
                 // capturing the same receiver suppresses this one.
                 auto suppressed = [&]() {
-                  if (kStage) {
+                  if constexpr (kStage) {
                     for (int q = 0; q < na; ++q) {
                       const AncRec& r = anc[warp][q];
                       ++anc_tests;
@@ -530,20 +529,21 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k
                       if (w) return true;
                     }
                     return false;
-                  }
-                  for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
-                    const NodeHot a = A.nodes[p];
-                    ++anc_tests;
-                    int w = reception32(make_float3(a.s[0], a.s[1], a.s[2]),
-                                        make_float3(a.u[0], a.u[1], a.u[2]), a.len, a.S, c, tanb);
-                    if (w < 0) {
-                      ++n64;
-                      w = capture_exact(A.nodes_cold, p, c64, P.tan_beta);
+                  } else {
+                    for (uint32_t p = nd.parent; p != 0xFFFFFFFFu && p < A.node_cap;) {
+                      const NodeHot a = A.nodes[p];
+                      ++anc_tests;
+                      int w = reception32(make_float3(a.s[0], a.s[1], a.s[2]),
+                                          make_float3(a.u[0], a.u[1], a.u[2]), a.len, a.S, c, tanb);
+                      if (w < 0) {
+                        ++n64;
+                        w = capture_exact(A.nodes_cold, p, c64, P.tan_beta);
+                      }
+                      if (w) return true;
+                      p = a.parent;
                     }
-                    if (w) return true;
-                    p = a.parent;
+                    return false;
                   }
-                  return false;
                 };
                 if (kStage) {
                   if (suppressed()) continue;

@@ -178,11 +178,11 @@ struct __align__(16) ClassInfo {
   uint32_t pad2;
 };
 
-// What the capture stage needs of a class, formed once when the class is
-// interned: the FP32 image source, the FP32 image-correction filter terms
-// from it to the class's last triangle (mesh position tpos), and that
-// triangle's correction cone without the request-dependent margin (see
-// k_capture).
+// What the capture stage needs of a class: the FP32 image source and the
+// FP32 image-correction filter terms from it to the class's last triangle
+// (mesh position tpos), written when the class is interned, and that
+// triangle's correction cone without the request-dependent margin, formed in
+// FP64 after the trace (k_class_cones).
 struct __align__(16) ClassCap {
   float img[3];
   int tpos;        // corr32 index of the last triangle

@@ -370,7 +370,6 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
   int cand_r[kCand], cand_leaf[kCand];
   float cand_t[kCand];
   int ncand = 0;
-  bool overflowed = false;
   if (sc.root_leaf) pending_leaf = 0;
   else stack[sp++] = 0;
   bool stack_overflow = false;
@@ -389,7 +388,7 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
           ++ncand;
           if (k == 2) tcut = fminf(tcut, thi * (1.0f + kTieSlack) + 1e-30f);
         } else {
-          overflowed = true;  // too many contenders: resolve this one now
+          // too many contenders: resolve this one now
           ++st.fp64_tri;
           double t, P[3], dist;
           if (mt64(sc.tri64[r], o, d, t, P, dist) &&
@@ -491,7 +490,6 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
       best.leaf = cand_leaf[i];
     }
   }
-  (void)overflowed;
   bool ok = !stack_overflow;
   if (ok && best.rank != INT_MAX) {
     // every ancestor of the winner's leaf must pass the FP64 slab test

@@ -54,7 +54,8 @@ __device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long 
 }
 
 // The capture-stage record of a class with image source img (FP64) whose
-// last ray starts on the triangle at mesh position tpos.
+// last ray starts on the triangle at mesh position tpos: the FP32 image source
+// and correction-filter terms (the cone follows in k_class_cones).
 __device__ void write_class_cap(const DevScene& sc, const double* img, int tpos, ClassCap& cc) {
   const Tri32 T = sc.corr32[tpos];
   const float3 o = make_float3(float(img[0]), float(img[1]), float(img[2]));
