@@ -36,7 +36,6 @@ SEGMENT_BYTES = 84   # algorithmic bytes per executed segment (trace)
 EVENT_BYTES = 16     # per capture event (group-table rank + count update)
 # DRAM bytes (read + write) per segment of the level-9 urban solve, measured
 # with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass, timed solve)
-K_TRACE_SHARE = 15.17 / (15.17 + 5.81)
 TRAFFIC_PER_SEGMENT = {"k_capture": 2186.0e6 / 29924326, "k_trace": 11016.0e6 / 29924326}
 
 
@@ -443,7 +442,8 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     dev_ms, seg, stage = [], [], {"trace_ms": 0.0, "capture_ms": 0.0, "correct_ms": 0.0,
-                                 "field_ms": 0.0, "capture_kernel_ms": 0.0}
+                                 "field_ms": 0.0, "capture_kernel_ms": 0.0,
+                                 "trace_kernel_ms": 0.0, "trace_kernel_launches": 0.0}
     counts = None
     with Clocks(local) as ck:
         # NVTX range "timed": lets a profiler select exactly these solves
@@ -478,19 +478,17 @@ def main():
         peak, peak_kind = peaks()
         steps = args.steps
         n_nodes = counts["segments"]
-        depth = wl.request.max_reflection + wl.request.max_transmission
         cap_ms = stage["capture_kernel_ms"] / steps  # the capture kernel alone
-        tr_ms = stage["trace_ms"] / steps
-        # The trace stage is k_find + k_trace per depth; k_trace's share of it
-        # is K_TRACE_SHARE (ncu launch list of this workload).
-        if cap_ms >= K_TRACE_SHARE * tr_ms:
+        tr_ms = stage["trace_kernel_ms"] / steps      # k_trace alone, all its launches
+        tr_launches = max(1.0, stage["trace_kernel_launches"] / steps)
+        if cap_ms >= tr_ms:  # the kernel with the larger total time
             kern, ms = "k_capture", cap_ms
             alg = n_nodes * NODE_BYTES + captured * EVENT_BYTES
             traffic = TRAFFIC_PER_SEGMENT["k_capture"] * n_nodes
         else:
-            kern, ms = "k_trace", tr_ms / (depth + 1)
-            alg = n_nodes * SEGMENT_BYTES / (depth + 1)
-            traffic = TRAFFIC_PER_SEGMENT["k_trace"] * n_nodes / (depth + 1)
+            kern, ms = "k_trace", tr_ms / tr_launches
+            alg = n_nodes * SEGMENT_BYTES / tr_launches
+            traffic = TRAFFIC_PER_SEGMENT["k_trace"] * n_nodes / tr_launches
         if wl.name != "urban_L9_R6T1":
             traffic = None  # measured for the level-9 workload only
         achieved = alg / (ms / 1e3) / 1e9

@@ -147,10 +147,12 @@ typedef struct sbr_field_error {
 /* Stage times from CUDA events on the engine's stream.  device_ms spans
  * everything after the receivers are on the device (grid, trace, capture,
  * correction, field) and before results are copied back; capture_kernel_ms
- * is the capture kernel alone (inside capture_ms). */
+ * is the capture kernel alone (inside capture_ms), trace_kernel_ms the
+ * FP64 resolution-and-spawn kernel alone over its trace_kernel_launches
+ * launches (inside trace_ms, which also holds the FP32 candidate search). */
 typedef struct sbr_timing {
   double total_ms, trace_ms, capture_ms, correct_ms, field_ms, h2d_ms, d2h_ms, device_ms;
-  double capture_kernel_ms;
+  double capture_kernel_ms, trace_kernel_ms, trace_kernel_launches;
 } sbr_timing;
 
 /* ---- scene ---------------------------------------------------------- */

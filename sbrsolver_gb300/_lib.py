@@ -85,7 +85,8 @@ class Completion(C.Structure):
 class Timing(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("total_ms", "trace_ms", "capture_ms", "correct_ms",
                                            "field_ms", "h2d_ms", "d2h_ms", "device_ms",
-                                           "capture_kernel_ms")]
+                                           "capture_kernel_ms", "trace_kernel_ms",
+                                           "trace_kernel_launches")]
 
 
 _lib = None

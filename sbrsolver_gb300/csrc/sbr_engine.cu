@@ -105,6 +105,7 @@ struct Workspace {
   cudaEvent_t ev[8] = {};
   cudaEvent_t fork = nullptr, join = nullptr;
   cudaEvent_t cap_ev[2] = {};  // around the capture kernel
+  std::vector<cudaEvent_t> tr_ev;  // before and after each k_trace launch
   DBuf<TxParams> txp;
   DBuf<double> rx;
   DBuf<int> rx_req;
@@ -152,6 +153,7 @@ struct Workspace {
     if (fork) cudaEventDestroy(fork);
     for (auto& e : cap_ev)
       if (e) cudaEventDestroy(e);
+    for (auto& e : tr_ev) cudaEventDestroy(e);
     if (join) cudaEventDestroy(join);
     if (stream) cudaStreamDestroy(stream);
     if (side) cudaStreamDestroy(side);
@@ -765,6 +767,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fnd.ncand = W.ncand.p;
     ta.cand = W.cand.p;
     ta.ncand = W.ncand.p;
+    size_t n_tr = 0;  // k_trace launches (timed one by one)
     for (int d = 0; d <= max_depth; ++d) {
       ta.depth = fnd.depth = d;
       ta.in = fnd.in = (d % 2 == 0) ? W.q1.p : W.q0.p;
@@ -775,7 +778,15 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         ta.hi = fnd.hi = std::min(bound, lo + chunk);
         CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
         ++nl, k_find<<<find_grid(), 128, 0, st>>>(fnd);
+        if (2 * n_tr + 2 > W.tr_ev.size()) {
+          W.tr_ev.resize(2 * n_tr + 2, nullptr);
+          for (auto& e : W.tr_ev)
+            if (!e) CK(cudaEventCreate(&e));
+        }
+        CK(cudaEventRecord(W.tr_ev[2 * n_tr], st));
         ++nl, k_trace<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
+        CK(cudaEventRecord(W.tr_ev[2 * n_tr + 1], st));
+        ++n_tr;
       }
     }
     // correction cones of the classes the trace interned
@@ -1049,6 +1060,14 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     float cap_k = 0;
     CK(cudaEventElapsedTime(&cap_k, W.cap_ev[0], W.cap_ev[1]));
     out.timing.capture_kernel_ms = cap_k;
+    double tr_k = 0;
+    for (size_t i = 0; i < n_tr; ++i) {
+      float x = 0;
+      CK(cudaEventElapsedTime(&x, W.tr_ev[2 * i], W.tr_ev[2 * i + 1]));
+      tr_k += x;
+    }
+    out.timing.trace_kernel_ms = tr_k;
+    out.timing.trace_kernel_launches = double(n_tr);
     float all = 0, dev = 0;
     CK(cudaEventElapsedTime(&all, W.ev[0], W.ev[7]));
     CK(cudaEventElapsedTime(&dev, W.ev[1], W.ev[6]));

@@ -36,7 +36,7 @@ def test_struct_layouts_match_header(tmp_path):
     checks = {"sbr_request": (_lib.Request, ["n_rx", "rx", "stage_counts", "field_check", "pattern"]),
               "sbr_counts": (_lib.Counts, ["keys", "near_edge_paths", "gpu_kernels"]),
               "sbr_path": (_lib.Path, ["launch", "field", "near_edge"]),
-              "sbr_timing": (_lib.Timing, ["device_ms", "capture_kernel_ms"]),
+              "sbr_timing": (_lib.Timing, ["device_ms", "capture_kernel_ms", "trace_kernel_launches"]),
               "sbr_field_error": (_lib.FieldError, ["max_rel_vec"]),
               "sbr_completion": (_lib.Completion, ["counts", "result"]),
               "sbr_material": (_lib.Material, ["rel_conductivity", "width"]),
