@@ -3,19 +3,23 @@
 //   sbr_grid.cuh     receivers -> uniform grid (bbox, count, scan, scatter)
 //   sbr_trace.cuh    RayLaunch (RTSolver.cpp:128-257) as a wavefront: per bounce
 //                    depth an FP32 candidate search (k_find) and the FP64
-//                    closest hit, tree node and children (k_trace)
+//                    closest hit, tree node and children (k_trace); then each
+//                    path class's correction cone in FP64 (k_class_cones)
 //   sbr_capture.cuh  RayCapture (RTSolver.cpp:259-297, 805-863) with image
 //                    correction's first step as a prefilter (k_capture), FP64
-//                    decisions, MultiPathCorrection and ancestor suppression
+//                    decisions, MultiPathCorrection (its outcome kept per
+//                    (class, receiver)) and ancestor suppression
 //                    (k_capture_finish)
-//   sbr_paths.cuh    DirectPathCorrection per receiver (k_direct), duplicate
-//                    removal (RTSolver.cpp:435-459), the survivors'
-//                    geometry and field (FieldCompute.cpp:71-151) and the
+//   sbr_paths.cuh    DirectPathCorrection per receiver (k_direct, on a side
+//                    stream during the trace), duplicate removal
+//                    (RTSolver.cpp:435-459), the survivors' corrected
+//                    geometry (k_path), field terms per segment (k_seg) and
+//                    field (k_combine) (FieldCompute.cpp:71-151), and the
 //                    per-receiver sum in (launch, BFS) order
 //                    (FieldCompute.cpp:11-25)
-// One CUDA stream per workspace; the host synchronises once per solve, after
-// the capacity counters (a solve whose tables overflowed is repeated with
-// larger ones).
+// Each workspace has a stream and a side stream; the host synchronises once
+// per solve, after the capacity counters (a solve whose tables overflowed is
+// repeated with larger ones).
 #include <cuda_runtime.h>
 
 #include <algorithm>
