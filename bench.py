@@ -132,24 +132,9 @@ def cpu_baseline(wl, level: int = 5, threads: int = 0):
 
 
 def batched_workload(seed: int = 0x5B5 + 2, n_tx: int = 256):
-    """256 transmitters on the urban scene: seeded street-level positions,
-    levels U{6..9}, patterns U{Hertzian, half-wave, isotropic}, 5 reflections,
-    4,096 shared receivers on a 64 x 64 grid at 1.5 m."""
-    import numpy as np
+    """256 transmitters on the urban scene (sbrsolver_gb300.scenes.batched_workload)."""
     from sbrsolver_gb300 import scenes
-    wl = scenes.urban_scene()
-    rng = np.random.default_rng(seed)
-    g = -500.0 + (1000.0 / 64) * (np.arange(64) + 0.5)
-    rx = np.array([(x, y, 1.5) for x in g for y in g], np.float64)
-    reqs = []
-    for _ in range(n_tx):
-        # street crossings of the 50 m lattice, 10-40 m high
-        tx = (float(rng.integers(-10, 10) * 50.0), float(rng.integers(-10, 10) * 50.0),
-              float(rng.uniform(10, 40)))
-        reqs.append(scenes.Request(tx=tx, rx=rx, max_reflection=5, max_transmission=0,
-                                   frequency=28e9, tessellation=int(rng.integers(6, 10)),
-                                   antenna=int(rng.integers(0, 3))))
-    return wl, reqs
+    return scenes.batched_workload(seed, n_tx)
 
 
 def serving_stream(scene_wls, n: int, seed: int = 0x5B5 + 4):

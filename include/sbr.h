@@ -301,20 +301,26 @@ sbr_status sbr_write_launch_rays_vtk(const char* path, const double* origin, int
 
 /* ---- allocation-free field sum -------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
- * memory (code inside CUDA graph capture, processes whose device memory
- * belongs to another framework's pool, services that must not grow after
- * start-up): sums per-path fields into per-receiver fields in each
- * receiver's (launch, BFS) rank order, exactly as sbr_solve does, using only
- * a fixed 4 MiB array compiled into the library (held on every GPU that
- * loads it until exit).  All pointers are device pointers owned by the
- * caller: path_receiver[n_paths] (0-based), path_rank[n_paths]
+ * memory: processes whose device memory is held by another framework's
+ * caching allocator, services that must keep a fixed device footprint after
+ * start-up, and latency-bound loops that cannot afford cudaMalloc/cudaFree
+ * (which may synchronise the device).  Sums per-path fields into
+ * per-receiver fields in each receiver's (launch, BFS) rank order, with the
+ * arithmetic sbr_solve's own sum uses (FP64 for SBR_FIELD_FP64, compensated
+ * FP32 for both FP32 precisions; paths of equal rank are added in path-index
+ * order), using only a fixed 4 MiB array compiled into the library (held on
+ * every GPU that loads it until exit).  All pointers are device pointers
+ * owned by the caller: path_receiver[n_paths] (0-based), path_rank[n_paths]
  * (launch << 17 | heap, see sbr_path), path_field[6 * n_paths],
- * field_out[6 * n_rx].  Limits: 1 <= n_rx <= 262144, 0 <= n_paths <= 262144;
- * larger sizes are rejected with SBR_ERR_INVALID_ARG.  Runs on `stream`
- * (a cudaStream_t, NULL = default stream) and returns after it completes.
- * The first call on a device looks up the array's device address and should
- * come before any stream capture.  Calls share the array: calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * field_out[6 * n_rx].  Limits: 1 <= n_rx <= 262144, 0 <= n_paths <= 262144,
+ * at most 2048 paths on one receiver; larger sizes, receiver indices outside
+ * [0, n_rx) and precisions other than SBR_FIELD_FP64 / SBR_FIELD_FP32 /
+ * SBR_FIELD_FP32_PHASE are rejected with SBR_ERR_INVALID_ARG.  Runs on
+ * `stream` (a cudaStream_t of the current device, NULL = default stream) and
+ * returns after it completes.  The first call on a device looks up the
+ * array's device address and should come before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller. */
 sbr_status sbr_receiver_field_sum_noalloc(const int* path_receiver, const long long* path_rank,
                                           const double* path_field, int n_paths, int n_rx,
                                           int field_precision, double* field_out,

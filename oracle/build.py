@@ -49,13 +49,17 @@ def build_oracle(force: bool = False) -> str:
     return LIB
 
 
-def build_reference() -> str | None:
-    ref = os.environ.get("SBR_REFERENCE_DIR", "/root/reference")
-    if not os.path.exists(os.path.join(ref, "SBRSolver_rev2", "RTSolver.cpp")):
+def build_reference(ref: str | None = None) -> str | None:
+    """Compiles the reference's own sources from the checkout `ref` (or
+    $SBR_REFERENCE_DIR) into oracle/_ref/ref_harness; None when no checkout
+    is given or it holds no sources (as on a machine without the reference)."""
+    ref = ref or os.environ.get("SBR_REFERENCE_DIR")
+    if not ref or not os.path.exists(os.path.join(ref, "SBRSolver_rev2", "RTSolver.cpp")):
         return None
-    _run(["bash", os.path.join(HERE, "build_ref.sh")])
+    _run(["bash", os.path.join(HERE, "build_ref.sh"), ref])
     return REF_HARNESS
 
 
 if __name__ == "__main__":
-    print(build_oracle(force="-f" in sys.argv), build_reference())
+    args = [a for a in sys.argv[1:] if a != "-f"]
+    print(build_oracle(force="-f" in sys.argv), build_reference(args[0] if args else None))

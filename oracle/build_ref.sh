@@ -4,13 +4,18 @@
 # reference checkout; only the Eigen-subset header (oracle/compat) and the
 # harness (oracle/ref_harness.cpp) come from this repository.  Outputs go to
 # oracle/_ref/ only (git-ignored).
-#   SBR_REFERENCE_DIR   reference checkout (default /root/reference)
+# Usage: build_ref.sh <reference checkout>  (or SBR_REFERENCE_DIR=<checkout>)
 # -ffp-contract=off keeps a*b+c as two rounded operations on every host
 # (aarch64 g++ would otherwise fuse them), matching the GPU's __dmul_rn /
 # __dadd_rn arithmetic.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${SBR_REFERENCE_DIR:-/root/reference}/SBRSolver_rev2"
+root="${1:-${SBR_REFERENCE_DIR:-}}"
+if [ -z "$root" ]; then
+  echo "usage: $0 <reference checkout> (or set SBR_REFERENCE_DIR)" >&2
+  exit 2
+fi
+ref="$root/SBRSolver_rev2"
 out="$here/_ref"
 if [ ! -f "$ref/RTSolver.cpp" ]; then
   echo "reference sources not found at $ref" >&2

@@ -483,34 +483,44 @@ double request_bytes(const sbr_request& q) {
          L * tree_width(R, T) * 2 * sizeof(RayRec) + double(q.n_rx) * 256.0;
 }
 
+// SM count of the current device, queried once per device.
+static int device_sms() {
+  static std::atomic<int> cache[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int>& c = cache[dev & 63];
+  int n = c.load(std::memory_order_relaxed);
+  if (!n) {
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    n = std::max(1, n);
+    c.store(n, std::memory_order_relaxed);
+  }
+  return n;
+}
+
+// Resident blocks per SM of a kernel at a block size, queried once per kernel.
+template <class K>
+static int blocks_per_sm(K kernel, int block) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+  return std::max(1, per_sm);
+}
+
 // Persistent grid of the FP32 search: as many blocks as fit on the device.
 static int find_grid() {
-  static int g = [] {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find, 128, 0);
-    return std::max(1, sms) * std::max(1, per_sm);
-  }();
-  return g;
+  static const int per_sm = blocks_per_sm(k_find, 128);
+  return device_sms() * per_sm;
 }
 
 // Capture grid: every block resident at once (the work counter balances).
 static int capture_grid() {
-  static int g = [] {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_capture<false>, 32 * kCapWarps, 0);
-    return std::max(1, sms) * std::max(1, per_sm);
-  }();
-  return g;
+  static const int per_sm = blocks_per_sm(k_capture<false>, 32 * kCapWarps);
+  return device_sms() * per_sm;
 }
 
 static int grid_for(long long n, int block) {
-  int dev_sms = 152;
-  long long g = (n + block - 1) / block;
-  return int(std::max<long long>(1, std::min<long long>(g, (long long)dev_sms * 32)));
+  const long long g = (n + block - 1) / block;
+  return int(std::max<long long>(1, std::min<long long>(g, (long long)device_sms() * 32)));
 }
 
 static FieldConsts field_consts() {
@@ -829,7 +839,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     } else {
       ++nl, k_capture<false><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
       CK(cudaEventRecord(W.cap_ev[1], st));
-      ++nl, k_capture_finish<<<152 * 16, 128, 0, st>>>(ca);
+      ++nl, k_capture_finish<<<device_sms() * 16, 128, 0, st>>>(ca);
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[4], st));

@@ -445,3 +445,23 @@ def large_scene(seed: int = 0x5B5 + 3, level: int = 10, n_rx: int = 50000,
     req = Request(tx=tx, rx=rx, max_reflection=max_reflection, max_transmission=0,
                   frequency=f, tessellation=level, antenna=2)
     return Workload(f"large_L{level}_R{max_reflection}", scene, req, {"seed": seed})
+
+
+def batched_workload(seed: int = 0x5B5 + 2, n_tx: int = 256):
+    """Many transmitters on the urban canyon: n_tx seeded street-crossing
+    positions 10-40 m high, icosahedron levels U{6..9}, patterns U{isotropic,
+    Hertzian, half-wave}, 5 reflections, no transmission, 28 GHz, and 4,096
+    receivers shared by every request on a 64 x 64 grid at 1.5 m.  Returns
+    the workload (its request is the urban canyon's own) and the requests."""
+    wl = urban_scene()
+    rng = np.random.default_rng(seed)
+    g = -500.0 + (1000.0 / 64) * (np.arange(64) + 0.5)
+    rx = np.array([(x, y, 1.5) for x in g for y in g], np.float64)
+    reqs = []
+    for _ in range(n_tx):
+        tx = (float(rng.integers(-10, 10) * 50.0), float(rng.integers(-10, 10) * 50.0),
+              float(rng.uniform(10, 40)))
+        reqs.append(Request(tx=tx, rx=rx, max_reflection=5, max_transmission=0,
+                            frequency=28e9, tessellation=int(rng.integers(6, 10)),
+                            antenna=int(rng.integers(0, 3))))
+    return wl, reqs

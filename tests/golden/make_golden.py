@@ -29,7 +29,7 @@ from sbrsolver_gb300 import scenes  # noqa: E402
 import build as oracle_build  # noqa: E402  (oracle/build.py)
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("SBR_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("SBR_REFERENCE_DIR", "")  # the reference checkout (required)
 
 
 def parse_report(path: str) -> dict:
@@ -77,8 +77,7 @@ def to_npz(rep: dict, stages: dict, inputs_sha: str, extra: dict, path: str) -> 
 
 
 def run_case(wl, name: str, extra: dict | None = None) -> dict:
-    with tempfile.TemporaryDirectory(dir=os.path.join(ROOT, "_work") if os.path.isdir(
-            os.path.join(ROOT, "_work")) else None) as d:
+    with tempfile.TemporaryDirectory() as d:
         case = scenes.write_oracle_case(wl, d)
         subprocess.run([oracle_build.REF_HARNESS, "case", case], check=True)
         rep = parse_report(os.path.join(d, "out.txt"))
@@ -144,7 +143,7 @@ def coefficient_sweep() -> None:
     magnitudes are compared exactly at printed precision; the shipped phases
     sit exactly pi away from the current sign convention (FieldCompute.cpp:249,
     277), so only phase modulo pi is pinned."""
-    with tempfile.TemporaryDirectory(dir=os.path.join(ROOT, "_work")) as d:
+    with tempfile.TemporaryDirectory() as d:
         out = os.path.join(d, "coeff.csv")
         subprocess.run([oracle_build.REF_HARNESS, "coeff", "1000", "1.8e9", "1", "0", "1", "-10",
                         out], check=True)
@@ -159,9 +158,8 @@ def coefficient_sweep() -> None:
 
 
 def main() -> None:
-    os.makedirs(os.path.join(ROOT, "_work"), exist_ok=True)
-    if oracle_build.build_reference() is None:
-        raise SystemExit("reference checkout not found")
+    if oracle_build.build_reference(REF) is None:
+        raise SystemExit("reference checkout not found: set SBR_REFERENCE_DIR to it")
     main_wl = scenes.reference_main_scene()
     rep = run_case(main_wl, "reference_main")
     pins = pin_reference_main(rep)
@@ -186,7 +184,7 @@ def main() -> None:
              "urban_L5_R3T2_rx1600_slab")
     # icosahedron launch directions, bit-exact
     for lvl in (0, 1, 2, 5):
-        with tempfile.TemporaryDirectory(dir=os.path.join(ROOT, "_work")) as d:
+        with tempfile.TemporaryDirectory() as d:
             f = os.path.join(d, "ico.bin")
             subprocess.run([oracle_build.REF_HARNESS, "ico", str(lvl), f], check=True)
             v = np.fromfile(f, np.float64).reshape(-1, 3)

@@ -2,6 +2,7 @@
 facet ids, coplanar ids, interaction kinds, ray counts) and received fields
 within 1e-4 relative magnitude / 1e-3 rad phase, through the C ABI."""
 import os
+import warnings
 
 import numpy as np
 import pytest
@@ -134,7 +135,12 @@ def test_edge_cases(built):
     ref = _oracle(wl1)
     res = api.solve(sc, api.request_from_workload(wl1.request))
     assert path_keys(res.paths) == path_keys(ref["paths"])
-    assert not field_close(res.field, ref["field"])
+    # the receiver at the transmitter has a zero-length direct path: its field
+    # is not finite on either side, and must be non-finite in the same places
+    assert not np.all(np.isfinite(ref["field"][0]))
+    with warnings.catch_warnings():
+        warnings.simplefilter("error", RuntimeWarning)
+        assert not field_close(res.field, ref["field"])
     # bad requests
     bad = scenes.small_scene()
     bad.request.tessellation = 13
