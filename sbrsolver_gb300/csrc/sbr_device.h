@@ -114,6 +114,15 @@ struct __align__(16) RayRec {
   int orank;       // depth-first rank of the triangle the ray starts on, -1 for a launch
 };
 
+// FP32 copy of a ray, made by the candidate search when it loads the ray
+// (it converts the FP64 origin and direction anyway), for the FP32 checks and
+// the node record of the ray's resolution, which then convert nothing (an
+// FP64 -> FP32 conversion costs an FP64 pipe slot): origin (o.w unused) and
+// unit direction (d.w unused).
+struct __align__(16) RayF32 {
+  float4 o, d;
+};
+
 // One executed segment (tree node), split in two arrays: the FP32 part the
 // capture stage reads for every node and ancestor, and the FP64 part it
 // reads only for the rare tests inside the FP32 error margin.

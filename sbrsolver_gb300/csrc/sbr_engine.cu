@@ -118,6 +118,7 @@ struct Workspace {
   DBuf<int> cell_base, cell_counts, cell_starts, cell_cursor;
   DBuf<float4> rx32;
   DBuf<RayRec> q0, q1;
+  DBuf<RayF32> ray32;                  // FP32 copies of a chunk's rays (k_find -> k_trace)
   DBuf<NodeHot> nodes;
   DBuf<NodeCold> nodes_cold;
   DBuf<unsigned long long> cls_keys, cop_keys, dd_keys, dd_rank;
@@ -512,6 +513,12 @@ static int find_grid() {
   return device_sms() * per_sm;
 }
 
+// Persistent grid of the FP64 resolution: as many blocks as fit on the device.
+static int trace_grid() {
+  static const int per_sm = blocks_per_sm(k_trace, 128);
+  return device_sms() * per_sm;
+}
+
 // Capture grid: every block resident at once (the work counter balances).
 static int capture_grid() {
   static const int per_sm = blocks_per_sm(k_capture<false>, 32 * kCapWarps);
@@ -767,7 +774,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     const long long chunk = std::max<long long>(1, std::min(kTraceChunk, max_width));
     W.cand.ensure(size_t(chunk) * kCand);
     W.ncand.ensure(size_t(chunk));
-    W.find_work.ensure(1);
+    W.ray32.ensure(size_t(chunk));
+    W.find_work.ensure(2);  // [0] k_find's work counter, [1] k_trace's
     FindArgs fnd;
     fnd.sc = S.dev;
     fnd.txp = W.txp.p;
@@ -779,8 +787,13 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fnd.work = W.find_work.p;
     fnd.cand = W.cand.p;
     fnd.ncand = W.ncand.p;
+    fnd.ray32 = W.ray32.p;
+    fnd.steps = kFindSteps;
+    fnd.refill = kFindRefill;
     ta.cand = W.cand.p;
     ta.ncand = W.ncand.p;
+    ta.ray32 = W.ray32.p;
+    ta.work = W.find_work.p + 1;
     size_t n_tr = 0;  // k_trace launches (timed one by one)
     for (int d = 0; d <= max_depth; ++d) {
       ta.depth = fnd.depth = d;
@@ -790,7 +803,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       for (long long lo = 0; lo < bound; lo += chunk) {
         ta.lo = fnd.lo = lo;
         ta.hi = fnd.hi = std::min(bound, lo + chunk);
-        CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(W.find_work.p, 0, 2 * sizeof(unsigned long long), st));
         ++nl, k_find<<<find_grid(), 128, 0, st>>>(fnd);
         if (2 * n_tr + 2 > W.tr_ev.size()) {
           W.tr_ev.resize(2 * n_tr + 2, nullptr);
@@ -798,7 +811,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
             if (!e) CK(cudaEventCreate(&e));
         }
         CK(cudaEventRecord(W.tr_ev[2 * n_tr], st));
-        ++nl, k_trace<<<grid_for(ta.hi - lo, 128), 128, 0, st>>>(ta);
+        ++nl, k_trace<<<std::min<long long>(trace_grid(), (ta.hi - lo + 127) / 128), 128, 0, st>>>(ta);
         CK(cudaEventRecord(W.tr_ev[2 * n_tr + 1], st));
         ++n_tr;
       }

@@ -104,8 +104,8 @@ __device__ __forceinline__ bool slab64(const double* bb, const double* o, const 
 
 // BVH::RayIntersects (BVH/BVH.h:276-328) exactly: depth-first, both children,
 // children[0] first, strict '<' on distance so the first visited wins ties.
-__device__ bool exact_closest(const DevScene& sc, const double* o, const double* d, Hit& best,
-                              unsigned* overflow) {
+__device__ __noinline__ bool exact_closest(const DevScene& sc, const double* o, const double* d,
+                                           Hit& best, unsigned* overflow) {
   int stack[kStack];
   int sp = 0;
   stack[sp++] = 0;
@@ -350,8 +350,8 @@ __device__ __forceinline__ int slab_certain(const float* bb, int flatmask, const
 // reference's strict '<' in visit order.  The winner is accepted only if every
 // ancestor box of its leaf passes the reference's FP64 slab test; otherwise
 // the ray is re-run with the reference-order traversal.
-__device__ bool closest_hit(const DevScene& sc, const double* o, const double* d, Hit& best,
-                            TraceStats& st, unsigned* overflow) {
+__device__ __noinline__ bool closest_hit(const DevScene& sc, const double* o, const double* d,
+                                         Hit& best, TraceStats& st, unsigned* overflow) {
   const float3 o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
   const float3 d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
   const float3 inv = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
@@ -520,7 +520,6 @@ __device__ bool closest_hit(const DevScene& sc, const double* o, const double* d
 constexpr int kCand = 8;
 constexpr unsigned char kFindFallback = 0xFF;
 
-// Resolution of a ray's contenders (rank, FP32 t lower bound as bits).
 // Whether the reference's test of the triangle a ray starts on certainly
 // fails (so its FP64 test can be skipped).  The ray's origin is the hit
 // point the parent ray's FP64 test produced on that triangle, within about
@@ -540,61 +539,6 @@ __device__ __forceinline__ bool origin_rejected(const Tri32& T, const float3& o3
   const float dn = dx * nx + dy * ny + dz * nz;
   const float nn = sqrtf(nx * nx + ny * ny + nz * nz), dd = sqrtf(dx * dx + dy * dy + dz * dz);
   return fabsf(dn) >= 1e-2f * nn * dd;
-}
-
-__device__ bool resolve_hit(const DevScene& sc, const double* o, const double* d,
-                            const float3& o32, const float3& d32, const uint2* cand, int nc,
-                            Hit& best, TraceStats& st, unsigned* overflow, int orank = -1) {
-  if (nc == kFindFallback)  // more contenders than kept, or a deep stack: one-pass search
-    return closest_hit(sc, o, d, best, st, overflow);
-  int cr[kCand];
-  float ct[kCand];
-  for (int i = 0; i < nc; ++i) {
-    const uint2 c = cand[i];
-    const float t = __uint_as_float(c.y);
-    int j = i - 1;
-    while (j >= 0 && ct[j] > t) {  // insertion by lower bound (stable)
-      ct[j + 1] = ct[j];
-      cr[j + 1] = cr[j];
-      --j;
-    }
-    ct[j + 1] = t;
-    cr[j + 1] = int(c.x);
-  }
-  best.rank = INT_MAX;
-  best.dist = __longlong_as_double(0x7ff0000000000000ll);
-  best.t = best.dist;
-  for (int i = 0; i < nc; ++i) {
-    if (best.rank != INT_MAX && ct[i] > float(best.t) * (1.0f + kTieSlack) + 1e-30f) break;
-    const int r = cr[i];
-    if (r == orank && origin_rejected(sc.tri32[r], o32, d32)) continue;
-    ++st.fp64_tri;
-    double t, P[3], dist;
-    if (mt64(sc.tri64[r], o, d, t, P, dist) &&
-        (dist < best.dist || (dist == best.dist && r < best.rank))) {
-      best.dist = dist;
-      best.t = t;
-      best.p[0] = P[0];
-      best.p[1] = P[1];
-      best.p[2] = P[2];
-      best.rank = r;
-    }
-  }
-  if (best.rank == INT_MAX) return false;
-  best.leaf = sc.tri64[best.rank].node;
-  // every ancestor of the winner's leaf must pass the reference's slab test
-  const float3 i32 = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
-  for (const AncBox* a = sc.anc + sc.anc_off[best.leaf];; ++a) {
-    const AncBox b = *a;
-    if (b.node < 0) break;
-    int v = slab_certain(b.fb, b.flat, o32, d32, i32);
-    if (v < 0) v = slab64(sc.ref[b.node].bb, o, d) ? 1 : 0;
-    if (!v) {
-      ++st.fallback;
-      return exact_closest(sc, o, d, best, overflow);
-    }
-  }
-  return true;
 }
 
 // HitReceptionSphere (RTSolver.cpp:805-863), FP64 in the reference's order.

@@ -41,6 +41,8 @@ struct TraceArgs {
   long long lo, hi;    // this launch covers rays [lo, hi) of the depth
   const uint2* cand;   // contenders of those rays (k_find)
   const unsigned char* ncand;
+  const RayF32* ray32; // FP32 copies of those rays (k_find)
+  unsigned long long* work;  // rays of the chunk handed out (zero at launch)
 };
 
 __device__ __forceinline__ int find_request(const TxParams* txp, int n_tx, long long g) {
@@ -169,7 +171,8 @@ __device__ __forceinline__ void root_ray(const TxParams* txp, int n_tx, const do
 // half the warp is idle or nobody is busy), so warps stay full while rays of
 // very different lengths finish at different times.  A step is one node
 // visit or one triangle test, so lanes in a leaf and lanes between nodes
-// advance at the same pace.
+// advance at the same pace.  The FP32 copy of each ray it loads is kept for
+// k_trace (ray32).
 struct FindArgs {
   DevScene sc;
   const TxParams* txp;
@@ -184,17 +187,14 @@ struct FindArgs {
   unsigned long long* work;    // rays of the chunk handed out (zero at launch)
   uint2* cand;                 // kCand per ray of the chunk
   unsigned char* ncand;        // contenders per ray, kFindFallback = exact traversal
+  RayF32* ray32;               // FP32 copy per ray of the chunk
+  int steps;                   // traversal steps between refills
+  int refill;                  // idle lanes that trigger a refill
 };
 
-// Traversal steps between refills, and the idle lanes that trigger one.
-#ifndef SBR_FIND_STEPS
-#define SBR_FIND_STEPS 32
-#endif
-#ifndef SBR_FIND_REFILL
-#define SBR_FIND_REFILL 16
-#endif
-constexpr int kFindSteps = SBR_FIND_STEPS;
-constexpr int kFindRefill = SBR_FIND_REFILL;
+// Defaults of the search's tunables (the autotuner may choose others).
+constexpr int kFindSteps = 32;
+constexpr int kFindRefill = 16;
 
 __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
@@ -207,14 +207,14 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
   float3 o32 = make_float3(0, 0, 0), d32 = o32, inv = o32;
   float no = 0.0f, nd = 0.0f, m = 0.0f, tcut = INFINITY;
   int stack[kStack];
-  int sp = 0, pending = -1, nc = 0;
+  int sp = 0, pending = -1, nc = 0, orank = -1;
   bool fail = false;
   uint2* out = nullptr;
   while (true) {
     const bool idle = ray < 0 && !exhausted;
     const unsigned im = __ballot_sync(0xffffffffu, idle);
     const unsigned busy = __ballot_sync(0xffffffffu, ray >= 0);
-    if (im && (__popc(im) >= kFindRefill || busy == 0)) {
+    if (im && (__popc(im) >= A.refill || busy == 0)) {
       const int leader = __ffs(im) - 1;
       unsigned long long base = 0;
       if (int(lane) == leader) base = atomicAdd(A.work, (unsigned long long)__popc(im));
@@ -224,6 +224,7 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
         if (k < n) {
           ray = k;
           double o[3], d[3];
+          orank = -1;
           if (A.depth == 0) {
             int q;
             long long li;
@@ -242,9 +243,15 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
               x64::normalize(v, d);
               for (int a = 0; a < 3; ++a) r.d[a] = d[a];
             }
+            orank = r.orank;
           }
           o32 = make_float3(float(o[0]), float(o[1]), float(o[2]));
           d32 = make_float3(float(d[0]), float(d[1]), float(d[2]));
+          {
+            float4* f = reinterpret_cast<float4*>(A.ray32 + k);
+            f[0] = make_float4(o32.x, o32.y, o32.z, 0.0f);
+            f[1] = make_float4(d32.x, d32.y, d32.z, 0.0f);
+          }
           inv = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
           no = sqrtf(o32.x * o32.x + o32.y * o32.y + o32.z * o32.z);
           nd = sqrtf(d32.x * d32.x + d32.y * d32.y + d32.z * d32.z);
@@ -267,20 +274,26 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
     }
     if (ray < 0) continue;
     bool done = false;
-    for (int it = 0; it < kFindSteps && !done; ++it) {
+    for (int it = 0; it < A.steps && !done; ++it) {
       if (pending >= 0) {
         // one triangle of the pending leaf per step, so lanes testing
         // triangles and lanes stepping through nodes cost one step each
         const int j = pending >> 3, left = (pending & 7) - 1;
         pending = left > 0 ? ((j + 1) << 3 | left) : -1;
         float tlo, thi;
-        const int k = tri_classify(A.sc.stri[j], o32, d32, no, nd, tlo, thi);
+        const Tri32 T = A.sc.stri[j];
+        const int k = tri_classify(T, o32, d32, no, nd, tlo, thi);
         if (k == 0 || tlo > tcut) continue;
+        const int rk = __ldg(A.sc.srank + j);
+        // the triangle the ray starts on, left at a clear angle: the
+        // reference's test of it certainly fails (origin_rejected); such a
+        // contender is never certain (k == 2), so dropping it changes no cut
+        if (rk == orank && origin_rejected(T, o32, d32)) continue;
         if (nc == kCand) {
           fail = done = true;
           break;
         }
-        out[nc++] = make_uint2(unsigned(__ldg(A.sc.srank + j)), __float_as_uint(tlo));
+        out[nc++] = make_uint2(unsigned(rk), __float_as_uint(tlo));
         if (k == 2) tcut = fminf(tcut, thi * (1.0f + kTieSlack) + 1e-30f);
         continue;
       }
@@ -349,149 +362,263 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
 #ifndef SBR_TRACE_BLOCKS
 #define SBR_TRACE_BLOCKS 4
 #endif
+
+// The tree node of a resolved ray and its children (RTSolver.cpp:142-257):
+// node record, reflected and transmitted rays, path-class interning.
+__device__ __forceinline__ void finish_ray(const TraceArgs& A, const RayRec& r, const float3& o32,
+                                           const float3& d32, bool hit, const Hit& h) {
+  const TxParams& P = A.txp[r.tx];
+  const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
+  {  // per-request segment count, one atomic per request present in the warp
+    const unsigned peers = __match_any_sync(__activemask(), r.tx);
+    if (int(lane_id()) == __ffs(peers) - 1)
+      atomicAdd(&A.seg_per_tx[r.tx], (unsigned long long)__popc(peers));
+  }
+  const bool root = A.depth == 0;
+  if (ni < A.node_cap) {
+    NodeCold n;
+    NodeHot m;
+    n.s[0] = r.o[0]; n.s[1] = r.o[1]; n.s[2] = r.o[2];
+    if (hit) {
+      n.t[0] = h.p[0]; n.t[1] = h.p[1]; n.t[2] = h.p[2];
+      m.len = float(h.dist);
+    } else {
+      const double sc = root ? 1E10 : 1E2;  // RTSolver.cpp:231,249
+      n.t[0] = x64::add(r.o[0], x64::mul(r.d[0], sc));
+      n.t[1] = x64::add(r.o[1], x64::mul(r.d[1], sc));
+      n.t[2] = x64::add(r.o[2], x64::mul(r.d[2], sc));
+      m.len = float(sc);
+    }
+    n.S = r.S;
+    n.pad = 0.0;
+    m.s[0] = o32.x; m.s[1] = o32.y; m.s[2] = o32.z;
+    m.S = float(r.S);
+    m.u[0] = d32.x; m.u[1] = d32.y; m.u[2] = d32.z;
+    m.parent = r.parent;
+    m.cls = r.cls;
+    m.launch = r.launch;
+    m.heap = r.heap;
+    m.tx = r.tx;
+    m.pad0 = m.pad1 = m.pad2 = 0;
+    A.nodes_cold[ni] = n;
+    A.nodes[ni] = m;
+  } else {
+    atomicOr(&A.ctr->overflow, kOvNodes);
+  }
+  // children (RTSolver.cpp:186-221)
+  unsigned nch = 0;
+  bool do_r = false, do_t = false;
+  if (hit) {
+    do_r = r.rc < P.R;
+    do_t = r.tc < P.T;
+    nch = unsigned(do_r) + unsigned(do_t);
+  }
+  const unsigned long long base = warp_reserve(&A.ctr->queue[A.depth + 1], nch);
+  if (nch) {
+    const Tri64& T = A.sc.tri64[h.rank];
+    const double cum = x64::add(r.total, h.dist);  // node pathLength
+    RayRec c;
+    c.o[0] = h.p[0]; c.o[1] = h.p[1]; c.o[2] = h.p[2];
+    c.total = cum;
+    c.S = x64::add(r.S, cum);
+    c.parent = uint32_t(ni);
+    c.launch = r.launch;
+    c.tx = r.tx;
+    c.orank = h.rank;
+    const int cop = A.tri_cop[h.rank];
+    const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
+    const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop,
+                                         &A.ctr->lost_cop);
+    // image source of the parent ray's class (the transmitter for a launch)
+    const double* pimg = is_root_class(r.cls) ? P.tx : A.cls_info[r.cls].img;
+    unsigned long long slot = base;
+    if (do_t) {  // transmitted: same direction, heap 2h, same image source
+      c.d[0] = r.d[0]; c.d[1] = r.d[1]; c.d[2] = r.d[2];
+      c.heap = r.heap * 2;
+      c.rc = r.rc;
+      c.tc = r.tc + 1;
+      const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
+      bool fresh = false;
+      c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
+                        &A.ctr->lost_cls, &fresh);
+      c.cop = cop_cls;
+      if (fresh) {  // only the thread that interned the class writes its records
+        write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
+        write_class_cap(A.sc, pimg, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
+        list_class(A, c.cls);
+      }
+      if (slot < A.out_cap) A.out[slot] = c;
+      else atomicOr(&A.ctr->overflow, kOvQueue);
+      ++slot;
+    }
+    if (do_r) {  // reflected: Reflect(d, n), heap 2h+1; k_find normalises it
+      const double dn = x64::dot(T.n, r.d);
+      for (int a = 0; a < 3; ++a) c.d[a] = x64::sub(r.d[a], x64::mul(x64::mul(2.0, T.n[a]), dn));
+      c.heap = r.heap * 2 + 1;
+      c.rc = r.rc + 1;
+      c.tc = r.tc;
+      const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1);
+      bool fresh = false;
+      c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
+                        &A.ctr->lost_cls, &fresh);
+      c.cop = cop_cls;
+      if (fresh) {  // only the thread that interned the class writes its records
+        // ImagePoint (RTSolver.cpp:910-924) across the triangle the
+        // reference finds at this id's position of its mesh vector
+        const CorrTri& M = A.sc.corr[A.sc.rank_to_id[h.rank]];
+        double w[3], img[3];
+        x64::sub3(pimg, M.v1, w);
+        const double dist = x64::dot(M.n, w);
+        for (int a = 0; a < 3; ++a) img[a] = x64::sub(pimg[a], x64::mul(x64::mul(2.0, dist), M.n[a]));
+        write_class(A.cls_info[c.cls], img, r.cls, h.rank, cop_cls, 1, A.depth + 1);
+        write_class_cap(A.sc, img, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
+        list_class(A, c.cls);
+      }
+      if (slot < A.out_cap) A.out[slot] = c;
+      else atomicOr(&A.ctr->overflow, kOvQueue);
+    }
+  }
+}
+
+// Every ancestor box of the winner's leaf in the reference BVH must pass the
+// reference's slab test, else the ray takes the reference-order traversal.
+__device__ __forceinline__ bool reachable_or_exact(const DevScene& sc, const RayRec& r,
+                                                   const float3& o32, const float3& d32, Hit& best,
+                                                   TraceStats& st, unsigned* overflow) {
+  best.leaf = sc.tri64[best.rank].node;
+  const float3 i32 = make_float3(1.0f / d32.x, 1.0f / d32.y, 1.0f / d32.z);
+  for (const AncBox* a = sc.anc + sc.anc_off[best.leaf];; ++a) {
+    const AncBox b = *a;
+    if (b.node < 0) break;
+    int v = slab_certain(b.fb, b.flat, o32, d32, i32);
+    if (v < 0) v = slab64(sc.ref[b.node].bb, r.o, r.d) ? 1 : 0;
+    if (!v) {
+      ++st.fallback;
+      return exact_closest(sc, r.o, r.d, best, overflow);
+    }
+  }
+  return true;
+}
+
+// FP64 resolution of the contenders k_find left: they are tested in
+// ascending order of their FP32 lower bound on t until none can reach the
+// best exact distance; the answer is the lexicographic minimum (distance,
+// depth-first rank), the reference's strict '<' in visit order, accepted if
+// its leaf is reachable in the reference BVH (reachable_or_exact).  The kernel
+// is persistent: each lane holds one ray and runs at most one
+// FP64 triangle test per round, so the warp's FP64 instructions serve every
+// lane that has a test due, whether it is a ray's first contender or a later
+// one.  A lane whose ray is resolved writes the node and children in the
+// same round and takes a new ray (one atomic per warp); a ray needing a
+// second test no longer holds the whole warp through a second pass of the
+// test with a few lanes.
 __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
   const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
-  const long long n_in = min(n_all, A.hi);
+  const long long n = min(n_all, A.hi) - A.lo;
+  if (n <= 0) return;
+  const unsigned lane = lane_id();
   TraceStats st{0, 0};
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = A.lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in;
-       i += stride) {
-    RayRec r;
-    if (A.depth == 0) {
-      int q;
-      long long li;
-      root_ray(A.txp, A.n_tx, A.dirs, i, r.o, r.d, q, li);
-      r.total = 0.0;
-      r.S = 0.0;
-      r.parent = 0xFFFFFFFFu;
-      r.orank = -1;
-      r.cls = kRootBase + uint32_t(q);
-      r.cop = kRootClass;
-      r.launch = uint32_t(li);
-      r.heap = 1;
-      r.rc = r.tc = 0;
-      r.tx = uint32_t(q);
-    } else {
-      r = A.in[i];
-    }
-    const TxParams& P = A.txp[r.tx];
-    Hit h;
-    const long long c = i - A.lo;
-    // the ray in FP32, converted once (each conversion costs an FP64 pipe slot)
-    const float3 o32 = make_float3(float(r.o[0]), float(r.o[1]), float(r.o[2]));
-    const float3 d32 = make_float3(float(r.d[0]), float(r.d[1]), float(r.d[2]));
-    const bool hit = resolve_hit(A.sc, r.o, r.d, o32, d32, A.cand + size_t(c) * kCand,
-                                 A.ncand[c], h, st, &A.ctr->overflow, r.orank);
-    const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
-    {  // per-request segment count, one atomic per request present in the warp
-      const unsigned peers = __match_any_sync(__activemask(), r.tx);
-      if (int(lane_id()) == __ffs(peers) - 1)
-        atomicAdd(&A.seg_per_tx[r.tx], (unsigned long long)__popc(peers));
-    }
-    const bool root = A.depth == 0;
-    if (ni < A.node_cap) {
-      NodeCold n;
-      NodeHot m;
-      n.s[0] = r.o[0]; n.s[1] = r.o[1]; n.s[2] = r.o[2];
-      if (hit) {
-        n.t[0] = h.p[0]; n.t[1] = h.p[1]; n.t[2] = h.p[2];
-        m.len = float(h.dist);
-      } else {
-        const double sc = root ? 1E10 : 1E2;  // RTSolver.cpp:231,249
-        n.t[0] = x64::add(r.o[0], x64::mul(r.d[0], sc));
-        n.t[1] = x64::add(r.o[1], x64::mul(r.d[1], sc));
-        n.t[2] = x64::add(r.o[2], x64::mul(r.d[2], sc));
-        m.len = float(sc);
-      }
-      n.S = r.S;
-      n.pad = 0.0;
-      m.s[0] = o32.x; m.s[1] = o32.y; m.s[2] = o32.z;
-      m.S = float(r.S);
-      m.u[0] = d32.x; m.u[1] = d32.y; m.u[2] = d32.z;
-      m.parent = r.parent;
-      m.cls = r.cls;
-      m.launch = r.launch;
-      m.heap = r.heap;
-      m.tx = r.tx;
-      m.pad0 = m.pad1 = m.pad2 = 0;
-      A.nodes_cold[ni] = n;
-      A.nodes[ni] = m;
-    } else {
-      atomicOr(&A.ctr->overflow, kOvNodes);
-    }
-    // children (RTSolver.cpp:186-221)
-    unsigned nch = 0;
-    bool do_r = false, do_t = false;
-    if (hit) {
-      do_r = r.rc < P.R;
-      do_t = r.tc < P.T;
-      nch = unsigned(do_r) + unsigned(do_t);
-    }
-    const unsigned long long base = warp_reserve(&A.ctr->queue[A.depth + 1], nch);
-    if (nch) {
-      const Tri64& T = A.sc.tri64[h.rank];
-      const double cum = x64::add(r.total, h.dist);  // node pathLength
-      RayRec c;
-      c.o[0] = h.p[0]; c.o[1] = h.p[1]; c.o[2] = h.p[2];
-      c.total = cum;
-      c.S = x64::add(r.S, cum);
-      c.parent = uint32_t(ni);
-      c.launch = r.launch;
-      c.tx = r.tx;
-      c.orank = h.rank;
-      const int cop = A.tri_cop[h.rank];
-      const unsigned long long ck = (unsigned long long)r.cop << 32 | uint32_t(cop);
-      const uint32_t cop_cls = ht_insert(A.cop_tab, ck, &A.ctr->overflow, kOvCop, &A.ctr->used_cop,
-                                           &A.ctr->lost_cop);
-      // image source of the parent ray's class (the transmitter for a launch)
-      const double* pimg = is_root_class(r.cls) ? P.tx : A.cls_info[r.cls].img;
-      unsigned long long slot = base;
-      if (do_t) {  // transmitted: same direction, heap 2h, same image source
-        c.d[0] = r.d[0]; c.d[1] = r.d[1]; c.d[2] = r.d[2];
-        c.heap = r.heap * 2;
-        c.rc = r.rc;
-        c.tc = r.tc + 1;
-        const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1 | 1u);
-        bool fresh = false;
-        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
-                          &A.ctr->lost_cls, &fresh);
-        c.cop = cop_cls;
-        if (fresh) {  // only the thread that interned the class writes its records
-          write_class(A.cls_info[c.cls], pimg, r.cls, h.rank, cop_cls, 2, A.depth + 1);
-          write_class_cap(A.sc, pimg, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
-          list_class(A, c.cls);
+  long long c = -1;  // the lane's ray (index in the chunk), -1 = none
+  bool exhausted = false;
+  RayRec r;
+  float3 o32 = make_float3(0.0f, 0.0f, 0.0f), d32 = o32;
+  int cr[kCand];
+  float ct[kCand];
+  int nc = 0, next = 0;
+  Hit best;
+  best.rank = INT_MAX;
+  while (true) {
+    const bool idle = c < 0 && !exhausted;
+    const unsigned im = __ballot_sync(0xffffffffu, idle);
+    if (im) {
+      const int leader = __ffs(im) - 1;
+      unsigned long long base = 0;
+      if (int(lane) == leader) base = atomicAdd(A.work, (unsigned long long)__popc(im));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (idle) {
+        const long long k = (long long)base + __popc(im & ((1u << lane) - 1u));
+        if (k < n) {
+          c = k;
+          const long long i = A.lo + k;
+          if (A.depth == 0) {
+            int q;
+            long long li;
+            root_ray(A.txp, A.n_tx, A.dirs, i, r.o, r.d, q, li);
+            r.total = 0.0;
+            r.S = 0.0;
+            r.parent = 0xFFFFFFFFu;
+            r.orank = -1;
+            r.cls = kRootBase + uint32_t(q);
+            r.cop = kRootClass;
+            r.launch = uint32_t(li);
+            r.heap = 1;
+            r.rc = r.tc = 0;
+            r.tx = uint32_t(q);
+          } else {
+            r = A.in[i];
+          }
+          // the FP32 copy k_find made (a conversion costs an FP64 pipe slot)
+          const float4* f = reinterpret_cast<const float4*>(A.ray32 + k);
+          const float4 fo = f[0], fd = f[1];
+          o32 = make_float3(fo.x, fo.y, fo.z);
+          d32 = make_float3(fd.x, fd.y, fd.z);
+          nc = A.ncand[k];
+          if (nc != kFindFallback) {
+            const uint2* cand = A.cand + size_t(k) * kCand;
+            for (int j = 0; j < nc; ++j) {
+              const uint2 e = cand[j];
+              const float t = __uint_as_float(e.y);
+              int m = j - 1;
+              while (m >= 0 && ct[m] > t) {  // insertion by lower bound (stable)
+                ct[m + 1] = ct[m];
+                cr[m + 1] = cr[m];
+                --m;
+              }
+              ct[m + 1] = t;
+              cr[m + 1] = int(e.x);
+            }
+          }
+          next = 0;
+          best.rank = INT_MAX;
+          best.dist = __longlong_as_double(0x7ff0000000000000ll);
+          best.t = best.dist;
+        } else {
+          exhausted = true;
         }
-        if (slot < A.out_cap) A.out[slot] = c;
-        else atomicOr(&A.ctr->overflow, kOvQueue);
-        ++slot;
       }
-      if (do_r) {  // reflected: Reflect(d, n), heap 2h+1; k_find normalises it
-        const double dn = x64::dot(T.n, r.d);
-        for (int a = 0; a < 3; ++a) c.d[a] = x64::sub(r.d[a], x64::mul(x64::mul(2.0, T.n[a]), dn));
-        c.heap = r.heap * 2 + 1;
-        c.rc = r.rc + 1;
-        c.tc = r.tc;
-        const unsigned long long key = (unsigned long long)r.cls << 32 | (uint32_t(h.rank) << 1);
-        bool fresh = false;
-        c.cls = ht_insert(A.cls_tab, key, &A.ctr->overflow, kOvClass, &A.ctr->used_cls,
-                          &A.ctr->lost_cls, &fresh);
-        c.cop = cop_cls;
-        if (fresh) {  // only the thread that interned the class writes its records
-          // ImagePoint (RTSolver.cpp:910-924) across the triangle the
-          // reference finds at this id's position of its mesh vector
-          const CorrTri& M = A.sc.corr[A.sc.rank_to_id[h.rank]];
-          double w[3], img[3];
-          x64::sub3(pimg, M.v1, w);
-          const double dist = x64::dot(M.n, w);
-          for (int a = 0; a < 3; ++a) img[a] = x64::sub(pimg[a], x64::mul(x64::mul(2.0, dist), M.n[a]));
-          write_class(A.cls_info[c.cls], img, r.cls, h.rank, cop_cls, 1, A.depth + 1);
-          write_class_cap(A.sc, img, A.sc.rank_to_id[h.rank], A.cls_cap[c.cls]);
-          list_class(A, c.cls);
+    }
+    if (__ballot_sync(0xffffffffu, c >= 0) == 0) break;  // every lane is out of rays
+    if (c < 0) continue;
+    bool done, hit;
+    if (nc == kFindFallback) {  // more contenders than kept, or a deep stack: one-pass search
+      hit = closest_hit(A.sc, r.o, r.d, best, st, &A.ctr->overflow);
+      done = true;
+    } else {
+      if (next < nc) {  // the next contender, nearest lower bound first
+        const int rk = cr[next++];
+        ++st.fp64_tri;
+        double t, P[3], dist;
+        if (mt64(A.sc.tri64[rk], r.o, r.d, t, P, dist) &&
+            (dist < best.dist || (dist == best.dist && rk < best.rank))) {
+          best.dist = dist;
+          best.t = t;
+          best.p[0] = P[0];
+          best.p[1] = P[1];
+          best.p[2] = P[2];
+          best.rank = rk;
         }
-        if (slot < A.out_cap) A.out[slot] = c;
-        else atomicOr(&A.ctr->overflow, kOvQueue);
       }
+      // resolved when no further contender can reach the best exact distance
+      done = !(next < nc &&
+               (best.rank == INT_MAX || ct[next] <= float(best.t) * (1.0f + kTieSlack) + 1e-30f));
+      hit = false;
+      if (done && best.rank != INT_MAX)
+        hit = reachable_or_exact(A.sc, r, o32, d32, best, st, &A.ctr->overflow);
+    }
+    if (done) {
+      finish_ray(A, r, o32, d32, hit, best);
+      c = -1;
     }
   }
   if (st.fp64_tri) atomicAdd(&A.ctr->fp64_tri, (unsigned long long)st.fp64_tri);
