@@ -583,6 +583,249 @@ __global__ void __launch_bounds__(32 * kCapWarps, kStage ? 4 : SBR_CAP_BLOCKS) k
   }
 }
 
+// ---- fast path, flattened over the nodes of a batch ------------------------
+//
+// The same tests as k_capture's fast path with the same chunks, cell boxes
+// and margins, so the same (node, receiver) pairs reach k_capture_finish.
+// The warp stages B nodes (one lane each: node record, class record, last
+// triangle, loosened correction cone, clipped span), then works through the
+// whole batch at three flattened levels instead of node by node: the batch's
+// (node, chunk) items with one lane per item (cell box, cone test), those
+// items' rows of cells with one lane per row (the row's receiver run), and
+// those rows' receivers with one lane per receiver (correction prefilter,
+// FP32 reception test).  Each level is an inclusive prefix count over the
+// lanes; an item finds its parent by a binary search over the counts.  A
+// node with a handful of candidates (about six per node at level 9) thus no
+// longer holds all 32 lanes through its own chunk, row and receiver passes.
+
+__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
+  for (int o = 1; o < 32; o <<= 1) {
+    const int x = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += x;
+  }
+  return v;
+}
+
+// The first lane whose inclusive count exceeds k (0 <= k < the total).
+__device__ __forceinline__ int warp_find(int incl, int k) {
+  int rl = 0;
+  for (int step = 16; step; step >>= 1) {
+    const int v = __shfl_sync(0xffffffffu, incl, rl + step - 1);
+    if (v <= k) rl += step;
+  }
+  return rl;
+}
+
+constexpr int kFastB = 16;  // nodes staged per warp and batch
+
+__global__ void __launch_bounds__(32 * kCapWarps, SBR_CAP_BLOCKS) k_capture_fast(CaptureArgs A) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
+  const unsigned long long n_nodes = min(A.ctr->nodes, A.node_cap);
+  unsigned long long cand = 0;
+  constexpr int B = kFastB;
+  __shared__ NodeHot s_nh[kCapWarps][B];
+  __shared__ Tri32 s_tl[kCapWarps][B];      // the class's last triangle
+  __shared__ float s_fl[kCapWarps][B][12];  // image source + correction filter terms
+  __shared__ float s_cn[kCapWarps][B][16];  // loosened correction cone
+  __shared__ NodeSpan s_sp[kCapWarps][B];   // clipped span and chunking
+  __shared__ ChunkBox s_ck[kCapWarps][32];  // the current 32 (node, chunk) items
+  __shared__ int s_ckn[kCapWarps][32];      // their node (batch index) | chunk << 8
+  for (unsigned long long base = next_batch(A.work, lane, B); base < n_nodes;
+       base = next_batch(A.work, lane, B)) {
+    int nck = 0;  // chunks of this lane's node
+    {
+      const unsigned long long my = base + lane;
+      if (lane < B && my < n_nodes) {
+        const NodeHot h = A.nodes[my];
+        s_nh[warp][lane] = h;
+        const float cmax = A.gb[h.tx].cmax;
+        int cone_ok = 0;
+        if (!is_root_class(h.cls)) {
+          const ClassCap c = A.cls_cap[h.cls];
+          s_tl[warp][lane] = A.sc.corr32[c.tpos];
+          float* fl = s_fl[warp][lane];
+          for (int q = 0; q < 3; ++q) fl[q] = c.img[q];
+          for (int q = 0; q < 8; ++q) fl[3 + q] = c.F[q];
+          // the cone's planes loosened by 2 m, m = 2^-19 |n| (cmax + |img| + |T| + 1)
+          float* cn = s_cn[warp][lane];
+          cone_ok = 1;
+          for (int k = 0; k < 3; ++k) {
+            const float m = 1.9073486328125e-06f * (c.nn[k] * cmax + c.w[k]);
+            cone_ok &= (c.gc[k] > 4.0f * m && isfinite(m)) ? 1 : 0;
+            cn[4 * k + 0] = c.n[k][0];
+            cn[4 * k + 1] = c.n[k][1];
+            cn[4 * k + 2] = c.n[k][2];
+            cn[4 * k + 3] = c.n[k][3] - 2.0f * m;
+            cn[12 + k] = c.inv_nx[k];
+          }
+        }
+        const NodeSpan sp = node_span(h, A.txp[h.tx], A.grids[h.tx], cmax, cone_ok);
+        s_sp[warp][lane] = sp;
+        nck = sp.nchunk;
+      }
+      __syncwarp();
+    }
+    const int ck_incl = warp_incl_scan(nck, lane);
+    const int n_ck = __shfl_sync(FULL, ck_incl, 31);
+    for (int k0 = 0; k0 < n_ck; k0 += 32) {
+      // level 1: one lane per (node, chunk) item
+      const int k = k0 + lane;
+      const int j = warp_find(ck_incl, min(k, n_ck - 1));
+      const int j_incl = __shfl_sync(FULL, ck_incl, j), j_n = __shfl_sync(FULL, nck, j);
+      int nrows = 0;
+      if (k < n_ck) {
+        const int ch = k - (j_incl - j_n);
+        const NodeHot& nd = s_nh[warp][j];
+        const NodeSpan& sp = s_sp[warp][j];
+        const ChunkBox cb = chunk_box(nd, A.grids[nd.tx], sp, ch, A.gb[nd.tx].cmax,
+                                      A.txp[nd.tx].tan_beta32, sp.use_cone != 0, s_cn[warp][j]);
+        s_ck[warp][lane] = cb;
+        s_ckn[warp][lane] = j | ch << 8;
+        nrows = cb.nrows;
+      }
+      __syncwarp();
+      const int r_incl = warp_incl_scan(nrows, lane);
+      const int n_r = __shfl_sync(FULL, r_incl, 31);
+      for (int r0 = 0; r0 < n_r; r0 += 32) {
+        // level 2: one lane per row of cells: the part of its chunk within rb
+        // of the row's y/z band, cut to the cone, as a run of receivers
+        const int r = r0 + lane;
+        const int ci = warp_find(r_incl, min(r, n_r - 1));
+        const int ci_incl = __shfl_sync(FULL, r_incl, ci), ci_n = __shfl_sync(FULL, nrows, ci);
+        int beg = 0, cnt = 0;
+        if (r < n_r) {
+          const int ridx = r - (ci_incl - ci_n);
+          const ChunkBox& cb = s_ck[warp][ci];
+          const int jn = s_ckn[warp][ci] & 0xff;
+          const NodeHot& nd = s_nh[warp][jn];
+          const RxGrid& g = A.grids[nd.tx];
+          const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
+          const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
+          // Reciprocals for the cell-range arithmetic: every range is widened
+          // by at least 2e-3 m + cell/100, far more than the few ulps a product
+          // with a reciprocal differs from the quotient.
+          const float inv_uy = __frcp_rn(u.y), inv_uz = __frcp_rn(u.z);
+          const float rb = cb.rb;
+          const int ny = cb.c1[1] - cb.c0[1] + 1;
+          // one layer of cells (receivers on a plane) needs no division
+          const bool flat = cb.c1[2] == cb.c0[2];
+          const int iy = cb.c0[1] + (flat ? ridx : ridx % ny);
+          const int iz = cb.c0[2] + (flat ? 0 : ridx / ny);
+          const float y0 = g.org[1] + iy * g.cell - rb, y1 = g.org[1] + (iy + 1) * g.cell + rb;
+          const float z0 = g.org[2] + iz * g.cell - rb, z1 = g.org[2] + (iz + 1) * g.cell + rb;
+          float la = cb.a, lb = cb.b;
+          bool ok = true;
+          if (fabsf(u.y) > 1e-20f) {
+            const float t1 = (y0 - s.y) * inv_uy, t2 = (y1 - s.y) * inv_uy;
+            la = fmaxf(la, fminf(t1, t2));
+            lb = fminf(lb, fmaxf(t1, t2));
+          } else if (s.y < y0 || s.y > y1) {
+            ok = false;
+          }
+          if (fabsf(u.z) > 1e-20f) {
+            const float t1 = (z0 - s.z) * inv_uz, t2 = (z1 - s.z) * inv_uz;
+            la = fmaxf(la, fminf(t1, t2));
+            lb = fminf(lb, fmaxf(t1, t2));
+          } else if (s.z < z0 || s.z > z1) {
+            ok = false;
+          }
+          if (ok && la <= lb) {
+            const float inv_cell = g.inv_cell;
+            const float xa = s.x + la * u.x, xb = s.x + lb * u.x;
+            int x0 = max(cb.c0[0], int(floorf((fminf(xa, xb) - rb - g.org[0]) * inv_cell)));
+            int x1 = min(cb.c1[0], int(floorf((fmaxf(xa, xb) + rb - g.org[0]) * inv_cell)));
+            if (s_sp[warp][jn].use_cone && x0 <= x1)
+              cone_cells(s_cn[warp][jn], g, inv_cell, iy, iz, x0, x1);
+            if (x0 <= x1) {
+              const int row = (iz * g.dim[1] + iy) * g.dim[0];
+              beg = g.cell_start[row + x0];
+              cnt = g.cell_start[row + x1 + 1] - beg;
+            }
+          }
+        }
+        const int c_incl = warp_incl_scan(cnt, lane);
+        const int n_c = __shfl_sync(FULL, c_incl, 31);
+        for (int q0 = 0; q0 < n_c; q0 += 32) {
+          // level 3: one lane per candidate receiver
+          const int q = q0 + lane;
+          const int rl = warp_find(c_incl, min(q, n_c - 1));
+          const int rincl = __shfl_sync(FULL, c_incl, rl);
+          const int rcnt = __shfl_sync(FULL, cnt, rl);
+          const int rbeg = __shfl_sync(FULL, beg, rl);
+          const int rci = __shfl_sync(FULL, ci, rl);
+          if (q >= n_c) continue;
+          const int ckn = s_ckn[warp][rci];
+          const int jn = ckn & 0xff, ch = ckn >> 8;
+          const NodeHot& nd = s_nh[warp][jn];
+          const NodeSpan& sp = s_sp[warp][jn];
+          const float a = s_ck[warp][rci].a, b = s_ck[warp][rci].b, mr = s_ck[warp][rci].mr;
+          const RxGrid& g = A.grids[nd.tx];
+          const float3 s = make_float3(nd.s[0], nd.s[1], nd.s[2]);
+          const float3 u = make_float3(nd.u[0], nd.u[1], nd.u[2]);
+          const float4 c4 = g.rx32[rbeg + (q - (rincl - rcnt))];
+          const float3 c = make_float3(c4.x, c4.y, c4.z);
+          const float wx = c.x - s.x, wy = c.y - s.y, wz = c.z - s.z;
+          const float lam = u.x * wx + u.y * wy + u.z * wz;
+          if (ch > 0 && lam < a) continue;                 // owned by an earlier chunk
+          if (ch < sp.nchunk - 1 && lam >= b) continue;    // owned by a later chunk
+          const int gi = __float_as_int(c4.w);
+          ++cand;
+          if (is_root_class(nd.cls)) {
+            if (!A.direct_ok[gi]) continue;
+          } else {
+            // MultiPathCorrection's last step must cross the class's last
+            // triangle: FP32 filter from the image source towards the receiver
+            const float* fl = s_fl[warp][jn];
+            const TriFrom Fl{fl[3], fl[4], fl[5], fl[6], fl[7], fl[8], fl[9], fl[10]};
+            const float3 dd = make_float3(c.x - fl[0], c.y - fl[1], c.z - fl[2]);
+            if (!tri_filter_from(s_tl[warp][jn], Fl, dd,
+                                 sqrt_up(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z)))
+              continue;
+          }
+          const float tanb = A.txp[nd.tx].tan_beta32;
+          const float len = nd.len, S = nd.S;
+          int v;
+          if (lam < a || lam > b) {
+            // outside the chunk's own range: full-margin test
+            v = reception32(s, u, len, S, c, tanb);
+          } else {
+            const float ml = kRecK * (sp.ns + A.gb[nd.tx].cmax + 1.0f);
+            if (lam < -ml) {
+              v = 0;
+            } else if (lam <= ml) {
+              v = -1;
+            } else {
+              const float lcl = fminf(lam, len);
+              const float px = s.x + lcl * u.x, py = s.y + lcl * u.y, pz = s.z + lcl * u.z;
+              const float np = sqrt_up(px * px + py * py + pz * pz);
+              const float ex = c.x - px, ey = c.y - py, ez = c.z - pz;
+              const float d2 = ex * ex + ey * ey + ez * ez;
+              const float rad = (S + np) * tanb;
+              const float rh = rad + mr, rl2 = rad - mr;
+              v = d2 > rh * rh ? 0 : ((rl2 > 0.0f && d2 < rl2 * rl2) ? 1 : -1);
+            }
+          }
+          // the exact reception test, image correction and ancestor
+          // suppression run densely in k_capture_finish
+          if (v == 0) continue;
+          const unsigned long long slot = warp_reserve(&A.ctr->pairs, 1);
+          if (slot < A.pair_cap)
+            A.pairs[slot] =
+                make_uint2(uint32_t(base + jn), uint32_t(gi) | (v < 0 ? 0x80000000u : 0u));
+          else
+            atomicOr(&A.ctr->overflow, kOvPairs);
+        }
+      }
+      __syncwarp();  // the next group of items overwrites s_ck
+    }
+    __syncwarp();  // the next batch overwrites the staged records
+  }
+  for (int o = 16; o; o >>= 1) cand += __shfl_xor_sync(FULL, cand, o);
+  if (lane == 0 && cand) atomicAdd(&A.ctr->cand, cand);
+}
+
 // The FP64 part of capture for the pairs k_capture could not settle in FP32:
 // the exact reception test where the FP32 one was unsure, then image
 // correction (MultiPathCorrection / DirectPathCorrection) and suppression by

@@ -521,7 +521,7 @@ static int trace_grid() {
 
 // Capture grid: every block resident at once (the work counter balances).
 static int capture_grid() {
-  static const int per_sm = blocks_per_sm(k_capture<false>, 32 * kCapWarps);
+  static const int per_sm = blocks_per_sm(k_capture_fast, 32 * kCapWarps);
   return device_sms() * per_sm;
 }
 
@@ -850,7 +850,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       ++nl, k_capture<true><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
       CK(cudaEventRecord(W.cap_ev[1], st));
     } else {
-      ++nl, k_capture<false><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
+      ++nl, k_capture_fast<<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
       CK(cudaEventRecord(W.cap_ev[1], st));
       ++nl, k_capture_finish<<<device_sms() * 16, 128, 0, st>>>(ca);
     }
