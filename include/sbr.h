@@ -299,6 +299,16 @@ sbr_status sbr_write_paths_vtk(const char* path, const sbr_path* paths, int n_pa
  * an icosahedron level as unit segments from `origin` (3 doubles). */
 sbr_status sbr_write_launch_rays_vtk(const char* path, const double* origin, int tessellation);
 
+/* ---- fault injection (tests) ------------------------------------------ */
+/* No counterpart in the reference, which reports no errors from the solve.
+ * Lets a caller's tests see how the library and its server behave when the
+ * device runs out of memory, without exhausting a shared GPU: with after >= 0
+ * the (after+1)-th device allocation the library attempts from now on fails
+ * as cudaMalloc fails on a full device (the call is not made), so the entry
+ * point that needed it returns SBR_ERR_OOM; after < 0 disarms.  The count is
+ * process-wide and covers every thread.  No GPU needed. */
+sbr_status sbr_fault_inject_alloc(long long after);
+
 /* ---- allocation-free field sum -------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory: processes whose device memory is held by another framework's

@@ -28,7 +28,9 @@ class _Req(C.Structure):
                 ("frequency", C.c_double), ("pt", C.c_double), ("use_fresnel", C.c_int),
                 ("tessellation", C.c_int), ("antenna", C.c_int), ("n_rx", C.c_int),
                 ("rx", C.POINTER(C.c_double)), ("n_materials", C.c_int),
-                ("materials", C.POINTER(_Mat))]
+                ("materials", C.POINTER(_Mat)), ("pattern", C.POINTER(C.c_float)),
+                ("pat_nt", C.c_int), ("pat_np", C.c_int), ("pat_dt", C.c_double),
+                ("pat_dp", C.c_double)]
 
 
 class _Path(C.Structure):
@@ -109,9 +111,12 @@ def icosphere(level: int) -> np.ndarray:
     return out.reshape(n, 3)
 
 
-def solve(scene: OracleScene, request, materials: Sequence, threads: int = 0) -> dict:
+def solve(scene: OracleScene, request, materials: Sequence, threads: int = 0,
+          pattern=None) -> dict:
     """request: sbrsolver_gb300.scenes.Request; materials: MaterialProperties
-    tuples.  Returns field (n_rx, 3) complex, counts and paths (receiver-major,
+    tuples; pattern (antenna 3 only): (table, d_theta, d_phi) with table an
+    (n_theta, n_phi, 4) array of g_theta dB, arg_theta deg, g_phi dB, arg_phi
+    deg.  Returns field (n_rx, 3) complex, counts and paths (receiver-major,
     then launch, then BFS order, as the reference enumerates them)."""
     lib = load()
     rx = np.ascontiguousarray(request.rx, np.float64).reshape(-1, 3)
@@ -132,6 +137,11 @@ def solve(scene: OracleScene, request, materials: Sequence, threads: int = 0) ->
     q.rx = rx.ctypes.data_as(C.POINTER(C.c_double))
     q.n_materials = len(materials)
     q.materials = mats
+    if pattern is not None:
+        tab = np.ascontiguousarray(pattern[0], np.float32)
+        q.pattern = tab.ctypes.data_as(C.POINTER(C.c_float))
+        q.pat_nt, q.pat_np = int(tab.shape[0]), int(tab.shape[1])
+        q.pat_dt, q.pat_dp = float(pattern[1]), float(pattern[2])
     h = C.c_void_p()
     rc = lib.oracle_solve(scene.h, C.byref(q), int(threads), C.byref(h))
     if rc:

@@ -652,6 +652,46 @@ C3 pattern(int type, double theta, double pt) {  // FieldCompute.cpp:153-183
   return e;
 }
 
+// Antenna type 3: a tabulated pattern on a regular (theta, phi) grid in
+// degrees, the TXPattern.dat layout (Preprocessor.cpp:3-35,
+// common/DataStructures.h:32-37).  The reference reads such a table but never
+// applies it; this project defines its use: each grid point's complex
+// amplitude 10^(g/20) e^(j arg) is interpolated bilinearly (theta clamped to
+// the grid, phi periodic) and E_theta, E_phi = sqrt(60 Pt) * amplitude, the
+// scaling of the analytic patterns (sqrt(60 Pt G)).  E_r = 0.
+struct Pattern {
+  const float* gp = nullptr;  // nt * np * 4: g_theta, arg_theta, g_phi, arg_phi
+  int nt = 0, np = 0;
+  double dt = 1, dp = 1;
+
+  cd amplitude(int i, int j, int c) const {
+    const float* g = gp + 4 * (size_t(i) * np + j) + 2 * c;
+    const double mag = std::pow(10.0, double(g[0]) / 20.0);
+    const double arg = double(g[1]) * (3.14159265358979323846 / 180.0);
+    return cd(mag * std::cos(arg), mag * std::sin(arg));
+  }
+  C3 field(double theta, double phi, double pt) const {
+    const double deg = 180.0 / kPi;
+    double u = std::min(std::max(theta * deg / dt, 0.0), double(nt - 1));
+    int i0 = nt > 1 ? std::min(int(std::floor(u)), nt - 2) : 0;
+    const int i1 = nt > 1 ? i0 + 1 : 0;
+    const double wu = nt > 1 ? u - i0 : 0.0;
+    double v = phi * deg / dp;
+    v -= std::floor(v / np) * np;  // into [0, np)
+    int j0 = std::min(int(std::floor(v)), np - 1);
+    const int j1 = (j0 + 1) % np;
+    const double wv = v - j0;
+    const double s = std::sqrt(60 * pt);
+    C3 e;
+    for (int c = 0; c < 2; ++c) {
+      const cd a = (1 - wu) * ((1 - wv) * amplitude(i0, j0, c) + wv * amplitude(i0, j1, c)) +
+                   wu * ((1 - wv) * amplitude(i1, j0, c) + wv * amplitude(i1, j1, c));
+      e.v[1 + c] = s * a;
+    }
+    return e;
+  }
+};
+
 struct FieldCtx {
   const Scene* s;
   const std::vector<MaterialProperties_c>* mats;
@@ -659,6 +699,7 @@ struct FieldCtx {
   double freq, pt;
   bool fresnel;
   int antenna;
+  Pattern pat;
 };
 
 // FieldCompute.cpp:71-151; triangle frames are looked up by position in the
@@ -681,7 +722,7 @@ C3 field_for_path(const FieldCtx& c, const std::vector<PathRay>& path) {
     if (r.tri == -1) next = glob;
     else next = c.s->tris[c.s->mesh_order[r.tri]].cs;
     if (i == 0) {
-      inc = pattern(c.antenna, th, c.pt);
+      inc = c.antenna == 3 ? c.pat.field(th, ph, c.pt) : pattern(c.antenna, th, c.pt);
     } else {
       inc = mul(mul(glob, transpose(cur)), tot);
       inc = mul(transpose(transformation(th, ph)), inc);
@@ -783,7 +824,14 @@ struct Solver {
   void receiver(int k, RxOut& o) const {
     const V3 c = rx[k];
     const V3 tx(rq.tx[0], rq.tx[1], rq.tx[2]);
-    FieldCtx fc{&s, &mats, M3(), rq.frequency, rq.pt, rq.use_fresnel != 0, rq.antenna};
+    FieldCtx fc{&s, &mats, M3(), rq.frequency, rq.pt, rq.use_fresnel != 0, rq.antenna, Pattern()};
+    if (rq.antenna == 3) {
+      fc.pat.gp = rq.pattern;
+      fc.pat.nt = rq.pat_nt;
+      fc.pat.np = rq.pat_np;
+      fc.pat.dt = rq.pat_dt;
+      fc.pat.dp = rq.pat_dp;
+    }
     for (int i = 0; i < 9; ++i) fc.txcs.m[i] = rq.tx_coord_sys[i];
     std::map<std::vector<int>, int> seen;
     std::vector<int> caps, parent;
@@ -961,6 +1009,9 @@ int oracle_icosphere(int level, double* out, long cap) {
 
 int oracle_solve(const oracle_scene* sc, const oracle_request* rq, int threads,
                  oracle_result** out) {
+  if (rq->antenna == 3 && (!rq->pattern || rq->pat_nt < 1 || rq->pat_np < 1 ||
+                           !(rq->pat_dt > 0) || !(rq->pat_dp > 0)))
+    return 2;
   orc::Solver sv(sc->s, *rq);
   sv.threads = threads > 0 ? unsigned(threads) : std::max(1u, std::thread::hardware_concurrency());
   for (int i = 0; i < rq->n_materials; ++i) sv.mats.push_back(rq->materials[i]);

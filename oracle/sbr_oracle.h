@@ -29,6 +29,13 @@ typedef struct {
   const double* rx; /* 3 per receiver */
   int n_materials;
   const MaterialProperties_c* materials;
+  /* antenna 3 (tabulated): the TXPattern.dat grid (data/TXPattern.dat, read
+   * by Preprocessor::ReadPatternFile, Preprocessor.cpp:3-35) as
+   * pat_nt x pat_np rows of (g_theta dB, arg_theta deg, g_phi dB, arg_phi deg),
+   * theta-major, steps pat_dt / pat_dp degrees from theta = phi = 0. */
+  const float* pattern;
+  int pat_nt, pat_np;
+  double pat_dt, pat_dp;
 } oracle_request;
 
 typedef struct {

@@ -25,7 +25,7 @@ EXPORTS = (
     "sbr_write_field_csv", "sbr_write_receivers_vtk", "sbr_write_paths_vtk",
     "sbr_write_launch_rays_vtk", "sbr_scene_set_materials", "sbr_stl_read",
     "sbr_generate_rx_line", "sbr_generate_rx_plane", "sbr_pattern_create", "sbr_pattern_read",
-    "sbr_pattern_info", "sbr_pattern_destroy",
+    "sbr_pattern_info", "sbr_pattern_destroy", "sbr_fault_inject_alloc",
 )
 
 
@@ -139,6 +139,7 @@ def load(path: str = LIB_PATH):
             "sbr_pattern_read": [C.c_char_p, P(vp)],
             "sbr_pattern_info": [vp, P(I), P(I), P(D), P(D)],
             "sbr_pattern_destroy": [vp],
+            "sbr_fault_inject_alloc": [C.c_longlong],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

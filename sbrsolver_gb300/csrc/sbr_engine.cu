@@ -62,6 +62,20 @@ struct CudaError {
     if (_e != cudaSuccess) throw CudaError{_e, std::string(#x)};          \
   } while (0)
 
+// ------------------------------------------------------------ fault injection
+// Host-side fault injection for tests (sbr_fault_inject_alloc): when armed
+// with n >= 0, the (n+1)-th device allocation the library attempts fails as
+// cudaMalloc fails on an exhausted device, without calling it.  -1 = off.
+static std::atomic<long long> g_alloc_fault{-1};
+
+static bool injected_alloc_failure() {
+  long long v = g_alloc_fault.load(std::memory_order_relaxed);
+  while (v >= 0) {
+    if (g_alloc_fault.compare_exchange_weak(v, v - 1, std::memory_order_relaxed)) return v == 0;
+  }
+  return false;
+}
+
 // ------------------------------------------------------------ device buffer
 template <class T>
 struct DBuf {
@@ -78,7 +92,8 @@ struct DBuf {
     release();
     if (want == 0) return;
     void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, want * sizeof(T));
+    cudaError_t e = injected_alloc_failure() ? cudaErrorMemoryAllocation
+                                             : cudaMalloc(&q, want * sizeof(T));
     if (e != cudaSuccess) {
       cudaGetLastError();
       throw CudaError{e, "cudaMalloc " + std::to_string(want * sizeof(T)) + " bytes"};
@@ -113,6 +128,7 @@ struct Workspace {
   DBuf<TxParams> txp;
   DBuf<double> rx;
   DBuf<int> rx_req;
+  DBuf<int> rx_bad;  // set when a device-resident receiver has a non-finite coordinate
   DBuf<GridBuild> gb;
   DBuf<RxGrid> grids;
   DBuf<int> cell_base, cell_counts, cell_starts, cell_cursor;
@@ -572,7 +588,19 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         q.max_reflection + q.max_transmission > kMaxDepth)
       throw std::string("max_reflection + max_transmission must be 0..16");
     if (q.tessellation < 0 || q.tessellation > 12) throw std::string("tessellation must be 0..12");
-    if (!(q.frequency > 0)) throw std::string("frequency must be > 0");
+    if (!(q.frequency > 0) || !std::isfinite(q.frequency))
+      throw std::string("frequency must be finite and > 0");
+    if (!std::isfinite(q.pt)) throw std::string("pt must be finite");
+    for (int a = 0; a < 3; ++a)
+      if (!std::isfinite(q.tx[a])) throw std::string("transmitter coordinates must be finite");
+    for (int a = 0; a < 9; ++a)
+      if (!std::isfinite(q.tx_coord_sys[a]))
+        throw std::string("tx_coord_sys entries must be finite");
+    if (q.n_rx > 0 && !q.rx_on_device)
+      for (size_t i = 0; i < 3 * size_t(q.n_rx); ++i)
+        if (!std::isfinite(q.rx[i]))
+          throw std::string("receiver coordinates must be finite (receiver ") +
+              std::to_string(i / 3) + " of request " + std::to_string(r) + ")";
     if (q.antenna < 0 || q.antenna > 3) throw std::string("antenna must be 0, 1, 2 or 3");
     if (q.antenna == SBR_ANTENNA_TABULATED && !q.pattern)
       throw std::string("antenna 3 (tabulated) needs a pattern");
@@ -662,7 +690,9 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
   int max_rx = 1;
   for (auto& p : tp) max_rx = std::max(max_rx, p.n_rx);
   dim3 rg(std::min(1024, (max_rx + 255) / 256), n_req);
-  ++nl, k_rx_bounds<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.gb.p);
+  W.rx_bad.ensure(1);
+  CK(cudaMemsetAsync(W.rx_bad.p, 0, sizeof(int), st));
+  ++nl, k_rx_bounds<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.gb.p, W.rx_bad.p);
   ++nl, k_grid_shape<<<1, 1, 0, st>>>(W.gb.p, W.grids.p, W.txp.p, n_req, max_cells, W.cell_base.p);
   ++nl, k_rx_count<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p, W.cell_counts.p);
   ++nl, k_scan_exclusive<<<1, 1024, 0, st>>>(W.cell_counts.p, W.cell_starts.p, int(cell_cap));
@@ -866,8 +896,11 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[5], st));
     Counters c;
+    int rx_bad = 0;
     CK(cudaMemcpyAsync(&c, W.ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&rx_bad, W.rx_bad.p, sizeof rx_bad, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (rx_bad) throw std::string("receiver coordinates must be finite");
     if (c.overflow & kOvStack) throw std::string("BVH deeper than the traversal stack");
     // keep every hash table at most half full for the next solve
     auto grow = [](uint32_t& cap, unsigned long long used) {
@@ -1170,6 +1203,11 @@ using namespace sbr;
 extern "C" {
 
 const char* sbr_last_error(void) { return g_err.c_str(); }
+
+sbr_status sbr_fault_inject_alloc(long long after) {
+  g_alloc_fault.store(after < 0 ? -1 : after, std::memory_order_relaxed);
+  return SBR_OK;
+}
 const char* sbr_version(void) { return "sbr-gb300 0.1 (sm_103a)"; }
 
 // Wall thicknesses must be finite and non-negative; empty string when valid.
@@ -1189,6 +1227,13 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
     if (!material_error(materials, n_materials).empty())
       throw material_error(materials, n_materials);
     const int nt = int(n.size() / 3);
+    for (size_t i = 0; i < v.size(); ++i)
+      if (!std::isfinite(v[i]))
+        throw std::string("vertex coordinates must be finite (triangle ") +
+            std::to_string(i / 9) + ")";
+    for (size_t i = 0; i < n.size(); ++i)
+      if (!std::isfinite(n[i]))
+        throw std::string("facet normals must be finite (triangle ") + std::to_string(i / 3) + ")";
     if (mat_ids)
       for (int i = 0; i < nt; ++i)
         if (mat_ids[i] < 0 || mat_ids[i] >= n_materials)

@@ -31,13 +31,22 @@ struct GridBuild {
   int ncell;
 };
 
-__global__ void k_rx_bounds(const double* rx, const TxParams* txp, int n_tx, GridBuild* gb) {
+// Bounds of each request's receivers.  A receiver with a non-finite
+// coordinate (possible only for receivers the caller placed on the device;
+// host receivers are checked before upload) sets *bad and is left out of the
+// bounds; the solve then fails with an argument error.
+__global__ void k_rx_bounds(const double* rx, const TxParams* txp, int n_tx, GridBuild* gb,
+                            int* bad) {
   const int r = blockIdx.y;  // request
   if (r >= n_tx) return;
   const TxParams& P = txp[r];
   int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN}, cm = INT_MIN;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_rx; i += gridDim.x * blockDim.x) {
     const double* c = rx + 3 * size_t(P.rx_first + i);
+    if (!(isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2]))) {
+      atomicOr(bad, 1);
+      continue;
+    }
     float c32[3] = {float(c[0]), float(c[1]), float(c[2])};
     for (int a = 0; a < 3; ++a) {
       mn[a] = min(mn[a], f2o(c32[a]));

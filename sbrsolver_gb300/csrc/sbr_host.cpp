@@ -196,6 +196,16 @@ bool read_stl(const std::string& path, std::vector<float>& v, std::vector<float>
       err = "truncated binary STL header in " + path;
       return false;
     }
+    // the header's facet count must fit the file (84-byte header, 50 bytes
+    // per facet) before any storage is sized from it
+    in.seekg(0, std::ios::end);
+    const unsigned long long size = (unsigned long long)(std::streamoff)in.tellg();
+    in.seekg(84);
+    if (size < 84ull + 50ull * cnt) {
+      err = "truncated binary STL in " + path + ": header counts " + std::to_string(cnt) +
+            " facets, the file holds " + std::to_string((size - 84) / 50);
+      return false;
+    }
     v.resize(size_t(cnt) * 9);
     n.resize(size_t(cnt) * 3);
     for (uint32_t t = 0; t < cnt; ++t) {

@@ -165,3 +165,57 @@ def test_fast_capture_equals_plain_capture_at_scale(built, which):
     assert api.same_path_set(fast.paths, plain.paths)
     np.testing.assert_array_equal(fast.field, plain.field)
     sc.close()
+
+
+def _bary_edge_distance(tri, p):
+    """min(u, v, 1-u-v) of point p on triangle tri (3x3), the barycentric
+    distance from the triangle's nearest edge (as sbr_path.near_edge uses)."""
+    v1 = tri[0].astype(np.float64)
+    e1, e2 = tri[1].astype(np.float64) - v1, tri[2].astype(np.float64) - v1
+    w = np.asarray(p, np.float64) - v1
+    d00, d01, d11 = e1 @ e1, e1 @ e2, e2 @ e2
+    d20, d21 = w @ e1, w @ e2
+    den = d00 * d11 - d01 * d01
+    u = (d11 * d20 - d01 * d21) / den
+    v = (d00 * d21 - d01 * d20) / den
+    return min(u, v, 1.0 - u - v)
+
+
+def test_near_edge_paths_listed(built):
+    """Paths with an interaction point within 1e-6 (barycentric) of a
+    triangle edge are listed separately (sbr_path.near_edge).  The ground's
+    two triangles share the diagonal y = x; the transmitter stands over it
+    and each receiver is placed so that its ground reflection lands 0, 1e-4,
+    1e-3 and 1 m off the diagonal (barycentric 0, 5e-7, 5e-6, 5e-3).  The
+    path set equals the oracle's, and each flag equals the one computed on
+    the CPU from the oracle's corrected points."""
+    mb = scenes._MeshBuilder()
+    scenes._ground(mb, 100.0, 0)
+    scene = mb.build("diagonal", [(2.4e9, 0.0, 0.0, 15.0, 0.0, 0.005)])
+    ht, hr = 10.0, 1.5
+    frac = ht / (ht + hr)  # where the specular point splits the Tx -> Rx projection
+    offsets = [0.0, 1e-4, 1e-3, 1.0]
+    rx = np.array([(30.0 + 7 * k, 30.0 + 7 * k + off / frac, hr) for k, off in enumerate(offsets)])
+    req = scenes.Request(tx=(-20.0, -20.0, ht), rx=rx, max_reflection=1, max_transmission=0,
+                         frequency=2.4e9, tessellation=6, antenna=2)
+    wl = scenes.Workload("diagonal", scene, req)
+    ref = _oracle(wl)
+    sc = api.DeviceScene.from_scene(scene)
+    res = api.solve(sc, api.request_from_workload(req))
+    order = sc.mesh_order()
+    sc.close()
+    assert path_keys(res.paths) == path_keys(ref["paths"])
+    expect, seen = [], {}
+    for p in ref["paths"]:
+        flag = 0
+        for r in range(p["n_rays"] - 1):
+            d = _bary_edge_distance(scene.tri[order[p["tri"][r]]], p["points"][r][3:6])
+            flag |= int(d < 1e-6)
+            seen[p["receiver"]] = d
+        expect.append(flag)
+    got = [int(p["near_edge"]) for p in res.paths]
+    assert got == expect
+    # every receiver has its ground reflection, at the planned distances
+    assert sorted(seen) == [0, 1, 2, 3]
+    assert seen[0] < 1e-12 and 4e-7 < seen[1] < 6e-7 and 4e-6 < seen[2] < 6e-6 and seen[3] > 1e-3
+    assert got.count(1) == 2 and res.counts["near_edge_paths"] == 2

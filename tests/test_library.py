@@ -110,3 +110,54 @@ def test_no_gpu_fails_loudly(built):
     with pytest.raises(_lib.SbrError) as e:
         api.DeviceScene.from_scene(wl.scene)
     assert e.value.status in (_lib.ERR_CUDA, _lib.ERR_OOM)
+
+
+def test_truncated_stl_is_io_error(built, tmp_path):
+    """A binary STL cut short, or one whose header counts more facets than
+    the file holds, is refused before any storage is sized from the count."""
+    lib = _lib.load()
+    wl = scenes.small_scene()
+    whole = tmp_path / "whole.stl"
+    scenes.write_stl(wl.scene, str(whole))
+    data = whole.read_bytes()
+    n = C.c_int()
+    assert lib.sbr_stl_read(str(whole).encode(), C.byref(n), None, None) == _lib.OK
+    assert n.value == wl.scene.n_tri
+    cut = tmp_path / "cut.stl"
+    cut.write_bytes(data[: 84 + 50 * 7 + 20])  # 7 whole facets and part of the 8th
+    assert lib.sbr_stl_read(str(cut).encode(), C.byref(n), None, None) == _lib.ERR_IO
+    assert b"truncated" in lib.sbr_last_error()
+    huge = tmp_path / "huge.stl"  # header claims 2^32 - 1 facets
+    huge.write_bytes(data[:80] + (0xFFFFFFFF).to_bytes(4, "little") + data[84:84 + 500])
+    assert lib.sbr_stl_read(str(huge).encode(), C.byref(n), None, None) == _lib.ERR_IO
+    assert b"4294967295" in lib.sbr_last_error()
+    head = tmp_path / "head.stl"
+    head.write_bytes(data[:60])
+    assert lib.sbr_stl_read(str(head).encode(), C.byref(n), None, None) == _lib.ERR_IO
+    out = C.c_void_p()
+    m = (_lib.Material * 1)(_lib.Material(1e9, 0, 0, 5, 0, 0.1))
+    assert lib.sbr_scene_create_from_stl(str(cut).encode(), None, m, 1, C.byref(out)) == _lib.ERR_IO
+    assert not out.value
+
+
+@pytest.mark.parametrize("where", ["vertex", "normal"])
+def test_non_finite_scene_rejected(built, where):
+    """NaN / inf in the triangle list is an argument error, found before any
+    device work."""
+    wl = scenes.small_scene()
+    tri, nrm = wl.scene.tri.copy(), wl.scene.normal.copy()
+    if where == "vertex":
+        tri[5, 1, 2] = np.nan
+    else:
+        nrm[9, 0] = np.inf
+    with pytest.raises(_lib.SbrError) as e:
+        api.DeviceScene(api.Mesh(tri, nrm, wl.scene.material_id),
+                        [api.MaterialProperties(*m) for m in wl.scene.materials])
+    assert e.value.status == _lib.ERR_INVALID_ARG
+    assert "finite" in str(e.value)
+
+
+def test_fault_hook_arms_and_disarms(built):
+    lib = _lib.load()
+    assert lib.sbr_fault_inject_alloc(3) == _lib.OK
+    assert lib.sbr_fault_inject_alloc(-1) == _lib.OK
