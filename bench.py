@@ -34,9 +34,10 @@ NODE_BYTES = 96      # NodeRec
 RAY_BYTES = 96       # RayRec
 SEGMENT_BYTES = 84   # algorithmic bytes per executed segment (trace)
 EVENT_BYTES = 16     # per capture event (group-table rank + count update)
-# DRAM bytes (read + write) per segment of the level-9 urban solve, measured
-# with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass, timed solve)
-TRAFFIC_PER_SEGMENT = {"k_capture": 2186.0e6 / 29924326, "k_trace": 11016.0e6 / 29924326}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of k_trace's
+# first launch of the level-9 urban solve (its 2,621,442 launch rays), from
+# one ncu capture of that launch alone: profiles/k_trace_urban_L9_first_launch.md
+TRACE_FIRST_LAUNCH_DRAM_BYTES = None
 
 
 def _env_int(k, d):
@@ -62,7 +63,7 @@ class Clocks:
         try:
             self.f = tempfile.TemporaryFile("w+")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -164,49 +165,81 @@ def serving_stream(scene_wls, n: int, seed: int = 0x5B5 + 4):
     return out
 
 
-def run_batched(precision: str):
+def run_batched(precision: str, best_rate: float = 0.0):
     """256 transmitters as one batched call against 256 plain calls, overall
-    and per icosahedron level (each level's requests batched on their own)."""
+    and per icosahedron level (each level's requests batched on their own).
+
+    The batch's launch shapes come from the library's autotuner (run first,
+    untimed).  Both paths are reported in wall-clock time through the C ABI
+    and in device time (sbr_timing.device_ms).  The Amdahl ceiling is the
+    speed-up the batch would show if every one of its segments ran at the
+    best segment rate measured on this scene in this run (`best_rate`, the
+    fastest of the batched solves and the single level-9 benchmark solve):
+    plain time / (segments / best rate)."""
     from sbrsolver_gb300 import api
     wl, reqs = batched_workload()
     sc = api.DeviceScene.from_scene(wl.scene)
     qs = [api.request_from_workload(r, precision) for r in reqs]
     api.solve(sc, qs, with_paths=False)  # warm-up: sizes the buffers for the batch
-    t_req, seg_req = [], []
+    t0 = time.perf_counter()
+    tuned = sc.autotune(qs, rounds=1)
+    tune_s = time.perf_counter() - t0
+    t_req, d_req, seg_req = [], [], []
     t0 = time.perf_counter()
     for q in qs:
         t1 = time.perf_counter()
-        seg_req.append(api.solve(sc, q, with_paths=False).counts["segments"])
+        r = api.solve(sc, q, with_paths=False)
         t_req.append(time.perf_counter() - t1)
+        d_req.append(r.timing["device_ms"] / 1e3)
+        seg_req.append(r.counts["segments"])
     t_plain = time.perf_counter() - t0
     seg_plain = sum(seg_req)
     t0 = time.perf_counter()
     rb = api.solve(sc, qs, with_paths=False)
     t_batch = time.perf_counter() - t0
+    d_batch = rb.timing["device_ms"] / 1e3
     by_level = {}
+    rates = [rb.counts["segments"] / d_batch, best_rate]
     for lvl in sorted({r.tessellation for r in reqs}):
         idx = [i for i, r in enumerate(reqs) if r.tessellation == lvl]
         sub = [qs[i] for i in idx]
+        api.solve(sc, sub, with_paths=False)  # sizes the workspace for this sub-batch
         t0 = time.perf_counter()
         rs = api.solve(sc, sub, with_paths=False)
         tb = time.perf_counter() - t0
+        db = rs.timing["device_ms"] / 1e3
+        rates.append(rs.counts["segments"] / db)
         tp = sum(t_req[i] for i in idx)
+        dp = sum(d_req[i] for i in idx)
+        seg = sum(seg_req[i] for i in idx)
         by_level[str(lvl)] = {"requests": len(idx), "segments": rs.counts["segments"],
-                              "plain": sum(seg_req[i] for i in idx) / tp,
-                              "batched": rs.counts["segments"] / tb,
-                              "speedup": (rs.counts["segments"] / tb) /
-                                         (sum(seg_req[i] for i in idx) / tp)}
+                              "segment_share": seg / seg_plain,
+                              "plain_time_share": tp / t_plain,
+                              "plain": seg / tp, "batched": rs.counts["segments"] / tb,
+                              "speedup": (rs.counts["segments"] / tb) / (seg / tp),
+                              "plain_device": seg / dp, "batched_device": rs.counts["segments"] / db,
+                              "speedup_device": (rs.counts["segments"] / db) / (seg / dp)}
     err = None
     if precision != "fp64":  # untimed: the batch's field error against FP64
         qc = [api.request_from_workload(r, precision, field_check=True) for r in reqs]
         rc = api.solve(sc, qc, with_paths=False)
         err = api.field_error_stats(rc.field, rc.field_fp64)
     sc.close()
+    best = max(rates)
+    d_plain = sum(d_req)
     return {"workload": "urban 256 Tx, levels 6-9, R5, 4096 shared receivers",
             "requests": len(qs), "segments": rb.counts["segments"],
             "batched": rb.counts["segments"] / t_batch, "plain": seg_plain / t_plain,
             "unit": "segments/s", "batched_s": t_batch, "plain_s": t_plain,
             "speedup": (rb.counts["segments"] / t_batch) / (seg_plain / t_plain),
+            "batched_device_s": d_batch, "plain_device_s": d_plain,
+            "speedup_device": (rb.counts["segments"] / d_batch) / (seg_plain / d_plain),
+            "ceiling": {"best_rate": best,
+                        "speedup": t_plain / (seg_plain / best),
+                        "speedup_device": d_plain / (seg_plain / best),
+                        "rule": "plain time / (segments / best segment rate measured on "
+                                "this scene in this run)"},
+            "autotuned": dict(tuned, tuning_s=tune_s),
             "by_level": by_level, "field_precision": precision,
             "field_error_vs_fp64": err}
 
@@ -369,7 +402,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "fp32_phase"])
@@ -379,6 +412,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--tuning", default="",
+                    help="launch shapes of the benchmark scene, e.g. trace_kernel=2,find_steps=16 "
+                         "(sbr_tuning field names; default: the library's)")
     args = ap.parse_args()
     rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
     dist = None
@@ -404,6 +440,8 @@ def main():
     t_scene = time.perf_counter()
     scene = api.DeviceScene.from_scene(wl.scene)
     scene_ms = 1e3 * (time.perf_counter() - t_scene)
+    if args.tuning:
+        scene.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tuning.split(","))})
     rx_dev = torch.tensor(wl.request.rx, dtype=torch.float64, device=f"cuda:{local}")
     torch.cuda.synchronize()
     q_dev, _keep = api.request_from_workload(wl.request, args.precision)
@@ -428,7 +466,8 @@ def main():
     torch.cuda.synchronize()
     dev_ms, seg, stage = [], [], {"trace_ms": 0.0, "capture_ms": 0.0, "correct_ms": 0.0,
                                  "field_ms": 0.0, "capture_kernel_ms": 0.0,
-                                 "trace_kernel_ms": 0.0, "trace_kernel_launches": 0.0}
+                                 "trace_kernel_ms": 0.0, "trace_kernel_launches": 0.0,
+                                 "trace_kernel_first_ms": 0.0}
     counts = None
     with Clocks(local) as ck:
         # NVTX range "timed": lets a profiler select exactly these solves
@@ -465,17 +504,16 @@ def main():
         n_nodes = counts["segments"]
         cap_ms = stage["capture_kernel_ms"] / steps  # the capture kernel alone
         tr_ms = stage["trace_kernel_ms"] / steps      # k_trace alone, all its launches
-        tr_launches = max(1.0, stage["trace_kernel_launches"] / steps)
         if cap_ms >= tr_ms:  # the kernel with the larger total time
-            kern, ms = "k_capture", cap_ms
+            kern, ms, launch = "k_capture_fast", cap_ms, "the one launch per solve"
             alg = n_nodes * NODE_BYTES + captured * EVENT_BYTES
-            traffic = TRAFFIC_PER_SEGMENT["k_capture"] * n_nodes
+            traffic = None
         else:
-            kern, ms = "k_trace", tr_ms / tr_launches
-            alg = n_nodes * SEGMENT_BYTES / tr_launches
-            traffic = TRAFFIC_PER_SEGMENT["k_trace"] * n_nodes / tr_launches
-        if wl.name != "urban_L9_R6T1":
-            traffic = None  # measured for the level-9 workload only
+            # k_trace's first launch: the launch rays, one segment each
+            kern, ms = "k_trace", stage["trace_kernel_first_ms"] / steps
+            launch = f"first launch ({counts['launches']} launch rays)"
+            alg = counts["launches"] * SEGMENT_BYTES
+            traffic = TRACE_FIRST_LAUNCH_DRAM_BYTES if wl.name == "urban_L9_R6T1" else None
         achieved = alg / (ms / 1e3) / 1e9
         launches_per_step = counts["gpu_kernels"]  # counted by the library
         line = {
@@ -489,6 +527,7 @@ def main():
                        "max_transmission": wl.request.max_transmission,
                        "field_precision": args.precision,
                        "parallelism": f"replicas{world}",
+                       "launch_shapes": scene.tuning(req_host),
                        "l2": "working set (node pool) larger than L2 each step"},
             "counts": dict(counts, captured=captured),
             "scene_create_ms": scene_ms,
@@ -499,16 +538,18 @@ def main():
             "e2e": {"value": tot_e2e / max_e2e, "unit": "segments/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * max_e2e / steps},
-            "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": kern, "launch": launch,
+                         "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg,
                          "traffic_frac": (traffic / (ms / 1e3) / 1e9 / peak) if traffic else None,
-                         "launch_ms": ms},
+                         "launch_ms": ms,
+                         "kernel_ms_per_step": {"k_trace": tr_ms, "k_capture_fast": cap_ms}},
             "gpu_launches": launches_per_step * steps,
             "clocks": clocks,
         }
         if not args.no_batched and args.level == 9:
-            line["batched"] = run_batched(args.precision)
+            line["batched"] = run_batched(args.precision, best_rate=tot_seg / max_t)
         if not args.no_serving and args.level == 9:
             line["serving"] = run_serving(args.precision)
         if not args.no_precision and args.level == 9:

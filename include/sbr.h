@@ -119,6 +119,10 @@ typedef struct sbr_counts {
   long long near_edge_paths;    /* surviving paths with an interaction point within 1e-6
                                    (barycentric) of its triangle's edge */
   long long gpu_kernels;        /* kernel launches of the solve (a batch's, for its parts) */
+  long long fp64_field_paths;   /* SBR_FIELD_FP32: paths whose field was taken in FP64 (an
+                                   ill-conditioned path, or one of an uncertified receiver) */
+  long long fp64_field_receivers; /* SBR_FIELD_FP32: receivers whose error bound could not
+                                     certify the tolerance, recomputed and summed in FP64 */
 } sbr_counts;
 
 /* One surviving path; its rays are [ray_offset, ray_offset + n_rays) in the
@@ -149,10 +153,12 @@ typedef struct sbr_field_error {
  * correction, field) and before results are copied back; capture_kernel_ms
  * is the capture kernel alone (inside capture_ms), trace_kernel_ms the
  * FP64 resolution-and-spawn kernel alone over its trace_kernel_launches
- * launches (inside trace_ms, which also holds the FP32 candidate search). */
+ * launches (inside trace_ms, which also holds the FP32 candidate search),
+ * trace_kernel_first_ms its first launch alone (the launch rays: one
+ * segment per launch direction of every request). */
 typedef struct sbr_timing {
   double total_ms, trace_ms, capture_ms, correct_ms, field_ms, h2d_ms, d2h_ms, device_ms;
-  double capture_kernel_ms, trace_kernel_ms, trace_kernel_launches;
+  double capture_kernel_ms, trace_kernel_ms, trace_kernel_launches, trace_kernel_first_ms;
 } sbr_timing;
 
 /* ---- scene ---------------------------------------------------------- */
@@ -161,6 +167,27 @@ typedef struct sbr_timing {
 sbr_status sbr_scene_create(int n_triangles, const float* vertices, const float* normals,
                             const int* material_ids, const sbr_material* materials,
                             int n_materials, sbr_scene** out);
+/* As sbr_scene_create, with flags.  By default the GPU builds the coplanar
+ * groups (Preprocessor.cpp:116-246), the triangle frames and boxes
+ * (Triangle.cpp:37-70) and the search BVH, while the host builds the
+ * reference BVH (BVH.h:135-230, whose tie order only the host's std::sort
+ * reproduces); SBR_SCENE_HOST_PREP builds everything on the host.  Both give
+ * identical tables. */
+#define SBR_SCENE_HOST_PREP 1u
+sbr_status sbr_scene_create_ex(int n_triangles, const float* vertices, const float* normals,
+                               const int* material_ids, const sbr_material* materials,
+                               int n_materials, unsigned flags, sbr_scene** out);
+/* The scene's prepared tables, by triangle id (file order): frame rows
+ * (9 doubles: x, y, z rows), box (6: min xyz, max xyz), box centre (3);
+ * any pointer may be NULL. */
+sbr_status sbr_scene_triangle_frames(const sbr_scene* scene, double* frames, double* boxes,
+                                     double* centers);
+/* The search BVH: *n_nodes in: capacity of nodes (14 4-byte words per node:
+ * lo[2][3], hi[2][3] floats, child[2] ints, a child < 0 being the leaf
+ * ~(first << 3 | count)), out: node count; order: the depth-first rank of
+ * each leaf slot (as many as triangles).  NULL nodes/order: sizes only. */
+sbr_status sbr_scene_search_bvh(const sbr_scene* scene, int* n_nodes, int* max_depth,
+                                float* nodes, int* order);
 sbr_status sbr_scene_create_from_stl(const char* path, const int* material_ids,
                                      const sbr_material* materials, int n_materials,
                                      sbr_scene** out);
@@ -197,6 +224,18 @@ sbr_status sbr_result_counts(const sbr_result* result, sbr_counts* out);
 /* 6 doubles per receiver (Ex re, Ex im, Ey re, Ey im, Ez re, Ez im), requests
  * concatenated in order. */
 sbr_status sbr_result_field(const sbr_result* result, double* out);
+/* Per receiver, a bound on the absolute error of each of its three complex
+ * field components (n_rx doubles).  SBR_FIELD_FP32 requests: every path's
+ * FP32 error is bounded by (16 kappa + 1) FP32 ulps of its field, kappa its
+ * condition number (largest field it could carry over the field it ends
+ * with; paths with kappa > 32 or a Fresnel coefficient near a pole of its
+ * formula are computed in FP64); a receiver's bound is the sum over its
+ * paths plus 2 ulps of the summed field.  A receiver whose bound exceeds half
+ * the tolerance (1e-4 relative magnitude) of a component is recomputed and
+ * summed in FP64 (bound 0), so every FP32 component meets 1e-4 / 1e-3 rad.
+ * 0 for SBR_FIELD_FP64 (the reference's arithmetic), -1 for
+ * SBR_FIELD_FP32_PHASE (no bound: a study mode). */
+sbr_status sbr_result_field_bound(const sbr_result* result, double* out);
 /* Field error of an FP32-precision result against FP64 (request field_check);
  * SBR_ERR_NOT_READY when the result carries no FP64 field. */
 sbr_status sbr_result_field_error(const sbr_result* result, sbr_field_error* out);
@@ -299,6 +338,38 @@ sbr_status sbr_write_paths_vtk(const char* path, const sbr_path* paths, int n_pa
  * an icosahedron level as unit segments from `origin` (3 doubles). */
 sbr_status sbr_write_launch_rays_vtk(const char* path, const double* origin, int tessellation);
 
+/* ---- launch shapes and the autotuner ------------------------------------ */
+/* No counterpart in the reference, whose solve is one single-threaded CPU
+ * loop (RTSolver.cpp:82-121).  The launch shapes of the trace and capture
+ * kernels; 0 in a field means the library's default. */
+typedef struct sbr_tuning {
+  int find_steps;            /* FP32 search: traversal steps between refills (32) */
+  int find_refill;           /* FP32 search: idle lanes that trigger a warp's refill, <= 32 (16) */
+  int find_blocks_per_sm;    /* FP32 search: resident 128-thread blocks per SM (all that fit) */
+  int trace_blocks_per_sm;   /* FP64 resolution: resident 128-thread blocks per SM (all that fit) */
+  int capture_blocks_per_sm; /* capture: resident blocks per SM (all that fit) */
+  int trace_chunk_log2;      /* rays per search/resolution launch pair = 2^this, 16..26 (24) */
+  int trace_kernel;          /* FP64 resolution: 1 = one ray per lane (registers), 2 = 64 rays
+                                per warp in shared memory, tests handed out to full warps */
+} sbr_tuning;
+/* The scene's default shapes, used by request mixes sbr_autotune has not
+ * tuned.  Values above what fits on an SM are clamped. */
+sbr_status sbr_scene_set_tuning(sbr_scene* scene, const sbr_tuning* tuning);
+/* The shapes a solve of this request mix would use, defaults filled in
+ * (requests may be NULL with n_requests 0: the scene's default). */
+sbr_status sbr_scene_get_tuning(sbr_scene* scene, const sbr_request* requests, int n_requests,
+                                sbr_tuning* out);
+/* Autotuner: solves the batch repeatedly, changing one shape at a time over
+ * its candidates and keeping a change that cuts the batch's device time
+ * (sbr_timing.device_ms, the better of two solves) by at least 1 %, for up
+ * to `rounds` passes over the shapes (1..8).  The choice is kept for this
+ * request mix (its requests' levels and bounce limits) and used by every
+ * later solve of the same mix on this scene; out / best_ms (may be NULL)
+ * receive it and its device time.  Other solves on the same scene while it
+ * runs see the candidate shapes. */
+sbr_status sbr_autotune(sbr_scene* scene, const sbr_request* requests, int n_requests, int rounds,
+                        sbr_tuning* out, double* best_ms);
+
 /* ---- fault injection (tests) ------------------------------------------ */
 /* No counterpart in the reference, which reports no errors from the solve.
  * Lets a caller's tests see how the library and its server behave when the
@@ -317,8 +388,9 @@ sbr_status sbr_fault_inject_alloc(long long after);
  * (which may synchronise the device).  Sums per-path fields into
  * per-receiver fields in each receiver's (launch, BFS) rank order, with the
  * arithmetic sbr_solve's own sum uses (FP64 for SBR_FIELD_FP64, compensated
- * FP32 for both FP32 precisions; paths of equal rank are added in path-index
- * order), using only a fixed 4 MiB array compiled into the library (held on
+ * FP32 for both FP32 precisions, where sbr_solve itself switches to FP64 for
+ * the receivers its FP32 error bound cannot certify; paths of equal rank are
+ * added in path-index order), using only a fixed 4 MiB array compiled into the library (held on
  * every GPU that loads it until exit).  All pointers are device pointers
  * owned by the caller: path_receiver[n_paths] (0-based), path_rank[n_paths]
  * (launch << 17 | heap, see sbr_path), path_field[6 * n_paths],

@@ -26,6 +26,8 @@ EXPORTS = (
     "sbr_write_launch_rays_vtk", "sbr_scene_set_materials", "sbr_stl_read",
     "sbr_generate_rx_line", "sbr_generate_rx_plane", "sbr_pattern_create", "sbr_pattern_read",
     "sbr_pattern_info", "sbr_pattern_destroy", "sbr_fault_inject_alloc",
+    "sbr_scene_set_tuning", "sbr_scene_get_tuning", "sbr_autotune", "sbr_result_field_bound",
+    "sbr_scene_create_ex", "sbr_scene_triangle_frames", "sbr_scene_search_bvh",
 )
 
 
@@ -67,7 +69,8 @@ class Counts(C.Structure):
                                              "fp64_capture_tests", "launches",
                                              "capture_candidates", "ancestor_tests",
                                              "classes", "groups", "keys",
-                                             "near_edge_paths", "gpu_kernels")]
+                                             "near_edge_paths", "gpu_kernels",
+                                             "fp64_field_paths", "fp64_field_receivers")]
 
 
 class Path(C.Structure):
@@ -82,11 +85,17 @@ class Completion(C.Structure):
                 ("counts", Counts), ("result", C.c_void_p)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("find_steps", "find_refill", "find_blocks_per_sm",
+                                        "trace_blocks_per_sm", "capture_blocks_per_sm",
+                                        "trace_chunk_log2", "trace_kernel")]
+
+
 class Timing(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("total_ms", "trace_ms", "capture_ms", "correct_ms",
                                            "field_ms", "h2d_ms", "d2h_ms", "device_ms",
                                            "capture_kernel_ms", "trace_kernel_ms",
-                                           "trace_kernel_launches")]
+                                           "trace_kernel_launches", "trace_kernel_first_ms")]
 
 
 _lib = None
@@ -140,6 +149,14 @@ def load(path: str = LIB_PATH):
             "sbr_pattern_info": [vp, P(I), P(I), P(D), P(D)],
             "sbr_pattern_destroy": [vp],
             "sbr_fault_inject_alloc": [C.c_longlong],
+            "sbr_scene_set_tuning": [vp, P(Tuning)],
+            "sbr_scene_get_tuning": [vp, P(Request), I, P(Tuning)],
+            "sbr_autotune": [vp, P(Request), I, I, P(Tuning), P(D)],
+            "sbr_result_field_bound": [vp, P(D)],
+            "sbr_scene_create_ex": [I, P(C.c_float), P(C.c_float), P(I), P(Material), I,
+                                    C.c_uint, P(vp)],
+            "sbr_scene_triangle_frames": [vp, P(D), P(D), P(D)],
+            "sbr_scene_search_bvh": [vp, P(I), P(I), P(C.c_float), P(I)],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

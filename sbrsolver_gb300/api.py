@@ -163,25 +163,49 @@ class BVH:
 class DeviceScene:
     """Resident scene (triangles, BVH, materials) on the GPU."""
 
-    def __init__(self, mesh: Mesh, materials: Sequence[MaterialProperties]):
+    def __init__(self, mesh: Mesh, materials: Sequence[MaterialProperties],
+                 host_prep: bool = False):
+        """host_prep: build every table on the host (SBR_SCENE_HOST_PREP)
+        instead of the coplanar groups, frames and search BVH on the GPU."""
         lib = _lib.load()
         mats = (_lib.Material * len(materials))(*[m.as_c() for m in materials])
         v = np.ascontiguousarray(mesh.vertices, np.float32)
         n = np.ascontiguousarray(mesh.normals, np.float32)
         ids = np.ascontiguousarray(mesh.materialId, np.int32)
         h = C.c_void_p()
-        _lib.check(lib.sbr_scene_create(
+        _lib.check(lib.sbr_scene_create_ex(
             len(mesh), v.ctypes.data_as(C.POINTER(C.c_float)),
             n.ctypes.data_as(C.POINTER(C.c_float)), ids.ctypes.data_as(C.POINTER(C.c_int)),
-            mats, len(materials), C.byref(h)))
+            mats, len(materials), 1 if host_prep else 0, C.byref(h)))
         self.handle = h
         self.n_triangles = len(mesh)
         self._lib = lib
 
     @classmethod
-    def from_scene(cls, scene: Scene) -> "DeviceScene":
+    def from_scene(cls, scene: Scene, host_prep: bool = False) -> "DeviceScene":
         mats = [MaterialProperties(*m) for m in scene.materials]
-        return cls(Mesh(scene.tri, scene.normal, scene.material_id), mats)
+        return cls(Mesh(scene.tri, scene.normal, scene.material_id), mats, host_prep)
+
+    def triangle_frames(self) -> tuple:
+        """(frames (n, 3, 3), boxes (n, 6), centres (n, 3)) by triangle id."""
+        n = self.n_triangles
+        f, b, c = np.zeros((n, 3, 3)), np.zeros((n, 6)), np.zeros((n, 3))
+        dp = C.POINTER(C.c_double)
+        _lib.check(self._lib.sbr_scene_triangle_frames(self.handle, f.ctypes.data_as(dp),
+                                                       b.ctypes.data_as(dp), c.ctypes.data_as(dp)))
+        return f, b, c
+
+    def search_bvh(self) -> dict:
+        """The search BVH: nodes (raw 56-byte records as int32 words), the
+        leaf order (depth-first ranks) and the depth."""
+        nn, md = C.c_int(0), C.c_int(0)
+        _lib.check(self._lib.sbr_scene_search_bvh(self.handle, C.byref(nn), C.byref(md), None, None))
+        words = np.zeros(14 * nn.value, np.int32)
+        order = np.zeros(self.n_triangles, np.int32)
+        _lib.check(self._lib.sbr_scene_search_bvh(
+            self.handle, C.byref(nn), C.byref(md), words.ctypes.data_as(C.POINTER(C.c_float)),
+            order.ctypes.data_as(C.POINTER(C.c_int))))
+        return {"nodes": words.reshape(-1, 14), "order": order, "max_depth": md.value}
 
     def info(self) -> _lib.SceneInfo:
         out = _lib.SceneInfo()
@@ -202,6 +226,31 @@ class DeviceScene:
         _lib.check(self._lib.sbr_scene_coplanar_ids(self.handle, out.ctypes.data_as(C.POINTER(C.c_int))))
         return out
 
+    def set_tuning(self, **shapes) -> None:
+        """The scene's default launch shapes (sbr_tuning field names; 0 or
+        absent = the library default)."""
+        t = _lib.Tuning(**{k: int(v) for k, v in shapes.items()})
+        _lib.check(self._lib.sbr_scene_set_tuning(self.handle, C.byref(t)))
+
+    def tuning(self, requests=None) -> dict:
+        """The launch shapes a solve of `requests` (a request tuple or a list
+        of them; None = the scene default) would use, defaults filled in."""
+        arr, n = _request_array(requests)
+        out = _lib.Tuning()
+        _lib.check(self._lib.sbr_scene_get_tuning(self.handle, arr, n, C.byref(out)))
+        return {k: int(getattr(out, k)) for k, _ in _lib.Tuning._fields_}
+
+    def autotune(self, requests, rounds: int = 1) -> dict:
+        """Runs the library's autotuner on this batch (sbr_autotune) and
+        returns the chosen shapes plus the batch's device time with them."""
+        arr, n = _request_array(requests)
+        out, ms = _lib.Tuning(), C.c_double()
+        _lib.check(self._lib.sbr_autotune(self.handle, arr, n, int(rounds), C.byref(out),
+                                          C.byref(ms)))
+        d = {k: int(getattr(out, k)) for k, _ in _lib.Tuning._fields_}
+        d["device_ms"] = ms.value
+        return d
+
     def close(self) -> None:
         if self.handle:
             self._lib.sbr_scene_destroy(self.handle)
@@ -214,6 +263,15 @@ class DeviceScene:
             pass
 
 
+def _request_array(requests):
+    """(sbr_request array, count) from None, one request tuple or a list."""
+    if requests is None:
+        return None, 0
+    if isinstance(requests, tuple) and isinstance(requests[0], _lib.Request):
+        requests = [requests]
+    return (_lib.Request * len(requests))(*[r[0] for r in requests]), len(requests)
+
+
 @dataclass
 class Result:
     field: np.ndarray          # (n_rx, 3) complex128
@@ -223,6 +281,9 @@ class Result:
     # requests with field_check: FP64 field of the same paths and the error of `field`
     field_fp64: Optional[np.ndarray] = None
     field_error: Optional[dict] = None
+    # per receiver: bound on each component's absolute error (0 = FP64 arithmetic,
+    # -1 = none: the FP32-phase study mode); sbr_result_field_bound
+    field_bound: Optional[np.ndarray] = None
 
 
 def make_request(tx, tx_coord_sys, max_reflection, max_transmission, frequency, pt, use_fresnel,
@@ -318,6 +379,10 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
                     "field": np.array(p.field[:], np.float64), "near_edge": p.near_edge})
         field_c = f.view(np.complex128).reshape(-1, 3)  # exact, inf stays inf
         res = Result(field_c, counts, timing, paths)
+        if n_rx:
+            fb = np.zeros(n_rx, np.float64)
+            if lib.sbr_result_field_bound(h, fb.ctypes.data_as(C.POINTER(C.c_double))) == 0:
+                res.field_bound = fb
         fe = _lib.FieldError()
         if lib.sbr_result_field_error(h, C.byref(fe)) == 0:
             res.field_error = {k: getattr(fe, k) for k, _ in _lib.FieldError._fields_}

@@ -28,9 +28,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sbr.h"
@@ -44,6 +46,7 @@
 #include "sbr_trace.cuh"
 #include "sbr_capture.cuh"
 #include "sbr_paths.cuh"
+#include "sbr_prep.cuh"
 
 namespace sbr {
 
@@ -129,6 +132,9 @@ struct Workspace {
   DBuf<double> rx;
   DBuf<int> rx_req;
   DBuf<int> rx_bad;  // set when a device-resident receiver has a non-finite coordinate
+  DBuf<double> path_bound, field_bound;  // FP32 field mode: error bounds per path / receiver
+  DBuf<int> rx_flag;                     // FP32 field mode: receivers recomputed in FP64
+  DBuf<unsigned long long> fstat;
   DBuf<GridBuild> gb;
   DBuf<RxGrid> grids;
   DBuf<int> cell_base, cell_counts, cell_starts, cell_cursor;
@@ -181,8 +187,33 @@ struct Workspace {
   }
 };
 
+// Launch shapes of the trace and capture kernels (sbr_tuning); 0 = default.
+struct Tuning {
+  int find_steps = 0, find_refill = 0, find_bps = 0, trace_bps = 0, capture_bps = 0;
+  int chunk_log2 = 0;
+  int trace_kernel = 0;  // FP64 resolution: 1 = k_trace (a ray per lane), 2 = k_trace_pool
+};
+
+// A request mix's identity for the autotuner's cache: the sorted
+// (level, reflections, transmissions) of its requests.
+static std::string mix_key(const sbr_request* reqs, int n) {
+  std::vector<long long> k;
+  k.reserve(size_t(n));
+  for (int i = 0; i < n; ++i)
+    k.push_back((long long)reqs[i].tessellation << 40 | (long long)reqs[i].max_reflection << 20 |
+                reqs[i].max_transmission);
+  std::sort(k.begin(), k.end());
+  std::string s;
+  for (long long v : k) s += std::to_string(v) + ",";
+  return s;
+}
+
 struct SceneImpl {
   HostScene host;
+  // launch shapes: the scene default and autotuned choices per request mix
+  std::mutex tune_mu;
+  Tuning tuning;
+  std::map<std::string, Tuning> tuned;
   std::vector<sbr_material> materials;
   int device = 0;
   cudaStream_t stream = nullptr;  // scene uploads
@@ -230,6 +261,7 @@ struct sbr_scene {
 struct sbr_result {
   std::vector<double> field;
   std::vector<double> field64;  // FP64 shadow field (field_check requests), else empty
+  std::vector<double> field_bound;  // per receiver (sbr_result_field_bound)
   std::vector<sbr_path> paths;
   std::vector<int> tri, cop, kind;
   std::vector<double> points;
@@ -523,27 +555,271 @@ static int blocks_per_sm(K kernel, int block) {
   return std::max(1, per_sm);
 }
 
-// Persistent grid of the FP32 search: as many blocks as fit on the device.
-static int find_grid() {
+// Persistent grids: `want` resident blocks per SM (0 = as many as fit),
+// never more than fit, so every block of a persistent kernel is resident.
+static int persistent_grid(int fit, int want) {
+  return device_sms() * (want > 0 ? std::min(want, fit) : fit);
+}
+
+// Blocks of each persistent kernel that fit on one SM.
+static int find_fit() {
   static const int per_sm = blocks_per_sm(k_find, 128);
-  return device_sms() * per_sm;
+  return per_sm;
 }
-
-// Persistent grid of the FP64 resolution: as many blocks as fit on the device.
-static int trace_grid() {
+static int trace_fit() {
   static const int per_sm = blocks_per_sm(k_trace, 128);
-  return device_sms() * per_sm;
+  return per_sm;
+}
+// k_trace_pool keeps its rays in dynamic shared memory (one PoolSlots per warp).
+constexpr size_t kPoolSmem = sizeof(PoolSlots) * kPoolWarps;
+static int pool_fit() {
+  static const int per_sm = [] {
+    cudaFuncSetAttribute(k_trace_pool, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPoolSmem));
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_pool, 32 * kPoolWarps, kPoolSmem);
+    return std::max(1, n);
+  }();
+  return per_sm;
+}
+static int capture_fit() {
+  static const int per_sm = blocks_per_sm(k_capture_fast, 32 * kCapWarps);
+  return per_sm;
 }
 
-// Capture grid: every block resident at once (the work counter balances).
-static int capture_grid() {
-  static const int per_sm = blocks_per_sm(k_capture_fast, 32 * kCapWarps);
-  return device_sms() * per_sm;
+// FP32 search.
+static int find_grid(const Tuning& t) { return persistent_grid(find_fit(), t.find_bps); }
+
+// FP64 resolution.
+static int trace_grid(const Tuning& t) { return persistent_grid(trace_fit(), t.trace_bps); }
+
+// Capture: the work counter balances the blocks.
+static int capture_grid(const Tuning& t) { return persistent_grid(capture_fit(), t.capture_bps); }
+
+// The FP64 resolution kernel solves use unless tuned otherwise.
+constexpr int kDefaultTraceKernel = 1;
+
+// A tuning with every default filled in (the shapes a solve really uses).
+static Tuning resolved(Tuning t) {
+  if (t.find_steps <= 0) t.find_steps = kFindSteps;
+  if (t.find_refill <= 0) t.find_refill = kFindRefill;
+  t.find_refill = std::min(t.find_refill, 32);
+  t.find_bps = t.find_bps > 0 ? std::min(t.find_bps, find_fit()) : find_fit();
+  t.trace_bps = t.trace_bps > 0 ? std::min(t.trace_bps, trace_fit()) : trace_fit();
+  t.capture_bps = t.capture_bps > 0 ? std::min(t.capture_bps, capture_fit()) : capture_fit();
+  if (t.chunk_log2 <= 0) t.chunk_log2 = 24;
+  t.chunk_log2 = std::min(std::max(t.chunk_log2, 16), 26);
+  if (t.trace_kernel <= 0 || t.trace_kernel > 2) t.trace_kernel = kDefaultTraceKernel;
+  return t;
 }
 
 static int grid_for(long long n, int block) {
   const long long g = (n + block - 1) / block;
   return int(std::max<long long>(1, std::min<long long>(g, (long long)device_sms() * 32)));
+}
+
+// ------------------------------------------------------------ scene preparation on the device
+
+// What the device builds of a scene (sbr_prep.cuh): per triangle (file
+// order) the coplanar group, frame rows, box and box centre; the search BVH
+// over triangle ids, in the host build's node numbering.
+struct DeviceTables {
+  std::vector<int> cop;
+  std::vector<double> cs, bb, center;
+  SearchBVH search;
+  int degenerate = 0;
+};
+
+template <class T>
+static void swap_buf(DBuf<T>& a, DBuf<T>& b) {
+  std::swap(a.p, b.p);
+  std::swap(a.n, b.n);
+}
+
+// Stable LSD radix sort of perm by word[perm[i]], one varying bit per pass.
+static void sort_perm_by(DBuf<int>& perm, DBuf<int>& tmp, DBuf<int>& flags, DBuf<int>& scan,
+                         DBuf<unsigned>& vb, const uint32_t* word, int n, cudaStream_t st) {
+  if (n < 2) return;
+  CK(cudaMemsetAsync(vb.p, 0, sizeof(unsigned), st));
+  prep::k_varying_bits<<<grid_for(n, 256), 256, 0, st>>>(word, n, vb.p);
+  unsigned bits = 0;
+  CK(cudaMemcpyAsync(&bits, vb.p, sizeof bits, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int b = 0; b < 32; ++b) {
+    if (!((bits >> b) & 1u)) continue;
+    prep::k_bit_flags<<<grid_for(n, 256), 256, 0, st>>>(word, perm.p, n, b, flags.p);
+    k_scan_exclusive<<<1, 1024, 0, st>>>(flags.p, scan.p, n);
+    prep::k_bit_scatter<<<grid_for(n, 256), 256, 0, st>>>(word, perm.p, n, b, scan.p, tmp.p);
+    swap_buf(perm, tmp);
+  }
+  CK(cudaGetLastError());
+}
+
+// Builds the tables on the current device, on stream st.  v: 9 floats per
+// triangle, nrm: 3.
+static void device_prepare(const float* v_host, const float* n_host, int nt, cudaStream_t st,
+                           DeviceTables& T) {
+  const int nv = 3 * nt, ne = 3 * nt;
+  DBuf<float> v, nrm;
+  v.upload(v_host, 9 * size_t(nt), st);
+  nrm.upload(n_host, 3 * size_t(nt), st);
+  DBuf<uint32_t> wx, wy, wz;
+  DBuf<int> perm, tmp, flags, scan, uid, parent, misc;
+  DBuf<unsigned> vb;
+  const size_t big = size_t(std::max(nv, ne));
+  wx.ensure(big);
+  wy.ensure(big);
+  wz.ensure(big);
+  perm.ensure(big);
+  tmp.ensure(big);
+  flags.ensure(big);
+  scan.ensure(big + 1);
+  uid.ensure(nv);
+  parent.ensure(nt);
+  misc.ensure(4);
+  vb.ensure(1);
+  // -- vertex merge: sort the vertices by (x, y, z) bits, number the runs
+  prep::k_vertex_words<<<grid_for(nv, 256), 256, 0, st>>>(v.p, nv, wx.p, wy.p, wz.p, perm.p);
+  sort_perm_by(perm, tmp, flags, scan, vb, wz.p, nv, st);
+  sort_perm_by(perm, tmp, flags, scan, vb, wy.p, nv, st);
+  sort_perm_by(perm, tmp, flags, scan, vb, wx.p, nv, st);
+  prep::k_run_starts<<<grid_for(nv, 256), 256, 0, st>>>(wx.p, wy.p, wz.p, perm.p, nv, flags.p);
+  k_scan_exclusive<<<1, 1024, 0, st>>>(flags.p, scan.p, nv);
+  prep::k_vertex_ids<<<grid_for(nv, 256), 256, 0, st>>>(perm.p, flags.p, scan.p, nv, uid.p);
+  // -- edges of merged vertices, grouped by sorting; coplanar groups by
+  // hooking roots until no pair of an edge's triangles has two roots
+  CK(cudaMemsetAsync(misc.p, 0, 4 * sizeof(int), st));
+  prep::k_edges<<<grid_for(nt, 256), 256, 0, st>>>(uid.p, nt, wx.p, wy.p, perm.p, misc.p);
+  sort_perm_by(perm, tmp, flags, scan, vb, wy.p, ne, st);  // larger id first (LSD)
+  sort_perm_by(perm, tmp, flags, scan, vb, wx.p, ne, st);
+  prep::k_run_starts<<<grid_for(ne, 256), 256, 0, st>>>(wx.p, wy.p, nullptr, perm.p, ne, flags.p);
+  {
+    std::vector<int> id(nt);
+    for (int t = 0; t < nt; ++t) id[t] = t;
+    parent.upload(id.data(), id.size(), st);
+  }
+  for (int round = 0;; ++round) {
+    if (round > 200) throw std::string("device coplanar grouping did not converge");
+    CK(cudaMemsetAsync(misc.p + 1, 0, sizeof(int), st));
+    prep::k_hook<<<grid_for(ne, 256), 256, 0, st>>>(wx.p, wy.p, perm.p, flags.p, ne, nrm.p,
+                                                    parent.p, misc.p + 1);
+    prep::k_compress<<<grid_for(nt, 256), 256, 0, st>>>(parent.p, nt, nullptr);
+    int changed = 0;
+    CK(cudaMemcpyAsync(&changed, misc.p + 1, sizeof changed, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (!changed) break;
+  }
+  prep::k_compress<<<grid_for(nt, 256), 256, 0, st>>>(parent.p, nt, tmp.p);
+  k_scan_exclusive<<<1, 1024, 0, st>>>(tmp.p, scan.p, nt);
+  DBuf<int> cop;
+  cop.ensure(nt);
+  prep::k_group_ids<<<grid_for(nt, 256), 256, 0, st>>>(parent.p, scan.p, nt, cop.p);
+  // -- frames and boxes
+  DBuf<double> cs, bb, center;
+  cs.ensure(9 * size_t(nt));
+  bb.ensure(6 * size_t(nt));
+  center.ensure(3 * size_t(nt));
+  prep::k_frames<<<grid_for(nt, 128), 128, 0, st>>>(v.p, nrm.p, nt, cs.p, bb.p, center.p);
+  CK(cudaGetLastError());
+  // -- search BVH, one level of nodes at a time
+  DBuf<float> blo, bhi, cen;
+  blo.ensure(3 * size_t(nt));
+  bhi.ensure(3 * size_t(nt));
+  cen.ensure(3 * size_t(nt));
+  DBuf<int> ord, otmp;
+  ord.ensure(nt);
+  otmp.ensure(nt);
+  prep::k_tri_boxes<<<grid_for(nt, 256), 256, 0, st>>>(v.p, nt, blo.p, bhi.p, cen.p, ord.p);
+  DBuf<prep::Seg> segs, next;
+  DBuf<prep::SegPlan> plans;
+  DBuf<prep::BNode> nodes;
+  const size_t max_nodes = size_t(nt) + 1;
+  segs.ensure(max_nodes * 2 + 2);
+  next.ensure(max_nodes * 2 + 2);
+  plans.ensure(max_nodes * 2 + 2);
+  nodes.ensure(max_nodes);
+  DBuf<int> ctl;  // [0] nodes, [1] next segments, [2] max depth, [3] root ref, [4] median too big
+  ctl.ensure(8);
+  DBuf<float> root_box;
+  root_box.ensure(6);
+  CK(cudaMemsetAsync(ctl.p, 0, 8 * sizeof(int), st));
+  {
+    const prep::Seg root{0, nt, 1, -1, 0};
+    segs.upload(&root, 1, st);
+  }
+  int n_segs = 1;
+  for (int level = 0; n_segs > 0; ++level) {
+    if (level > 200) throw std::string("device search BVH deeper than 200 levels");
+    prep::k_plan<<<n_segs, 256, 0, st>>>(segs.p, n_segs, ord.p, blo.p, bhi.p, cen.p, nodes.p,
+                                         ctl.p, plans.p, ctl.p + 2, ctl.p + 3, root_box.p);
+    prep::k_partition<<<n_segs, 256, 0, st>>>(segs.p, n_segs, plans.p, ord.p, otmp.p, cen.p);
+    prep::k_median<<<n_segs, 256, 0, st>>>(segs.p, n_segs, plans.p, ord.p, otmp.p, cen.p,
+                                           ctl.p + 4);
+    CK(cudaMemsetAsync(ctl.p + 1, 0, sizeof(int), st));
+    prep::k_children<<<grid_for(n_segs, 256), 256, 0, st>>>(segs.p, n_segs, plans.p, next.p,
+                                                            ctl.p + 1);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&n_segs, ctl.p + 1, sizeof n_segs, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    swap_buf(segs, next);
+  }
+  int c[8];
+  CK(cudaMemcpyAsync(c, ctl.p, sizeof c, cudaMemcpyDeviceToHost, st));
+  T.cop.resize(nt);
+  T.cs.resize(9 * size_t(nt));
+  T.bb.resize(6 * size_t(nt));
+  T.center.resize(3 * size_t(nt));
+  CK(cudaMemcpyAsync(T.cop.data(), cop.p, sizeof(int) * nt, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(T.cs.data(), cs.p, sizeof(double) * T.cs.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(T.bb.data(), bb.p, sizeof(double) * T.bb.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(T.center.data(), center.p, sizeof(double) * T.center.size(),
+                     cudaMemcpyDeviceToHost, st));
+  float rb[6];
+  CK(cudaMemcpyAsync(rb, root_box.p, sizeof rb, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaMemcpy(&T.degenerate, misc.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (c[4]) throw std::string("device search BVH: a median split of more than 8192 triangles");
+  const int n_nodes = c[0];
+  std::vector<prep::BNode> bn(size_t(std::max(1, n_nodes)));
+  if (n_nodes)
+    CK(cudaMemcpy(bn.data(), nodes.p, sizeof(prep::BNode) * n_nodes, cudaMemcpyDeviceToHost));
+  T.search.order.resize(nt);
+  CK(cudaMemcpy(T.search.order.data(), ord.p, sizeof(int) * nt, cudaMemcpyDeviceToHost));
+  T.search.max_depth = c[2];
+  // depth-first numbering (node 0 = a copy of the root), children[0] first
+  T.search.nodes.assign(size_t(n_nodes) + 1, SearchNode{});
+  const int root_ref = c[3];
+  if (root_ref >= 0) {
+    std::vector<int> dfs(size_t(n_nodes), -1);
+    std::vector<int> stack{root_ref};
+    int id = 1;
+    while (!stack.empty()) {
+      const int b = stack.back();
+      stack.pop_back();
+      dfs[size_t(b)] = id++;
+      if (bn[size_t(b)].child[1] >= 0) stack.push_back(bn[size_t(b)].child[1]);
+      if (bn[size_t(b)].child[0] >= 0) stack.push_back(bn[size_t(b)].child[0]);
+    }
+    for (int b = 0; b < n_nodes; ++b) {
+      SearchNode& o = T.search.nodes[size_t(dfs[size_t(b)])];
+      for (int k = 0; k < 2; ++k) {
+        for (int a = 0; a < 3; ++a) {
+          o.lo[k][a] = bn[size_t(b)].lo[k][a];
+          o.hi[k][a] = bn[size_t(b)].hi[k][a];
+        }
+        const int ch = bn[size_t(b)].child[k];
+        o.child[k] = ch >= 0 ? dfs[size_t(ch)] : ch;
+      }
+    }
+    T.search.nodes[0] = T.search.nodes[1];
+  } else {  // the whole scene is one leaf
+    SearchNode& o = T.search.nodes[0];
+    for (int a = 0; a < 3; ++a) {
+      o.lo[0][a] = o.lo[1][a] = rb[a];
+      o.hi[0][a] = o.hi[1][a] = rb[3 + a];
+    }
+    o.child[0] = root_ref;
+    o.child[1] = ~0;
+  }
 }
 
 static FieldConsts field_consts() {
@@ -563,7 +839,7 @@ static FieldConsts field_consts() {
 // force_check: compute the FP64 shadow field even if no request here asks for
 // it (another pass of the same batch did).
 static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int n_req,
-                       sbr_result& out, bool force_check = false) {
+                       sbr_result& out, const Tuning& tu, bool force_check = false) {
   long long nl = 0;  // kernel launches of this solve (all attempts)
   cudaStream_t st = W.stream;
   if (S.host.mesh_order.empty()) throw std::string("scene is not initialised");
@@ -799,7 +1075,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     // search (k_find) stores the chunk's contenders, then k_trace resolves
     // them in FP64 and spawns the next depth.  The ray count of a depth > 0
     // is on the device; chunks past it return at once.
-    constexpr long long kTraceChunk = 1LL << 24;
+    const long long kTraceChunk = 1LL << (tu.chunk_log2 > 0 ? std::min(tu.chunk_log2, 26) : 24);
     const long long max_width = std::max<long long>(launches, (long long)W.cap_queue);
     const long long chunk = std::max<long long>(1, std::min(kTraceChunk, max_width));
     W.cand.ensure(size_t(chunk) * kCand);
@@ -818,8 +1094,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fnd.cand = W.cand.p;
     fnd.ncand = W.ncand.p;
     fnd.ray32 = W.ray32.p;
-    fnd.steps = kFindSteps;
-    fnd.refill = kFindRefill;
+    fnd.steps = tu.find_steps > 0 ? tu.find_steps : kFindSteps;
+    fnd.refill = tu.find_refill > 0 ? std::min(tu.find_refill, 32) : kFindRefill;
     ta.cand = W.cand.p;
     ta.ncand = W.ncand.p;
     ta.ray32 = W.ray32.p;
@@ -834,14 +1110,20 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         ta.lo = fnd.lo = lo;
         ta.hi = fnd.hi = std::min(bound, lo + chunk);
         CK(cudaMemsetAsync(W.find_work.p, 0, 2 * sizeof(unsigned long long), st));
-        ++nl, k_find<<<find_grid(), 128, 0, st>>>(fnd);
+        ++nl, k_find<<<find_grid(tu), 128, 0, st>>>(fnd);
         if (2 * n_tr + 2 > W.tr_ev.size()) {
           W.tr_ev.resize(2 * n_tr + 2, nullptr);
           for (auto& e : W.tr_ev)
             if (!e) CK(cudaEventCreate(&e));
         }
         CK(cudaEventRecord(W.tr_ev[2 * n_tr], st));
-        ++nl, k_trace<<<std::min<long long>(trace_grid(), (ta.hi - lo + 127) / 128), 128, 0, st>>>(ta);
+        if (resolved(tu).trace_kernel == 2) {
+          const long long need = (ta.hi - lo + 32 * kPoolSlots - 1) / (32 * kPoolSlots);
+          const int grid = int(std::min<long long>(device_sms() * pool_fit(), std::max(1LL, need)));
+          ++nl, k_trace_pool<<<grid, 32 * kPoolWarps, kPoolSmem, st>>>(ta);
+        } else {
+          ++nl, k_trace<<<std::min<long long>(trace_grid(tu), (ta.hi - lo + 127) / 128), 128, 0, st>>>(ta);
+        }
         CK(cudaEventRecord(W.tr_ev[2 * n_tr + 1], st));
         ++n_tr;
       }
@@ -877,10 +1159,10 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     CK(cudaStreamWaitEvent(st, W.join, 0));
     CK(cudaEventRecord(W.cap_ev[0], st));
     if (stage_counts) {
-      ++nl, k_capture<true><<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
+      ++nl, k_capture<true><<<capture_grid(tu), 32 * kCapWarps, 0, st>>>(ca);
       CK(cudaEventRecord(W.cap_ev[1], st));
     } else {
-      ++nl, k_capture_fast<<<capture_grid(), 32 * kCapWarps, 0, st>>>(ca);
+      ++nl, k_capture_fast<<<capture_grid(tu), 32 * kCapWarps, 0, st>>>(ca);
       CK(cudaEventRecord(W.cap_ev[1], st));
       ++nl, k_capture_finish<<<device_sms() * 16, 128, 0, st>>>(ca);
     }
@@ -983,6 +1265,17 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fa.path_pts = W.path_pts.p;
     fa.seg = W.seg.p;
     fa.path_mat = W.path_mat.p;
+    bool any_fp32 = false;  // a request in the FP32 field mode (error bounds, escalation)
+    for (int r = 0; r < n_req; ++r) any_fp32 |= tp[r].precision == 1;
+    W.path_bound.ensure(nsa);
+    W.rx_flag.ensure(std::max(1, rx_total));
+    W.field_bound.ensure(std::max(1, rx_total));
+    W.fstat.ensure(2);
+    CK(cudaMemsetAsync(W.rx_flag.p, 0, sizeof(int) * std::max(1, rx_total), st));
+    CK(cudaMemsetAsync(W.fstat.p, 0, 2 * sizeof(unsigned long long), st));
+    fa.path_bound = W.path_bound.p;
+    fa.rx_flag = W.rx_flag.p;
+    fa.fstat = W.fstat.p;
     if (ns) {
       ++nl, k_path<<<grid_for(ns, 64), 64, 0, st>>>(fa);
       ++nl, k_seg<<<grid_for(ns * (kMaxDepth + 1), 64), 64, 0, st>>>(fa);
@@ -996,9 +1289,15 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       ++nl, k_surv_scatter<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv,
                                                         W.s_starts.p, W.s_cursor.p, W.s_order.p);
     if (rx_total)
-      ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
-                                                        rx_total, W.path_field.p, -1, W.rx_req.p,
-                                                        W.txp.p, W.field.p);
+      ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(
+          W.surv.p, W.s_starts.p, W.s_order.p, rx_total, W.path_field.p, -1, W.rx_req.p, W.txp.p,
+          W.field.p, W.path_bound.p, W.field_bound.p, W.rx_flag.p, W.fstat.p);
+    if (any_fp32 && rx_total) {  // receivers the FP32 bound could not certify, in FP64
+      if (ns) ++nl, k_escalate<<<grid_for(ns, 64), 64, 0, st>>>(fa);
+      ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(
+          W.surv.p, W.s_starts.p, W.s_order.p, rx_total, W.path_field.p, 0, W.rx_req.p, W.txp.p,
+          W.field.p, nullptr, W.field_bound.p, nullptr, nullptr, W.rx_flag.p);
+    }
     CK(cudaGetLastError());
     CK(cudaEventRecord(W.ev[6], st));
     if (field_check) {  // FP64 shadow of the same paths, outside the timed stages
@@ -1007,6 +1306,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       FieldArgs f64 = fa;
       f64.precision = 0;
       f64.path_field = W.path_field64.p;
+      f64.path_bound = nullptr;
       if (ns) {
         ++nl, k_seg<<<grid_for(ns * (kMaxDepth + 1), 64), 64, 0, st>>>(f64);
         ++nl, k_combine<<<grid_for(ns, 64), 64, 0, st>>>(f64);
@@ -1022,6 +1322,12 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     if (rx_total)
       CK(cudaMemcpyAsync(out.field.data(), W.field.p, sizeof(double) * 6 * rx_total,
                          cudaMemcpyDeviceToHost, st));
+    out.field_bound.resize(size_t(rx_total));
+    unsigned long long fst[2] = {0, 0};
+    if (rx_total)
+      CK(cudaMemcpyAsync(out.field_bound.data(), W.field_bound.p, sizeof(double) * rx_total,
+                         cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(fst, W.fstat.p, sizeof fst, cudaMemcpyDeviceToHost, st));
     out.field64.clear();
     if (field_check) {
       out.field64.resize(6 * size_t(rx_total));
@@ -1109,6 +1415,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     out.counts.near_edge_paths = 0;
     for (const sbr_path& p : out.paths) out.counts.near_edge_paths += p.near_edge;
     out.counts.gpu_kernels = nl;
+    out.counts.fp64_field_paths = (long long)fst[0];
+    out.counts.fp64_field_receivers = (long long)fst[1];
     float ms[8] = {};
     for (int i = 1; i < 8; ++i) CK(cudaEventElapsedTime(&ms[i], W.ev[i - 1], W.ev[i]));
     out.timing.h2d_ms = ms[1];
@@ -1125,6 +1433,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       float x = 0;
       CK(cudaEventElapsedTime(&x, W.tr_ev[2 * i], W.tr_ev[2 * i + 1]));
       tr_k += x;
+      if (i == 0) out.timing.trace_kernel_first_ms = x;
     }
     out.timing.trace_kernel_ms = tr_k;
     out.timing.trace_kernel_launches = double(n_tr);
@@ -1152,6 +1461,8 @@ std::vector<sbr_result*> split_result(const sbr_result& b) {
     const size_t nf = 6 * size_t(b.rx_per_request[r]);
     x->field.assign(b.field.begin() + f0, b.field.begin() + f0 + nf);
     if (!b.field64.empty()) x->field64.assign(b.field64.begin() + f0, b.field64.begin() + f0 + nf);
+    if (b.field_bound.size() * 6 == b.field.size())
+      x->field_bound.assign(b.field_bound.begin() + f0 / 6, b.field_bound.begin() + (f0 + nf) / 6);
     f0 += nf;
     for (const sbr_path& p : b.paths) {
       if (p.request != r) continue;
@@ -1186,6 +1497,17 @@ std::vector<sbr_result*> split_result(const sbr_result& b) {
 
 using namespace sbr;
 
+// The launch shapes a solve of this request mix uses: the autotuned choice
+// for the mix if there is one, else the scene's default.
+static Tuning tuning_for(SceneImpl& S, const sbr_request* reqs, int n) {
+  std::lock_guard<std::mutex> lock(S.tune_mu);
+  if (reqs && n > 0) {
+    auto it = S.tuned.find(mix_key(reqs, n));
+    if (it != S.tuned.end()) return it->second;
+  }
+  return S.tuning;
+}
+
 #define ABI_GUARD(...)                                                     \
   try {                                                                     \
     __VA_ARGS__                                                             \
@@ -1219,7 +1541,8 @@ static std::string material_error(const sbr_material* m, int n) {
 }
 
 static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, const int* mat_ids,
-                               const sbr_material* materials, int n_materials, sbr_scene** out) {
+                               const sbr_material* materials, int n_materials, unsigned flags,
+                               sbr_scene** out) {
   ABI_GUARD({
     if (!out) throw std::string("out is NULL");
     *out = nullptr;
@@ -1241,11 +1564,6 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
     auto sc = std::make_unique<sbr_scene>();
     SceneImpl& S = sc->impl;
     std::string err;
-    if (!prepare_scene(nt, v.data(), n.data(), mat_ids, S.host, err)) throw err;
-    if (S.host.max_depth + 4 > kStack)
-      throw std::string("BVH depth ") + std::to_string(S.host.max_depth) +
-          " exceeds the traversal stack (" + std::to_string(kStack) + ")";
-    S.materials.assign(materials, materials + n_materials);
     int dev_count = 0;
     if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
       cudaGetLastError();
@@ -1253,6 +1571,66 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
     }
     CK(cudaGetDevice(&S.device));
     CK(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+    // The device builds the coplanar groups, frames and search BVH on its own
+    // host thread and stream while this thread builds the reference BVH
+    // (SBR_SCENE_HOST_PREP: everything on the host).
+    const bool on_device = !(flags & SBR_SCENE_HOST_PREP);
+    DeviceTables dt;
+    std::string dev_err;
+    bool dev_failed = false;
+    CudaError dev_cuda{cudaSuccess, ""};
+    std::thread dev_thread;
+    if (on_device)
+      dev_thread = std::thread([&] {
+        try {
+          CK(cudaSetDevice(S.device));
+          cudaStream_t st = nullptr;
+          CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+          struct Del {
+            cudaStream_t s;
+            ~Del() { cudaStreamDestroy(s); }
+          } del{st};
+          device_prepare(v.data(), n.data(), nt, st, dt);
+        } catch (const CudaError& e) {
+          dev_failed = true;
+          dev_cuda = e;
+        } catch (const std::string& e) {
+          dev_failed = true;
+          dev_err = e;
+        } catch (...) {
+          dev_failed = true;
+          dev_err = "device scene preparation failed";
+        }
+      });
+    struct Join {
+      std::thread& t;
+      ~Join() {
+        if (t.joinable()) t.join();
+      }
+    } join{dev_thread};
+    const bool host_ok = prepare_scene(nt, v.data(), n.data(), mat_ids, S.host, err, !on_device);
+    if (dev_thread.joinable()) dev_thread.join();
+    if (!host_ok) throw err;
+    if (on_device) {
+      if (dev_failed) {
+        if (dev_cuda.e != cudaSuccess) throw dev_cuda;
+        throw dev_err;
+      }
+      if (dt.degenerate)
+        throw std::string("degenerate triangle(s) after vertex merge: ") +
+            std::to_string(dt.degenerate);
+      for (int t = 0; t < nt; ++t) {
+        HostTri& tr = S.host.tris[size_t(t)];
+        tr.cop = dt.cop[size_t(t)];
+        std::memcpy(tr.cs, &dt.cs[9 * size_t(t)], sizeof tr.cs);
+      }
+      S.host.search = std::move(dt.search);
+      map_search_order(S.host);
+    }
+    if (S.host.max_depth + 4 > kStack)
+      throw std::string("BVH depth ") + std::to_string(S.host.max_depth) +
+          " exceeds the traversal stack (" + std::to_string(kStack) + ")";
+    S.materials.assign(materials, materials + n_materials);
     upload_scene(S);
     upload_mesh_order(S, S.host.mesh_order);
     *out = sc.release();
@@ -1260,16 +1638,62 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
   })
 }
 
-sbr_status sbr_scene_create(int n_triangles, const float* vertices, const float* normals,
-                            const int* material_ids, const sbr_material* materials,
-                            int n_materials, sbr_scene** out) {
+sbr_status sbr_scene_create_ex(int n_triangles, const float* vertices, const float* normals,
+                               const int* material_ids, const sbr_material* materials,
+                               int n_materials, unsigned flags, sbr_scene** out) {
   if (n_triangles <= 0 || !vertices || !normals) {
     set_err("sbr_scene_create: empty triangle list");
     return SBR_ERR_INVALID_ARG;
   }
+  if (flags & ~unsigned(SBR_SCENE_HOST_PREP)) {
+    set_err("sbr_scene_create_ex: unknown flags");
+    return SBR_ERR_INVALID_ARG;
+  }
   std::vector<float> v(vertices, vertices + 9 * size_t(n_triangles));
   std::vector<float> n(normals, normals + 3 * size_t(n_triangles));
-  return scene_common(v, n, material_ids, materials, n_materials, out);
+  return scene_common(v, n, material_ids, materials, n_materials, flags, out);
+}
+
+sbr_status sbr_scene_create(int n_triangles, const float* vertices, const float* normals,
+                            const int* material_ids, const sbr_material* materials,
+                            int n_materials, sbr_scene** out) {
+  return sbr_scene_create_ex(n_triangles, vertices, normals, material_ids, materials, n_materials,
+                             0u, out);
+}
+
+sbr_status sbr_scene_triangle_frames(const sbr_scene* scene, double* frames, double* boxes,
+                                     double* centers) {
+  if (!scene) {
+    set_err("sbr_scene_triangle_frames: NULL scene");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const auto& tris = scene->impl.host.tris;
+  for (size_t t = 0; t < tris.size(); ++t) {
+    if (frames) std::memcpy(frames + 9 * t, tris[t].cs, sizeof tris[t].cs);
+    if (boxes) std::memcpy(boxes + 6 * t, tris[t].bb, sizeof tris[t].bb);
+    if (centers) std::memcpy(centers + 3 * t, tris[t].center, sizeof tris[t].center);
+  }
+  return SBR_OK;
+}
+
+sbr_status sbr_scene_search_bvh(const sbr_scene* scene, int* n_nodes, int* max_depth,
+                                float* nodes, int* order) {
+  if (!scene || !n_nodes) {
+    set_err("sbr_scene_search_bvh: NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const SearchBVH& B = scene->impl.host.search;
+  if (nodes && *n_nodes < int(B.nodes.size())) {
+    set_err("sbr_scene_search_bvh: node buffer too small");
+    *n_nodes = int(B.nodes.size());
+    return SBR_ERR_CAPACITY;
+  }
+  *n_nodes = int(B.nodes.size());
+  if (max_depth) *max_depth = B.max_depth;
+  static_assert(sizeof(SearchNode) == 14 * 4, "search node layout");
+  if (nodes) std::memcpy(nodes, B.nodes.data(), sizeof(SearchNode) * B.nodes.size());
+  if (order) std::memcpy(order, B.order.data(), sizeof(int) * B.order.size());
+  return SBR_OK;
 }
 
 sbr_status sbr_scene_create_from_stl(const char* path, const int* material_ids,
@@ -1281,7 +1705,7 @@ sbr_status sbr_scene_create_from_stl(const char* path, const int* material_ids,
     set_err(path ? err : std::string("path is NULL"));
     return SBR_ERR_IO;
   }
-  return scene_common(v, n, material_ids, materials, n_materials, out);
+  return scene_common(v, n, material_ids, materials, n_materials, 0u, out);
 }
 
 sbr_status sbr_scene_info_get(const sbr_scene* scene, sbr_scene_info* out) {
@@ -1443,6 +1867,7 @@ sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_
     bool batch_check = false;  // every pass carries the FP64 shadow if any request wants it
     for (int r = 0; r < n_requests; ++r)
       batch_check |= requests[r].field_check && requests[r].field_precision != SBR_FIELD_FP64;
+    const Tuning tu = tuning_for(S, requests, n_requests);
     auto res = std::make_unique<sbr_result>();
     int first = 0;
     while (first < n_requests) {
@@ -1450,11 +1875,11 @@ sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_
       double acc = est(requests[first]);
       while (last < n_requests && acc + est(requests[last]) <= budget) acc += est(requests[last++]);
       if (first == 0 && last == n_requests) {
-        solve_impl(S, *W, requests, n_requests, *res);
+        solve_impl(S, *W, requests, n_requests, *res, tu);
         break;
       }
       sbr_result part;
-      solve_impl(S, *W, requests + first, last - first, part, batch_check);
+      solve_impl(S, *W, requests + first, last - first, part, tu, batch_check);
       const long long ray_base = (long long)res->tri.size();
       for (sbr_path p : part.paths) {
         p.request += first;
@@ -1471,6 +1896,8 @@ sbr_status sbr_solve_batch(sbr_scene* scene, const sbr_request* requests, int n_
                                        part.launches_per_request.end());
       res->field.insert(res->field.end(), part.field.begin(), part.field.end());
       res->field64.insert(res->field64.end(), part.field64.begin(), part.field64.end());
+      res->field_bound.insert(res->field_bound.end(), part.field_bound.begin(),
+                              part.field_bound.end());
       res->tri.insert(res->tri.end(), part.tri.begin(), part.tri.end());
       res->cop.insert(res->cop.end(), part.cop.begin(), part.cop.end());
       res->kind.insert(res->kind.end(), part.kind.begin(), part.kind.end());
@@ -1493,6 +1920,135 @@ sbr_status sbr_solve(sbr_scene* scene, const sbr_request* request, sbr_result** 
   return sbr_solve_batch(scene, request, 1, out);
 }
 
+static void tuning_to_c(const Tuning& t, sbr_tuning* o) {
+  o->trace_kernel = t.trace_kernel;
+  o->find_steps = t.find_steps;
+  o->find_refill = t.find_refill;
+  o->find_blocks_per_sm = t.find_bps;
+  o->trace_blocks_per_sm = t.trace_bps;
+  o->capture_blocks_per_sm = t.capture_bps;
+  o->trace_chunk_log2 = t.chunk_log2;
+}
+
+sbr_status sbr_scene_set_tuning(sbr_scene* scene, const sbr_tuning* t) {
+  if (!scene || !t) {
+    set_err("sbr_scene_set_tuning: NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  if (t->find_steps < 0 || t->find_refill < 0 || t->find_refill > 32 ||
+      t->find_blocks_per_sm < 0 || t->trace_blocks_per_sm < 0 || t->capture_blocks_per_sm < 0 ||
+      (t->trace_chunk_log2 != 0 && (t->trace_chunk_log2 < 16 || t->trace_chunk_log2 > 26)) ||
+      t->trace_kernel < 0 || t->trace_kernel > 2) {
+    set_err("sbr_scene_set_tuning: fields must be >= 0, find_refill <= 32, trace_chunk_log2 "
+            "0 or 16..26 and trace_kernel 0..2");
+    return SBR_ERR_INVALID_ARG;
+  }
+  SceneImpl& S = scene->impl;
+  std::lock_guard<std::mutex> lock(S.tune_mu);
+  S.tuning.find_steps = t->find_steps;
+  S.tuning.find_refill = t->find_refill;
+  S.tuning.find_bps = t->find_blocks_per_sm;
+  S.tuning.trace_bps = t->trace_blocks_per_sm;
+  S.tuning.capture_bps = t->capture_blocks_per_sm;
+  S.tuning.chunk_log2 = t->trace_chunk_log2;
+  S.tuning.trace_kernel = t->trace_kernel;
+  return SBR_OK;
+}
+
+sbr_status sbr_scene_get_tuning(sbr_scene* scene, const sbr_request* requests, int n_requests,
+                                sbr_tuning* out) {
+  if (!scene || !out || n_requests < 0 || (n_requests > 0 && !requests)) {
+    set_err("sbr_scene_get_tuning: bad arguments");
+    return SBR_ERR_INVALID_ARG;
+  }
+  ABI_GUARD({
+    CK(cudaSetDevice(scene->impl.device));
+    tuning_to_c(resolved(tuning_for(scene->impl, requests, n_requests)), out);
+    return SBR_OK;
+  })
+}
+
+sbr_status sbr_autotune(sbr_scene* scene, const sbr_request* requests, int n_requests, int rounds,
+                        sbr_tuning* out, double* best_ms) {
+  if (!scene || !requests || n_requests <= 0 || rounds < 1 || rounds > 8) {
+    set_err("sbr_autotune: need a scene, a non-empty batch and 1..8 rounds");
+    return SBR_ERR_INVALID_ARG;
+  }
+  SceneImpl& S = scene->impl;
+  const std::string key = mix_key(requests, n_requests);
+  Tuning cur;
+  {
+    std::lock_guard<std::mutex> lock(S.tune_mu);
+    auto it = S.tuned.find(key);
+    cur = it != S.tuned.end() ? it->second : S.tuning;
+  }
+  sbr_status st = SBR_OK;
+  ABI_GUARD({
+    CK(cudaSetDevice(S.device));
+    cur = resolved(cur);
+  })
+  // device time of the batch under tuning t: the better of two solves
+  auto time_of = [&](const Tuning& t, double& ms) -> sbr_status {
+    {
+      std::lock_guard<std::mutex> lock(S.tune_mu);
+      S.tuned[key] = t;
+    }
+    ms = 1e300;
+    for (int k = 0; k < 2; ++k) {
+      sbr_result* r = nullptr;
+      const sbr_status s = sbr_solve_batch(scene, requests, n_requests, &r);
+      if (s != SBR_OK) return s;
+      ms = std::min(ms, r->timing.device_ms);
+      sbr_result_destroy(r);
+    }
+    return SBR_OK;
+  };
+  double best = 0, ms = 0;
+  if ((st = time_of(cur, best)) != SBR_OK) return st;  // also sizes the workspace
+  if ((st = time_of(cur, best)) != SBR_OK) return st;
+  const int ff = find_fit(), tf = trace_fit(), cf = capture_fit();
+  auto span = [](int fit) {
+    std::vector<int> v;
+    for (int b = std::max(1, fit / 2); b <= fit; ++b) v.push_back(b);
+    return v;
+  };
+  const std::vector<int> steps{8, 16, 32, 64, 128}, refill{4, 8, 16, 24, 32}, chunk{20, 22, 24},
+      kernels{1, 2};
+  for (int round = 0; round < rounds; ++round) {
+    bool moved = false;
+    for (int p = 0; p < 7; ++p) {
+      const std::vector<int> cand = p == 0   ? kernels
+                                    : p == 1 ? steps
+                                    : p == 2 ? refill
+                                    : p == 3 ? span(ff)
+                                    : p == 4 ? span(tf)
+                                    : p == 5 ? span(cf)
+                                             : chunk;
+      for (int v : cand) {
+        Tuning t = cur;
+        int* f[7] = {&t.trace_kernel, &t.find_steps, &t.find_refill, &t.find_bps, &t.trace_bps,
+                     &t.capture_bps, &t.chunk_log2};
+        if (*f[p] == v) continue;
+        *f[p] = v;
+        if ((st = time_of(t, ms)) != SBR_OK) return st;
+        if (ms < 0.99 * best) {  // a change must gain at least 1 %
+          best = ms;
+          cur = t;
+          moved = true;
+        }
+      }
+    }
+    if (!moved) break;
+  }
+  {
+    std::lock_guard<std::mutex> lock(S.tune_mu);
+    S.tuned[key] = cur;
+  }
+  if (out) tuning_to_c(cur, out);
+  if (best_ms) *best_ms = best;
+  return SBR_OK;
+}
+
 sbr_status sbr_result_counts(const sbr_result* r, sbr_counts* out) {
   if (!r || !out) {
     set_err("NULL argument");
@@ -1508,6 +2064,19 @@ sbr_status sbr_result_field(const sbr_result* r, double* out) {
     return SBR_ERR_INVALID_ARG;
   }
   std::copy(r->field.begin(), r->field.end(), out);
+  return SBR_OK;
+}
+
+sbr_status sbr_result_field_bound(const sbr_result* r, double* out) {
+  if (!r || !out) {
+    set_err("NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  if (r->field_bound.size() * 6 != r->field.size()) {
+    set_err("sbr_result_field_bound: no bounds in this result");
+    return SBR_ERR_NOT_READY;
+  }
+  std::copy(r->field_bound.begin(), r->field_bound.end(), out);
   return SBR_OK;
 }
 

@@ -174,18 +174,31 @@ __device__ __forceinline__ Cx<double> slab_phase(double theta_i, Cx<double> eps_
   return cexp_(cx(0.0, -2.0) * q);
 }
 
+template <class R>
+__device__ __forceinline__ R cabs_(Cx<R> z) {
+  return hypot(z.re, z.im);
+}
+
 // GetTransAngle + GetTMCoeff/GetTECoeff for air -> eps_t; returns the
 // coefficient pair (TM, TE) applied to E_theta, E_phi.  ph: slab_phase.
+// cond (optional) receives the smallest ratio |denominator| / (sum of the
+// magnitudes of its two terms) over the coefficients' denominators: near 0
+// the coefficient sits near a pole of its formula, where the rounding of its
+// inputs is amplified by about the inverse of that ratio.
 template <class R>
 __device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, Cx<R> ph, bool inf_wall,
-                             R eta0, Cx<R>& c_tm, Cx<R>& c_te) {
+                             R eta0, Cx<R>& c_tm, Cx<R>& c_te, R* cond = nullptr) {
   const Cx<R> ni = cx(R(1)), nt = csqrt(eps_t);
   const Cx<R> ti = cx(theta_i);
   const Cx<R> tt = casin_((ni / nt) * csin_(ti));
   const Cx<R> etai = eta0 / ni, etat = eta0 / nt;
   const Cx<R> ci = ccos_(ti), ct = ccos_(tt);
-  const Cx<R> g_te = -((etat / ct) - (etai / ci)) / ((etat / ct) + (etai / ci));
-  const Cx<R> g_tm = (-(etat * ct) + etai * ci) / (etat * ct + etai * ci);
+  const Cx<R> a_te = etat / ct, b_te = etai / ci, a_tm = etat * ct, b_tm = etai * ci;
+  const Cx<R> g_te = -(a_te - b_te) / (a_te + b_te);
+  const Cx<R> g_tm = (-a_tm + b_tm) / (a_tm + b_tm);
+  if (cond)
+    *cond = fmin(cabs_(a_te + b_te) / (cabs_(a_te) + cabs_(b_te)),
+                 cabs_(a_tm + b_tm) / (cabs_(a_tm) + cabs_(b_tm)));
   if (inf_wall) {
     c_tm = reflect ? g_tm : cx(R(0));
     c_te = reflect ? g_te : cx(R(0));
@@ -195,6 +208,9 @@ __device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, Cx<R> ph, boo
   // gives reflection 0 and transmission 1.
   const Cx<R> one = cx(R(1));
   const Cx<R> den_tm = one - g_tm * g_tm * ph, den_te = one - g_te * g_te * ph;
+  if (cond)
+    *cond = fmin(*cond, fmin(cabs_(den_tm) / (R(1) + cabs_(g_tm * g_tm * ph)),
+                             cabs_(den_te) / (R(1) + cabs_(g_te * g_te * ph))));
   if (reflect) {
     c_tm = (g_tm * (one - ph)) / den_tm;
     c_te = (g_te * (one - ph)) / den_te;
@@ -214,11 +230,17 @@ __device__ void fresnel_pair(bool reflect, R theta_i, Cx<R> eps_t, Cx<R> ph, boo
 // the same operations, in the same order, as one sequential pass would.
 // R: real type of the rotation/Fresnel arithmetic.  Values of type R are
 // stored as doubles, which holds floats exactly.
+// FP32 field mode: interactions whose Fresnel denominators cancel below
+// this fraction of their terms take the FP64 coefficients (fresnel_pair).
+constexpr float kFresnelCond32 = 0.125f;
+
 struct SegTerms {
   double r;               // segment length (FP64)
   double st, ct, sp, cp;  // sin / cos of the direction's theta and phi
   double ctm[2], cte[2];  // TM / TE coefficients of the interaction at the start
   double inc[6];          // launch segment: the pattern's field (r, theta, phi)
+  int fp64_fresnel;       // FP32 mode: the coefficients came from the FP64 formula
+  int pad;
 };
 
 // The frame a segment starts in: the transmitter's for the launch segment,
@@ -250,36 +272,88 @@ __device__ void seg_terms(int i, const double (*pts)[3], const double* const* fr
   R vg[3] = {R(vg64[0]), R(vg64[1]), R(vg64[2])};
   R vl[3];
   mv(cur, vg, vl);
-  // CartesianToSpherical (VecMatDef.h:132-155); r is kept in FP64.  In FP64
-  // it is the length of the rotated vector, as in the reference.  With FP32
-  // frames it is the length of the global vector: a frame rounded to FP32 is
-  // orthonormal only to ~1e-7, which would move r by ~1e-7 r (1e-3 rad of
-  // phase for a 50 m segment at 28 GHz).
+  // CartesianToSpherical (VecMatDef.h:132-155); r is kept in FP64, the length
+  // of the vector rotated by the FP64 frame, as in the reference (the FP32
+  // mode forms it the same way below).
   if constexpr (sizeof(R) == sizeof(double)) {
     double vl64[3];
     for (int j = 0; j < 3; ++j)
       vl64[j] = (cur.m[3 * j] * vg64[0] + cur.m[3 * j + 1] * vg64[1]) + cur.m[3 * j + 2] * vg64[2];
     out.r = sqrt((vl64[0] * vl64[0] + vl64[1] * vl64[1]) + vl64[2] * vl64[2]);
-  } else {
-    out.r = sqrt((vg64[0] * vg64[0] + vg64[1] * vg64[1]) + vg64[2] * vg64[2]);
   }
   R th, ph;
   if (vl[0] == R(0) && vl[1] == R(0) && vl[2] == R(0)) th = R(K.pi_hi * 0.5);
   else th = atan2(sqrt(vl[0] * vl[0] + vl[1] * vl[1]), vl[2]);
   ph = atan2(vl[1], vl[0]);
   if (ph < R(0)) ph = R((double(ph) + 2.0 * K.pi_hi) + 2.0 * K.pi_lo);
-  out.st = double(sin(th));
-  out.ct = double(cos(th));
-  out.sp = double(sin(ph));
-  out.cp = double(cos(ph));
+  if constexpr (sizeof(R) == sizeof(double)) {
+    out.st = sin(th);
+    out.ct = cos(th);
+    out.sp = sin(ph);
+    out.cp = cos(ph);
+  } else {
+    // FP32 mode: the segment rotated into its frame in FP64 (a few FP64
+    // operations per segment), then the basis from its components, which
+    // keeps each of sin/cos theta, phi to a few FP32 ulps even for
+    // directions near the frame's axis, where an FP32 rotation or sin(theta)
+    // of theta near 0 or pi loses most of their relative precision
+    const double* fr = i == 0 ? txcs : frames[i - 1];
+    double w64[3];
+    float w[3];
+    for (int j = 0; j < 3; ++j) {
+      const double r0 = fr ? fr[3 * j] : (j == 0 ? 1.0 : 0.0);
+      const double r1 = fr ? fr[3 * j + 1] : (j == 1 ? 1.0 : 0.0);
+      const double r2 = fr ? fr[3 * j + 2] : (j == 2 ? 1.0 : 0.0);
+      w64[j] = (r0 * vg64[0] + r1 * vg64[1]) + r2 * vg64[2];
+      w[j] = float(w64[j]);
+    }
+    // the segment length as the FP64 mode (and the reference) takes it: of
+    // the vector rotated by the FP64 frame, which a triangle's single-
+    // precision file normal leaves orthonormal only to ~1e-7, so the
+    // global length would move the phase k*L of a long path by ~1e-4 rad
+    out.r = sqrt((w64[0] * w64[0] + w64[1] * w64[1]) + w64[2] * w64[2]);
+    const float rho = sqrtf(w[0] * w[0] + w[1] * w[1]);
+    const float len = sqrtf(rho * rho + w[2] * w[2]);
+    if (len > 0.0f) {
+      out.st = double(rho / len);
+      out.ct = double(w[2] / len);
+    } else {  // the zero vector: theta = pi/2, phi = 0 (VecMatDef.h:132-155)
+      out.st = 1.0;
+      out.ct = 0.0;
+    }
+    out.sp = rho > 0.0f ? double(w[1] / rho) : 0.0;
+    out.cp = rho > 0.0f ? double(w[0] / rho) : 1.0;
+    th = atan2(rho, w[2]);  // the pattern's angles
+    if (len == 0.0f) th = R(K.pi_hi * 0.5);
+    ph = atan2(w[1], w[0]);
+    if (ph < R(0)) ph = R((double(ph) + 2.0 * K.pi_hi) + 2.0 * K.pi_lo);
+  }
   for (int j = 0; j < 6; ++j) out.inc[j] = 0.0;
+  out.fp64_fresnel = 0;
+  out.pad = 0;
   if (i == 0) {
     Cx<R> inc[3] = {cx(R(0)), cx(R(0)), cx(R(0))};
-    if (antenna == 0) inc[0] = cx(R(0), R(sqrt(60.0 * pt)));
-    if (antenna == 1) inc[1] = cx(R(0), R(sqrt(60.0 * pt * 1.5)) * sin(th));
-    else if (antenna == 2)
-      inc[1] = cx(R(0), R(sqrt(60.0 * pt)) * (cos(R(K.pi_hi) * cos(th) / R(2)) / sin(th)));
-    else if (antenna == 3 && pat) {
+    if constexpr (sizeof(R) == sizeof(double)) {
+      if (antenna == 0) inc[0] = cx(R(0), R(sqrt(60.0 * pt)));
+      if (antenna == 1) inc[1] = cx(R(0), R(sqrt(60.0 * pt * 1.5)) * sin(th));
+      else if (antenna == 2)
+        inc[1] = cx(R(0), R(sqrt(60.0 * pt)) * (cos(R(K.pi_hi) * cos(th) / R(2)) / sin(th)));
+    } else {
+      // FP32: sin and cos of theta from the segment's components (accurate
+      // to ulps, unlike sin(theta) near the dipole axis, where theta's own
+      // FP32 rounding is most of sin(theta)).  The half-wave pattern's
+      // cos(pi/2 cos th) is sin(pi s) with s = sin^2(th/2) = st^2 / (2 (1 + ct))
+      // or cos^2(th/2) = st^2 / (2 (1 - ct)), whichever is at most 1/2: no
+      // cancellation near the axis, where cos(pi/2 cos th) -> 0.
+      const float st = float(out.st), ct = float(out.ct);
+      if (antenna == 0) inc[0] = cx(R(0), R(sqrt(60.0 * pt)));
+      if (antenna == 1) inc[1] = cx(R(0), R(sqrt(60.0 * pt * 1.5)) * st);
+      else if (antenna == 2) {
+        const float h2 = (st * st) / (2.0f * (ct >= 0.0f ? 1.0f + ct : 1.0f - ct));
+        inc[1] = cx(R(0), R(sqrt(60.0 * pt)) * (sinf(float(K.pi_hi) * h2) / st));
+      }
+    }
+    if (antenna == 3 && pat) {
       double a[4];
       pattern_at(*pat, double(th) * (180.0 / K.pi_hi), double(ph) * (180.0 / K.pi_hi), a);
       const double amp = sqrt(60.0 * pt);
@@ -293,31 +367,46 @@ __device__ void seg_terms(int i, const double (*pts)[3], const double* const* fr
   }
   Cx<R> ctm = cx(R(1)), cte = cx(R(1));
   if (kind[i] != 0) {
-    // AngleBetween(vecGlobal, current row 2) in radians (VecMatDef.h:56-77)
-    R a[3] = {vg[0], vg[1], vg[2]}, b[3] = {cur.m[6], cur.m[7], cur.m[8]};
-    R za = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
-    if (za > R(0)) { R s = sqrt(za); a[0] /= s; a[1] /= s; a[2] /= s; }
-    R zb = (b[0] * b[0] + b[1] * b[1]) + b[2] * b[2];
-    if (zb > R(0)) { R s = sqrt(zb); b[0] /= s; b[1] /= s; b[2] /= s; }
-    R ratio = (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
-    R ang;
-    if (ratio < R(0)) {
-      R e0 = -a[0] - b[0], e1 = -a[1] - b[1], e2 = -a[2] - b[2];
-      R y = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
-      ang = R((K.pi_hi - double(y)) + K.pi_lo);
+    // AngleBetween(vecGlobal, current row 2) in radians (VecMatDef.h:56-77),
+    // in FP64 for every precision: the reference's coefficients have poles
+    // (its angle convention puts some reflections past 90 degrees), and near
+    // one even the FP32 rounding of the angle moves a coefficient by 1e-5
+    const double* fr = i == 0 ? txcs : frames[i - 1];
+    double a[3] = {vg64[0], vg64[1], vg64[2]};
+    double b[3] = {fr ? fr[6] : 0.0, fr ? fr[7] : 0.0, fr ? fr[8] : 1.0};
+    double za = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
+    if (za > 0.0) { double s = sqrt(za); a[0] /= s; a[1] /= s; a[2] /= s; }
+    double zb = (b[0] * b[0] + b[1] * b[1]) + b[2] * b[2];
+    if (zb > 0.0) { double s = sqrt(zb); b[0] /= s; b[1] /= s; b[2] /= s; }
+    double ratio = (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+    double ang;
+    if (ratio < 0.0) {
+      double e0 = -a[0] - b[0], e1 = -a[1] - b[1], e2 = -a[2] - b[2];
+      double y = 2.0 * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / 2.0);
+      ang = (K.pi_hi - y) + K.pi_lo;
     } else {
-      R e0 = a[0] - b[0], e1 = a[1] - b[1], e2 = a[2] - b[2];
-      ang = R(2) * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / R(2));
+      double e0 = a[0] - b[0], e1 = a[1] - b[1], e2 = a[2] - b[2];
+      ang = 2.0 * asin(sqrt((e0 * e0 + e1 * e1) + e2 * e2) / 2.0);
     }
     const Material& m = mats[mat[i]];
     const Cx<double> eps64 = cx(m.eps_re, -1.0 * m.sigma / (K.e0 * 2.0 * K.pi_hi * freq));
     const Cx<R> eps_t = cx(R(eps64.re), R(eps64.im));
-    Cx<R> sph = cx(R(1));
-    if (!fresnel) {
-      const Cx<double> p64 = slab_phase(double(ang), eps64, lam64, m.width, 2.0 * K.pi_hi);
-      sph = cx(R(p64.re), R(p64.im));
+    Cx<double> p64 = cx(1.0);
+    if (!fresnel) p64 = slab_phase(ang, eps64, lam64, m.width, 2.0 * K.pi_hi);
+    const Cx<R> sph = cx(R(p64.re), R(p64.im));
+    R cond = R(1);
+    fresnel_pair<R>(kind[i] == 1, R(ang), eps_t, sph, fresnel, R(K.eta0), ctm, cte, &cond);
+    if constexpr (sizeof(R) != sizeof(double)) {
+      // near a pole the FP32 coefficients carry errors of ~2^-24 / cond:
+      // take them from the FP64 formula there
+      if (!(cond >= kFresnelCond32)) {
+        Cx<double> tm64, te64;
+        fresnel_pair<double>(kind[i] == 1, ang, eps64, p64, fresnel, K.eta0, tm64, te64);
+        ctm = cx(R(tm64.re), R(tm64.im));
+        cte = cx(R(te64.re), R(te64.im));
+        out.fp64_fresnel = 1;
+      }
     }
-    fresnel_pair<R>(kind[i] == 1, ang, eps_t, sph, fresnel, R(K.eta0), ctm, cte);
   }
   out.ctm[0] = double(ctm.re);
   out.ctm[1] = double(ctm.im);
@@ -329,13 +418,23 @@ __device__ void seg_terms(int i, const double (*pts)[3], const double* const* fr
 // (FieldCompute.cpp:99-148): E * exp(-j k L) / L, k L in FP64.
 // fp32_phase: take the path length and the phase k*L in FP32 (only to measure
 // what FP64 phase buys).
+//
+// kappa (optional, FP32 mode) receives the path's condition number for this
+// arithmetic: the largest field the path could carry, |E_launch| times each
+// interaction's largest coefficient magnitude (at least 1), over the field it
+// ends with.  Rotations and coefficients each err by a few ulps of the field
+// they act on, so the path's FP32 error is a few ulps of |E| times kappa
+// (measured: at most 7 ulps x kappa); kappa >> 1 means the path's field is
+// the small remainder of much larger terms.
 template <class R, bool fp32_phase = false>
 __device__ void path_combine(int n, const SegTerms* seg, const double (*pts)[3],
                              const double* const* frames, const int* kind, const double* txcs,
-                             double freq, const FieldConsts& K, Cx<double>* out) {
+                             double freq, const FieldConsts& K, Cx<double>* out,
+                             float* kappa = nullptr) {
   const double lam64 = 2.99792458e8 / freq;
   Cx<R> tot[3] = {cx(R(0)), cx(R(0)), cx(R(0))};
   double L = 0.0;
+  float gain = 1.0f, in0 = 0.0f;
   for (int i = 0; i < n; ++i) {
     const SegTerms& t = seg[i];
     const M3<R> cur = start_frame<R>(i, frames, txcs);
@@ -345,7 +444,10 @@ __device__ void path_combine(int n, const SegTerms* seg, const double (*pts)[3],
     const M3<R> T{{st * cp, ct * cp, -sp, st * sp, ct * sp, cp, ct, -st, R(0)}};
     Cx<R> inc[3];
     if (i == 0) {
-      for (int j = 0; j < 3; ++j) inc[j] = cx(R(t.inc[2 * j]), R(t.inc[2 * j + 1]));
+      for (int j = 0; j < 3; ++j) {
+        inc[j] = cx(R(t.inc[2 * j]), R(t.inc[2 * j + 1]));
+        in0 += float(t.inc[2 * j] * t.inc[2 * j] + t.inc[2 * j + 1] * t.inc[2 * j + 1]);
+      }
     } else {
       Cx<R> g[3];
       mtv(cur, tot, g);   // RotateToNewCoordSys(E, current, global) = current^T E
@@ -355,6 +457,8 @@ __device__ void path_combine(int n, const SegTerms* seg, const double (*pts)[3],
       tot[0] = inc[0];
       tot[1] = inc[1] * cx(R(t.ctm[0]), R(t.ctm[1]));
       tot[2] = inc[2] * cx(R(t.cte[0]), R(t.cte[1]));
+      if (kappa)
+        gain *= fmaxf(1.0f, fmaxf(float(hypot(t.ctm[0], t.ctm[1])), float(hypot(t.cte[0], t.cte[1]))));
     } else {
       tot[0] = inc[0];
       tot[1] = inc[1];
@@ -363,6 +467,11 @@ __device__ void path_combine(int n, const SegTerms* seg, const double (*pts)[3],
     Cx<R> c[3];
     mcv(T, tot, c);     // SphericalToCartesianVector = T
     mtv(cur, c, tot);   // back to global: current^T
+  }
+  if (kappa) {
+    float o = 0.0f;
+    for (int j = 0; j < 3; ++j) o += float(tot[j].re) * float(tot[j].re) + float(tot[j].im) * float(tot[j].im);
+    *kappa = o > 0.0f ? gain * sqrtf(in0) / sqrtf(o) : INFINITY;
   }
   // E * exp(-j k L) / L with k L in FP64 and reduced mod 2 pi before sin/cos
   if (fp32_phase) {

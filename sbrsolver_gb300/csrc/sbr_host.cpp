@@ -233,7 +233,7 @@ void build_search_bvh_ids(const float* v, int n_tri, SearchBVH& out);
 }  // namespace
 
 bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, HostScene& out,
-                   std::string& err) {
+                   std::string& err, bool host_tables) {
   out = HostScene();
   if (n_tri <= 0 || !v || !nrm) {
     err = "empty triangle list";
@@ -243,7 +243,8 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
   // over triangle ids on its own thread while the reference BVH is built, and
   // its leaves are mapped to depth-first ranks at the end.
   SearchBVH search;
-  std::thread search_thread([&] { build_search_bvh_ids(v, n_tri, search); });
+  std::thread search_thread;
+  if (host_tables) search_thread = std::thread([&] { build_search_bvh_ids(v, n_tri, search); });
   struct Joiner {
     std::thread& t;
     ~Joiner() {
@@ -270,13 +271,17 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
     }
   };
   const size_t nv = size_t(n_tri) * 3;
-  std::unordered_map<Key, int, KeyHash> ids;
-  ids.reserve(nv);
   std::vector<int> uid(nv);
-  for (size_t i = 0; i < nv; ++i) {
-    Key k{v[3 * i], v[3 * i + 1], v[3 * i + 2]};
-    auto it = ids.emplace(k, int(ids.size())).first;
-    uid[i] = it->second;
+  if (host_tables) {
+    std::unordered_map<Key, int, KeyHash> ids;
+    ids.reserve(nv);
+    for (size_t i = 0; i < nv; ++i) {
+      Key k{v[3 * i], v[3 * i + 1], v[3 * i + 2]};
+      auto it = ids.emplace(k, int(ids.size())).first;
+      uid[i] = it->second;
+    }
+  } else {  // merged on the device; the ids here only need to be distinct
+    for (size_t i = 0; i < nv; ++i) uid[i] = int(i);
   }
   std::vector<int> vidx;
   std::vector<size_t> src;
@@ -327,8 +332,9 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
   }
   out.extent = *std::max_element(slice_ext.begin(), slice_ext.end());
 
-  // Coplanar ids (Preprocessor.cpp:116-246).
+  // Coplanar ids (Preprocessor.cpp:116-246), unless the device builds them.
   const int nt = int(out.tris.size());
+  if (host_tables) {
   std::vector<int> parent(nt);
   std::iota(parent.begin(), parent.end(), 0);
   auto find = [&](int a) {
@@ -369,6 +375,7 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
     int r = find(t);
     if (comp[r] < 0) comp[r] = next++;
     out.tris[t].cop = comp[r];
+  }
   }
 
   // SAH BVH with the reference's splits; nodes renumbered depth-first.  Every
@@ -506,12 +513,18 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
       st.push_back({bn[it.b].c0, me, it.depth + 1, me, 0});
     }
   }
-  search_thread.join();
-  out.search = std::move(search);
-  std::vector<int> rank_of(out.tris.size());
-  for (size_t r = 0; r < out.dfs_tris.size(); ++r) rank_of[size_t(out.dfs_tris[r])] = int(r);
-  for (int& o : out.search.order) o = rank_of[size_t(o)];
+  if (host_tables) {
+    search_thread.join();
+    out.search = std::move(search);
+    map_search_order(out);
+  }
   return true;
+}
+
+void map_search_order(HostScene& H) {
+  std::vector<int> rank_of(H.tris.size());
+  for (size_t r = 0; r < H.dfs_tris.size(); ++r) rank_of[size_t(H.dfs_tris[r])] = int(r);
+  for (int& o : H.search.order) o = rank_of[size_t(o)];
 }
 
 namespace {
@@ -595,8 +608,10 @@ struct SearchBuild {
       // cost of a node relative to its leaf: one box test per triangle saved
       const float leaf_cost = box.area() * n;
       if (best >= 0 && (n > 7 || best_cost + box.area() < leaf_cost)) {
-        mid = int(std::partition(ord.begin() + b, ord.begin() + e,
-                                 [&](int p) { return bin_of(p) <= best; }) -
+        // stable, so the leaf order is a function of the input alone (the
+        // device build reproduces it)
+        mid = int(std::stable_partition(ord.begin() + b, ord.begin() + e,
+                                        [&](int p) { return bin_of(p) <= best; }) -
                   ord.begin());
       } else if (n <= 7) {
         return leaf(b, n);
@@ -607,8 +622,12 @@ struct SearchBuild {
     if (depth > 48) mid = -1;  // keep the tree shallow enough for the traversal stack
     if (mid <= b || mid >= e) {  // no usable SAH split: median along the axis
       mid = b + n / 2;
-      std::nth_element(ord.begin() + b, ord.begin() + mid, ord.begin() + e,
-                       [&](int x, int y) { return cen[3 * x + ax] < cen[3 * y + ax]; });
+      // ordered by (centroid, triangle id): no ties, so the halves are
+      // determined by the input alone
+      std::sort(ord.begin() + b, ord.begin() + e, [&](int x, int y) {
+        const float cx = cen[3 * x + ax], cy = cen[3 * y + ax];
+        return cx < cy || (cx == cy && x < y);
+      });
     }
     const int me = int(out->nodes.size());
     out->nodes.emplace_back();
@@ -639,10 +658,13 @@ void build_search_bvh_ids(const float* v, int n_tri, SearchBVH& out) {
   sb.blo.resize(3 * size_t(n));
   sb.bhi.resize(3 * size_t(n));
   sb.cen.resize(3 * size_t(n));
+  // -0 is read as +0 (they compare equal; the boxes then do not depend on
+  // which of the two a min or max met first, so the device build matches)
+  auto pz = [](float x) { return x == 0.0f ? 0.0f : x; };
   for (int t = 0; t < n; ++t) {
     const float* p = v + 9 * size_t(t);
     for (int a = 0; a < 3; ++a) {
-      const float x = p[a], y = p[3 + a], z = p[6 + a];
+      const float x = pz(p[a]), y = pz(p[3 + a]), z = pz(p[6 + a]);
       sb.blo[3 * t + a] = std::min({x, y, z});
       sb.bhi[3 * t + a] = std::max({x, y, z});
       sb.cen[3 * t + a] = 0.5f * (sb.blo[3 * t + a] + sb.bhi[3 * t + a]);

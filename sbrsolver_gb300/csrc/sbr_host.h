@@ -67,8 +67,14 @@ bool read_stl(const std::string& path, std::vector<float>& v, std::vector<float>
 
 // Triangle soup -> prepared scene.  mat may be null (all 0).  The merge drops
 // facets whose vertices collapse, exactly like the reference reader.
+// host_tables = false leaves the coplanar ids (HostTri::cop) and the search
+// BVH to the caller (the device builds them), and skips the vertex merge
+// they need.
 bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, HostScene& out,
-                   std::string& err);
+                   std::string& err, bool host_tables = true);
+
+// The search BVH's triangle ids -> depth-first ranks of the reference BVH.
+void map_search_order(HostScene& H);
 
 // Builds H.search from the triangles in depth-first rank order.
 void build_search_bvh(HostScene& H);

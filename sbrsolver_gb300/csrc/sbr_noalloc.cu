@@ -110,7 +110,9 @@ __global__ void k_scatter(const int* recv, int n, int n_rx, int* s) {
 
 // The sum of one receiver's paths in the given order: FP64 for
 // SBR_FIELD_FP64, compensated FP32 (Neumaier) for both FP32 precisions,
-// exactly as the solve's own per-receiver sum (k_rx_sum) forms it.
+// exactly as the solve's own per-receiver sum (k_rx_sum) forms it (for the
+// receivers the solve's FP32 error bound certifies; it sums the others in
+// FP64).
 template <class Idx>
 __device__ void sum_in_order(Idx idx, int n, const double* pf, int precision, double* out) {
   if (precision != SBR_FIELD_FP64) {

@@ -171,7 +171,16 @@ struct FieldArgs {
   double* path_pts;     // (kMaxDepth + 2) * 3 per survivor
   SegTerms* seg;        // (kMaxDepth + 1) per survivor
   int* path_mat;        // (kMaxDepth + 1) per survivor: material of each ray's start
+  // FP32 field mode: bound on each component's absolute error per survivor
+  // (0: computed in FP64; -1: no bound, the FP32-phase study mode)
+  double* path_bound;
+  const int* rx_flag;   // receivers whose paths k_escalate recomputes in FP64
+  unsigned long long* fstat;  // [0] paths whose field FP32 mode took in FP64, [1] receivers
 };
+
+// FP32 field mode: a path whose condition number (path_combine's kappa)
+// exceeds this is computed in FP64.
+constexpr float kKappaMax32 = 32.0f;
 
 // Barycentric distance of a point (on the triangle's plane) from the
 // triangle's edges is below tol: min(u, v, 1-u-v) < tol.
@@ -279,19 +288,70 @@ __global__ void k_combine(FieldArgs A) {
     const TxParams& P = A.txp[A.rx_req[sv.rx]];
     PathView v;
     path_view(A, i, v);
-    const SegTerms* seg = A.seg + size_t(i) * (kMaxDepth + 1);
+    SegTerms* seg = A.seg + size_t(i) * (kMaxDepth + 1);
     Cx<double> e[3];
     const int prec = A.precision < 0 ? P.precision : A.precision;
-    if (prec == 2)
+    double bound = 0.0;
+    if (prec == 2) {
       path_combine<float, true>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e);
-    else if (prec == 1)
-      path_combine<float>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e);
-    else
+      bound = -1.0;
+    } else if (prec == 1) {
+      float kappa = 0.0f;
+      path_combine<float>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e, &kappa);
+      bool pole = false;
+      for (int r = 0; r < v.n; ++r) pole |= seg[r].fp64_fresnel != 0;
+      if (pole || !(kappa <= kKappaMax32)) {
+        // an ill-conditioned path: its terms and field again, in FP64
+        const PatternTab pat{P.pat, P.pat_nt, P.pat_np, P.pat_dt, P.pat_dp};
+        for (int r = 0; r < v.n; ++r)
+          seg_terms<double>(r, v.pts, v.frames, v.kind, v.mat, A.sc.mats, P.txcs, P.freq, P.pt,
+                            P.antenna, P.fresnel != 0, A.K, seg[r], &pat);
+        path_combine<double>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e);
+        atomicAdd(&A.fstat[0], 1ull);
+      } else {
+        // each component errs by at most (7 kappa) ulps of |E| (measured on
+        // every path of the urban canyon); the bound takes 16 kappa, plus
+        // the FP32 rounding of the path field when the sum reads it
+        const double mag = sqrt(e[0].re * e[0].re + e[0].im * e[0].im + e[1].re * e[1].re +
+                                e[1].im * e[1].im + e[2].re * e[2].re + e[2].im * e[2].im);
+        bound = (16.0 * double(kappa) + 1.0) * 0x1p-24 * mag;
+      }
+    } else {
       path_combine<double>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e);
+    }
+    if (A.path_bound) A.path_bound[i] = bound;
     for (int j = 0; j < 3; ++j) {
       A.path_field[6 * i + 2 * j] = e[j].re;
       A.path_field[6 * i + 2 * j + 1] = e[j].im;
     }
+  }
+}
+
+// FP32 field mode, receivers k_rx_sum could not certify: every path of such
+// a receiver gets its terms and field again in FP64 (k_rx_sum then sums the
+// receiver in FP64).
+__global__ void k_escalate(FieldArgs A) {
+  const unsigned long long ns = min(A.ctr->survivors, A.cap);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ns;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const Survivor sv = A.surv[i];
+    if (!A.rx_flag[sv.rx] || A.path_bound[i] == 0.0) continue;  // taken in FP64 already
+    const TxParams& P = A.txp[A.rx_req[sv.rx]];
+    PathView v;
+    path_view(A, i, v);
+    SegTerms* seg = A.seg + size_t(i) * (kMaxDepth + 1);
+    const PatternTab pat{P.pat, P.pat_nt, P.pat_np, P.pat_dt, P.pat_dp};
+    for (int r = 0; r < v.n; ++r)
+      seg_terms<double>(r, v.pts, v.frames, v.kind, v.mat, A.sc.mats, P.txcs, P.freq, P.pt,
+                        P.antenna, P.fresnel != 0, A.K, seg[r], &pat);
+    Cx<double> e[3];
+    path_combine<double>(v.n, seg, v.pts, v.frames, v.kind, P.txcs, P.freq, A.K, e);
+    for (int j = 0; j < 3; ++j) {
+      A.path_field[6 * i + 2 * j] = e[j].re;
+      A.path_field[6 * i + 2 * j + 1] = e[j].im;
+    }
+    A.path_bound[i] = 0.0;
+    atomicAdd(&A.fstat[0], 1ull);
   }
 }
 
@@ -318,10 +378,22 @@ __global__ void k_surv_scatter(const Survivor* surv, const Counters* ctr, unsign
 // Sort each receiver's survivors by (launch, BFS) rank and sum their fields in
 // that order: FP64, or compensated FP32 (Neumaier) for the FP32 precisions.
 // precision -1 takes each receiver's request precision, 0 forces FP64.
+//
+// FP32 field mode (precision 1, with path_bound): the receiver's error bound
+// is the sum of its paths' bounds plus the compensated sum's own rounding
+// (2 ulps of the result).  The receiver is certified when that bound is
+// within half the field tolerance (1e-4 relative magnitude) of each
+// component, or, for a component below 1e-9 of the receiver's largest, of
+// that largest one; bound[r] then states it.  Otherwise rx_flag[r] is set:
+// k_escalate recomputes its paths in FP64 and a second call (only = rx_flag,
+// force_precision 0) sums it in FP64, with bound 0.
 __global__ void k_rx_sum(const Survivor* surv, const int* starts, int* order, int n_rx,
                          const double* path_field, int force_precision, const int* rx_req,
-                         const TxParams* txp, double* field) {
+                         const TxParams* txp, double* field, const double* path_bound = nullptr,
+                         double* bound = nullptr, int* rx_flag = nullptr,
+                         unsigned long long* fstat = nullptr, const int* only = nullptr) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rx; r += gridDim.x * blockDim.x) {
+    if (only && !only[r]) continue;
     const int precision = force_precision < 0 ? txp[rx_req[r]].precision : force_precision;
     const int b = starts[r], e = starts[r + 1];
     for (int i = b + 1; i < e; ++i) {
@@ -336,19 +408,47 @@ __global__ void k_rx_sum(const Survivor* surv, const int* starts, int* order, in
     }
     if (precision != 0) {  // both FP32 modes: compensated FP32 sum
       float s[6] = {0, 0, 0, 0, 0, 0}, c[6] = {0, 0, 0, 0, 0, 0};
-      for (int i = b; i < e; ++i)
+      double B = 0.0;
+      for (int i = b; i < e; ++i) {
         for (int k = 0; k < 6; ++k) {
           const float x = float(path_field[6 * size_t(order[i]) + k]);
           const float t = s[k] + x;
           c[k] += fabsf(s[k]) >= fabsf(x) ? (s[k] - t) + x : (x - t) + s[k];
           s[k] = t;
         }
-      for (int k = 0; k < 6; ++k) field[6 * size_t(r) + k] = double(s[k]) + double(c[k]);
+        if (path_bound) {
+          const double pb = path_bound[order[i]];
+          B = (pb < 0.0 || B < 0.0) ? -1.0 : B + pb;
+        }
+      }
+      double f[6];
+      for (int k = 0; k < 6; ++k) f[k] = field[6 * size_t(r) + k] = double(s[k]) + double(c[k]);
+      if (path_bound && bound) {
+        if (precision != 1 || B < 0.0) {
+          bound[r] = -1.0;  // FP32-phase study mode: no bound
+        } else {
+          double mag[3], big = 0.0;
+          for (int j = 0; j < 3; ++j) {
+            mag[j] = sqrt(f[2 * j] * f[2 * j] + f[2 * j + 1] * f[2 * j + 1]);
+            big = fmax(big, mag[j]);
+          }
+          B = B * (1.0 + 1e-6) + 0x1p-23 * big;
+          bool ok = true;
+          for (int j = 0; j < 3; ++j)
+            ok &= B <= 0.5e-4 * (mag[j] > 1e-9 * big ? mag[j] : big);
+          bound[r] = B;
+          if (!ok) {
+            rx_flag[r] = 1;
+            atomicAdd(&fstat[1], 1ull);
+          }
+        }
+      }
     } else {
       double s[6] = {0, 0, 0, 0, 0, 0};
       for (int i = b; i < e; ++i)
         for (int k = 0; k < 6; ++k) s[k] = __dadd_rn(s[k], path_field[6 * size_t(order[i]) + k]);
       for (int k = 0; k < 6; ++k) field[6 * size_t(r) + k] = s[k];
+      if (bound) bound[r] = 0.0;
     }
   }
 }

@@ -626,3 +626,244 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
 }
 
 }  // namespace sbr
+
+namespace sbr {
+
+// ---- FP64 resolution with the rays in shared memory ----------------------
+//
+// The same resolution as k_trace, scheduled so the FP64 work runs on full
+// warps.  k_trace keeps one ray per lane, so a warp's FP64 instructions
+// serve only the lanes whose ray has a test (or a node to write) due that
+// round: about a third of the lanes, measured.  Here each warp keeps
+// kPoolSlots rays in shared memory, twice its lanes; every round it lists
+// the slots with a test due and hands them out to its lanes in order (the
+// n-th lane takes the n-th listed slot), then lists the resolved slots and
+// hands those out for the node record and children, then refills the empty
+// slots (one atomic per warp).  A ray's tests still run one at a time in
+// ascending order of their lower bounds, so every decision is k_trace's.
+constexpr int kPoolSlots = 64;
+constexpr int kPoolWarps = 4;  // warps per block
+
+struct PoolSlots {  // one warp's slots, structure of arrays
+  double o[3][kPoolSlots], d[3][kPoolSlots];
+  double total[kPoolSlots], S[kPoolSlots];
+  double bt[kPoolSlots], bdist[kPoolSlots], bp[3][kPoolSlots];
+  float o32[3][kPoolSlots], d32[3][kPoolSlots];
+  float ct[kCand][kPoolSlots];
+  int cr[kCand][kPoolSlots];
+  int brank[kPoolSlots], orank[kPoolSlots];
+  uint32_t parent[kPoolSlots], cls[kPoolSlots], cop[kPoolSlots], launch[kPoolSlots];
+  uint32_t heap[kPoolSlots], tx[kPoolSlots];
+  uint16_t rc[kPoolSlots], tc[kPoolSlots];
+  uint8_t nc[kPoolSlots], nx[kPoolSlots], active[kPoolSlots], pad[kPoolSlots];
+};
+
+// The position of the j-th (0-based) set bit of m, which has more than j
+// set bits: a binary search on the counts of bits below each split.
+__device__ __forceinline__ int nth_set_bit(unsigned m, int j) {
+  int p = 0;
+  for (int w = 16; w >= 1; w >>= 1) {
+    const int c = __popc(m & (((1u << w) - 1u) << p));  // set bits in [p, p + w)
+    if (c <= j) {
+      j -= c;
+      p += w;
+    }
+  }
+  return p;
+}
+
+// The position of the j-th (0-based) set bit of the 64-slot mask (m0, m1).
+__device__ __forceinline__ int nth_slot(unsigned m0, unsigned m1, int j) {
+  const int c0 = __popc(m0);
+  return j < c0 ? nth_set_bit(m0, j) : 32 + nth_set_bit(m1, j - c0);
+}
+
+__global__ void __launch_bounds__(32 * kPoolWarps, 3) k_trace_pool(TraceArgs A) {
+  if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
+  const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
+  const long long n = min(n_all, A.hi) - A.lo;
+  if (n <= 0) return;
+  extern __shared__ __align__(16) unsigned char pool_smem[];
+  PoolSlots& P = reinterpret_cast<PoolSlots*>(pool_smem)[threadIdx.x >> 5];
+  const unsigned lane = lane_id();
+  TraceStats st{0, 0};
+  P.active[lane] = 0;
+  P.active[lane + 32] = 0;
+  bool exhausted = false;
+  __syncwarp();
+  while (true) {
+    // ---- refill the empty slots
+    const unsigned e0 = __ballot_sync(0xffffffffu, !P.active[lane]);
+    const unsigned e1 = __ballot_sync(0xffffffffu, !P.active[lane + 32]);
+    const int n_empty = __popc(e0) + __popc(e1);
+    if (!exhausted && n_empty > 0) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(A.work, (unsigned long long)n_empty);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((long long)base + n_empty >= n) exhausted = true;
+      for (int j = int(lane); j < n_empty; j += 32) {
+        const long long k = (long long)base + j;
+        if (k >= n) break;
+        const int s = nth_slot(e0, e1, j);
+        const long long i = A.lo + k;
+        RayRec r;
+        if (A.depth == 0) {
+          int q;
+          long long li;
+          root_ray(A.txp, A.n_tx, A.dirs, i, r.o, r.d, q, li);
+          r.total = 0.0;
+          r.S = 0.0;
+          r.parent = 0xFFFFFFFFu;
+          r.orank = -1;
+          r.cls = kRootBase + uint32_t(q);
+          r.cop = kRootClass;
+          r.launch = uint32_t(li);
+          r.heap = 1;
+          r.rc = r.tc = 0;
+          r.tx = uint32_t(q);
+        } else {
+          r = A.in[i];
+        }
+        for (int a = 0; a < 3; ++a) {
+          P.o[a][s] = r.o[a];
+          P.d[a][s] = r.d[a];
+        }
+        P.total[s] = r.total;
+        P.S[s] = r.S;
+        P.parent[s] = r.parent;
+        P.cls[s] = r.cls;
+        P.cop[s] = r.cop;
+        P.launch[s] = r.launch;
+        P.heap[s] = r.heap;
+        P.rc[s] = r.rc;
+        P.tc[s] = r.tc;
+        P.tx[s] = r.tx;
+        P.orank[s] = r.orank;
+        const float4* f = reinterpret_cast<const float4*>(A.ray32 + k);
+        const float4 fo = f[0], fd = f[1];
+        P.o32[0][s] = fo.x;
+        P.o32[1][s] = fo.y;
+        P.o32[2][s] = fo.z;
+        P.d32[0][s] = fd.x;
+        P.d32[1][s] = fd.y;
+        P.d32[2][s] = fd.z;
+        const int nc = A.ncand[k];
+        P.nc[s] = uint8_t(nc);
+        if (nc != kFindFallback) {
+          // contenders by ascending lower bound (stable insertion)
+          float ct[kCand];
+          int cr[kCand];
+          const uint2* cand = A.cand + size_t(k) * kCand;
+          for (int c = 0; c < nc; ++c) {
+            const uint2 e = cand[c];
+            const float t = __uint_as_float(e.y);
+            int m = c - 1;
+            while (m >= 0 && ct[m] > t) {
+              ct[m + 1] = ct[m];
+              cr[m + 1] = cr[m];
+              --m;
+            }
+            ct[m + 1] = t;
+            cr[m + 1] = int(e.x);
+          }
+          for (int c = 0; c < nc; ++c) {
+            P.ct[c][s] = ct[c];
+            P.cr[c][s] = cr[c];
+          }
+        }
+        P.nx[s] = 0;
+        P.brank[s] = INT_MAX;
+        P.bdist[s] = __longlong_as_double(0x7ff0000000000000ll);
+        P.bt[s] = P.bdist[s];
+        P.active[s] = 1;
+      }
+    }
+    __syncwarp();
+    const unsigned a0 = __ballot_sync(0xffffffffu, P.active[lane]);
+    const unsigned a1 = __ballot_sync(0xffffffffu, P.active[lane + 32]);
+    if (!(a0 | a1) && exhausted) break;
+    // ---- one FP64 test for every slot with one due, slots handed out in order
+    auto due = [&](int s) {
+      return P.active[s] && P.nc[s] != kFindFallback && P.nx[s] < P.nc[s];
+    };
+    const unsigned t0 = __ballot_sync(0xffffffffu, due(int(lane)));
+    const unsigned t1 = __ballot_sync(0xffffffffu, due(int(lane) + 32));
+    const int n_test = __popc(t0) + __popc(t1);
+    for (int j = int(lane); j < n_test; j += 32) {
+      const int s = nth_slot(t0, t1, j);
+      const int rk = P.cr[P.nx[s]][s];
+      P.nx[s] = uint8_t(P.nx[s] + 1);
+      ++st.fp64_tri;
+      const double o[3] = {P.o[0][s], P.o[1][s], P.o[2][s]};
+      const double d[3] = {P.d[0][s], P.d[1][s], P.d[2][s]};
+      double t, Q[3], dist;
+      if (mt64(A.sc.tri64[rk], o, d, t, Q, dist) &&
+          (dist < P.bdist[s] || (dist == P.bdist[s] && rk < P.brank[s]))) {
+        P.bdist[s] = dist;
+        P.bt[s] = t;
+        P.bp[0][s] = Q[0];
+        P.bp[1][s] = Q[1];
+        P.bp[2][s] = Q[2];
+        P.brank[s] = rk;
+      }
+    }
+    __syncwarp();
+    // ---- resolved slots: no further contender can reach the best distance
+    auto resolved = [&](int s) {
+      if (!P.active[s]) return false;
+      if (P.nc[s] == kFindFallback) return true;
+      const int nx = P.nx[s];
+      return !(nx < P.nc[s] &&
+               (P.brank[s] == INT_MAX || P.ct[nx][s] <= float(P.bt[s]) * (1.0f + kTieSlack) + 1e-30f));
+    };
+    const unsigned r0 = __ballot_sync(0xffffffffu, resolved(int(lane)));
+    const unsigned r1 = __ballot_sync(0xffffffffu, resolved(int(lane) + 32));
+    const int n_res = __popc(r0) + __popc(r1);
+    for (int j0 = 0; j0 < n_res; j0 += 32) {
+      const int j = j0 + int(lane);
+      if (j < n_res) {
+        const int s = nth_slot(r0, r1, j);
+        RayRec r;
+        for (int a = 0; a < 3; ++a) {
+          r.o[a] = P.o[a][s];
+          r.d[a] = P.d[a][s];
+        }
+        r.total = P.total[s];
+        r.S = P.S[s];
+        r.parent = P.parent[s];
+        r.cls = P.cls[s];
+        r.cop = P.cop[s];
+        r.launch = P.launch[s];
+        r.heap = P.heap[s];
+        r.rc = P.rc[s];
+        r.tc = P.tc[s];
+        r.tx = P.tx[s];
+        r.orank = P.orank[s];
+        const float3 o32 = make_float3(P.o32[0][s], P.o32[1][s], P.o32[2][s]);
+        const float3 d32 = make_float3(P.d32[0][s], P.d32[1][s], P.d32[2][s]);
+        Hit best;
+        best.rank = P.brank[s];
+        best.dist = P.bdist[s];
+        best.t = P.bt[s];
+        best.p[0] = P.bp[0][s];
+        best.p[1] = P.bp[1][s];
+        best.p[2] = P.bp[2][s];
+        bool hit;
+        if (P.nc[s] == kFindFallback) {  // more contenders than kept: one-pass search
+          hit = closest_hit(A.sc, r.o, r.d, best, st, &A.ctr->overflow);
+        } else {
+          hit = best.rank != INT_MAX && reachable_or_exact(A.sc, r, o32, d32, best, st,
+                                                            &A.ctr->overflow);
+        }
+        finish_ray(A, r, o32, d32, hit, best);
+        P.active[s] = 0;
+      }
+      // finish_ray's warp-wide reservations need every lane: the loop bound is uniform
+    }
+    __syncwarp();
+  }
+  if (st.fp64_tri) atomicAdd(&A.ctr->fp64_tri, (unsigned long long)st.fp64_tri);
+  if (st.fallback) atomicAdd(&A.ctr->fallback, (unsigned long long)st.fallback);
+}
+
+}  // namespace sbr

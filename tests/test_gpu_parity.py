@@ -219,3 +219,47 @@ def test_near_edge_paths_listed(built):
     assert sorted(seen) == [0, 1, 2, 3]
     assert seen[0] < 1e-12 and 4e-7 < seen[1] < 6e-7 and 4e-6 < seen[2] < 6e-6 and seen[3] > 1e-3
     assert got.count(1) == 2 and res.counts["near_edge_paths"] == 2
+
+
+def test_launch_shapes_do_not_change_results(built):
+    """Launch shapes (sbr_tuning) change only speed: extreme shapes (65,536-ray
+    chunks, so the level-7 request's launch rays span three launch pairs; one
+    FP64 resolution block per SM; refills at 4 idle lanes every 8 steps) give
+    bit-identical paths and fields, and the autotuner's choice too."""
+    wl = scenes.urban_scene(level=6, rx_pitch=50.0, max_reflection=4, max_transmission=1)
+    b = scenes.urban_scene(level=7, rx_pitch=100.0, max_reflection=3, max_transmission=0)
+    b.request.tx = (120.0, -80.0, 15.0)
+    sc = api.DeviceScene.from_scene(wl.scene)
+    qs = [api.request_from_workload(wl.request), api.request_from_workload(b.request)]
+    ref = api.solve(sc, qs, with_paths="arrays")
+    assert sc.tuning(qs) == sc.tuning()  # no mix tuned yet: the scene default
+    sc.set_tuning(find_steps=8, find_refill=4, find_blocks_per_sm=2, trace_blocks_per_sm=1,
+                  capture_blocks_per_sm=1, trace_chunk_log2=16)
+    t = sc.tuning(qs)
+    assert t["trace_chunk_log2"] == 16 and t["trace_blocks_per_sm"] == 1
+    odd = api.solve(sc, qs, with_paths="arrays")
+    assert api.same_path_set(odd.paths, ref.paths)
+    np.testing.assert_array_equal(odd.field, ref.field)
+    assert odd.counts["gpu_kernels"] > ref.counts["gpu_kernels"]  # more launch pairs
+    # both FP64 resolution kernels (a ray per lane; 64 rays per warp in shared
+    # memory), with the default shapes and the extreme ones
+    for shapes in ({}, dict(find_steps=8, find_refill=4, trace_chunk_log2=16)):
+        for kernel in (1, 2):
+            sc.set_tuning(trace_kernel=kernel, **shapes)
+            assert sc.tuning(qs)["trace_kernel"] == kernel
+            r = api.solve(sc, qs, with_paths="arrays")
+            assert api.same_path_set(r.paths, ref.paths), (kernel, shapes)
+            np.testing.assert_array_equal(r.field, ref.field)
+            assert r.counts["fp64_triangle_tests"] == ref.counts["fp64_triangle_tests"]
+    sc.set_tuning()  # back to the defaults
+    chosen = sc.autotune(qs, rounds=1)
+    assert chosen["device_ms"] > 0
+    assert {k: v for k, v in chosen.items() if k != "device_ms"} == sc.tuning(qs)
+    tuned = api.solve(sc, qs, with_paths="arrays")
+    assert api.same_path_set(tuned.paths, ref.paths)
+    np.testing.assert_array_equal(tuned.field, ref.field)
+    with pytest.raises(Exception):
+        sc.set_tuning(find_refill=33)
+    with pytest.raises(Exception):
+        sc.set_tuning(trace_kernel=3)
+    sc.close()

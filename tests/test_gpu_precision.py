@@ -101,3 +101,50 @@ def test_mixed_precision_batch(built):
         np.testing.assert_array_equal(rb.field[k * n:(k + 1) * n], alone.field)
     assert not np.array_equal(rb.field[n:2 * n], rb.field[:n])  # FP32 differs in low bits
     sc.close()
+
+
+@pytest.mark.parametrize("case", ["urban_L6_R6T1", "urban_L5_slab", "large_L7"])
+def test_fp32_bound_holds_and_certifies(built, case):
+    """The FP32 mode's stated per-receiver bound (sbr_result_field_bound)
+    really bounds every component's error against the FP64 field of the same
+    paths; receivers it could not certify were recomputed in FP64 (bound 0,
+    bit-equal to the FP64 field); so every component is within 1e-4 / 1e-3
+    rad.  The urban canyon at 28 GHz has receivers whose paths cancel to
+    1e-4 of their sum, which FP32 cannot resolve: those are the escalated
+    ones."""
+    if case == "urban_L6_R6T1":
+        wl = scenes.urban_scene(level=6, rx_pitch=10.0)
+    elif case == "urban_L5_slab":
+        wl = scenes.slab_walls(scenes.urban_scene(level=5, rx_pitch=25.0, max_reflection=3,
+                                                  max_transmission=2), (0.5, 0.2, 0.01))
+        wl.request.use_fresnel = False
+    else:
+        wl = scenes.large_scene(level=7)
+        wl.request.rx = wl.request.rx[::25].copy()
+    sc = api.DeviceScene.from_scene(wl.scene)
+    res = api.solve(sc, api.request_from_workload(wl.request, "fp32", field_check=True),
+                    with_paths=False)
+    sc.close()
+    b = res.field_bound
+    assert b is not None and np.all(b >= 0)
+    err = np.abs(res.field - res.field_fp64)
+    assert np.all(err <= b[:, None] * (1 + 1e-9) + 1e-300)
+    zero = b == 0
+    np.testing.assert_array_equal(res.field[zero], res.field_fp64[zero])
+    assert not field_close(res.field, res.field_fp64)
+    with_field = np.abs(res.field_fp64).max(axis=1) > 0
+    assert res.counts["fp64_field_receivers"] <= int((zero & with_field).sum())
+    assert int((~zero).sum()) > 0  # FP32 certified a part of the receivers itself
+    if case == "urban_L6_R6T1":
+        assert res.counts["fp64_field_receivers"] > 0
+
+
+def test_fp64_and_phase_study_bounds(built):
+    wl = scenes.urban_scene(level=4, rx_pitch=50.0)
+    sc = api.DeviceScene.from_scene(wl.scene)
+    r64 = api.solve(sc, api.request_from_workload(wl.request, "fp64"), with_paths=False)
+    rph = api.solve(sc, api.request_from_workload(wl.request, "fp32_phase"), with_paths=False)
+    sc.close()
+    assert np.all(r64.field_bound == 0)
+    has = np.abs(rph.field).max(axis=1) > 0
+    assert np.all(rph.field_bound[has] == -1)

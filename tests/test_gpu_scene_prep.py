@@ -1,0 +1,76 @@
+"""Scene preparation on the GPU (sbr_prep.cuh) against the host build.
+
+By default a scene's coplanar groups (Preprocessor.cpp:116-246), triangle
+frames and boxes (Triangle.cpp:37-70) and search BVH are built on the GPU
+while the host builds the reference BVH; SBR_SCENE_HOST_PREP builds them all
+on the host.  The two must give identical tables, bit for bit, and the
+same solve."""
+import time
+
+import numpy as np
+import pytest
+
+from sbrsolver_gb300 import api, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(name):
+    if name == "small":
+        return scenes.small_scene()
+    if name == "urban":
+        return scenes.urban_scene(level=5, rx_pitch=100.0)
+    wl = scenes.large_scene(level=5)
+    wl.request.rx = wl.request.rx[::100].copy()
+    return wl
+
+
+@pytest.mark.parametrize("name", ["small", "urban", "large"])
+def test_device_tables_equal_host_tables(built, name):
+    wl = _scene(name)
+    t0 = time.perf_counter()
+    host = api.DeviceScene.from_scene(wl.scene, host_prep=True)
+    t1 = time.perf_counter()
+    dev = api.DeviceScene.from_scene(wl.scene)
+    t2 = time.perf_counter()
+    print(f"{name}: {wl.scene.n_tri} triangles, host preparation {1e3 * (t1 - t0):.0f} ms, "
+          f"device {1e3 * (t2 - t1):.0f} ms")
+    np.testing.assert_array_equal(dev.coplanar_ids(), host.coplanar_ids())
+    np.testing.assert_array_equal(dev.mesh_order(), host.mesh_order())
+    for a, b in zip(dev.triangle_frames(), host.triangle_frames()):
+        np.testing.assert_array_equal(a.view(np.int64), b.view(np.int64))  # bit for bit
+    sa, sb = dev.search_bvh(), host.search_bvh()
+    assert sa["max_depth"] == sb["max_depth"]
+    np.testing.assert_array_equal(sa["order"], sb["order"])
+    np.testing.assert_array_equal(sa["nodes"], sb["nodes"])
+    assert len(sa["nodes"]) > 1
+    q = api.request_from_workload(wl.request)
+    ra = api.solve(dev, q, with_paths="arrays")
+    rb = api.solve(host, q, with_paths="arrays")
+    assert api.same_path_set(ra.paths, rb.paths) and ra.counts["paths"] > 0
+    np.testing.assert_array_equal(ra.field, rb.field)
+    dev.close()
+    host.close()
+
+
+def test_device_prep_edge_cases(built):
+    """One triangle, two triangles (the search BVH is a leaf), and a scene
+    with a degenerate triangle (refused, as the host refuses it)."""
+    wl = scenes.small_scene()
+    for n in (1, 2, 9):
+        mesh = api.Mesh(wl.scene.tri[:n], wl.scene.normal[:n], wl.scene.material_id[:n])
+        mats = [api.MaterialProperties(*m) for m in wl.scene.materials]
+        a = api.DeviceScene(mesh, mats)
+        b = api.DeviceScene(mesh, mats, host_prep=True)
+        np.testing.assert_array_equal(a.search_bvh()["nodes"], b.search_bvh()["nodes"])
+        np.testing.assert_array_equal(a.coplanar_ids(), b.coplanar_ids())
+        a.close()
+        b.close()
+    tri = wl.scene.tri.copy()
+    tri[3, 2] = tri[3, 1]  # two vertices of triangle 3 coincide
+    mesh = api.Mesh(tri, wl.scene.normal, wl.scene.material_id)
+    for host_prep in (False, True):
+        with pytest.raises(Exception) as e:
+            api.DeviceScene(mesh, [api.MaterialProperties(*m) for m in wl.scene.materials],
+                            host_prep=host_prep)
+        assert "degenerate" in str(e.value)

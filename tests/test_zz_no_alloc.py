@@ -14,6 +14,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
+from helpers import field_close
 from sbrsolver_gb300 import _lib, api, scenes
 
 pytestmark = pytest.mark.gpu
@@ -45,10 +46,18 @@ def test_noalloc_field_sum_matches_solve(built, precision):
     pf = torch.tensor(np.array([p["field"] for p in res.paths]).reshape(-1), dtype=torch.float64,
                       device="cuda")
     ref = np.stack([res.field.real, res.field.imag], -1).reshape(n_rx, 6)
+    # the solve's FP32 mode sums in FP64 the receivers its error bound could
+    # not certify (field_bound 0); this entry point always sums an FP32
+    # precision in compensated FP32, so those receivers agree within the
+    # field tolerance, every other receiver to the last bits
+    same = np.ones(n_rx, bool) if precision != "fp32" else res.field_bound != 0
     for _ in range(2):
         st, out = _call(lib, torch, recv, rank, pf, len(res.paths), n_rx, PRECISION[precision])
         _lib.check(st)
-        np.testing.assert_allclose(out.cpu().numpy().reshape(n_rx, 6), ref, rtol=1e-12, atol=0)
+        got = out.cpu().numpy().reshape(n_rx, 6)
+        np.testing.assert_allclose(got[same], ref[same], rtol=1e-12, atol=0)
+        c = np.ascontiguousarray(got).view(np.complex128).reshape(-1, 3)
+        assert not field_close(c, res.field)
     sc.close()
 
 
