@@ -1118,7 +1118,9 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         }
         CK(cudaEventRecord(W.tr_ev[2 * n_tr], st));
         if (resolved(tu).trace_kernel == 2) {
-          const long long need = (ta.hi - lo + 32 * kPoolSlots - 1) / (32 * kPoolSlots);
+          // one block per 128 rays at most, as k_trace: a small launch still
+          // spreads over many warps (each then fills only part of its slots)
+          const long long need = (ta.hi - lo + 127) / 128;
           const int grid = int(std::min<long long>(device_sms() * pool_fit(), std::max(1LL, need)));
           ++nl, k_trace_pool<<<grid, 32 * kPoolWarps, kPoolSmem, st>>>(ta);
         } else {

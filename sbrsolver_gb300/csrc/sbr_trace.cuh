@@ -635,14 +635,14 @@ namespace sbr {
 // warps.  k_trace keeps one ray per lane, so a warp's FP64 instructions
 // serve only the lanes whose ray has a test (or a node to write) due that
 // round: about a third of the lanes, measured.  Here each warp keeps
-// kPoolSlots rays in shared memory, twice its lanes; every round it lists
+// kPoolSlots rays in shared memory, more than its lanes; every round it lists
 // the slots with a test due and hands them out to its lanes in order (the
 // n-th lane takes the n-th listed slot), then lists the resolved slots and
 // hands those out for the node record and children, then refills the empty
 // slots (one atomic per warp).  A ray's tests still run one at a time in
 // ascending order of their lower bounds, so every decision is k_trace's.
-constexpr int kPoolSlots = 64;
-constexpr int kPoolWarps = 4;  // warps per block
+constexpr int kPoolSlots = 48;  // at most 64 (two ballot words)
+constexpr int kPoolWarps = 4;   // warps per block
 
 struct PoolSlots {  // one warp's slots, structure of arrays
   double o[3][kPoolSlots], d[3][kPoolSlots];
@@ -678,7 +678,7 @@ __device__ __forceinline__ int nth_slot(unsigned m0, unsigned m1, int j) {
   return j < c0 ? nth_set_bit(m0, j) : 32 + nth_set_bit(m1, j - c0);
 }
 
-__global__ void __launch_bounds__(32 * kPoolWarps, 3) k_trace_pool(TraceArgs A) {
+__global__ void __launch_bounds__(32 * kPoolWarps, 4) k_trace_pool(TraceArgs A) {
   if (A.ctr->overflow & kOvTrace) return;  // this solve will be repeated
   const long long n_all = rays_at_depth(A.ctr, A.depth, A.n_root, A.out_cap);
   const long long n = min(n_all, A.hi) - A.lo;
@@ -687,14 +687,15 @@ __global__ void __launch_bounds__(32 * kPoolWarps, 3) k_trace_pool(TraceArgs A) 
   PoolSlots& P = reinterpret_cast<PoolSlots*>(pool_smem)[threadIdx.x >> 5];
   const unsigned lane = lane_id();
   TraceStats st{0, 0};
+  const bool hi_slot = lane + 32 < unsigned(kPoolSlots);  // this lane's second slot exists
   P.active[lane] = 0;
-  P.active[lane + 32] = 0;
+  if (hi_slot) P.active[lane + 32] = 0;
   bool exhausted = false;
   __syncwarp();
   while (true) {
     // ---- refill the empty slots
     const unsigned e0 = __ballot_sync(0xffffffffu, !P.active[lane]);
-    const unsigned e1 = __ballot_sync(0xffffffffu, !P.active[lane + 32]);
+    const unsigned e1 = __ballot_sync(0xffffffffu, hi_slot && !P.active[lane + 32]);
     const int n_empty = __popc(e0) + __popc(e1);
     if (!exhausted && n_empty > 0) {
       unsigned long long base = 0;
@@ -780,14 +781,14 @@ __global__ void __launch_bounds__(32 * kPoolWarps, 3) k_trace_pool(TraceArgs A) 
     }
     __syncwarp();
     const unsigned a0 = __ballot_sync(0xffffffffu, P.active[lane]);
-    const unsigned a1 = __ballot_sync(0xffffffffu, P.active[lane + 32]);
+    const unsigned a1 = __ballot_sync(0xffffffffu, hi_slot && P.active[lane + 32]);
     if (!(a0 | a1) && exhausted) break;
     // ---- one FP64 test for every slot with one due, slots handed out in order
     auto due = [&](int s) {
       return P.active[s] && P.nc[s] != kFindFallback && P.nx[s] < P.nc[s];
     };
     const unsigned t0 = __ballot_sync(0xffffffffu, due(int(lane)));
-    const unsigned t1 = __ballot_sync(0xffffffffu, due(int(lane) + 32));
+    const unsigned t1 = __ballot_sync(0xffffffffu, hi_slot && due(int(lane) + 32));
     const int n_test = __popc(t0) + __popc(t1);
     for (int j = int(lane); j < n_test; j += 32) {
       const int s = nth_slot(t0, t1, j);
@@ -817,7 +818,7 @@ __global__ void __launch_bounds__(32 * kPoolWarps, 3) k_trace_pool(TraceArgs A) 
                (P.brank[s] == INT_MAX || P.ct[nx][s] <= float(P.bt[s]) * (1.0f + kTieSlack) + 1e-30f));
     };
     const unsigned r0 = __ballot_sync(0xffffffffu, resolved(int(lane)));
-    const unsigned r1 = __ballot_sync(0xffffffffu, resolved(int(lane) + 32));
+    const unsigned r1 = __ballot_sync(0xffffffffu, hi_slot && resolved(int(lane) + 32));
     const int n_res = __popc(r0) + __popc(r1);
     for (int j0 = 0; j0 < n_res; j0 += 32) {
       const int j = j0 + int(lane);
