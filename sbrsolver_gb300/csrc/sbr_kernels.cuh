@@ -48,7 +48,9 @@ __device__ __forceinline__ bool mt64(const Tri64& T, const double* o, const doub
   cross(d, T.e2, h);
   const double a = dot(T.e1, h);
   if (a > -kEps64 && a < kEps64) return false;
-  const double f = div(1.0, a);
+  // 1.0 / a (Triangle.cpp): the correctly rounded reciprocal is the same
+  // double as the correctly rounded quotient 1.0 / a
+  const double f = __drcp_rn(a);
   double s[3];
   sub3(o, T.v1, s);
   const double u = mul(f, dot(s, h));
