@@ -123,6 +123,10 @@ typedef struct sbr_counts {
                                    ill-conditioned path, or one of an uncertified receiver) */
   long long fp64_field_receivers; /* SBR_FIELD_FP32: receivers whose error bound could not
                                      certify the tolerance, recomputed and summed in FP64 */
+  long long pipeline_graph;     /* 1: the device pipeline ran as one CUDA graph launch (the
+                                   same pipeline, i.e. request structure, capacities and
+                                   launch shapes, ran before on this scene: captured the
+                                   second time, replayed after) */
 } sbr_counts;
 
 /* One surviving path; its rays are [ray_offset, ray_offset + n_rays) in the
@@ -351,6 +355,10 @@ typedef struct sbr_tuning {
   int trace_chunk_log2;      /* rays per search/resolution launch pair = 2^this, 16..26 (24) */
   int trace_kernel;          /* FP64 resolution: 1 = one ray per lane (registers), 2 = 64 rays
                                 per warp in shared memory, tests handed out to full warps */
+  int pipeline_graph;        /* 0 (default) or 1: a device pipeline that ran before (same
+                                request structure, capacities and shapes) is captured as a
+                                CUDA graph and replayed from then on; -1: every solve issues
+                                its operations one by one */
 } sbr_tuning;
 /* The scene's default shapes, used by request mixes sbr_autotune has not
  * tuned.  Values above what fits on an SM are clamped. */

@@ -70,7 +70,8 @@ class Counts(C.Structure):
                                              "capture_candidates", "ancestor_tests",
                                              "classes", "groups", "keys",
                                              "near_edge_paths", "gpu_kernels",
-                                             "fp64_field_paths", "fp64_field_receivers")]
+                                             "fp64_field_paths", "fp64_field_receivers",
+                                             "pipeline_graph")]
 
 
 class Path(C.Structure):
@@ -88,7 +89,8 @@ class Completion(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("find_steps", "find_refill", "find_blocks_per_sm",
                                         "trace_blocks_per_sm", "capture_blocks_per_sm",
-                                        "trace_chunk_log2", "trace_kernel")]
+                                        "trace_chunk_log2", "trace_kernel",
+                                        "pipeline_graph")]
 
 
 class Timing(C.Structure):

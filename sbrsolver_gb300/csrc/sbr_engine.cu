@@ -110,6 +110,32 @@ struct DBuf {
   }
 };
 
+// Pinned host buffer: the staging of what a solve uploads (a captured graph
+// copies from it when it replays).
+template <class T>
+struct HBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~HBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  void ensure(size_t want) {
+    if (want <= n) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    void* q = nullptr;
+    cudaError_t e = injected_alloc_failure() ? cudaErrorMemoryAllocation
+                                             : cudaMallocHost(&q, want * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw CudaError{e, "cudaMallocHost " + std::to_string(want * sizeof(T)) + " bytes"};
+    }
+    p = static_cast<T*>(q);
+    n = want;
+  }
+};
+
 static uint32_t next_pow2(uint64_t x) {
   uint64_t p = 1;
   while (p < x) p <<= 1;
@@ -164,6 +190,26 @@ struct Workspace {
   DBuf<uint2> cand;                    // FP32 search contenders, kCand per ray of a chunk
   DBuf<unsigned char> ncand;
   DBuf<unsigned long long> find_work;  // work counter of the running search launch
+  // pinned staging of a solve's uploads
+  HBuf<TxParams> h_txp;
+  HBuf<int> h_rxreq;
+  HBuf<double> h_rx;
+  HBuf<GridBuild> h_gb;
+  // the device pipeline as a CUDA graph: captured the second time the same
+  // pipeline (pipeline_key) runs, replayed whenever it comes again.  A few
+  // graphs are kept (the passes of a split batch, a serving loop's request
+  // mixes alternate); the least recently used one goes first.
+  struct PipelineGraph {
+    std::string key;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;      // kernel launches the graph holds
+    unsigned long long used = 0;
+  };
+  std::vector<PipelineGraph> graphs;
+  std::vector<std::string> seen;  // keys that ran eagerly, most recent last
+  unsigned long long graph_tick = 0;
+  long long pipeline_kernels = 0;  // kernels the last pipeline ran
   // capacities (grown from occupancy and on overflow)
   unsigned long long cap_nodes = 1 << 20, cap_queue = 1 << 19, cap_surv = 1 << 14;
   unsigned long long cap_corr = 1 << 16, cap_pairs = 1 << 20;
@@ -175,6 +221,10 @@ struct Workspace {
   double r_cls = 0.01, r_cop = 0.004, r_corr = 0.01, r_dd = 5e-4, r_surv = 5e-4, r_pairs = 0.1,
          r_cc = 0.01;
   ~Workspace() {
+    for (auto& g : graphs) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      if (g.graph) cudaGraphDestroy(g.graph);
+    }
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (fork) cudaEventDestroy(fork);
@@ -192,6 +242,7 @@ struct Tuning {
   int find_steps = 0, find_refill = 0, find_bps = 0, trace_bps = 0, capture_bps = 0;
   int chunk_log2 = 0;
   int trace_kernel = 0;  // FP64 resolution: 1 = k_trace (a ray per lane), 2 = k_trace_pool
+  int graph = 0;         // pipeline as a CUDA graph on repeat: 1 (0 = default), -1 = never
 };
 
 // A request mix's identity for the autotuner's cache: the sorted
@@ -609,6 +660,7 @@ static Tuning resolved(Tuning t) {
   if (t.chunk_log2 <= 0) t.chunk_log2 = 24;
   t.chunk_log2 = std::min(std::max(t.chunk_log2, 16), 26);
   if (t.trace_kernel <= 0 || t.trace_kernel > 2) t.trace_kernel = kDefaultTraceKernel;
+  t.graph = t.graph < 0 ? -1 : 1;
   return t;
 }
 
@@ -836,6 +888,123 @@ static FieldConsts field_consts() {
   return K;
 }
 
+// Everything the recorded pipeline's operations depend on besides the
+// contents of the staged uploads: the request structure (levels, depths,
+// receiver counts and offsets, field precisions, device receiver pointers),
+// the capacities, every buffer and scene pointer, the launch shapes and the
+// solve's flags.  Two solves with the same key run the same operations.
+static std::string pipeline_key(const SceneImpl& S, const Workspace& W, const sbr_request* reqs,
+                                const std::vector<TxParams>& tp, int n_req, int rx_total,
+                                long long launches, int max_depth, size_t cell_cap,
+                                long long chunk, const Tuning& tu, int stage_counts,
+                                bool field_check) {
+  std::string k;
+  auto put = [&k](const void* v, size_t n) { k.append(static_cast<const char*>(v), n); };
+  auto put_v = [&put](auto v) { put(&v, sizeof v); };
+  put(&S.dev, sizeof S.dev);
+  put_v(n_req);
+  put_v(rx_total);
+  put_v(launches);
+  put_v(max_depth);
+  put_v(cell_cap);
+  put_v(chunk);
+  put_v(stage_counts);
+  put_v(field_check);
+  const Tuning t = resolved(tu);
+  put(&t, sizeof t);
+  for (int r = 0; r < n_req; ++r) {
+    put_v(tp[r].rx_first);
+    put_v(tp[r].n_rx);
+    put_v(tp[r].n_launch);
+    put_v(tp[r].level);
+    put_v(tp[r].R);
+    put_v(tp[r].T);
+    put_v(tp[r].precision);
+    put_v(reqs[r].rx_on_device ? reqs[r].rx : nullptr);
+  }
+  const unsigned long long caps[9] = {W.cap_nodes, W.cap_queue, W.cap_cls, W.cap_cop, W.cap_dd,
+                                      W.cap_cc,    W.cap_corr,  W.cap_surv, W.cap_pairs};
+  put(caps, sizeof caps);
+  const void* ptrs[] = {W.txp.p, W.rx.p, W.rx_req.p, W.rx_bad.p, W.path_bound.p, W.field_bound.p,
+                        W.rx_flag.p, W.fstat.p, W.gb.p, W.grids.p, W.cell_base.p, W.cell_counts.p,
+                        W.cell_starts.p, W.cell_cursor.p, W.rx32.p, W.q0.p, W.q1.p, W.ray32.p,
+                        W.nodes.p, W.nodes_cold.p, W.cls_keys.p, W.cop_keys.p, W.dd_keys.p,
+                        W.dd_rank.p, W.cc_keys.p, W.cls_list.p, W.cc_val.p, W.cls_info.p,
+                        W.cls_cap.p, W.corr_list.p, W.pairs.p, W.direct_ok.p, W.surv.p,
+                        W.s_counts.p, W.s_starts.p, W.s_cursor.p, W.s_order.p, W.path_field.p,
+                        W.path_pts.p, W.field.p, W.seg.p, W.path_mat.p, W.path_field64.p,
+                        W.field64.p, W.path_nray.p, W.path_tri.p, W.path_cop.p, W.path_kind.p,
+                        W.path_near.p, W.ctr.p, W.seg_tx.p, W.cand.p, W.ncand.p, W.find_work.p,
+                        W.h_txp.p, W.h_rxreq.p, W.h_rx.p, W.h_gb.p, S.dir_table.p,
+                        S.tri_cop.p, S.rank_to_id.p};
+  put(ptrs, sizeof ptrs);
+  put_v(W.tr_ev.size());
+  return k;
+}
+
+enum PipelineRun { kEager, kCaptured, kReplayed };
+constexpr size_t kPipelineGraphs = 8;  // graphs kept per workspace
+constexpr size_t kPipelineSeen = 16;   // eager keys remembered per workspace
+
+// Runs the device pipeline on st: replays the graph captured for the key, or
+// captures (then launches) one the second time a key runs, or else runs the
+// operations eagerly.  *entry: the graph that ran (captured or replayed).
+template <class Record>
+static PipelineRun run_pipeline(Workspace& W, cudaStream_t st, Record& record,
+                                const std::string& key, bool use_graphs,
+                                Workspace::PipelineGraph** entry) {
+  *entry = nullptr;
+  if (!use_graphs) {
+    record();
+    return kEager;
+  }
+  for (auto& g : W.graphs)
+    if (g.key == key) {
+      CK(cudaGraphLaunch(g.exec, st));
+      g.used = ++W.graph_tick;
+      *entry = &g;
+      return kReplayed;
+    }
+  auto it = std::find(W.seen.begin(), W.seen.end(), key);
+  if (it == W.seen.end()) {
+    record();
+    if (W.seen.size() == kPipelineSeen) W.seen.erase(W.seen.begin());
+    W.seen.push_back(key);
+    return kEager;
+  }
+  W.seen.erase(it);
+  if (W.graphs.size() == kPipelineGraphs) {  // drop the least recently used
+    auto lru = std::min_element(W.graphs.begin(), W.graphs.end(),
+                                [](const auto& a, const auto& b) { return a.used < b.used; });
+    CK(cudaGraphExecDestroy(lru->exec));
+    CK(cudaGraphDestroy(lru->graph));
+    W.graphs.erase(lru);
+  }
+  Workspace::PipelineGraph g;
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  try {
+    record();
+  } catch (...) {
+    cudaGraph_t h = nullptr;
+    cudaStreamEndCapture(st, &h);
+    if (h) cudaGraphDestroy(h);
+    cudaGetLastError();
+    throw;
+  }
+  CK(cudaStreamEndCapture(st, &g.graph));
+  const cudaError_t e = cudaGraphInstantiate(&g.exec, g.graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g.graph);
+    CK(e);
+  }
+  g.key = key;
+  g.used = ++W.graph_tick;
+  W.graphs.push_back(std::move(g));
+  *entry = &W.graphs.back();
+  CK(cudaGraphLaunch((*entry)->exec, st));
+  return kCaptured;
+}
+
 // force_check: compute the FP64 shadow field even if no request here asks for
 // it (another pass of the same batch did).
 static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int n_req,
@@ -917,67 +1086,38 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
   for (int r = 0; r < n_req; ++r) field_check |= reqs[r].field_check && tp[r].precision != 0;
   if (n_req >= int(0xFFFFFFFFu - kRootBase)) throw std::string("too many requests in one batch");
   auto t0 = std::chrono::steady_clock::now();
-  CK(cudaEventRecord(W.ev[0], st));
-  W.txp.upload(tp.data(), tp.size(), st);
-  // receivers
-  W.rx.ensure(std::max(1, 3 * rx_total));
-  W.direct_ok.ensure(std::max(1, rx_total));
-  {
-    std::vector<int> req_of(std::max(1, rx_total));
-    for (int r = 0; r < n_req; ++r) {
-      const sbr_request& q = reqs[r];
-      if (q.n_rx)
-        CK(cudaMemcpyAsync(W.rx.p + 3 * size_t(tp[r].rx_first), q.rx, 3 * sizeof(double) * q.n_rx,
-                           q.rx_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
-      for (int i = 0; i < q.n_rx; ++i) req_of[tp[r].rx_first + i] = r;
-    }
-    W.rx_req.upload(req_of.data(), req_of.size(), st);
-  }
-  CK(cudaEventRecord(W.ev[1], st));
-  // ---- receiver grid
-  // cells per request: the grid aims at ~2 receivers per cell
-  int max_cells = 64;
+  // ---- host staging: everything the device pipeline uploads is staged in
+  // pinned memory first, so the pipeline is a fixed sequence of stream
+  // operations (a CUDA graph can replay it)
+  int max_cells = 64;  // cells per request: the grid aims at ~2 receivers per cell
   for (auto& p : tp)
     max_cells = std::max(max_cells, int(std::min(4.0 * p.n_rx / kMinRxPerCell, 4e6)) + 64);
   max_cells = std::min(max_cells, 1 << 21);
-  W.gb.ensure(n_req);
-  {
-    std::vector<GridBuild> g0(n_req);
-    for (auto& g : g0) {
-      for (int a = 0; a < 3; ++a) {
-        g.bmin[a] = INT_MAX;
-        g.bmax[a] = INT_MIN;
-      }
-      g.cmax_o = INT_MIN;
-      g.cmax = 0;
-      g.ncell = 0;
-    }
-    CK(cudaMemcpyAsync(W.gb.p, g0.data(), sizeof(GridBuild) * n_req, cudaMemcpyHostToDevice, st));
-  }
-  W.grids.ensure(n_req);
-  W.cell_base.ensure(n_req + 1);
   const size_t cell_cap = size_t(n_req) * (max_cells + 1) + 1;
-  W.cell_counts.ensure(cell_cap);
-  W.cell_starts.ensure(cell_cap + 1);
-  W.cell_cursor.ensure(cell_cap);
-  W.rx32.ensure(std::max(1, rx_total));
-  CK(cudaMemsetAsync(W.cell_counts.p, 0, sizeof(int) * cell_cap, st));
-  CK(cudaMemsetAsync(W.cell_cursor.p, 0, sizeof(int) * cell_cap, st));
   int max_rx = 1;
   for (auto& p : tp) max_rx = std::max(max_rx, p.n_rx);
-  dim3 rg(std::min(1024, (max_rx + 255) / 256), n_req);
-  W.rx_bad.ensure(1);
-  CK(cudaMemsetAsync(W.rx_bad.p, 0, sizeof(int), st));
-  ++nl, k_rx_bounds<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.gb.p, W.rx_bad.p);
-  ++nl, k_grid_shape<<<1, 1, 0, st>>>(W.gb.p, W.grids.p, W.txp.p, n_req, max_cells, W.cell_base.p);
-  ++nl, k_rx_count<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p, W.cell_counts.p);
-  ++nl, k_scan_exclusive<<<1, 1024, 0, st>>>(W.cell_counts.p, W.cell_starts.p, int(cell_cap));
-  ++nl, k_rx_scatter<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p,
-                                   W.cell_starts.p, W.cell_cursor.p, W.rx32.p);
-  ++nl, k_grid_finish<<<(n_req + 127) / 128, 128, 0, st>>>(W.grids.p, W.cell_starts.p, W.cell_base.p,
-                                                    W.rx32.p, n_req);
-  CK(cudaGetLastError());
-
+  const dim3 rg(std::min(1024, (max_rx + 255) / 256), n_req);
+  W.h_txp.ensure(size_t(n_req));
+  std::memcpy(W.h_txp.p, tp.data(), sizeof(TxParams) * n_req);
+  W.h_rxreq.ensure(size_t(std::max(1, rx_total)));
+  W.h_rx.ensure(3 * size_t(std::max(1, rx_total)));
+  for (int r = 0; r < n_req; ++r) {
+    const sbr_request& q = reqs[r];
+    for (int i = 0; i < q.n_rx; ++i) W.h_rxreq.p[tp[r].rx_first + i] = r;
+    if (q.n_rx && !q.rx_on_device)
+      std::memcpy(W.h_rx.p + 3 * size_t(tp[r].rx_first), q.rx, 3 * sizeof(double) * q.n_rx);
+  }
+  W.h_gb.ensure(size_t(n_req));
+  for (int r = 0; r < n_req; ++r) {
+    GridBuild& g = W.h_gb.p[r];
+    for (int a = 0; a < 3; ++a) {
+      g.bmin[a] = INT_MAX;
+      g.bmax[a] = INT_MIN;
+    }
+    g.cmax_o = INT_MIN;
+    g.cmax = 0;
+    g.ncell = 0;
+  }
   const FieldConsts K = field_consts();
   {
     // Size node pool and queues at the ray-tree bounds so a pass needs no
@@ -1032,8 +1172,114 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.cc_val.ensure(W.cap_cc);
     W.dd_rank.ensure(W.cap_dd);
     W.surv.ensure(W.cap_surv);
-    CK(cudaMemsetAsync(W.ctr.p, 0, sizeof(Counters), st));
     W.seg_tx.ensure(n_req);
+    // receivers and their grid
+    W.txp.ensure(size_t(n_req));
+    W.rx.ensure(std::max(1, 3 * rx_total));
+    W.direct_ok.ensure(std::max(1, rx_total));
+    W.rx_req.ensure(size_t(std::max(1, rx_total)));
+    W.gb.ensure(n_req);
+    W.grids.ensure(n_req);
+    W.cell_base.ensure(n_req + 1);
+    W.cell_counts.ensure(cell_cap);
+    W.cell_starts.ensure(cell_cap + 1);
+    W.cell_cursor.ensure(cell_cap);
+    W.rx32.ensure(std::max(1, rx_total));
+    W.rx_bad.ensure(1);
+    // trace chunks: each depth runs in chunks of at most kTraceChunk rays
+    const long long kTraceChunk = 1LL << (tu.chunk_log2 > 0 ? std::min(tu.chunk_log2, 26) : 24);
+    const long long max_width = std::max<long long>(launches, (long long)W.cap_queue);
+    const long long chunk = std::max<long long>(1, std::min(kTraceChunk, max_width));
+    W.cand.ensure(size_t(chunk) * kCand);
+    W.ncand.ensure(size_t(chunk));
+    W.ray32.ensure(size_t(chunk));
+    W.find_work.ensure(2);  // [0] k_find's work counter, [1] k_trace's
+    size_t n_launch_pairs = 0;  // k_find / k_trace launch pairs of the trace
+    {
+      for (int d = 0; d <= max_depth; ++d) {
+        const long long bound = d == 0 ? launches : (long long)W.cap_queue;
+        n_launch_pairs += size_t((bound + chunk - 1) / chunk);
+      }
+      if (2 * n_launch_pairs > W.tr_ev.size()) {
+        W.tr_ev.resize(2 * n_launch_pairs, nullptr);
+        for (auto& e : W.tr_ev)
+          if (!e) CK(cudaEventCreate(&e));
+      }
+    }
+    // the field stage, sized by the survivor capacity
+    {
+      const size_t nsa = std::max<size_t>(1, W.cap_surv);
+      W.path_field.ensure(6 * nsa);
+      W.path_nray.ensure(nsa);
+      W.path_tri.ensure(nsa * (kMaxDepth + 1));
+      W.path_cop.ensure(nsa * (kMaxDepth + 1));
+      W.path_kind.ensure(nsa * (kMaxDepth + 1));
+      W.path_near.ensure(nsa);
+      W.path_pts.ensure(nsa * (kMaxDepth + 2) * 3);
+      W.seg.ensure(nsa * (kMaxDepth + 1));
+      W.path_mat.ensure(nsa * (kMaxDepth + 1));
+      W.field.ensure(std::max(1, 6 * rx_total));
+      W.s_counts.ensure(rx_total + 1);
+      W.s_starts.ensure(rx_total + 2);
+      W.s_cursor.ensure(rx_total + 1);
+      W.s_order.ensure(nsa);
+      W.path_bound.ensure(nsa);
+      W.rx_flag.ensure(std::max(1, rx_total));
+      W.field_bound.ensure(std::max(1, rx_total));
+      W.fstat.ensure(2);
+      if (field_check) {
+        W.path_field64.ensure(nsa * 6);
+        W.field64.ensure(std::max(1, 6 * rx_total));
+      }
+    }
+    (void)resolved(tu);  // the occupancy queries run before any recording
+    (void)pool_fit();
+    // ---- the device pipeline: a fixed sequence of stream operations
+    const long long nl_before = nl;
+    size_t n_tr = 0;  // k_trace launches (timed one by one)
+    // Timing events: recorded as event nodes when the pipeline is being
+    // captured (a plain record inside a capture only orders the streams; the
+    // external flag is refused outside a capture).
+    auto mark = [&](cudaEvent_t e) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      CK(cudaStreamIsCapturing(st, &cs));
+      if (cs == cudaStreamCaptureStatusActive)
+        CK(cudaEventRecordWithFlags(e, st, cudaEventRecordExternal));
+      else
+        CK(cudaEventRecord(e, st));
+    };
+    auto record = [&]() {
+  mark(W.ev[0]);
+  CK(cudaMemcpyAsync(W.txp.p, W.h_txp.p, sizeof(TxParams) * n_req, cudaMemcpyHostToDevice, st));
+  for (int r = 0; r < n_req; ++r) {
+    const sbr_request& q = reqs[r];
+    if (!q.n_rx) continue;
+    const size_t o = 3 * size_t(tp[r].rx_first);
+    if (q.rx_on_device)
+      CK(cudaMemcpyAsync(W.rx.p + o, q.rx, 3 * sizeof(double) * q.n_rx, cudaMemcpyDeviceToDevice, st));
+    else
+      CK(cudaMemcpyAsync(W.rx.p + o, W.h_rx.p + o, 3 * sizeof(double) * q.n_rx,
+                         cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaMemcpyAsync(W.rx_req.p, W.h_rxreq.p, sizeof(int) * std::max(1, rx_total),
+                     cudaMemcpyHostToDevice, st));
+  mark(W.ev[1]);
+  // ---- receiver grid
+  CK(cudaMemcpyAsync(W.gb.p, W.h_gb.p, sizeof(GridBuild) * n_req, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(W.cell_counts.p, 0, sizeof(int) * cell_cap, st));
+  CK(cudaMemsetAsync(W.cell_cursor.p, 0, sizeof(int) * cell_cap, st));
+  CK(cudaMemsetAsync(W.rx_bad.p, 0, sizeof(int), st));
+  ++nl, k_rx_bounds<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.gb.p, W.rx_bad.p);
+  ++nl, k_grid_shape<<<1, 1, 0, st>>>(W.gb.p, W.grids.p, W.txp.p, n_req, max_cells, W.cell_base.p);
+  ++nl, k_rx_count<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p, W.cell_counts.p);
+  ++nl, k_scan_exclusive<<<1, 1024, 0, st>>>(W.cell_counts.p, W.cell_starts.p, int(cell_cap));
+  ++nl, k_rx_scatter<<<rg, 256, 0, st>>>(W.rx.p, W.txp.p, n_req, W.grids.p, W.cell_base.p,
+                                   W.cell_starts.p, W.cell_cursor.p, W.rx32.p);
+  ++nl, k_grid_finish<<<(n_req + 127) / 128, 128, 0, st>>>(W.grids.p, W.cell_starts.p, W.cell_base.p,
+                                                    W.rx32.p, n_req);
+  CK(cudaGetLastError());
+
+    CK(cudaMemsetAsync(W.ctr.p, 0, sizeof(Counters), st));
     CK(cudaMemsetAsync(W.seg_tx.p, 0, sizeof(unsigned long long) * n_req, st));
     const int fb = 256;
     ++nl, k_fill_u64<<<grid_for(W.cap_cls, fb), fb, 0, st>>>(W.cls_keys.p, W.cap_cls, kEmptyKey);
@@ -1042,7 +1288,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ++nl, k_fill_u64<<<grid_for(W.cap_dd, fb), fb, 0, st>>>(W.dd_rank.p, W.cap_dd, kEmptyKey);
     ++nl, k_fill_u64<<<grid_for(W.cap_cc, fb), fb, 0, st>>>(W.cc_keys.p, W.cap_cc, kEmptyKey);
     CK(cudaMemsetAsync(W.cc_val.p, 0, W.cap_cc, st));
-    CK(cudaEventRecord(W.ev[2], st));
+    mark(W.ev[2]);
     // The direct-path test of every receiver (DirectPathCorrection) needs
     // only the scene and the receivers: it runs on the side stream while the
     // trace runs, and the capture stage waits for it.
@@ -1071,17 +1317,10 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ta.ctr = W.ctr.p;
     ta.seg_per_tx = W.seg_tx.p;
     ta.n_root = launches;
-    // Each depth runs in chunks of at most kTraceChunk rays: the FP32
-    // search (k_find) stores the chunk's contenders, then k_trace resolves
-    // them in FP64 and spawns the next depth.  The ray count of a depth > 0
-    // is on the device; chunks past it return at once.
-    const long long kTraceChunk = 1LL << (tu.chunk_log2 > 0 ? std::min(tu.chunk_log2, 26) : 24);
-    const long long max_width = std::max<long long>(launches, (long long)W.cap_queue);
-    const long long chunk = std::max<long long>(1, std::min(kTraceChunk, max_width));
-    W.cand.ensure(size_t(chunk) * kCand);
-    W.ncand.ensure(size_t(chunk));
-    W.ray32.ensure(size_t(chunk));
-    W.find_work.ensure(2);  // [0] k_find's work counter, [1] k_trace's
+    // Each depth runs in chunks (the FP32 search, k_find, stores the chunk's
+    // contenders, then k_trace resolves them in FP64 and spawns the next
+    // depth).  The ray count of a depth > 0 is on the device; chunks past it
+    // return at once.
     FindArgs fnd;
     fnd.sc = S.dev;
     fnd.txp = W.txp.p;
@@ -1100,7 +1339,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ta.ncand = W.ncand.p;
     ta.ray32 = W.ray32.p;
     ta.work = W.find_work.p + 1;
-    size_t n_tr = 0;  // k_trace launches (timed one by one)
+    n_tr = 0;
     for (int d = 0; d <= max_depth; ++d) {
       ta.depth = fnd.depth = d;
       ta.in = fnd.in = (d % 2 == 0) ? W.q1.p : W.q0.p;
@@ -1111,12 +1350,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         ta.hi = fnd.hi = std::min(bound, lo + chunk);
         CK(cudaMemsetAsync(W.find_work.p, 0, 2 * sizeof(unsigned long long), st));
         ++nl, k_find<<<find_grid(tu), 128, 0, st>>>(fnd);
-        if (2 * n_tr + 2 > W.tr_ev.size()) {
-          W.tr_ev.resize(2 * n_tr + 2, nullptr);
-          for (auto& e : W.tr_ev)
-            if (!e) CK(cudaEventCreate(&e));
-        }
-        CK(cudaEventRecord(W.tr_ev[2 * n_tr], st));
+        mark(W.tr_ev[2 * n_tr]);
         if (resolved(tu).trace_kernel == 2) {
           // one block per 128 rays at most, as k_trace: a small launch still
           // spreads over many warps (each then fills only part of its slots)
@@ -1126,7 +1360,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
         } else {
           ++nl, k_trace<<<std::min<long long>(trace_grid(tu), (ta.hi - lo + 127) / 128), 128, 0, st>>>(ta);
         }
-        CK(cudaEventRecord(W.tr_ev[2 * n_tr + 1], st));
+        mark(W.tr_ev[2 * n_tr + 1]);
         ++n_tr;
       }
     }
@@ -1134,7 +1368,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ++nl, k_class_cones<<<grid_for(W.cap_cls / 2, 128), 128, 0, st>>>(
         W.cls_list.p, W.ctr.p, W.cap_cls, W.cls_info.p, S.dev, W.cls_cap.p);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(W.ev[3], st));
+    mark(W.ev[3]);
     // ---- capture
     CaptureArgs ca;
     ca.sc = S.dev;
@@ -1159,17 +1393,17 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     ca.work = W.find_work.p;  // the trace is done with it
     CK(cudaMemsetAsync(W.find_work.p, 0, sizeof(unsigned long long), st));
     CK(cudaStreamWaitEvent(st, W.join, 0));
-    CK(cudaEventRecord(W.cap_ev[0], st));
+    mark(W.cap_ev[0]);
     if (stage_counts) {
       ++nl, k_capture<true><<<capture_grid(tu), 32 * kCapWarps, 0, st>>>(ca);
-      CK(cudaEventRecord(W.cap_ev[1], st));
+      mark(W.cap_ev[1]);
     } else {
       ++nl, k_capture_fast<<<capture_grid(tu), 32 * kCapWarps, 0, st>>>(ca);
-      CK(cudaEventRecord(W.cap_ev[1], st));
+      mark(W.cap_ev[1]);
       ++nl, k_capture_finish<<<device_sms() * 16, 128, 0, st>>>(ca);
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(W.ev[4], st));
+    mark(W.ev[4]);
     // ---- duplicate removal over the corrected captures
     const HashTable dd{W.dd_keys.p, W.cap_dd - 1};
     ++nl, k_dedup<<<grid_for(W.cap_corr, 256), 256, 0, st>>>(W.corr_list.p, W.cap_corr, W.cls_info.p,
@@ -1178,7 +1412,85 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
                                                         dd, W.dd_rank.p, W.surv.p, W.cap_surv,
                                                         W.ctr.p);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(W.ev[5], st));
+    mark(W.ev[5]);
+    // ---- field + ordered per-receiver sum, sized by the survivor capacity
+    // (the kernels take the count from the device), so the whole solve runs
+    // without a host round trip until its results are read
+    const unsigned long long ns_cap = W.cap_surv;
+    FieldArgs fa;
+    fa.sc = S.dev;
+    fa.txp = W.txp.p;
+    fa.rx = W.rx.p;
+    fa.rx_req = W.rx_req.p;
+    fa.cls_info = W.cls_info.p;
+    fa.rank_to_id = S.rank_to_id.p;
+    fa.surv = W.surv.p;
+    fa.ctr = W.ctr.p;
+    fa.cap = W.cap_surv;
+    fa.K = K;
+    fa.precision = -1;
+    fa.path_field = W.path_field.p;
+    fa.path_nray = W.path_nray.p;
+    fa.path_tri = W.path_tri.p;
+    fa.path_cop = W.path_cop.p;
+    fa.path_kind = W.path_kind.p;
+    fa.path_near_edge = W.path_near.p;
+    fa.path_pts = W.path_pts.p;
+    fa.seg = W.seg.p;
+    fa.path_mat = W.path_mat.p;
+    bool any_fp32 = false;  // a request in the FP32 field mode (error bounds, escalation)
+    for (int r = 0; r < n_req; ++r) any_fp32 |= tp[r].precision == 1;
+    CK(cudaMemsetAsync(W.rx_flag.p, 0, sizeof(int) * std::max(1, rx_total), st));
+    CK(cudaMemsetAsync(W.fstat.p, 0, 2 * sizeof(unsigned long long), st));
+    fa.path_bound = W.path_bound.p;
+    fa.rx_flag = W.rx_flag.p;
+    fa.fstat = W.fstat.p;
+    ++nl, k_path<<<grid_for(ns_cap, 64), 64, 0, st>>>(fa);
+    ++nl, k_seg<<<grid_for(ns_cap * (kMaxDepth + 1), 64), 64, 0, st>>>(fa);
+    ++nl, k_combine<<<grid_for(ns_cap, 64), 64, 0, st>>>(fa);
+    CK(cudaMemsetAsync(W.s_counts.p, 0, sizeof(int) * (rx_total + 1), st));
+    CK(cudaMemsetAsync(W.s_cursor.p, 0, sizeof(int) * (rx_total + 1), st));
+    ++nl, k_surv_hist<<<grid_for(ns_cap, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv, W.s_counts.p);
+    ++nl, k_scan_exclusive<<<1, 1024, 0, st>>>(W.s_counts.p, W.s_starts.p, rx_total);
+    ++nl, k_surv_scatter<<<grid_for(ns_cap, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv,
+                                                          W.s_starts.p, W.s_cursor.p, W.s_order.p);
+    if (rx_total)
+      ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(
+          W.surv.p, W.s_starts.p, W.s_order.p, rx_total, W.path_field.p, -1, W.rx_req.p, W.txp.p,
+          W.field.p, W.path_bound.p, W.field_bound.p, W.rx_flag.p, W.fstat.p);
+    if (any_fp32 && rx_total) {  // receivers the FP32 bound could not certify, in FP64
+      ++nl, k_escalate<<<grid_for(ns_cap, 64), 64, 0, st>>>(fa);
+      ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(
+          W.surv.p, W.s_starts.p, W.s_order.p, rx_total, W.path_field.p, 0, W.rx_req.p, W.txp.p,
+          W.field.p, nullptr, W.field_bound.p, nullptr, nullptr, W.rx_flag.p);
+    }
+    CK(cudaGetLastError());
+    mark(W.ev[6]);
+    if (field_check) {  // FP64 shadow of the same paths, outside the timed stages
+      FieldArgs f64 = fa;
+      f64.precision = 0;
+      f64.path_field = W.path_field64.p;
+      f64.path_bound = nullptr;
+      ++nl, k_seg<<<grid_for(ns_cap * (kMaxDepth + 1), 64), 64, 0, st>>>(f64);
+      ++nl, k_combine<<<grid_for(ns_cap, 64), 64, 0, st>>>(f64);
+      if (rx_total)
+        ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
+                                                          rx_total, W.path_field64.p, 0,
+                                                          W.rx_req.p, W.txp.p, W.field64.p);
+      CK(cudaGetLastError());
+    }
+    };  // record
+    Workspace::PipelineGraph* graph = nullptr;
+    const PipelineRun how =
+        run_pipeline(W, st, record,
+                     pipeline_key(S, W, reqs, tp, n_req, rx_total, launches, max_depth, cell_cap,
+                                  chunk, tu, stage_counts, field_check),
+                     resolved(tu).graph > 0, &graph);
+    if (how == kReplayed) nl = nl_before + graph->kernels;
+    if (how == kCaptured) graph->kernels = nl - nl_before;
+    W.pipeline_kernels = nl - nl_before;
+    n_tr = n_launch_pairs;
+    const int graph_run = how == kEager ? 0 : 1;
     Counters c;
     int rx_bad = 0;
     CK(cudaMemcpyAsync(&c, W.ctr.p, sizeof c, cudaMemcpyDeviceToHost, st));
@@ -1229,96 +1541,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       upd(W.r_surv, c.survivors / n);
       upd(W.r_pairs, c.pairs / n);
     }
-    // ---- field + ordered per-receiver sum
     const unsigned long long ns = c.survivors;
-    const size_t nsa = std::max<size_t>(1, ns);
-    W.path_field.ensure(6 * nsa);
-    W.path_nray.ensure(nsa);
-    W.path_tri.ensure(nsa * (kMaxDepth + 1));
-    W.path_cop.ensure(nsa * (kMaxDepth + 1));
-    W.path_kind.ensure(nsa * (kMaxDepth + 1));
-    W.path_near.ensure(nsa);
-    W.path_pts.ensure(nsa * (kMaxDepth + 2) * 3);
-    W.seg.ensure(nsa * (kMaxDepth + 1));
-    W.path_mat.ensure(nsa * (kMaxDepth + 1));
-    W.field.ensure(std::max(1, 6 * rx_total));
-    W.s_counts.ensure(rx_total + 1);
-    W.s_starts.ensure(rx_total + 2);
-    W.s_cursor.ensure(rx_total + 1);
-    W.s_order.ensure(nsa);
-    FieldArgs fa;
-    fa.sc = S.dev;
-    fa.txp = W.txp.p;
-    fa.rx = W.rx.p;
-    fa.rx_req = W.rx_req.p;
-    fa.cls_info = W.cls_info.p;
-    fa.rank_to_id = S.rank_to_id.p;
-    fa.surv = W.surv.p;
-    fa.ctr = W.ctr.p;
-    fa.cap = W.cap_surv;
-    fa.K = K;
-    fa.precision = -1;
-    fa.path_field = W.path_field.p;
-    fa.path_nray = W.path_nray.p;
-    fa.path_tri = W.path_tri.p;
-    fa.path_cop = W.path_cop.p;
-    fa.path_kind = W.path_kind.p;
-    fa.path_near_edge = W.path_near.p;
-    fa.path_pts = W.path_pts.p;
-    fa.seg = W.seg.p;
-    fa.path_mat = W.path_mat.p;
-    bool any_fp32 = false;  // a request in the FP32 field mode (error bounds, escalation)
-    for (int r = 0; r < n_req; ++r) any_fp32 |= tp[r].precision == 1;
-    W.path_bound.ensure(nsa);
-    W.rx_flag.ensure(std::max(1, rx_total));
-    W.field_bound.ensure(std::max(1, rx_total));
-    W.fstat.ensure(2);
-    CK(cudaMemsetAsync(W.rx_flag.p, 0, sizeof(int) * std::max(1, rx_total), st));
-    CK(cudaMemsetAsync(W.fstat.p, 0, 2 * sizeof(unsigned long long), st));
-    fa.path_bound = W.path_bound.p;
-    fa.rx_flag = W.rx_flag.p;
-    fa.fstat = W.fstat.p;
-    if (ns) {
-      ++nl, k_path<<<grid_for(ns, 64), 64, 0, st>>>(fa);
-      ++nl, k_seg<<<grid_for(ns * (kMaxDepth + 1), 64), 64, 0, st>>>(fa);
-      ++nl, k_combine<<<grid_for(ns, 64), 64, 0, st>>>(fa);
-    }
-    CK(cudaMemsetAsync(W.s_counts.p, 0, sizeof(int) * (rx_total + 1), st));
-    CK(cudaMemsetAsync(W.s_cursor.p, 0, sizeof(int) * (rx_total + 1), st));
-    if (ns) ++nl, k_surv_hist<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv, W.s_counts.p);
-    ++nl, k_scan_exclusive<<<1, 1024, 0, st>>>(W.s_counts.p, W.s_starts.p, rx_total);
-    if (ns)
-      ++nl, k_surv_scatter<<<grid_for(ns, 256), 256, 0, st>>>(W.surv.p, W.ctr.p, W.cap_surv,
-                                                        W.s_starts.p, W.s_cursor.p, W.s_order.p);
-    if (rx_total)
-      ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(
-          W.surv.p, W.s_starts.p, W.s_order.p, rx_total, W.path_field.p, -1, W.rx_req.p, W.txp.p,
-          W.field.p, W.path_bound.p, W.field_bound.p, W.rx_flag.p, W.fstat.p);
-    if (any_fp32 && rx_total) {  // receivers the FP32 bound could not certify, in FP64
-      if (ns) ++nl, k_escalate<<<grid_for(ns, 64), 64, 0, st>>>(fa);
-      ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(
-          W.surv.p, W.s_starts.p, W.s_order.p, rx_total, W.path_field.p, 0, W.rx_req.p, W.txp.p,
-          W.field.p, nullptr, W.field_bound.p, nullptr, nullptr, W.rx_flag.p);
-    }
-    CK(cudaGetLastError());
-    CK(cudaEventRecord(W.ev[6], st));
-    if (field_check) {  // FP64 shadow of the same paths, outside the timed stages
-      W.path_field64.ensure(nsa * 6);
-      W.field64.ensure(std::max(1, 6 * rx_total));
-      FieldArgs f64 = fa;
-      f64.precision = 0;
-      f64.path_field = W.path_field64.p;
-      f64.path_bound = nullptr;
-      if (ns) {
-        ++nl, k_seg<<<grid_for(ns * (kMaxDepth + 1), 64), 64, 0, st>>>(f64);
-        ++nl, k_combine<<<grid_for(ns, 64), 64, 0, st>>>(f64);
-      }
-      if (rx_total)
-        ++nl, k_rx_sum<<<grid_for(rx_total, 128), 128, 0, st>>>(W.surv.p, W.s_starts.p, W.s_order.p,
-                                                          rx_total, W.path_field64.p, 0,
-                                                          W.rx_req.p, W.txp.p, W.field64.p);
-      CK(cudaGetLastError());
-    }
     // ---- results to the host
     out.field.resize(6 * size_t(rx_total));
     if (rx_total)
@@ -1417,6 +1640,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     out.counts.near_edge_paths = 0;
     for (const sbr_path& p : out.paths) out.counts.near_edge_paths += p.near_edge;
     out.counts.gpu_kernels = nl;
+    out.counts.pipeline_graph = graph_run;
     out.counts.fp64_field_paths = (long long)fst[0];
     out.counts.fp64_field_receivers = (long long)fst[1];
     float ms[8] = {};
@@ -1930,6 +2154,7 @@ static void tuning_to_c(const Tuning& t, sbr_tuning* o) {
   o->trace_blocks_per_sm = t.trace_bps;
   o->capture_blocks_per_sm = t.capture_bps;
   o->trace_chunk_log2 = t.chunk_log2;
+  o->pipeline_graph = t.graph;
 }
 
 sbr_status sbr_scene_set_tuning(sbr_scene* scene, const sbr_tuning* t) {
@@ -1940,9 +2165,10 @@ sbr_status sbr_scene_set_tuning(sbr_scene* scene, const sbr_tuning* t) {
   if (t->find_steps < 0 || t->find_refill < 0 || t->find_refill > 32 ||
       t->find_blocks_per_sm < 0 || t->trace_blocks_per_sm < 0 || t->capture_blocks_per_sm < 0 ||
       (t->trace_chunk_log2 != 0 && (t->trace_chunk_log2 < 16 || t->trace_chunk_log2 > 26)) ||
-      t->trace_kernel < 0 || t->trace_kernel > 2) {
+      t->trace_kernel < 0 || t->trace_kernel > 2 || t->pipeline_graph < -1 ||
+      t->pipeline_graph > 1) {
     set_err("sbr_scene_set_tuning: fields must be >= 0, find_refill <= 32, trace_chunk_log2 "
-            "0 or 16..26 and trace_kernel 0..2");
+            "0 or 16..26, trace_kernel 0..2 and pipeline_graph -1..1");
     return SBR_ERR_INVALID_ARG;
   }
   SceneImpl& S = scene->impl;
@@ -1954,6 +2180,7 @@ sbr_status sbr_scene_set_tuning(sbr_scene* scene, const sbr_tuning* t) {
   S.tuning.capture_bps = t->capture_blocks_per_sm;
   S.tuning.chunk_log2 = t->trace_chunk_log2;
   S.tuning.trace_kernel = t->trace_kernel;
+  S.tuning.graph = t->pipeline_graph;
   return SBR_OK;
 }
 
