@@ -10,7 +10,8 @@ One JSON line on rank 0.  `value` = segments / device time with the scene
 and receivers resident (CUDA events on the engine's stream, from the first
 kernel to the last, results left on the device).  `e2e` = the same metric
 through the C ABI with host buffers: receivers copied in and fields + all
-surviving paths copied out inside the timed region (wall clock).
+surviving paths copied out (into flat numpy arrays, the form of
+sbr_result_paths) inside the timed region (wall clock).
 Several GPUs (torchrun) run independent replicas, one per GPU; value sums
 their segments over the slowest rank's time.
 """
@@ -489,7 +490,7 @@ def main():
     e2e_seg = 0
     d2h = 0
     for _ in range(args.steps):
-        r = api.solve(scene, req_host, with_paths=True)
+        r = api.solve(scene, req_host, with_paths="arrays")
         e2e_seg += r.counts["segments"]
         d2h = 6 * 8 * len(wl.request.rx) + r.counts["paths"] * 64 + r.counts["rays"] * (12 + 48)
     torch.cuda.synchronize()
@@ -537,7 +538,9 @@ def main():
             "stages_ms": {k: v / steps for k, v in stage.items()},
             "e2e": {"value": tot_e2e / max_e2e, "unit": "segments/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": 1e3 * max_e2e / steps},
+                    "ms_per_step": 1e3 * max_e2e / steps,
+                    "call": "api.solve(scene, request with host receivers, "
+                            "with_paths='arrays'): fields and every path array read back"},
             "roofline": {"bound": "hbm", "kernel": kern, "launch": launch,
                          "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,

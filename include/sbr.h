@@ -79,6 +79,12 @@ typedef struct sbr_scene_info {
   int n_triangles, n_bvh_nodes, bvh_depth, n_coplanar;
   double extent;          /* max |coordinate| of the scene */
   long long device_bytes; /* resident scene size */
+  /* wall time of the scene's preparation (ms): the whole of sbr_scene_create;
+   * the host's part (triangle records; every table with SBR_SCENE_HOST_PREP);
+   * on the device: vertex merge, coplanar groups and frames; the search BVH;
+   * the reference BVH; then the upload of the finished tables */
+  double prep_total_ms, prep_host_ms, prep_device_tables_ms, prep_search_bvh_ms,
+      prep_reference_bvh_ms, prep_upload_ms;
 } sbr_scene_info;
 
 /* Arguments of RTSolver::ExecuteRayTracing (RTSolver.h:25-37) plus the
@@ -192,6 +198,14 @@ sbr_status sbr_scene_triangle_frames(const sbr_scene* scene, double* frames, dou
  * each leaf slot (as many as triangles).  NULL nodes/order: sizes only. */
 sbr_status sbr_scene_search_bvh(const sbr_scene* scene, int* n_nodes, int* max_depth,
                                 float* nodes, int* order);
+/* The reference BVH (BVH/BVH.h:135-230), nodes in depth-first order
+ * (children[0] subtree first): *n_nodes in: capacity, out: node count;
+ * boxes: 6 doubles per node (min xyz, max xyz); links: 6 ints per node
+ * (child 0, child 1 (-1 for a leaf), first, count (leaf range of order),
+ * parent, depth); order: the triangle ids of the leaves in visit order (as
+ * many as triangles).  NULL boxes/links/order: sizes only. */
+sbr_status sbr_scene_reference_bvh(const sbr_scene* scene, int* n_nodes, int* max_depth,
+                                   double* boxes, int* links, int* order);
 sbr_status sbr_scene_create_from_stl(const char* path, const int* material_ids,
                                      const sbr_material* materials, int n_materials,
                                      sbr_scene** out);
@@ -408,9 +422,13 @@ sbr_status sbr_fault_inject_alloc(long long after);
  * SBR_FIELD_FP32_PHASE are rejected with SBR_ERR_INVALID_ARG.  Runs on
  * `stream` (a cudaStream_t of the current device, NULL = default stream) and
  * returns after it completes.  The first call on a device looks up the
- * array's device address and should come before any stream capture.  Calls
- * share the array: calls that overlap on the GPU race and must be serialised
- * by the caller. */
+ * array's device address and must come before any stream capture.  A later
+ * call on a stream that is being captured into a CUDA graph only enqueues its
+ * kernels and returns SBR_OK: the host-side argument checks still apply, but
+ * receiver indices outside [0, n_rx) and receivers over the per-receiver
+ * limit are then skipped without a report (their fields stay zero).  Calls
+ * share the array: calls (or graph launches) that overlap on the GPU race
+ * and must be serialised by the caller. */
 sbr_status sbr_receiver_field_sum_noalloc(const int* path_receiver, const long long* path_rank,
                                           const double* path_field, int n_paths, int n_rx,
                                           int field_precision, double* field_out,

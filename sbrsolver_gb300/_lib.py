@@ -28,6 +28,7 @@ EXPORTS = (
     "sbr_pattern_info", "sbr_pattern_destroy", "sbr_fault_inject_alloc",
     "sbr_scene_set_tuning", "sbr_scene_get_tuning", "sbr_autotune", "sbr_result_field_bound",
     "sbr_scene_create_ex", "sbr_scene_triangle_frames", "sbr_scene_search_bvh",
+    "sbr_scene_reference_bvh",
 )
 
 
@@ -45,7 +46,10 @@ class Material(C.Structure):
 
 class SceneInfo(C.Structure):
     _fields_ = [("n_triangles", C.c_int), ("n_bvh_nodes", C.c_int), ("bvh_depth", C.c_int),
-                ("n_coplanar", C.c_int), ("extent", C.c_double), ("device_bytes", C.c_longlong)]
+                ("n_coplanar", C.c_int), ("extent", C.c_double), ("device_bytes", C.c_longlong),
+                ("prep_total_ms", C.c_double), ("prep_host_ms", C.c_double),
+                ("prep_device_tables_ms", C.c_double), ("prep_search_bvh_ms", C.c_double),
+                ("prep_reference_bvh_ms", C.c_double), ("prep_upload_ms", C.c_double)]
 
 
 class Request(C.Structure):
@@ -159,6 +163,7 @@ def load(path: str = LIB_PATH):
                                     C.c_uint, P(vp)],
             "sbr_scene_triangle_frames": [vp, P(D), P(D), P(D)],
             "sbr_scene_search_bvh": [vp, P(I), P(I), P(C.c_float), P(I)],
+            "sbr_scene_reference_bvh": [vp, P(I), P(I), P(C.c_double), P(I), P(I)],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

@@ -207,6 +207,23 @@ class DeviceScene:
             order.ctypes.data_as(C.POINTER(C.c_int))))
         return {"nodes": words.reshape(-1, 14), "order": order, "max_depth": md.value}
 
+    def reference_bvh(self) -> dict:
+        """The reference BVH in depth-first order: node boxes (n, 6), links
+        (n, 6: child 0, child 1, first, count, parent, depth), the leaves'
+        triangle ids in visit order, and the depth."""
+        nn, md = C.c_int(0), C.c_int(0)
+        _lib.check(self._lib.sbr_scene_reference_bvh(self.handle, C.byref(nn), C.byref(md), None,
+                                                     None, None))
+        boxes = np.zeros(6 * nn.value, np.float64)
+        links = np.zeros(6 * nn.value, np.int32)
+        order = np.zeros(self.n_triangles, np.int32)
+        ip = C.POINTER(C.c_int)
+        _lib.check(self._lib.sbr_scene_reference_bvh(
+            self.handle, C.byref(nn), C.byref(md), boxes.ctypes.data_as(C.POINTER(C.c_double)),
+            links.ctypes.data_as(ip), order.ctypes.data_as(ip)))
+        return {"boxes": boxes.reshape(-1, 6), "links": links.reshape(-1, 6), "order": order,
+                "max_depth": md.value}
+
     def info(self) -> _lib.SceneInfo:
         out = _lib.SceneInfo()
         _lib.check(self._lib.sbr_scene_info_get(self.handle, C.byref(out)))
@@ -360,23 +377,27 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
             _lib.check(lib.sbr_result_paths(h, P, tri.ctypes.data_as(ip), cop.ctypes.data_as(ip),
                                             kind.ctypes.data_as(ip),
                                             pts.ctypes.data_as(C.POINTER(C.c_double))))
+            # the whole path set as flat arrays (cheap at 1e5-1e6 paths)
+            A = np.ctypeslib.as_array(P)
+            arrays = {k: np.array(A[k]) for k in ("request", "receiver", "launch", "heap",
+                                                  "ray_offset", "n_rays", "field", "near_edge")}
+            arrays.update(tri=tri[:cnt.rays], cop=cop[:cnt.rays], kind=kind[:cnt.rays],
+                          points=pts[:6 * cnt.rays].reshape(-1, 6))
             if with_paths == "arrays":
-                # the whole path set as flat arrays (cheap at 1e5-1e6 paths)
-                A = np.ctypeslib.as_array(P)
-                paths = {k: np.array(A[k]) for k in ("request", "receiver", "launch", "heap",
-                                                     "ray_offset", "n_rays", "field",
-                                                     "near_edge")}
-                paths.update(tri=tri[:cnt.rays], cop=cop[:cnt.rays], kind=kind[:cnt.rays],
-                             points=pts[:6 * cnt.rays].reshape(-1, 6))
-                P = ()
-            for p in P:
-                o, n = int(p.ray_offset), int(p.n_rays)
-                paths.append({
-                    "request": p.request, "receiver": p.receiver, "launch": int(p.launch),
-                    "heap": p.heap, "n_rays": n, "tri": tri[o:o + n].tolist(),
-                    "cop": cop[o:o + n].tolist(), "kind": kind[o:o + n].tolist(),
-                    "points": pts[6 * o:6 * (o + n)].reshape(n, 6).copy(),
-                    "field": np.array(p.field[:], np.float64), "near_edge": p.near_edge})
+                paths = arrays
+            else:  # one dict per path, sliced from the flat arrays
+                cols = {k: arrays[k].tolist() for k in ("request", "receiver", "launch", "heap",
+                                                        "ray_offset", "n_rays", "near_edge")}
+                tl, cl, kl = (arrays[k].tolist() for k in ("tri", "cop", "kind"))
+                pts6, fld = arrays["points"], arrays["field"]
+                for i in range(int(cnt.paths)):
+                    o, n = cols["ray_offset"][i], cols["n_rays"][i]
+                    paths.append({
+                        "request": cols["request"][i], "receiver": cols["receiver"][i],
+                        "launch": cols["launch"][i], "heap": cols["heap"][i], "n_rays": n,
+                        "tri": tl[o:o + n], "cop": cl[o:o + n], "kind": kl[o:o + n],
+                        "points": pts6[o:o + n], "field": fld[i],  # views
+                        "near_edge": cols["near_edge"][i]})
         field_c = f.view(np.complex128).reshape(-1, 3)  # exact, inf stays inf
         res = Result(field_c, counts, timing, paths)
         if n_rx:

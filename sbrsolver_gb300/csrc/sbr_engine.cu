@@ -32,6 +32,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <functional>
 #include <thread>
 #include <vector>
 
@@ -47,6 +48,7 @@
 #include "sbr_capture.cuh"
 #include "sbr_paths.cuh"
 #include "sbr_prep.cuh"
+#include "sbr_refbvh.cuh"
 
 namespace sbr {
 
@@ -285,6 +287,7 @@ struct SceneImpl {
   DevScene dev{};
   long long dev_bytes = 0;
   int n_cop = 0;
+  double prep_ms[6] = {};  // sbr_scene_info prep_* in order
   // launch directions per icosahedron level (0..12), resident once built
   std::mutex dirs_mu;
   std::vector<std::unique_ptr<DBuf<double>>> dirs;
@@ -336,75 +339,95 @@ static void pattern_params(const sbr_pattern* p, int scene_device, TxParams& P) 
   P.pat = reinterpret_cast<const float4*>(dev);
 }
 
+// Runs f(b, e) over slices of [0, n) on the host's cores.
+static void host_parallel(size_t n, const std::function<void(size_t, size_t)>& f) {
+  const size_t T = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), 32));
+  if (n < 8192 || T == 1) {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (size_t k = 1; k < T; ++k) pool.emplace_back(f, n * k / T, n * (k + 1) / T);
+  f(0, n / T);
+  for (auto& t : pool) t.join();
+}
+
 static void upload_scene(SceneImpl& S) {
   const HostScene& H = S.host;
   const int nt = int(H.tris.size()), nn = int(H.nodes.size());
   std::vector<Node32> n32(nn);
   std::vector<RefNode> ref(nn);
   const double margin_m = std::ldexp(H.extent + 1.0, -14);
-  for (int i = 0; i < nn; ++i) {
-    const HostNode& h = H.nodes[i];
-    RefNode& r = ref[i];
-    std::memcpy(r.bb, h.bb, sizeof r.bb);
-    r.flat = 0;
-    for (int a = 0; a < 6; ++a) r.fb[a] = float(h.bb[a]);
-    for (int a = 0; a < 3; ++a) {
-      // boxes of float vertices are floats; a non-float bound (empty box
-      // sentinel) disables the FP32 decision for that node
-      if (double(r.fb[a]) != h.bb[a] || double(r.fb[3 + a]) != h.bb[3 + a]) r.flat |= 8;
-      if (h.bb[a] == h.bb[3 + a]) r.flat |= 1 << a;
-    }
-    r.c0 = h.c0;
-    r.c1 = h.c1;
-    r.first = h.first;
-    r.count = h.count;
-    r.parent = h.parent;
-    Node32& m = n32[i];
-    std::memset(&m, 0, sizeof m);
-    if (h.c0 >= 0) {
-      const int cs[2] = {h.c0, h.c1};
-      for (int k = 0; k < 2; ++k) {
-        const HostNode& c = H.nodes[cs[k]];
-        float* lo = k == 0 ? m.lo0 : m.lo1;
-        float* hi = k == 0 ? m.hi0 : m.hi1;
-        for (int a = 0; a < 3; ++a) {
-          // outward rounding keeps the FP32 box around the FP64 one
-          lo[a] = std::nextafter(float(c.bb[a]), -INFINITY);
-          hi[a] = std::nextafter(float(c.bb[3 + a]), INFINITY);
+  host_parallel(size_t(nn), [&](size_t b, size_t e) {
+    for (int i = int(b); i < int(e); ++i) {
+      const HostNode& h = H.nodes[i];
+      RefNode& r = ref[i];
+      std::memcpy(r.bb, h.bb, sizeof r.bb);
+      r.flat = 0;
+      for (int a = 0; a < 6; ++a) r.fb[a] = float(h.bb[a]);
+      for (int a = 0; a < 3; ++a) {
+        // boxes of float vertices are floats; a non-float bound (empty box
+        // sentinel) disables the FP32 decision for that node
+        if (double(r.fb[a]) != h.bb[a] || double(r.fb[3 + a]) != h.bb[3 + a]) r.flat |= 8;
+        if (h.bb[a] == h.bb[3 + a]) r.flat |= 1 << a;
+      }
+      r.c0 = h.c0;
+      r.c1 = h.c1;
+      r.first = h.first;
+      r.count = h.count;
+      r.parent = h.parent;
+      Node32& m = n32[i];
+      std::memset(&m, 0, sizeof m);
+      if (h.c0 >= 0) {
+        const int cs[2] = {h.c0, h.c1};
+        for (int k = 0; k < 2; ++k) {
+          const HostNode& c = H.nodes[cs[k]];
+          float* lo = k == 0 ? m.lo0 : m.lo1;
+          float* hi = k == 0 ? m.hi0 : m.hi1;
+          for (int a = 0; a < 3; ++a) {
+            // outward rounding keeps the FP32 box around the FP64 one
+            lo[a] = std::nextafter(float(c.bb[a]), -INFINITY);
+            hi[a] = std::nextafter(float(c.bb[3 + a]), INFINITY);
+          }
+          m.child[k] = c.c0 >= 0 ? cs[k] : ~cs[k];
         }
-        m.child[k] = c.c0 >= 0 ? cs[k] : ~cs[k];
       }
     }
-  }
+  });
   std::vector<Tri32> t32(nt);
   std::vector<Tri64> t64(nt);
   std::vector<int> cop(nt), r2i(nt);
-  for (int r = 0; r < nt; ++r) {
-    const HostTri& t = H.tris[H.dfs_tris[r]];
-    Tri64& d = t64[r];
-    Tri32& f = t32[r];
-    for (int a = 0; a < 3; ++a) {
-      d.v1[a] = t.v1[a];
-      d.e1[a] = t.v2[a] - t.v1[a];
-      d.e2[a] = t.v3[a] - t.v1[a];
-      d.n[a] = t.n[a];
-      f.v1[a] = float(d.v1[a]);
-      f.e1[a] = float(d.e1[a]);
-      f.e2[a] = float(d.e2[a]);
+  host_parallel(size_t(nt), [&](size_t b, size_t e) {
+    for (int r = int(b); r < int(e); ++r) {
+      const HostTri& t = H.tris[H.dfs_tris[r]];
+      Tri64& d = t64[r];
+      Tri32& f = t32[r];
+      for (int a = 0; a < 3; ++a) {
+        d.v1[a] = t.v1[a];
+        d.e1[a] = t.v2[a] - t.v1[a];
+        d.e2[a] = t.v3[a] - t.v1[a];
+        d.n[a] = t.n[a];
+        f.v1[a] = float(d.v1[a]);
+        f.e1[a] = float(d.e1[a]);
+        f.e2[a] = float(d.e2[a]);
+      }
+      f.nv1 = float(std::sqrt(d.v1[0] * d.v1[0] + d.v1[1] * d.v1[1] + d.v1[2] * d.v1[2])) * 1.0001f;
+      f.ne1 = float(std::sqrt(d.e1[0] * d.e1[0] + d.e1[1] * d.e1[1] + d.e1[2] * d.e1[2])) * 1.0001f;
+      f.ne2 = float(std::sqrt(d.e2[0] * d.e2[0] + d.e2[1] * d.e2[1] + d.e2[2] * d.e2[2])) * 1.0001f;
+      d.id = t.id;
+      d.cop = t.cop;
+      d.mat = t.mat;
+      d.node = -1;
+      cop[r] = t.cop;
+      r2i[r] = t.id;
     }
-    f.nv1 = float(std::sqrt(d.v1[0] * d.v1[0] + d.v1[1] * d.v1[1] + d.v1[2] * d.v1[2])) * 1.0001f;
-    f.ne1 = float(std::sqrt(d.e1[0] * d.e1[0] + d.e1[1] * d.e1[1] + d.e1[2] * d.e1[2])) * 1.0001f;
-    f.ne2 = float(std::sqrt(d.e2[0] * d.e2[0] + d.e2[1] * d.e2[1] + d.e2[2] * d.e2[2])) * 1.0001f;
-    d.id = t.id;
-    d.cop = t.cop;
-    d.mat = t.mat;
-    d.node = -1;
-    cop[r] = t.cop;
-    r2i[r] = t.id;
-  }
-  for (int i = 0; i < nn; ++i)
-    if (H.nodes[i].c0 < 0)
-      for (int r = H.nodes[i].first; r < H.nodes[i].first + H.nodes[i].count; ++r) t64[r].node = i;
+  });
+  host_parallel(size_t(nn), [&](size_t b, size_t e) {
+    for (int i = int(b); i < int(e); ++i)
+      if (H.nodes[i].c0 < 0)
+        for (int r = H.nodes[i].first; r < H.nodes[i].first + H.nodes[i].count; ++r)
+          t64[r].node = i;
+  });
   S.n_cop = 0;
   for (auto& t : H.tris) S.n_cop = std::max(S.n_cop, t.cop + 1);
   std::vector<Material> mats(S.materials.size());
@@ -420,20 +443,24 @@ static void upload_scene(SceneImpl& S) {
   {  // search BVH
     const SearchBVH& B = H.search;
     std::vector<Node32> sn(B.nodes.size());
-    for (size_t i = 0; i < B.nodes.size(); ++i) {
-      Node32& m = sn[i];
-      std::memset(&m, 0, sizeof m);
-      for (int a = 0; a < 3; ++a) {
-        m.lo0[a] = B.nodes[i].lo[0][a];
-        m.hi0[a] = B.nodes[i].hi[0][a];
-        m.lo1[a] = B.nodes[i].lo[1][a];
-        m.hi1[a] = B.nodes[i].hi[1][a];
+    host_parallel(B.nodes.size(), [&](size_t lo, size_t hi) {
+      for (size_t i = lo; i < hi; ++i) {
+        Node32& m = sn[i];
+        std::memset(&m, 0, sizeof m);
+        for (int a = 0; a < 3; ++a) {
+          m.lo0[a] = B.nodes[i].lo[0][a];
+          m.hi0[a] = B.nodes[i].hi[0][a];
+          m.lo1[a] = B.nodes[i].lo[1][a];
+          m.hi1[a] = B.nodes[i].hi[1][a];
+        }
+        m.child[0] = B.nodes[i].child[0];
+        m.child[1] = B.nodes[i].child[1];
       }
-      m.child[0] = B.nodes[i].child[0];
-      m.child[1] = B.nodes[i].child[1];
-    }
+    });
     std::vector<Tri32> st32(B.order.size());
-    for (size_t j = 0; j < B.order.size(); ++j) st32[j] = t32[B.order[j]];
+    host_parallel(B.order.size(), [&](size_t lo, size_t hi) {
+      for (size_t j = lo; j < hi; ++j) st32[j] = t32[B.order[j]];
+    });
     S.snode.upload(sn.data(), sn.size(), st);
     S.stri.upload(st32.data(), st32.size(), st);
     S.srank.upload(B.order.data(), B.order.size(), st);
@@ -443,23 +470,28 @@ static void upload_scene(SceneImpl& S) {
     CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
   }
   {  // every reference leaf's boxes up to the root, one run per leaf
-    std::vector<AncBox> ab;
+    // (the leaf, its ancestors to the root, then an end marker)
     std::vector<int> off(nn, -1);
+    size_t total = 0;
     for (int i = 0; i < nn; ++i) {
       if (H.nodes[i].c0 >= 0) continue;
-      off[i] = int(ab.size());
-      for (int n = i; n >= 0; n = H.nodes[n].parent) {
-        AncBox b;
-        std::memcpy(b.fb, ref[n].fb, sizeof b.fb);
-        b.flat = ref[n].flat;
-        b.node = n;
-        ab.push_back(b);
-      }
-      AncBox end;
-      std::memset(&end, 0, sizeof end);
-      end.node = -1;
-      ab.push_back(end);
+      off[i] = int(total);
+      total += size_t(H.nodes[i].depth) + 2;
     }
+    std::vector<AncBox> ab(total);
+    host_parallel(size_t(nn), [&](size_t lo, size_t hi) {
+      for (int i = int(lo); i < int(hi); ++i) {
+        if (H.nodes[i].c0 >= 0) continue;
+        AncBox* o = &ab[size_t(off[i])];
+        for (int n = i; n >= 0; n = H.nodes[n].parent, ++o) {
+          std::memcpy(o->fb, ref[n].fb, sizeof o->fb);
+          o->flat = ref[n].flat;
+          o->node = n;
+        }
+        std::memset(o, 0, sizeof *o);
+        o->node = -1;
+      }
+    });
     S.anc.upload(ab.data(), ab.size(), st);
     S.anc_off.upload(off.data(), off.size(), st);
     S.dev.anc = S.anc.p;
@@ -493,32 +525,34 @@ static void upload_mesh_order(SceneImpl& S, const std::vector<int>& order) {
   const HostScene& H = S.host;
   const int nt = int(H.tris.size());
   std::vector<CorrTri> c(nt);
-  for (int i = 0; i < nt; ++i) {
-    const HostTri& t = H.tris[order[i]];
-    CorrTri& d = c[i];
-    for (int a = 0; a < 3; ++a) {
-      d.v1[a] = t.v1[a];
-      d.e1[a] = t.v2[a] - t.v1[a];
-      d.e2[a] = t.v3[a] - t.v1[a];
-      d.n[a] = t.n[a];
-    }
-    std::memcpy(d.cs, t.cs, sizeof d.cs);
-    d.mat = t.mat;
-    d.pad = 0;
-  }
   std::vector<Tri32> c32(nt);
-  for (int i = 0; i < nt; ++i) {
-    Tri32& f = c32[i];
-    for (int a = 0; a < 3; ++a) {
-      f.v1[a] = float(c[i].v1[a]);
-      f.e1[a] = float(c[i].e1[a]);
-      f.e2[a] = float(c[i].e2[a]);
+  host_parallel(size_t(nt), [&](size_t lo, size_t hi) {
+    for (int i = int(lo); i < int(hi); ++i) {
+      const HostTri& t = H.tris[order[i]];
+      CorrTri& d = c[i];
+      for (int a = 0; a < 3; ++a) {
+        d.v1[a] = t.v1[a];
+        d.e1[a] = t.v2[a] - t.v1[a];
+        d.e2[a] = t.v3[a] - t.v1[a];
+        d.n[a] = t.n[a];
+      }
+      std::memcpy(d.cs, t.cs, sizeof d.cs);
+      d.mat = t.mat;
+      d.pad = 0;
     }
-    auto n3 = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
-    f.nv1 = float(n3(c[i].v1)) * 1.0001f;
-    f.ne1 = float(n3(c[i].e1)) * 1.0001f;
-    f.ne2 = float(n3(c[i].e2)) * 1.0001f;
-  }
+    for (int i = int(lo); i < int(hi); ++i) {
+      Tri32& f = c32[i];
+      for (int a = 0; a < 3; ++a) {
+        f.v1[a] = float(c[i].v1[a]);
+        f.e1[a] = float(c[i].e1[a]);
+        f.e2[a] = float(c[i].e2[a]);
+      }
+      auto n3 = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+      f.nv1 = float(n3(c[i].v1)) * 1.0001f;
+      f.ne1 = float(n3(c[i].e1)) * 1.0001f;
+      f.ne2 = float(n3(c[i].e2)) * 1.0001f;
+    }
+  });
   S.corr.upload(c.data(), c.size(), S.stream);
   S.corr32.upload(c32.data(), c32.size(), S.stream);
   S.dev.corr = S.corr.p;
@@ -669,6 +703,12 @@ static int grid_for(long long n, int block) {
   return int(std::max<long long>(1, std::min<long long>(g, (long long)device_sms() * 32)));
 }
 
+// Blocks to give every one of n items its own thread (no cap: for kernels
+// without a grid-stride loop).
+static int grid_all(long long n, int block) {
+  return int(std::max<long long>(1, (n + block - 1) / block));
+}
+
 // ------------------------------------------------------------ scene preparation on the device
 
 // What the device builds of a scene (sbr_prep.cuh): per triangle (file
@@ -679,6 +719,12 @@ struct DeviceTables {
   std::vector<double> cs, bb, center;
   SearchBVH search;
   int degenerate = 0;
+  // the reference BVH: nodes depth-first, leaf triangle order, the caller's
+  // triangle order after BVH::ConstructBVH
+  std::vector<HostNode> nodes;
+  std::vector<int> dfs_tris, mesh_order;
+  int max_depth = 0;
+  double tables_ms = 0, search_ms = 0, ref_ms = 0;  // wall time of each part
 };
 
 template <class T>
@@ -687,9 +733,19 @@ static void swap_buf(DBuf<T>& a, DBuf<T>& b) {
   std::swap(a.n, b.n);
 }
 
+// Exclusive scan of in[0, n) into out[0, n], out[n] = total, over many
+// blocks; sums: scratch of at least n / kScanTile + 1 ints.
+static void scan_exclusive(const int* in, int* out, int n, int* sums, cudaStream_t st) {
+  const int nb = std::max(1, (n + kScanTile - 1) / kScanTile);
+  k_tile_sums<<<nb, kScanThreads, 0, st>>>(in, n, sums);
+  k_sums_scan<<<1, 1024, 0, st>>>(sums, nb, out + n);
+  k_tile_scan<<<nb, kScanThreads, 0, st>>>(in, n, sums, out);
+}
+
 // Stable LSD radix sort of perm by word[perm[i]], one varying bit per pass.
 static void sort_perm_by(DBuf<int>& perm, DBuf<int>& tmp, DBuf<int>& flags, DBuf<int>& scan,
-                         DBuf<unsigned>& vb, const uint32_t* word, int n, cudaStream_t st) {
+                         DBuf<int>& sums, DBuf<unsigned>& vb, const uint32_t* word, int n,
+                         cudaStream_t st) {
   if (n < 2) return;
   CK(cudaMemsetAsync(vb.p, 0, sizeof(unsigned), st));
   prep::k_varying_bits<<<grid_for(n, 256), 256, 0, st>>>(word, n, vb.p);
@@ -699,23 +755,256 @@ static void sort_perm_by(DBuf<int>& perm, DBuf<int>& tmp, DBuf<int>& flags, DBuf
   for (int b = 0; b < 32; ++b) {
     if (!((bits >> b) & 1u)) continue;
     prep::k_bit_flags<<<grid_for(n, 256), 256, 0, st>>>(word, perm.p, n, b, flags.p);
-    k_scan_exclusive<<<1, 1024, 0, st>>>(flags.p, scan.p, n);
+    scan_exclusive(flags.p, scan.p, n, sums.p, st);
     prep::k_bit_scatter<<<grid_for(n, 256), 256, 0, st>>>(word, perm.p, n, b, scan.p, tmp.p);
     swap_buf(perm, tmp);
   }
   CK(cudaGetLastError());
 }
 
+// The reference BVH on the device (sbr_refbvh.cuh), one tree level at a
+// time: each level's nodes get their box, three exact sorts with a surface
+// area sweep each, and a final sort along the chosen axis; the host then
+// numbers the nodes depth-first as the host build does.  v: the device
+// copy of the vertices (9 floats per triangle).
+struct RefSort {
+  DBuf<double> key;
+  DBuf<int> idx, lpos, rpos, tile_seg, cnt_l, cnt_r, off_l, off_r;
+  DBuf<int2> totals;
+  DBuf<refbvh::SortSeg> big, big_next, small, tiny, heap;
+  DBuf<int> ctl;
+  int sms = 1;
+};
+
+static int read_ctl(RefSort& R, int* h, cudaStream_t st) {
+  CK(cudaMemcpyAsync(h, R.ctl.p, sizeof(int) * refbvh::kCtlWords, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (h[refbvh::kError])
+    throw std::string("device reference BVH: sort invariant violated (code ") +
+        std::to_string(h[refbvh::kError]) + ")";
+  return 0;
+}
+
+// Sorts the objects of the listed nodes (of their split nodes when `best`
+// is given) by key, in the reference sort's order; idx receives the
+// permutation.
+static void ref_sort(RefSort& R, const refbvh::RNode* nodes, const int* active, int m,
+                     const refbvh::NodeBest* best, cudaStream_t st) {
+  using namespace refbvh;
+  int h[kCtlWords];
+  CK(cudaMemsetAsync(R.ctl.p, 0, sizeof(int) * kNodes, st));  // list counters only
+  k_file_nodes<<<grid_all(m, 128), 128, 0, st>>>(nodes, active, m, best, R.big.p, R.small.p,
+                                                 R.tiny.p, R.heap.p, R.ctl.p);
+  CK(cudaGetLastError());
+  read_ctl(R, h, st);
+  int n_big = h[kBig], n_tiles = h[kTiles];
+  for (int round = 0; n_big > 0; ++round) {
+    if (round > 64) throw std::string("device reference BVH: too many partition rounds");
+    k_tile_map<<<n_big, 256, 0, st>>>(R.big.p, R.ctl.p + kBig, R.tile_seg.p);
+    k_pivot<<<grid_all(n_big, 128), 128, 0, st>>>(R.big.p, n_big, R.key.p, R.idx.p);
+    k_count<<<n_tiles, kTileThreads, 0, st>>>(R.big.p, R.tile_seg.p, R.key.p, R.cnt_l.p,
+                                              R.cnt_r.p);
+    k_tile_offsets<<<grid_all(n_big, 128), 128, 0, st>>>(R.big.p, n_big, R.cnt_l.p, R.cnt_r.p,
+                                                         R.off_l.p, R.off_r.p, R.totals.p);
+    k_stops<<<n_tiles, kTileThreads, 0, st>>>(R.big.p, R.tile_seg.p, R.key.p, R.off_l.p,
+                                              R.off_r.p, R.totals.p, R.lpos.p, R.rpos.p);
+    k_exchange<<<n_tiles, kTileThreads, 0, st>>>(R.big.p, R.tile_seg.p, R.totals.p, R.lpos.p,
+                                                 R.rpos.p, R.key.p, R.idx.p);
+    CK(cudaMemsetAsync(R.ctl.p + kBigNext, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(R.ctl.p + kTilesNext, 0, sizeof(int), st));
+    k_cut<<<grid_all(n_big, 128), 128, 0, st>>>(R.big.p, n_big, R.totals.p, R.lpos.p, R.rpos.p,
+                                                R.big_next.p, R.small.p, R.tiny.p, R.heap.p,
+                                                R.ctl.p);
+    CK(cudaGetLastError());
+    read_ctl(R, h, st);
+    n_big = h[kBigNext];
+    n_tiles = h[kTilesNext];
+    CK(cudaMemcpyAsync(R.ctl.p + kBig, R.ctl.p + kBigNext, sizeof(int), cudaMemcpyDeviceToDevice,
+                       st));
+    std::swap(R.big.p, R.big_next.p);
+    std::swap(R.big.n, R.big_next.n);
+  }
+  if (h[kSmall])
+    k_small<<<std::min(h[kSmall], R.sms * 8), 32, kSmallSmem, st>>>(R.small.p, R.ctl.p + kSmall,
+                                                                    R.key.p, R.idx.p, R.ctl.p);
+  if (h[kTiny])
+    k_tiny<<<grid_all(h[kTiny], 128), 128, 0, st>>>(R.tiny.p, R.ctl.p + kTiny, R.key.p, R.idx.p);
+  if (h[kHeap])
+    k_heap<<<grid_all(h[kHeap], 64), 64, 0, st>>>(R.heap.p, R.ctl.p + kHeap, R.key.p, R.idx.p);
+  CK(cudaGetLastError());
+}
+
+static void device_ref_bvh(const float* v, int nt, cudaStream_t st, DeviceTables& T) {
+  using namespace refbvh;
+  const int n = nt;
+  const size_t nz = size_t(std::max(1, n));
+  DBuf<float4> lo, hi, lo2, hi2;
+  lo.ensure(nz);
+  hi.ensure(nz);
+  lo2.ensure(nz);
+  hi2.ensure(nz);
+  k_boxes<<<grid_all(n, 256), 256, 0, st>>>(v, nt, lo.p, hi.p);
+  RefSort R;
+  R.sms = device_sms();
+  R.key.ensure(nz);
+  R.idx.ensure(nz);
+  R.lpos.ensure(nz);
+  R.rpos.ensure(nz);
+  const size_t tiles = nz / (kTile / 2) + 16, lists = nz / 2 + 16;
+  R.tile_seg.ensure(tiles);
+  R.cnt_l.ensure(tiles);
+  R.cnt_r.ensure(tiles);
+  R.off_l.ensure(tiles);
+  R.off_r.ensure(tiles);
+  R.totals.ensure(nz / kSmallMax + 16);
+  R.big.ensure(nz / kSmallMax + 16);
+  R.big_next.ensure(nz / kSmallMax + 16);
+  R.small.ensure(lists);
+  R.tiny.ensure(lists);
+  R.heap.ensure(lists);
+  R.ctl.ensure(kCtlWords);
+  CK(cudaMemsetAsync(R.ctl.p, 0, sizeof(int) * kCtlWords, st));
+  DBuf<RNode> nodes;
+  nodes.ensure(2 * nz + 1);
+  DBuf<NodeBest> best;
+  best.ensure(nz);
+  const size_t tcap = nz + nz / kWarpTile + 16;  // warp tiles of a level
+  DBuf<int2> node_tiles;
+  node_tiles.ensure(nz);
+  DBuf<int> tile_node;
+  tile_node.ensure(tcap);
+  DBuf<ExactBox> tbox;
+  tbox.ensure(tcap);
+  DBuf<BoxF> tagg, pre, post;
+  tagg.ensure(tcap);
+  pre.ensure(tcap);
+  post.ensure(tcap);
+  DBuf<TileBest> tbest;
+  tbest.ensure(tcap);
+  DBuf<double> sa_root;
+  sa_root.ensure(nz);
+  DBuf<int> node_of, active, next, ids, mesh;
+  node_of.ensure(nz);
+  active.ensure(nz);
+  next.ensure(nz);
+  ids.ensure(nz);
+  mesh.ensure(nz);
+  {
+    RNode root{};
+    root.f = 0;
+    root.l = n;
+    root.c0 = root.c1 = -1;
+    nodes.upload(&root, 1, st);
+    const int zero = 0, one = 1;
+    active.upload(&zero, 1, st);
+    CK(cudaMemcpyAsync(R.ctl.p + kNodes, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+  }
+  int m = 1;
+  for (int level = 0; m > 0; ++level) {
+    if (level > 4096) throw std::string("device reference BVH: too many levels");
+    CK(cudaMemsetAsync(node_of.p, 0xff, sizeof(int) * nz, st));
+    CK(cudaMemsetAsync(R.ctl.p + kSweepTiles, 0, sizeof(int), st));
+    k_level_tiles<<<grid_all(m, 128), 128, 0, st>>>(nodes.p, active.p, m, node_tiles.p,
+                                                    tile_node.p, R.ctl.p);
+    int hl[kCtlWords];
+    read_ctl(R, hl, st);
+    const int n_tiles = hl[kSweepTiles];
+    const long long tile_threads = 32LL * n_tiles, node_threads = 32LL * m;
+    k_tile_exact_box<<<grid_all(tile_threads, 256), 256, 0, st>>>(
+        nodes.p, active.p, node_tiles.p, tile_node.p, n_tiles, lo.p, hi.p, node_of.p, tbox.p);
+    k_node_box<<<grid_all(node_threads, 256), 256, 0, st>>>(nodes.p, active.p, m, node_tiles.p,
+                                                            tbox.p, sa_root.p, best.p);
+    for (int axis = 0; axis <= 3; ++axis) {  // x, y, z, then the chosen axis
+      const NodeBest* b = axis == 3 ? best.p : nullptr;
+      k_keys<<<grid_all(n, 256), 256, 0, st>>>(lo.p, hi.p, node_of.p, b, axis, n, R.key.p,
+                                               R.idx.p);
+      ref_sort(R, nodes.p, active.p, m, b, st);
+      k_gather<<<grid_all(n, 256), 256, 0, st>>>(lo.p, hi.p, R.idx.p, n, lo2.p, hi2.p);
+      std::swap(lo.p, lo2.p);
+      std::swap(hi.p, hi2.p);
+      if (axis < 3) {  // the surface area sweep over this order
+        k_tile_boxes<<<grid_all(tile_threads, 256), 256, 0, st>>>(
+            nodes.p, active.p, node_tiles.p, tile_node.p, n_tiles, lo.p, hi.p, tagg.p);
+        k_tile_carries<<<grid_all(node_threads, 256), 256, 0, st>>>(node_tiles.p, m, tagg.p,
+                                                                    pre.p, post.p);
+        k_tile_sweep<<<grid_all(tile_threads, 256), 256, 0, st>>>(
+            nodes.p, active.p, node_tiles.p, tile_node.p, n_tiles, lo.p, hi.p, pre.p, post.p,
+            sa_root.p, tbest.p);
+        k_node_best<<<grid_all(node_threads, 256), 256, 0, st>>>(node_tiles.p, m, tbest.p,
+                                                                 axis, best.p);
+      }
+    }
+    if (level == 0) k_ids<<<grid_all(n, 256), 256, 0, st>>>(lo.p, n, mesh.p);
+    CK(cudaMemsetAsync(R.ctl.p + kActiveNext, 0, sizeof(int), st));
+    k_children<<<grid_all(m, 128), 128, 0, st>>>(nodes.p, active.p, m, best.p, next.p, R.ctl.p);
+    CK(cudaGetLastError());
+    int h[kCtlWords];
+    read_ctl(R, h, st);
+    m = h[kActiveNext];
+    std::swap(active.p, next.p);
+  }
+  int h[kCtlWords];
+  read_ctl(R, h, st);
+  const int n_nodes = h[kNodes];
+  k_ids<<<grid_all(n, 256), 256, 0, st>>>(lo.p, n, ids.p);
+  std::vector<RNode> rn(static_cast<size_t>(n_nodes));
+  std::vector<int> order(nz);
+  T.mesh_order.resize(nz);
+  CK(cudaMemcpyAsync(rn.data(), nodes.p, sizeof(RNode) * n_nodes, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(order.data(), ids.p, sizeof(int) * nz, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(T.mesh_order.data(), mesh.p, sizeof(int) * nz, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  T.mesh_order.resize(size_t(n));
+  // depth-first numbering, children[0] first (sbr_host.cpp prepare_scene)
+  T.nodes.clear();
+  T.nodes.reserve(size_t(n_nodes));
+  T.dfs_tris.clear();
+  T.dfs_tris.reserve(size_t(n));
+  T.max_depth = 0;
+  struct Item {
+    int b, parent, depth, which;
+  };
+  std::vector<Item> stack{{0, -1, 0, 0}};
+  while (!stack.empty()) {
+    const Item it = stack.back();
+    stack.pop_back();
+    const int me = int(T.nodes.size());
+    T.nodes.emplace_back();
+    HostNode& hn = T.nodes.back();
+    const RNode& r = rn[size_t(it.b)];
+    std::memcpy(hn.bb, r.bb, sizeof hn.bb);
+    hn.parent = it.parent;
+    hn.depth = it.depth;
+    T.max_depth = std::max(T.max_depth, it.depth);
+    if (it.parent >= 0) {
+      if (it.which == 0) T.nodes[size_t(it.parent)].c0 = me;
+      else T.nodes[size_t(it.parent)].c1 = me;
+    }
+    if (r.c0 < 0) {
+      hn.first = int(T.dfs_tris.size());
+      hn.count = r.l - r.f;
+      T.dfs_tris.insert(T.dfs_tris.end(), order.begin() + r.f, order.begin() + r.l);
+    } else {
+      stack.push_back({r.c1, me, it.depth + 1, 1});
+      stack.push_back({r.c0, me, it.depth + 1, 0});
+    }
+  }
+}
+
 // Builds the tables on the current device, on stream st.  v: 9 floats per
 // triangle, nrm: 3.
 static void device_prepare(const float* v_host, const float* n_host, int nt, cudaStream_t st,
                            DeviceTables& T) {
+  auto ms_since = [](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+  };
+  auto t0 = std::chrono::steady_clock::now();
   const int nv = 3 * nt, ne = 3 * nt;
   DBuf<float> v, nrm;
   v.upload(v_host, 9 * size_t(nt), st);
   nrm.upload(n_host, 3 * size_t(nt), st);
   DBuf<uint32_t> wx, wy, wz;
-  DBuf<int> perm, tmp, flags, scan, uid, parent, misc;
+  DBuf<int> perm, tmp, flags, scan, uid, parent, misc, sums;
   DBuf<unsigned> vb;
   const size_t big = size_t(std::max(nv, ne));
   wx.ensure(big);
@@ -725,24 +1014,25 @@ static void device_prepare(const float* v_host, const float* n_host, int nt, cud
   tmp.ensure(big);
   flags.ensure(big);
   scan.ensure(big + 1);
+  sums.ensure(big / kScanTile + 2);
   uid.ensure(nv);
   parent.ensure(nt);
   misc.ensure(4);
   vb.ensure(1);
   // -- vertex merge: sort the vertices by (x, y, z) bits, number the runs
   prep::k_vertex_words<<<grid_for(nv, 256), 256, 0, st>>>(v.p, nv, wx.p, wy.p, wz.p, perm.p);
-  sort_perm_by(perm, tmp, flags, scan, vb, wz.p, nv, st);
-  sort_perm_by(perm, tmp, flags, scan, vb, wy.p, nv, st);
-  sort_perm_by(perm, tmp, flags, scan, vb, wx.p, nv, st);
+  sort_perm_by(perm, tmp, flags, scan, sums, vb, wz.p, nv, st);
+  sort_perm_by(perm, tmp, flags, scan, sums, vb, wy.p, nv, st);
+  sort_perm_by(perm, tmp, flags, scan, sums, vb, wx.p, nv, st);
   prep::k_run_starts<<<grid_for(nv, 256), 256, 0, st>>>(wx.p, wy.p, wz.p, perm.p, nv, flags.p);
-  k_scan_exclusive<<<1, 1024, 0, st>>>(flags.p, scan.p, nv);
+  scan_exclusive(flags.p, scan.p, nv, sums.p, st);
   prep::k_vertex_ids<<<grid_for(nv, 256), 256, 0, st>>>(perm.p, flags.p, scan.p, nv, uid.p);
   // -- edges of merged vertices, grouped by sorting; coplanar groups by
   // hooking roots until no pair of an edge's triangles has two roots
   CK(cudaMemsetAsync(misc.p, 0, 4 * sizeof(int), st));
   prep::k_edges<<<grid_for(nt, 256), 256, 0, st>>>(uid.p, nt, wx.p, wy.p, perm.p, misc.p);
-  sort_perm_by(perm, tmp, flags, scan, vb, wy.p, ne, st);  // larger id first (LSD)
-  sort_perm_by(perm, tmp, flags, scan, vb, wx.p, ne, st);
+  sort_perm_by(perm, tmp, flags, scan, sums, vb, wy.p, ne, st);  // larger id first (LSD)
+  sort_perm_by(perm, tmp, flags, scan, sums, vb, wx.p, ne, st);
   prep::k_run_starts<<<grid_for(ne, 256), 256, 0, st>>>(wx.p, wy.p, nullptr, perm.p, ne, flags.p);
   {
     std::vector<int> id(nt);
@@ -761,7 +1051,7 @@ static void device_prepare(const float* v_host, const float* n_host, int nt, cud
     if (!changed) break;
   }
   prep::k_compress<<<grid_for(nt, 256), 256, 0, st>>>(parent.p, nt, tmp.p);
-  k_scan_exclusive<<<1, 1024, 0, st>>>(tmp.p, scan.p, nt);
+  scan_exclusive(tmp.p, scan.p, nt, sums.p, st);
   DBuf<int> cop;
   cop.ensure(nt);
   prep::k_group_ids<<<grid_for(nt, 256), 256, 0, st>>>(parent.p, scan.p, nt, cop.p);
@@ -772,6 +1062,13 @@ static void device_prepare(const float* v_host, const float* n_host, int nt, cud
   center.ensure(3 * size_t(nt));
   prep::k_frames<<<grid_for(nt, 128), 128, 0, st>>>(v.p, nrm.p, nt, cs.p, bb.p, center.p);
   CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  T.tables_ms = ms_since(t0);
+  // -- the reference BVH
+  t0 = std::chrono::steady_clock::now();
+  device_ref_bvh(v.p, nt, st, T);
+  T.ref_ms = ms_since(t0);
+  t0 = std::chrono::steady_clock::now();
   // -- search BVH, one level of nodes at a time
   DBuf<float> blo, bhi, cen;
   blo.ensure(3 * size_t(nt));
@@ -829,6 +1126,7 @@ static void device_prepare(const float* v_host, const float* n_host, int nt, cud
   CK(cudaMemcpyAsync(rb, root_box.p, sizeof rb, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaMemcpy(&T.degenerate, misc.p, sizeof(int), cudaMemcpyDeviceToHost));
+  T.search_ms = ms_since(t0);
   if (c[4]) throw std::string("device search BVH: a median split of more than 8192 triangles");
   const int n_nodes = c[0];
   std::vector<prep::BNode> bn(size_t(std::max(1, n_nodes)));
@@ -1787,6 +2085,11 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
       for (int i = 0; i < nt; ++i)
         if (mat_ids[i] < 0 || mat_ids[i] >= n_materials)
           throw std::string("material id out of range at triangle ") + std::to_string(i);
+    const auto t_start = std::chrono::steady_clock::now();
+    auto ms_since = [](std::chrono::steady_clock::time_point a) {
+      return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a)
+          .count();
+    };
     auto sc = std::make_unique<sbr_scene>();
     SceneImpl& S = sc->impl;
     std::string err;
@@ -1797,9 +2100,9 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
     }
     CK(cudaGetDevice(&S.device));
     CK(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
-    // The device builds the coplanar groups, frames and search BVH on its own
-    // host thread and stream while this thread builds the reference BVH
-    // (SBR_SCENE_HOST_PREP: everything on the host).
+    // The device builds the coplanar groups, frames, search BVH and
+    // reference BVH on its own host thread and stream while this thread forms
+    // the triangle records (SBR_SCENE_HOST_PREP: everything on the host).
     const bool on_device = !(flags & SBR_SCENE_HOST_PREP);
     DeviceTables dt;
     std::string dev_err;
@@ -1834,8 +2137,14 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
         if (t.joinable()) t.join();
       }
     } join{dev_thread};
-    const bool host_ok = prepare_scene(nt, v.data(), n.data(), mat_ids, S.host, err, !on_device);
+    const auto t_host = std::chrono::steady_clock::now();
+    const bool host_ok =
+        prepare_scene(nt, v.data(), n.data(), mat_ids, S.host, err, !on_device, !on_device);
+    S.prep_ms[1] = ms_since(t_host);
     if (dev_thread.joinable()) dev_thread.join();
+    S.prep_ms[2] = dt.tables_ms;
+    S.prep_ms[3] = dt.search_ms;
+    S.prep_ms[4] = dt.ref_ms;
     if (!host_ok) throw err;
     if (on_device) {
       if (dev_failed) {
@@ -1850,6 +2159,10 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
         tr.cop = dt.cop[size_t(t)];
         std::memcpy(tr.cs, &dt.cs[9 * size_t(t)], sizeof tr.cs);
       }
+      S.host.nodes = std::move(dt.nodes);
+      S.host.dfs_tris = std::move(dt.dfs_tris);
+      S.host.mesh_order = std::move(dt.mesh_order);
+      S.host.max_depth = dt.max_depth;
       S.host.search = std::move(dt.search);
       map_search_order(S.host);
     }
@@ -1857,8 +2170,12 @@ static sbr_status scene_common(std::vector<float>& v, std::vector<float>& n, con
       throw std::string("BVH depth ") + std::to_string(S.host.max_depth) +
           " exceeds the traversal stack (" + std::to_string(kStack) + ")";
     S.materials.assign(materials, materials + n_materials);
+    const auto t_up = std::chrono::steady_clock::now();
     upload_scene(S);
     upload_mesh_order(S, S.host.mesh_order);
+    CK(cudaStreamSynchronize(S.stream));
+    S.prep_ms[5] = ms_since(t_up);
+    S.prep_ms[0] = ms_since(t_start);
     *out = sc.release();
     return SBR_OK;
   })
@@ -1922,6 +2239,38 @@ sbr_status sbr_scene_search_bvh(const sbr_scene* scene, int* n_nodes, int* max_d
   return SBR_OK;
 }
 
+sbr_status sbr_scene_reference_bvh(const sbr_scene* scene, int* n_nodes, int* max_depth,
+                                   double* boxes, int* links, int* order) {
+  if (!scene || !n_nodes) {
+    set_err("sbr_scene_reference_bvh: NULL argument");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const HostScene& H = scene->impl.host;
+  const int nn = int(H.nodes.size());
+  if ((boxes || links) && *n_nodes < nn) {
+    set_err("sbr_scene_reference_bvh: node buffers too small");
+    *n_nodes = nn;
+    return SBR_ERR_CAPACITY;
+  }
+  *n_nodes = nn;
+  if (max_depth) *max_depth = H.max_depth;
+  for (int k = 0; k < nn; ++k) {
+    const HostNode& h = H.nodes[size_t(k)];
+    if (boxes) std::memcpy(boxes + 6 * size_t(k), h.bb, sizeof h.bb);
+    if (links) {
+      int* o = links + 6 * size_t(k);
+      o[0] = h.c0;
+      o[1] = h.c1;
+      o[2] = h.first;
+      o[3] = h.count;
+      o[4] = h.parent;
+      o[5] = h.depth;
+    }
+  }
+  if (order) std::memcpy(order, H.dfs_tris.data(), sizeof(int) * H.dfs_tris.size());
+  return SBR_OK;
+}
+
 sbr_status sbr_scene_create_from_stl(const char* path, const int* material_ids,
                                      const sbr_material* materials, int n_materials,
                                      sbr_scene** out) {
@@ -1946,6 +2295,12 @@ sbr_status sbr_scene_info_get(const sbr_scene* scene, sbr_scene_info* out) {
   out->n_coplanar = S.n_cop;
   out->extent = S.host.extent;
   out->device_bytes = S.dev_bytes;
+  out->prep_total_ms = S.prep_ms[0];
+  out->prep_host_ms = S.prep_ms[1];
+  out->prep_device_tables_ms = S.prep_ms[2];
+  out->prep_search_bvh_ms = S.prep_ms[3];
+  out->prep_reference_bvh_ms = S.prep_ms[4];
+  out->prep_upload_ms = S.prep_ms[5];
   return SBR_OK;
 }
 

@@ -194,6 +194,78 @@ __global__ void k_scan_exclusive(const int* in, int* out, int n) {
   if (t == T - 1) out[n] = part[T - 1];
 }
 
+// Exclusive scan of n ints over many blocks (same result as k_scan_exclusive,
+// out[n] = total): tile sums, one block scans the sums, then every tile
+// scans its items from its offset.  Thread t of a tile owns kScanItems
+// consecutive items.
+constexpr int kScanThreads = 512, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_scan_incl(int v, int* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += y;
+  }
+  if (lane == 31) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    int t = lane < nw ? sh[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < nw) sh[lane] = t;
+  }
+  __syncthreads();
+  const int r = v + (w ? sh[w - 1] : 0);
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_tile_sums(const int* in, int n, int* sums) {
+  __shared__ int sh[32];
+  const long long base = (long long)blockIdx.x * kScanTile;
+  int s = 0;
+  for (int i = threadIdx.x; i < kScanTile; i += blockDim.x)
+    if (base + i < n) s += in[base + i];
+  s = block_scan_incl(s, sh);
+  if (threadIdx.x == blockDim.x - 1) sums[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(1024) k_sums_scan(int* sums, int nb, int* total) {
+  __shared__ int sh[32];
+  __shared__ int last;
+  int carry = 0;
+  for (int c = 0; c < nb; c += blockDim.x) {
+    const int i = c + threadIdx.x;
+    const int v = i < nb ? sums[i] : 0;
+    const int incl = block_scan_incl(v, sh);
+    if (i < nb) sums[i] = carry + incl - v;
+    if (threadIdx.x == blockDim.x - 1) last = incl;
+    __syncthreads();
+    carry += last;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_tile_scan(const int* in, int n, const int* sums,
+                                                            int* out) {
+  __shared__ int sh[32];
+  const long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int v[kScanItems];
+  int s = 0;
+  for (int j = 0; j < kScanItems; ++j) {
+    v[j] = base + j < n ? in[base + j] : 0;
+    s += v[j];
+  }
+  int run = sums[blockIdx.x] + block_scan_incl(s, sh) - s;
+  for (int j = 0; j < kScanItems; ++j) {
+    if (base + j < n) out[base + j] = run;
+    run += v[j];
+  }
+}
+
 __global__ void k_rx_scatter(const double* rx, const TxParams* txp, int n_tx, const RxGrid* grids,
                              const int* cell_base, const int* starts, int* cursor, float4* rx32) {
   const int r = blockIdx.y;

@@ -76,55 +76,79 @@ void merge_box(const double* b1, const double* b2, double* r) {
   }
 }
 
+// A triangle as the SAH build sees it: its box (float values: the box of
+// float vertices) and id.  The build permutes one array of these in place, a
+// node owning a contiguous range, so its sorts and sweeps read memory in
+// order instead of chasing ids into the triangle records.
+struct BuildRec {
+  float lo[3], hi[3];
+  int id, pad;
+  // the box centre exactly as the reference computes it (bb min + max) / 2
+  double center(int a) const { return (double(lo[a]) + double(hi[a])) / 2.0; }
+};
+
 struct BuildNode {
   double bb[6];
   int c0 = -1, c1 = -1;
-  std::vector<int> objs;  // leaf: triangle ids in the reference's order
+  int lo = 0, hi = 0;  // range of the build array; a leaf's triangles in the reference's order
 };
 
-// One step of the reference's SAH build (BVH/BVH.h:135-230) on a node whose
-// object list is `objs` (sorted in place exactly as the reference does).
-// Returns the split index, or -1 for a leaf.
-int sah_split(const std::vector<HostTri>& tris, std::vector<int>& objs, double* bb,
-              std::vector<double>& sa1, std::vector<double>& sa2) {
+struct SplitScratch {
+  std::vector<std::pair<double, int>> kv;
+  std::vector<BuildRec> tmp;
+  std::vector<double> sa1, sa2;
+};
+
+// One step of the reference's SAH build (BVH/BVH.h:135-230) on the node whose
+// objects are R[lo, hi) (sorted in place exactly as the reference sorts its
+// object list).  Returns the split index (relative to lo), or -1 for a leaf.
+int sah_split(std::vector<BuildRec>& R, int lo, int hi, double* bb, SplitScratch& s) {
+  const int n = hi - lo;
+  BuildRec* r = R.data() + lo;
   empty_box(bb);
-  for (int o : objs) merge_box(tris[o].bb, bb, bb);
-  const int n = int(objs.size());
+  for (int i = 0; i < n; ++i) {
+    const double b[6] = {r[i].lo[0], r[i].lo[1], r[i].lo[2], r[i].hi[0], r[i].hi[1], r[i].hi[2]};
+    merge_box(b, bb, bb);
+  }
   double best_cost = 1.0 * n;
   int best_axis = -1, best_split = -1;
   const double sa_root = surface_area(bb);
-  sa1.assign(size_t(n) + 1, std::numeric_limits<double>::max());
-  sa2.assign(size_t(n) + 1, std::numeric_limits<double>::max());
+  s.sa1.assign(size_t(n) + 1, std::numeric_limits<double>::max());
+  s.sa2.assign(size_t(n) + 1, std::numeric_limits<double>::max());
+  s.kv.resize(size_t(n));
+  s.tmp.resize(size_t(n));
   // std::sort's result depends only on the outcomes of its comparisons, so
-  // sorting (key, id) pairs by key leaves the ids in exactly the order the
-  // reference's sort of ids by tris[id].center[axis] does, with the keys at
-  // hand instead of behind an indirection.
-  std::vector<std::pair<double, int>> kv(objs.size());
+  // sorting (key, position) pairs by key and then moving the records leaves
+  // them in exactly the order the reference's sort of ids by
+  // tris[id].center[axis] does.
   auto sort_axis = [&](int axis) {
-    for (size_t i = 0; i < objs.size(); ++i) kv[i] = {tris[objs[i]].center[axis], objs[i]};
-    std::sort(kv.begin(), kv.end(), [](const std::pair<double, int>& a,
-                                       const std::pair<double, int>& b) { return a.first < b.first; });
-    for (size_t i = 0; i < objs.size(); ++i) objs[i] = kv[i].second;
+    for (int i = 0; i < n; ++i) s.kv[size_t(i)] = {r[i].center(axis), i};
+    std::sort(s.kv.begin(), s.kv.end(), [](const std::pair<double, int>& a,
+                                           const std::pair<double, int>& b) { return a.first < b.first; });
+    for (int i = 0; i < n; ++i) s.tmp[size_t(i)] = r[s.kv[size_t(i)].second];
+    std::copy(s.tmp.begin(), s.tmp.end(), r);
   };
   for (int axis = 0; axis < 3; ++axis) {
     sort_axis(axis);
     double b1[6];
     empty_box(b1);
-    sa1[0] = surface_area(b1);
+    s.sa1[0] = surface_area(b1);
     for (int i = 0; i < n; ++i) {
-      merge_box(b1, tris[objs[i]].bb, b1);
-      sa1[i] = surface_area(b1);
+      const double b[6] = {r[i].lo[0], r[i].lo[1], r[i].lo[2], r[i].hi[0], r[i].hi[1], r[i].hi[2]};
+      merge_box(b1, b, b1);
+      s.sa1[size_t(i)] = surface_area(b1);
     }
     double b2[6];
     empty_box(b2);
-    sa2[n] = surface_area(b2);
+    s.sa2[size_t(n)] = surface_area(b2);
     for (int i = n - 1; i >= 0; --i) {
-      merge_box(b2, tris[objs[i]].bb, b2);
-      sa2[i] = surface_area(b2);
+      const double b[6] = {r[i].lo[0], r[i].lo[1], r[i].lo[2], r[i].hi[0], r[i].hi[1], r[i].hi[2]};
+      merge_box(b2, b, b2);
+      s.sa2[size_t(i)] = surface_area(b2);
     }
     for (int i = 1; i < n - 1; ++i) {
       const int j = n - i;
-      const double cost = 2 * 1.0 + (i * sa1[i] + j * sa2[i]) * 1.0 / sa_root;
+      const double cost = 2 * 1.0 + (i * s.sa1[size_t(i)] + j * s.sa2[size_t(i)]) * 1.0 / sa_root;
       if (cost < best_cost) {
         best_cost = cost;
         best_axis = axis;
@@ -233,7 +257,7 @@ void build_search_bvh_ids(const float* v, int n_tri, SearchBVH& out);
 }  // namespace
 
 bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, HostScene& out,
-                   std::string& err, bool host_tables) {
+                   std::string& err, bool host_tables, bool ref_bvh) {
   out = HostScene();
   if (n_tri <= 0 || !v || !nrm) {
     err = "empty triangle list";
@@ -378,16 +402,29 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
   }
   }
 
+  if (!ref_bvh) return true;  // the device builds the reference BVH
+
   // SAH BVH with the reference's splits; nodes renumbered depth-first.  Every
   // node's split depends only on its own object list, so the tree does not
   // depend on the order nodes are split in: nodes above a size threshold are
   // split here, the subtrees below it in parallel, then merged.
+  std::vector<BuildRec> R(static_cast<size_t>(nt));
+  for (int t = 0; t < nt; ++t) {
+    const HostTri& tr = out.tris[size_t(t)];
+    BuildRec& b = R[size_t(t)];
+    for (int a = 0; a < 3; ++a) {
+      b.lo[a] = float(tr.bb[a]);  // float vertices: the box values are floats
+      b.hi[a] = float(tr.bb[3 + a]);
+    }
+    b.id = t;
+    b.pad = 0;
+  }
   std::vector<BuildNode> bn;
   bn.reserve(size_t(2) * nt);
   bn.emplace_back();
-  bn[0].objs.resize(nt);
-  std::iota(bn[0].objs.begin(), bn[0].objs.end(), 0);
-  const size_t big = std::max<size_t>(4096, size_t(nt) / 64);
+  bn[0].lo = 0;
+  bn[0].hi = nt;
+  const int big = std::max(4096, nt / 64);
   const unsigned nthreads =
       std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
   // runs f(0..n-1) on up to nthreads threads
@@ -408,63 +445,66 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
     while (!frontier.empty()) {
       std::vector<int> split(frontier.size());
       parallel_for(frontier.size(), [&](size_t k) {
-        std::vector<double> sa1, sa2;
-        BuildNode& b = bn[frontier[k]];
-        split[k] = sah_split(out.tris, b.objs, b.bb, sa1, sa2);
+        SplitScratch sc;
+        BuildNode& b = bn[size_t(frontier[k])];
+        split[k] = sah_split(R, b.lo, b.hi, b.bb, sc);
       });
-      if (frontier[0] == 0) out.mesh_order = bn[0].objs;  // the caller's vector after ConstructBVH
+      if (frontier[0] == 0) {  // the caller's vector after ConstructBVH
+        out.mesh_order.resize(size_t(nt));
+        for (int t = 0; t < nt; ++t) out.mesh_order[size_t(t)] = R[size_t(t)].id;
+      }
       std::vector<int> next;
       for (size_t k = 0; k < frontier.size(); ++k) {
         const int idx = frontier[k];
         if (split[k] < 0) continue;  // a leaf keeps its objects
-        int c0 = int(bn.size());
+        const int c0 = int(bn.size());
         bn.emplace_back();
-        int c1 = int(bn.size());
+        const int c1 = int(bn.size());
         bn.emplace_back();
-        bn[idx].c0 = c0;
-        bn[idx].c1 = c1;
-        std::vector<int>& objs = bn[idx].objs;
-        bn[c0].objs.assign(objs.begin(), objs.begin() + split[k]);
-        bn[c1].objs.assign(objs.begin() + split[k], objs.end());
-        std::vector<int>().swap(objs);
-        for (int c : {c0, c1}) (bn[c].objs.size() >= big ? next : subtrees).push_back(c);
+        BuildNode& b = bn[size_t(idx)];
+        b.c0 = c0;
+        b.c1 = c1;
+        bn[size_t(c0)].lo = b.lo;
+        bn[size_t(c0)].hi = b.lo + split[k];
+        bn[size_t(c1)].lo = b.lo + split[k];
+        bn[size_t(c1)].hi = b.hi;
+        for (int c : {c0, c1})
+          (bn[size_t(c)].hi - bn[size_t(c)].lo >= big ? next : subtrees).push_back(c);
       }
       frontier.swap(next);
     }
   }
   {
-    // each subtree into its own node list (local index 0 = the subtree root)
+    // each subtree into its own node list (local index 0 = the subtree root);
+    // the subtrees own disjoint ranges of R
     std::vector<std::vector<BuildNode>> local(subtrees.size());
     parallel_for(subtrees.size(), [&](size_t k) {
-      std::vector<double> sa1, sa2;
-      {
-        std::vector<BuildNode>& ln = local[k];
+      SplitScratch sc;
+      std::vector<BuildNode>& ln = local[k];
+      ln.emplace_back();
+      ln[0].lo = bn[size_t(subtrees[k])].lo;
+      ln[0].hi = bn[size_t(subtrees[k])].hi;
+      std::vector<int> work{0};
+      while (!work.empty()) {
+        const int idx = work.back();
+        work.pop_back();
+        const int lo = ln[size_t(idx)].lo, hi = ln[size_t(idx)].hi;
+        double bb[6];
+        const int split = sah_split(R, lo, hi, bb, sc);
+        std::memcpy(ln[size_t(idx)].bb, bb, sizeof bb);
+        if (split < 0) continue;
+        const int c0 = int(ln.size());
         ln.emplace_back();
-        ln[0].objs.swap(bn[subtrees[k]].objs);
-        std::vector<int> work{0};
-        while (!work.empty()) {
-          int idx = work.back();
-          work.pop_back();
-          std::vector<int> objs;
-          objs.swap(ln[idx].objs);
-          double bb[6];
-          int split = sah_split(out.tris, objs, bb, sa1, sa2);
-          std::memcpy(ln[idx].bb, bb, sizeof bb);
-          if (split < 0) {
-            ln[idx].objs.swap(objs);
-            continue;
-          }
-          int c0 = int(ln.size());
-          ln.emplace_back();
-          int c1 = int(ln.size());
-          ln.emplace_back();
-          ln[idx].c0 = c0;
-          ln[idx].c1 = c1;
-          ln[c0].objs.assign(objs.begin(), objs.begin() + split);
-          ln[c1].objs.assign(objs.begin() + split, objs.end());
-          work.push_back(c1);
-          work.push_back(c0);
-        }
+        const int c1 = int(ln.size());
+        ln.emplace_back();
+        ln[size_t(idx)].c0 = c0;
+        ln[size_t(idx)].c1 = c1;
+        ln[size_t(c0)].lo = lo;
+        ln[size_t(c0)].hi = lo + split;
+        ln[size_t(c1)].lo = lo + split;
+        ln[size_t(c1)].hi = hi;
+        work.push_back(c1);
+        work.push_back(c0);
       }
     });
     for (size_t k = 0; k < subtrees.size(); ++k) {
@@ -474,13 +514,12 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
       for (size_t j = 1; j < ln.size(); ++j) {
         ln[j].c0 = map(ln[j].c0);
         ln[j].c1 = map(ln[j].c1);
-        bn.push_back(std::move(ln[j]));
+        bn.push_back(ln[j]);
       }
-      BuildNode& r = bn[subtrees[k]];
+      BuildNode& r = bn[size_t(subtrees[k])];
       std::memcpy(r.bb, ln[0].bb, sizeof r.bb);
       r.c0 = map(ln[0].c0);
       r.c1 = map(ln[0].c1);
-      r.objs.swap(ln[0].objs);
     }
   }
   // Depth-first renumbering, children[0] first.
@@ -506,8 +545,8 @@ bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, 
     }
     if (bn[it.b].c0 < 0) {
       hn.first = int(out.dfs_tris.size());
-      hn.count = int(bn[it.b].objs.size());
-      out.dfs_tris.insert(out.dfs_tris.end(), bn[it.b].objs.begin(), bn[it.b].objs.end());
+      hn.count = bn[it.b].hi - bn[it.b].lo;
+      for (int q = bn[it.b].lo; q < bn[it.b].hi; ++q) out.dfs_tris.push_back(R[size_t(q)].id);
     } else {
       st.push_back({bn[it.b].c1, me, it.depth + 1, me, 1});
       st.push_back({bn[it.b].c0, me, it.depth + 1, me, 0});

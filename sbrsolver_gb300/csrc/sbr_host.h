@@ -71,7 +71,7 @@ bool read_stl(const std::string& path, std::vector<float>& v, std::vector<float>
 // BVH to the caller (the device builds them), and skips the vertex merge
 // they need.
 bool prepare_scene(int n_tri, const float* v, const float* nrm, const int* mat, HostScene& out,
-                   std::string& err, bool host_tables = true);
+                   std::string& err, bool host_tables = true, bool ref_bvh = true);
 
 // The search BVH's triangle ids -> depth-first ranks of the reference BVH.
 void map_search_order(HostScene& H);

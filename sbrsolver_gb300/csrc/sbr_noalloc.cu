@@ -15,7 +15,9 @@
 // not pass the symbol itself to a kernel; its device address is looked up once
 // per device with cudaGetSymbolAddress, on the first call made while that
 // device is current.  That first call therefore performs the set-up and
-// should come before any stream capture.  Every call shares the array and
+// must come before any stream capture; later calls may be captured into a
+// CUDA graph (they then only enqueue kernels and report no device-side
+// input errors).  Every call shares the array and
 // leaves the previous call's contents behind, so the counters are cleared at
 // the start of each call; calls that overlap on the GPU (for example on two
 // streams at once) race on the array and must be serialised by the caller.
@@ -295,7 +297,21 @@ sbr_status sbr_receiver_field_sum_noalloc(const int* path_receiver, const long l
   sbr_status st = scratch_for_current_device(&s, &sms, &dev, g_err);
   if (st != SBR_OK) return st;
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
-  if (cs) {  // the scratch address looked up is the current device's
+  // While the stream is being captured into a CUDA graph the call only
+  // enqueues its kernels: a capture admits neither the pageable read-back
+  // nor the synchronisation (nor, in the global capture mode, queries beyond
+  // the capture status).  The kernels still skip out-of-range receivers and
+  // over-long receivers (those fields stay zero); their flags are not
+  // reported then.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  {
+    const cudaError_t e = cudaStreamIsCapturing(cs, &cap);
+    if (e != cudaSuccess) {
+      g_err = std::string("sbr_receiver_field_sum_noalloc: ") + cudaGetErrorString(e);
+      return SBR_ERR_CUDA;
+    }
+  }
+  if (cs && cap == cudaStreamCaptureStatusNone) {  // the scratch address is the current device's
     int sdev = -1;
     cudaError_t e = cudaStreamGetDevice(cs, &sdev);
     if (e != cudaSuccess || sdev != dev) {
@@ -303,7 +319,8 @@ sbr_status sbr_receiver_field_sum_noalloc(const int* path_receiver, const long l
       return SBR_ERR_INVALID_ARG;
     }
   }
-  cudaGetLastError();  // an earlier, unrelated launch error is not this call's
+  if (cap == cudaStreamCaptureStatusNone)
+    cudaGetLastError();  // an earlier, unrelated launch error is not this call's
   const int gb = sms * 4;
   k_clear<<<gb, 256, 0, cs>>>(s, n_rx);
   if (n_paths) k_hist<<<gb, 256, 0, cs>>>(path_receiver, n_paths, n_rx, s);
@@ -313,6 +330,7 @@ sbr_status sbr_receiver_field_sum_noalloc(const int* path_receiver, const long l
   k_sum_large<<<sms * 2, kLargeThreads, 0, cs>>>(path_rank, path_field, field_precision, s,
                                                  field_out);
   cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && cap != cudaStreamCaptureStatusNone) return SBR_OK;
   int bad = 0;
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&bad, s + kError, sizeof(int), cudaMemcpyDeviceToHost, cs);

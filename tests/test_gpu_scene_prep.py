@@ -1,10 +1,11 @@
 """Scene preparation on the GPU (sbr_prep.cuh) against the host build.
 
 By default a scene's coplanar groups (Preprocessor.cpp:116-246), triangle
-frames and boxes (Triangle.cpp:37-70) and search BVH are built on the GPU
-while the host builds the reference BVH; SBR_SCENE_HOST_PREP builds them all
-on the host.  The two must give identical tables, bit for bit, and the
-same solve."""
+frames and boxes (Triangle.cpp:37-70), search BVH and reference BVH
+(BVH/BVH.h:135-230, with std::sort's order of equal keys restated on the
+device) are built on the GPU; SBR_SCENE_HOST_PREP builds them all on the
+host.  The two must give identical tables, bit for bit, and the same
+solve."""
 import time
 
 import numpy as np
@@ -33,12 +34,21 @@ def test_device_tables_equal_host_tables(built, name):
     t1 = time.perf_counter()
     dev = api.DeviceScene.from_scene(wl.scene)
     t2 = time.perf_counter()
+    inf = dev.info()
     print(f"{name}: {wl.scene.n_tri} triangles, host preparation {1e3 * (t1 - t0):.0f} ms, "
-          f"device {1e3 * (t2 - t1):.0f} ms")
+          f"device {1e3 * (t2 - t1):.0f} ms (in the library {inf.prep_total_ms:.1f}: host "
+          f"records {inf.prep_host_ms:.1f}, merge/coplanar/frames {inf.prep_device_tables_ms:.1f}, "
+          f"search BVH {inf.prep_search_bvh_ms:.1f}, reference BVH "
+          f"{inf.prep_reference_bvh_ms:.1f}, upload {inf.prep_upload_ms:.1f})")
     np.testing.assert_array_equal(dev.coplanar_ids(), host.coplanar_ids())
     np.testing.assert_array_equal(dev.mesh_order(), host.mesh_order())
     for a, b in zip(dev.triangle_frames(), host.triangle_frames()):
         np.testing.assert_array_equal(a.view(np.int64), b.view(np.int64))  # bit for bit
+    ra_, rb_ = dev.reference_bvh(), host.reference_bvh()
+    assert ra_["max_depth"] == rb_["max_depth"] and len(ra_["links"]) == len(rb_["links"])
+    np.testing.assert_array_equal(ra_["links"], rb_["links"])
+    np.testing.assert_array_equal(ra_["order"], rb_["order"])
+    np.testing.assert_array_equal(ra_["boxes"].view(np.int64), rb_["boxes"].view(np.int64))
     sa, sb = dev.search_bvh(), host.search_bvh()
     assert sa["max_depth"] == sb["max_depth"]
     np.testing.assert_array_equal(sa["order"], sb["order"])
@@ -63,9 +73,28 @@ def test_device_prep_edge_cases(built):
         a = api.DeviceScene(mesh, mats)
         b = api.DeviceScene(mesh, mats, host_prep=True)
         np.testing.assert_array_equal(a.search_bvh()["nodes"], b.search_bvh()["nodes"])
+        for k in ("links", "order", "boxes"):
+            np.testing.assert_array_equal(a.reference_bvh()[k], b.reference_bvh()[k])
+        np.testing.assert_array_equal(a.mesh_order(), b.mesh_order())
         np.testing.assert_array_equal(a.coplanar_ids(), b.coplanar_ids())
         a.close()
         b.close()
+    # 5,000 copies of one triangle stacked along z: every x and y key equal,
+    # so the device sort's partition rounds and warp sorts see nothing but
+    # ties, as std::sort does on the host
+    base = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]], np.float32)
+    k = np.arange(5000, dtype=np.float32)[:, None, None]
+    stack_tri = base[None] + np.concatenate([0 * k, 0 * k, 0.01 * k], axis=2)
+    stack_nrm = np.tile(np.array([[0.0, 0.0, 1.0]], np.float32), (5000, 1))
+    mesh = api.Mesh(stack_tri.astype(np.float32), stack_nrm, np.zeros(5000, np.int32))
+    mats = [api.MaterialProperties(*m) for m in wl.scene.materials]
+    a = api.DeviceScene(mesh, mats)
+    b = api.DeviceScene(mesh, mats, host_prep=True)
+    for key in ("links", "order", "boxes"):
+        np.testing.assert_array_equal(a.reference_bvh()[key], b.reference_bvh()[key])
+    np.testing.assert_array_equal(a.mesh_order(), b.mesh_order())
+    a.close()
+    b.close()
     tri = wl.scene.tri.copy()
     tri[3, 2] = tri[3, 1]  # two vertices of triangle 3 coincide
     mesh = api.Mesh(tri, wl.scene.normal, wl.scene.material_id)

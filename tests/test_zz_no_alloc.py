@@ -142,3 +142,37 @@ def test_noalloc_rejects_bad_input(built):
     got = out.cpu().numpy().reshape(2, 6)
     np.testing.assert_array_equal(got[0], np.arange(6, 12))
     np.testing.assert_array_equal(got[1], np.arange(12, 18) + np.arange(0, 6))
+
+
+def test_noalloc_inside_cuda_graph(built):
+    """Captured into a CUDA graph (torch.cuda.graph), the call only enqueues
+    its kernels; replays sum whatever the path buffers hold at replay time."""
+    torch = pytest.importorskip("torch")
+    lib = _lib.load()
+    rng = np.random.default_rng(11)
+    n_rx, n = 48, 400
+    recv = rng.integers(0, n_rx, n).astype(np.int32)
+    recv[:60] = 3  # one receiver with a block-wide sort
+    rank = rng.integers(0, 1 << 30, n).astype(np.int64)
+    pf = rng.normal(size=(n, 6))
+    t = lambda a, dt: torch.tensor(a, dtype=dt, device="cuda")  # noqa: E731
+    d_recv, d_rank, d_pf = t(recv, torch.int32), t(rank, torch.int64), t(pf.reshape(-1),
+                                                                        torch.float64)
+    st, _ = _call(lib, torch, d_recv, d_rank, d_pf, n, n_rx, 0)  # set-up outside the capture
+    _lib.check(st)
+    out = torch.zeros(n_rx * 6, dtype=torch.float64, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g):
+        st = lib.sbr_receiver_field_sum_noalloc(
+            C.c_void_p(d_recv.data_ptr()), C.c_void_p(d_rank.data_ptr()),
+            C.c_void_p(d_pf.data_ptr()), n, n_rx, 0, C.c_void_p(out.data_ptr()),
+            C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(st)
+    for scale in (1.0, -0.5):
+        d_pf.copy_(t(scale * pf.reshape(-1), torch.float64))
+        out.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy().reshape(n_rx, 6),
+                                      _ordered_sum(recv, rank, scale * pf, n_rx, 0))
