@@ -774,6 +774,7 @@ struct RefSort {
   DBuf<refbvh::SortSeg> big, big_next, small, tiny, heap;
   DBuf<int> ctl;
   int sms = 1;
+  int small_cap = 0;  // entries of the small-segment list (both ends)
 };
 
 static int read_ctl(RefSort& R, int* h, cudaStream_t st) {
@@ -794,7 +795,7 @@ static void ref_sort(RefSort& R, const refbvh::RNode* nodes, const int* active, 
   int h[kCtlWords];
   CK(cudaMemsetAsync(R.ctl.p, 0, sizeof(int) * kNodes, st));  // list counters only
   k_file_nodes<<<grid_all(m, 128), 128, 0, st>>>(nodes, active, m, best, R.big.p, R.small.p,
-                                                 R.tiny.p, R.heap.p, R.ctl.p);
+                                                 R.small_cap, R.tiny.p, R.heap.p, R.ctl.p);
   CK(cudaGetLastError());
   read_ctl(R, h, st);
   int n_big = h[kBig], n_tiles = h[kTiles];
@@ -813,8 +814,8 @@ static void ref_sort(RefSort& R, const refbvh::RNode* nodes, const int* active, 
     CK(cudaMemsetAsync(R.ctl.p + kBigNext, 0, sizeof(int), st));
     CK(cudaMemsetAsync(R.ctl.p + kTilesNext, 0, sizeof(int), st));
     k_cut<<<grid_all(n_big, 128), 128, 0, st>>>(R.big.p, n_big, R.totals.p, R.lpos.p, R.rpos.p,
-                                                R.big_next.p, R.small.p, R.tiny.p, R.heap.p,
-                                                R.ctl.p);
+                                                R.big_next.p, R.small.p, R.small_cap, R.tiny.p,
+                                                R.heap.p, R.ctl.p);
     CK(cudaGetLastError());
     read_ctl(R, h, st);
     n_big = h[kBigNext];
@@ -825,8 +826,13 @@ static void ref_sort(RefSort& R, const refbvh::RNode* nodes, const int* active, 
     std::swap(R.big.n, R.big_next.n);
   }
   if (h[kSmall])
-    k_small<<<std::min(h[kSmall], R.sms * 8), 32, kSmallSmem, st>>>(R.small.p, R.ctl.p + kSmall,
-                                                                    R.key.p, R.idx.p, R.ctl.p);
+    k_small<kSmallMax><<<std::min(h[kSmall], R.sms * 8), 32, small_smem<kSmallMax>(), st>>>(
+        R.small.p, R.ctl.p + kSmall, 0, R.key.p, R.idx.p, R.ctl.p);
+  if (h[kShort])
+    k_small<kShortMax><<<std::min(h[kShort], R.sms * 32), 32, small_smem<kShortMax>(), st>>>(
+        R.small.p, R.ctl.p + kShort, R.small_cap, R.key.p, R.idx.p, R.ctl.p);
+  if (h[kSmall] + h[kShort] > R.small_cap)
+    throw std::string("device reference BVH: small segment list overflow");
   if (h[kTiny])
     k_tiny<<<grid_all(h[kTiny], 128), 128, 0, st>>>(R.tiny.p, R.ctl.p + kTiny, R.key.p, R.idx.p);
   if (h[kHeap])
@@ -860,6 +866,8 @@ static void device_ref_bvh(const float* v, int nt, cudaStream_t st, DeviceTables
   R.big.ensure(nz / kSmallMax + 16);
   R.big_next.ensure(nz / kSmallMax + 16);
   R.small.ensure(lists);
+  R.small_cap = int(lists);
+
   R.tiny.ensure(lists);
   R.heap.ensure(lists);
   R.ctl.ensure(kCtlWords);
@@ -883,6 +891,9 @@ static void device_ref_bvh(const float* v, int nt, cudaStream_t st, DeviceTables
   tbest.ensure(tcap);
   DBuf<double> sa_root;
   sa_root.ensure(nz);
+  DBuf<int> tiled, small_nodes;  // a level's nodes with tiles / of kNodeSmall or fewer objects
+  tiled.ensure(nz);
+  small_nodes.ensure(nz);
   DBuf<int> node_of, active, next, ids, mesh;
   node_of.ensure(nz);
   active.ensure(nz);
@@ -903,17 +914,23 @@ static void device_ref_bvh(const float* v, int nt, cudaStream_t st, DeviceTables
   for (int level = 0; m > 0; ++level) {
     if (level > 4096) throw std::string("device reference BVH: too many levels");
     CK(cudaMemsetAsync(node_of.p, 0xff, sizeof(int) * nz, st));
-    CK(cudaMemsetAsync(R.ctl.p + kSweepTiles, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(R.ctl.p + kSweepTiles, 0, 3 * sizeof(int), st));  // tiles, both lists
     k_level_tiles<<<grid_all(m, 128), 128, 0, st>>>(nodes.p, active.p, m, node_tiles.p,
-                                                    tile_node.p, R.ctl.p);
+                                                    tile_node.p, tiled.p, small_nodes.p, R.ctl.p);
     int hl[kCtlWords];
     read_ctl(R, hl, st);
-    const int n_tiles = hl[kSweepTiles];
-    const long long tile_threads = 32LL * n_tiles, node_threads = 32LL * m;
-    k_tile_exact_box<<<grid_all(tile_threads, 256), 256, 0, st>>>(
-        nodes.p, active.p, node_tiles.p, tile_node.p, n_tiles, lo.p, hi.p, node_of.p, tbox.p);
-    k_node_box<<<grid_all(node_threads, 256), 256, 0, st>>>(nodes.p, active.p, m, node_tiles.p,
-                                                            tbox.p, sa_root.p, best.p);
+    const int n_tiles = hl[kSweepTiles], n_tiled = hl[kTiledNodes], n_small = hl[kSmallNodes];
+    const long long tile_threads = 32LL * n_tiles, node_threads = 32LL * n_tiled;
+    if (n_tiles) {
+      k_tile_exact_box<<<grid_all(tile_threads, 256), 256, 0, st>>>(
+          nodes.p, active.p, node_tiles.p, tile_node.p, n_tiles, lo.p, hi.p, node_of.p, tbox.p);
+      k_node_box<<<grid_all(node_threads, 256), 256, 0, st>>>(
+          nodes.p, active.p, tiled.p, n_tiled, node_tiles.p, tbox.p, sa_root.p, best.p);
+    }
+    if (n_small)
+      k_small_node_box<<<grid_all(n_small, 128), 128, 0, st>>>(nodes.p, active.p, small_nodes.p,
+                                                               n_small, lo.p, hi.p, node_of.p,
+                                                               sa_root.p, best.p);
     for (int axis = 0; axis <= 3; ++axis) {  // x, y, z, then the chosen axis
       const NodeBest* b = axis == 3 ? best.p : nullptr;
       k_keys<<<grid_all(n, 256), 256, 0, st>>>(lo.p, hi.p, node_of.p, b, axis, n, R.key.p,
@@ -922,17 +939,21 @@ static void device_ref_bvh(const float* v, int nt, cudaStream_t st, DeviceTables
       k_gather<<<grid_all(n, 256), 256, 0, st>>>(lo.p, hi.p, R.idx.p, n, lo2.p, hi2.p);
       std::swap(lo.p, lo2.p);
       std::swap(hi.p, hi2.p);
-      if (axis < 3) {  // the surface area sweep over this order
+      if (axis < 3 && n_tiles) {  // the surface area sweep over this order
         k_tile_boxes<<<grid_all(tile_threads, 256), 256, 0, st>>>(
             nodes.p, active.p, node_tiles.p, tile_node.p, n_tiles, lo.p, hi.p, tagg.p);
-        k_tile_carries<<<grid_all(node_threads, 256), 256, 0, st>>>(node_tiles.p, m, tagg.p,
-                                                                    pre.p, post.p);
+        k_tile_carries<<<grid_all(node_threads, 256), 256, 0, st>>>(tiled.p, n_tiled,
+                                                                    node_tiles.p, tagg.p, pre.p,
+                                                                    post.p);
         k_tile_sweep<<<grid_all(tile_threads, 256), 256, 0, st>>>(
             nodes.p, active.p, node_tiles.p, tile_node.p, n_tiles, lo.p, hi.p, pre.p, post.p,
             sa_root.p, tbest.p);
-        k_node_best<<<grid_all(node_threads, 256), 256, 0, st>>>(node_tiles.p, m, tbest.p,
-                                                                 axis, best.p);
+        k_node_best<<<grid_all(node_threads, 256), 256, 0, st>>>(tiled.p, n_tiled, node_tiles.p,
+                                                                 tbest.p, axis, best.p);
       }
+      if (axis < 3 && n_small)
+        k_small_node_sweep<<<grid_all(n_small, 128), 128, 0, st>>>(
+            nodes.p, active.p, small_nodes.p, n_small, lo.p, hi.p, sa_root.p, axis, best.p);
     }
     if (level == 0) k_ids<<<grid_all(n, 256), 256, 0, st>>>(lo.p, n, mesh.p);
     CK(cudaMemsetAsync(R.ctl.p + kActiveNext, 0, sizeof(int), st));

@@ -41,6 +41,7 @@ namespace refbvh {
 constexpr int kTile = 2048;        // elements per block of the partition rounds
 constexpr int kTileThreads = 256;  // 8 consecutive elements per thread
 constexpr int kSmallMax = 2048;    // longest segment one warp sorts in shared memory
+constexpr int kShortMax = 256;     // segments up to this long use the lighter warp sort
 constexpr int kInsertion = 16;     // segments this short wait for insertion sort
 
 struct __align__(16) SortSeg {
@@ -63,11 +64,12 @@ struct __align__(16) NodeBest {
 
 // Control words: sort list counts and the next level's sizes.
 enum Ctl {
-  kBig = 0, kBigNext, kSmall, kTiny, kHeap, kTiles, kTilesNext, kNodes, kActiveNext,
-  kSweepTiles, kError, kCtlWords
+  kBig = 0, kBigNext, kSmall, kShort, kTiny, kHeap, kTiles, kTilesNext, kNodes, kActiveNext,
+  kSweepTiles, kTiledNodes, kSmallNodes, kError, kCtlWords
 };
 
 __device__ __forceinline__ int floor_log2(int n) { return 31 - __clz(n); }
+
 
 // Box centre along axis a exactly as the reference computes it from the
 // box of float vertices: (min + max) / 2 in FP64.
@@ -214,15 +216,19 @@ __device__ void heap_sort(K* key, I* idx, long n) {
 // Files a segment of the sort: nothing to do (<= 1), insertion list (<= 16),
 // heap list (no depth budget left), a warp's list (<= kSmallMax), else the
 // partition rounds (with its tiles reserved).
+// small: capacity small_cap; segments of at most kShortMax are filed from
+// its end, longer ones from its start.
 __device__ __forceinline__ void file_segment(int f, int l, int d, SortSeg* big, SortSeg* small,
-                                             SortSeg* tiny, SortSeg* heap, int* ctl, int big_slot,
-                                             int tiles_slot) {
+                                             int small_cap, SortSeg* tiny, SortSeg* heap, int* ctl,
+                                             int big_slot, int tiles_slot) {
   const int n = l - f;
   if (n <= 1) return;
   if (n <= kInsertion) {
     tiny[atomicAdd(ctl + kTiny, 1)] = SortSeg{f, l, d, 0};
   } else if (d == 0) {
     heap[atomicAdd(ctl + kHeap, 1)] = SortSeg{f, l, d, 0};
+  } else if (n <= kShortMax) {  // the short ones fill the small list from its end
+    small[small_cap - 1 - atomicAdd(ctl + kShort, 1)] = SortSeg{f, l, d, 0};
   } else if (n <= kSmallMax) {
     small[atomicAdd(ctl + kSmall, 1)] = SortSeg{f, l, d, 0};
   } else {
@@ -235,15 +241,16 @@ __device__ __forceinline__ void file_segment(int f, int l, int d, SortSeg* big, 
 // Initial segments: the objects of each listed node (a split node only,
 // for the final sort along its best axis).
 __global__ void k_file_nodes(const RNode* nodes, const int* active, int m, const NodeBest* best,
-                             SortSeg* big, SortSeg* small, SortSeg* tiny, SortSeg* heap,
-                             int* ctl) {
+                             SortSeg* big, SortSeg* small, int small_cap, SortSeg* tiny,
+                             SortSeg* heap, int* ctl) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= m) return;
   if (best && best[a].axis < 0) return;
   const RNode& nd = nodes[active[a]];
   const int n = nd.l - nd.f;
   if (n < 2) return;
-  file_segment(nd.f, nd.l, 2 * floor_log2(n), big, small, tiny, heap, ctl, kBig, kTiles);
+  file_segment(nd.f, nd.l, 2 * floor_log2(n), big, small, small_cap, tiny, heap, ctl, kBig,
+               kTiles);
 }
 
 // Tile -> segment map of the partition rounds.
@@ -392,8 +399,8 @@ __global__ void __launch_bounds__(kTileThreads) k_exchange(const SortSeg* big,
 
 // Round step 6: the cut of every big segment and its two parts filed.
 __global__ void k_cut(const SortSeg* big, int n_big, const int2* totals, const int* lpos,
-                      const int* rpos, SortSeg* big_next, SortSeg* small, SortSeg* tiny,
-                      SortSeg* heap, int* ctl) {
+                      const int* rpos, SortSeg* big_next, SortSeg* small, int small_cap,
+                      SortSeg* tiny, SortSeg* heap, int* ctl) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_big) return;
   const SortSeg g = big[s];
@@ -411,29 +418,37 @@ __global__ void k_cut(const SortSeg* big, int n_big, const int2* totals, const i
     atomicOr(ctl + kError, 1);
     return;
   }
-  file_segment(g.f, cut, g.d - 1, big_next, small, tiny, heap, ctl, kBigNext, kTilesNext);
-  file_segment(cut, g.l, g.d - 1, big_next, small, tiny, heap, ctl, kBigNext, kTilesNext);
+  file_segment(g.f, cut, g.d - 1, big_next, small, small_cap, tiny, heap, ctl, kBigNext,
+               kTilesNext);
+  file_segment(cut, g.l, g.d - 1, big_next, small, small_cap, tiny, heap, ctl, kBigNext,
+               kTilesNext);
 }
 
 // A warp per segment of at most kSmallMax: the segment is sorted in shared
 // memory (partition by the warp, exchanges spread over its lanes), then the
 // leftover segments of at most 16 are insertion sorted, one per lane.
-constexpr size_t kSmallSmem = size_t(kSmallMax) * (8 + 4 + 2 + 2 + 4);
+template <int kCap>
+constexpr size_t small_smem() {
+  return size_t(kCap) * (8 + 4 + 2 + 2 + 4);
+}
 
+// segs: the list; n_segs: its count; from_end > 0: the list is read from
+// its end (entry from_end - 1 - s, from_end being the list's capacity).
+template <int kCap>
 __global__ void __launch_bounds__(32) k_small(const SortSeg* segs, const int* n_segs,
-                                              double* key, int* idx, int* ctl) {
+                                              int from_end, double* key, int* idx, int* ctl) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* sk = reinterpret_cast<double*>(smem);
-  int* si = reinterpret_cast<int*>(sk + kSmallMax);
-  short* lp = reinterpret_cast<short*>(si + kSmallMax);
-  short* rp = lp + kSmallMax;
-  int* tiny = reinterpret_cast<int*>(rp + kSmallMax);
+  int* si = reinterpret_cast<int*>(sk + kCap);
+  short* lp = reinterpret_cast<short*>(si + kCap);
+  short* rp = lp + kCap;
+  int* tiny = reinterpret_cast<int*>(rp + kCap);
   __shared__ int3 stack[64];
   const int lane = threadIdx.x;
   const unsigned below = (1u << lane) - 1u;
   const int n = *n_segs;
   for (int s = blockIdx.x; s < n; s += gridDim.x) {
-    const SortSeg g = segs[s];
+    const SortSeg g = segs[from_end > 0 ? from_end - 1 - s : s];
     const int len = g.l - g.f;
     for (int i = lane; i < len; i += 32) {
       sk[i] = key[g.f + i];
@@ -644,17 +659,86 @@ struct __align__(16) TileBest {
   int i, pad;
 };
 
-// Tiles of every active node: per node its first tile and tile count, per
-// tile its node.
+constexpr int kNodeSmall = 16;  // nodes this small are handled by one thread each
+
+// Tiles of every active node of more than kNodeSmall objects (per node its
+// first tile and tile count, per tile its node), and the lists of those
+// nodes and of the small ones.
 __global__ void k_level_tiles(const RNode* nodes, const int* active, int m, int2* node_tiles,
-                              int* tile_node, int* ctl) {
+                              int* tile_node, int* tiled, int* small_nodes, int* ctl) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= m) return;
   const RNode& nd = nodes[active[a]];
-  const int nt = max(1, (nd.l - nd.f + kWarpTile - 1) / kWarpTile);
+  const int n = nd.l - nd.f;
+  if (n <= kNodeSmall) {
+    small_nodes[atomicAdd(ctl + kSmallNodes, 1)] = a;
+    node_tiles[a] = make_int2(0, 0);
+    return;
+  }
+  const int nt = (n + kWarpTile - 1) / kWarpTile;
   const int t0 = atomicAdd(ctl + kSweepTiles, nt);
   node_tiles[a] = make_int2(t0, nt);
+  tiled[atomicAdd(ctl + kTiledNodes, 1)] = a;
   for (int t = 0; t < nt; ++t) tile_node[t0 + t] = a;
+}
+
+// A small node's set-up, one thread each: its positions marked, its box
+// formed object by object as the host forms it (box = std::min(object, box),
+// std::max(object, box)), the surface area and the leaf cost as the best.
+__global__ void k_small_node_box(RNode* nodes, const int* active, const int* small_nodes, int k,
+                                 const float4* lo, const float4* hi, int* node_of,
+                                 double* sa_root, NodeBest* best) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  const int a = small_nodes[j];
+  RNode& nd = nodes[active[a]];
+  float b[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int p = nd.f; p < nd.l; ++p) {
+    node_of[p] = a;
+    const float4 L = lo[p], H = hi[p];
+    const float x[6] = {L.x, L.y, L.z, H.x, H.y, H.z};
+    for (int c = 0; c < 3; ++c) {
+      if (!(b[c] < x[c])) b[c] = x[c];
+      if (!(x[3 + c] < b[3 + c])) b[3 + c] = x[3 + c];
+    }
+  }
+  for (int c = 0; c < 6; ++c) nd.bb[c] = double(b[c]);
+  sa_root[a] = surface_area(b[0], b[1], b[2], b[3], b[4], b[5]);
+  best[a] = NodeBest{double(nd.l - nd.f), -1, -1};
+}
+
+// A small node's sweep over one axis order, one thread each, in the
+// reference loop's order: prefix areas, then suffix areas with the costs,
+// a cost kept when it is below the best so far.
+__global__ void k_small_node_sweep(const RNode* nodes, const int* active, const int* small_nodes,
+                                   int k, const float4* lo, const float4* hi,
+                                   const double* sa_root, int axis, NodeBest* best) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  const int a = small_nodes[j];
+  const RNode& nd = nodes[active[a]];
+  const int n = nd.l - nd.f;
+  if (n < 3) return;
+  double sa1[kNodeSmall];
+  BoxF run = box_empty();
+  for (int i = 0; i < n; ++i) {
+    run = box_merge(run, rec_box(lo[nd.f + i], hi[nd.f + i]));
+    sa1[i] = surface_area(run.l[0], run.l[1], run.l[2], run.h[0], run.h[1], run.h[2]);
+  }
+  double sa2[kNodeSmall];
+  run = box_empty();
+  for (int i = n - 1; i >= 0; --i) {
+    run = box_merge(run, rec_box(lo[nd.f + i], hi[nd.f + i]));
+    sa2[i] = surface_area(run.l[0], run.l[1], run.l[2], run.h[0], run.h[1], run.h[2]);
+  }
+  NodeBest b = best[a];
+  const double sr = sa_root[a];
+  for (int i = 1; i < n - 1; ++i) {
+    const double num = __dadd_rn(__dmul_rn(double(i), sa1[i]), __dmul_rn(double(n - i), sa2[i]));
+    const double cost = __dadd_rn(2.0, __ddiv_rn(__dmul_rn(num, 1.0), sr));
+    if (cost < b.cost) b = NodeBest{cost, axis, i};
+  }
+  best[a] = b;
 }
 
 // Level set-up per tile: positions marked with their node, and the tile's
@@ -686,10 +770,12 @@ __global__ void k_tile_exact_box(const RNode* nodes, const int* active, const in
 
 // Node box from its tiles, its surface area, and the leaf cost as the best
 // so far; a warp per node.
-__global__ void k_node_box(RNode* nodes, const int* active, int m, const int2* node_tiles,
-                           const ExactBox* tbox, double* sa_root, NodeBest* best) {
-  const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (a >= m) return;
+__global__ void k_node_box(RNode* nodes, const int* active, const int* tiled, int k,
+                           const int2* node_tiles, const ExactBox* tbox, double* sa_root,
+                           NodeBest* best) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= k) return;
+  const int a = tiled[w];
   const int2 nt = node_tiles[a];
   ExactBox e;
   for (int c = 0; c < 6; ++c) {
@@ -726,10 +812,11 @@ __global__ void k_tile_boxes(const RNode* nodes, const int* active, const int2* 
 
 // Per node, the box of the objects before each of its tiles (pre) and
 // after it (post); a warp per node, 32 tiles at a time.
-__global__ void k_tile_carries(const int2* node_tiles, int m, const BoxF* tagg, BoxF* pre,
-                               BoxF* post) {
-  const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (a >= m) return;
+__global__ void k_tile_carries(const int* tiled, int k, const int2* node_tiles, const BoxF* tagg,
+                               BoxF* pre, BoxF* post) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= k) return;
+  const int a = tiled[w];
   const int2 nt = node_tiles[a];
   BoxF run = box_empty();
   for (int c = 0; c < nt.y; c += 32) {
@@ -839,10 +926,11 @@ __global__ void k_tile_sweep(const RNode* nodes, const int* active, const int2* 
 // The node's cheapest split of this axis, kept if it beats the best so far
 // (earlier axes win ties, as the strict < of the reference's loop decides);
 // a warp per node.
-__global__ void k_node_best(const int2* node_tiles, int m, const TileBest* tbest, int axis,
-                            NodeBest* best) {
-  const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (a >= m) return;
+__global__ void k_node_best(const int* tiled, int k, const int2* node_tiles, const TileBest* tbest,
+                            int axis, NodeBest* best) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= k) return;
+  const int a = tiled[w];
   const int2 nt = node_tiles[a];
   double bc = INFINITY;
   int bi = INT_MAX;
