@@ -13,8 +13,8 @@
 //     most 7 triangles), node for node and in the same depth-first numbering
 //     as the host build.
 //
-// The reference BVH stays on the host: its shape depends on std::sort's
-// handling of equal centroids, which only the host's std::sort reproduces.
+// The reference BVH, whose shape depends on the order std::sort leaves
+// equal centroids in, is built by sbr_refbvh.cuh.
 #pragma once
 
 #include <cuda_runtime.h>
