@@ -400,6 +400,35 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_scene_prep(api, scenes, reps: int = 3) -> dict:
+    """Scene preparation of the large terrain: the library's own phase times
+    (sbr_scene_info.prep_*) for the device build, best of `reps` after one
+    untimed creation (CUDA context and module start-up), and the host build
+    (SBR_SCENE_HOST_PREP) once."""
+    wl = scenes.large_scene(level=5)
+    api.DeviceScene.from_scene(wl.scene).close()
+    fields = ("prep_total_ms", "prep_host_ms", "prep_device_tables_ms", "prep_search_bvh_ms",
+              "prep_reference_bvh_ms", "prep_upload_ms")
+    runs = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        sc = api.DeviceScene.from_scene(wl.scene)
+        wall = 1e3 * (time.perf_counter() - t)
+        inf = sc.info()
+        runs.append(dict({f: getattr(inf, f) for f in fields}, wall_ms=wall))
+        sc.close()
+    t = time.perf_counter()
+    sc = api.DeviceScene.from_scene(wl.scene, host_prep=True)
+    host_ms = 1e3 * (time.perf_counter() - t)
+    inf = sc.info()
+    sc.close()
+    best = min(runs, key=lambda r: r["wall_ms"])
+    return {"metric": "scene preparation", "workload": "large terrain", "triangles": wl.scene.n_tri,
+            "bvh_nodes": inf.n_bvh_nodes, "bvh_depth": inf.bvh_depth, "unit": "ms",
+            "device_build": best, "device_runs_wall_ms": [r["wall_ms"] for r in runs],
+            "host_build_wall_ms": host_ms}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -416,6 +445,9 @@ def main():
     ap.add_argument("--tuning", default="",
                     help="launch shapes of the benchmark scene, e.g. trace_kernel=2,find_steps=16 "
                          "(sbr_tuning field names; default: the library's)")
+    ap.add_argument("--scene-prep", action="store_true",
+                    help="only time the scene preparation of the large terrain (580,484 "
+                         "triangles), device-built and host-built, and print that JSON line")
     args = ap.parse_args()
     rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
     dist = None
@@ -436,6 +468,10 @@ def main():
     from sbrsolver_gb300 import api, scenes
     from sbrsolver_gb300.build import build_library
     build_library()
+    if args.scene_prep:
+        if rank == 0:
+            print(json.dumps(run_scene_prep(api, scenes)))
+        return
 
     wl = scenes.urban_scene(level=args.level)
     t_scene = time.perf_counter()

@@ -164,6 +164,90 @@ __device__ __forceinline__ void root_ray(const TxParams* txp, int n_tx, const do
   }
 }
 
+// Ray i of bounce depth `depth`: a launch ray (depth 0) or a queued child.
+__device__ __forceinline__ void load_ray(const TxParams* txp, int n_tx, const double* const* dirs,
+                                         const RayRec* in, int depth, long long i, RayRec& r) {
+  if (depth == 0) {
+    int q;
+    long long li;
+    root_ray(txp, n_tx, dirs, i, r.o, r.d, q, li);
+    r.total = 0.0;
+    r.S = 0.0;
+    r.parent = 0xFFFFFFFFu;
+    r.orank = -1;
+    r.cls = kRootBase + uint32_t(q);
+    r.cop = kRootClass;
+    r.launch = uint32_t(li);
+    r.heap = 1;
+    r.rc = r.tc = 0;
+    r.tx = uint32_t(q);
+  } else {
+    r = in[i];
+  }
+}
+
+// The tree node of a resolved ray (RTSolver.cpp:142-257): its record (hot
+// FP32 part and cold FP64 part), the segment counted for its request.  A
+// ray that hits nothing ends at src + 1e10 d (a launch) or src + 100 d
+// (RTSolver.cpp:231,249).  Returns the node index.
+__device__ __forceinline__ unsigned long long emit_node(NodeHot* nodes, NodeCold* cold,
+                                                        unsigned long long cap, Counters* ctr,
+                                                        unsigned long long* seg_per_tx,
+                                                        const RayRec& r, bool root,
+                                                        const float3& o32, const float3& d32,
+                                                        bool hit, const Hit& h) {
+  const unsigned long long ni = warp_reserve(&ctr->nodes, 1);
+  {  // per-request segment count, one atomic per request present in the warp
+    const unsigned peers = __match_any_sync(__activemask(), r.tx);
+    if (int(lane_id()) == __ffs(peers) - 1)
+      atomicAdd(&seg_per_tx[r.tx], (unsigned long long)__popc(peers));
+  }
+  if (ni < cap) {
+    NodeCold n;
+    NodeHot m;
+    n.s[0] = r.o[0]; n.s[1] = r.o[1]; n.s[2] = r.o[2];
+    if (hit) {
+      n.t[0] = h.p[0]; n.t[1] = h.p[1]; n.t[2] = h.p[2];
+      m.len = float(h.dist);
+    } else {
+      const double sc = root ? 1E10 : 1E2;  // RTSolver.cpp:231,249
+      n.t[0] = x64::add(r.o[0], x64::mul(r.d[0], sc));
+      n.t[1] = x64::add(r.o[1], x64::mul(r.d[1], sc));
+      n.t[2] = x64::add(r.o[2], x64::mul(r.d[2], sc));
+      m.len = float(sc);
+    }
+    n.S = r.S;
+    n.pad = 0.0;
+    m.s[0] = o32.x; m.s[1] = o32.y; m.s[2] = o32.z;
+    m.S = float(r.S);
+    m.u[0] = d32.x; m.u[1] = d32.y; m.u[2] = d32.z;
+    m.parent = r.parent;
+    m.cls = r.cls;
+    m.launch = r.launch;
+    m.heap = r.heap;
+    m.tx = r.tx;
+    m.pad0 = m.pad1 = m.pad2 = 0;
+    cold[ni] = n;
+    nodes[ni] = m;
+  } else {
+    atomicOr(&ctr->overflow, kOvNodes);
+  }
+  return ni;
+}
+
+// The position of the j-th (0-based) set bit of m (j < popc(m)).
+__device__ __forceinline__ int nth_set_bit(unsigned m, int j) {
+  int p = 0;
+  for (int w = 16; w >= 1; w >>= 1) {
+    const int c = __popc(m & (((1u << w) - 1u) << p));  // set bits in [p, p + w)
+    if (c <= j) {
+      j -= c;
+      p += w;
+    }
+  }
+  return p;
+}
+
 // ---- FP32 candidate search (persistent, rays refilled per warp) ----------
 //
 // Each lane traverses one ray at a time.  Lanes whose ray is finished take a
@@ -368,43 +452,8 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
 __device__ __forceinline__ void finish_ray(const TraceArgs& A, const RayRec& r, const float3& o32,
                                            const float3& d32, bool hit, const Hit& h) {
   const TxParams& P = A.txp[r.tx];
-  const unsigned long long ni = warp_reserve(&A.ctr->nodes, 1);
-  {  // per-request segment count, one atomic per request present in the warp
-    const unsigned peers = __match_any_sync(__activemask(), r.tx);
-    if (int(lane_id()) == __ffs(peers) - 1)
-      atomicAdd(&A.seg_per_tx[r.tx], (unsigned long long)__popc(peers));
-  }
-  const bool root = A.depth == 0;
-  if (ni < A.node_cap) {
-    NodeCold n;
-    NodeHot m;
-    n.s[0] = r.o[0]; n.s[1] = r.o[1]; n.s[2] = r.o[2];
-    if (hit) {
-      n.t[0] = h.p[0]; n.t[1] = h.p[1]; n.t[2] = h.p[2];
-      m.len = float(h.dist);
-    } else {
-      const double sc = root ? 1E10 : 1E2;  // RTSolver.cpp:231,249
-      n.t[0] = x64::add(r.o[0], x64::mul(r.d[0], sc));
-      n.t[1] = x64::add(r.o[1], x64::mul(r.d[1], sc));
-      n.t[2] = x64::add(r.o[2], x64::mul(r.d[2], sc));
-      m.len = float(sc);
-    }
-    n.S = r.S;
-    n.pad = 0.0;
-    m.s[0] = o32.x; m.s[1] = o32.y; m.s[2] = o32.z;
-    m.S = float(r.S);
-    m.u[0] = d32.x; m.u[1] = d32.y; m.u[2] = d32.z;
-    m.parent = r.parent;
-    m.cls = r.cls;
-    m.launch = r.launch;
-    m.heap = r.heap;
-    m.tx = r.tx;
-    m.pad0 = m.pad1 = m.pad2 = 0;
-    A.nodes_cold[ni] = n;
-    A.nodes[ni] = m;
-  } else {
-    atomicOr(&A.ctr->overflow, kOvNodes);
-  }
+  const unsigned long long ni = emit_node(A.nodes, A.nodes_cold, A.node_cap, A.ctr, A.seg_per_tx,
+                                          r, A.depth == 0, o32, d32, hit, h);
   // children (RTSolver.cpp:186-221)
   unsigned nch = 0;
   bool do_r = false, do_t = false;
@@ -529,41 +578,34 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
   Hit best;
   best.rank = INT_MAX;
   while (true) {
-    const bool idle = c < 0 && !exhausted;
-    const unsigned im = __ballot_sync(0xffffffffu, idle);
-    if (im) {
+    // Refill: the idle lanes take the next window of rays (the j-th idle
+    // lane the window's j-th ray, so the loads stay in order).  A ray k_find
+    // left without a contender hits nothing: its lane writes the node at once
+    // and stays idle, so such rays never hold a lane through a round of FP64
+    // tests.  Windows repeat until no lane is idle or the chunk is done;
+    // `exhausted` is the same on every lane.
+    unsigned im = __ballot_sync(0xffffffffu, c < 0);
+    while (im && !exhausted) {
+      const int want = __popc(im);
       const int leader = __ffs(im) - 1;
       unsigned long long base = 0;
-      if (int(lane) == leader) base = atomicAdd(A.work, (unsigned long long)__popc(im));
+      if (int(lane) == leader) base = atomicAdd(A.work, (unsigned long long)want);
       base = __shfl_sync(0xffffffffu, base, leader);
-      if (idle) {
-        const long long k = (long long)base + __popc(im & ((1u << lane) - 1u));
-        if (k < n) {
+      if ((long long)base + want >= n) exhausted = true;
+      const long long k = (long long)base + __popc(im & ((1u << lane) - 1u));
+      if (c < 0 && k < n) {
+        load_ray(A.txp, A.n_tx, A.dirs, A.in, A.depth, A.lo + k, r);
+        const float4* f = reinterpret_cast<const float4*>(A.ray32 + k);
+        const float4 fo = f[0], fd = f[1];
+        o32 = make_float3(fo.x, fo.y, fo.z);
+        d32 = make_float3(fd.x, fd.y, fd.z);
+        nc = A.ncand[k];
+        if (nc == 0) {
+          Hit none;
+          emit_node(A.nodes, A.nodes_cold, A.node_cap, A.ctr, A.seg_per_tx, r, A.depth == 0,
+                    o32, d32, false, none);
+        } else {
           c = k;
-          const long long i = A.lo + k;
-          if (A.depth == 0) {
-            int q;
-            long long li;
-            root_ray(A.txp, A.n_tx, A.dirs, i, r.o, r.d, q, li);
-            r.total = 0.0;
-            r.S = 0.0;
-            r.parent = 0xFFFFFFFFu;
-            r.orank = -1;
-            r.cls = kRootBase + uint32_t(q);
-            r.cop = kRootClass;
-            r.launch = uint32_t(li);
-            r.heap = 1;
-            r.rc = r.tc = 0;
-            r.tx = uint32_t(q);
-          } else {
-            r = A.in[i];
-          }
-          // the FP32 copy k_find made (a conversion costs an FP64 pipe slot)
-          const float4* f = reinterpret_cast<const float4*>(A.ray32 + k);
-          const float4 fo = f[0], fd = f[1];
-          o32 = make_float3(fo.x, fo.y, fo.z);
-          d32 = make_float3(fd.x, fd.y, fd.z);
-          nc = A.ncand[k];
           if (nc != kFindFallback) {
             const uint2* cand = A.cand + size_t(k) * kCand;
             for (int j = 0; j < nc; ++j) {
@@ -583,10 +625,9 @@ __global__ void __launch_bounds__(128, SBR_TRACE_BLOCKS) k_trace(TraceArgs A) {
           best.rank = INT_MAX;
           best.dist = __longlong_as_double(0x7ff0000000000000ll);
           best.t = best.dist;
-        } else {
-          exhausted = true;
         }
       }
+      im = __ballot_sync(0xffffffffu, c < 0);
     }
     if (__ballot_sync(0xffffffffu, c >= 0) == 0) break;  // every lane is out of rays
     if (c < 0) continue;
@@ -658,20 +699,6 @@ struct PoolSlots {  // one warp's slots, structure of arrays
   uint8_t nc[kPoolSlots], nx[kPoolSlots], active[kPoolSlots], pad[kPoolSlots];
 };
 
-// The position of the j-th (0-based) set bit of m, which has more than j
-// set bits: a binary search on the counts of bits below each split.
-__device__ __forceinline__ int nth_set_bit(unsigned m, int j) {
-  int p = 0;
-  for (int w = 16; w >= 1; w >>= 1) {
-    const int c = __popc(m & (((1u << w) - 1u) << p));  // set bits in [p, p + w)
-    if (c <= j) {
-      j -= c;
-      p += w;
-    }
-  }
-  return p;
-}
-
 // The position of the j-th (0-based) set bit of the 64-slot mask (m0, m1).
 __device__ __forceinline__ int nth_slot(unsigned m0, unsigned m1, int j) {
   const int c0 = __popc(m0);
@@ -706,24 +733,15 @@ __global__ void __launch_bounds__(32 * kPoolWarps, 4) k_trace_pool(TraceArgs A) 
         const long long k = (long long)base + j;
         if (k >= n) break;
         const int s = nth_slot(e0, e1, j);
-        const long long i = A.lo + k;
         RayRec r;
-        if (A.depth == 0) {
-          int q;
-          long long li;
-          root_ray(A.txp, A.n_tx, A.dirs, i, r.o, r.d, q, li);
-          r.total = 0.0;
-          r.S = 0.0;
-          r.parent = 0xFFFFFFFFu;
-          r.orank = -1;
-          r.cls = kRootBase + uint32_t(q);
-          r.cop = kRootClass;
-          r.launch = uint32_t(li);
-          r.heap = 1;
-          r.rc = r.tc = 0;
-          r.tx = uint32_t(q);
-        } else {
-          r = A.in[i];
+        load_ray(A.txp, A.n_tx, A.dirs, A.in, A.depth, A.lo + k, r);
+        if (A.ncand[k] == 0) {  // no contender: it hits nothing; its slot stays empty
+          const float4* f = reinterpret_cast<const float4*>(A.ray32 + k);
+          const float4 fo = f[0], fd = f[1];
+          Hit none;
+          emit_node(A.nodes, A.nodes_cold, A.node_cap, A.ctr, A.seg_per_tx, r, A.depth == 0,
+                    make_float3(fo.x, fo.y, fo.z), make_float3(fd.x, fd.y, fd.z), false, none);
+          continue;
         }
         for (int a = 0; a < 3; ++a) {
           P.o[a][s] = r.o[a];
