@@ -103,3 +103,40 @@ def test_device_prep_edge_cases(built):
             api.DeviceScene(mesh, [api.MaterialProperties(*m) for m in wl.scene.materials],
                             host_prep=host_prep)
         assert "degenerate" in str(e.value)
+
+
+def _tie_heavy_scene(seed: int, n: int):
+    """Random triangles whose box centres collide a lot: vertex coordinates on a
+    coarse lattice (a few distinct values per axis), some triangles repeated
+    at another height, so every sort of the reference BVH build sees long runs
+    of equal keys."""
+    rng = np.random.default_rng(seed)
+    q = rng.integers(2, 12)  # lattice points per axis
+    base = rng.integers(0, q, size=(n, 3, 3)).astype(np.float32) * np.float32(2.5)
+    base[:, 1, 0] += np.float32(1.0)  # keep the three vertices apart
+    base[:, 2, 1] += np.float32(1.0)
+    base[:, :, 2] += (np.arange(n, dtype=np.float32) * np.float32(1e-3))[:, None]  # no merges
+    e1 = base[:, 1] - base[:, 0]
+    e2 = base[:, 2] - base[:, 0]
+    nrm = np.cross(e1, e2)
+    ln = np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm = np.where(ln > 0, nrm / np.where(ln > 0, ln, 1), np.float32([0, 0, 1]))  # collinear: any
+    return base, nrm.astype(np.float32)
+
+
+@pytest.mark.parametrize("seed,n", [(1, 3000), (2, 20000), (3, 70000)])
+def test_reference_bvh_random_ties(built, seed, n):
+    tri, nrm = _tie_heavy_scene(seed, n)
+    wl = scenes.small_scene()
+    mats = [api.MaterialProperties(*m) for m in wl.scene.materials]
+    mesh = api.Mesh(tri, nrm, np.zeros(n, np.int32))
+    a = api.DeviceScene(mesh, mats)
+    b = api.DeviceScene(mesh, mats, host_prep=True)
+    ra, rb = a.reference_bvh(), b.reference_bvh()
+    assert ra["max_depth"] == rb["max_depth"]
+    for key in ("links", "order"):
+        np.testing.assert_array_equal(ra[key], rb[key])
+    np.testing.assert_array_equal(ra["boxes"].view(np.int64), rb["boxes"].view(np.int64))
+    np.testing.assert_array_equal(a.mesh_order(), b.mesh_order())
+    a.close()
+    b.close()
