@@ -38,7 +38,7 @@ EVENT_BYTES = 16     # per capture event (group-table rank + count update)
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of k_trace's
 # first launch of the level-9 urban solve (its 2,621,442 launch rays), from
 # one ncu capture of that launch alone: profiles/k_trace_urban_L9_first_launch.md
-TRACE_FIRST_LAUNCH_DRAM_BYTES = 275898880 + 689526784
+TRACE_FIRST_LAUNCH_DRAM_BYTES = 277407488 + 698306816
 
 
 def _env_int(k, d):
