@@ -94,7 +94,7 @@ class Tuning(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("find_steps", "find_refill", "find_blocks_per_sm",
                                         "trace_blocks_per_sm", "capture_blocks_per_sm",
                                         "trace_chunk_log2", "trace_kernel",
-                                        "pipeline_graph")]
+                                        "pipeline_graph", "find_tris_per_step")]
 
 
 class Timing(C.Structure):

@@ -245,6 +245,7 @@ struct Tuning {
   int chunk_log2 = 0;
   int trace_kernel = 0;  // FP64 resolution: 1 = k_trace (a ray per lane), 2 = k_trace_pool
   int graph = 0;         // pipeline as a CUDA graph on repeat: 1 (0 = default), -1 = never
+  int find_tris = 0;     // FP32 search: leaf triangles per step, 1 or 2 (0 = default)
 };
 
 // A request mix's identity for the autotuner's cache: the sorted
@@ -682,6 +683,7 @@ static int capture_grid(const Tuning& t) { return persistent_grid(capture_fit(),
 
 // The FP64 resolution kernel solves use unless tuned otherwise.
 constexpr int kDefaultTraceKernel = 1;
+constexpr int kFindTris = 1;  // leaf triangles per FP32 search step
 
 // A tuning with every default filled in (the shapes a solve really uses).
 static Tuning resolved(Tuning t) {
@@ -695,6 +697,7 @@ static Tuning resolved(Tuning t) {
   t.chunk_log2 = std::min(std::max(t.chunk_log2, 16), 26);
   if (t.trace_kernel <= 0 || t.trace_kernel > 2) t.trace_kernel = kDefaultTraceKernel;
   t.graph = t.graph < 0 ? -1 : 1;
+  if (t.find_tris <= 0 || t.find_tris > 2) t.find_tris = kFindTris;
   return t;
 }
 
@@ -1654,6 +1657,7 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     fnd.ray32 = W.ray32.p;
     fnd.steps = tu.find_steps > 0 ? tu.find_steps : kFindSteps;
     fnd.refill = tu.find_refill > 0 ? std::min(tu.find_refill, 32) : kFindRefill;
+    fnd.tris_per_step = resolved(tu).find_tris;
     ta.cand = W.cand.p;
     ta.ncand = W.ncand.p;
     ta.ray32 = W.ray32.p;
@@ -2531,6 +2535,7 @@ static void tuning_to_c(const Tuning& t, sbr_tuning* o) {
   o->capture_blocks_per_sm = t.capture_bps;
   o->trace_chunk_log2 = t.chunk_log2;
   o->pipeline_graph = t.graph;
+  o->find_tris_per_step = t.find_tris;
 }
 
 sbr_status sbr_scene_set_tuning(sbr_scene* scene, const sbr_tuning* t) {
@@ -2542,9 +2547,10 @@ sbr_status sbr_scene_set_tuning(sbr_scene* scene, const sbr_tuning* t) {
       t->find_blocks_per_sm < 0 || t->trace_blocks_per_sm < 0 || t->capture_blocks_per_sm < 0 ||
       (t->trace_chunk_log2 != 0 && (t->trace_chunk_log2 < 16 || t->trace_chunk_log2 > 26)) ||
       t->trace_kernel < 0 || t->trace_kernel > 2 || t->pipeline_graph < -1 ||
-      t->pipeline_graph > 1) {
+      t->pipeline_graph > 1 || t->find_tris_per_step < 0 || t->find_tris_per_step > 2) {
     set_err("sbr_scene_set_tuning: fields must be >= 0, find_refill <= 32, trace_chunk_log2 "
-            "0 or 16..26, trace_kernel 0..2 and pipeline_graph -1..1");
+            "0 or 16..26, trace_kernel 0..2, pipeline_graph -1..1 and find_tris_per_step "
+            "0..2");
     return SBR_ERR_INVALID_ARG;
   }
   SceneImpl& S = scene->impl;
@@ -2557,6 +2563,7 @@ sbr_status sbr_scene_set_tuning(sbr_scene* scene, const sbr_tuning* t) {
   S.tuning.chunk_log2 = t->trace_chunk_log2;
   S.tuning.trace_kernel = t->trace_kernel;
   S.tuning.graph = t->pipeline_graph;
+  S.tuning.find_tris = t->find_tris_per_step;
   return SBR_OK;
 }
 
@@ -2618,21 +2625,22 @@ sbr_status sbr_autotune(sbr_scene* scene, const sbr_request* requests, int n_req
     return v;
   };
   const std::vector<int> steps{8, 16, 32, 64, 128}, refill{4, 8, 16, 24, 32}, chunk{20, 22, 24},
-      kernels{1, 2};
+      kernels{1, 2}, tris{1, 2};
   for (int round = 0; round < rounds; ++round) {
     bool moved = false;
-    for (int p = 0; p < 7; ++p) {
+    for (int p = 0; p < 8; ++p) {
       const std::vector<int> cand = p == 0   ? kernels
                                     : p == 1 ? steps
                                     : p == 2 ? refill
                                     : p == 3 ? span(ff)
                                     : p == 4 ? span(tf)
                                     : p == 5 ? span(cf)
-                                             : chunk;
+                                    : p == 6 ? chunk
+                                             : tris;
       for (int v : cand) {
         Tuning t = cur;
-        int* f[7] = {&t.trace_kernel, &t.find_steps, &t.find_refill, &t.find_bps, &t.trace_bps,
-                     &t.capture_bps, &t.chunk_log2};
+        int* f[8] = {&t.trace_kernel, &t.find_steps, &t.find_refill, &t.find_bps, &t.trace_bps,
+                     &t.capture_bps, &t.chunk_log2, &t.find_tris};
         if (*f[p] == v) continue;
         *f[p] = v;
         if ((st = time_of(t, ms)) != SBR_OK) return st;

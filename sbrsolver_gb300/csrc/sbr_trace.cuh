@@ -274,6 +274,7 @@ struct FindArgs {
   RayF32* ray32;               // FP32 copy per ray of the chunk
   int steps;                   // traversal steps between refills
   int refill;                  // idle lanes that trigger a refill
+  int tris_per_step;           // triangles of a leaf tested per step (1 or 2)
 };
 
 // Defaults of the search's tunables (the autotuner may choose others).
@@ -360,25 +361,28 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
     bool done = false;
     for (int it = 0; it < A.steps && !done; ++it) {
       if (pending >= 0) {
-        // one triangle of the pending leaf per step, so lanes testing
-        // triangles and lanes stepping through nodes cost one step each
-        const int j = pending >> 3, left = (pending & 7) - 1;
-        pending = left > 0 ? ((j + 1) << 3 | left) : -1;
-        float tlo, thi;
-        const Tri32 T = A.sc.stri[j];
-        const int k = tri_classify(T, o32, d32, no, nd, tlo, thi);
-        if (k == 0 || tlo > tcut) continue;
-        const int rk = __ldg(A.sc.srank + j);
-        // the triangle the ray starts on, left at a clear angle: the
-        // reference's test of it certainly fails (origin_rejected); such a
-        // contender is never certain (k == 2), so dropping it changes no cut
-        if (rk == orank && origin_rejected(T, o32, d32)) continue;
-        if (nc == kCand) {
-          fail = done = true;
-          break;
+        // up to tris_per_step triangles of the pending leaf per step (a node
+        // visit tests two child boxes), so lanes testing triangles and lanes
+        // stepping through nodes take steps of comparable cost
+        for (int q = 0; q < A.tris_per_step && pending >= 0; ++q) {
+          const int j = pending >> 3, left = (pending & 7) - 1;
+          pending = left > 0 ? ((j + 1) << 3 | left) : -1;
+          float tlo, thi;
+          const Tri32 T = A.sc.stri[j];
+          const int k = tri_classify(T, o32, d32, no, nd, tlo, thi);
+          if (k == 0 || tlo > tcut) continue;
+          const int rk = __ldg(A.sc.srank + j);
+          // the triangle the ray starts on, left at a clear angle: the
+          // reference's test of it certainly fails (origin_rejected); such a
+          // contender is never certain (k == 2), so dropping it changes no cut
+          if (rk == orank && origin_rejected(T, o32, d32)) continue;
+          if (nc == kCand) {
+            fail = done = true;
+            break;
+          }
+          out[nc++] = make_uint2(unsigned(rk), __float_as_uint(tlo));
+          if (k == 2) tcut = fminf(tcut, thi * (1.0f + kTieSlack) + 1e-30f);
         }
-        out[nc++] = make_uint2(unsigned(rk), __float_as_uint(tlo));
-        if (k == 2) tcut = fminf(tcut, thi * (1.0f + kTieSlack) + 1e-30f);
         continue;
       }
       if (sp == 0) {
