@@ -245,7 +245,8 @@ def run_batched(precision: str, best_rate: float = 0.0):
             "field_error_vs_fp64": err}
 
 
-def run_serving(precision: str, n_req: int = 96, rates=(10.0, 50.0, 500.0), slots: int = 2):
+def run_serving(precision: str, n_req: int = 96, rates=(10.0, 50.0, 500.0), slots: int = 2,
+                policy=None, graphs: bool = True):
     """The config-4 mix through the server at Poisson arrival rates `rates`
     (req/s), against the same requests solved one at a time.  At the highest
     rate the queue saturates, so its throughput is the sustained capacity.
@@ -256,6 +257,9 @@ def run_serving(precision: str, n_req: int = 96, rates=(10.0, 50.0, 500.0), slot
     from sbrsolver_gb300 import api, scenes
     wls = [scenes.small_scene(), scenes.urban_scene(), scenes.large_scene()]
     scs = [api.DeviceScene.from_scene(w.scene) for w in wls]
+    if not graphs:
+        for sc in scs:
+            sc.set_tuning(pipeline_graph=-1)
     stream = serving_stream(wls, n_req)
     qs = [(si, api.request_from_workload(r, precision)) for si, r in stream]
     for si, q in qs:
@@ -279,6 +283,8 @@ def run_serving(precision: str, n_req: int = 96, rates=(10.0, 50.0, 500.0), slot
             free = max(free, a) + sv
             plain_lat.append(1e3 * (free - a))
         srv = api.Server(scs, slots=slots)
+        if policy is not None:
+            srv.set_policy(*policy)
         lat, seg_s, done = [], 0, 0
         t0 = time.perf_counter()
         nxt = 0

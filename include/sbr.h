@@ -299,6 +299,15 @@ sbr_status sbr_server_submit(sbr_server* server, int scene, const sbr_request* r
 sbr_status sbr_server_poll(sbr_server* server, sbr_completion* out, int max, int* n_out,
                            int timeout_ms);
 sbr_status sbr_server_pending(sbr_server* server, int* queued, long long* in_flight_bytes);
+/* Admission and batching policy (takes effect for the next request a worker
+ * picks): requests whose device-memory estimate is at most batch_bytes are
+ * solved together with the queued ones of the same scene that are also that
+ * small, up to max_batch per device pass (1 = never batch); a request's
+ * priority is its estimate minus aging_bytes_per_s for every second it has
+ * waited (0 = smallest first, large = arrival order).  Defaults: 2 GiB, 64,
+ * 16e9. */
+sbr_status sbr_server_set_policy(sbr_server* server, long long batch_bytes, int max_batch,
+                                double aging_bytes_per_s);
 /* Finishes queued and running requests, then stops. */
 sbr_status sbr_server_destroy(sbr_server* server);
 

@@ -21,7 +21,8 @@ EXPORTS = (
     "sbr_solve_batch", "sbr_result_counts", "sbr_result_field", "sbr_result_paths",
     "sbr_result_timing", "sbr_result_destroy", "sbr_last_error", "sbr_version",
     "sbr_receiver_field_sum_noalloc", "sbr_server_create", "sbr_server_submit", "sbr_server_poll",
-    "sbr_server_pending", "sbr_server_destroy", "sbr_result_field_error", "sbr_result_field_fp64",
+    "sbr_server_pending", "sbr_server_destroy", "sbr_server_set_policy",
+    "sbr_result_field_error", "sbr_result_field_fp64",
     "sbr_write_field_csv", "sbr_write_receivers_vtk", "sbr_write_paths_vtk",
     "sbr_write_launch_rays_vtk", "sbr_scene_set_materials", "sbr_stl_read",
     "sbr_generate_rx_line", "sbr_generate_rx_plane", "sbr_pattern_create", "sbr_pattern_read",
@@ -142,6 +143,7 @@ def load(path: str = LIB_PATH):
             "sbr_server_poll": [vp, P(Completion), I, P(I), I],
             "sbr_server_pending": [vp, P(I), P(C.c_longlong)],
             "sbr_server_destroy": [vp],
+            "sbr_server_set_policy": [vp, C.c_longlong, C.c_int, C.c_double],
             "sbr_write_field_csv": [C.c_char_p, P(D), I, P(D)],
             "sbr_write_receivers_vtk": [C.c_char_p, P(D), I, P(D)],
             "sbr_write_paths_vtk": [C.c_char_p, P(Path), I, P(D), P(D), I],

@@ -59,15 +59,13 @@ long long estimate_bytes(const sbr_request& q) {
   return (long long)sbr::request_bytes(q) + (64LL << 20);
 }
 
-constexpr size_t kMaxBatch = 64;
-// Waiting time converted to priority: a request that has waited one second
-// ranks like one whose estimate is 16 GB smaller.
-#ifndef SBR_SERVER_AGING
-#define SBR_SERVER_AGING 16e9
-#endif
-constexpr double kAgingBytesPerSec = SBR_SERVER_AGING;
-// Requests at most this large (device-memory estimate) are batched together.
-constexpr long long kSmallBytes = 512LL << 20;
+// Default policy (sbr_server_set_policy changes it): requests at most 2 GiB
+// large (device-memory estimate) are batched, up to 64 in one pass; waiting
+// time converted to priority at 16 GB per second (a request that has waited
+// one second ranks like one whose estimate is 16 GB smaller).
+constexpr long long kDefaultBatchBytes = 2LL << 30;
+constexpr int kDefaultMaxBatch = 64;
+constexpr double kDefaultAging = 16e9;
 
 }  // namespace
 
@@ -82,6 +80,9 @@ struct sbr_server {
   std::deque<sbr_completion> done;
   std::vector<std::thread> workers;
   int device = 0;
+  long long batch_bytes = kDefaultBatchBytes;  // requests at most this large are batched
+  size_t max_batch = size_t(kDefaultMaxBatch);
+  double aging = kDefaultAging;  // priority bytes per second waited
 
   // Index of the queued request to run next (least aged cost among those
   // that fit the budget), or -1.  Caller holds mu.
@@ -94,7 +95,7 @@ struct sbr_server {
       const long long need = std::min(j.est_bytes, budget);
       if (!(in_flight == 0 || in_flight + need <= budget)) continue;
       const double waited = std::chrono::duration<double>(now - j.submitted).count();
-      const double cost = double(j.est_bytes) - kAgingBytesPerSec * waited;
+      const double cost = double(j.est_bytes) - aging * waited;
       if (best < 0 || cost < best_cost) {
         best = long(k);
         best_cost = cost;
@@ -120,9 +121,9 @@ struct sbr_server {
         batch.push_back(std::move(queue[size_t(sel)]));
         queue.erase(queue.begin() + sel);
         est = std::min(batch[0].est_bytes, budget);
-        if (batch[0].est_bytes <= kSmallBytes) {
-          for (auto it = queue.begin(); it != queue.end() && batch.size() < kMaxBatch;) {
-            if (it->scene == batch[0].scene && it->est_bytes <= kSmallBytes &&
+        if (batch[0].est_bytes <= batch_bytes) {
+          for (auto it = queue.begin(); it != queue.end() && batch.size() < max_batch;) {
+            if (it->scene == batch[0].scene && it->est_bytes <= batch_bytes &&
                 in_flight + est + it->est_bytes <= budget) {
               est += it->est_bytes;
               batch.push_back(std::move(*it));
@@ -266,6 +267,21 @@ sbr_status sbr_server_pending(sbr_server* srv, int* queued, long long* in_flight
   std::lock_guard<std::mutex> lock(srv->mu);
   if (queued) *queued = int(srv->queue.size());
   if (in_flight_bytes) *in_flight_bytes = srv->in_flight;
+  return SBR_OK;
+}
+
+sbr_status sbr_server_set_policy(sbr_server* server, long long batch_bytes, int max_batch,
+                                double aging_bytes_per_s) {
+  if (!server || batch_bytes < 0 || max_batch < 1 || max_batch > 4096 ||
+      !(aging_bytes_per_s >= 0.0)) {
+    sbr::set_error_message("sbr_server_set_policy: need a server, batch_bytes >= 0, "
+                           "1 <= max_batch <= 4096 and aging_bytes_per_s >= 0");
+    return SBR_ERR_INVALID_ARG;
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  server->batch_bytes = batch_bytes;
+  server->max_batch = size_t(max_batch);
+  server->aging = aging_bytes_per_s;
   return SBR_OK;
 }
 

@@ -31,11 +31,17 @@ def _requests():
     return small, urban, reqs
 
 
-def test_results_identical_alone_and_in_the_mix(built):
+@pytest.mark.parametrize("policy", [None, (0, 1, 0.0), (64 << 30, 64, 1e15)],
+                         ids=["default", "never_batched", "batch_everything_fifo"])
+def test_results_identical_alone_and_in_the_mix(built, policy):
     small, urban, reqs = _requests()
     sc = [api.DeviceScene.from_scene(small.scene), api.DeviceScene.from_scene(urban.scene)]
     alone = [api.solve(sc[s], api.request_from_workload(r), with_paths=True) for s, r in reqs]
     srv = api.Server(sc, slots=4)
+    if policy is not None:
+        srv.set_policy(*policy)
+    with pytest.raises(Exception):
+        srv.set_policy(1 << 30, 0, 1e9)  # at least one request per pass
     keep = []
     for tag, (s, r) in enumerate(reqs):
         q = api.request_from_workload(r)
