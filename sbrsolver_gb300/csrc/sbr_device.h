@@ -14,6 +14,8 @@
 //     hand anything within the margin to the FP64 form.
 #pragma once
 
+#include <climits>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -37,6 +39,17 @@ struct __align__(16) Node32 {
   int child[2];
   int pad[2];
 };
+
+// Four-wide node of the search BVH (128 bytes): up to four child boxes, each
+// coordinate as a four-lane vector, and the child refs (>= 0: node index,
+// < 0: ~(first << 3 | count) of a leaf, kEmptyChild: no child).
+struct __align__(16) Node4 {
+  float lo[3][4];
+  float hi[3][4];
+  int child[4];
+  int pad[4];
+};
+constexpr int kEmptyChild = INT_MIN;
 
 // FP64 reference node (depth-first numbering), with its box also as floats
 // (exact: box bounds are float vertex coordinates) and a mask of its flat
@@ -88,8 +101,9 @@ struct DevScene {
   const Tri32* corr32;     // FP32 filter copy of corr
   const int* rank_to_id;   // triangle id of each depth-first rank
   const Material* mats;
-  // search BVH of the FP32 candidate search (child < 0: ~(first << 3 | count))
-  const Node32* snode;
+  // search BVH of the FP32 candidate search, four-wide (child < 0:
+  // ~(first << 3 | count))
+  const Node4* snode4;
   const Tri32* stri;    // triangles in search leaf order
   const int* srank;     // their depth-first ranks
   const AncBox* anc;    // per reference leaf: its boxes up to the root

@@ -275,7 +275,7 @@ struct SceneImpl {
   DBuf<RefNode> ref;
   DBuf<Tri32> tri32;
   DBuf<Tri64> tri64;
-  DBuf<Node32> snode;
+  DBuf<Node4> snode4;
   DBuf<Tri32> stri;
   DBuf<int> srank;
   DBuf<AncBox> anc;
@@ -441,31 +441,77 @@ static void upload_scene(SceneImpl& S) {
   S.tri32.upload(t32.data(), t32.size(), st);
   S.tri64.upload(t64.data(), t64.size(), st);
   S.mats.upload(mats.data(), mats.size(), st);
-  {  // search BVH
+  {  // search BVH, collapsed to four-wide nodes
     const SearchBVH& B = H.search;
-    std::vector<Node32> sn(B.nodes.size());
-    host_parallel(B.nodes.size(), [&](size_t lo, size_t hi) {
-      for (size_t i = lo; i < hi; ++i) {
-        Node32& m = sn[i];
-        std::memset(&m, 0, sizeof m);
+    // A node's two child slots are widened by replacing the internal child
+    // with the largest box (surface area) by its two children, until four
+    // slots or only leaves; the boxes are the binary tree's own.  Nodes are
+    // numbered depth-first (parent first).
+    struct Slot {
+      float lo[3], hi[3];
+      int ref;
+    };
+    auto area = [](const Slot& x) {
+      const float dx = x.hi[0] - x.lo[0], dy = x.hi[1] - x.lo[1], dz = x.hi[2] - x.lo[2];
+      return dx * dy + dy * dz + dz * dx;
+    };
+    std::vector<Node4> sn;
+    sn.reserve(B.nodes.size());
+    std::function<int(int)> build4 = [&](int b) -> int {
+      Slot s[4];
+      int ns = 0;
+      for (int k = 0; k < 2; ++k) {
         for (int a = 0; a < 3; ++a) {
-          m.lo0[a] = B.nodes[i].lo[0][a];
-          m.hi0[a] = B.nodes[i].hi[0][a];
-          m.lo1[a] = B.nodes[i].lo[1][a];
-          m.hi1[a] = B.nodes[i].hi[1][a];
+          s[ns].lo[a] = B.nodes[size_t(b)].lo[k][a];
+          s[ns].hi[a] = B.nodes[size_t(b)].hi[k][a];
         }
-        m.child[0] = B.nodes[i].child[0];
-        m.child[1] = B.nodes[i].child[1];
+        s[ns++].ref = B.nodes[size_t(b)].child[k];
       }
-    });
+      while (ns < 4) {
+        int pick = -1;
+        float best = -1.0f;
+        for (int i = 0; i < ns; ++i)
+          if (s[i].ref >= 0 && area(s[i]) > best) {
+            best = area(s[i]);
+            pick = i;
+          }
+        if (pick < 0) break;
+        const SearchNode& c = B.nodes[size_t(s[pick].ref)];
+        for (int i = ns; i > pick + 1; --i) s[i] = s[i - 1];
+        for (int k = 0; k < 2; ++k) {
+          Slot& o = s[pick + k];
+          for (int a = 0; a < 3; ++a) {
+            o.lo[a] = c.lo[k][a];
+            o.hi[a] = c.hi[k][a];
+          }
+          o.ref = c.child[k];
+        }
+        ++ns;
+      }
+      const int me = int(sn.size());
+      sn.emplace_back();
+      int refs[4];
+      for (int i = 0; i < ns; ++i) refs[i] = s[i].ref >= 0 ? build4(s[i].ref) : s[i].ref;
+      Node4& o = sn[size_t(me)];
+      std::memset(&o, 0, sizeof o);
+      for (int i = 0; i < 4; ++i) {
+        for (int a = 0; a < 3; ++a) {
+          o.lo[a][i] = i < ns ? s[i].lo[a] : INFINITY;
+          o.hi[a][i] = i < ns ? s[i].hi[a] : -INFINITY;
+        }
+        o.child[i] = i < ns ? refs[i] : kEmptyChild;
+      }
+      return me;
+    };
+    build4(0);
     std::vector<Tri32> st32(B.order.size());
     host_parallel(B.order.size(), [&](size_t lo, size_t hi) {
       for (size_t j = lo; j < hi; ++j) st32[j] = t32[B.order[j]];
     });
-    S.snode.upload(sn.data(), sn.size(), st);
+    S.snode4.upload(sn.data(), sn.size(), st);
     S.stri.upload(st32.data(), st32.size(), st);
     S.srank.upload(B.order.data(), B.order.size(), st);
-    S.dev.snode = S.snode.p;
+    S.dev.snode4 = S.snode4.p;
     S.dev.stri = S.stri.p;
     S.dev.srank = S.srank.p;
     CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
@@ -515,7 +561,7 @@ static void upload_scene(SceneImpl& S) {
   S.dev_bytes = (long long)(n32.size() * sizeof(Node32) + ref.size() * sizeof(RefNode) +
                             t32.size() * sizeof(Tri32) + t64.size() * sizeof(Tri64) +
                             2 * nt * sizeof(int) + nt * sizeof(CorrTri) +
-                            S.snode.n * sizeof(Node32) + S.stri.n * sizeof(Tri32) +
+                            S.snode4.n * sizeof(Node4) + S.stri.n * sizeof(Tri32) +
                             S.srank.n * sizeof(int) + S.anc.n * sizeof(AncBox) +
                             S.anc_off.n * sizeof(int));
   CK(cudaStreamSynchronize(st));

@@ -394,49 +394,53 @@ __global__ void __launch_bounds__(128, 8) k_find(FindArgs A) {
         pending = ~ni;
         continue;
       }
-      float4 f0, f1, f2;
-      int2 ch;
-      load_node(A.sc.snode, ni, f0, f1, f2, ch);
-      float tn0, tf0, tn1, tf1;
-      slab32(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, o32, inv, m, tn0, tf0);
-      slab32(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, o32, inv, m, tn1, tf1);
-      const bool h0 = tn0 <= tf0 && tf0 >= 0.0f && tn0 <= tcut;
-      const bool h1 = tn1 <= tf1 && tf1 >= 0.0f && tn1 <= tcut;
-      int first = 0, second = 0;
-      bool has_first = false, has_second = false;
-      if (h0 && h1) {
-        has_first = has_second = true;
-        if (tn1 < tn0) {
-          first = ch.y;
-          second = ch.x;
-        } else {
-          first = ch.x;
-          second = ch.y;
+      // a four-wide node: the children the ray's slab test keeps (within
+      // tcut), nearest first; the farther ones go on the stack, the nearest
+      // on top (a leaf as the nearest becomes the pending leaf at once)
+      const float4* p = reinterpret_cast<const float4*>(A.sc.snode4 + ni);
+      const float4 lx = __ldg(p), ly = __ldg(p + 1), lz = __ldg(p + 2);
+      const float4 hx = __ldg(p + 3), hy = __ldg(p + 4), hz = __ldg(p + 5);
+      const int4 cr = __ldg(reinterpret_cast<const int4*>(p + 6));
+      auto visit = [&](float ax, float ay, float az, float bx, float by, float bz, int c,
+                       float& t) -> int {
+        float tn, tf;
+        slab32(ax, ay, az, bx, by, bz, o32, inv, m, tn, tf);
+        const bool h = c != kEmptyChild && tn <= tf && tf >= 0.0f && tn <= tcut;
+        t = h ? tn : INFINITY;
+        return h ? c : kEmptyChild;
+      };
+      float t0, t1, t2, t3;
+      int c0 = visit(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, cr.x, t0);
+      int c1 = visit(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, cr.y, t1);
+      int c2 = visit(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, cr.z, t2);
+      int c3 = visit(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, cr.w, t3);
+      auto order = [](float& ta, int& ca, float& tb, int& cb) {
+        if (tb < ta) {
+          const float t = ta;
+          ta = tb;
+          tb = t;
+          const int c = ca;
+          ca = cb;
+          cb = c;
         }
-      } else if (h0) {
-        has_first = true;
-        first = ch.x;
-      } else if (h1) {
-        has_first = true;
-        first = ch.y;
+      };
+      order(t0, c0, t1, c1);  // sorting network for four
+      order(t2, c2, t3, c3);
+      order(t0, c0, t2, c2);
+      order(t1, c1, t3, c3);
+      order(t1, c1, t2, c2);
+      const int need = int(c0 != kEmptyChild) + int(c1 != kEmptyChild) +
+                       int(c2 != kEmptyChild) + int(c3 != kEmptyChild);
+      if (sp + need > kStack) {
+        fail = done = true;
+        break;
       }
-      if (has_second) {
-        if (sp >= kStack) {
-          fail = done = true;
-          break;
-        }
-        stack[sp++] = second;  // node, or ~leaf code
-      }
-      if (has_first) {
-        if (first < 0) {
-          pending = ~first;
-        } else {
-          if (sp >= kStack) {
-            fail = done = true;
-            break;
-          }
-          stack[sp++] = first;
-        }
+      if (c3 != kEmptyChild) stack[sp++] = c3;  // node, or ~leaf code
+      if (c2 != kEmptyChild) stack[sp++] = c2;
+      if (c1 != kEmptyChild) stack[sp++] = c1;
+      if (c0 != kEmptyChild) {
+        if (c0 < 0) pending = ~c0;
+        else stack[sp++] = c0;
       }
     }
     if (done) {
