@@ -382,7 +382,7 @@ typedef struct sbr_tuning {
                                 request structure, capacities and shapes) is captured as a
                                 CUDA graph and replayed from then on; -1: every solve issues
                                 its operations one by one */
-  int find_tris_per_step;    /* FP32 search: triangles of a leaf tested per step, 1 or 2 (1) */
+  int find_tris_per_step;    /* FP32 search: triangles of a leaf tested per step, 1 or 2 (2) */
 } sbr_tuning;
 /* The scene's default shapes, used by request mixes sbr_autotune has not
  * tuned.  Values above what fits on an SM are clamped. */

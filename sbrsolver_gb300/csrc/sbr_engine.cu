@@ -729,7 +729,7 @@ static int capture_grid(const Tuning& t) { return persistent_grid(capture_fit(),
 
 // The FP64 resolution kernel solves use unless tuned otherwise.
 constexpr int kDefaultTraceKernel = 1;
-constexpr int kFindTris = 1;  // leaf triangles per FP32 search step
+constexpr int kFindTris = 2;  // leaf triangles per FP32 search step
 
 // A tuning with every default filled in (the shapes a solve really uses).
 static Tuning resolved(Tuning t) {
