@@ -6,6 +6,7 @@ frames and boxes (Triangle.cpp:37-70), search BVH and reference BVH
 device) are built on the GPU; SBR_SCENE_HOST_PREP builds them all on the
 host.  The two must give identical tables, bit for bit, and the same
 solve."""
+import os
 import time
 
 import numpy as np
@@ -134,6 +135,38 @@ def test_reference_bvh_random_ties(built, seed, n):
     b = api.DeviceScene(mesh, mats, host_prep=True)
     ra, rb = a.reference_bvh(), b.reference_bvh()
     assert ra["max_depth"] == rb["max_depth"]
+    for key in ("links", "order"):
+        np.testing.assert_array_equal(ra[key], rb[key])
+    np.testing.assert_array_equal(ra["boxes"].view(np.int64), rb["boxes"].view(np.int64))
+    np.testing.assert_array_equal(a.mesh_order(), b.mesh_order())
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("n", [1000, 3000])
+def test_reference_bvh_heap_sort(built, n):
+    """Box centres along x that drive std::sort past its depth budget into its
+    heap sort at the root (tests/golden/make_introsort_killer.cpp): 1,000 keys
+    (a warp's sort in shared memory) and 3,000 (partition rounds, then the heap
+    sort of a long segment in global memory).  The device tree must equal the
+    host one."""
+    keys = np.loadtxt(os.path.join(os.path.dirname(__file__), "golden",
+                                   f"introsort_killer_{n}.txt"), dtype=np.int64)
+    assert len(keys) == n and len(np.unique(keys)) == n
+    x = keys.astype(np.float32) * np.float32(0.25)
+    y = np.arange(n, dtype=np.float32) * np.float32(0.5)
+    tri = np.zeros((n, 3, 3), np.float32)  # triangles in the planes x = const
+    tri[:, :, 0] = x[:, None]
+    tri[:, :, 1] = y[:, None]
+    tri[:, 1, 1] += np.float32(1.0)
+    tri[:, 2, 2] = np.float32(1.0)
+    nrm = np.tile(np.array([[1.0, 0.0, 0.0]], np.float32), (n, 1))
+    wl = scenes.small_scene()
+    mats = [api.MaterialProperties(*m) for m in wl.scene.materials]
+    mesh = api.Mesh(tri, nrm, np.zeros(n, np.int32))
+    a = api.DeviceScene(mesh, mats)
+    b = api.DeviceScene(mesh, mats, host_prep=True)
+    ra, rb = a.reference_bvh(), b.reference_bvh()
     for key in ("links", "order"):
         np.testing.assert_array_equal(ra[key], rb[key])
     np.testing.assert_array_equal(ra["boxes"].view(np.int64), rb["boxes"].view(np.int64))
