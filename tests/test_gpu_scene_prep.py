@@ -143,6 +143,36 @@ def test_reference_bvh_random_ties(built, seed, n):
     b.close()
 
 
+def test_reference_bvh_flat_scene(built):
+    """A ground grid of 3,200 triangles, all at z = 0: every box is flat, every
+    surface area 0 and every split cost 0/0, so the host's tree is one leaf;
+    the device's must be the same."""
+    k = 40
+    xs, ys = np.meshgrid(np.arange(k, dtype=np.float32), np.arange(k, dtype=np.float32))
+    x0, y0 = xs.ravel(), ys.ravel()
+    z = np.zeros_like(x0)
+    a = np.stack([np.stack([x0, y0, z], 1), np.stack([x0 + 1, y0, z], 1),
+                  np.stack([x0 + 1, y0 + 1, z], 1)], 1)
+    b = np.stack([np.stack([x0, y0, z], 1), np.stack([x0 + 1, y0 + 1, z], 1),
+                  np.stack([x0, y0 + 1, z], 1)], 1)
+    tri = np.concatenate([a, b]).astype(np.float32)
+    nrm = np.tile(np.array([[0.0, 0.0, 1.0]], np.float32), (len(tri), 1))
+    wl = scenes.small_scene()
+    mats = [api.MaterialProperties(*m) for m in wl.scene.materials]
+    mesh = api.Mesh(tri, nrm, np.zeros(len(tri), np.int32))
+    d = api.DeviceScene(mesh, mats)
+    h = api.DeviceScene(mesh, mats, host_prep=True)
+    rd, rh = d.reference_bvh(), h.reference_bvh()
+    assert len(rh["links"]) == 1  # one leaf
+    for key in ("links", "order"):
+        np.testing.assert_array_equal(rd[key], rh[key])
+    np.testing.assert_array_equal(rd["boxes"].view(np.int64), rh["boxes"].view(np.int64))
+    np.testing.assert_array_equal(d.mesh_order(), h.mesh_order())
+    np.testing.assert_array_equal(d.coplanar_ids(), h.coplanar_ids())
+    d.close()
+    h.close()
+
+
 @pytest.mark.parametrize("n", [1000, 3000])
 def test_reference_bvh_heap_sort(built, n):
     """Box centres along x that drive std::sort past its depth budget into its
