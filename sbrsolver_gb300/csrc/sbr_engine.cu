@@ -517,7 +517,8 @@ static void upload_scene(SceneImpl& S) {
     CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
   }
   {  // every reference leaf's boxes up to the root, one run per leaf
-    // (the leaf, its ancestors to the root, then an end marker)
+    // (the leaf, its ancestors to the root, then an end marker), written on
+    // the device from the reference nodes uploaded above
     std::vector<int> off(nn, -1);
     size_t total = 0;
     for (int i = 0; i < nn; ++i) {
@@ -525,22 +526,12 @@ static void upload_scene(SceneImpl& S) {
       off[i] = int(total);
       total += size_t(H.nodes[i].depth) + 2;
     }
-    std::vector<AncBox> ab(total);
-    host_parallel(size_t(nn), [&](size_t lo, size_t hi) {
-      for (int i = int(lo); i < int(hi); ++i) {
-        if (H.nodes[i].c0 >= 0) continue;
-        AncBox* o = &ab[size_t(off[i])];
-        for (int n = i; n >= 0; n = H.nodes[n].parent, ++o) {
-          std::memcpy(o->fb, ref[n].fb, sizeof o->fb);
-          o->flat = ref[n].flat;
-          o->node = n;
-        }
-        std::memset(o, 0, sizeof *o);
-        o->node = -1;
-      }
-    });
-    S.anc.upload(ab.data(), ab.size(), st);
+    if (total > size_t(INT_MAX)) throw std::string("reference BVH too deep for the ancestor table");
+    S.anc.ensure(std::max<size_t>(1, total));
     S.anc_off.upload(off.data(), off.size(), st);
+    prep::k_anc_fill<<<std::max(1, std::min(4096, (nn + 255) / 256)), 256, 0, st>>>(
+        S.ref.p, nn, S.anc_off.p, S.anc.p);
+    CK(cudaGetLastError());
     S.dev.anc = S.anc.p;
     S.dev.anc_off = S.anc_off.p;
     CK(cudaStreamSynchronize(st));

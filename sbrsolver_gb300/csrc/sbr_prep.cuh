@@ -505,5 +505,29 @@ __global__ void k_children(const Seg* segs, int n_segs, const SegPlan* plans, Se
   }
 }
 
+// ---- ancestor boxes of the reference leaves --------------------------------
+
+// Per reference leaf, its box and its ancestors' up to the root as AncBox
+// records (the FP32 copy, the flat-axis mask, the node) from off[leaf], then
+// an end marker; k_trace's reachability check walks one run per hit.
+__global__ void k_anc_fill(const RefNode* ref, int nn, const int* off, AncBox* anc) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+    if (ref[i].c0 >= 0) continue;
+    AncBox* o = anc + off[i];
+    for (int n = i; n >= 0; n = ref[n].parent, ++o) {
+      AncBox b;
+      for (int a = 0; a < 6; ++a) b.fb[a] = ref[n].fb[a];
+      b.flat = ref[n].flat;
+      b.node = n;
+      *o = b;
+    }
+    AncBox end;
+    for (int a = 0; a < 6; ++a) end.fb[a] = 0.0f;
+    end.flat = 0;
+    end.node = -1;
+    *o = end;
+  }
+}
+
 }  // namespace prep
 }  // namespace sbr
