@@ -253,9 +253,10 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int j) {
 // Each lane traverses one ray at a time.  Lanes whose ray is finished take a
 // new one from the chunk's work counter (one atomic per warp, when at least
 // half the warp is idle or nobody is busy), so warps stay full while rays of
-// very different lengths finish at different times.  A step is one node
-// visit or one triangle test, so lanes in a leaf and lanes between nodes
-// advance at the same pace.  The FP32 copy of each ray it loads is kept for
+// very different lengths finish at different times.  The search tree is
+// four-wide; a step is one node visit (four child boxes) or up to
+// tris_per_step triangle tests, so lanes in a leaf and lanes between nodes
+// advance at a similar pace.  The FP32 copy of each ray it loads is kept for
 // k_trace (ray32).
 struct FindArgs {
   DevScene sc;
