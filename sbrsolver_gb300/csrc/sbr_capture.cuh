@@ -616,7 +616,7 @@ __device__ __forceinline__ int warp_find(int incl, int k) {
   return rl;
 }
 
-constexpr int kFastB = 16;  // nodes staged per warp and batch
+constexpr int kFastB = 32;  // nodes staged per warp and batch (one per lane)
 
 __global__ void __launch_bounds__(32 * kCapWarps, SBR_CAP_BLOCKS) k_capture_fast(CaptureArgs A) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
