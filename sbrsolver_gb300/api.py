@@ -352,6 +352,17 @@ def solve(scene: DeviceScene, requests, with_paths=True) -> Result:
     return _collect(h, sum(r[0].n_rx for r in requests), with_paths)
 
 
+_PATH_DTYPE = None
+
+
+def _path_dtype():
+    """numpy's structured dtype of sbr_path (formed once)."""
+    global _PATH_DTYPE
+    if _PATH_DTYPE is None:
+        _PATH_DTYPE = np.ctypeslib.as_array((_lib.Path * 1)()).dtype
+    return _PATH_DTYPE
+
+
 def _collect(h, n_rx: int, with_paths: bool) -> Result:
     """Reads an sbr_result into a Result and destroys it."""
     lib = _lib.load()
@@ -378,7 +389,7 @@ def _collect(h, n_rx: int, with_paths: bool) -> Result:
                                             kind.ctypes.data_as(ip),
                                             pts.ctypes.data_as(C.POINTER(C.c_double))))
             # the whole path set as flat arrays (cheap at 1e5-1e6 paths)
-            A = np.ctypeslib.as_array(P)
+            A = np.frombuffer(P, dtype=_path_dtype())
             arrays = {k: np.array(A[k]) for k in ("request", "receiver", "launch", "heap",
                                                   "ray_offset", "n_rays", "field", "near_edge")}
             arrays.update(tri=tri[:cnt.rays], cop=cop[:cnt.rays], kind=kind[:cnt.rays],
