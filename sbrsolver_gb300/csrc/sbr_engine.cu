@@ -197,6 +197,7 @@ struct Workspace {
   HBuf<int> h_rxreq;
   HBuf<double> h_rx;
   HBuf<GridBuild> h_gb;
+  HBuf<unsigned char> h_res;  // a solve's results on their way to the host
   // the device pipeline as a CUDA graph: captured the second time the same
   // pipeline (pipeline_key) runs, replayed whenever it comes again.  A few
   // graphs are kept (the passes of a split batch, a serving loop's request
@@ -1902,42 +1903,66 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
       upd(W.r_pairs, c.pairs / n);
     }
     const unsigned long long ns = c.survivors;
-    // ---- results to the host
-    out.field.resize(6 * size_t(rx_total));
-    if (rx_total)
-      CK(cudaMemcpyAsync(out.field.data(), W.field.p, sizeof(double) * 6 * rx_total,
-                         cudaMemcpyDeviceToHost, st));
-    out.field_bound.resize(size_t(rx_total));
-    unsigned long long fst[2] = {0, 0};
-    if (rx_total)
-      CK(cudaMemcpyAsync(out.field_bound.data(), W.field_bound.p, sizeof(double) * rx_total,
-                         cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(fst, W.fstat.p, sizeof fst, cudaMemcpyDeviceToHost, st));
-    out.field64.clear();
-    if (field_check) {
-      out.field64.resize(6 * size_t(rx_total));
-      if (rx_total)
-        CK(cudaMemcpyAsync(out.field64.data(), W.field64.p, sizeof(double) * 6 * rx_total,
-                           cudaMemcpyDeviceToHost, st));
-    }
-    std::vector<int> order(ns), nray(ns), starts(rx_total + 1), pnear(ns);
-    std::vector<Survivor> sv(ns);
-    std::vector<double> pf(6 * ns), pts(ns * (kMaxDepth + 2) * 3);
-    std::vector<int> ptri(ns * (kMaxDepth + 1)), pcop(ns * (kMaxDepth + 1)),
-        pkind(ns * (kMaxDepth + 1));
+    // ---- results to the host, through the workspace's pinned staging (every
+    // array copied by DMA into one area, one synchronisation)
+    size_t need = 0;
+    auto at = [&need](size_t bytes) {
+      const size_t o = need;
+      need += (bytes + 15) & ~size_t(15);
+      return o;
+    };
+    const size_t nrs = size_t(ns) * (kMaxDepth + 1), nps = size_t(ns) * (kMaxDepth + 2) * 3;
+    const size_t b_field = sizeof(double) * 6 * size_t(rx_total);
+    const size_t o_field = at(b_field), o_fb = at(sizeof(double) * size_t(rx_total));
+    const size_t o_fst = at(2 * sizeof(unsigned long long));
+    const size_t o_f64 = at(field_check ? b_field : 0);
+    const size_t o_order = at(sizeof(int) * ns), o_nray = at(sizeof(int) * ns);
+    const size_t o_near = at(sizeof(int) * ns), o_sv = at(sizeof(Survivor) * ns);
+    const size_t o_pf = at(sizeof(double) * 6 * ns);
+    const size_t o_tri = at(sizeof(int) * nrs), o_cop = at(sizeof(int) * nrs);
+    const size_t o_kind = at(sizeof(int) * nrs), o_pts = at(sizeof(double) * nps);
+    if (need > W.h_res.n) W.h_res.ensure(need + need / 4 + (size_t(64) << 10));  // pinning is slow
+    unsigned char* hr = W.h_res.p;
+    auto get = [&](size_t o, const void* src, size_t bytes) {
+      if (bytes) CK(cudaMemcpyAsync(hr + o, src, bytes, cudaMemcpyDeviceToHost, st));
+    };
+    get(o_field, W.field.p, b_field);
+    get(o_fb, W.field_bound.p, sizeof(double) * size_t(rx_total));
+    get(o_fst, W.fstat.p, 2 * sizeof(unsigned long long));
+    if (field_check) get(o_f64, W.field64.p, b_field);
     if (ns) {
-      CK(cudaMemcpyAsync(order.data(), W.s_order.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(nray.data(), W.path_nray.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pnear.data(), W.path_near.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(sv.data(), W.surv.p, sizeof(Survivor) * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pf.data(), W.path_field.p, sizeof(double) * 6 * ns, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(ptri.data(), W.path_tri.p, sizeof(int) * ptri.size(), cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pcop.data(), W.path_cop.p, sizeof(int) * pcop.size(), cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pkind.data(), W.path_kind.p, sizeof(int) * pkind.size(), cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(pts.data(), W.path_pts.p, sizeof(double) * pts.size(), cudaMemcpyDeviceToHost, st));
+      get(o_order, W.s_order.p, sizeof(int) * ns);
+      get(o_nray, W.path_nray.p, sizeof(int) * ns);
+      get(o_near, W.path_near.p, sizeof(int) * ns);
+      get(o_sv, W.surv.p, sizeof(Survivor) * ns);
+      get(o_pf, W.path_field.p, sizeof(double) * 6 * ns);
+      get(o_tri, W.path_tri.p, sizeof(int) * nrs);
+      get(o_cop, W.path_cop.p, sizeof(int) * nrs);
+      get(o_kind, W.path_kind.p, sizeof(int) * nrs);
+      get(o_pts, W.path_pts.p, sizeof(double) * nps);
     }
     CK(cudaEventRecord(W.ev[7], st));
     CK(cudaStreamSynchronize(st));
+    const double* hfield = reinterpret_cast<const double*>(hr + o_field);
+    out.field.assign(hfield, hfield + 6 * size_t(rx_total));
+    const double* hfb = reinterpret_cast<const double*>(hr + o_fb);
+    out.field_bound.assign(hfb, hfb + size_t(rx_total));
+    unsigned long long fst[2];
+    std::memcpy(fst, hr + o_fst, sizeof fst);
+    out.field64.clear();
+    if (field_check) {
+      const double* h64 = reinterpret_cast<const double*>(hr + o_f64);
+      out.field64.assign(h64, h64 + 6 * size_t(rx_total));
+    }
+    const int* order = reinterpret_cast<const int*>(hr + o_order);
+    const int* nray = reinterpret_cast<const int*>(hr + o_nray);
+    const int* pnear = reinterpret_cast<const int*>(hr + o_near);
+    const Survivor* sv = reinterpret_cast<const Survivor*>(hr + o_sv);
+    const double* pf = reinterpret_cast<const double*>(hr + o_pf);
+    const int* ptri = reinterpret_cast<const int*>(hr + o_tri);
+    const int* pcop = reinterpret_cast<const int*>(hr + o_cop);
+    const int* pkind = reinterpret_cast<const int*>(hr + o_kind);
+    const double* pts = reinterpret_cast<const double*>(hr + o_pts);
     // assemble paths in receiver order, then (launch, BFS) order
     std::vector<int> req_of(rx_total);
     for (int r = 0; r < n_req; ++r)
