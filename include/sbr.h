@@ -375,7 +375,7 @@ typedef struct sbr_tuning {
   int find_blocks_per_sm;    /* FP32 search: resident 128-thread blocks per SM (all that fit) */
   int trace_blocks_per_sm;   /* FP64 resolution: resident 128-thread blocks per SM (all that fit) */
   int capture_blocks_per_sm; /* capture: resident blocks per SM (all that fit) */
-  int trace_chunk_log2;      /* rays per search/resolution launch pair = 2^this, 16..26 (24) */
+  int trace_chunk_log2;      /* rays per search/resolution launch pair = 2^this, 16..26 (25) */
   int trace_kernel;          /* FP64 resolution: 1 = one ray per lane (registers), 2 = 64 rays
                                 per warp in shared memory, tests handed out to full warps */
   int pipeline_graph;        /* 0 (default) or 1: a device pipeline that ran before (same

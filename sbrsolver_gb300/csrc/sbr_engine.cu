@@ -722,6 +722,10 @@ static int capture_grid(const Tuning& t) { return persistent_grid(capture_fit(),
 // The FP64 resolution kernel solves use unless tuned otherwise.
 constexpr int kDefaultTraceKernel = 1;
 constexpr int kFindTris = 2;  // leaf triangles per FP32 search step
+// Rays per search/resolution launch pair: 2^25 holds a level-9 launch's
+// widest depth at six reflections and one transmission (7 rays per launch)
+// in one pair; the chunk never exceeds the depth's queue capacity.
+constexpr int kTraceChunkLog2 = 25;
 
 // A tuning with every default filled in (the shapes a solve really uses).
 static Tuning resolved(Tuning t) {
@@ -731,7 +735,7 @@ static Tuning resolved(Tuning t) {
   t.find_bps = t.find_bps > 0 ? std::min(t.find_bps, find_fit()) : find_fit();
   t.trace_bps = t.trace_bps > 0 ? std::min(t.trace_bps, trace_fit()) : trace_fit();
   t.capture_bps = t.capture_bps > 0 ? std::min(t.capture_bps, capture_fit()) : capture_fit();
-  if (t.chunk_log2 <= 0) t.chunk_log2 = 24;
+  if (t.chunk_log2 <= 0) t.chunk_log2 = kTraceChunkLog2;
   t.chunk_log2 = std::min(std::max(t.chunk_log2, 16), 26);
   if (t.trace_kernel <= 0 || t.trace_kernel > 2) t.trace_kernel = kDefaultTraceKernel;
   t.graph = t.graph < 0 ? -1 : 1;
@@ -1547,7 +1551,8 @@ static void solve_impl(SceneImpl& S, Workspace& W, const sbr_request* reqs, int 
     W.rx32.ensure(std::max(1, rx_total));
     W.rx_bad.ensure(1);
     // trace chunks: each depth runs in chunks of at most kTraceChunk rays
-    const long long kTraceChunk = 1LL << (tu.chunk_log2 > 0 ? std::min(tu.chunk_log2, 26) : 24);
+    const long long kTraceChunk =
+        1LL << (tu.chunk_log2 > 0 ? std::min(tu.chunk_log2, 26) : kTraceChunkLog2);
     const long long max_width = std::max<long long>(launches, (long long)W.cap_queue);
     const long long chunk = std::max<long long>(1, std::min(kTraceChunk, max_width));
     W.cand.ensure(size_t(chunk) * kCand);
@@ -2686,7 +2691,8 @@ sbr_status sbr_autotune(sbr_scene* scene, const sbr_request* requests, int n_req
     for (int b = std::max(1, fit / 2); b <= fit; ++b) v.push_back(b);
     return v;
   };
-  const std::vector<int> steps{8, 16, 32, 64, 128}, refill{4, 8, 16, 24, 32}, chunk{20, 22, 24},
+  const std::vector<int> steps{8, 16, 32, 64, 128}, refill{4, 8, 16, 24, 32},
+      chunk{20, 22, 24, 25, 26},
       kernels{1, 2}, tris{1, 2};
   for (int round = 0; round < rounds; ++round) {
     bool moved = false;
