@@ -246,7 +246,7 @@ def run_batched(precision: str, best_rate: float = 0.0):
 
 
 def run_serving(precision: str, n_req: int = 96, rates=(10.0, 50.0, 500.0), slots: int = 2,
-                policy=None, graphs: bool = True):
+                policy=None, graphs: bool = True, arrival_seed: int = 99):
     """The config-4 mix through the server at Poisson arrival rates `rates`
     (req/s), against the same requests solved one at a time.  At the highest
     rate the queue saturates, so its throughput is the sustained capacity.
@@ -274,7 +274,7 @@ def run_serving(precision: str, n_req: int = 96, rates=(10.0, 50.0, 500.0), slot
     plain = seg / (time.perf_counter() - t0)
     sweep = []
     for rate in rates:
-        rng = np.random.default_rng(99)
+        rng = np.random.default_rng(arrival_seed)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, len(qs)))
         # the plain path under the same arrivals: one request at a time in
         # arrival order, each taking its measured service time

@@ -304,10 +304,11 @@ sbr_status sbr_server_pending(sbr_server* server, int* queued, long long* in_fli
  * solved together with the queued ones of the same scene that are also that
  * small, up to max_batch per device pass (1 = never batch); a request's
  * priority is its estimate minus aging_bytes_per_s for every second it has
- * waited (0 = smallest first, large = arrival order).  Defaults: 2 GiB, 64,
- * 16e9. */
+ * waited (0 = smallest first, large = arrival order); at most max_large
+ * requests larger than batch_bytes run at once (0 = as many as the slots;
+ * small batches still run beside them).  Defaults: 2 GiB, 64, 16e9, 0. */
 sbr_status sbr_server_set_policy(sbr_server* server, long long batch_bytes, int max_batch,
-                                double aging_bytes_per_s);
+                                double aging_bytes_per_s, int max_large);
 /* Finishes queued and running requests, then stops. */
 sbr_status sbr_server_destroy(sbr_server* server);
 

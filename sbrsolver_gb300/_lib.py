@@ -143,7 +143,7 @@ def load(path: str = LIB_PATH):
             "sbr_server_poll": [vp, P(Completion), I, P(I), I],
             "sbr_server_pending": [vp, P(I), P(C.c_longlong)],
             "sbr_server_destroy": [vp],
-            "sbr_server_set_policy": [vp, C.c_longlong, C.c_int, C.c_double],
+            "sbr_server_set_policy": [vp, C.c_longlong, C.c_int, C.c_double, C.c_int],
             "sbr_write_field_csv": [C.c_char_p, P(D), I, P(D)],
             "sbr_write_receivers_vtk": [C.c_char_p, P(D), I, P(D)],
             "sbr_write_paths_vtk": [C.c_char_p, P(Path), I, P(D), P(D), I],

@@ -480,10 +480,11 @@ class Server:
         self._nrx = {}
 
     def set_policy(self, batch_bytes: int = 2 << 30, max_batch: int = 64,
-                   aging_bytes_per_s: float = 16e9) -> None:
-        """Batching and priority policy (sbr_server_set_policy)."""
+                   aging_bytes_per_s: float = 16e9, max_large: int = 0) -> None:
+        """Batching, priority and large-request concurrency policy
+        (sbr_server_set_policy)."""
         _lib.check(self._lib.sbr_server_set_policy(self.handle, int(batch_bytes), int(max_batch),
-                                                   float(aging_bytes_per_s)))
+                                                   float(aging_bytes_per_s), int(max_large)))
 
     def submit(self, scene: int, request: tuple, tag: int) -> None:
         self._nrx[int(tag)] = request[0].n_rx

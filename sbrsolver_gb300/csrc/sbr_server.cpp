@@ -8,11 +8,14 @@
 // the requests already running: cost = its device-memory estimate (which
 // scales with its ray-tree bound, i.e. its work) minus kAgingBytesPerSec per
 // second it has waited, so short requests go first and every request is
-// served within about a second of becoming the oldest.  If the chosen
-// request is small, the worker also takes the queued small requests on the
-// same scene (up to kMaxBatch, within the budget) and solves them together in
-// one device pass (sbr_solve_batch), which fills the GPU far better than
-// small requests one by one.  Every solve checks a workspace (buffers + CUDA
+// served within about a second of becoming the oldest.  The policy may cap
+// how many requests too large to batch run at once (small batches still run
+// beside them); by default only the slots bound it, since one large solve at
+// a time lowered the saturated throughput of a mixed stream by 2-5 % without
+// lowering its tail latency.  If the chosen request is small, the worker also
+// takes the queued small requests on the same scene (up to kMaxBatch, within
+// the budget) and solves them together in one device pass (sbr_solve_batch),
+// which fills the GPU far better than small requests one by one.  Every solve checks a workspace (buffers + CUDA
 // stream) out of the process-wide pool, so work admitted while other work is
 // on the GPU runs on its own stream and overlaps with it.  Each result is
 // exactly what sbr_solve returns for that request alone: requests share only
@@ -62,10 +65,12 @@ long long estimate_bytes(const sbr_request& q) {
 // Default policy (sbr_server_set_policy changes it): requests at most 2 GiB
 // large (device-memory estimate) are batched, up to 64 in one pass; waiting
 // time converted to priority at 16 GB per second (a request that has waited
-// one second ranks like one whose estimate is 16 GB smaller).
+// one second ranks like one whose estimate is 16 GB smaller); no cap on the
+// larger requests running at once beyond the slots.
 constexpr long long kDefaultBatchBytes = 2LL << 30;
 constexpr int kDefaultMaxBatch = 64;
 constexpr double kDefaultAging = 16e9;
+constexpr int kDefaultMaxLarge = 0;
 
 }  // namespace
 
@@ -83,15 +88,19 @@ struct sbr_server {
   long long batch_bytes = kDefaultBatchBytes;  // requests at most this large are batched
   size_t max_batch = size_t(kDefaultMaxBatch);
   double aging = kDefaultAging;  // priority bytes per second waited
+  int max_large = kDefaultMaxLarge;  // larger-than-batch_bytes solves at once (0 = no limit)
+  int large_running = 0;
 
   // Index of the queued request to run next (least aged cost among those
-  // that fit the budget), or -1.  Caller holds mu.
+  // that fit the budget and the limit on large solves), or -1.  Caller holds mu.
   long pick() const {
     const Clock::time_point now = Clock::now();
+    const bool large_full = max_large > 0 && large_running >= max_large;
     long best = -1;
     double best_cost = 0;
     for (size_t k = 0; k < queue.size(); ++k) {
       const Job& j = queue[k];
+      if (large_full && j.est_bytes > batch_bytes) continue;
       const long long need = std::min(j.est_bytes, budget);
       if (!(in_flight == 0 || in_flight + need <= budget)) continue;
       const double waited = std::chrono::duration<double>(now - j.submitted).count();
@@ -109,6 +118,7 @@ struct sbr_server {
     for (;;) {
       std::vector<Job> batch;
       long long est = 0;
+      bool large = false;
       {
         std::unique_lock<std::mutex> lock(mu);
         long sel = -1;
@@ -121,7 +131,10 @@ struct sbr_server {
         batch.push_back(std::move(queue[size_t(sel)]));
         queue.erase(queue.begin() + sel);
         est = std::min(batch[0].est_bytes, budget);
-        if (batch[0].est_bytes <= batch_bytes) {
+        large = batch[0].est_bytes > batch_bytes;
+        if (large) {
+          ++large_running;
+        } else {
           for (auto it = queue.begin(); it != queue.end() && batch.size() < max_batch;) {
             if (it->scene == batch[0].scene && it->est_bytes <= batch_bytes &&
                 in_flight + est + it->est_bytes <= budget) {
@@ -176,6 +189,7 @@ struct sbr_server {
       {
         std::lock_guard<std::mutex> lock(mu);
         in_flight -= est;
+        if (large) --large_running;
         for (auto& c : out) done.push_back(c);
       }
       cv_work.notify_all();
@@ -271,17 +285,22 @@ sbr_status sbr_server_pending(sbr_server* srv, int* queued, long long* in_flight
 }
 
 sbr_status sbr_server_set_policy(sbr_server* server, long long batch_bytes, int max_batch,
-                                double aging_bytes_per_s) {
+                                double aging_bytes_per_s, int max_large) {
   if (!server || batch_bytes < 0 || max_batch < 1 || max_batch > 4096 ||
-      !(aging_bytes_per_s >= 0.0)) {
+      !(aging_bytes_per_s >= 0.0) || max_large < 0) {
     sbr::set_error_message("sbr_server_set_policy: need a server, batch_bytes >= 0, "
-                           "1 <= max_batch <= 4096 and aging_bytes_per_s >= 0");
+                           "1 <= max_batch <= 4096, aging_bytes_per_s >= 0 and "
+                           "max_large >= 0");
     return SBR_ERR_INVALID_ARG;
   }
-  std::lock_guard<std::mutex> lock(server->mu);
-  server->batch_bytes = batch_bytes;
-  server->max_batch = size_t(max_batch);
-  server->aging = aging_bytes_per_s;
+  {
+    std::lock_guard<std::mutex> lock(server->mu);
+    server->batch_bytes = batch_bytes;
+    server->max_batch = size_t(max_batch);
+    server->aging = aging_bytes_per_s;
+    server->max_large = max_large;
+  }
+  server->cv_work.notify_all();  // a looser limit may admit a queued request now
   return SBR_OK;
 }
 

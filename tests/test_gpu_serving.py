@@ -31,8 +31,10 @@ def _requests():
     return small, urban, reqs
 
 
-@pytest.mark.parametrize("policy", [None, (0, 1, 0.0), (64 << 30, 64, 1e15)],
-                         ids=["default", "never_batched", "batch_everything_fifo"])
+@pytest.mark.parametrize("policy", [None, (0, 1, 0.0), (64 << 30, 64, 1e15),
+                                    (2 << 30, 64, 16e9, 1), (0, 1, 16e9, 2)],
+                         ids=["default", "never_batched", "batch_everything_fifo",
+                              "one_large_at_once", "unbatched_two_at_once"])
 def test_results_identical_alone_and_in_the_mix(built, policy):
     small, urban, reqs = _requests()
     sc = [api.DeviceScene.from_scene(small.scene), api.DeviceScene.from_scene(urban.scene)]
@@ -42,6 +44,8 @@ def test_results_identical_alone_and_in_the_mix(built, policy):
         srv.set_policy(*policy)
     with pytest.raises(Exception):
         srv.set_policy(1 << 30, 0, 1e9)  # at least one request per pass
+    with pytest.raises(Exception):
+        srv.set_policy(1 << 30, 8, 1e9, -1)  # a limit on large solves is >= 0
     keep = []
     for tag, (s, r) in enumerate(reqs):
         q = api.request_from_workload(r)

@@ -70,7 +70,7 @@ def test_null_arguments_are_rejected(built):
     assert lib.sbr_result_counts(None, None) == _lib.ERR_INVALID_ARG
     assert lib.sbr_scene_destroy(None) == _lib.OK
     assert lib.sbr_result_destroy(None) == _lib.OK
-    assert lib.sbr_server_set_policy(None, 1 << 30, 8, 1e9) == _lib.ERR_INVALID_ARG
+    assert lib.sbr_server_set_policy(None, 1 << 30, 8, 1e9, 1) == _lib.ERR_INVALID_ARG
     assert b"set_policy" in lib.sbr_last_error()
 
 
