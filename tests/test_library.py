@@ -163,3 +163,59 @@ def test_fault_hook_arms_and_disarms(built):
     lib = _lib.load()
     assert lib.sbr_fault_inject_alloc(3) == _lib.OK
     assert lib.sbr_fault_inject_alloc(-1) == _lib.OK
+
+
+def _header_prototypes():
+    """Every function include/sbr.h declares: name -> parameter types."""
+    hdr = open(os.path.join(ROOT, "include", "sbr.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", " ", hdr, flags=re.S)
+    protos = {}
+    for name, params in re.findall(r"\b(sbr_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", hdr):
+        params = " ".join(params.split())
+        protos[name] = [] if params in ("", "void") else [p.strip() for p in params.split(",")]
+    return protos
+
+
+def _kind_of_c(param: str):
+    """(kind, bytes) of a C parameter declaration: pointers, then scalars."""
+    if "*" in param:
+        return ("ptr", 8)
+    words = param.split()[:-1]  # drop the parameter name
+    if "double" in words:
+        return ("float", 8)
+    if words.count("long") == 2:
+        return ("signed", 8)
+    if "unsigned" in words or "uint32_t" in words:
+        return ("unsigned", 4)
+    if "int" in words:
+        return ("signed", 4)
+    raise AssertionError(f"unclassified parameter type: {param!r}")
+
+
+def _kind_of_ctypes(t):
+    if t in (C.c_void_p, C.c_char_p) or issubclass(t, C._Pointer):
+        return ("ptr", 8)
+    code = t._type_
+    if code == "d":
+        return ("float", C.sizeof(t))
+    if code in "bhilq":
+        return ("signed", C.sizeof(t))
+    if code in "BHILQ":
+        return ("unsigned", C.sizeof(t))
+    raise AssertionError(f"unclassified ctypes type: {t!r}")
+
+
+def test_bindings_match_header_prototypes(built):
+    """Each ctypes binding passes as many arguments as the header declares,
+    each of the same kind and width (pointer, signed or unsigned integer,
+    double), so a change of a C signature cannot go unnoticed by the
+    Python side."""
+    protos = _header_prototypes()
+    assert set(protos) == set(_lib.EXPORTS)
+    lib = _lib.load()
+    for name, params in protos.items():
+        argtypes = getattr(lib, name).argtypes
+        assert argtypes is not None, name
+        assert len(argtypes) == len(params), (name, params, argtypes)
+        for p, t in zip(params, argtypes):
+            assert _kind_of_c(p) == _kind_of_ctypes(t), (name, p, t)
