@@ -235,6 +235,49 @@ def slab_walls(wl: Workload, widths: Sequence[float]) -> Workload:
     return wl
 
 
+# A transmitter frame rotated 53.13 degrees about z and 67.38 degrees about x:
+# the product of two rotations with Pythagorean-triple entries (3-4-5 and
+# 5-12-13), each entry one correctly rounded division, so the matrix is the
+# same bits on every machine.
+ROTATED_TX_FRAME = (3 / 5, -4 / 13, 48 / 65,
+                    4 / 5, 3 / 13, -36 / 65,
+                    0.0, 12 / 13, 5 / 13)
+
+
+def request_variant(name: str) -> Workload:
+    """Request options the reference's main() never sets, on seeded scenes:
+    the isotropic and half-wave patterns (FieldCompute.cpp:153-183), a
+    rotated transmitter frame (txCoordSys), a transmit power other than 1 W
+    and the Fresnel switch off (RTSolver.h:25-37).
+
+    small_L5_R4T1_halfwave_rotated: small scene, level 5, 4 reflections and 1
+      transmission, half-wave dipole in the rotated frame, 2.5 W at 3.5 GHz.
+    urban_L5_R3T1_rx1600_halfwave_rotated: urban canyon at level 5 with
+      receivers every 25 m, 3 reflections and 1 transmission, the same
+      antenna, frame, power and frequency.
+    urban_L5_R3T1_rx1600_isotropic_nofresnel: the same urban solve with the
+      isotropic pattern at 0.1 W and 60 GHz and the slab coefficients of
+      zero-width walls (the reference's useFresnelCoeff = false: reflection 0,
+      transmission 1)."""
+    if name == "small_L5_R4T1_halfwave_rotated":
+        wl = small_scene()
+        q = wl.request
+        q.tessellation, q.max_reflection, q.max_transmission = 5, 4, 1
+        q.antenna, q.tx_coord_sys, q.pt, q.frequency = 2, ROTATED_TX_FRAME, 2.5, 3.5e9
+    elif name == "urban_L5_R3T1_rx1600_halfwave_rotated":
+        wl = urban_scene(level=5, rx_pitch=25.0, max_reflection=3, max_transmission=1)
+        q = wl.request
+        q.antenna, q.tx_coord_sys, q.pt, q.frequency = 2, ROTATED_TX_FRAME, 2.5, 3.5e9
+    elif name == "urban_L5_R3T1_rx1600_isotropic_nofresnel":
+        wl = urban_scene(level=5, rx_pitch=25.0, max_reflection=3, max_transmission=1)
+        q = wl.request
+        q.antenna, q.pt, q.frequency, q.use_fresnel = 0, 0.1, 60e9, False
+    else:
+        raise KeyError(name)
+    wl.name = name
+    return wl
+
+
 def urban_scene(seed: int = 0x5B5 + 1, level: int = 9, rx_pitch: float = 10.0,
                 max_reflection: int = 6, max_transmission: int = 1) -> Workload:
     """Synthetic urban canyon: 1 km x 1 km ground plus 400 boxes on a 50 m

@@ -1,6 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run here, where the reference checkout exists:  python tests/golden/make_golden.py
+Run where the reference checkout exists:
+    SBR_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [--variants]
 It compiles the reference's own sources (oracle/build_ref.sh -> oracle/_ref/
 ref_harness), runs each case through RTSolver::ExecuteRayTracing, and stores
 the surviving paths and fields per receiver as .npz.  For the reference's
@@ -157,6 +158,17 @@ def coefficient_sweep() -> None:
     print("coeff_test.csv: magnitudes identical, phases equal modulo pi")
 
 
+VARIANTS = ("small_L5_R4T1_halfwave_rotated", "urban_L5_R3T1_rx1600_halfwave_rotated",
+            "urban_L5_R3T1_rx1600_isotropic_nofresnel")
+
+
+def request_variants() -> None:
+    """Request options main() never sets (patterns, frame, power, Fresnel
+    switch; sbrsolver_gb300.scenes.request_variant), through the reference."""
+    for name in VARIANTS:
+        run_case(scenes.request_variant(name), name)
+
+
 def main() -> None:
     if oracle_build.build_reference(REF) is None:
         raise SystemExit("reference checkout not found: set SBR_REFERENCE_DIR to it")
@@ -182,6 +194,7 @@ def main() -> None:
     run_case(scenes.slab_walls(scenes.urban_scene(level=5, rx_pitch=25.0, max_reflection=3,
                                                   max_transmission=2), (0.5, 0.2, 0.01)),
              "urban_L5_R3T2_rx1600_slab")
+    request_variants()
     # icosahedron launch directions, bit-exact
     for lvl in (0, 1, 2, 5):
         with tempfile.TemporaryDirectory() as d:
@@ -195,5 +208,9 @@ def main() -> None:
 if __name__ == "__main__":
     if "--outputs-only" in sys.argv:  # refresh only shipped_outputs.json
         shipped_output_hashes()
+    elif "--variants" in sys.argv:  # (re)write only the request-variant fixtures
+        if oracle_build.build_reference(REF) is None:
+            raise SystemExit("reference checkout not found: set SBR_REFERENCE_DIR to it")
+        request_variants()
     else:
         main()

@@ -30,11 +30,14 @@ def _case(name):
         return scenes.urban_scene(level=5, rx_pitch=100.0)
     if name == "urban_L4_R3T2_rx400":
         return scenes.urban_scene(level=4, rx_pitch=50.0, max_reflection=3, max_transmission=2)
-    raise KeyError(name)
+    return scenes.request_variant(name)
 
 
 CASES = ["reference_main", "small_L6_R3", "small_L4_R3T1_hertzian", "urban_L5_R6T1_rx100",
-         "urban_L4_R3T2_rx400", "urban_L5_R3T2_rx1600_slab"]
+         "urban_L4_R3T2_rx400", "urban_L5_R3T2_rx1600_slab",
+         # pattern, transmitter frame, power and Fresnel-switch variants
+         "small_L5_R4T1_halfwave_rotated", "urban_L5_R3T1_rx1600_halfwave_rotated",
+         "urban_L5_R3T1_rx1600_isotropic_nofresnel"]
 # slab coefficients instead of infinite walls: ground 0.5 m, concrete walls
 # 0.2 m, glass 0.01 m thick
 SLAB_WIDTHS = (0.5, 0.2, 0.01)
