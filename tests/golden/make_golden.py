@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
 Run where the reference checkout exists:
-    SBR_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [--variants]
+    SBR_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [--variants | --bvh]
 It compiles the reference's own sources (oracle/build_ref.sh -> oracle/_ref/
 ref_harness), runs each case through RTSolver::ExecuteRayTracing, and stores
 the surviving paths and fields per receiver as .npz.  For the reference's
@@ -158,6 +158,109 @@ def coefficient_sweep() -> None:
     print("coeff_test.csv: magnitudes identical, phases equal modulo pi")
 
 
+def parse_scene_dump(path: str) -> dict:
+    """The harness's `scene` dump (the reference's mesh after
+    StlToGeometry + BVH::ConstructBVH) as arrays in a numbering-free form:
+    mesh_order (triangle id at each position of the sorted triangle vector),
+    coplanar ids and frame rows by triangle id, and the tree in depth-first
+    order from the root (children[0] before children[1], BVH.h:276-328):
+    node boxes, leaf sizes (-1 for an inner node) and the leaves' triangle
+    ids in visit order."""
+    with open(path) as fh:
+        n = int(fh.readline().split()[1])
+        mesh_order = np.zeros(n, np.int32)
+        cop = np.zeros(n, np.int32)
+        frames = np.zeros((n, 9), np.float64)
+        for k in range(n):
+            t = fh.readline().split()
+            i = int(t[1])
+            mesh_order[k] = i
+            cop[i] = int(t[2])
+            frames[i] = [float(x) for x in t[3:12]]
+        m = int(fh.readline().split()[1])
+        children = np.zeros((m, 2), np.int64)
+        boxes = np.zeros((m, 6), np.float64)
+        objs = []
+        for k in range(m):
+            t = fh.readline().split()
+            children[k] = (int(t[1]), int(t[2]))
+            # the boxes hold float values (bounds of float vertices), printed
+            # with 9 significant digits: read back as float, then widened
+            boxes[k] = np.array(t[3:9], np.float32)
+            objs.append([int(x) for x in t[10:10 + int(t[9])]])
+    pre_boxes, leaf_n, leaf_ids, stack = [], [], [], [0]
+    while stack:
+        k = stack.pop()
+        pre_boxes.append(boxes[k])
+        if children[k][0] < 0:
+            leaf_n.append(len(objs[k]))
+            leaf_ids += objs[k]
+        else:
+            leaf_n.append(-1)
+            stack += [int(children[k][1]), int(children[k][0])]
+    return {"mesh_order": mesh_order, "coplanar": cop, "frames": frames,
+            "boxes": np.array(pre_boxes, np.float64).reshape(-1, 6),
+            "leaf_n": np.array(leaf_n, np.int32), "leaf_ids": np.array(leaf_ids, np.int32)}
+
+
+BVH_ARRAYS = ("mesh_order", "coplanar", "frames", "boxes", "leaf_n", "leaf_ids")
+
+
+def reference_bvh_fixtures() -> None:
+    """The reference's own scene preparation (StlToGeometry, ConstructBVH)
+    on the seeded small, urban and terrain scenes and on three meshes with
+    many equal sort keys (stored in the fixture, so the test needs no
+    generator): a lattice of colliding box centres, centres ordered to drive
+    std::sort into its heap sort, and a flat grid.  The terrain (580,484
+    triangles) keeps sha256 digests of its arrays."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from test_gpu_scene_prep import _tie_heavy_scene  # noqa: E402
+    meshes = {"small": scenes.small_scene().scene, "urban": scenes.urban_scene(level=2).scene,
+              "large": scenes.large_scene().scene}
+    tri, nrm = _tie_heavy_scene(1, 3000)
+    meshes["ties"] = scenes.Scene("ties", tri, nrm, np.zeros(len(tri), np.int32), [])
+    keys = np.loadtxt(os.path.join(OUT, "introsort_killer_3000.txt"), dtype=np.int64)
+    n = len(keys)
+    tri = np.zeros((n, 3, 3), np.float32)
+    tri[:, :, 0] = (keys.astype(np.float32) * np.float32(0.25))[:, None]
+    tri[:, :, 1] = (np.arange(n, dtype=np.float32) * np.float32(0.5))[:, None]
+    tri[:, 1, 1] += np.float32(1.0)
+    tri[:, 2, 2] = np.float32(1.0)
+    nrm = np.tile(np.array([[1.0, 0.0, 0.0]], np.float32), (n, 1))
+    meshes["heap_sort"] = scenes.Scene("heap_sort", tri, nrm, np.zeros(n, np.int32), [])
+    k = 40
+    xs, ys = np.meshgrid(np.arange(k, dtype=np.float32), np.arange(k, dtype=np.float32))
+    x0, y0 = xs.ravel(), ys.ravel()
+    z = np.zeros_like(x0)
+    a = np.stack([np.stack([x0, y0, z], 1), np.stack([x0 + 1, y0, z], 1),
+                  np.stack([x0 + 1, y0 + 1, z], 1)], 1)
+    b = np.stack([np.stack([x0, y0, z], 1), np.stack([x0 + 1, y0 + 1, z], 1),
+                  np.stack([x0, y0 + 1, z], 1)], 1)
+    tri = np.concatenate([a, b]).astype(np.float32)
+    nrm = np.tile(np.array([[0.0, 0.0, 1.0]], np.float32), (len(tri), 1))
+    meshes["flat"] = scenes.Scene("flat", tri, nrm, np.zeros(len(tri), np.int32), [])
+    for name, sc in meshes.items():
+        with tempfile.TemporaryDirectory() as d:
+            stl = os.path.join(d, "scene.stl")
+            scenes.write_stl(sc, stl)
+            out = os.path.join(d, "dump.txt")
+            subprocess.run([oracle_build.REF_HARNESS, "scene", stl, out], check=True)
+            rep = parse_scene_dump(out)
+        h = hashlib.sha256(np.ascontiguousarray(sc.tri, "<f4").tobytes() +
+                           np.ascontiguousarray(sc.normal, "<f4").tobytes()).hexdigest()
+        extra = {"inputs_sha256": h, "n_nodes": len(rep["leaf_n"])}
+        if name == "large":
+            for key in BVH_ARRAYS:
+                extra[key + "_sha256"] = hashlib.sha256(np.ascontiguousarray(rep[key]).tobytes()).hexdigest()
+        else:
+            extra.update(rep)
+            if name in ("ties", "heap_sort", "flat"):
+                extra.update(tri=sc.tri, normal=sc.normal)
+        np.savez_compressed(os.path.join(OUT, f"refbvh_{name}.npz"), **extra)
+        print(f"refbvh_{name}: {sc.n_tri} triangles, {extra['n_nodes']} nodes, "
+              f"{int((rep['leaf_n'] >= 0).sum())} leaves")
+
+
 VARIANTS = ("small_L5_R4T1_halfwave_rotated", "urban_L5_R3T1_rx1600_halfwave_rotated",
             "urban_L5_R3T1_rx1600_isotropic_nofresnel")
 
@@ -195,6 +298,7 @@ def main() -> None:
                                                   max_transmission=2), (0.5, 0.2, 0.01)),
              "urban_L5_R3T2_rx1600_slab")
     request_variants()
+    reference_bvh_fixtures()
     # icosahedron launch directions, bit-exact
     for lvl in (0, 1, 2, 5):
         with tempfile.TemporaryDirectory() as d:
@@ -208,6 +312,10 @@ def main() -> None:
 if __name__ == "__main__":
     if "--outputs-only" in sys.argv:  # refresh only shipped_outputs.json
         shipped_output_hashes()
+    elif "--bvh" in sys.argv:  # (re)write only the reference-BVH fixtures
+        if oracle_build.build_reference(REF) is None:
+            raise SystemExit("reference checkout not found: set SBR_REFERENCE_DIR to it")
+        reference_bvh_fixtures()
     elif "--variants" in sys.argv:  # (re)write only the request-variant fixtures
         if oracle_build.build_reference(REF) is None:
             raise SystemExit("reference checkout not found: set SBR_REFERENCE_DIR to it")
