@@ -365,6 +365,13 @@ sbr_status sbr_write_paths_vtk(const char* path, const sbr_path* paths, int n_pa
 /* RTSolver::SaveIcosahedronAsVtk (RTSolver.cpp:719-766): the launch rays of
  * an icosahedron level as unit segments from `origin` (3 doubles). */
 sbr_status sbr_write_launch_rays_vtk(const char* path, const double* origin, int tessellation);
+/* GenerateRaysOnIcosahedron (Icosahedron.cpp:80-109, whose origin argument
+ * is unused): the unit launch directions of subdivision level `tessellation`
+ * (0..12), 3 doubles per ray in the reference's vertex order, the directions
+ * sbr_solve launches.  *n_rays receives 10*4^level + 2; directions may be NULL
+ * to query it, else it needs room for cap >= *n_rays rays.  Host only. */
+sbr_status sbr_launch_directions(int tessellation, double* directions, long long cap,
+                                 long long* n_rays);
 
 /* ---- launch shapes and the autotuner ------------------------------------ */
 /* No counterpart in the reference, whose solve is one single-threaded CPU

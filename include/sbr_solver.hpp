@@ -9,6 +9,7 @@
 //   Preprocessor::GenerateRXLine  Preprocessor.cpp:270-284
 //   Preprocessor::ReadLocationFile Preprocessor.h:21
 //   Preprocessor::ReadPatternFile Preprocessor.cpp:3-35 (+ AntennaPattern, antenna type 3)
+//   GenerateRaysOnIcosahedron     Icosahedron.h:8, Icosahedron.cpp:80-109
 //   BVH<Triangle>::ConstructBVH   BVH/BVH.h:25,135-230
 //   RTSolver::Init / ExecuteRayTracing / Save*   RTSolver.h:18-45
 //   FieldCompute::FieldAtReceiver FieldCompute.h:39
@@ -223,6 +224,21 @@ inline bool ReadLocationFile(std::string fileName, VecVec3& output) {
 }
 
 }  // namespace Preprocessor
+
+// Icosahedron.cpp:80-109: the unit launch directions of a subdivision level in
+// the reference's vertex order, heap-allocated like the reference's (the
+// caller deletes the vector); the origin does not change them there either.
+inline std::vector<Vec3>* GenerateRaysOnIcosahedron(int tessellation, Vec3 origin) {
+  (void)origin;
+  long long n = 0;
+  check(sbr_launch_directions(tessellation, nullptr, 0, &n));
+  std::vector<double> d(3 * size_t(n));
+  check(sbr_launch_directions(tessellation, d.data(), n, &n));
+  auto* out = new std::vector<Vec3>;
+  out->reserve(size_t(n));
+  for (long long i = 0; i < n; ++i) out->emplace_back(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+  return out;
+}
 
 // ------------------------------------------------------------------ scene
 

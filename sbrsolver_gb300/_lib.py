@@ -29,7 +29,7 @@ EXPORTS = (
     "sbr_pattern_info", "sbr_pattern_destroy", "sbr_fault_inject_alloc",
     "sbr_scene_set_tuning", "sbr_scene_get_tuning", "sbr_autotune", "sbr_result_field_bound",
     "sbr_scene_create_ex", "sbr_scene_triangle_frames", "sbr_scene_search_bvh",
-    "sbr_scene_reference_bvh",
+    "sbr_scene_reference_bvh", "sbr_launch_directions",
 )
 
 
@@ -166,6 +166,7 @@ def load(path: str = LIB_PATH):
             "sbr_scene_triangle_frames": [vp, P(D), P(D), P(D)],
             "sbr_scene_search_bvh": [vp, P(I), P(I), P(C.c_float), P(I)],
             "sbr_scene_reference_bvh": [vp, P(I), P(I), P(C.c_double), P(I), P(I)],
+            "sbr_launch_directions": [I, P(D), C.c_longlong, P(C.c_longlong)],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

@@ -575,6 +575,18 @@ def write_pattern_file(path: str, gain_phase: np.ndarray, d_theta: float, d_phi:
                 fh.write(f"{i * d_theta:g} {j * d_phi:g} {g[0]:.6g} {g[1]:.6g} {g[2]:.6g} {g[3]:.6g}\n")
 
 
+def GenerateRaysOnIcosahedron(tessellation: int, origin=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """The unit launch directions of an icosahedron level, (10*4^L + 2, 3), in
+    the reference's vertex order (Icosahedron.cpp:80-109; like the
+    reference, the origin does not change them): sbr_launch_directions."""
+    lib = _lib.load()
+    n = C.c_longlong(0)
+    _lib.check(lib.sbr_launch_directions(int(tessellation), None, 0, C.byref(n)))
+    out = np.zeros((n.value, 3), np.float64)
+    _lib.check(lib.sbr_launch_directions(int(tessellation), _dp(out), n.value, C.byref(n)))
+    return out
+
+
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 

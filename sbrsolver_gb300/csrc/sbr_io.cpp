@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstring>
 #include <fstream>
 #include <numeric>
 #include <string>
@@ -309,6 +310,26 @@ sbr_status sbr_write_launch_rays_vtk(const char* path, const double* origin, int
   ofs << "LaunchID 1 " << n << " int\n";
   for (size_t i = 0; i < n; ++i) ofs << " " << i << "\n";
   return close_or_fail(ofs, path, "sbr_write_launch_rays_vtk");
+}
+
+sbr_status sbr_launch_directions(int tessellation, double* directions, long long cap,
+                                 long long* n_rays) {
+  if (!n_rays || tessellation < 0 || tessellation > 12 || (directions && cap < 0)) {
+    sbr::set_error_message("sbr_launch_directions: need n_rays, a level in 0..12 and cap >= 0");
+    return SBR_ERR_INVALID_ARG;
+  }
+  const long long n = 10LL * (1LL << (2 * tessellation)) + 2;
+  *n_rays = n;
+  if (!directions) return SBR_OK;
+  if (cap < n) {
+    sbr::set_error_message("sbr_launch_directions: room for " + std::to_string(cap) +
+                           " rays, the level has " + std::to_string(n));
+    return SBR_ERR_CAPACITY;
+  }
+  std::vector<double> d;
+  sbr::icosphere(tessellation, d);
+  std::memcpy(directions, d.data(), sizeof(double) * d.size());
+  return SBR_OK;
 }
 
 }  // extern "C"

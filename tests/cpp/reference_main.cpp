@@ -39,6 +39,10 @@ int main(int argc, char** argv) {
                   triangle_mesh.size(), t.triangleId, t.v3.x(), t.v3.y(), t.v3.z(),
                   rxLocation.size(), rxLocation.back().x(), rxLocation.back().y(),
                   rxLocation.back().z(), plane.size());
+      std::vector<Vec3>* rays = GenerateRaysOnIcosahedron(2, Vec3(0, 0, 5));
+      std::printf("rays %zu last %.17g %.17g %.17g\n", rays->size(), rays->back().x(),
+                  rays->back().y(), rays->back().z());
+      delete rays;
       for (Triangle* p : triangle_mesh) delete p;
       return 0;
     }

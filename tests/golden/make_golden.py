@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
 Run where the reference checkout exists:
-    SBR_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [--variants | --bvh]
+    SBR_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [--variants | --bvh | --ico]
 It compiles the reference's own sources (oracle/build_ref.sh -> oracle/_ref/
 ref_harness), runs each case through RTSolver::ExecuteRayTracing, and stores
 the surviving paths and fields per receiver as .npz.  For the reference's
@@ -261,6 +261,24 @@ def reference_bvh_fixtures() -> None:
               f"{int((rep['leaf_n'] >= 0).sum())} leaves")
 
 
+def icosphere_digests() -> None:
+    """sha256 of the reference's launch directions (GenerateRaysOnIcosahedron,
+    Icosahedron.cpp:80-109; little-endian float64, x y z per ray) at levels
+    6-10, the levels of the benchmark workloads, whose arrays are too large to
+    commit."""
+    import json
+    out = {}
+    for lvl in range(6, 11):
+        with tempfile.TemporaryDirectory() as d:
+            f = os.path.join(d, "ico.bin")
+            subprocess.run([oracle_build.REF_HARNESS, "ico", str(lvl), f], check=True)
+            b = open(f, "rb").read()
+        out[str(lvl)] = {"rays": len(b) // 24, "sha256": hashlib.sha256(b).hexdigest()}
+    with open(os.path.join(OUT, "icosphere_digests.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+    print("icosahedron digests of levels 6-10 written")
+
+
 VARIANTS = ("small_L5_R4T1_halfwave_rotated", "urban_L5_R3T1_rx1600_halfwave_rotated",
             "urban_L5_R3T1_rx1600_isotropic_nofresnel")
 
@@ -307,11 +325,16 @@ def main() -> None:
             v = np.fromfile(f, np.float64).reshape(-1, 3)
         np.save(os.path.join(OUT, f"icosphere_L{lvl}.npy"), v)
     print("icosahedron levels 0,1,2,5 written")
+    icosphere_digests()
 
 
 if __name__ == "__main__":
     if "--outputs-only" in sys.argv:  # refresh only shipped_outputs.json
         shipped_output_hashes()
+    elif "--ico" in sys.argv:  # (re)write only the launch-direction digests
+        if oracle_build.build_reference(REF) is None:
+            raise SystemExit("reference checkout not found: set SBR_REFERENCE_DIR to it")
+        icosphere_digests()
     elif "--bvh" in sys.argv:  # (re)write only the reference-BVH fixtures
         if oracle_build.build_reference(REF) is None:
             raise SystemExit("reference checkout not found: set SBR_REFERENCE_DIR to it")

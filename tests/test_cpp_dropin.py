@@ -8,6 +8,7 @@ import os
 import shutil
 import subprocess
 
+import numpy as np
 import pytest
 
 from sbrsolver_gb300 import scenes
@@ -35,8 +36,15 @@ def program(built, tmp_path_factory):
 def test_preprocessing_without_gpu(program):
     exe, stl, d = program
     out = subprocess.run([exe, stl, str(d), "prep"], capture_output=True, text=True, check=True)
-    assert out.stdout.split() == ["triangles", "2", "last", "1", "(-5", "1000", "0)", "receivers",
-                                  "3000", "last", "(0", "2999", "3)", "plane", "121"]
+    first, second = out.stdout.splitlines()
+    assert first.split() == ["triangles", "2", "last", "1", "(-5", "1000", "0)", "receivers",
+                             "3000", "last", "(0", "2999", "3)", "plane", "121"]
+    # GenerateRaysOnIcosahedron: the reference's level-2 directions, last one bit for bit
+    ico = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                               "icosphere_L2.npy"))
+    t = second.split()
+    assert t[:3] == ["rays", str(len(ico)), "last"]
+    assert [float(x) for x in t[3:]] == list(ico[-1])
 
 
 @pytest.mark.gpu

@@ -1,5 +1,6 @@
 """The oracle (CPU restatement) against golden fixtures produced by the
 reference's own sources (tests/golden/make_golden.py)."""
+import ctypes as C
 import os
 
 import numpy as np
@@ -80,6 +81,37 @@ def test_icosphere_bit_exact(built, level):
     ref = np.load(os.path.join(GOLD, f"icosphere_L{level}.npy"))
     np.testing.assert_array_equal(orc.icosphere(level), ref)
     assert len(ref) == 10 * 4 ** level + 2
+
+
+@pytest.mark.parametrize("level", [6, 7, 8, 9, 10])
+def test_icosphere_digests(built, level):
+    """The launch directions of the benchmark levels, from the oracle and from
+    the library (host code, no GPU), hash like the reference's
+    (tests/golden/icosphere_digests.json)."""
+    import hashlib
+    import json
+
+    from sbrsolver_gb300 import api
+    ref = json.load(open(os.path.join(GOLD, "icosphere_digests.json")))[str(level)]
+    for v in (orc.icosphere(level), api.GenerateRaysOnIcosahedron(level)):
+        v = np.ascontiguousarray(v, "<f8")
+        assert len(v) == ref["rays"] == 10 * 4 ** level + 2
+        assert hashlib.sha256(v.tobytes()).hexdigest() == ref["sha256"]
+
+
+def test_launch_directions_arguments(built):
+    from sbrsolver_gb300 import _lib, api
+    lib = _lib.load()
+    n = C.c_longlong(0)
+    assert lib.sbr_launch_directions(13, None, 0, C.byref(n)) == _lib.ERR_INVALID_ARG
+    assert lib.sbr_launch_directions(2, None, 0, None) == _lib.ERR_INVALID_ARG
+    assert lib.sbr_launch_directions(2, None, 0, C.byref(n)) == _lib.OK and n.value == 162
+    small = np.zeros((161, 3))
+    assert lib.sbr_launch_directions(2, small.ctypes.data_as(C.POINTER(C.c_double)), 161,
+                                     C.byref(n)) == _lib.ERR_CAPACITY
+    for lvl in (0, 1, 2, 5):
+        np.testing.assert_array_equal(api.GenerateRaysOnIcosahedron(lvl),
+                                      np.load(os.path.join(GOLD, f"icosphere_L{lvl}.npy")))
 
 
 def test_scene_inputs_are_reproducible(tmp_path):
